@@ -1,0 +1,271 @@
+// Broad phase: linear BVH over the element boxes.
+//
+// Leaf boxes follow the reference exactly (CD_TRI/CD_BOND::min/max_*_coord,
+// dcollid.cpp:852-932, padded by 1e-6 as AABB.cpp:6-36 does), and node boxes
+// are exact min/max unions, so the overlap tests prune nothing that the
+// reference's incremental tree would report: the pair set is the same set of
+// all box-overlapping leaf pairs, whatever the tree shape. Morton keys (10 bits
+// per axis) are sorted by the hand-written radix sort; the hierarchy is the
+// Karras (2012) construction; refit walks up with arrival counters.
+#include "cc_launch.h"
+
+namespace ccg {
+
+namespace {
+
+__device__ __forceinline__ unsigned long long enc_double(double x) {
+    unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double dec_double(unsigned long long e) {
+    unsigned long long u = (e & 0x8000000000000000ull) ? (e & 0x7fffffffffffffffull) : ~e;
+    return __longlong_as_double((long long)u);
+}
+
+__global__ void k_bbox_init(unsigned long long* bb) {
+    int t = threadIdx.x;
+    if (t < 3) bb[t] = ~0ull;
+    else if (t < 6) bb[t] = 0ull;
+}
+
+template <int MOVING>
+__global__ void k_leaf_boxes(const int* __restrict__ ev, int ne, int nt, const double4_32a* __restrict__ xo,
+                             const double4_32a* __restrict__ av, double dt, Box6* __restrict__ box,
+                             unsigned long long* bb) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    double lo[3] = {kBig, kBig, kBig}, hi[3] = {-kBig, -kBig, -kBig};
+    bool valid = e < ne;
+    if (valid) {
+        int np = (e < nt) ? 3 : 2;
+        double mx[3] = {-kBig, -kBig, -kBig}, mn[3] = {kBig, kBig, kBig};
+        for (int i = 0; i < np; ++i) {
+            int p = ev[3 * e + i];
+            double4_32a x = xo[p];
+            double xs[3] = {x.x, x.y, x.z};
+            if (MOVING) {
+                double4_32a v = av[p];
+                double vs[3] = {v.x, v.y, v.z};
+                for (int d = 0; d < 3; ++d) {
+                    mx[d] = smax(mx[d], xs[d]);
+                    mx[d] = smax(mx[d], xs[d] + vs[d] * dt);
+                    mn[d] = smin(mn[d], xs[d]);
+                    mn[d] = smin(mn[d], xs[d] + vs[d] * dt);
+                }
+            } else {
+                for (int d = 0; d < 3; ++d) {
+                    mx[d] = smax(xs[d], mx[d]);
+                    mn[d] = smin(xs[d], mn[d]);
+                }
+            }
+        }
+        Box6 b;
+        for (int d = 0; d < 3; ++d) {
+            b.lo[d] = mn[d] - kBoxPad;
+            b.hi[d] = mx[d] + kBoxPad;
+            lo[d] = b.lo[d];
+            hi[d] = b.hi[d];
+        }
+        box[e] = b;
+    }
+    // union of the leaf boxes (the root box of any tree over them)
+    for (int d = 0; d < 3; ++d) {
+        double l = lo[d], h = hi[d];
+        for (int o = 16; o > 0; o >>= 1) {
+            l = fmin(l, __shfl_xor_sync(0xffffffffu, l, o));
+            h = fmax(h, __shfl_xor_sync(0xffffffffu, h, o));
+        }
+        if ((threadIdx.x & 31) == 0 && l <= h) {
+            atomicMin(&bb[d], enc_double(l));
+            atomicMax(&bb[3 + d], enc_double(h));
+        }
+    }
+}
+
+__device__ __forceinline__ unsigned int expand_bits10(unsigned int v) {
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+__global__ void k_morton(const Box6* __restrict__ box, int n, const unsigned long long* bb,
+                         unsigned long long* keys, unsigned int* order) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    Box6 b = box[e];
+    unsigned int q[3];
+    for (int d = 0; d < 3; ++d) {
+        double lo = dec_double(bb[d]), hi = dec_double(bb[3 + d]);
+        double c = 0.5 * (b.lo[d] + b.hi[d]);
+        double ext = hi - lo;
+        double t = ext > 0.0 ? (c - lo) / ext : 0.0;
+        t = fmin(fmax(t, 0.0), 1.0);
+        unsigned int v = (unsigned int)(t * 1023.0);
+        q[d] = v > 1023u ? 1023u : v;
+    }
+    keys[e] = (unsigned long long)((expand_bits10(q[0]) << 2) | (expand_bits10(q[1]) << 1) | expand_bits10(q[2]));
+    order[e] = (unsigned int)e;
+}
+
+__device__ __forceinline__ int delta(const unsigned long long* keys, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    unsigned long long a = keys[i], b = keys[j];
+    if (a == b) return 64 + __clz((unsigned int)(i ^ j));
+    return __clzll(a ^ b);
+}
+
+// Karras, "Maximizing parallelism in the construction of BVHs, octrees and
+// k-d trees" (HPG 2012), with index tie-breaking for equal keys.
+__global__ void k_karras(const unsigned long long* __restrict__ keys, int n, int* child, int* range_hi,
+                         int* parent) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = delta(keys, n, i, i - d);
+    int lmax = 2;
+    while (delta(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+    int j = i + l * d;
+    int dnode = delta(keys, n, i, j);
+    int s = 0;
+    int t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (delta(keys, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    int gamma = i + s * d + (d < 0 ? d : 0);
+    int lo = i < j ? i : j, hi = i < j ? j : i;
+    int left = (lo == gamma) ? ~gamma : gamma;
+    int right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+    child[2 * i] = left;
+    child[2 * i + 1] = right;
+    range_hi[i] = hi;
+    if (left >= 0) parent[left] = i; else parent[n - 1 + ~left] = i;
+    if (right >= 0) parent[right] = i; else parent[n - 1 + ~right] = i;
+    if (i == 0) parent[0] = -1;
+}
+
+__device__ __forceinline__ Box6 load_box_cg(const Box6* p) {
+    const double2* q = reinterpret_cast<const double2*>(p);
+    double2 a = __ldcg(q), b = __ldcg(q + 1), c = __ldcg(q + 2);
+    Box6 r;
+    r.lo[0] = a.x; r.lo[1] = a.y; r.lo[2] = b.x;
+    r.hi[0] = b.y; r.hi[1] = c.x; r.hi[2] = c.y;
+    return r;
+}
+
+__global__ void k_refit(const Box6* __restrict__ box, const unsigned int* __restrict__ order, int n,
+                        const int* __restrict__ child, const int* __restrict__ parent, int* flags,
+                        Box6* node_box) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int node = parent[n - 1 + i];
+    while (node >= 0) {
+        __threadfence();
+        if (atomicAdd(&flags[node], 1) == 0) return;
+        __threadfence();
+        int c0 = child[2 * node], c1 = child[2 * node + 1];
+        Box6 a = c0 >= 0 ? load_box_cg(&node_box[c0]) : box[order[~c0]];
+        Box6 b = c1 >= 0 ? load_box_cg(&node_box[c1]) : box[order[~c1]];
+        Box6 m;
+        for (int d = 0; d < 3; ++d) {
+            m.lo[d] = smin(a.lo[d], b.lo[d]);
+            m.hi[d] = smax(a.hi[d], b.hi[d]);
+        }
+        node_box[node] = m;
+        node = parent[node];
+    }
+}
+
+__device__ __forceinline__ bool overlap(const Box6& a, const Box6& b) {
+    return (a.lo[0] <= b.hi[0] && a.hi[0] >= b.lo[0]) && (a.lo[1] <= b.hi[1] && a.hi[1] >= b.lo[1]) &&
+           (a.lo[2] <= b.hi[2] && a.hi[2] >= b.lo[2]);
+}
+
+__device__ __forceinline__ void emit_pair(int a, int b, int2* pairs, int cap, PassCounters* ctr) {
+    int slot = atomicAdd(&ctr->npairs, 1);
+    if (slot < cap)
+        pairs[slot] = make_int2(a, b);
+    else
+        atomicOr(&ctr->err, kErrPairOverflow);
+}
+
+// One thread per sorted leaf i reports every leaf j > i whose box overlaps.
+__global__ void k_traverse(const Box6* __restrict__ box, const unsigned int* __restrict__ order, int n,
+                           const int* __restrict__ child, const int* __restrict__ range_hi,
+                           const Box6* __restrict__ node_box, int2* pairs, int cap, PassCounters* ctr) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    int ei = (int)order[i];
+    Box6 q = box[ei];
+    int stk[kTraversalStack];
+    int sp = 0;
+    stk[sp++] = 0;
+    while (sp > 0) {
+        int node = stk[--sp];
+        for (int k = 0; k < 2; ++k) {
+            int c = child[2 * node + k];
+            if (c < 0) {
+                int j = ~c;
+                if (j > i) {
+                    int ej = (int)order[j];
+                    if (overlap(q, box[ej])) emit_pair(ei, ej, pairs, cap, ctr);
+                }
+            } else if (range_hi[c] > i && overlap(q, node_box[c])) {
+                if (sp < kTraversalStack)
+                    stk[sp++] = c;
+                else
+                    atomicOr(&ctr->err, kErrStack);
+            }
+        }
+    }
+}
+
+__global__ void k_brute_pairs(const Box6* __restrict__ box, int n, int2* pairs, int cap, PassCounters* ctr) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Box6 q = box[i];
+    for (int j = i + 1; j < n; ++j)
+        if (overlap(q, box[j])) emit_pair(i, j, pairs, cap, ctr);
+}
+
+inline int nblk(int n, int t) { return (n + t - 1) / t; }
+
+}  // namespace
+
+void leaf_boxes(const int* ev, int ne, int nt, const double4_32a* xo, const double4_32a* av, double dt, int moving,
+                Box6* box, unsigned long long* bbox_enc, cudaStream_t s) {
+    k_bbox_init<<<1, 32, 0, s>>>(bbox_enc);
+    if (ne <= 0) return;
+    if (moving)
+        k_leaf_boxes<1><<<nblk(ne, 256), 256, 0, s>>>(ev, ne, nt, xo, av, dt, box, bbox_enc);
+    else
+        k_leaf_boxes<0><<<nblk(ne, 256), 256, 0, s>>>(ev, ne, nt, xo, av, dt, box, bbox_enc);
+}
+
+void bvh_build(const Box6* box, BvhBufs& b, cudaStream_t s) {
+    int n = b.n;
+    if (n <= 1) return;
+    k_morton<<<nblk(n, 256), 256, 0, s>>>(box, n, b.bbox_enc, b.keys, b.order);
+    radix_sort_pairs(b.keys, b.order, n, 30, b.sort_temp, s);
+    k_karras<<<nblk(n - 1, 256), 256, 0, s>>>(b.keys, n, b.child, b.range_hi, b.parent);
+    cudaMemsetAsync(b.flags, 0, sizeof(int) * (size_t)(n - 1), s);
+    k_refit<<<nblk(n, 256), 256, 0, s>>>(box, b.order, n, b.child, b.parent, b.flags, b.node_box);
+}
+
+void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCounters* ctr, cudaStream_t s) {
+    int n = b.n;
+    if (n <= 1) return;
+    k_traverse<<<nblk(n - 1, 128), 128, 0, s>>>(box, b.order, n, b.child, b.range_hi, b.node_box, pairs, cap,
+                                                  ctr);
+}
+
+void brute_pairs(const Box6* box, int ne, int2* pairs, int cap, PassCounters* ctr, cudaStream_t s) {
+    if (ne <= 1) return;
+    k_brute_pairs<<<nblk(ne, 128), 128, 0, s>>>(box, ne, pairs, cap, ctr);
+}
+
+}  // namespace ccg

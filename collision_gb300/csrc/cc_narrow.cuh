@@ -1,0 +1,497 @@
+// Narrow phase on the GPU: proximity (t = 0) and continuous (CCD) tests of
+// one element pair, and the repulsion / inelastic / friction impulses of each
+// hit, emitted as keyed per-point contributions instead of the reference's
+// in-place accumulation (dcollid3d.cpp:925-1300).
+//
+// One thread handles one element pair; positions stay in registers (the
+// reference writes them into the shared POINT coordinates, dcollid3d.cpp:333-339).
+#pragma once
+
+#include "cc_common.cuh"
+
+namespace ccg {
+
+struct NarrowCtx {
+    const double4_32a* xo;       // x_old per point
+    const double4_32a* av;       // average velocity per point
+    const uint8_t* fixed;    // is_fixed per point
+    const int* ev;           // 3 point ids per element (bonds: third is -1)
+    const int* esurf;        // surface id per element (-1 for bonds)
+    const uint8_t* erigid;   // element has a fixed point (isRigidBody(hse))
+    const int* rank;         // leaf rank of each element in the reference tree
+    int nt;                  // elements [0, nt) are triangles
+    int pass;
+    int zone;                // impact-zone mode (s_detImpZone)
+    Params p;
+    Contrib* contrib;
+    int contrib_cap;
+    PassCounters* ctr;
+    int* uf_parent;
+    VisitRec* rec;
+    int rec_cap;
+};
+
+struct CallState {
+    unsigned long long keybase;
+    int plist[6];
+    int np;
+    int dcount[6];
+    int sub;
+};
+
+__device__ __forceinline__ bool is_static(const NarrowCtx& c, int p) { return c.fixed[p] != 0; }
+
+__device__ __forceinline__ void emit(const NarrowCtx& c, CallState& st, int vertex, const double* imp,
+                                     const double* fric, int has_fric) {
+    for (int i = 0; i < st.np; ++i)
+        if (st.plist[i] == vertex) { st.dcount[i]++; break; }
+    int slot = atomicAdd(&c.ctr->ncontrib, 1);
+    if (slot >= c.contrib_cap) {
+        atomicOr(&c.ctr->err, kErrContribOverflow);
+        return;
+    }
+    Contrib& o = c.contrib[slot];
+    o.key = st.keybase | (unsigned long long)st.sub;
+    o.vertex = vertex;
+    o.flags = has_fric;
+    for (int j = 0; j < 3; ++j) { o.imp[j] = imp[j]; o.fric[j] = fric[j]; }
+}
+
+// ---------------------------------------------------------------- unions
+__device__ __forceinline__ int uf_find(int* parent, int x) {
+    // path halving; concurrent halving writes only shorten paths
+    while (true) {
+        int p = parent[x];
+        if (p == x) return x;
+        int gp = parent[p];
+        if (gp != p) parent[x] = gp;
+        x = gp;
+    }
+}
+
+__device__ __forceinline__ void uf_union(int* parent, int a, int b) {
+    while (true) {
+        a = uf_find(parent, a);
+        b = uf_find(parent, b);
+        if (a == b) return;
+        if (a > b) { int t = a; a = b; b = t; }
+        if (atomicCAS(&parent[b], b, a) == b) return;
+    }
+}
+
+// createImpZone(pts, 4), dcollid.cpp:473-484: the four points join one zone.
+__device__ __forceinline__ void create_imp_zone(const NarrowCtx& c, const int* pts) {
+    uf_union(c.uf_parent, pts[0], pts[1]);
+    uf_union(c.uf_parent, pts[0], pts[2]);
+    uf_union(c.uf_parent, pts[0], pts[3]);
+}
+
+// -------------------------------------------------------------- impulses
+// PointToTriImpulse, dcollid3d.cpp:925-1107 (fixed and free points).
+static __device__ void point_to_tri_impulse(const NarrowCtx& c, CallState& st, const int* pts, const double* nor,
+                                     double* w, double dist) {
+    double v_rel[3] = {0.0, 0.0, 0.0}, vn, vt;
+    double impulse = 0.0, m_impulse, sum_w = 0.0;
+    const double k = c.p.k, m = c.p.m, dt = c.p.dt, lambda = c.p.lambda, h = c.p.thickness;
+    double av[4][3];
+    for (int q = 0; q < 4; ++q) load3(c.av, pts[q], av[q]);
+    bool st0 = is_static(c, pts[0]), st1 = is_static(c, pts[1]), st2 = is_static(c, pts[2]),
+         st3 = is_static(c, pts[3]);
+    dist = h - dist;
+    for (int i = 0; i < 3; ++i) {
+        v_rel[i] += av[3][i];
+        for (int j = 0; j < 3; ++j) v_rel[i] -= w[j] * av[j][i];
+    }
+    vn = dot3(v_rel, nor);
+    if (dot3(v_rel, v_rel) > sqr(vn))
+        vt = sqrt(dot3(v_rel, v_rel) - sqr(vn));
+    else
+        vt = 0.0;
+    bool tri_static[3] = {st0, st1, st2};
+    if (vn < 0) {
+        if (st3 || (st0 && st1 && st2))
+            impulse = vn;
+        else
+            impulse = vn * 0.5;
+        for (int i = 0; i < 3; ++i) {
+            if (tri_static[i]) w[i] = 0.0;
+            sum_w += w[i];
+        }
+        if (fabs(sum_w) > kMachEps) {
+            double inv = 1.0 / sum_w;
+            for (int i = 0; i < 3; ++i) w[i] = inv * w[i];
+        }
+    }
+    bool all_rigid = st0 && st1 && st2 && st3;
+    if (vn * dt < 0.1 * dist) {
+        if (!all_rigid) {
+            double tmp = -smin(dt * k * dist / m, (0.1 * dist / dt - vn));
+            impulse += tmp;
+        }
+    }
+    if (fabs(sum_w) < kMachEps)
+        m_impulse = impulse;
+    else
+        m_impulse = 2.0 * impulse / (1.0 + dot3(w, w));
+    if (all_rigid) return;
+    int has_fric = fabs(vt) > kRoundEps;
+    double imp[3], fric[3];
+    for (int i = 0; i < 3; ++i) {
+        if (tri_static[i]) continue;
+        double t_impulse = m_impulse;
+        for (int j = 0; j < 3; ++j) {
+            imp[j] = w[i] * t_impulse * nor[j];
+            fric[j] = has_fric ? smax(-fabs(lambda * w[i] * t_impulse / vt), -1.0) * (v_rel[j] - vn * nor[j]) : 0.0;
+        }
+        emit(c, st, pts[i], imp, fric, has_fric);
+    }
+    if (!st3) {
+        double t_impulse = m_impulse;
+        for (int j = 0; j < 3; ++j) {
+            imp[j] = -(t_impulse * nor[j]);
+            fric[j] = has_fric ? smax(-fabs(lambda * t_impulse / vt), -1.0) * (v_rel[j] - vn * nor[j]) : 0.0;
+        }
+        emit(c, st, pts[3], imp, fric, has_fric);
+    }
+}
+
+// EdgeToEdgeImpulse, dcollid3d.cpp:1109-1300 (fixed and free points).
+static __device__ void edge_to_edge_impulse(const NarrowCtx& c, CallState& st, const int* pts, const double* nor,
+                                     double a, double b, double dist) {
+    double v_rel[3], vn, vt;
+    double impulse = 0.0, m_impulse;
+    const double k = c.p.k, m = c.p.m, dt = c.p.dt, lambda = c.p.lambda, h = c.p.thickness;
+    double wa[2] = {1.0 - a, a}, wb[2] = {1.0 - b, b};
+    double av[4][3];
+    for (int q = 0; q < 4; ++q) load3(c.av, pts[q], av[q]);
+    bool sq[4] = {is_static(c, pts[0]), is_static(c, pts[1]), is_static(c, pts[2]), is_static(c, pts[3])};
+    dist = h - dist;
+    for (int j = 0; j < 3; ++j) {
+        v_rel[j] = (1.0 - b) * av[2][j] + b * av[3][j];
+        v_rel[j] -= (1.0 - a) * av[0][j] + a * av[1][j];
+    }
+    vn = dot3(v_rel, nor);
+    if (dot3(v_rel, v_rel) > sqr(vn))
+        vt = sqrt(dot3(v_rel, v_rel) - sqr(vn));
+    else
+        vt = 0.0;
+    if (vn < 0.0) {
+        if ((sq[0] && sq[1]) || (sq[2] && sq[3]))
+            impulse = vn;
+        else
+            impulse = vn * 0.5;
+        if (sq[0]) wa[0] = 0.0;
+        if (sq[1]) wa[1] = 0.0;
+        if (sq[2]) wb[0] = 0.0;
+        if (sq[3]) wb[1] = 0.0;
+    }
+    bool all_rigid = sq[0] && sq[1] && sq[2] && sq[3];
+    if (vn * dt < 0.1 * dist) {
+        if (!all_rigid) {
+            double tmp = -smin(dt * k * dist / m, (0.1 * dist / dt - vn));
+            impulse += tmp;
+        }
+    }
+    if (wa[0] + wa[1] < kMachEps || wb[0] + wb[1] < kMachEps)
+        m_impulse = impulse;
+    else
+        m_impulse = 2.0 * impulse / (wa[0] * wa[0] + wa[1] * wa[1] + wb[0] * wb[0] + wb[1] * wb[1]);
+    if (all_rigid) return;
+    int has_fric = fabs(vt) > kRoundEps;
+    const double wgt[4] = {wa[0], wa[1], wb[0], wb[1]};
+    double imp[3], fric[3];
+    for (int q = 0; q < 4; ++q) {
+        if (sq[q]) continue;
+        double t_impulse = m_impulse;
+        for (int j = 0; j < 3; ++j) {
+            double d = wgt[q] * t_impulse * nor[j];
+            imp[j] = (q < 2) ? d : -d;
+            fric[j] = has_fric ? smax(-fabs(lambda * wgt[q] * t_impulse / vt), -1.0) * (v_rel[j] - vn * nor[j]) : 0.0;
+        }
+        emit(c, st, pts[q], imp, fric, has_fric);
+    }
+}
+
+// ------------------------------------------------------- point / edge tests
+// PointToTri, dcollid3d.cpp:778-922. pts[0..2] the triangle, pts[3] the
+// point; X holds the four positions the reference keeps in Coords.
+static __device__ bool point_to_tri(const NarrowCtx& c, CallState& st, const int* pts, const double (*X)[3], double h) {
+    double w[3] = {0.0, 0.0, 0.0};
+    double x13[3], x23[3], x43[3];
+    double nor[3] = {0.0, 0.0, 0.0}, nor_mag, dist, det;
+    for (int i = 0; i < 3; ++i) {
+        x13[i] = X[0][i] - X[2][i];
+        x23[i] = X[1][i] - X[2][i];
+        x43[i] = X[3][i] - X[2][i];
+    }
+    det = dot3(x13, x13) * dot3(x23, x23) - dot3(x13, x23) * dot3(x13, x23);
+    if (fabs(det) < 1000 * kMachEps) return false;
+    cross3(x13, x23, nor);
+    nor_mag = mag3(nor);
+    double xo[4][3];
+    for (int q = 0; q < 4; ++q) load3(c.xo, pts[q], xo[q]);
+    double x43_old[3];
+    for (int i = 0; i < 3; ++i) x43_old[i] = xo[3][i] - xo[2][i];
+    dist = dot3(x43_old, nor);
+    for (int i = 0; i < 3; ++i) nor[i] /= nor_mag * ((dist >= 0) ? 1.0 : -1.0);
+    dist = fabs(dot3(x43, nor));
+    w[0] = (dot3(x13, x43) * dot3(x23, x23) - dot3(x23, x43) * dot3(x13, x23)) / det;
+    w[1] = (dot3(x13, x13) * dot3(x23, x43) - dot3(x13, x23) * dot3(x13, x43)) / det;
+    w[2] = 1 - w[0] - w[1];
+    if (fabs(w[0]) < kRoundEps || fabs(w[1]) < kRoundEps || fabs(w[2]) < kRoundEps) {
+        double vec[3];
+        for (int j = 0; j < 3; ++j) vec[j] = xo[3][j];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) vec[j] -= w[i] * xo[i][j];
+        double vec_mag = mag3(vec);
+        if (vec_mag > kRoundEps)
+            for (int j = 0; j < 3; ++j) nor[j] = vec[j];
+    }
+    nor_mag = mag3(nor);
+    if (nor_mag > kRoundEps) {
+        for (int i = 0; i < 3; ++i) nor[i] /= nor_mag;
+    } else {
+        atomicOr(&c.ctr->err, kErrNan);  // "nan nor vec": the reference exits
+        return false;
+    }
+    if (dist > h) return false;
+    for (int i = 0; i < 3; ++i)
+        if (w[i] > 1 + c.p.eps || w[i] < -c.p.eps) return false;
+    atomicAdd(&c.ctr->ncontacts, 1);
+    point_to_tri_impulse(c, st, pts, nor, w, dist);
+    return true;
+}
+
+// EdgeToEdge, dcollid3d.cpp:643-776. Edges (pts[0],pts[1]) and (pts[2],pts[3]).
+static __device__ bool edge_to_edge(const NarrowCtx& c, CallState& st, const int* pts, const double (*X)[3], double h) {
+    double x21[3], x43[3], x31[3], tmp[3], v1[3], v2[3], nor[3];
+    double a, b, nor_mag, dist;
+    for (int i = 0; i < 3; ++i) {
+        x21[i] = X[1][i] - X[0][i];
+        x43[i] = X[3][i] - X[2][i];
+        x31[i] = X[2][i] - X[0][i];
+    }
+    cross3(x21, x43, tmp);
+    if (mag3(tmp) < kRoundEps) return false;
+    double d4343 = dot3(x43, x43), d2131 = dot3(x21, x31), d2143 = dot3(x21, x43), d4331 = dot3(x43, x31),
+           d2121 = dot3(x21, x21);
+    a = (d4343 * d2131 - d2143 * d4331) / (d2121 * d4343 - d2143 * d2143);
+    b = (d2143 * d2131 - d2121 * d4331) / (d2121 * d4343 - d2143 * d2143);
+    a = smax(smin(a, 1.0), 0.0);
+    b = smax(smin(b, 1.0), 0.0);
+    for (int i = 0; i < 3; ++i) {
+        v1[i] = a * x21[i];
+        v2[i] = b * x43[i];
+    }
+    for (int i = 0; i < 3; ++i) {
+        v1[i] = X[0][i] + v1[i];
+        v2[i] = X[2][i] + v2[i];
+    }
+    for (int i = 0; i < 3; ++i) nor[i] = v2[i] - v1[i];
+    nor_mag = mag3(nor);
+    if (nor_mag < 1000 * kMachEps) {
+        double xo[4][3];
+        for (int q = 0; q < 4; ++q) load3(c.xo, pts[q], xo[q]);
+        for (int j = 0; j < 3; ++j) {
+            nor[j] = (1.0 - b) * xo[2][j] + b * xo[3][j];
+            nor[j] -= (1.0 - a) * xo[0][j] + a * xo[1][j];
+        }
+    }
+    double s = 0.0;
+    for (int i = 0; i < 3; ++i) s += sqr(v1[i] - v2[i]);
+    dist = sqrt(s);
+    if (dist > h) return false;
+    nor_mag = mag3(nor);
+    if (nor_mag < kMachEps) {
+        atomicOr(&c.ctr->err, kErrNan);  // "Normal vector is nan": the reference exits
+        return false;
+    }
+    for (int i = 0; i < 3; ++i) nor[i] /= nor_mag;
+    atomicAdd(&c.ctr->ncontacts, 1);
+    edge_to_edge_impulse(c, st, pts, nor, a, b, dist);
+    return true;
+}
+
+// ------------------------------------------------------------------- CCD
+// isCoplanar, dcollid3d.cpp:371-482: roots of the coplanarity cubic in
+// [0, dt], shifted by -MACH_EPS and sorted; roots[3] holds dt.
+static __device__ bool is_coplanar(const double (*xo4)[3], const double (*av4)[3], double dt, double* roots) {
+    double v[4][3], x[4][3];
+    for (int j = 0; j < 3; ++j) {
+        v[0][j] = av4[0][j];
+        x[0][j] = xo4[0][j];
+    }
+    for (int i = 1; i < 4; ++i)
+        for (int j = 0; j < 3; ++j) {
+            v[i][j] = av4[i][j] - av4[0][j];
+            x[i][j] = xo4[i][j] - xo4[0][j];
+        }
+    double a, b, c, d;
+    double vv[3], vx[3], xx[3];
+    vv[0] = v[1][1] * v[2][2] - v[1][2] * v[2][1];
+    vv[1] = v[1][0] * v[2][2] - v[1][2] * v[2][0];
+    vv[2] = v[1][0] * v[2][1] - v[1][1] * v[2][0];
+    vx[0] = v[1][1] * x[2][2] - v[1][2] * x[2][1] - v[2][1] * x[1][2] + v[2][2] * x[1][1];
+    vx[1] = v[1][0] * x[2][2] - v[1][2] * x[2][0] - v[2][0] * x[1][2] + v[2][2] * x[1][0];
+    vx[2] = v[1][0] * x[2][1] - v[1][1] * x[2][0] - v[2][0] * x[1][1] + v[2][1] * x[1][0];
+    xx[0] = x[1][1] * x[2][2] - x[1][2] * x[2][1];
+    xx[1] = x[1][0] * x[2][2] - x[1][2] * x[2][0];
+    xx[2] = x[1][0] * x[2][1] - x[1][1] * x[2][0];
+    a = v[3][0] * vv[0] - v[3][1] * vv[1] + v[3][2] * vv[2];
+    b = x[3][0] * vv[0] - x[3][1] * vv[1] + x[3][2] * vv[2] + v[3][0] * vx[0] - v[3][1] * vx[1] + v[3][2] * vx[2];
+    c = x[3][0] * vx[0] - x[3][1] * vx[1] + x[3][2] * vx[2] + v[3][0] * xx[0] - v[3][1] * xx[1] + v[3][2] * xx[2];
+    d = x[3][0] * xx[0] - x[3][1] * xx[1] + x[3][2] * xx[2];
+    if (fabs(a) > kMachEps) {
+        b /= a; c /= a; d /= a;
+        a = b; b = c; c = d;
+        double Q = (a * a - 3 * b) / 9;
+        double R = (2 * a * a * a - 9 * a * b + 27 * c) / 54;
+        double Q3 = Q * Q * Q;
+        double R2 = R * R;
+        if (R2 < Q3) {
+            double Qsqrt = sqrt(Q);
+            double theta = acos(R / sqrt(Q3));
+            roots[0] = -2 * Qsqrt * cos(theta / 3) - a / 3;
+            roots[1] = -2 * Qsqrt * cos((theta + 2 * kPi) / 3) - a / 3;
+            roots[2] = -2 * Qsqrt * cos((theta - 2 * kPi) / 3) - a / 3;
+        } else {
+            double sgn = (R > 0) ? 1.0 : -1.0;
+            double A = -sgn * pow(fabs(R) + sqrt(R2 - Q3), 1.0 / 3.0);
+            double B = (fabs(A) < kRoundEps) ? 0.0 : Q / A;
+            roots[0] = (A + B) - a / 3.0;
+            if (fabs(A - B) < kRoundEps) roots[1] = roots[2] = -0.5 * (A + B) - a / 3.0;
+        }
+    } else {
+        a = b; b = c; c = d;
+        double delta = b * b - 4.0 * a * c;
+        if (fabs(a) > kRoundEps && delta > 0) {
+            double ds = sqrt(delta);
+            roots[0] = (-b + ds) / (2.0 * a);
+            roots[1] = (-b - ds) / (2.0 * a);
+        } else if (fabs(a) < kRoundEps && fabs(b) > kRoundEps) {
+            roots[0] = -c / b;
+        }
+    }
+    for (int i = 0; i < 3; ++i) {
+        roots[i] = roots[i] - kMachEps;
+        if (roots[i] < 0 || roots[i] > dt) roots[i] = -1;
+    }
+    double t;
+    if (roots[0] > roots[1]) { t = roots[0]; roots[0] = roots[1]; roots[1] = t; }
+    if (roots[0] > roots[2]) { t = roots[0]; roots[0] = roots[2]; roots[2] = t; }
+    if (roots[1] > roots[2]) { t = roots[1]; roots[1] = roots[2]; roots[2] = t; }
+    return roots[0] > kMachEps || roots[1] > kMachEps || roots[2] > kMachEps;
+}
+
+// MovingPointToTri / MovingEdgeToEdge, dcollid3d.cpp:327-369: the static
+// test with h = eps at each root of the cubic and at dt, first hit wins.
+template <bool EE>
+static __device__ bool moving_test(const NarrowCtx& c, CallState& st, const int* pts) {
+    double xo4[4][3], av4[4][3];
+    for (int q = 0; q < 4; ++q) {
+        load3(c.xo, pts[q], xo4[q]);
+        load3(c.av, pts[q], av4[q]);
+    }
+    double dt = c.p.dt;
+    double roots[4] = {-1, -1, -1, dt};
+    if (!is_coplanar(xo4, av4, dt, roots)) return false;
+    for (int i = 0; i < 4; ++i) {
+        if (roots[i] < 0) continue;
+        double X[4][3];
+        for (int q = 0; q < 4; ++q)
+            for (int k = 0; k < 3; ++k) X[q][k] = xo4[q][k] + roots[i] * av4[q][k];
+        bool hit = EE ? edge_to_edge(c, st, pts, X, c.p.eps) : point_to_tri(c, st, pts, X, c.p.eps);
+        if (hit) return true;
+    }
+    return false;
+}
+
+template <bool EE>
+__device__ __forceinline__ bool static_test(const NarrowCtx& c, CallState& st, const int* pts) {
+    double X[4][3];
+    for (int q = 0; q < 4; ++q) load3(c.xo, pts[q], X[q]);
+    return EE ? edge_to_edge(c, st, pts, X, c.p.thickness) : point_to_tri(c, st, pts, X, c.p.thickness);
+}
+
+template <bool MOVING, bool EE>
+__device__ __forceinline__ bool sub_test(const NarrowCtx& c, CallState& st, const int* pts) {
+    if (MOVING) return moving_test<EE>(c, st, pts);
+    return static_test<EE>(c, st, pts);
+}
+
+// ------------------------------------------------------ element-pair tests
+// TriToTri (dcollid3d.cpp:570-627) and MovingTriToTri (dcollid3d.cpp:274-325).
+// A = found element, B = query element.
+template <bool MOVING>
+static __device__ bool tri_to_tri(const NarrowCtx& c, CallState& st, const int* A, const int* B) {
+    int pts[4];
+    bool status = false;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            if (A[i] == B[j]) return false;
+    int sub = 0;
+    for (int k = 0; k < 2; ++k)
+        for (int i = 0; i < 3; ++i, ++sub) {
+            // proximity tests B's triangle against A's points first; CCD the reverse
+            const int* tri = MOVING ? ((k == 0) ? A : B) : ((k == 0) ? B : A);
+            const int* pt = MOVING ? ((k == 0) ? B : A) : ((k == 0) ? A : B);
+            for (int j = 0; j < 3; ++j) pts[j] = tri[j];
+            pts[3] = pt[i];
+            st.sub = sub;
+            if (sub_test<MOVING, false>(c, st, pts)) status = true;
+            if (MOVING && status && c.zone) create_imp_zone(c, pts);
+        }
+    for (int i = 0; i < 3; ++i) {
+        pts[0] = A[i];
+        pts[1] = A[(i + 1) % 3];
+        for (int j = 0; j < 3; ++j, ++sub) {
+            pts[2] = B[j];
+            pts[3] = B[(j + 1) % 3];
+            st.sub = sub;
+            if (sub_test<MOVING, true>(c, st, pts)) status = true;
+            if (MOVING && status && c.zone) create_imp_zone(c, pts);
+        }
+    }
+    return status;
+}
+
+// TriToBond (dcollid3d.cpp:485-533) and MovingTriToBond (dcollid3d.cpp:203-244).
+template <bool MOVING>
+static __device__ bool tri_to_bond(const NarrowCtx& c, CallState& st, const int* T, const int* Bd) {
+    int pts[4];
+    bool status = false;
+    for (int i = 0; i < 3; ++i)
+        if (T[i] == Bd[0] || T[i] == Bd[1]) return false;
+    for (int i = 0; i < 3; ++i) pts[i] = T[i];
+    for (int e = 0; e < 2; ++e) {
+        pts[3] = Bd[e];
+        st.sub = e;
+        if (sub_test<MOVING, false>(c, st, pts)) status = true;
+        if (MOVING && status && c.zone) create_imp_zone(c, pts);
+    }
+    pts[2] = Bd[0];
+    pts[3] = Bd[1];
+    for (int i = 0; i < 3; ++i) {
+        pts[0] = T[i];
+        pts[1] = T[(i + 1) % 3];
+        st.sub = 2 + i;
+        if (sub_test<MOVING, true>(c, st, pts)) status = true;
+        if (MOVING && status && c.zone) create_imp_zone(c, pts);
+    }
+    return status;
+}
+
+// BondToBond (dcollid3d.cpp:535-568) and MovingBondToBond (dcollid3d.cpp:246-272).
+template <bool MOVING>
+static __device__ bool bond_to_bond(const NarrowCtx& c, CallState& st, const int* A, const int* B) {
+    int pts[4] = {A[0], A[1], B[0], B[1]};
+    for (int i = 0; i < 4; ++i)
+        for (int j = i + 1; j < 4; ++j)
+            if (pts[i] == pts[j]) return false;
+    st.sub = 0;
+    bool status = sub_test<MOVING, true>(c, st, pts);
+    if (MOVING && status && c.zone) create_imp_zone(c, pts);
+    return status;
+}
+
+}  // namespace ccg

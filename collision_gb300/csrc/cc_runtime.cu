@@ -1,0 +1,611 @@
+// Host runtime of the collision library: the solver object, the pass loop of
+// resolveCollision (dcollid.cpp:317-362) and the C ABI of
+// include/collision_gb300.h.
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/collision_gb300.h"
+#include "cc_launch.h"
+#include "cc_tree_order.h"
+
+using namespace ccg;
+
+namespace {
+
+template <class T>
+cudaError_t dalloc(T** p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    return cudaMalloc((void**)p, n * sizeof(T));
+}
+
+template <class T>
+void dfree(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+__global__ void k_reset_counters(PassCounters* c) {
+    int keep = c->err & kErrNan;
+    c->npairs = 0; c->ncontrib = 0; c->nhit_pairs = 0; c->nrec = 0;
+    c->nvisits = 0; c->ncontacts = 0; c->err = keep;
+}
+
+unsigned long long enc_host(double x) {
+    unsigned long long u;
+    std::memcpy(&u, &x, 8);
+    return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+double dec_host(unsigned long long e) {
+    unsigned long long u = (e & 0x8000000000000000ull) ? (e & 0x7fffffffffffffffull) : ~e;
+    double x;
+    std::memcpy(&x, &u, 8);
+    return x;
+}
+
+}  // namespace
+
+struct cc_solver {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    // topology
+    int nv = 0, nt = 0, nb = 0, ne = 0;
+    int* d_ev = nullptr;
+    int* d_esurf = nullptr;
+    uint8_t* d_erigid = nullptr;
+    uint8_t* d_fixed = nullptr;
+    uint8_t* d_in_elem = nullptr;
+    StrainEdge* d_edges = nullptr;
+    int nedges = 0;
+
+    // state
+    double4_32a* d_xo = nullptr;
+    double4_32a* d_av = nullptr;
+    int* d_uf = nullptr;
+    // staging for host-buffer calls
+    double* d_xold_in = nullptr;
+    double* d_xcand_in = nullptr;
+    double* d_vel = nullptr;
+    double* d_xout = nullptr;
+    uint8_t* d_hc = nullptr;
+
+    // pass buffers
+    Box6* d_box = nullptr;
+    BvhBufs bvh{};
+    int2* d_pairs = nullptr;
+    int pair_cap = 0;
+    Contrib* d_contrib = nullptr;
+    int contrib_cap = 0;
+    ApplyBufs apply{};
+    ZoneBufs zone{};
+    PassCounters* d_ctr = nullptr;
+    PassCounters* h_ctr = nullptr;
+    unsigned long long* h_bbox = nullptr;
+    int* d_rank[2] = {nullptr, nullptr};
+    RefTreeOrder tree[2];
+    double volume = 0.0;
+    uint8_t* d_flag0 = nullptr;
+    uint8_t* d_dirty = nullptr;
+    int* d_strain_passes = nullptr;
+    std::vector<Box6> h_boxes;
+    std::vector<int> h_rank;
+
+    // recording
+    bool record = false;
+    VisitRec* d_rec = nullptr;
+    int rec_cap = 0;
+    std::vector<VisitRec> visits;
+    std::vector<int> pass_kinds;
+
+    cc_params prm{1e-3, 1e-4, 1e-6, 1000.0, 0.01, 0.02, 0.0};
+    double lo[3] = {-1e30, -1e30, -1e30}, hi[3] = {1e30, 1e30, 1e30};
+    long long counters[10] = {0};
+    int pass_index = 0;
+    int zone_cap = 10000;
+
+    ~cc_solver() { release(); }
+
+    void release_mesh() {
+        dfree(d_ev); dfree(d_esurf); dfree(d_erigid); dfree(d_fixed); dfree(d_in_elem); dfree(d_edges);
+        dfree(d_xo); dfree(d_av); dfree(d_uf);
+        dfree(d_xold_in); dfree(d_xcand_in); dfree(d_vel); dfree(d_xout); dfree(d_hc);
+        dfree(d_box); dfree(bvh.keys); dfree(bvh.order); dfree(bvh.child); dfree(bvh.range_hi); dfree(bvh.parent);
+        dfree(bvh.flags); dfree(bvh.node_box); dfree(bvh.bbox_enc);
+        if (bvh.sort_temp) cudaFree(bvh.sort_temp);
+        bvh.sort_temp = nullptr;
+        dfree(d_pairs); dfree(d_contrib);
+        dfree(apply.cnt); dfree(apply.off); dfree(apply.cur); dfree(apply.idx);
+        if (apply.scan_temp) cudaFree(apply.scan_temp);
+        apply.scan_temp = nullptr;
+        dfree(zone.root); dfree(zone.zcnt); dfree(zone.keys); dfree(zone.vals); dfree(zone.nmembers);
+        if (zone.sort_temp) cudaFree(zone.sort_temp);
+        zone.sort_temp = nullptr;
+        dfree(d_rank[0]); dfree(d_rank[1]);
+        dfree(d_flag0); dfree(d_dirty); dfree(d_strain_passes); dfree(d_rec);
+        pair_cap = contrib_cap = rec_cap = 0;
+        nv = nt = nb = ne = nedges = 0;
+        tree[0] = RefTreeOrder();
+        tree[1] = RefTreeOrder();
+    }
+
+    void release() {
+        if (device >= 0) cudaSetDevice(device);
+        release_mesh();
+        dfree(d_ctr);
+        if (h_ctr) cudaFreeHost(h_ctr);
+        if (h_bbox) cudaFreeHost(h_bbox);
+        h_ctr = nullptr;
+        h_bbox = nullptr;
+        if (stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+
+    cc_status fail(cc_status st, const std::string& msg) {
+        err = msg;
+        return st;
+    }
+    cc_status cuda_check(const char* where) {
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return fail(CC_CUDA_ERROR, std::string(where) + ": " + cudaGetErrorString(e));
+        return CC_OK;
+    }
+
+    cc_status grow_pairs(int cap) {
+        dfree(d_pairs);
+        if (dalloc(&d_pairs, (size_t)cap) != cudaSuccess) return fail(CC_NO_MEMORY, "pair buffer");
+        pair_cap = cap;
+        if (record) {
+            dfree(d_rec);
+            if (dalloc(&d_rec, (size_t)cap) != cudaSuccess) return fail(CC_NO_MEMORY, "record buffer");
+            rec_cap = cap;
+        }
+        return CC_OK;
+    }
+    cc_status grow_contrib(int cap) {
+        dfree(d_contrib);
+        dfree(apply.idx);
+        if (dalloc(&d_contrib, (size_t)cap) != cudaSuccess || dalloc(&apply.idx, (size_t)cap) != cudaSuccess)
+            return fail(CC_NO_MEMORY, "contribution buffer");
+        contrib_cap = cap;
+        return CC_OK;
+    }
+
+    cc_status assemble(const cc_mesh* m);
+    cc_status resolve(const double* x_old, const double* x_cand, double* vel, uint8_t* hc, double* x_out,
+                      int* has_collision);
+    cc_status detect_pass(int moving, int zone_mode, bool* is_collision);
+    cc_status update_tree(int which);
+    Params params() const { return Params{prm.dt, prm.thickness, prm.eps, prm.k, prm.m, prm.lambda, prm.cr}; }
+};
+
+cc_status cc_solver::assemble(const cc_mesh* m) {
+    if (!m || m->n_points < 0 || m->n_tris < 0 || m->n_bonds < 0) return fail(CC_BAD_INPUT, "bad mesh sizes");
+    if ((m->n_tris && (!m->tris || !m->tri_rest_len)) || (m->n_bonds && (!m->bonds || !m->bond_rest_len)))
+        return fail(CC_BAD_INPUT, "missing element arrays");
+    long long ne_ll = (long long)m->n_tris + m->n_bonds;
+    if (ne_ll >= (1ll << 22)) return fail(CC_BAD_INPUT, "more than 2^22-1 elements");
+    cudaSetDevice(device);
+    release_mesh();
+    nv = m->n_points; nt = m->n_tris; nb = m->n_bonds; ne = nt + nb;
+    std::vector<int> ev((size_t)ne * 3, -1), esurf((size_t)ne, -1);
+    std::vector<uint8_t> fixed((size_t)nv, 0), in_elem((size_t)nv, 0), erigid((size_t)ne, 0);
+    if (m->fixed)
+        for (int i = 0; i < nv; ++i) fixed[i] = m->fixed[i] ? 1 : 0;
+    for (int t = 0; t < nt; ++t) {
+        for (int k = 0; k < 3; ++k) {
+            int v = m->tris[3 * t + k];
+            if (v < 0 || v >= nv) return fail(CC_BAD_INPUT, "triangle point id out of range");
+            ev[3 * t + k] = v;
+        }
+        if (ev[3 * t] == ev[3 * t + 1] || ev[3 * t] == ev[3 * t + 2] || ev[3 * t + 1] == ev[3 * t + 2])
+            return fail(CC_BAD_INPUT, "triangle with a repeated point");
+        esurf[t] = m->tri_surface ? m->tri_surface[t] : 0;
+    }
+    for (int b = 0; b < nb; ++b) {
+        for (int k = 0; k < 2; ++k) {
+            int v = m->bonds[2 * b + k];
+            if (v < 0 || v >= nv) return fail(CC_BAD_INPUT, "bond point id out of range");
+            ev[3 * (nt + b) + k] = v;
+        }
+    }
+    std::vector<StrainEdge> edges;
+    edges.reserve((size_t)3 * nt + nb);
+    for (int e = 0; e < ne; ++e) {
+        int np = e < nt ? 3 : 2;
+        bool rigid = false;
+        for (int i = 0; i < np; ++i) {
+            in_elem[ev[3 * e + i]] = 1;
+            if (fixed[ev[3 * e + i]]) rigid = true;
+        }
+        erigid[e] = rigid ? 1 : 0;
+        if (rigid) continue;  // isRigidBody(hse), dcollid.cpp:495
+        if (np == 3) {
+            for (int j = 0; j < 3; ++j)
+                edges.push_back(StrainEdge{ev[3 * e + j], ev[3 * e + (j + 1) % 3], m->tri_rest_len[3 * e + j]});
+        } else {
+            edges.push_back(StrainEdge{ev[3 * e], ev[3 * e + 1], m->bond_rest_len[e - nt]});
+        }
+    }
+    nedges = (int)edges.size();
+
+    bool ok = true;
+    ok &= dalloc(&d_ev, (size_t)ne * 3) == cudaSuccess;
+    ok &= dalloc(&d_esurf, (size_t)ne) == cudaSuccess;
+    ok &= dalloc(&d_erigid, (size_t)ne) == cudaSuccess;
+    ok &= dalloc(&d_fixed, (size_t)nv) == cudaSuccess;
+    ok &= dalloc(&d_in_elem, (size_t)nv) == cudaSuccess;
+    ok &= dalloc(&d_edges, (size_t)nedges) == cudaSuccess;
+    ok &= dalloc(&d_xo, (size_t)nv) == cudaSuccess;
+    ok &= dalloc(&d_av, (size_t)nv) == cudaSuccess;
+    ok &= dalloc(&d_uf, (size_t)nv) == cudaSuccess;
+    ok &= dalloc(&d_xold_in, (size_t)nv * 3) == cudaSuccess;
+    ok &= dalloc(&d_xcand_in, (size_t)nv * 3) == cudaSuccess;
+    ok &= dalloc(&d_vel, (size_t)nv * 3) == cudaSuccess;
+    ok &= dalloc(&d_xout, (size_t)nv * 3) == cudaSuccess;
+    ok &= dalloc(&d_hc, (size_t)nv) == cudaSuccess;
+    ok &= dalloc(&d_box, (size_t)ne) == cudaSuccess;
+    bvh.n = ne;
+    ok &= dalloc(&bvh.keys, (size_t)ne) == cudaSuccess;
+    ok &= dalloc(&bvh.order, (size_t)ne) == cudaSuccess;
+    ok &= dalloc(&bvh.child, (size_t)2 * ne) == cudaSuccess;
+    ok &= dalloc(&bvh.range_hi, (size_t)ne) == cudaSuccess;
+    ok &= dalloc(&bvh.parent, (size_t)2 * ne) == cudaSuccess;
+    ok &= dalloc(&bvh.flags, (size_t)ne) == cudaSuccess;
+    ok &= dalloc(&bvh.node_box, (size_t)ne) == cudaSuccess;
+    ok &= dalloc(&bvh.bbox_enc, 6) == cudaSuccess;
+    ok &= cudaMalloc(&bvh.sort_temp, radix_sort_temp_bytes(ne > 0 ? ne : 1)) == cudaSuccess;
+    ok &= dalloc(&apply.cnt, (size_t)nv) == cudaSuccess;
+    ok &= dalloc(&apply.off, (size_t)nv) == cudaSuccess;
+    ok &= dalloc(&apply.cur, (size_t)nv) == cudaSuccess;
+    ok &= cudaMalloc(&apply.scan_temp, scan_temp_bytes(nv > 0 ? nv : 1)) == cudaSuccess;
+    ok &= dalloc(&zone.root, (size_t)nv) == cudaSuccess;
+    ok &= dalloc(&zone.zcnt, (size_t)nv) == cudaSuccess;
+    ok &= dalloc(&zone.keys, (size_t)nv) == cudaSuccess;
+    ok &= dalloc(&zone.vals, (size_t)nv) == cudaSuccess;
+    ok &= dalloc(&zone.nmembers, 1) == cudaSuccess;
+    ok &= cudaMalloc(&zone.sort_temp, radix_sort_temp_bytes(nv > 0 ? nv : 1)) == cudaSuccess;
+    ok &= dalloc(&d_rank[0], (size_t)ne) == cudaSuccess;
+    ok &= dalloc(&d_rank[1], (size_t)ne) == cudaSuccess;
+    ok &= dalloc(&d_flag0, (size_t)nedges) == cudaSuccess;
+    ok &= dalloc(&d_dirty, (size_t)nv) == cudaSuccess;
+    ok &= dalloc(&d_strain_passes, 1) == cudaSuccess;
+    if (!ok) return fail(CC_NO_MEMORY, "device allocation failed");
+    cc_status st = grow_pairs(16 * ne + 4096);
+    if (st) return st;
+    st = grow_contrib(8 * ne + 4096);
+    if (st) return st;
+    cudaMemcpyAsync(d_ev, ev.data(), sizeof(int) * ev.size(), cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d_esurf, esurf.data(), sizeof(int) * esurf.size(), cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d_erigid, erigid.data(), erigid.size(), cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d_fixed, fixed.data(), fixed.size(), cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d_in_elem, in_elem.data(), in_elem.size(), cudaMemcpyHostToDevice, stream);
+    if (nedges)
+        cudaMemcpyAsync(d_edges, edges.data(), sizeof(StrainEdge) * edges.size(), cudaMemcpyHostToDevice, stream);
+    cudaMemsetAsync(d_av, 0, sizeof(double4_32a) * (size_t)(nv > 0 ? nv : 1), stream);
+    h_boxes.resize((size_t)ne);
+    h_rank.resize((size_t)ne);
+    volume = 0.0;
+    cudaStreamSynchronize(stream);
+    return cuda_check("assemble");
+}
+
+// Tree build / rebuild bookkeeping of aabbProximity / aabbCollision
+// (dcollid.cpp:366-428): both trees share one volume; a tree is (re)built
+// on first use or when its root volume has grown by more than 20%.
+cc_status cc_solver::update_tree(int which) {
+    cudaMemcpyAsync(h_bbox, bvh.bbox_enc, 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream);
+    if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("leaf boxes");
+    double rlo[3], rhi[3];
+    for (int d = 0; d < 3; ++d) {
+        rlo[d] = dec_host(h_bbox[d]);
+        rhi[d] = dec_host(h_bbox[3 + d]);
+    }
+    double v = box_volume(rlo, rhi);
+    bool rebuild = !tree[which].built() || (v - volume) > 0.2 * volume;
+    if (!rebuild) return CC_OK;
+    cudaMemcpyAsync(h_boxes.data(), d_box, sizeof(Box6) * (size_t)ne, cudaMemcpyDeviceToHost, stream);
+    if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("leaf boxes to host");
+    volume = tree[which].build(h_boxes.data(), ne);
+    tree[which].ranks(h_rank.data());
+    cudaMemcpyAsync(d_rank[which], h_rank.data(), sizeof(int) * (size_t)ne, cudaMemcpyHostToDevice, stream);
+    counters[8]++;
+    return CC_OK;
+}
+
+// One detection pass: boxes, tree bookkeeping, candidate pairs, narrow
+// phase, impulses applied (aabbProximity/aabbCollision + updateAverageVelocity,
+// dcollid.cpp:390-406, 430-468), and in zone mode the rigid zone update
+// (dcollid.cpp:236-262). Retried with larger buffers on overflow.
+cc_status cc_solver::detect_pass(int moving, int zone_mode, bool* is_collision) {
+    int pass = pass_index++;
+    pass_kinds.push_back(moving ? (zone_mode ? kPassZone : kPassCcd) : kPassProx);
+    counters[0]++;
+    if (moving) counters[zone_mode ? 2 : 1]++;
+    leaf_boxes(d_ev, ne, nt, d_xo, d_av, prm.dt, moving, d_box, bvh.bbox_enc, stream);
+    cc_status st = update_tree(moving);
+    if (st) return st;
+    bvh_build(d_box, bvh, stream);
+    counters[9] += 8;
+    Params p = params();
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        k_reset_counters<<<1, 1, 0, stream>>>(d_ctr);
+        bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream);
+        NarrowArgs a;
+        a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
+        a.rank = d_rank[moving]; a.nt = nt; a.pass = pass; a.zone = zone_mode; a.p = p; a.pairs = d_pairs;
+        a.contrib = d_contrib; a.contrib_cap = contrib_cap; a.ctr = d_ctr; a.uf_parent = d_uf;
+        a.rec = record ? d_rec : nullptr; a.rec_cap = rec_cap;
+        narrow_pass(a, moving, pair_cap, stream);
+        apply_contribs(d_contrib, d_ctr, contrib_cap, nv, d_av, d_hc, apply, stream);
+        counters[9] += 8;
+        cudaMemcpyAsync(h_ctr, d_ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, stream);
+        if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("detection pass");
+        int e = h_ctr->err;
+        if (e & kErrNan) return fail(CC_NAN_DETECTED, "non-finite velocity or normal (the reference exits here)");
+        if (e & kErrStack) return fail(CC_STACK_OVERFLOW, "BVH traversal stack overflow");
+        if (e & kErrPairOverflow) {
+            st = grow_pairs(2 * h_ctr->npairs + 1024);
+            if (st) return st;
+            continue;
+        }
+        if (e & kErrContribOverflow) {
+            st = grow_contrib(2 * h_ctr->ncontrib + 1024);
+            if (st) return st;
+            continue;
+        }
+        if (e & kErrRecordOverflow) {
+            st = grow_pairs(pair_cap);
+            if (st) return st;
+            continue;
+        }
+        break;
+    }
+    if (h_ctr->err) return fail(CC_PAIR_OVERFLOW, "buffers kept overflowing");
+    counters[3] += h_ctr->npairs;
+    counters[4] += h_ctr->nvisits;
+    counters[5] += h_ctr->nhit_pairs;
+    counters[6] += h_ctr->ncontacts;
+    if (record && h_ctr->nrec > 0) {
+        size_t base = visits.size();
+        visits.resize(base + (size_t)h_ctr->nrec);
+        cudaMemcpyAsync(visits.data() + base, d_rec, sizeof(VisitRec) * (size_t)h_ctr->nrec,
+                        cudaMemcpyDeviceToHost, stream);
+    }
+    if (zone_mode) {
+        zone_velocity(d_uf, d_in_elem, d_fixed, d_xo, d_av, nv, p, zone, d_ctr, stream);
+        counters[9] += 5;
+        cudaMemcpyAsync(h_ctr, d_ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, stream);
+    }
+    if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("pass tail");
+    if (h_ctr->err & kErrNan) return fail(CC_NAN_DETECTED, "non-finite zone velocity (the reference exits here)");
+    *is_collision = h_ctr->nhit_pairs > 0;
+    return CC_OK;
+}
+
+cc_status cc_solver::resolve(const double* x_old, const double* x_cand, double* vel, uint8_t* hc, double* x_out,
+                             int* has_collision) {
+    std::memset(counters, 0, sizeof(counters));
+    pass_index = 0;
+    visits.clear();
+    pass_kinds.clear();
+    if (has_collision) *has_collision = 0;
+    if (ne == 0) {
+        // the reference dereferences an empty tree here; nothing collides
+        if (nv) cudaMemcpyAsync(x_out, x_cand, sizeof(double) * 3 * (size_t)nv, cudaMemcpyDeviceToDevice, stream);
+        cudaStreamSynchronize(stream);
+        return cuda_check("empty mesh");
+    }
+    // d_hc doubles as the device copy of has_collsn
+    if (hc != d_hc) cudaMemcpyAsync(d_hc, hc, (size_t)nv, cudaMemcpyDeviceToDevice, stream);
+    k_reset_counters<<<1, 1, 0, stream>>>(d_ctr);
+    cudaMemsetAsync(&d_ctr->err, 0, sizeof(int), stream);
+    step_init(x_old, x_cand, nv, d_in_elem, prm.dt, d_xo, d_av, d_ctr, stream);
+    uf_init(d_uf, nv, stream);
+    counters[9] += 4;
+    bool is_coll = false;
+    cc_status st = detect_pass(0, 0, &is_coll);
+    if (st) return st;
+    int hcol = 0;
+    is_coll = true;
+    int niter = 1, cd_count = 0;
+    while (is_coll) {
+        st = detect_pass(1, 0, &is_coll);
+        if (st) return st;
+        if (cd_count++ == 0 && is_coll) hcol = 1;
+        if (++niter > kMaxCcdIter) break;
+    }
+    if (is_coll) {
+        int it = 0;
+        while (is_coll) {
+            if (it++ >= zone_cap) return fail(CC_ITER_CAP, "impact-zone loop did not converge");
+            st = detect_pass(1, 1, &is_coll);
+            if (st) return st;
+        }
+    }
+    Params p = params();
+    finalize_positions(d_in_elem, d_xo, d_av, d_hc, x_cand, x_out, nv, p, lo, hi, stream);
+    strain_limit(d_edges, nedges, d_xo, d_av, d_flag0, d_dirty, nv, prm.dt, d_strain_passes, stream);
+    final_velocity(d_in_elem, d_hc, d_av, vel, nv, stream);
+    if (hc != d_hc) cudaMemcpyAsync(hc, d_hc, (size_t)nv, cudaMemcpyDeviceToDevice, stream);
+    counters[9] += 3;
+    int sp = 0;
+    cudaMemcpyAsync(&sp, d_strain_passes, sizeof(int), cudaMemcpyDeviceToHost, stream);
+    if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("finalize");
+    counters[7] = nedges ? sp : 1;
+    if (has_collision) *has_collision = hcol;
+    return cuda_check("resolve");
+}
+
+// ------------------------------------------------------------------ C ABI
+extern "C" {
+
+cc_status cc_create(int device, cc_solver** out) {
+    if (!out) return CC_BAD_INPUT;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return CC_CUDA_ERROR;
+    cc_solver* s = new cc_solver;
+    s->device = device;
+    cudaSetDevice(device);
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        dalloc(&s->d_ctr, 1) != cudaSuccess || cudaMallocHost(&s->h_ctr, sizeof(PassCounters)) != cudaSuccess ||
+        cudaMallocHost(&s->h_bbox, 6 * sizeof(unsigned long long)) != cudaSuccess) {
+        delete s;
+        return CC_CUDA_ERROR;
+    }
+    cudaMemset(s->d_ctr, 0, sizeof(PassCounters));
+    *out = s;
+    return CC_OK;
+}
+
+void cc_destroy(cc_solver* s) { delete s; }
+
+cc_status cc_assemble(cc_solver* s, const cc_mesh* mesh) {
+    if (!s) return CC_BAD_INPUT;
+    return s->assemble(mesh);
+}
+
+cc_status cc_set_params(cc_solver* s, const cc_params* p) {
+    if (!s || !p) return CC_BAD_INPUT;
+    s->prm = *p;
+    return CC_OK;
+}
+
+cc_status cc_set_domain_boundary(cc_solver* s, const double lo[3], const double hi[3]) {
+    if (!s || !lo || !hi) return CC_BAD_INPUT;
+    for (int d = 0; d < 3; ++d) {
+        s->lo[d] = lo[d];
+        s->hi[d] = hi[d];
+    }
+    return CC_OK;
+}
+
+cc_status cc_resolve(cc_solver* s, const double* x_old, const double* x_cand, double* vel, uint8_t* has_collsn,
+                     double* x_out, int* has_collision) {
+    if (!s) return CC_BAD_INPUT;
+    if (s->nv && (!x_old || !x_cand || !vel || !has_collsn || !x_out)) return s->fail(CC_BAD_INPUT, "null array");
+    cudaSetDevice(s->device);
+    size_t b3 = sizeof(double) * 3 * (size_t)s->nv;
+    if (s->nv) {
+        cudaMemcpyAsync(s->d_xold_in, x_old, b3, cudaMemcpyHostToDevice, s->stream);
+        cudaMemcpyAsync(s->d_xcand_in, x_cand, b3, cudaMemcpyHostToDevice, s->stream);
+        cudaMemcpyAsync(s->d_vel, vel, b3, cudaMemcpyHostToDevice, s->stream);
+        cudaMemcpyAsync(s->d_hc, has_collsn, (size_t)s->nv, cudaMemcpyHostToDevice, s->stream);
+    }
+    cc_status st = s->resolve(s->d_xold_in, s->d_xcand_in, s->d_vel, s->d_hc, s->d_xout, has_collision);
+    if (st) return st;
+    if (s->nv) {
+        cudaMemcpyAsync(x_out, s->d_xout, b3, cudaMemcpyDeviceToHost, s->stream);
+        cudaMemcpyAsync(vel, s->d_vel, b3, cudaMemcpyDeviceToHost, s->stream);
+        cudaMemcpyAsync(has_collsn, s->d_hc, (size_t)s->nv, cudaMemcpyDeviceToHost, s->stream);
+    }
+    if (cudaStreamSynchronize(s->stream) != cudaSuccess) return s->cuda_check("read back");
+    return CC_OK;
+}
+
+cc_status cc_resolve_device(cc_solver* s, const double* x_old, const double* x_cand, double* vel,
+                            uint8_t* has_collsn, double* x_out, int* has_collision) {
+    if (!s) return CC_BAD_INPUT;
+    cudaSetDevice(s->device);
+    return s->resolve(x_old, x_cand, vel, has_collsn, x_out, has_collision);
+}
+
+int cc_get_counters(cc_solver* s, long long* out, int n) {
+    if (!s || !out) return 0;
+    int m = n < 10 ? n : 10;
+    for (int i = 0; i < m; ++i) out[i] = s->counters[i];
+    return m;
+}
+
+cc_status cc_set_recording(cc_solver* s, int on) {
+    if (!s) return CC_BAD_INPUT;
+    cudaSetDevice(s->device);
+    s->record = on != 0;
+    if (s->record && s->pair_cap && s->rec_cap < s->pair_cap) return s->grow_pairs(s->pair_cap);
+    return CC_OK;
+}
+
+int cc_get_visits(cc_solver* s, int* out, int cap) {
+    if (!s) return -1;
+    int n = (int)s->visits.size();
+    if (out)
+        for (int i = 0; i < n && i < cap; ++i) {
+            const VisitRec& r = s->visits[i];
+            int* o = out + 13 * i;
+            o[0] = r.pass; o[1] = r.kind; o[2] = r.a; o[3] = r.b; o[4] = r.status;
+            for (int k = 0; k < 6; ++k) o[5 + k] = r.dcount[k];
+            o[11] = r.rank_b; o[12] = r.rank_a;
+        }
+    return n;
+}
+
+int cc_get_pass_kinds(cc_solver* s, int* out, int cap) {
+    if (!s) return -1;
+    int n = (int)s->pass_kinds.size();
+    if (out)
+        for (int i = 0; i < n && i < cap; ++i) out[i] = s->pass_kinds[i];
+    return n;
+}
+
+cc_status cc_get_zone_roots(cc_solver* s, int* out) {
+    if (!s || !out) return CC_BAD_INPUT;
+    cudaSetDevice(s->device);
+    if (s->nv == 0) return CC_OK;
+    std::vector<int> parent((size_t)s->nv);
+    cudaMemcpyAsync(parent.data(), s->d_uf, sizeof(int) * (size_t)s->nv, cudaMemcpyDeviceToHost, s->stream);
+    if (cudaStreamSynchronize(s->stream) != cudaSuccess) return s->cuda_check("zone roots");
+    for (int i = 0; i < s->nv; ++i) {
+        int r = i, guard = 0;
+        while (parent[r] != r && guard++ < s->nv) r = parent[r];
+        out[i] = r;
+    }
+    return CC_OK;
+}
+
+cc_status cc_get_leaf_ranks(cc_solver* s, int which, int* out) {
+    if (!s || !out || which < 0 || which > 1 || !s->tree[which].built()) return CC_BAD_INPUT;
+    s->tree[which].ranks(out);
+    return CC_OK;
+}
+
+int cc_debug_candidate_pairs(cc_solver* s, int moving, int brute_force, int* out, int cap) {
+    if (!s || s->ne == 0) return 0;
+    cudaSetDevice(s->device);
+    leaf_boxes(s->d_ev, s->ne, s->nt, s->d_xo, s->d_av, s->prm.dt, moving, s->d_box, s->bvh.bbox_enc, s->stream);
+    if (!brute_force) bvh_build(s->d_box, s->bvh, s->stream);
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        k_reset_counters<<<1, 1, 0, s->stream>>>(s->d_ctr);
+        cudaMemsetAsync(&s->d_ctr->err, 0, sizeof(int), s->stream);
+        if (brute_force)
+            brute_pairs(s->d_box, s->ne, s->d_pairs, s->pair_cap, s->d_ctr, s->stream);
+        else
+            bvh_pairs(s->d_box, s->bvh, s->d_pairs, s->pair_cap, s->d_ctr, s->stream);
+        cudaMemcpyAsync(s->h_ctr, s->d_ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, s->stream);
+        if (cudaStreamSynchronize(s->stream) != cudaSuccess) return -1;
+        if (s->h_ctr->err & kErrPairOverflow) {
+            if (s->grow_pairs(2 * s->h_ctr->npairs + 1024)) return -1;
+            continue;
+        }
+        if (s->h_ctr->err) return -1;
+        break;
+    }
+    int n = s->h_ctr->npairs;
+    if (out && n > 0) {
+        int m = n < cap ? n : cap;
+        cudaMemcpyAsync(out, s->d_pairs, sizeof(int2) * (size_t)m, cudaMemcpyDeviceToHost, s->stream);
+        cudaStreamSynchronize(s->stream);
+    }
+    return n;
+}
+
+int cc_last_error(cc_solver* s, char* buf, int len) {
+    if (!s || !buf || len <= 0) return 0;
+    std::snprintf(buf, (size_t)len, "%s", s->err.c_str());
+    return (int)s->err.size();
+}
+
+}  // extern "C"

@@ -1,0 +1,197 @@
+"""CollisionSolver3d: the reference's solver surface over the GPU library.
+
+Mirrors antdvid/Collision's CollisionSolver3d (collid.h:128-244): the
+parameter setters (there class statics, collid.h:180-193; here per solver),
+setDomainBoundary, resolveCollision and hasCollision. assembleFromMesh takes
+triangle / bond lists and replaces assembleFromInterface (collid.h:242),
+whose FronTier interface is not part of this library.
+
+Positions and velocities are numpy arrays of shape (n_points, 3) float64 on
+the host (resolveCollision: copies inside the call) or torch CUDA tensors
+(resolveCollisionDevice: no copies).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .scenes import DEFAULTS, PARAM_NAMES
+
+
+def _c(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+class CollisionSolver3d:
+    def __init__(self, device: int = 0):
+        self._lib = _lib.load()
+        h = C.c_void_p()
+        st = self._lib.cc_create(int(device), C.byref(h))
+        if st != 0:
+            raise _lib.CCError(st, f"cc_create(device={device}) failed")
+        self._h = h
+        self._params = dict(DEFAULTS)
+        self._has_collision = False
+        self._nv = 0
+        self._ne = 0
+        self._push_params()
+
+    # ------------------------------------------------------------ lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.cc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != 0:
+            buf = C.create_string_buffer(512)
+            self._lib.cc_last_error(self._h, buf, 512)
+            raise _lib.CCError(st, buf.value.decode(errors="replace"))
+
+    # --------------------------------------------------------- parameters
+    def _push_params(self):
+        p = _lib.cc_params(*[float(self._params[k]) for k in PARAM_NAMES])
+        self._check(self._lib.cc_set_params(self._h, C.byref(p)))
+
+    def _set(self, k, v):
+        self._params[k] = float(v)
+        self._push_params()
+
+    def setTimeStepSize(self, dt): self._set("dt", dt)
+    def getTimeStepSize(self): return self._params["dt"]
+    def setFabricThickness(self, h): self._set("thickness", h)
+    def getFabricThickness(self): return self._params["thickness"]
+    def setRoundingTolerance(self, eps): self._set("eps", eps)
+    def getRoundingTolerance(self): return self._params["eps"]
+    def setSpringConstant(self, k): self._set("k", k)
+    def getSpringConstant(self): return self._params["k"]
+    def setPointMass(self, m): self._set("m", m)
+    def getPointMass(self): return self._params["m"]
+    def setFrictionConstant(self, lam): self._set("lam", lam)
+    def getFrictionConstant(self): return self._params["lam"]
+    def setRestitutionCoef(self, cr): self._set("cr", cr)
+    def getRestitutionCoef(self): return self._params["cr"]
+
+    def setParams(self, params: dict):
+        self._params.update({k: float(v) for k, v in params.items() if k in PARAM_NAMES})
+        self._push_params()
+
+    def setDomainBoundary(self, L, U):
+        lo = _c(L, np.float64)
+        hi = _c(U, np.float64)
+        self._check(self._lib.cc_set_domain_boundary(self._h, lo.ctypes.data, hi.ctypes.data))
+
+    # ------------------------------------------------------------- mesh
+    def assembleFromMesh(self, n_points, tris=None, tri_surface=None, tri_rest=None, bonds=None,
+                         bond_rest=None, fixed=None):
+        tris = _c(tris if tris is not None else np.zeros((0, 3)), np.int32).reshape(-1, 3)
+        nt = tris.shape[0]
+        tri_surface = _c(tri_surface if tri_surface is not None else np.zeros(nt), np.int32)
+        tri_rest = _c(tri_rest if tri_rest is not None else np.zeros((nt, 3)), np.float64).reshape(-1, 3)
+        bonds = _c(bonds if bonds is not None else np.zeros((0, 2)), np.int32).reshape(-1, 2)
+        nb = bonds.shape[0]
+        bond_rest = _c(bond_rest if bond_rest is not None else np.zeros(nb), np.float64)
+        fixed = _c(fixed if fixed is not None else np.zeros(n_points), np.uint8)
+        self._keep = (tris, tri_surface, tri_rest, bonds, bond_rest, fixed)
+        m = _lib.cc_mesh(int(n_points), nt, tris.ctypes.data, tri_surface.ctypes.data, tri_rest.ctypes.data,
+                         nb, bonds.ctypes.data, bond_rest.ctypes.data, fixed.ctypes.data)
+        self._check(self._lib.cc_assemble(self._h, C.byref(m)))
+        self._nv = int(n_points)
+        self._ne = nt + nb
+
+    def assembleFromScene(self, scene):
+        """Mesh, parameters and domain of a collision_gb300.scenes.Scene."""
+        self.assembleFromMesh(scene.nv, scene.tris, scene.tri_surf, scene.tri_rest, scene.bonds,
+                              scene.bond_rest, scene.fixed)
+        self.setParams(scene.params)
+        self.setDomainBoundary(scene.domain[:3], scene.domain[3:])
+
+    # -------------------------------------------------------------- step
+    def resolveCollision(self, x_old, x_cand, vel, has_collsn):
+        """One resolveCollision() on host arrays. Returns (x_new, vel, has_collsn)."""
+        x_old = _c(x_old, np.float64)
+        x_cand = _c(x_cand, np.float64)
+        vel = np.array(vel, dtype=np.float64, copy=True, order="C")
+        hc = np.array(has_collsn, dtype=np.uint8, copy=True, order="C")
+        x_out = np.empty_like(x_old)
+        hcol = C.c_int(0)
+        self._check(self._lib.cc_resolve(self._h, x_old.ctypes.data, x_cand.ctypes.data, vel.ctypes.data,
+                                         hc.ctypes.data, x_out.ctypes.data, C.byref(hcol)))
+        self._has_collision = bool(hcol.value)
+        return x_out, vel, hc
+
+    def resolveCollisionDevice(self, x_old, x_cand, vel, has_collsn, x_out):
+        """One resolveCollision() on device tensors (torch, on this solver's
+        device, contiguous float64 / uint8). vel and has_collsn are updated in
+        place; x_out receives the final positions."""
+        hcol = C.c_int(0)
+        self._check(self._lib.cc_resolve_device(self._h, x_old.data_ptr(), x_cand.data_ptr(), vel.data_ptr(),
+                                                has_collsn.data_ptr(), x_out.data_ptr(), C.byref(hcol)))
+        self._has_collision = bool(hcol.value)
+
+    def hasCollision(self) -> bool:
+        return self._has_collision
+
+    # ------------------------------------------------------- inspection
+    COUNTER_NAMES = ("passes", "ccd_passes", "zone_passes", "candidate_pairs", "visits", "hit_pairs",
+                     "contacts", "strain_passes", "tree_builds", "kernel_launches")
+
+    def counters(self) -> dict:
+        out = (C.c_longlong * 10)()
+        n = self._lib.cc_get_counters(self._h, out, 10)
+        return dict(zip(self.COUNTER_NAMES[:n], list(out)[:n]))
+
+    def setRecording(self, on: bool):
+        self._check(self._lib.cc_set_recording(self._h, int(bool(on))))
+
+    def visits(self) -> np.ndarray:
+        """(n, 13) int32: pass, kind, a, b, status, dcount[6], rank_b, rank_a."""
+        n = self._lib.cc_get_visits(self._h, None, 0)
+        out = np.zeros((max(n, 0), 13), dtype=np.int32)
+        if n > 0:
+            self._lib.cc_get_visits(self._h, out.ctypes.data_as(C.POINTER(C.c_int)), n)
+        return out
+
+    def passKinds(self) -> np.ndarray:
+        n = self._lib.cc_get_pass_kinds(self._h, None, 0)
+        out = np.zeros(max(n, 0), dtype=np.int32)
+        if n > 0:
+            self._lib.cc_get_pass_kinds(self._h, out.ctypes.data_as(C.POINTER(C.c_int)), n)
+        return out
+
+    def zoneRoots(self) -> np.ndarray:
+        out = np.zeros(self._nv, dtype=np.int32)
+        self._check(self._lib.cc_get_zone_roots(self._h, out.ctypes.data_as(C.POINTER(C.c_int))))
+        return out
+
+    def leafRanks(self, which: int):
+        out = np.zeros(self._ne, dtype=np.int32)
+        st = self._lib.cc_get_leaf_ranks(self._h, int(which), out.ctypes.data_as(C.POINTER(C.c_int)))
+        return out if st == 0 else None
+
+    def candidatePairs(self, moving: bool, brute_force: bool = False) -> np.ndarray:
+        n = self._lib.cc_debug_candidate_pairs(self._h, int(moving), int(brute_force), None, 0)
+        if n < 0:
+            self._check(2)
+        out = np.zeros((n, 2), dtype=np.int32)
+        if n:
+            self._lib.cc_debug_candidate_pairs(self._h, int(moving), int(brute_force),
+                                               out.ctypes.data_as(C.POINTER(C.c_int)), n)
+        return out
+
+
+def ordered_visits(v: np.ndarray) -> np.ndarray:
+    """GPU visit records in the reference's visiting order: by pass, then
+    query-leaf rank, then found-leaf rank; returns the 11-column oracle form."""
+    if len(v) == 0:
+        return np.zeros((0, 11), dtype=np.int32)
+    idx = np.lexsort((v[:, 12], v[:, 11], v[:, 0]))
+    return v[idx, :11]

