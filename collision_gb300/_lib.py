@@ -80,6 +80,14 @@ def load(path: str = LIB_PATH):
     lib.cc_get_leaf_ranks.argtypes = [vp, C.c_int, ip]
     lib.cc_debug_candidate_pairs.restype = C.c_int
     lib.cc_debug_candidate_pairs.argtypes = [vp, C.c_int, C.c_int, ip, C.c_int]
+    lib.cc_set_stream.restype = C.c_int
+    lib.cc_set_stream.argtypes = [vp, vp]
+    lib.cc_set_profiling.restype = C.c_int
+    lib.cc_set_profiling.argtypes = [vp, C.c_int]
+    lib.cc_get_profile.restype = C.c_int
+    lib.cc_get_profile.argtypes = [vp, C.POINTER(C.c_double), lp, C.c_int]
+    lib.cc_profile_stage_name.restype = C.c_char_p
+    lib.cc_profile_stage_name.argtypes = [C.c_int]
     lib.cc_last_error.restype = C.c_int
     lib.cc_last_error.argtypes = [vp, C.c_char_p, C.c_int]
     _LIB = lib

@@ -238,34 +238,34 @@ inline int nblk(int n, int t) { return (n + t - 1) / t; }
 
 void leaf_boxes(const int* ev, int ne, int nt, const double4_32a* xo, const double4_32a* av, double dt, int moving,
                 Box6* box, unsigned long long* bbox_enc, cudaStream_t s) {
-    k_bbox_init<<<1, 32, 0, s>>>(bbox_enc);
+    count_launch(), k_bbox_init<<<1, 32, 0, s>>>(bbox_enc);
     if (ne <= 0) return;
     if (moving)
-        k_leaf_boxes<1><<<nblk(ne, 256), 256, 0, s>>>(ev, ne, nt, xo, av, dt, box, bbox_enc);
+        count_launch(), k_leaf_boxes<1><<<nblk(ne, 256), 256, 0, s>>>(ev, ne, nt, xo, av, dt, box, bbox_enc);
     else
-        k_leaf_boxes<0><<<nblk(ne, 256), 256, 0, s>>>(ev, ne, nt, xo, av, dt, box, bbox_enc);
+        count_launch(), k_leaf_boxes<0><<<nblk(ne, 256), 256, 0, s>>>(ev, ne, nt, xo, av, dt, box, bbox_enc);
 }
 
 void bvh_build(const Box6* box, BvhBufs& b, cudaStream_t s) {
     int n = b.n;
     if (n <= 1) return;
-    k_morton<<<nblk(n, 256), 256, 0, s>>>(box, n, b.bbox_enc, b.keys, b.order);
+    count_launch(), k_morton<<<nblk(n, 256), 256, 0, s>>>(box, n, b.bbox_enc, b.keys, b.order);
     radix_sort_pairs(b.keys, b.order, n, 30, b.sort_temp, s);
-    k_karras<<<nblk(n - 1, 256), 256, 0, s>>>(b.keys, n, b.child, b.range_hi, b.parent);
+    count_launch(), k_karras<<<nblk(n - 1, 256), 256, 0, s>>>(b.keys, n, b.child, b.range_hi, b.parent);
     cudaMemsetAsync(b.flags, 0, sizeof(int) * (size_t)(n - 1), s);
-    k_refit<<<nblk(n, 256), 256, 0, s>>>(box, b.order, n, b.child, b.parent, b.flags, b.node_box);
+    count_launch(), k_refit<<<nblk(n, 256), 256, 0, s>>>(box, b.order, n, b.child, b.parent, b.flags, b.node_box);
 }
 
 void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCounters* ctr, cudaStream_t s) {
     int n = b.n;
     if (n <= 1) return;
-    k_traverse<<<nblk(n - 1, 128), 128, 0, s>>>(box, b.order, n, b.child, b.range_hi, b.node_box, pairs, cap,
+    count_launch(), k_traverse<<<nblk(n - 1, 128), 128, 0, s>>>(box, b.order, n, b.child, b.range_hi, b.node_box, pairs, cap,
                                                   ctr);
 }
 
 void brute_pairs(const Box6* box, int ne, int2* pairs, int cap, PassCounters* ctr, cudaStream_t s) {
     if (ne <= 1) return;
-    k_brute_pairs<<<nblk(ne, 128), 128, 0, s>>>(box, ne, pairs, cap, ctr);
+    count_launch(), k_brute_pairs<<<nblk(ne, 128), 128, 0, s>>>(box, ne, pairs, cap, ctr);
 }
 
 }  // namespace ccg

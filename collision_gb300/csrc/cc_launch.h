@@ -9,6 +9,10 @@
 
 namespace ccg {
 
+// Kernels launched by this library since load (read by cc_get_counters).
+extern long long g_kernel_launches;
+inline void count_launch(int n = 1) { g_kernel_launches += n; }
+
 // ------------------------------------------------------------- primitives
 // Scratch bytes needed to sort n (key, value) pairs.
 size_t radix_sort_temp_bytes(int n);
@@ -111,8 +115,11 @@ struct StrainEdge {
     int p0, p1;
     double len0;
 };
-void strain_limit(const StrainEdge* edges, int nedges, const double4_32a* xo, double4_32a* av, uint8_t* flag0,
-                  uint8_t* dirty, int nv, double dt, int* passes_out, cudaStream_t s);
+// edges sorted by dependency level; level_off has nlevels+1 offsets;
+// step_buf holds strain_step_bytes(nedges).
+size_t strain_step_bytes(int nedges);
+void strain_limit(const StrainEdge* edges, int nedges, const int* level_off, int nlevels, const double4_32a* xo,
+                  double4_32a* av, double dt, void* step_buf, int* passes_out, cudaStream_t s);
 // updateFinalVelocity.
 void final_velocity(const uint8_t* in_elem, const uint8_t* has_collsn, const double4_32a* av, double* vel, int nv,
                     cudaStream_t s);

@@ -78,9 +78,9 @@ void narrow_pass(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s)
     int blocks = (max_pairs + threads - 1) / threads;
     if (blocks > 152 * 16) blocks = 152 * 16;
     if (moving)
-        k_narrow<true><<<blocks, threads, 0, s>>>(a, max_pairs);
+        count_launch(), k_narrow<true><<<blocks, threads, 0, s>>>(a, max_pairs);
     else
-        k_narrow<false><<<blocks, threads, 0, s>>>(a, max_pairs);
+        count_launch(), k_narrow<false><<<blocks, threads, 0, s>>>(a, max_pairs);
 }
 
 }  // namespace ccg

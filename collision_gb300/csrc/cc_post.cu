@@ -242,13 +242,15 @@ __global__ void k_finalize(const uint8_t* __restrict__ in_elem, const double4_32
     for (int j = 0; j < 3; ++j) x_out[3 * p + j] = xs[j] + v[j] * dt;
 }
 
-// One edge's strain test, reduceSuperelastOnce (dcollid.cpp:496-539).
-__device__ __forceinline__ bool strain_flag(const StrainEdge& e, const double4_32a* xo, const double4_32a* av, double dt) {
+// One edge's strain test, reduceSuperelastOnce (dcollid.cpp:496-539),
+// evaluated as the reference does.
+__device__ __forceinline__ bool strain_flag_exact(int p0, int p1, double len0, const double4_32a* xo,
+                                                  const double4_32a* av, double dt) {
     double x0[3], x1[3], v0[3], v1[3], c0[3], c1[3];
-    load3(xo, e.p0, x0);
-    load3(xo, e.p1, x1);
-    load3(av, e.p0, v0);
-    load3(av, e.p1, v1);
+    load3(xo, p0, x0);
+    load3(xo, p1, x1);
+    load3(av, p0, v0);
+    load3(av, p1, v1);
     for (int k = 0; k < 3; ++k) {
         c0[k] = x0[k] + dt * v0[k];
         c1[k] = x1[k] + dt * v1[k];
@@ -259,70 +261,126 @@ __device__ __forceinline__ bool strain_flag(const StrainEdge& e, const double4_3
     double len_new = sqrt(sn), len_old = sqrt(so);
     if (len_old > kRoundEps && len_new > kRoundEps) {
         double strain_rate = (len_new - len_old) / len_old;
-        double strain = (len_new - e.len0) / e.len0;
+        double strain = (len_new - len0) / len0;
         return fabs(strain) > kStrainTol || fabs(strain_rate) > kStrainTol;
     }
     return true;
 }
 
-// reduceSuperelast, dcollid.cpp:586-596: up to 10 Gauss-Seidel passes. The
-// sweep order matters (each averaged edge changes the points its successors
-// read), so one warp walks the edges in element order; every pass first
-// evaluates all edges against the pass-start velocities in parallel, and the
-// walk re-evaluates only edges whose points were averaged earlier in the pass.
-__global__ void __launch_bounds__(1024) k_strain(const StrainEdge* __restrict__ edges, int m,
-                                                 const double4_32a* __restrict__ xo, double4_32a* av, uint8_t* flag0,
-                                                 uint8_t* dirty, int nv, double dt, int* passes_out) {
+// Squared-length bounds that decide |(sqrt(s) - L)/L| > 0.1 without the
+// square root and the division: outside [lo_no, hi_no] the answer is "over",
+// inside [lo_def, hi_def] ... see strain_quick. The bounds sit 1e-9 (relative)
+// inside and outside the exact thresholds L*(1 -+ 0.1); the reference's own
+// rounding of sqrt, subtraction and division is below 1e-15, so a decision
+// taken here equals the reference's.
+struct StrainBounds {
+    double hi_def, hi_no, lo_no, lo_def;
+};
+__device__ __forceinline__ StrainBounds strain_bounds(double L) {
+    StrainBounds b;
+    double a = L * (1.1 * (1.0 + 1e-9)), c = L * (1.1 * (1.0 - 1e-9));
+    double d = L * (0.9 * (1.0 + 1e-9)), e = L * (0.9 * (1.0 - 1e-9));
+    b.hi_def = a * a;  // s above: over-stretched for sure
+    b.hi_no = c * c;   // s below (and above lo_no): not over-stretched
+    b.lo_no = d * d;
+    b.lo_def = e * e;  // s below: over-compressed for sure
+    return b;
+}
+// 1: over the limit, 0: within it, -1: too close to tell without the exact test.
+__device__ __forceinline__ int strain_quick(double s, const StrainBounds& b) {
+    if (s > b.hi_def || s < b.lo_def) return 1;
+    if (s < b.hi_no && s > b.lo_no) return 0;
+    return -1;
+}
+
+struct StrainEdgeStep {
+    int p0, p1;
+    double len0;
+    StrainBounds rest;  // from the rest length
+    StrainBounds prev;  // from the start-of-step length (strain rate)
+    int exact_only;     // degenerate lengths: always take the exact test
+    int pad;
+};
+
+// Per-step set-up of the strain sweep: the start-of-step length of every
+// edge (x_old does not change during the sweep) and both sets of bounds.
+__global__ void k_strain_setup(const StrainEdge* __restrict__ edges, int m, const double4_32a* __restrict__ xo,
+                               StrainEdgeStep* out) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= m) return;
+    StrainEdge ed = edges[e];
+    double x0[3], x1[3];
+    load3(xo, ed.p0, x0);
+    load3(xo, ed.p1, x1);
+    double so = 0.0;
+    for (int k = 0; k < 3; ++k) so += sqr(x0[k] - x1[k]);
+    double len_old = sqrt(so);
+    StrainEdgeStep r;
+    r.p0 = ed.p0;
+    r.p1 = ed.p1;
+    r.len0 = ed.len0;
+    r.rest = strain_bounds(ed.len0);
+    r.prev = strain_bounds(len_old);
+    // tiny or non-positive lengths: leave every decision to the exact test
+    r.exact_only = !(len_old > 1e-6 && ed.len0 > 1e-6);
+    r.pad = 0;
+    out[e] = r;
+}
+
+__device__ __forceinline__ bool strain_flag(const StrainEdgeStep& ed, const double4_32a* xo, const double4_32a* av,
+                                            double dt) {
+    if (!ed.exact_only) {
+        double4_32a a0 = xo[ed.p0], a1 = xo[ed.p1], b0 = av[ed.p0], b1 = av[ed.p1];
+        double d0 = (a0.x + dt * b0.x) - (a1.x + dt * b1.x);
+        double d1 = (a0.y + dt * b0.y) - (a1.y + dt * b1.y);
+        double d2 = (a0.z + dt * b0.z) - (a1.z + dt * b1.z);
+        double sn = 0.0;
+        sn += d0 * d0;
+        sn += d1 * d1;
+        sn += d2 * d2;
+        if (sn > 1e-18) {
+            int q0 = strain_quick(sn, ed.rest), q1 = strain_quick(sn, ed.prev);
+            if (q0 == 1 || q1 == 1) return true;
+            if (q0 == 0 && q1 == 0) return false;
+        }
+    }
+    return strain_flag_exact(ed.p0, ed.p1, ed.len0, xo, av, dt);
+}
+
+// reduceSuperelast, dcollid.cpp:586-596: up to 10 Gauss-Seidel passes over
+// the edges in element order, each averaging the two end velocities of an
+// over-strained edge before the next edge is tested. The edges arrive sorted
+// by dependency level (an edge's level is one more than the level of the
+// last earlier edge at either of its points), so the edges of one level share
+// no point and see exactly the values the sequential sweep gives them: the
+// level-by-level walk below is the reference's sweep, reordered only where
+// the order cannot matter.
+__global__ void __launch_bounds__(512) k_strain(const StrainEdgeStep* __restrict__ edges,
+                                                const int* __restrict__ level_off, int nlevels,
+                                                const double4_32a* __restrict__ xo, double4_32a* av, double dt,
+                                                int* passes_out) {
     __shared__ int s_has;
     int passes = 0;
     for (int pass = 0; pass < kStrainMaxIter; ++pass) {
-        for (int e = threadIdx.x; e < m; e += blockDim.x) flag0[e] = strain_flag(edges[e], xo, av, dt) ? 1 : 0;
-        for (int p = threadIdx.x; p < nv; p += blockDim.x) dirty[p] = 0;
+        if (threadIdx.x == 0) s_has = 0;
         __syncthreads();
         passes++;
-        if (threadIdx.x < 32) {
-            const int lane = threadIdx.x;
-            bool has = false;
-            for (int base = 0; base < m; base += 32) {
-                int e = base + lane;
-                bool valid = e < m;
-                StrainEdge ed;
-                if (valid) ed = edges[e];
-                unsigned pre0 = __ballot_sync(0xffffffffu, valid && flag0[valid ? e : 0]);
-                int cursor = 0;
-                while (true) {
-                    bool f = false;
-                    if (valid && lane >= cursor) {
-                        volatile uint8_t* dv = dirty;
-                        if (dv[ed.p0] || dv[ed.p1])
-                            f = strain_flag(ed, xo, av, dt);
-                        else
-                            f = flag0[e] != 0;
-                    }
-                    unsigned b = __ballot_sync(0xffffffffu, f);
-                    if (b == 0) break;
-                    int first = __ffs(b) - 1;
-                    if (lane == first) {
-                        double4_32a a0 = av[ed.p0], a1 = av[ed.p1];
-                        double t0 = a0.x + a1.x, t1 = a0.y + a1.y, t2 = a0.z + a1.z;
-                        t0 = 0.5 * t0; t1 = 0.5 * t1; t2 = 0.5 * t2;
-                        double4_32a nv4 = make_double4_32a(t0, t1, t2, 0.0);
-                        av[ed.p0] = nv4;
-                        av[ed.p1] = nv4;
-                        dirty[ed.p0] = 1;
-                        dirty[ed.p1] = 1;
-                    }
-                    has = true;
-                    __syncwarp();
-                    __threadfence_block();
-                    cursor = first + 1;
-                    if (cursor >= 32) break;
+        for (int l = 0; l < nlevels; ++l) {
+            int e1 = level_off[l + 1];
+            for (int e = level_off[l] + threadIdx.x; e < e1; e += blockDim.x) {
+                StrainEdgeStep ed = edges[e];
+                if (strain_flag(ed, xo, av, dt)) {
+                    double4_32a a0 = av[ed.p0], a1 = av[ed.p1];
+                    double t0 = a0.x + a1.x, t1 = a0.y + a1.y, t2 = a0.z + a1.z;
+                    t0 = 0.5 * t0; t1 = 0.5 * t1; t2 = 0.5 * t2;
+                    double4_32a nv4 = make_double4_32a(t0, t1, t2, 0.0);
+                    av[ed.p0] = nv4;
+                    av[ed.p1] = nv4;
+                    s_has = 1;
                 }
-                (void)pre0;
             }
-            if (lane == 0) s_has = has ? 1 : 0;
+            __syncthreads();
         }
-        __syncthreads();
         if (!s_has) break;
         __syncthreads();
     }
@@ -343,7 +401,7 @@ __global__ void k_final_velocity(const uint8_t* __restrict__ in_elem, const uint
 
 void step_init(const double* x_old, const double* x_cand, int nv, const uint8_t* in_elem, double dt, double4_32a* xo,
                double4_32a* av, PassCounters* ctr, cudaStream_t s) {
-    if (nv > 0) k_step_init<<<nblk(nv, 256), 256, 0, s>>>(x_old, x_cand, nv, in_elem, dt, xo, av, ctr);
+    if (nv > 0) count_launch(), k_step_init<<<nblk(nv, 256), 256, 0, s>>>(x_old, x_cand, nv, in_elem, dt, xo, av, ctr);
 }
 
 void apply_contribs(const Contrib* contrib, const PassCounters* ctr, int contrib_cap, int nv, double4_32a* av,
@@ -353,15 +411,15 @@ void apply_contribs(const Contrib* contrib, const PassCounters* ctr, int contrib
     cudaMemsetAsync(b.cur, 0, sizeof(int) * (size_t)nv, s);
     int blocks = nblk(contrib_cap, 256);
     if (blocks > 152 * 8) blocks = 152 * 8;
-    k_contrib_count<<<blocks, 256, 0, s>>>(contrib, ctr, contrib_cap, b.cnt);
+    count_launch(), k_contrib_count<<<blocks, 256, 0, s>>>(contrib, ctr, contrib_cap, b.cnt);
     exclusive_scan(b.cnt, b.off, nv, nullptr, b.scan_temp, s);
-    k_contrib_scatter<<<blocks, 256, 0, s>>>(contrib, ctr, contrib_cap, b.off, b.cur, b.idx);
-    k_apply<<<nblk(nv, 128), 128, 0, s>>>(contrib, const_cast<PassCounters*>(ctr), b.cnt, b.off, b.idx, nv, av,
+    count_launch(), k_contrib_scatter<<<blocks, 256, 0, s>>>(contrib, ctr, contrib_cap, b.off, b.cur, b.idx);
+    count_launch(), k_apply<<<nblk(nv, 128), 128, 0, s>>>(contrib, const_cast<PassCounters*>(ctr), b.cnt, b.off, b.idx, nv, av,
                                            has_collsn);
 }
 
 void uf_init(int* parent, int nv, cudaStream_t s) {
-    if (nv > 0) k_uf_init<<<nblk(nv, 256), 256, 0, s>>>(parent, nv);
+    if (nv > 0) count_launch(), k_uf_init<<<nblk(nv, 256), 256, 0, s>>>(parent, nv);
 }
 
 void zone_velocity(int* parent, const uint8_t* in_elem, const uint8_t* fixed, const double4_32a* xo, double4_32a* av,
@@ -369,8 +427,8 @@ void zone_velocity(int* parent, const uint8_t* in_elem, const uint8_t* fixed, co
     if (nv <= 0) return;
     cudaMemsetAsync(z.zcnt, 0, sizeof(int) * (size_t)nv, s);
     cudaMemsetAsync(z.nmembers, 0, sizeof(int), s);
-    k_uf_flatten<<<nblk(nv, 256), 256, 0, s>>>(parent, in_elem, nv, z.root, z.zcnt);
-    k_zone_keys<<<nblk(nv, 256), 256, 0, s>>>(z.root, z.zcnt, in_elem, nv, z.keys, z.vals, z.nmembers);
+    count_launch(), k_uf_flatten<<<nblk(nv, 256), 256, 0, s>>>(parent, in_elem, nv, z.root, z.zcnt);
+    count_launch(), k_zone_keys<<<nblk(nv, 256), 256, 0, s>>>(z.root, z.zcnt, in_elem, nv, z.keys, z.vals, z.nmembers);
     int nm = 0;
     cudaMemcpyAsync(&nm, z.nmembers, sizeof(int), cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
@@ -378,29 +436,33 @@ void zone_velocity(int* parent, const uint8_t* in_elem, const uint8_t* fixed, co
     int bits = 32;
     while (bits < 64 && ((unsigned long long)(nv - 1) >> (bits - 32)) != 0ull) ++bits;
     radix_sort_pairs(z.keys, z.vals, nm, bits, z.sort_temp, s);
-    k_zone_solve<<<nblk(nm, 128), 128, 0, s>>>(z.keys, z.vals, z.nmembers, fixed, xo, av, p, ctr);
+    count_launch(), k_zone_solve<<<nblk(nm, 128), 128, 0, s>>>(z.keys, z.vals, z.nmembers, fixed, xo, av, p, ctr);
 }
 
 void finalize_positions(const uint8_t* in_elem, const double4_32a* xo, double4_32a* av, uint8_t* has_collsn,
                         const double* x_cand, double* x_out, int nv, const Params& p, const double* lo,
                         const double* hi, cudaStream_t s) {
     if (nv > 0)
-        k_finalize<<<nblk(nv, 256), 256, 0, s>>>(in_elem, xo, av, has_collsn, x_cand, x_out, nv, p, lo[0], lo[1],
+        count_launch(), k_finalize<<<nblk(nv, 256), 256, 0, s>>>(in_elem, xo, av, has_collsn, x_cand, x_out, nv, p, lo[0], lo[1],
                                                  lo[2], hi[0], hi[1], hi[2]);
 }
 
-void strain_limit(const StrainEdge* edges, int nedges, const double4_32a* xo, double4_32a* av, uint8_t* flag0,
-                  uint8_t* dirty, int nv, double dt, int* passes_out, cudaStream_t s) {
-    if (nedges <= 0) {
+size_t strain_step_bytes(int nedges) { return sizeof(StrainEdgeStep) * (size_t)(nedges > 0 ? nedges : 1); }
+
+void strain_limit(const StrainEdge* edges, int nedges, const int* level_off, int nlevels, const double4_32a* xo,
+                  double4_32a* av, double dt, void* step_buf, int* passes_out, cudaStream_t s) {
+    if (nlevels <= 0) {
         cudaMemsetAsync(passes_out, 0, sizeof(int), s);
         return;
     }
-    k_strain<<<1, 1024, 0, s>>>(edges, nedges, xo, av, flag0, dirty, nv, dt, passes_out);
+    StrainEdgeStep* se = (StrainEdgeStep*)step_buf;
+    count_launch(), k_strain_setup<<<nblk(nedges, 256), 256, 0, s>>>(edges, nedges, xo, se);
+    count_launch(), k_strain<<<1, 512, 0, s>>>(se, level_off, nlevels, xo, av, dt, passes_out);
 }
 
 void final_velocity(const uint8_t* in_elem, const uint8_t* has_collsn, const double4_32a* av, double* vel, int nv,
                     cudaStream_t s) {
-    if (nv > 0) k_final_velocity<<<nblk(nv, 256), 256, 0, s>>>(in_elem, has_collsn, av, vel, nv);
+    if (nv > 0) count_launch(), k_final_velocity<<<nblk(nv, 256), 256, 0, s>>>(in_elem, has_collsn, av, vel, nv);
 }
 
 }  // namespace ccg

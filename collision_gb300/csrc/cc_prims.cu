@@ -6,6 +6,8 @@
 
 namespace ccg {
 
+long long g_kernel_launches = 0;
+
 namespace {
 
 constexpr int kScanThreads = 1024;
@@ -84,14 +86,14 @@ size_t scan_levels_bytes(int n) {
 void scan_rec(const int* in, int* out, int n, char* temp, cudaStream_t s) {
     int nb = ceil_div(n, kScanTile);
     if (nb <= 1) {
-        k_scan_tile<<<1, kScanThreads, 0, s>>>(in, out, n, nullptr);
+        count_launch(), k_scan_tile<<<1, kScanThreads, 0, s>>>(in, out, n, nullptr);
         return;
     }
     int* sums = (int*)temp;
     char* rest = temp + (((size_t)nb * sizeof(int) + 255) & ~(size_t)255);
-    k_scan_tile<<<nb, kScanThreads, 0, s>>>(in, out, n, sums);
+    count_launch(), k_scan_tile<<<nb, kScanThreads, 0, s>>>(in, out, n, sums);
     scan_rec(sums, sums, nb, rest, s);
-    k_scan_add<<<nb, kScanThreads, 0, s>>>(out, n, sums);
+    count_launch(), k_scan_add<<<nb, kScanThreads, 0, s>>>(out, n, sums);
 }
 
 // ------------------------------------------------------------------ sort
@@ -162,7 +164,7 @@ void exclusive_scan(const int* in, int* out, int n, int* total, void* temp, cuda
     int* last = (int*)((char*)temp + scan_levels_bytes(n));
     if (total) cudaMemcpyAsync(last, in + (n - 1), sizeof(int), cudaMemcpyDeviceToDevice, s);
     scan_rec(in, out, n, (char*)temp, s);
-    if (total) k_scan_total<<<1, 1, 0, s>>>(last, out + (n - 1), 1, total);
+    if (total) count_launch(), k_scan_total<<<1, 1, 0, s>>>(last, out + (n - 1), 1, total);
 }
 
 size_t radix_sort_temp_bytes(int n) {
@@ -195,9 +197,9 @@ void radix_sort_pairs(unsigned long long* keys, unsigned int* vals, int n, int b
     int passes = (bits + 7) / 8;
     for (int ps = 0; ps < passes; ++ps) {
         int shift = ps * 8;
-        k_radix_hist<<<nb, kSortThreads, 0, s>>>(ka, n, shift, hist, nb);
+        count_launch(), k_radix_hist<<<nb, kSortThreads, 0, s>>>(ka, n, shift, hist, nb);
         exclusive_scan(hist, off, (int)hist_n, nullptr, stemp, s);
-        k_radix_scatter<<<nb, kSortThreads, 0, s>>>(ka, va, kb, vb, n, shift, off, nb);
+        count_launch(), k_radix_scatter<<<nb, kSortThreads, 0, s>>>(ka, va, kb, vb, n, shift, off, nb);
         unsigned long long* tk = ka; ka = kb; kb = tk;
         unsigned int* tv = va; va = vb; vb = tv;
     }

@@ -2,6 +2,7 @@
 // resolveCollision (dcollid.cpp:317-362) and the C ABI of
 // include/collision_gb300.h.
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -13,6 +14,12 @@
 using namespace ccg;
 
 namespace {
+
+// Stages timed by cc_set_profiling / cc_get_profile.
+enum Stage { kStInit, kStBoxes, kStBvh, kStTraverse, kStNarrowProx, kStNarrowCcd, kStApply, kStZone,
+             kStFinalize, kStStrain, kNumStages };
+const char* kStageNames[kNumStages] = {"init", "leaf_boxes", "bvh_build", "traverse", "narrow_prox",
+                                       "narrow_ccd", "apply", "zone", "finalize", "strain"};
 
 template <class T>
 cudaError_t dalloc(T** p, size_t n) {
@@ -88,8 +95,9 @@ struct cc_solver {
     int* d_rank[2] = {nullptr, nullptr};
     RefTreeOrder tree[2];
     double volume = 0.0;
-    uint8_t* d_flag0 = nullptr;
-    uint8_t* d_dirty = nullptr;
+    int* d_level_off = nullptr;
+    int nlevels = 0;
+    void* d_strain_step = nullptr;
     int* d_strain_passes = nullptr;
     std::vector<Box6> h_boxes;
     std::vector<int> h_rank;
@@ -105,6 +113,41 @@ struct cc_solver {
     double lo[3] = {-1e30, -1e30, -1e30}, hi[3] = {1e30, 1e30, 1e30};
     long long counters[10] = {0};
     int pass_index = 0;
+    bool own_stream = true;
+    long long launches_last = 0;
+
+    // per-stage GPU time, measured with events on the solver's stream
+    bool profiling = false;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<int, int>> ev_marks;  // (stage, event index of its start; end = start+1)
+    double stage_ms[kNumStages] = {0};
+    long long stage_calls[kNumStages] = {0};
+    void prof(int stage, bool begin) {
+        if (!profiling) return;
+        size_t need = ev_marks.size() * 2 + 2;
+        while (ev_pool.size() < need) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            ev_pool.push_back(e);
+        }
+        if (begin) {
+            ev_marks.push_back({stage, (int)(ev_marks.size() * 2)});
+            cudaEventRecord(ev_pool[ev_marks.back().second], stream);
+        } else {
+            cudaEventRecord(ev_pool[ev_marks.back().second + 1], stream);
+        }
+    }
+    void prof_collect() {
+        if (!profiling) return;
+        for (auto& m : ev_marks) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, ev_pool[m.second], ev_pool[m.second + 1]) == cudaSuccess) {
+                stage_ms[m.first] += ms;
+                stage_calls[m.first]++;
+            }
+        }
+        ev_marks.clear();
+    }
     int zone_cap = 10000;
 
     ~cc_solver() { release(); }
@@ -125,7 +168,9 @@ struct cc_solver {
         if (zone.sort_temp) cudaFree(zone.sort_temp);
         zone.sort_temp = nullptr;
         dfree(d_rank[0]); dfree(d_rank[1]);
-        dfree(d_flag0); dfree(d_dirty); dfree(d_strain_passes); dfree(d_rec);
+        dfree(d_level_off); dfree(d_strain_passes); dfree(d_rec);
+        if (d_strain_step) cudaFree(d_strain_step);
+        d_strain_step = nullptr;
         pair_cap = contrib_cap = rec_cap = 0;
         nv = nt = nb = ne = nedges = 0;
         tree[0] = RefTreeOrder();
@@ -140,7 +185,9 @@ struct cc_solver {
         if (h_bbox) cudaFreeHost(h_bbox);
         h_ctr = nullptr;
         h_bbox = nullptr;
-        if (stream) cudaStreamDestroy(stream);
+        for (auto e : ev_pool) cudaEventDestroy(e);
+        ev_pool.clear();
+        if (stream && own_stream) cudaStreamDestroy(stream);
         stream = nullptr;
     }
 
@@ -177,6 +224,8 @@ struct cc_solver {
     cc_status assemble(const cc_mesh* m);
     cc_status resolve(const double* x_old, const double* x_cand, double* vel, uint8_t* hc, double* x_out,
                       int* has_collision);
+    cc_status resolve_impl(const double* x_old, const double* x_cand, double* vel, uint8_t* hc, double* x_out,
+                           int* has_collision);
     cc_status detect_pass(int moving, int zone_mode, bool* is_collision);
     cc_status update_tree(int which);
     Params params() const { return Params{prm.dt, prm.thickness, prm.eps, prm.k, prm.m, prm.lambda, prm.cr}; }
@@ -231,6 +280,26 @@ cc_status cc_solver::assemble(const cc_mesh* m) {
         }
     }
     nedges = (int)edges.size();
+    // dependency levels of the strain sweep: an edge waits for the last
+    // earlier edge at each of its points
+    std::vector<int> lvl((size_t)nedges), last((size_t)nv, 0);
+    nlevels = 0;
+    for (int i = 0; i < nedges; ++i) {
+        int l = 1 + std::max(last[edges[i].p0], last[edges[i].p1]);
+        lvl[i] = l;
+        last[edges[i].p0] = last[edges[i].p1] = l;
+        if (l > nlevels) nlevels = l;
+    }
+    std::vector<int> level_off((size_t)nlevels + 2, 0);
+    for (int i = 0; i < nedges; ++i) level_off[lvl[i]]++;  // counts at index level (1-based)
+    for (int l = 1; l <= nlevels + 1; ++l) level_off[l] += level_off[l - 1];
+    // level_off[l] now = edges with level <= l; shift to start offsets of level l+1 (0-based)
+    std::vector<StrainEdge> sorted((size_t)nedges);
+    {
+        std::vector<int> cur(level_off.begin(), level_off.end());
+        for (int i = 0; i < nedges; ++i) sorted[cur[lvl[i] - 1]++] = edges[i];
+    }
+    edges.swap(sorted);
 
     bool ok = true;
     ok &= dalloc(&d_ev, (size_t)ne * 3) == cudaSuccess;
@@ -270,8 +339,8 @@ cc_status cc_solver::assemble(const cc_mesh* m) {
     ok &= cudaMalloc(&zone.sort_temp, radix_sort_temp_bytes(nv > 0 ? nv : 1)) == cudaSuccess;
     ok &= dalloc(&d_rank[0], (size_t)ne) == cudaSuccess;
     ok &= dalloc(&d_rank[1], (size_t)ne) == cudaSuccess;
-    ok &= dalloc(&d_flag0, (size_t)nedges) == cudaSuccess;
-    ok &= dalloc(&d_dirty, (size_t)nv) == cudaSuccess;
+    ok &= dalloc(&d_level_off, (size_t)nlevels + 1) == cudaSuccess;
+    ok &= cudaMalloc(&d_strain_step, strain_step_bytes(nedges)) == cudaSuccess;
     ok &= dalloc(&d_strain_passes, 1) == cudaSuccess;
     if (!ok) return fail(CC_NO_MEMORY, "device allocation failed");
     cc_status st = grow_pairs(16 * ne + 4096);
@@ -283,8 +352,11 @@ cc_status cc_solver::assemble(const cc_mesh* m) {
     cudaMemcpyAsync(d_erigid, erigid.data(), erigid.size(), cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d_fixed, fixed.data(), fixed.size(), cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d_in_elem, in_elem.data(), in_elem.size(), cudaMemcpyHostToDevice, stream);
-    if (nedges)
+    if (nedges) {
         cudaMemcpyAsync(d_edges, edges.data(), sizeof(StrainEdge) * edges.size(), cudaMemcpyHostToDevice, stream);
+        cudaMemcpyAsync(d_level_off, level_off.data(), sizeof(int) * ((size_t)nlevels + 1), cudaMemcpyHostToDevice,
+                        stream);
+    }
     cudaMemsetAsync(d_av, 0, sizeof(double4_32a) * (size_t)(nv > 0 ? nv : 1), stream);
     h_boxes.resize((size_t)ne);
     h_rank.resize((size_t)ne);
@@ -325,23 +397,31 @@ cc_status cc_solver::detect_pass(int moving, int zone_mode, bool* is_collision) 
     pass_kinds.push_back(moving ? (zone_mode ? kPassZone : kPassCcd) : kPassProx);
     counters[0]++;
     if (moving) counters[zone_mode ? 2 : 1]++;
+    prof(kStBoxes, true);
     leaf_boxes(d_ev, ne, nt, d_xo, d_av, prm.dt, moving, d_box, bvh.bbox_enc, stream);
+    prof(kStBoxes, false);
     cc_status st = update_tree(moving);
     if (st) return st;
+    prof(kStBvh, true);
     bvh_build(d_box, bvh, stream);
-    counters[9] += 8;
+    prof(kStBvh, false);
     Params p = params();
     for (int attempt = 0; attempt < 8; ++attempt) {
-        k_reset_counters<<<1, 1, 0, stream>>>(d_ctr);
+        count_launch(), k_reset_counters<<<1, 1, 0, stream>>>(d_ctr);
+        prof(kStTraverse, true);
         bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream);
+        prof(kStTraverse, false);
         NarrowArgs a;
         a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
         a.rank = d_rank[moving]; a.nt = nt; a.pass = pass; a.zone = zone_mode; a.p = p; a.pairs = d_pairs;
         a.contrib = d_contrib; a.contrib_cap = contrib_cap; a.ctr = d_ctr; a.uf_parent = d_uf;
         a.rec = record ? d_rec : nullptr; a.rec_cap = rec_cap;
+        prof(moving ? kStNarrowCcd : kStNarrowProx, true);
         narrow_pass(a, moving, pair_cap, stream);
+        prof(moving ? kStNarrowCcd : kStNarrowProx, false);
+        prof(kStApply, true);
         apply_contribs(d_contrib, d_ctr, contrib_cap, nv, d_av, d_hc, apply, stream);
-        counters[9] += 8;
+        prof(kStApply, false);
         cudaMemcpyAsync(h_ctr, d_ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, stream);
         if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("detection pass");
         int e = h_ctr->err;
@@ -376,8 +456,9 @@ cc_status cc_solver::detect_pass(int moving, int zone_mode, bool* is_collision) 
                         cudaMemcpyDeviceToHost, stream);
     }
     if (zone_mode) {
+        prof(kStZone, true);
         zone_velocity(d_uf, d_in_elem, d_fixed, d_xo, d_av, nv, p, zone, d_ctr, stream);
-        counters[9] += 5;
+        prof(kStZone, false);
         cudaMemcpyAsync(h_ctr, d_ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, stream);
     }
     if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("pass tail");
@@ -388,6 +469,14 @@ cc_status cc_solver::detect_pass(int moving, int zone_mode, bool* is_collision) 
 
 cc_status cc_solver::resolve(const double* x_old, const double* x_cand, double* vel, uint8_t* hc, double* x_out,
                              int* has_collision) {
+    long long l0 = g_kernel_launches;
+    cc_status st0 = resolve_impl(x_old, x_cand, vel, hc, x_out, has_collision);
+    launches_last = g_kernel_launches - l0;
+    return st0;
+}
+
+cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, double* vel, uint8_t* hc,
+                                  double* x_out, int* has_collision) {
     std::memset(counters, 0, sizeof(counters));
     pass_index = 0;
     visits.clear();
@@ -401,11 +490,13 @@ cc_status cc_solver::resolve(const double* x_old, const double* x_cand, double* 
     }
     // d_hc doubles as the device copy of has_collsn
     if (hc != d_hc) cudaMemcpyAsync(d_hc, hc, (size_t)nv, cudaMemcpyDeviceToDevice, stream);
-    k_reset_counters<<<1, 1, 0, stream>>>(d_ctr);
+    count_launch(), k_reset_counters<<<1, 1, 0, stream>>>(d_ctr);
     cudaMemsetAsync(&d_ctr->err, 0, sizeof(int), stream);
+    ev_marks.clear();
+    prof(kStInit, true);
     step_init(x_old, x_cand, nv, d_in_elem, prm.dt, d_xo, d_av, d_ctr, stream);
     uf_init(d_uf, nv, stream);
-    counters[9] += 4;
+    prof(kStInit, false);
     bool is_coll = false;
     cc_status st = detect_pass(0, 0, &is_coll);
     if (st) return st;
@@ -427,15 +518,19 @@ cc_status cc_solver::resolve(const double* x_old, const double* x_cand, double* 
         }
     }
     Params p = params();
+    prof(kStFinalize, true);
     finalize_positions(d_in_elem, d_xo, d_av, d_hc, x_cand, x_out, nv, p, lo, hi, stream);
-    strain_limit(d_edges, nedges, d_xo, d_av, d_flag0, d_dirty, nv, prm.dt, d_strain_passes, stream);
+    prof(kStFinalize, false);
+    prof(kStStrain, true);
+    strain_limit(d_edges, nedges, d_level_off, nlevels, d_xo, d_av, prm.dt, d_strain_step, d_strain_passes, stream);
+    prof(kStStrain, false);
     final_velocity(d_in_elem, d_hc, d_av, vel, nv, stream);
     if (hc != d_hc) cudaMemcpyAsync(hc, d_hc, (size_t)nv, cudaMemcpyDeviceToDevice, stream);
-    counters[9] += 3;
     int sp = 0;
     cudaMemcpyAsync(&sp, d_strain_passes, sizeof(int), cudaMemcpyDeviceToHost, stream);
     if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("finalize");
     counters[7] = nedges ? sp : 1;
+    prof_collect();
     if (has_collision) *has_collision = hcol;
     return cuda_check("resolve");
 }
@@ -516,6 +611,7 @@ cc_status cc_resolve_device(cc_solver* s, const double* x_old, const double* x_c
 
 int cc_get_counters(cc_solver* s, long long* out, int n) {
     if (!s || !out) return 0;
+    s->counters[9] = s->launches_last;
     int m = n < 10 ? n : 10;
     for (int i = 0; i < m; ++i) out[i] = s->counters[i];
     return m;
@@ -578,7 +674,7 @@ int cc_debug_candidate_pairs(cc_solver* s, int moving, int brute_force, int* out
     leaf_boxes(s->d_ev, s->ne, s->nt, s->d_xo, s->d_av, s->prm.dt, moving, s->d_box, s->bvh.bbox_enc, s->stream);
     if (!brute_force) bvh_build(s->d_box, s->bvh, s->stream);
     for (int attempt = 0; attempt < 8; ++attempt) {
-        k_reset_counters<<<1, 1, 0, s->stream>>>(s->d_ctr);
+        count_launch(), k_reset_counters<<<1, 1, 0, s->stream>>>(s->d_ctr);
         cudaMemsetAsync(&s->d_ctr->err, 0, sizeof(int), s->stream);
         if (brute_force)
             brute_pairs(s->d_box, s->ne, s->d_pairs, s->pair_cap, s->d_ctr, s->stream);
@@ -601,6 +697,42 @@ int cc_debug_candidate_pairs(cc_solver* s, int moving, int brute_force, int* out
     }
     return n;
 }
+
+cc_status cc_set_stream(cc_solver* s, void* stream) {
+    if (!s) return CC_BAD_INPUT;
+    cudaSetDevice(s->device);
+    cudaStreamSynchronize(s->stream);
+    if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
+    if (stream) {
+        s->stream = (cudaStream_t)stream;
+        s->own_stream = false;
+    } else {
+        if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) return CC_CUDA_ERROR;
+        s->own_stream = true;
+    }
+    return CC_OK;
+}
+
+cc_status cc_set_profiling(cc_solver* s, int on) {
+    if (!s) return CC_BAD_INPUT;
+    s->profiling = on != 0;
+    for (int i = 0; i < kNumStages; ++i) {
+        s->stage_ms[i] = 0.0;
+        s->stage_calls[i] = 0;
+    }
+    return CC_OK;
+}
+
+int cc_get_profile(cc_solver* s, double* ms, long long* calls, int cap) {
+    if (!s) return -1;
+    for (int i = 0; i < kNumStages && i < cap; ++i) {
+        if (ms) ms[i] = s->stage_ms[i];
+        if (calls) calls[i] = s->stage_calls[i];
+    }
+    return kNumStages;
+}
+
+const char* cc_profile_stage_name(int i) { return (i >= 0 && i < kNumStages) ? kStageNames[i] : ""; }
 
 int cc_last_error(cc_solver* s, char* buf, int len) {
     if (!s || !buf || len <= 0) return 0;

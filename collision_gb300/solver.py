@@ -137,6 +137,19 @@ class CollisionSolver3d:
                                                 has_collsn.data_ptr(), x_out.data_ptr(), C.byref(hcol)))
         self._has_collision = bool(hcol.value)
 
+    def setStream(self, stream_handle: int | None):
+        """Run on a caller's CUDA stream (e.g. torch.cuda.current_stream().cuda_stream)."""
+        self._check(self._lib.cc_set_stream(self._h, stream_handle))
+
+    def setProfiling(self, on: bool):
+        self._check(self._lib.cc_set_profiling(self._h, int(bool(on))))
+
+    def profile(self) -> dict:
+        ms = (C.c_double * 32)()
+        calls = (C.c_longlong * 32)()
+        n = self._lib.cc_get_profile(self._h, ms, calls, 32)
+        return {self._lib.cc_profile_stage_name(i).decode(): (ms[i], calls[i]) for i in range(n)}
+
     def hasCollision(self) -> bool:
         return self._has_collision
 

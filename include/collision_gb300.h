@@ -139,6 +139,18 @@ cc_status cc_get_leaf_ranks(cc_solver* s, int which, int* out);
  * cross-checks. Writes up to cap (a,b) pairs, returns the count or -1. */
 int cc_debug_candidate_pairs(cc_solver* s, int moving, int brute_force, int* out, int cap);
 
+/* Run the solver on a caller's CUDA stream (cudaStream_t; NULL = a stream
+ * of its own). Work is ordered after everything already queued there. */
+cc_status cc_set_stream(cc_solver* s, void* stream);
+
+/* Per-stage GPU time of the following steps, measured with CUDA events on
+ * the solver's stream: cc_get_profile writes accumulated milliseconds and
+ * call counts per stage (names from cc_profile_stage_name) and returns the
+ * number of stages. */
+cc_status cc_set_profiling(cc_solver* s, int on);
+int cc_get_profile(cc_solver* s, double* ms, long long* calls, int cap);
+const char* cc_profile_stage_name(int i);
+
 /* Last error message of this solver (NUL-terminated, truncated to len). */
 int cc_last_error(cc_solver* s, char* buf, int len);
 
