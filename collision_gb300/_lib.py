@@ -88,6 +88,8 @@ def load(path: str = LIB_PATH):
     lib.cc_get_profile.argtypes = [vp, C.POINTER(C.c_double), lp, C.c_int]
     lib.cc_profile_stage_name.restype = C.c_char_p
     lib.cc_profile_stage_name.argtypes = [C.c_int]
+    lib.cc_selftest_math.restype = C.c_int
+    lib.cc_selftest_math.argtypes = [C.c_int, C.c_int, dp, dp, dp, C.c_int]
     lib.cc_last_error.restype = C.c_int
     lib.cc_last_error.argtypes = [vp, C.c_char_p, C.c_int]
     _LIB = lib

@@ -120,6 +120,8 @@ struct StrainEdge {
 size_t strain_step_bytes(int nedges);
 void strain_limit(const StrainEdge* edges, int nedges, const int* level_off, int nlevels, const double4_32a* xo,
                   double4_32a* av, double dt, void* step_buf, int* passes_out, cudaStream_t s);
+// Correctly rounded cos/sin/acos/pow (fn 0..3) on device arrays, for self-tests.
+void math_selftest(int fn, const double* a, const double* b, double* out, int n, cudaStream_t s);
 // updateFinalVelocity.
 void final_velocity(const uint8_t* in_elem, const uint8_t* has_collsn, const double4_32a* av, double* vel, int nv,
                     cudaStream_t s);

@@ -8,6 +8,7 @@
 #pragma once
 
 #include "cc_common.cuh"
+#include "cc_crmath.cuh"
 
 namespace ccg {
 
@@ -348,18 +349,51 @@ static __device__ bool is_coplanar(const double (*xo4)[3], const double (*av4)[3
         double R = (2 * a * a * a - 9 * a * b + 27 * c) / 54;
         double Q3 = Q * Q * Q;
         double R2 = R * R;
+        // The roots are first formed with the fast library functions. Their
+        // results are within 2 ulp of the correctly rounded ones, which moves
+        // a root by far less than `margin`; only when a root (or a branch
+        // threshold) falls within the margin of a decision are they formed
+        // again with the correctly rounded functions the reference's libm
+        // gives. Roots away from [0, dt] are discarded either way.
         if (R2 < Q3) {
             double Qsqrt = sqrt(Q);
-            double theta = acos(R / sqrt(Q3));
-            roots[0] = -2 * Qsqrt * cos(theta / 3) - a / 3;
-            roots[1] = -2 * Qsqrt * cos((theta + 2 * kPi) / 3) - a / 3;
-            roots[2] = -2 * Qsqrt * cos((theta - 2 * kPi) / 3) - a / 3;
+            double z = R / sqrt(Q3);
+            double theta = acos(z);
+            double f0 = -2 * Qsqrt * cos(theta / 3) - a / 3;
+            double f1 = -2 * Qsqrt * cos((theta + 2 * kPi) / 3) - a / 3;
+            double f2 = -2 * Qsqrt * cos((theta - 2 * kPi) / 3) - a / 3;
+            double margin = 1e-12 * (2 * fabs(Qsqrt) + fabs(a) + dt);
+            double lo = -margin, hi = dt + kMachEps + margin;
+            bool near_ = (f0 > lo && f0 < hi) || (f1 > lo && f1 < hi) || (f2 > lo && f2 < hi);
+            if (near_) {
+                theta = cr::acos(z);
+                f0 = -2 * Qsqrt * cr::cos(theta / 3) - a / 3;
+                f1 = -2 * Qsqrt * cr::cos((theta + 2 * kPi) / 3) - a / 3;
+                f2 = -2 * Qsqrt * cr::cos((theta - 2 * kPi) / 3) - a / 3;
+            }
+            roots[0] = f0;
+            roots[1] = f1;
+            roots[2] = f2;
         } else {
             double sgn = (R > 0) ? 1.0 : -1.0;
-            double A = -sgn * pow(fabs(R) + sqrt(R2 - Q3), 1.0 / 3.0);
+            double base = fabs(R) + sqrt(R2 - Q3);
+            double A = -sgn * pow(base, 1.0 / 3.0);
             double B = (fabs(A) < kRoundEps) ? 0.0 : Q / A;
-            roots[0] = (A + B) - a / 3.0;
-            if (fabs(A - B) < kRoundEps) roots[1] = roots[2] = -0.5 * (A + B) - a / 3.0;
+            double f0 = (A + B) - a / 3.0;
+            double f1 = -0.5 * (A + B) - a / 3.0;
+            double margin = 1e-12 * (fabs(A) + fabs(B) + fabs(a) + dt);
+            double lo = -margin, hi = dt + kMachEps + margin;
+            bool near_ = (f0 > lo && f0 < hi) || (f1 > lo && f1 < hi) ||
+                         fabs(fabs(A) - kRoundEps) <= 1e-12 * fabs(A) ||
+                         fabs(fabs(A - B) - kRoundEps) <= 1e-12 * (fabs(A) + fabs(B));
+            if (near_) {
+                A = -sgn * cr::pow(base, 1.0 / 3.0);
+                B = (fabs(A) < kRoundEps) ? 0.0 : Q / A;
+                f0 = (A + B) - a / 3.0;
+                f1 = -0.5 * (A + B) - a / 3.0;
+            }
+            roots[0] = f0;
+            if (fabs(A - B) < kRoundEps) roots[1] = roots[2] = f1;
         }
     } else {
         a = b; b = c; c = d;

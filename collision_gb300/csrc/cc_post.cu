@@ -119,7 +119,8 @@ __device__ __forceinline__ double det3(const double (*a)[3]) {
 }
 
 // updateImpactListVelocity, dcollid3d.cpp:70-200, one thread per zone over
-// its members in point order.
+// its members in point order; sin and cos correctly rounded, as the
+// reference's libm gives them.
 __global__ void k_zone_solve(const unsigned long long* __restrict__ keys, const unsigned int* __restrict__ vals,
                              const int* nmembers_p, const uint8_t* __restrict__ fixed,
                              const double4_32a* __restrict__ xo, double4_32a* av, Params prm, PassCounters* ctr) {
@@ -190,11 +191,11 @@ __global__ void k_zone_solve(const unsigned long long* __restrict__ keys, const 
             double sc = dot3(dx, w) / dot3(w, w);
             for (int d = 0; d < 3; ++d) xF[d] = sc * w[d];
             for (int d = 0; d < 3; ++d) xR[d] = dx[d] - xF[d];
-            double sw = sin(dt * mag_w) / mag_w;
+            double sw = cr::sin(dt * mag_w) / mag_w;
             for (int d = 0; d < 3; ++d) tmpV[d] = sw * w[d];
             cross3(tmpV, xR, wxR);
         }
-        double cw = cos(dt * mag_w);
+        double cw = cr::cos(dt * mag_w);
         for (int d = 0; d < 3; ++d) {
             x_new[d] = x_cm[d] + dt * v_cm[d] + xF[d] + cw * xR[d] + wxR[d];
             nv_[d] = (x_new[d] - xs[d]) / dt;
@@ -397,7 +398,24 @@ __global__ void k_final_velocity(const uint8_t* __restrict__ in_elem, const uint
     vel[3 * p + 2] = a.z;
 }
 
+__global__ void k_math_selftest(int fn, const double* a, const double* b, double* out, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double r;
+    switch (fn) {
+        case 0: r = cr::cos(a[i]); break;
+        case 1: r = cr::sin(a[i]); break;
+        case 2: r = cr::acos(a[i]); break;
+        default: r = cr::pow(a[i], b[i]); break;
+    }
+    out[i] = r;
+}
+
 }  // namespace
+
+void math_selftest(int fn, const double* a, const double* b, double* out, int n, cudaStream_t s) {
+    if (n > 0) count_launch(), k_math_selftest<<<nblk(n, 128), 128, 0, s>>>(fn, a, b, out, n);
+}
 
 void step_init(const double* x_old, const double* x_cand, int nv, const uint8_t* in_elem, double dt, double4_32a* xo,
                double4_32a* av, PassCounters* ctr, cudaStream_t s) {

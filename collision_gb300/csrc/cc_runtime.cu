@@ -734,6 +734,24 @@ int cc_get_profile(cc_solver* s, double* ms, long long* calls, int cap) {
 
 const char* cc_profile_stage_name(int i) { return (i >= 0 && i < kNumStages) ? kStageNames[i] : ""; }
 
+int cc_selftest_math(int device, int fn, const double* a, const double* b, double* out, int n) {
+    if (n <= 0) return 0;
+    if (cudaSetDevice(device) != cudaSuccess) return -1;
+    double *da = nullptr, *db = nullptr, *dout = nullptr;
+    size_t bytes = sizeof(double) * (size_t)n;
+    if (cudaMalloc(&da, bytes) != cudaSuccess || cudaMalloc(&db, bytes) != cudaSuccess ||
+        cudaMalloc(&dout, bytes) != cudaSuccess) {
+        cudaFree(da); cudaFree(db); cudaFree(dout);
+        return -1;
+    }
+    cudaMemcpy(da, a, bytes, cudaMemcpyHostToDevice);
+    cudaMemcpy(db, b ? b : a, bytes, cudaMemcpyHostToDevice);
+    math_selftest(fn, da, db, dout, n, 0);
+    cudaError_t e = cudaMemcpy(out, dout, bytes, cudaMemcpyDeviceToHost);
+    cudaFree(da); cudaFree(db); cudaFree(dout);
+    return e == cudaSuccess ? n : -1;
+}
+
 int cc_last_error(cc_solver* s, char* buf, int len) {
     if (!s || !buf || len <= 0) return 0;
     std::snprintf(buf, (size_t)len, "%s", s->err.c_str());

@@ -151,6 +151,12 @@ cc_status cc_set_profiling(cc_solver* s, int on);
 int cc_get_profile(cc_solver* s, double* ms, long long* calls, int cap);
 const char* cc_profile_stage_name(int i);
 
+/* Self-test of the correctly rounded math the FP64 path uses on the GPU:
+ * fn 0 cos(a), 1 sin(a), 2 acos(a), 3 pow(a, b), for n host values; returns
+ * n or -1. These functions reproduce the reference's libm (glibc) wherever
+ * its result is correctly rounded. */
+int cc_selftest_math(int device, int fn, const double* a, const double* b, double* out, int n);
+
 /* Last error message of this solver (NUL-terminated, truncated to len). */
 int cc_last_error(cc_solver* s, char* buf, int len);
 
