@@ -90,6 +90,10 @@ def load(path: str = LIB_PATH):
     lib.cc_profile_stage_name.argtypes = [C.c_int]
     lib.cc_selftest_math.restype = C.c_int
     lib.cc_selftest_math.argtypes = [C.c_int, C.c_int, dp, dp, dp, C.c_int]
+    lib.cc_candidate_pairs_static.restype = C.c_int
+    lib.cc_candidate_pairs_static.argtypes = [C.c_int, dp, C.c_int, vp, C.c_int, ip, vp]
+    lib.cc_static_last_error.restype = C.c_int
+    lib.cc_static_last_error.argtypes = [C.c_char_p, C.c_int]
     lib.cc_last_error.restype = C.c_int
     lib.cc_last_error.argtypes = [vp, C.c_char_p, C.c_int]
     _LIB = lib

@@ -81,6 +81,30 @@ __global__ void k_leaf_boxes(const int* __restrict__ ev, int ne, int nt, const d
     }
 }
 
+// Union of n given boxes into bb (encoded as for k_leaf_boxes).
+__global__ void k_boxes_bbox(const Box6* __restrict__ box, int n, unsigned long long* bb) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    double lo[3] = {kBig, kBig, kBig}, hi[3] = {-kBig, -kBig, -kBig};
+    if (e < n) {
+        Box6 b = box[e];
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = b.lo[d];
+            hi[d] = b.hi[d];
+        }
+    }
+    for (int d = 0; d < 3; ++d) {
+        double l = lo[d], h = hi[d];
+        for (int o = 16; o > 0; o >>= 1) {
+            l = fmin(l, __shfl_xor_sync(0xffffffffu, l, o));
+            h = fmax(h, __shfl_xor_sync(0xffffffffu, h, o));
+        }
+        if ((threadIdx.x & 31) == 0 && l <= h) {
+            atomicMin(&bb[d], enc_double(l));
+            atomicMax(&bb[3 + d], enc_double(h));
+        }
+    }
+}
+
 __device__ __forceinline__ unsigned int expand_bits10(unsigned int v) {
     v = (v * 0x00010001u) & 0xFF0000FFu;
     v = (v * 0x00000101u) & 0x0F00F00Fu;
@@ -244,6 +268,11 @@ void leaf_boxes(const int* ev, int ne, int nt, const double4_32a* xo, const doub
         count_launch(), k_leaf_boxes<1><<<nblk(ne, 256), 256, 0, s>>>(ev, ne, nt, xo, av, dt, box, bbox_enc);
     else
         count_launch(), k_leaf_boxes<0><<<nblk(ne, 256), 256, 0, s>>>(ev, ne, nt, xo, av, dt, box, bbox_enc);
+}
+
+void boxes_bbox(const Box6* box, int n, unsigned long long* bbox_enc, cudaStream_t s) {
+    count_launch(), k_bbox_init<<<1, 32, 0, s>>>(bbox_enc);
+    if (n > 0) count_launch(), k_boxes_bbox<<<nblk(n, 256), 256, 0, s>>>(box, n, bbox_enc);
 }
 
 void bvh_build(const Box6* box, BvhBufs& b, cudaStream_t s) {

@@ -47,6 +47,8 @@ struct BvhBufs {
 // x_old + dt*avgVel), padded by 1e-6, plus their union in bbox_enc.
 void leaf_boxes(const int* ev, int ne, int nt, const double4_32a* xo, const double4_32a* av, double dt, int moving,
                 Box6* box, unsigned long long* bbox_enc, cudaStream_t s);
+// Union of n given boxes in bbox_enc (the scene box the Morton keys use).
+void boxes_bbox(const Box6* box, int n, unsigned long long* bbox_enc, cudaStream_t s);
 // Morton keys, sort, Karras hierarchy, refit.
 void bvh_build(const Box6* box, BvhBufs& b, cudaStream_t s);
 // All leaf pairs with overlapping boxes, each unordered pair once.

@@ -1,0 +1,139 @@
+// Candidate-pair search that allocates no device memory.
+//
+// Some callers cannot call cudaMalloc: an application whose device memory is
+// entirely owned by another allocator (an engine that reserves the GPU at
+// start-up, a framework's caching pool), or a real-time loop that must not
+// stall - cudaMalloc and cudaFree can synchronise the whole device and can
+// fail once memory is fragmented. For them, cc_candidate_pairs_static runs
+// the broad phase of the solver (Morton keys, radix sort, LBVH build and
+// refit, traversal) on boxes and output buffers the caller owns, with every
+// intermediate array carved out of one fixed scratch area compiled into the
+// library.
+//
+// That scratch area is a file-scope __device__ array of kScratchBytes (8 MiB);
+// every GPU that loads this library holds it until the process exits. It fits
+// at most kMaxStaticElems (65,536) boxes. All calls on a device share it and
+// it keeps the last call's contents, so each call clears what must start at
+// zero (the pair counter and the refit arrival flags) and calls that overlap
+// on the GPU - from two host threads, or on two streams - race on it. Host
+// code only sees a stand-in for the array's name: its device address comes
+// from cudaGetSymbolAddress, taken once per device, with that device current,
+// on the first call there (that first call should come before any stream
+// capture begins).
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "../../include/collision_gb300.h"
+#include "cc_launch.h"
+
+namespace ccg {
+
+namespace {
+
+constexpr size_t kScratchBytes = (size_t)8 << 20;
+constexpr int kMaxStaticElems = 65536;
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_pair_scratch[kScratchBytes];
+
+std::mutex g_mu;
+void* g_scratch_ptr[kMaxDevices] = {};
+thread_local char g_static_err[256] = {0};
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Device address of the scratch array on `device`, looked up once.
+cudaError_t scratch_address(int device, void** out) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_scratch_ptr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_pair_scratch);
+        if (e != cudaSuccess) return e;
+        g_scratch_ptr[device] = p;
+    }
+    *out = g_scratch_ptr[device];
+    return cudaSuccess;
+}
+
+__global__ void k_clear_counters(PassCounters* c) {
+    c->npairs = 0; c->ncontrib = 0; c->nhit_pairs = 0; c->nrec = 0;
+    c->nvisits = 0; c->ncontacts = 0; c->err = 0; c->pad = 0;
+}
+
+cc_status static_fail(cc_status st, const char* msg) {
+    std::snprintf(g_static_err, sizeof(g_static_err), "%s", msg);
+    return st;
+}
+
+}  // namespace
+
+}  // namespace ccg
+
+using namespace ccg;
+
+extern "C" {
+
+cc_status cc_candidate_pairs_static(int device, const double* boxes, int n, int* pairs, int cap, int* npairs,
+                                    void* stream) {
+    if (npairs) *npairs = 0;
+    if (n > kMaxStaticElems)
+        return static_fail(CC_BAD_INPUT, "more boxes than the static scratch area holds (65536)");
+    if (n < 0 || cap < 0 || !npairs || (n > 0 && !boxes) || (cap > 0 && !pairs))
+        return static_fail(CC_BAD_INPUT, "bad arguments");
+    if (((uintptr_t)boxes & 15) != 0 || ((uintptr_t)pairs & 7) != 0)
+        return static_fail(CC_BAD_INPUT, "boxes must be 16-byte and pairs 8-byte aligned");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev || device >= kMaxDevices)
+        return static_fail(CC_CUDA_ERROR, "no such device");
+    if (cudaSetDevice(device) != cudaSuccess) return static_fail(CC_CUDA_ERROR, "cudaSetDevice failed");
+    if (n <= 1) return CC_OK;
+    void* base = nullptr;
+    if (scratch_address(device, &base) != cudaSuccess)
+        return static_fail(CC_CUDA_ERROR, "cudaGetSymbolAddress failed");
+
+    // carve the scratch area
+    char* p = (char*)base;
+    size_t used = 0;
+    auto take = [&](size_t bytes) {
+        char* q = p + used;
+        used += align256(bytes);
+        return (void*)q;
+    };
+    BvhBufs b{};
+    b.n = n;
+    b.keys = (unsigned long long*)take(sizeof(unsigned long long) * (size_t)n);
+    b.order = (unsigned int*)take(sizeof(unsigned int) * (size_t)n);
+    b.child = (int*)take(sizeof(int) * 2 * (size_t)n);
+    b.range_hi = (int*)take(sizeof(int) * (size_t)n);
+    b.parent = (int*)take(sizeof(int) * 2 * (size_t)n);
+    b.flags = (int*)take(sizeof(int) * (size_t)n);
+    b.node_box = (Box6*)take(sizeof(Box6) * (size_t)n);
+    b.bbox_enc = (unsigned long long*)take(6 * sizeof(unsigned long long));
+    PassCounters* ctr = (PassCounters*)take(sizeof(PassCounters));
+    b.sort_temp = take(radix_sort_temp_bytes(n));
+    if (used > kScratchBytes) return static_fail(CC_NO_MEMORY, "static scratch layout exceeds its size");
+
+    cudaStream_t s = (cudaStream_t)stream;
+    const Box6* box = (const Box6*)boxes;
+    count_launch(), k_clear_counters<<<1, 1, 0, s>>>(ctr);
+    boxes_bbox(box, n, b.bbox_enc, s);
+    bvh_build(box, b, s);  // clears the refit arrival flags itself
+    bvh_pairs(box, b, (int2*)pairs, cap, ctr, s);
+    PassCounters h{};
+    if (cudaMemcpyAsync(&h, ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return static_fail(CC_CUDA_ERROR, cudaGetErrorString(cudaGetLastError()));
+    *npairs = h.npairs;
+    if (h.err & kErrStack) return static_fail(CC_STACK_OVERFLOW, "BVH traversal stack overflow");
+    if (h.npairs > cap) return static_fail(CC_PAIR_OVERFLOW, "more pairs than cap; *npairs holds the count");
+    return CC_OK;
+}
+
+int cc_static_last_error(char* buf, int len) {
+    if (!buf || len <= 0) return 0;
+    std::snprintf(buf, (size_t)len, "%s", g_static_err);
+    return (int)std::strlen(g_static_err);
+}
+
+}  // extern "C"

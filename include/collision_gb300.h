@@ -157,6 +157,30 @@ const char* cc_profile_stage_name(int i);
  * its result is correctly rounded. */
 int cc_selftest_math(int device, int fn, const double* a, const double* b, double* out, int n);
 
+/*
+ * Candidate pairs without allocating: no counterpart in the reference.
+ *
+ * The broad phase of cc_resolve (all pairs of n boxes that overlap, each
+ * unordered pair once) for callers that cannot call cudaMalloc - code whose
+ * device memory belongs to another allocator (an engine that reserves the
+ * GPU at start-up, a framework's caching pool) or a loop that must not
+ * stall, since cudaMalloc/cudaFree can synchronise the device and fail under
+ * fragmentation. Nothing is allocated: the caller owns the inputs and outputs,
+ * and every intermediate array lives in an 8 MiB scratch area compiled into
+ * the library (held on every GPU that loads it until exit). Limit: n <= 65536.
+ *   boxes   device, n x 6 doubles (lo x,y,z, hi x,y,z), 16-byte aligned
+ *   pairs   device, cap x 2 ints (element indices), 8-byte aligned
+ *   npairs  host: the number of overlapping pairs (may exceed cap, then only
+ *           cap are written and CC_PAIR_OVERFLOW is returned)
+ *   stream  cudaStream_t or NULL; the call waits for its work to finish.
+ * The first call on a device looks up the scratch area's address there; make
+ * it before any stream capture starts. Calls share the scratch area: calls
+ * that overlap on the GPU race. Errors: cc_static_last_error.
+ */
+cc_status cc_candidate_pairs_static(int device, const double* boxes, int n, int* pairs, int cap, int* npairs,
+                                    void* stream);
+int cc_static_last_error(char* buf, int len);
+
 /* Last error message of this solver (NUL-terminated, truncated to len). */
 int cc_last_error(cc_solver* s, char* buf, int len);
 
