@@ -171,58 +171,66 @@ def run_gpu(args):
     stream = torch.cuda.Stream(device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
-    # ---------------------------------------------- device-resident run
-    s = CollisionSolver3d(dev)
-    s.assembleFromScene(sc)
-    s.setStream(stream.cuda_stream)
-    with torch.cuda.stream(stream):
-        x = torch.tensor(sc.x, dtype=torch.float64, device=dev)
-        v = torch.tensor(sc.v, dtype=torch.float64, device=dev)
-        hc = torch.zeros(sc.nv, dtype=torch.uint8, device=dev)
-        xc = torch.empty_like(x)
-        xo = torch.empty_like(x)
-    launches = []
-    step_ms = []
-    counters = []
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(args.steps)]
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            torch.add(x, v, alpha=dt, out=xc)
-            s.resolveCollisionDevice(x, xc, v, hc, xo)
-            x, xo = xo, x
-    stream.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    s.setProfiling(True)
-    with Clocks(dev) as clk, torch.cuda.stream(stream):
-        for k in range(args.steps):
-            flush.fill_(float(k))
-            evs[k][0].record(stream)
-            torch.add(x, v, alpha=dt, out=xc)
-            s.resolveCollisionDevice(x, xc, v, hc, xo)
-            evs[k][1].record(stream)
-            c = s.counters()
-            counters.append(c)
-            launches.append(c["kernel_launches"] + 1)  # + the candidate update
-            x, xo = xo, x
+    # ---------------------------------------------- device-resident runs
+    def device_run(mode):
+        """W untimed + K timed steps from the scene's start, each step
+        through cc_resolve_device; returns total timed ms and the counters."""
+        s = CollisionSolver3d(dev)
+        s.assembleFromScene(sc)
+        s.setMode(mode)
+        s.setStream(stream.cuda_stream)
+        with torch.cuda.stream(stream):
+            x = torch.tensor(sc.x, dtype=torch.float64, device=dev)
+            v = torch.tensor(sc.v, dtype=torch.float64, device=dev)
+            hc = torch.zeros(sc.nv, dtype=torch.uint8, device=dev)
+            xc = torch.empty_like(x)
+            xo = torch.empty_like(x)
+        launches, counters = [], []
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                torch.add(x, v, alpha=dt, out=xc)
+                s.resolveCollisionDevice(x, xc, v, hc, xo)
+                x, xo = xo, x
         stream.synchronize()
-    torch.cuda.synchronize()
-    for a, b in evs:
-        step_ms.append(a.elapsed_time(b))
-    prof = s.profile()
-    total_ms = float(sum(step_ms))
-    if ws > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-        torch.distributed.barrier()
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        s.setProfiling(True)
+        with Clocks(dev) as clk, torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.fill_(float(k))
+                evs[k][0].record(stream)
+                torch.add(x, v, alpha=dt, out=xc)
+                s.resolveCollisionDevice(x, xc, v, hc, xo)
+                evs[k][1].record(stream)
+                c = s.counters()
+                counters.append(c)
+                launches.append(c["kernel_launches"] + 1)  # + the candidate update
+                x, xo = xo, x
+            stream.synchronize()
+        torch.cuda.synchronize()
+        step_ms = [a.elapsed_time(b) for a, b in evs]
+        prof = s.profile()
+        s.close()
+        total_ms = float(sum(step_ms))
+        if ws > 1:
+            t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            total_ms = float(t.item())
+            torch.distributed.barrier()
+        return total_ms, step_ms, counters, launches, prof, clk.summary()
+
+    plain_ms, plain_steps, plain_ctr, _, plain_prof, _ = device_run(0)
+    total_ms, step_ms, counters, launches, prof, clocks = device_run(1)
     value = ws * args.steps / (total_ms / 1e3)
+    plain_value = ws * args.steps / (plain_ms / 1e3)
 
     # ------------------------------------------------------ end-to-end run
     s2 = CollisionSolver3d(dev)
     s2.assembleFromScene(sc)
+    s2.setMode(1)
     s2.setStream(stream.cuda_stream)
     pin = lambda a, dtp: torch.tensor(a, dtype=dtp).pin_memory()
     hx = pin(sc.x, torch.float64)
@@ -273,26 +281,26 @@ def run_gpu(args):
     peak_src = "measured" if hbm else "fallback"
     hbm = hbm or 6800.0
     tot = {k: sum(c[k] for c in counters) for k in counters[0]} if counters else {}
+    ptot = {k: sum(c[k] for c in plain_ctr) for k in plain_ctr[0]} if plain_ctr else {}
     # dominant kernel: the CCD narrow phase. Algorithmic bytes per visited
     # pair: the pair (8 B), both leaf ranks (8 B), both elements' point ids
     # (24 B) and the x_old + avgVel records of its up to 6 points (6 x 64 B);
     # plus 64 B per contribution written.
-    narrow_ms, narrow_calls = prof.get("narrow_ccd", (0.0, 0))
-    ccd_visits = tot.get("visits", 0)  # all passes; CCD share estimated below
+    narrow_ms, narrow_calls = plain_prof.get("narrow_ccd", (0.0, 0))
+    ccd_visits = ptot.get("visits", 0)  # all passes; CCD share estimated below
     bytes_per_visit = 8 + 8 + 24 + 6 * 64
     roof = None
     if narrow_calls:
         # visits of CCD passes: total visits minus proximity visits (one
         # proximity pass per step visits about as many pairs as one CCD pass)
-        passes = max(tot.get("passes", 1), 1)
+        passes = max(ptot.get("passes", 1), 1)
         ccd_share = (passes - args.steps) / passes
         algo = bytes_per_visit * ccd_visits * ccd_share / narrow_calls
         avg_s = narrow_ms / narrow_calls / 1e3
         achieved = algo / avg_s / 1e9
-        roof = {"bound": "hbm", "kernel": "k_narrow<true> (CCD narrow phase)", "achieved": achieved,
+        roof = {"bound": "hbm", "kernel": "k_narrow<true> (CCD narrow phase, plain FP64)", "achieved": achieved,
                 "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_src,
                 "traffic": None, "note": "FP64-ALU bound: FP64 is ~1.25 TFLOP/s nominal on GB300"}
-    clocks = clk.summary()
     cpu = None
     if not args.no_cpu_baseline:
         rate, n, t = cpu_oracle_rate(seed, args.cpu_budget, args.warmup + args.steps)
@@ -300,13 +308,18 @@ def run_gpu(args):
                "sample": f"{WORKLOAD} 129x129, first {n} steps of the trajectory ({t:.1f} s)"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64 (f32 filters)", "data": "synthetic",
             "config": {"workload": WORKLOAD, "grid": "129x129", "tris": 32768, "dt": 5e-4, "h": 5e-4,
-                       "path": "plain FP64", "l2": "flushed before every timed step",
+                       "path": "mixed: FP32 sub-test filters, FP64 tests (results identical to plain FP64)",
+                       "l2": "flushed before every timed step",
                        "parallelism": "replicas" if ws > 1 else "single"},
+            "plain_fp64": {"value": plain_value, "ms_per_step": plain_ms / args.steps,
+                           "fp64_subtests": int(sum(c.get("fp64_subtests", 0) for c in plain_ctr)),
+                           "stages_ms": {k: round(v[0], 3) for k, v in plain_prof.items()}},
             "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(sum(launches)),
+            "step_ms_quantiles": [round(float(q), 3) for q in np.quantile(step_ms, [0, 0.25, 0.5, 0.75, 1.0])],
             "counters": tot, "stages_ms": {k: round(v[0], 3) for k, v in prof.items()}}
     print(json.dumps(line), flush=True)
     if ws > 1:

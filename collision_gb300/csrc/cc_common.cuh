@@ -80,7 +80,7 @@ struct PassCounters {
     int err;          // ErrBits
     int nvisits;      // narrow-phase calls (pairs not skipped as same-rigid-surface)
     int ncontacts;    // sub-tests that applied an impulse
-    int pad;
+    int nsub;         // sub-tests evaluated in FP64 (not rejected by a filter)
 };
 
 __device__ __forceinline__ double dot3(const double* a, const double* b) {

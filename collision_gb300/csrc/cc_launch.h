@@ -76,8 +76,14 @@ struct NarrowArgs {
     int* uf_parent;
     VisitRec* rec;
     int rec_cap;
+    const float4* pbox_lo;  // null: plain FP64 (no filter)
+    const float4* pbox_hi;
+    float hpad, epad;
 };
 void narrow_pass(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s);
+// Outward-rounded FP32 point boxes for the mixed-precision filter.
+void point_boxes(const double4_32a* xo, const double4_32a* av, double dt, int nv, int moving, float4* lo,
+                 float4* hi, cudaStream_t s);
 
 // ------------------------------------------------------------- post-pass
 struct ApplyBufs {

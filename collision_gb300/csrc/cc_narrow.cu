@@ -21,6 +21,7 @@ __global__ void __launch_bounds__(128) k_narrow(NarrowArgs a, int max_pairs) {
     c.rank = a.rank; c.nt = a.nt; c.pass = a.pass; c.zone = a.zone; c.p = a.p;
     c.contrib = a.contrib; c.contrib_cap = a.contrib_cap; c.ctr = a.ctr; c.uf_parent = a.uf_parent;
     c.rec = a.rec; c.rec_cap = a.rec_cap;
+    c.pbox_lo = a.pbox_lo; c.pbox_hi = a.pbox_hi; c.hpad = a.hpad; c.epad = a.epad;
     int np = a.ctr->npairs;
     if (np > max_pairs) np = max_pairs;
     for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) {
@@ -45,6 +46,7 @@ __global__ void __launch_bounds__(128) k_narrow(NarrowArgs a, int max_pairs) {
         for (int i = 0; i < n1; ++i) st.plist[i] = P1[i];
         for (int i = 0; i < n2; ++i) st.plist[n1 + i] = P2[i];
         st.sub = 0;
+        st.nsub = 0;
         int A[3] = {P1[0], P1[1], n1 == 3 ? P1[2] : -1};
         int B[3] = {P2[0], P2[1], n2 == 3 ? P2[2] : -1};
         bool status;
@@ -55,6 +57,7 @@ __global__ void __launch_bounds__(128) k_narrow(NarrowArgs a, int max_pairs) {
         else
             status = bond_to_bond<MOVING>(c, st, A, B);
         atomicAdd(&c.ctr->nvisits, 1);
+        if (st.nsub) atomicAdd(&c.ctr->nsub, st.nsub);
         if (status) atomicAdd(&c.ctr->nhit_pairs, 1);
         if (c.rec) {
             int slot = atomicAdd(&c.ctr->nrec, 1);
@@ -70,7 +73,37 @@ __global__ void __launch_bounds__(128) k_narrow(NarrowArgs a, int max_pairs) {
     }
 }
 
+// FP32 box of every point over the pass's time window, rounded outward:
+// [x_old] for proximity, [x_old, x_old + dt*avgVel] for CCD.
+template <bool MOVING>
+__global__ void k_point_boxes(const double4_32a* __restrict__ xo, const double4_32a* __restrict__ av, double dt,
+                              int nv, float4* lo, float4* hi) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nv) return;
+    double4_32a x = xo[p];
+    double a[3] = {x.x, x.y, x.z}, b[3] = {x.x, x.y, x.z};
+    if (MOVING) {
+        double4_32a v = av[p];
+        double e[3] = {x.x + v.x * dt, x.y + v.y * dt, x.z + v.z * dt};
+        for (int d = 0; d < 3; ++d) {
+            a[d] = fmin(a[d], e[d]);
+            b[d] = fmax(b[d], e[d]);
+        }
+    }
+    lo[p] = make_float4(__double2float_rd(a[0]), __double2float_rd(a[1]), __double2float_rd(a[2]), 0.f);
+    hi[p] = make_float4(__double2float_ru(b[0]), __double2float_ru(b[1]), __double2float_ru(b[2]), 0.f);
+}
+
 }  // namespace
+
+void point_boxes(const double4_32a* xo, const double4_32a* av, double dt, int nv, int moving, float4* lo,
+                 float4* hi, cudaStream_t s) {
+    if (nv <= 0) return;
+    if (moving)
+        count_launch(), k_point_boxes<true><<<(nv + 255) / 256, 256, 0, s>>>(xo, av, dt, nv, lo, hi);
+    else
+        count_launch(), k_point_boxes<false><<<(nv + 255) / 256, 256, 0, s>>>(xo, av, dt, nv, lo, hi);
+}
 
 void narrow_pass(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s) {
     if (max_pairs <= 0) return;

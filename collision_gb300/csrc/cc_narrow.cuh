@@ -30,6 +30,12 @@ struct NarrowCtx {
     int* uf_parent;
     VisitRec* rec;
     int rec_cap;
+    // mixed precision: per-point FP32 boxes over the pass's time window
+    // (rounded outward), used to reject sub-tests that cannot hit
+    const float4* pbox_lo;
+    const float4* pbox_hi;
+    float hpad;   // h of the sub-tests, rounded up
+    float epad;   // eps (barycentric tolerance), rounded up
 };
 
 struct CallState {
@@ -38,6 +44,7 @@ struct CallState {
     int np;
     int dcount[6];
     int sub;
+    int nsub;   // sub-tests evaluated in FP64
 };
 
 __device__ __forceinline__ bool is_static(const NarrowCtx& c, int p) { return c.fixed[p] != 0; }
@@ -349,31 +356,41 @@ static __device__ bool is_coplanar(const double (*xo4)[3], const double (*av4)[3
         double R = (2 * a * a * a - 9 * a * b + 27 * c) / 54;
         double Q3 = Q * Q * Q;
         double R2 = R * R;
-        // The roots are first formed with the fast library functions. Their
-        // results are within 2 ulp of the correctly rounded ones, which moves
-        // a root by far less than `margin`; only when a root (or a branch
-        // threshold) falls within the margin of a decision are they formed
-        // again with the correctly rounded functions the reference's libm
-        // gives. Roots away from [0, dt] are discarded either way.
+        // The roots are first formed with the fast library functions, whose
+        // results lie within 2 ulp of the correctly rounded ones (CUDA's
+        // documented bound for acos, cos and pow). Carried through the root
+        // formulas that moves a root by at most 2.3e-15 times the root scale
+        // (2*sqrt(Q) + |a| in the trigonometric case, |A| + |B| + |a| in
+        // Cardano's), and `margin` is four times that. A root farther than
+        // the margin from the window [MACH_EPS, dt + MACH_EPS] is discarded
+        // whichever way it was formed; roots inside or near the window, and
+        // branch thresholds within the margin, are formed again with the
+        // correctly rounded functions the reference's libm gives.
         if (R2 < Q3) {
             double Qsqrt = sqrt(Q);
             double z = R / sqrt(Q3);
             double theta = acos(z);
-            double f0 = -2 * Qsqrt * cos(theta / 3) - a / 3;
-            double f1 = -2 * Qsqrt * cos((theta + 2 * kPi) / 3) - a / 3;
-            double f2 = -2 * Qsqrt * cos((theta - 2 * kPi) / 3) - a / 3;
-            double margin = 1e-12 * (2 * fabs(Qsqrt) + fabs(a) + dt);
-            double lo = -margin, hi = dt + kMachEps + margin;
-            bool near_ = (f0 > lo && f0 < hi) || (f1 > lo && f1 < hi) || (f2 > lo && f2 < hi);
-            if (near_) {
-                theta = cr::acos(z);
-                f0 = -2 * Qsqrt * cr::cos(theta / 3) - a / 3;
-                f1 = -2 * Qsqrt * cr::cos((theta + 2 * kPi) / 3) - a / 3;
-                f2 = -2 * Qsqrt * cr::cos((theta - 2 * kPi) / 3) - a / 3;
+            double f[3];
+            f[0] = -2 * Qsqrt * cos(theta / 3) - a / 3;
+            f[1] = -2 * Qsqrt * cos((theta + 2 * kPi) / 3) - a / 3;
+            f[2] = -2 * Qsqrt * cos((theta - 2 * kPi) / 3) - a / 3;
+            double margin = 1e-14 * (2 * fabs(Qsqrt) + fabs(a)) + 1e-300;
+            double lo = kMachEps - margin, hi = dt + kMachEps + margin;
+            bool near_[3];
+            bool any = false;
+            for (int i = 0; i < 3; ++i) {
+                near_[i] = f[i] > lo && f[i] < hi;
+                any |= near_[i];
             }
-            roots[0] = f0;
-            roots[1] = f1;
-            roots[2] = f2;
+            if (any) {
+                theta = cr::acos(z);
+                if (near_[0]) f[0] = -2 * Qsqrt * cr::cos(theta / 3) - a / 3;
+                if (near_[1]) f[1] = -2 * Qsqrt * cr::cos((theta + 2 * kPi) / 3) - a / 3;
+                if (near_[2]) f[2] = -2 * Qsqrt * cr::cos((theta - 2 * kPi) / 3) - a / 3;
+            }
+            roots[0] = f[0];
+            roots[1] = f[1];
+            roots[2] = f[2];
         } else {
             double sgn = (R > 0) ? 1.0 : -1.0;
             double base = fabs(R) + sqrt(R2 - Q3);
@@ -381,11 +398,12 @@ static __device__ bool is_coplanar(const double (*xo4)[3], const double (*av4)[3
             double B = (fabs(A) < kRoundEps) ? 0.0 : Q / A;
             double f0 = (A + B) - a / 3.0;
             double f1 = -0.5 * (A + B) - a / 3.0;
-            double margin = 1e-12 * (fabs(A) + fabs(B) + fabs(a) + dt);
-            double lo = -margin, hi = dt + kMachEps + margin;
+            double scale = fabs(A) + fabs(B) + fabs(a);
+            double margin = 1e-14 * scale + 1e-300;
+            double lo = kMachEps - margin, hi = dt + kMachEps + margin;
             bool near_ = (f0 > lo && f0 < hi) || (f1 > lo && f1 < hi) ||
-                         fabs(fabs(A) - kRoundEps) <= 1e-12 * fabs(A) ||
-                         fabs(fabs(A - B) - kRoundEps) <= 1e-12 * (fabs(A) + fabs(B));
+                         fabs(fabs(A) - kRoundEps) <= 1e-14 * fabs(A) + 1e-300 ||
+                         fabs(fabs(A - B) - kRoundEps) <= 1e-14 * scale + 1e-300;
             if (near_) {
                 A = -sgn * cr::pow(base, 1.0 / 3.0);
                 B = (fabs(A) < kRoundEps) ? 0.0 : Q / A;
@@ -447,8 +465,61 @@ __device__ __forceinline__ bool static_test(const NarrowCtx& c, CallState& st, c
     return EE ? edge_to_edge(c, st, pts, X, c.p.thickness) : point_to_tri(c, st, pts, X, c.p.thickness);
 }
 
+// Mixed-precision filter. Every position an FP64 test evaluates lies in its
+// point's box (x_old and x_old + dt*avgVel, both rounded outward to FP32):
+// the roots are in [0, dt] and x_old + t*avgVel rounds monotonically in t.
+//  - Edge-edge (dcollid3d.cpp:643-776): the closest points v1, v2 lie on the
+//    two segments, so dist >= the segments' distance >= the gap between
+//    their boxes; a hit needs dist <= h.
+//  - Point-triangle (dcollid3d.cpp:778-922): a hit needs the point within h
+//    of the plane and barycentric coordinates in [-eps, 1+eps], so its
+//    projection is within 4*eps*diameter of the triangle. The computed
+//    coordinates carry a solve error of about 1e-16/sin^2 of the smallest
+//    angle, which the reference's determinant cut (|det| >= 1000*MACH_EPS)
+//    keeps below 2^-10 for triangles up to unit size: the reach is padded by
+//    (8*eps + 2^-10) times the triangle's box extent.
+// When the padded boxes do not overlap, the FP64 test returns false and is
+// skipped; every other sub-test runs unchanged, so the results are the plain
+// FP64 path's.
+__device__ __forceinline__ bool mixed_may_hit(const NarrowCtx& c, const int* pts, bool ee) {
+    float4 l0 = c.pbox_lo[pts[0]], h0 = c.pbox_hi[pts[0]];
+    float4 l1 = c.pbox_lo[pts[1]], h1 = c.pbox_hi[pts[1]];
+    float4 l2 = c.pbox_lo[pts[2]], h2 = c.pbox_hi[pts[2]];
+    float4 l3 = c.pbox_lo[pts[3]], h3 = c.pbox_hi[pts[3]];
+    float alo[3], ahi[3], blo[3], bhi[3];
+    if (ee) {
+        alo[0] = fminf(l0.x, l1.x); alo[1] = fminf(l0.y, l1.y); alo[2] = fminf(l0.z, l1.z);
+        ahi[0] = fmaxf(h0.x, h1.x); ahi[1] = fmaxf(h0.y, h1.y); ahi[2] = fmaxf(h0.z, h1.z);
+        blo[0] = fminf(l2.x, l3.x); blo[1] = fminf(l2.y, l3.y); blo[2] = fminf(l2.z, l3.z);
+        bhi[0] = fmaxf(h2.x, h3.x); bhi[1] = fmaxf(h2.y, h3.y); bhi[2] = fmaxf(h2.z, h3.z);
+    } else {
+        alo[0] = fminf(fminf(l0.x, l1.x), l2.x); alo[1] = fminf(fminf(l0.y, l1.y), l2.y);
+        alo[2] = fminf(fminf(l0.z, l1.z), l2.z);
+        ahi[0] = fmaxf(fmaxf(h0.x, h1.x), h2.x); ahi[1] = fmaxf(fmaxf(h0.y, h1.y), h2.y);
+        ahi[2] = fmaxf(fmaxf(h0.z, h1.z), h2.z);
+        blo[0] = l3.x; blo[1] = l3.y; blo[2] = l3.z;
+        bhi[0] = h3.x; bhi[1] = h3.y; bhi[2] = h3.z;
+    }
+    float ext = __fadd_ru(__fadd_ru(__fsub_ru(ahi[0], alo[0]), __fsub_ru(ahi[1], alo[1])), __fsub_ru(ahi[2], alo[2]));
+    float pad;
+    if (ee) {
+        float extb = __fadd_ru(__fadd_ru(__fsub_ru(bhi[0], blo[0]), __fsub_ru(bhi[1], blo[1])),
+                               __fsub_ru(bhi[2], blo[2]));
+        pad = __fadd_ru(c.hpad, __fmul_ru(__fadd_ru(ext, extb), 0x1p-20f));
+    } else {
+        pad = __fadd_ru(c.hpad, __fmul_ru(ext, __fadd_ru(__fmul_ru(8.0f, c.epad), 0x1p-10f)));
+    }
+    for (int d = 0; d < 3; ++d) {
+        if (__fsub_rd(alo[d], pad) > bhi[d]) return false;
+        if (__fadd_ru(ahi[d], pad) < blo[d]) return false;
+    }
+    return true;
+}
+
 template <bool MOVING, bool EE>
 __device__ __forceinline__ bool sub_test(const NarrowCtx& c, CallState& st, const int* pts) {
+    if (c.pbox_lo && !mixed_may_hit(c, pts, EE)) return false;
+    st.nsub++;
     if (MOVING) return moving_test<EE>(c, st, pts);
     return static_test<EE>(c, st, pts);
 }

@@ -294,12 +294,13 @@ __device__ __forceinline__ int strain_quick(double s, const StrainBounds& b) {
     return -1;
 }
 
-struct StrainEdgeStep {
+struct __align__(16) StrainEdgeStep {
     int p0, p1;
     double len0;
     StrainBounds rest;  // from the rest length
     StrainBounds prev;  // from the start-of-step length (strain rate)
-    int exact_only;     // degenerate lengths: always take the exact test
+    double x0[3], x1[3];  // x_old of both points (constant through the sweep)
+    int exact_only;       // degenerate lengths: always take the exact test
     int pad;
 };
 
@@ -322,6 +323,10 @@ __global__ void k_strain_setup(const StrainEdge* __restrict__ edges, int m, cons
     r.len0 = ed.len0;
     r.rest = strain_bounds(ed.len0);
     r.prev = strain_bounds(len_old);
+    for (int k = 0; k < 3; ++k) {
+        r.x0[k] = x0[k];
+        r.x1[k] = x1[k];
+    }
     // tiny or non-positive lengths: leave every decision to the exact test
     r.exact_only = !(len_old > 1e-6 && ed.len0 > 1e-6);
     r.pad = 0;
@@ -331,10 +336,10 @@ __global__ void k_strain_setup(const StrainEdge* __restrict__ edges, int m, cons
 __device__ __forceinline__ bool strain_flag(const StrainEdgeStep& ed, const double4_32a* xo, const double4_32a* av,
                                             double dt) {
     if (!ed.exact_only) {
-        double4_32a a0 = xo[ed.p0], a1 = xo[ed.p1], b0 = av[ed.p0], b1 = av[ed.p1];
-        double d0 = (a0.x + dt * b0.x) - (a1.x + dt * b1.x);
-        double d1 = (a0.y + dt * b0.y) - (a1.y + dt * b1.y);
-        double d2 = (a0.z + dt * b0.z) - (a1.z + dt * b1.z);
+        double4_32a b0 = av[ed.p0], b1 = av[ed.p1];
+        double d0 = (ed.x0[0] + dt * b0.x) - (ed.x1[0] + dt * b1.x);
+        double d1 = (ed.x0[1] + dt * b0.y) - (ed.x1[1] + dt * b1.y);
+        double d2 = (ed.x0[2] + dt * b0.z) - (ed.x1[2] + dt * b1.z);
         double sn = 0.0;
         sn += d0 * d0;
         sn += d1 * d1;
@@ -348,6 +353,27 @@ __device__ __forceinline__ bool strain_flag(const StrainEdgeStep& ed, const doub
     return strain_flag_exact(ed.p0, ed.p1, ed.len0, xo, av, dt);
 }
 
+__device__ __forceinline__ bool strain_flag_counted(const StrainEdgeStep& ed, const double4_32a* xo,
+                                                    const double4_32a* av, double dt, int* n_exact) {
+    if (!ed.exact_only) {
+        double4_32a b0 = av[ed.p0], b1 = av[ed.p1];
+        double d0 = (ed.x0[0] + dt * b0.x) - (ed.x1[0] + dt * b1.x);
+        double d1 = (ed.x0[1] + dt * b0.y) - (ed.x1[1] + dt * b1.y);
+        double d2 = (ed.x0[2] + dt * b0.z) - (ed.x1[2] + dt * b1.z);
+        double sn = 0.0;
+        sn += d0 * d0;
+        sn += d1 * d1;
+        sn += d2 * d2;
+        if (sn > 1e-18) {
+            int q0 = strain_quick(sn, ed.rest), q1 = strain_quick(sn, ed.prev);
+            if (q0 == 1 || q1 == 1) return true;
+            if (q0 == 0 && q1 == 0) return false;
+        }
+    }
+    ++*n_exact;
+    return strain_flag_exact(ed.p0, ed.p1, ed.len0, xo, av, dt);
+}
+
 // reduceSuperelast, dcollid.cpp:586-596: up to 10 Gauss-Seidel passes over
 // the edges in element order, each averaging the two end velocities of an
 // over-strained edge before the next edge is tested. The edges arrive sorted
@@ -356,36 +382,61 @@ __device__ __forceinline__ bool strain_flag(const StrainEdgeStep& ed, const doub
 // no point and see exactly the values the sequential sweep gives them: the
 // level-by-level walk below is the reference's sweep, reordered only where
 // the order cannot matter.
-__global__ void __launch_bounds__(512) k_strain(const StrainEdgeStep* __restrict__ edges,
+__global__ void __launch_bounds__(256) k_strain(const StrainEdgeStep* __restrict__ edges,
                                                 const int* __restrict__ level_off, int nlevels,
                                                 const double4_32a* __restrict__ xo, double4_32a* av, double dt,
                                                 int* passes_out) {
-    __shared__ int s_has;
-    int passes = 0;
+    __shared__ int s_has, s_avg, s_exact;
+    if (threadIdx.x == 0) s_avg = s_exact = 0;
+    int passes = 0, n_avg = 0, n_exact = 0;
     for (int pass = 0; pass < kStrainMaxIter; ++pass) {
         if (threadIdx.x == 0) s_has = 0;
         __syncthreads();
         passes++;
+        // the records of the next level are loaded before the barrier that
+        // ends the current one: they do not depend on the velocities
+        int e = level_off[0] + threadIdx.x, e1 = level_off[1];
+        StrainEdgeStep cur;
+        bool have = e < e1;
+        if (have) cur = edges[e];
         for (int l = 0; l < nlevels; ++l) {
-            int e1 = level_off[l + 1];
-            for (int e = level_off[l] + threadIdx.x; e < e1; e += blockDim.x) {
-                StrainEdgeStep ed = edges[e];
-                if (strain_flag(ed, xo, av, dt)) {
-                    double4_32a a0 = av[ed.p0], a1 = av[ed.p1];
+            int ne = (l + 1 < nlevels) ? level_off[l + 1] + threadIdx.x : 0;
+            int ne1 = (l + 1 < nlevels) ? level_off[l + 2] : 0;
+            bool nhave = ne < ne1;
+            StrainEdgeStep nxt;
+            if (nhave) nxt = edges[ne];
+            while (have) {
+                if (strain_flag_counted(cur, xo, av, dt, &n_exact)) {
+                    ++n_avg;
+                    double4_32a a0 = av[cur.p0], a1 = av[cur.p1];
                     double t0 = a0.x + a1.x, t1 = a0.y + a1.y, t2 = a0.z + a1.z;
                     t0 = 0.5 * t0; t1 = 0.5 * t1; t2 = 0.5 * t2;
                     double4_32a nv4 = make_double4_32a(t0, t1, t2, 0.0);
-                    av[ed.p0] = nv4;
-                    av[ed.p1] = nv4;
+                    av[cur.p0] = nv4;
+                    av[cur.p1] = nv4;
                     s_has = 1;
                 }
+                e += blockDim.x;
+                have = e < e1;
+                if (have) cur = edges[e];
             }
             __syncthreads();
+            e = ne;
+            e1 = ne1;
+            have = nhave;
+            cur = nxt;
         }
         if (!s_has) break;
         __syncthreads();
     }
-    if (threadIdx.x == 0) *passes_out = passes;
+    atomicAdd(&s_avg, n_avg);
+    atomicAdd(&s_exact, n_exact);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        passes_out[0] = passes;
+        passes_out[1] = s_avg;
+        passes_out[2] = s_exact;
+    }
 }
 
 __global__ void k_final_velocity(const uint8_t* __restrict__ in_elem, const uint8_t* __restrict__ has_collsn,
@@ -475,7 +526,7 @@ void strain_limit(const StrainEdge* edges, int nedges, const int* level_off, int
     }
     StrainEdgeStep* se = (StrainEdgeStep*)step_buf;
     count_launch(), k_strain_setup<<<nblk(nedges, 256), 256, 0, s>>>(edges, nedges, xo, se);
-    count_launch(), k_strain<<<1, 512, 0, s>>>(se, level_off, nlevels, xo, av, dt, passes_out);
+    count_launch(), k_strain<<<1, 256, 0, s>>>(se, level_off, nlevels, xo, av, dt, passes_out);
 }
 
 void final_velocity(const uint8_t* in_elem, const uint8_t* has_collsn, const double4_32a* av, double* vel, int nv,

@@ -3,6 +3,7 @@
 // include/collision_gb300.h.
 #include <cstdio>
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -37,7 +38,7 @@ void dfree(T*& p) {
 __global__ void k_reset_counters(PassCounters* c) {
     int keep = c->err & kErrNan;
     c->npairs = 0; c->ncontrib = 0; c->nhit_pairs = 0; c->nrec = 0;
-    c->nvisits = 0; c->ncontacts = 0; c->err = keep;
+    c->nvisits = 0; c->ncontacts = 0; c->nsub = 0; c->err = keep;
 }
 
 unsigned long long enc_host(double x) {
@@ -111,7 +112,7 @@ struct cc_solver {
 
     cc_params prm{1e-3, 1e-4, 1e-6, 1000.0, 0.01, 0.02, 0.0};
     double lo[3] = {-1e30, -1e30, -1e30}, hi[3] = {1e30, 1e30, 1e30};
-    long long counters[10] = {0};
+    long long counters[13] = {0};
     int pass_index = 0;
     bool own_stream = true;
     long long launches_last = 0;
@@ -149,6 +150,9 @@ struct cc_solver {
         ev_marks.clear();
     }
     int zone_cap = 10000;
+    int mode = 0;  // 0 plain FP64, 1 mixed precision
+    float4* d_pbox_lo = nullptr;
+    float4* d_pbox_hi = nullptr;
 
     ~cc_solver() { release(); }
 
@@ -168,7 +172,7 @@ struct cc_solver {
         if (zone.sort_temp) cudaFree(zone.sort_temp);
         zone.sort_temp = nullptr;
         dfree(d_rank[0]); dfree(d_rank[1]);
-        dfree(d_level_off); dfree(d_strain_passes); dfree(d_rec);
+        dfree(d_level_off); dfree(d_strain_passes); dfree(d_rec); dfree(d_pbox_lo); dfree(d_pbox_hi);
         if (d_strain_step) cudaFree(d_strain_step);
         d_strain_step = nullptr;
         pair_cap = contrib_cap = rec_cap = 0;
@@ -340,8 +344,10 @@ cc_status cc_solver::assemble(const cc_mesh* m) {
     ok &= dalloc(&d_rank[0], (size_t)ne) == cudaSuccess;
     ok &= dalloc(&d_rank[1], (size_t)ne) == cudaSuccess;
     ok &= dalloc(&d_level_off, (size_t)nlevels + 1) == cudaSuccess;
+    ok &= dalloc(&d_pbox_lo, (size_t)nv) == cudaSuccess;
+    ok &= dalloc(&d_pbox_hi, (size_t)nv) == cudaSuccess;
     ok &= cudaMalloc(&d_strain_step, strain_step_bytes(nedges)) == cudaSuccess;
-    ok &= dalloc(&d_strain_passes, 1) == cudaSuccess;
+    ok &= dalloc(&d_strain_passes, 3) == cudaSuccess;
     if (!ok) return fail(CC_NO_MEMORY, "device allocation failed");
     cc_status st = grow_pairs(16 * ne + 4096);
     if (st) return st;
@@ -404,6 +410,7 @@ cc_status cc_solver::detect_pass(int moving, int zone_mode, bool* is_collision) 
     if (st) return st;
     prof(kStBvh, true);
     bvh_build(d_box, bvh, stream);
+    if (mode == 1) point_boxes(d_xo, d_av, prm.dt, nv, moving, d_pbox_lo, d_pbox_hi, stream);
     prof(kStBvh, false);
     Params p = params();
     for (int attempt = 0; attempt < 8; ++attempt) {
@@ -416,6 +423,18 @@ cc_status cc_solver::detect_pass(int moving, int zone_mode, bool* is_collision) 
         a.rank = d_rank[moving]; a.nt = nt; a.pass = pass; a.zone = zone_mode; a.p = p; a.pairs = d_pairs;
         a.contrib = d_contrib; a.contrib_cap = contrib_cap; a.ctr = d_ctr; a.uf_parent = d_uf;
         a.rec = record ? d_rec : nullptr; a.rec_cap = rec_cap;
+        a.pbox_lo = mode == 1 ? d_pbox_lo : nullptr;
+        a.pbox_hi = mode == 1 ? d_pbox_hi : nullptr;
+        {
+            // h of the sub-tests (thickness for proximity, eps for CCD) and
+            // the barycentric tolerance eps, rounded up to FP32
+            double h = moving ? prm.eps : prm.thickness;
+            float hf = (float)h, ef = (float)prm.eps;
+            if ((double)hf < h) hf = nextafterf(hf, 1e30f);
+            if ((double)ef < prm.eps) ef = nextafterf(ef, 1e30f);
+            a.hpad = hf;
+            a.epad = ef;
+        }
         prof(moving ? kStNarrowCcd : kStNarrowProx, true);
         narrow_pass(a, moving, pair_cap, stream);
         prof(moving ? kStNarrowCcd : kStNarrowProx, false);
@@ -449,6 +468,7 @@ cc_status cc_solver::detect_pass(int moving, int zone_mode, bool* is_collision) 
     counters[4] += h_ctr->nvisits;
     counters[5] += h_ctr->nhit_pairs;
     counters[6] += h_ctr->ncontacts;
+    counters[12] += h_ctr->nsub;
     if (record && h_ctr->nrec > 0) {
         size_t base = visits.size();
         visits.resize(base + (size_t)h_ctr->nrec);
@@ -526,10 +546,12 @@ cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, dou
     prof(kStStrain, false);
     final_velocity(d_in_elem, d_hc, d_av, vel, nv, stream);
     if (hc != d_hc) cudaMemcpyAsync(hc, d_hc, (size_t)nv, cudaMemcpyDeviceToDevice, stream);
-    int sp = 0;
-    cudaMemcpyAsync(&sp, d_strain_passes, sizeof(int), cudaMemcpyDeviceToHost, stream);
+    int sp[3] = {0, 0, 0};
+    if (nedges) cudaMemcpyAsync(sp, d_strain_passes, 3 * sizeof(int), cudaMemcpyDeviceToHost, stream);
     if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("finalize");
-    counters[7] = nedges ? sp : 1;
+    counters[7] = nedges ? sp[0] : 1;
+    counters[10] = sp[1];
+    counters[11] = sp[2];
     prof_collect();
     if (has_collision) *has_collision = hcol;
     return cuda_check("resolve");
@@ -612,7 +634,7 @@ cc_status cc_resolve_device(cc_solver* s, const double* x_old, const double* x_c
 int cc_get_counters(cc_solver* s, long long* out, int n) {
     if (!s || !out) return 0;
     s->counters[9] = s->launches_last;
-    int m = n < 10 ? n : 10;
+    int m = n < 13 ? n : 13;
     for (int i = 0; i < m; ++i) out[i] = s->counters[i];
     return m;
 }
@@ -710,6 +732,12 @@ cc_status cc_set_stream(cc_solver* s, void* stream) {
         if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) return CC_CUDA_ERROR;
         s->own_stream = true;
     }
+    return CC_OK;
+}
+
+cc_status cc_set_mode(cc_solver* s, int mode) {
+    if (!s || mode < 0 || mode > 1) return CC_BAD_INPUT;
+    s->mode = mode;
     return CC_OK;
 }
 

@@ -141,6 +141,12 @@ class CollisionSolver3d:
         """Run on a caller's CUDA stream (e.g. torch.cuda.current_stream().cuda_stream)."""
         self._check(self._lib.cc_set_stream(self._h, stream_handle))
 
+    PLAIN_FP64, MIXED = 0, 1
+
+    def setMode(self, mode: int):
+        """0: plain FP64; 1: FP32 filters in front of the same FP64 tests."""
+        self._check(self._lib.cc_set_mode(self._h, int(mode)))
+
     def setProfiling(self, on: bool):
         self._check(self._lib.cc_set_profiling(self._h, int(bool(on))))
 
@@ -155,11 +161,12 @@ class CollisionSolver3d:
 
     # ------------------------------------------------------- inspection
     COUNTER_NAMES = ("passes", "ccd_passes", "zone_passes", "candidate_pairs", "visits", "hit_pairs",
-                     "contacts", "strain_passes", "tree_builds", "kernel_launches")
+                     "contacts", "strain_passes", "tree_builds", "kernel_launches", "strain_averaged",
+                     "strain_exact", "fp64_subtests")
 
     def counters(self) -> dict:
-        out = (C.c_longlong * 10)()
-        n = self._lib.cc_get_counters(self._h, out, 10)
+        out = (C.c_longlong * 13)()
+        n = self._lib.cc_get_counters(self._h, out, 13)
         return dict(zip(self.COUNTER_NAMES[:n], list(out)[:n]))
 
     def setRecording(self, on: bool):

@@ -116,10 +116,20 @@ cc_status cc_resolve(cc_solver* s, const double* x_old, const double* x_cand, do
 cc_status cc_resolve_device(cc_solver* s, const double* x_old, const double* x_cand, double* vel,
                             uint8_t* has_collsn, double* x_out, int* has_collision);
 
+/* Arithmetic of the narrow phase:
+ *   0  plain FP64 (default): every sub-test evaluated in FP64 as the reference
+ *   1  mixed precision: FP32 swept boxes of each sub-test's points, rounded
+ *      outward and padded by the test's reach, reject sub-tests that cannot
+ *      hit; the others are evaluated in FP64 exactly as in mode 0, so the
+ *      results are the same as mode 0's. */
+cc_status cc_set_mode(cc_solver* s, int mode);
+
 /* Counters of the last step, in this order: detection passes, CCD passes,
  * impact-zone passes, candidate pairs (all passes), narrow-phase visits,
  * pairs that hit, contacts (sub-tests that applied an impulse), strain
- * passes, tree builds, kernel launches. Returns how many were written. */
+ * passes, tree builds, kernel launches, strain edges averaged, strain tests
+ * taken the exact way, sub-tests evaluated in FP64. Returns how many were
+ * written. */
 int cc_get_counters(cc_solver* s, long long* out, int n);
 
 /* Recording for parity checks: when on, every narrow-phase visit of the

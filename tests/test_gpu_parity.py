@@ -171,3 +171,33 @@ def test_bad_inputs_are_rejected(solver_cls):
     xc = scenes.candidate(sc, x, sc.v)
     s.resolveCollision(x, xc, sc.v, np.zeros(sc.nv, np.uint8))
     s.close()
+
+
+@pytest.mark.parametrize("make", [
+    lambda: scenes.cloth_on_sphere(n=12, z=0.252, radius=0.25, sub=2, side=0.4, mu=0.3, speed=3.0, seed=2),
+    lambda: scenes.folded_cloth(n=33, dt=5e-4, h=2e-3, seed=1, vscale=20.0),
+    lambda: scenes.strings(nstr=16, nseg=128, seglen=2e-3, seed=4, box_lo=(-0.2, -0.2, -0.05),
+                           box_hi=(0.2, 0.2, 0.049), z_range=(0.0502, 0.06), volume_z=(0.05, 0.08), speed=2.0),
+], ids=["sphere_zones", "folded", "strings"])
+def test_mixed_precision_equals_plain(solver_cls, make):
+    """The FP32 filters only skip sub-tests that cannot hit: the mixed path's
+    results, visit records and zones are the plain FP64 path's, bit for bit."""
+    from collision_gb300.solver import ordered_visits
+    sc = make()
+    plain, mixed = solver_cls(0), solver_cls(0)
+    for s, mode in ((plain, 0), (mixed, 1)):
+        s.assembleFromScene(sc)
+        s.setMode(mode)
+        s.setRecording(True)
+    x, v, hc = sc.x.copy(), sc.v.copy(), np.zeros(sc.nv, np.uint8)
+    for step in range(8):
+        xc = scenes.candidate(sc, x, v)
+        a = plain.resolveCollision(x, xc, v, hc)
+        b = mixed.resolveCollision(x, xc, v, hc)
+        for u, w in zip(a, b):
+            assert np.array_equal(u, w), f"step {step}"
+        assert record_sha(ordered_visits(plain.visits())) == record_sha(ordered_visits(mixed.visits()))
+        assert np.array_equal(zone_labels(plain.zoneRoots()), zone_labels(mixed.zoneRoots()))
+        x, v, hc = a
+    plain.close()
+    mixed.close()
