@@ -82,6 +82,8 @@ def load(path: str = LIB_PATH):
     lib.cc_debug_candidate_pairs.argtypes = [vp, C.c_int, C.c_int, ip, C.c_int]
     lib.cc_set_stream.restype = C.c_int
     lib.cc_set_stream.argtypes = [vp, vp]
+    lib.cc_set_strain_window.restype = C.c_int
+    lib.cc_set_strain_window.argtypes = [vp, C.c_int]
     lib.cc_set_mode.restype = C.c_int
     lib.cc_set_mode.argtypes = [vp, C.c_int]
     lib.cc_set_profiling.restype = C.c_int

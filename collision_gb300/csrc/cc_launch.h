@@ -122,12 +122,27 @@ void finalize_positions(const uint8_t* in_elem, const double4_32a* xo, double4_3
 struct StrainEdge {
     int p0, p1;
     double len0;
+    int s0, s1;  // shared-memory slots of p0, p1 in the window sweep
+};
+// Shared-memory window schedule of the strain sweep (see k_strain_window):
+// per level l, load_list[load_off[l] .. load_off[l+1]) are (point, slot)
+// pairs to copy in and wb_list[wb_off[l] .. wb_off[l+1]) pairs to write back
+// (wb level nlevels: after the last level).
+struct StrainWindow {
+    int nslots;
+    const int2* load_list;
+    const int* load_off;
+    const int2* wb_list;
+    const int* wb_off;
+    const int4* hdr;  // per level: (edge begin, end, load begin, end), (write-back begin, end, 0, 0)
+    int2 wb_final;    // write-backs after the last level
 };
 // edges sorted by dependency level; level_off has nlevels+1 offsets;
 // step_buf holds strain_step_bytes(nedges).
 size_t strain_step_bytes(int nedges);
 void strain_limit(const StrainEdge* edges, int nedges, const int* level_off, int nlevels, const double4_32a* xo,
-                  double4_32a* av, double dt, void* step_buf, int* passes_out, cudaStream_t s);
+                  double4_32a* av, int nv, double dt, void* step_buf, const StrainWindow* win, int* passes_out,
+                  cudaStream_t s);
 // Correctly rounded cos/sin/acos/pow (fn 0..3) on device arrays, for self-tests.
 void math_selftest(int fn, const double* a, const double* b, double* out, int n, cudaStream_t s);
 // updateFinalVelocity.

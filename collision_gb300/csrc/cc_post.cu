@@ -2,8 +2,12 @@
 // a pass's impulses, impact-zone rigid motion, the domain clamp, final
 // positions, strain limiting and final velocities (dcollid.cpp:116-220,
 // 290-310, 486-624, 677-751; dcollid3d.cpp:70-200).
+#include <cooperative_groups.h>
+
 #include "cc_launch.h"
 #include "cc_narrow.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace ccg {
 
@@ -301,13 +305,28 @@ struct __align__(16) StrainEdgeStep {
     StrainBounds prev;  // from the start-of-step length (strain rate)
     double x0[3], x1[3];  // x_old of both points (constant through the sweep)
     int exact_only;       // degenerate lengths: always take the exact test
+    int s0, s1;           // shared-memory slots of both points (window sweep)
     int pad;
+    // FP32 view for the window sweep's first decision: x_old(p0) - x_old(p1)
+    // and the four squared-length bounds rounded outward (see k_strain_window)
+    float dx[3];
+    float over_hi, under_hi, under_lo, over_lo;
+    float pad2[2];
+};
+
+// The part of an edge record the window sweep reads for every edge: the
+// slots, x_old(p0) - x_old(p1) and the four bounds in FP32 (48 bytes).
+struct __align__(16) StrainEdgeHot {
+    int s0, s1;
+    float dx[3];
+    float over_hi, under_hi, under_lo, over_lo;
+    int pad[3];
 };
 
 // Per-step set-up of the strain sweep: the start-of-step length of every
 // edge (x_old does not change during the sweep) and both sets of bounds.
 __global__ void k_strain_setup(const StrainEdge* __restrict__ edges, int m, const double4_32a* __restrict__ xo,
-                               StrainEdgeStep* out) {
+                               StrainEdgeStep* out, StrainEdgeHot* hot) {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= m) return;
     StrainEdge ed = edges[e];
@@ -329,8 +348,30 @@ __global__ void k_strain_setup(const StrainEdge* __restrict__ edges, int m, cons
     }
     // tiny or non-positive lengths: leave every decision to the exact test
     r.exact_only = !(len_old > 1e-6 && ed.len0 > 1e-6);
+    r.s0 = ed.s0;
+    r.s1 = ed.s1;
     r.pad = 0;
+    for (int k = 0; k < 3; ++k) r.dx[k] = (float)(x0[k] - x1[k]);
+    // strain flags when s > hi_def (either bound) or s < lo_def; it is clear
+    // when lo_no < s < hi_no for both; FP32 thresholds rounded outward
+    double hdef = fmin(r.rest.hi_def, r.prev.hi_def), ldef = fmax(r.rest.lo_def, r.prev.lo_def);
+    double hno = fmin(r.rest.hi_no, r.prev.hi_no), lno = fmax(r.rest.lo_no, r.prev.lo_no);
+    r.over_hi = __double2float_ru(hdef);
+    r.over_lo = __double2float_rd(ldef);
+    r.under_hi = __double2float_rd(hno);
+    r.under_lo = __double2float_ru(lno);
+    r.pad2[0] = r.pad2[1] = 0.f;
     out[e] = r;
+    StrainEdgeHot hh;
+    hh.s0 = r.s0;
+    hh.s1 = r.s1;
+    for (int k = 0; k < 3; ++k) hh.dx[k] = r.dx[k];
+    hh.over_hi = r.over_hi;
+    hh.under_hi = r.under_hi;
+    hh.under_lo = r.under_lo;
+    hh.over_lo = r.over_lo;
+    hh.pad[0] = hh.pad[1] = hh.pad[2] = 0;
+    hot[e] = hh;
 }
 
 __device__ __forceinline__ bool strain_flag(const StrainEdgeStep& ed, const double4_32a* xo, const double4_32a* av,
@@ -351,6 +392,34 @@ __device__ __forceinline__ bool strain_flag(const StrainEdgeStep& ed, const doub
         }
     }
     return strain_flag_exact(ed.p0, ed.p1, ed.len0, xo, av, dt);
+}
+
+// The strain decision for given end velocities v0, v1 (bounds first, the
+// exact test of dcollid.cpp:525-530 only inside the bounds' margin).
+__device__ __forceinline__ bool strain_flag_vals(const StrainEdgeStep& ed, const double* v0, const double* v1,
+                                                 double dt, int* n_exact) {
+    double c0[3], c1[3];
+    for (int k = 0; k < 3; ++k) {
+        c0[k] = ed.x0[k] + dt * v0[k];
+        c1[k] = ed.x1[k] + dt * v1[k];
+    }
+    double sn = 0.0;
+    for (int k = 0; k < 3; ++k) sn += sqr(c0[k] - c1[k]);
+    if (!ed.exact_only && sn > 1e-18) {
+        int q0 = strain_quick(sn, ed.rest), q1 = strain_quick(sn, ed.prev);
+        if (q0 == 1 || q1 == 1) return true;
+        if (q0 == 0 && q1 == 0) return false;
+    }
+    ++*n_exact;
+    double so = 0.0;
+    for (int k = 0; k < 3; ++k) so += sqr(ed.x0[k] - ed.x1[k]);
+    double len_new = sqrt(sn), len_old = sqrt(so);
+    if (len_old > kRoundEps && len_new > kRoundEps) {
+        double strain_rate = (len_new - len_old) / len_old;
+        double strain = (len_new - ed.len0) / ed.len0;
+        return fabs(strain) > kStrainTol || fabs(strain_rate) > kStrainTol;
+    }
+    return true;
 }
 
 __device__ __forceinline__ bool strain_flag_counted(const StrainEdgeStep& ed, const double4_32a* xo,
@@ -406,9 +475,10 @@ __global__ void __launch_bounds__(256) k_strain(const StrainEdgeStep* __restrict
             StrainEdgeStep nxt;
             if (nhave) nxt = edges[ne];
             while (have) {
-                if (strain_flag_counted(cur, xo, av, dt, &n_exact)) {
+                double4_32a a0 = av[cur.p0], a1 = av[cur.p1];
+                double v0[3] = {a0.x, a0.y, a0.z}, v1[3] = {a1.x, a1.y, a1.z};
+                if (strain_flag_vals(cur, v0, v1, dt, &n_exact)) {
                     ++n_avg;
-                    double4_32a a0 = av[cur.p0], a1 = av[cur.p1];
                     double t0 = a0.x + a1.x, t1 = a0.y + a1.y, t2 = a0.z + a1.z;
                     t0 = 0.5 * t0; t1 = 0.5 * t1; t2 = 0.5 * t2;
                     double4_32a nv4 = make_double4_32a(t0, t1, t2, 0.0);
@@ -433,6 +503,231 @@ __global__ void __launch_bounds__(256) k_strain(const StrainEdgeStep* __restrict
     atomicAdd(&s_exact, n_exact);
     __syncthreads();
     if (threadIdx.x == 0) {
+        passes_out[0] = passes;
+        passes_out[1] = s_avg;
+        passes_out[2] = s_exact;
+    }
+}
+
+// The same sweep with each point's velocity in shared memory while the
+// sweep uses it. Levels advance along the mesh like a wavefront, so a point
+// is live for only a few levels: at assembly every point gets a shared-memory
+// slot for its live interval (interval colouring; 418 slots for a 129x129
+// cloth). Its velocity is copied in with cp.async kWindowAhead levels before
+// its first edge and written back the level after its last one.
+//
+// FP64 runs at a small fraction of the FP32 rate on this GPU and the sweep
+// runs on one SM, so each slot also keeps an FP32 copy of the velocity and
+// an edge is first decided in FP32: s32 = |dx + dt (v0 - v1)|^2 from the
+// FP32 copies carries an error below 32 * 2^-24 * bnd^2 (bnd: sum of the
+// magnitudes entering it), and only when s32 +- that error straddles one of
+// the outward-rounded bounds does the FP64 decision (bounds, then the exact
+// test) run. The averaging itself is FP64, as in the reference.
+constexpr int kWindowAhead = 8;
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem));
+}
+
+// slot layout: [x y] [z -] as double2, then [x y z -] as float4
+struct WinSlot {
+    double2 a, b;
+    float4 f;
+    float4 pad;
+};
+
+__device__ __forceinline__ int strain_decide32(const StrainEdgeHot& ed, float4 f0, float4 f1, float dt32) {
+    float u[3], bnd = 0.f;
+    float v0[3] = {f0.x, f0.y, f0.z}, v1[3] = {f1.x, f1.y, f1.z};
+    float s32 = 0.f;
+    for (int k = 0; k < 3; ++k) {
+        float dv = __fsub_rn(v0[k], v1[k]);
+        u[k] = __fadd_rn(ed.dx[k], __fmul_rn(dt32, dv));
+        bnd = __fadd_ru(bnd, __fadd_ru(fabsf(ed.dx[k]), __fmul_ru(dt32, __fadd_ru(fabsf(v0[k]), fabsf(v1[k])))));
+        s32 = __fadd_rn(s32, __fmul_rn(u[k], u[k]));
+    }
+    float err = __fmul_ru(__fmul_ru(bnd, bnd), 32.0f * 5.9604645e-8f);
+    float lo = __fsub_rd(s32, err), hi = __fadd_ru(s32, err);
+    if (lo > ed.over_hi || hi < ed.over_lo) return 1;
+    if (hi < ed.under_hi && lo > ed.under_lo) return 0;
+    return -1;
+}
+
+__device__ __forceinline__ void strain_window_edge(const StrainEdgeHot& h, int e,
+                                                   const StrainEdgeStep* __restrict__ edges, WinSlot* s_win,
+                                                   float dt32, double dt, int* n_avg, int* n_exact, bool* has) {
+    WinSlot& w0 = s_win[h.s0];
+    WinSlot& w1 = s_win[h.s1];
+    int q = strain_decide32(h, w0.f, w1.f, dt32);
+    if (q == 0) return;
+    double2 a0 = w0.a, a1 = w0.b, b0 = w1.a, b1 = w1.b;
+    double v0[3] = {a0.x, a0.y, a1.x}, v1[3] = {b0.x, b0.y, b1.x};
+    if (q < 0) {
+        StrainEdgeStep full = edges[e];
+        if (!strain_flag_vals(full, v0, v1, dt, n_exact)) return;
+    }
+    ++*n_avg;
+    double t[3];
+    for (int k = 0; k < 3; ++k) {
+        t[k] = v0[k] + v1[k];
+        t[k] = 0.5 * t[k];
+    }
+    double2 na = make_double2(t[0], t[1]), nb = make_double2(t[2], 0.0);
+    float4 nf = make_float4((float)t[0], (float)t[1], (float)t[2], 0.f);
+    w0.a = na; w0.b = nb; w0.f = nf;
+    w1.a = na; w1.b = nb; w1.f = nf;
+    *has = true;
+}
+
+// Everything a thread needs for a level arrives kRing levels early in a
+// register ring: the level's ranges, and the thread's first edge record,
+// copy-in entry and write-back entry. Entries beyond the first per thread
+// (levels wider than the block) are read when needed.
+constexpr int kRing = 4;
+
+__global__ void __launch_bounds__(256) k_strain_window(const StrainEdgeStep* __restrict__ edges,
+                                                       const StrainEdgeHot* __restrict__ hot,
+                                                       const int4* __restrict__ hdr, int nlevels,
+                                                       const int2* __restrict__ load_list,
+                                                       const int2* __restrict__ wb_list, int2 wb_final,
+                                                       double4_32a* av, double dt, int* passes_out) {
+    extern __shared__ WinSlot s_win[];
+    __shared__ int s_has[2];
+    __shared__ int s_avg, s_exact;
+    if (threadIdx.x == 0) {
+        s_has[0] = s_has[1] = 0;
+        s_avg = s_exact = 0;
+    }
+    __syncthreads();
+    const int tid = threadIdx.x;
+    const float dt32 = __double2float_ru(dt);
+    int passes = 0, n_avg = 0, n_exact = 0;
+    for (int pass = 0; pass < kStrainMaxIter; ++pass) {
+        const int hs = pass & 1;
+        passes++;
+        bool has = false;
+        // hdr[2*l] = (edge begin, edge end, load begin, load end),
+        // hdr[2*l+1] = (write-back begin, write-back end, -, -)
+        int4 rh0[kRing], rh1[kRing];
+        StrainEdgeHot rhot[kRing];
+        int2 rld[kRing], rwb[kRing];
+        int lslot[kWindowAhead];  // slot this thread copied in, per recent level (-1: none)
+#pragma unroll
+        for (int j = 0; j < kWindowAhead; ++j) lslot[j] = -1;
+#pragma unroll
+        for (int j = 0; j < kRing; ++j) {
+            if (j < nlevels) {
+                rh0[j] = hdr[2 * j];
+                rh1[j] = hdr[2 * j + 1];
+                if (rh0[j].x + tid < rh0[j].y) rhot[j] = hot[rh0[j].x + tid];
+                if (rh0[j].z + tid < rh0[j].w) rld[j] = load_list[rh0[j].z + tid];
+                if (rh1[j].x + tid < rh1[j].y) rwb[j] = wb_list[rh1[j].x + tid];
+            }
+        }
+        for (int l = 0; l < nlevels; ++l) {
+            const int4 h0 = rh0[0], h1 = rh1[0];
+            const StrainEdgeHot cur = rhot[0];
+            const int2 ld = rld[0], wb = rwb[0];
+#pragma unroll
+            for (int j = 0; j + 1 < kRing; ++j) {
+                rh0[j] = rh0[j + 1];
+                rh1[j] = rh1[j + 1];
+                rhot[j] = rhot[j + 1];
+                rld[j] = rld[j + 1];
+                rwb[j] = rwb[j + 1];
+            }
+            {
+                const int lk = l + kRing;
+                if (lk < nlevels) {
+                    int4 a = hdr[2 * lk], b = hdr[2 * lk + 1];
+                    rh0[kRing - 1] = a;
+                    rh1[kRing - 1] = b;
+                    if (a.x + tid < a.y) rhot[kRing - 1] = hot[a.x + tid];
+                    if (a.z + tid < a.w) rld[kRing - 1] = load_list[a.z + tid];
+                    if (b.x + tid < b.y) rwb[kRing - 1] = wb_list[b.x + tid];
+                }
+            }
+            // copy in the points whose slot opens now
+            int my_slot = -1;
+            if (h0.z + tid < h0.w) {
+                my_slot = ld.y;
+                cp_async16(&s_win[ld.y].a, &av[ld.x]);
+                cp_async16(&s_win[ld.y].b, reinterpret_cast<const double2*>(&av[ld.x]) + 1);
+                for (int i = h0.z + tid + (int)blockDim.x; i < h0.w; i += blockDim.x) {
+                    int2 ps = load_list[i];
+                    cp_async16(&s_win[ps.y].a, &av[ps.x]);
+                    cp_async16(&s_win[ps.y].b, reinterpret_cast<const double2*>(&av[ps.x]) + 1);
+                }
+            }
+            asm volatile("cp.async.commit_group;\n" ::);
+            // FP32 copies of the points whose copy has now landed (each by the
+            // thread that issued it): all of level 0's at once, then those
+            // issued kWindowAhead levels ago, before their first edge
+            const int old_slot = lslot[0];
+#pragma unroll
+            for (int j = 0; j + 1 < kWindowAhead; ++j) lslot[j] = lslot[j + 1];
+            lslot[kWindowAhead - 1] = my_slot;
+            int cl = -1, cslot = -1;
+            if (l == 0) {
+                asm volatile("cp.async.wait_group 0;\n" ::);
+                cl = 0;
+                cslot = my_slot;
+            } else if (l < kWindowAhead) {
+                asm volatile("cp.async.wait_group 0;\n" ::);
+            } else {
+                asm volatile("cp.async.wait_group %0;\n" ::"n"(kWindowAhead));
+                if (l - kWindowAhead >= 1) {
+                    cl = l - kWindowAhead;
+                    cslot = old_slot;
+                }
+            }
+            if (cl >= 0) {
+                if (cslot >= 0) {
+                    WinSlot& w = s_win[cslot];
+                    w.f = make_float4((float)w.a.x, (float)w.a.y, (float)w.b.x, 0.f);
+                    // further entries of that level (wider than the block)
+                    int4 hc = hdr[2 * cl];
+                    for (int i = hc.z + tid + (int)blockDim.x; i < hc.w; i += blockDim.x) {
+                        WinSlot& w2 = s_win[load_list[i].y];
+                        w2.f = make_float4((float)w2.a.x, (float)w2.a.y, (float)w2.b.x, 0.f);
+                    }
+                }
+            }
+            __syncthreads();
+            // write back the points last used at the previous level
+            if (h1.x + tid < h1.y) {
+                double2 a = s_win[wb.y].a, b = s_win[wb.y].b;
+                av[wb.x] = make_double4_32a(a.x, a.y, b.x, 0.0);
+                for (int i = h1.x + tid + (int)blockDim.x; i < h1.y; i += blockDim.x) {
+                    int2 ps = wb_list[i];
+                    double2 a2 = s_win[ps.y].a, b2 = s_win[ps.y].b;
+                    av[ps.x] = make_double4_32a(a2.x, a2.y, b2.x, 0.0);
+                }
+            }
+            int e = h0.x + tid;
+            if (e < h0.y) {
+                strain_window_edge(cur, e, edges, s_win, dt32, dt, &n_avg, &n_exact, &has);
+                for (e += blockDim.x; e < h0.y; e += blockDim.x)
+                    strain_window_edge(hot[e], e, edges, s_win, dt32, dt, &n_avg, &n_exact, &has);
+            }
+        }
+        asm volatile("cp.async.wait_group 0;\n" ::);
+        if (has) s_has[hs] = 1;
+        __syncthreads();
+        for (int i = wb_final.x + tid; i < wb_final.y; i += blockDim.x) {
+            int2 ps = wb_list[i];
+            double2 a = s_win[ps.y].a, b = s_win[ps.y].b;
+            av[ps.x] = make_double4_32a(a.x, a.y, b.x, 0.0);
+        }
+        if (tid == 0) s_has[hs ^ 1] = 0;
+        __syncthreads();
+        if (!s_has[hs]) break;
+    }
+    atomicAdd(&s_avg, n_avg);
+    atomicAdd(&s_exact, n_exact);
+    __syncthreads();
+    if (tid == 0) {
         passes_out[0] = passes;
         passes_out[1] = s_avg;
         passes_out[2] = s_exact;
@@ -516,16 +811,28 @@ void finalize_positions(const uint8_t* in_elem, const double4_32a* xo, double4_3
                                                  lo[2], hi[0], hi[1], hi[2]);
 }
 
-size_t strain_step_bytes(int nedges) { return sizeof(StrainEdgeStep) * (size_t)(nedges > 0 ? nedges : 1); }
+size_t strain_step_bytes(int nedges) {
+    size_t n = (size_t)(nedges > 0 ? nedges : 1);
+    return sizeof(StrainEdgeStep) * n + sizeof(StrainEdgeHot) * n;
+}
 
 void strain_limit(const StrainEdge* edges, int nedges, const int* level_off, int nlevels, const double4_32a* xo,
-                  double4_32a* av, double dt, void* step_buf, int* passes_out, cudaStream_t s) {
+                  double4_32a* av, int nv, double dt, void* step_buf, const StrainWindow* win, int* passes_out,
+                  cudaStream_t s) {
     if (nlevels <= 0) {
         cudaMemsetAsync(passes_out, 0, sizeof(int), s);
         return;
     }
     StrainEdgeStep* se = (StrainEdgeStep*)step_buf;
-    count_launch(), k_strain_setup<<<nblk(nedges, 256), 256, 0, s>>>(edges, nedges, xo, se);
+    StrainEdgeHot* hot = (StrainEdgeHot*)(se + nedges);
+    count_launch(), k_strain_setup<<<nblk(nedges, 256), 256, 0, s>>>(edges, nedges, xo, se, hot);
+    if (win && win->nslots > 0 && (size_t)win->nslots * sizeof(WinSlot) <= 200 * 1024) {
+        size_t smem = (size_t)win->nslots * sizeof(WinSlot);
+        cudaFuncSetAttribute(k_strain_window, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        count_launch(), k_strain_window<<<1, 256, smem, s>>>(se, hot, win->hdr, nlevels, win->load_list,
+                                                              win->wb_list, win->wb_final, av, dt, passes_out);
+        return;
+    }
     count_launch(), k_strain<<<1, 256, 0, s>>>(se, level_off, nlevels, xo, av, dt, passes_out);
 }
 

@@ -3,6 +3,7 @@
 // include/collision_gb300.h.
 #include <cstdio>
 #include <algorithm>
+#include <queue>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -98,6 +99,16 @@ struct cc_solver {
     double volume = 0.0;
     int* d_level_off = nullptr;
     int nlevels = 0;
+    int win_nslots = 0;
+    std::vector<int2> h_win_load, h_win_wb;
+    std::vector<int> h_win_load_off, h_win_wb_off;
+    std::vector<int4> h_win_hdr;
+    int2 h_win_wb_final{0, 0};
+    int4* d_win_hdr = nullptr;
+    int2* d_win_load = nullptr;
+    int* d_win_load_off = nullptr;
+    int2* d_win_wb = nullptr;
+    int* d_win_wb_off = nullptr;
     void* d_strain_step = nullptr;
     int* d_strain_passes = nullptr;
     std::vector<Box6> h_boxes;
@@ -151,6 +162,7 @@ struct cc_solver {
     }
     int zone_cap = 10000;
     int mode = 0;  // 0 plain FP64, 1 mixed precision
+    bool strain_window = true;
     float4* d_pbox_lo = nullptr;
     float4* d_pbox_hi = nullptr;
 
@@ -173,6 +185,8 @@ struct cc_solver {
         zone.sort_temp = nullptr;
         dfree(d_rank[0]); dfree(d_rank[1]);
         dfree(d_level_off); dfree(d_strain_passes); dfree(d_rec); dfree(d_pbox_lo); dfree(d_pbox_hi);
+        dfree(d_win_load); dfree(d_win_load_off); dfree(d_win_wb); dfree(d_win_wb_off); dfree(d_win_hdr);
+        win_nslots = 0;
         if (d_strain_step) cudaFree(d_strain_step);
         d_strain_step = nullptr;
         pair_cap = contrib_cap = rec_cap = 0;
@@ -278,9 +292,9 @@ cc_status cc_solver::assemble(const cc_mesh* m) {
         if (rigid) continue;  // isRigidBody(hse), dcollid.cpp:495
         if (np == 3) {
             for (int j = 0; j < 3; ++j)
-                edges.push_back(StrainEdge{ev[3 * e + j], ev[3 * e + (j + 1) % 3], m->tri_rest_len[3 * e + j]});
+                edges.push_back(StrainEdge{ev[3 * e + j], ev[3 * e + (j + 1) % 3], m->tri_rest_len[3 * e + j], 0, 0});
         } else {
-            edges.push_back(StrainEdge{ev[3 * e], ev[3 * e + 1], m->bond_rest_len[e - nt]});
+            edges.push_back(StrainEdge{ev[3 * e], ev[3 * e + 1], m->bond_rest_len[e - nt], 0, 0});
         }
     }
     nedges = (int)edges.size();
@@ -304,6 +318,66 @@ cc_status cc_solver::assemble(const cc_mesh* m) {
         for (int i = 0; i < nedges; ++i) sorted[cur[lvl[i] - 1]++] = edges[i];
     }
     edges.swap(sorted);
+    // shared-memory window of the sweep: each point lives in a slot from a few
+    // levels before its first edge to two levels after its last one
+    {
+        const int ahead = 8;  // kWindowAhead in cc_post.cu
+        std::vector<int> first((size_t)nv, -1), lastl((size_t)nv, -1);
+        for (int l = 0; l < nlevels; ++l)
+            for (int i = level_off[l]; i < level_off[l + 1]; ++i)
+                for (int p : {edges[i].p0, edges[i].p1}) {
+                    if (first[p] < 0) first[p] = l;
+                    lastl[p] = l;
+                }
+        std::vector<std::pair<int, int>> order;  // (load level, point)
+        for (int p = 0; p < nv; ++p)
+            if (first[p] >= 0) order.push_back({std::max(0, first[p] - ahead), p});
+        std::sort(order.begin(), order.end());
+        std::vector<int> slot((size_t)nv, -1);
+        std::priority_queue<std::pair<int, int>, std::vector<std::pair<int, int>>, std::greater<>> busy;  // (end, slot)
+        std::priority_queue<int, std::vector<int>, std::greater<>> freeq;
+        win_nslots = 0;
+        for (auto& lp : order) {
+            int start = lp.first, p = lp.second;
+            while (!busy.empty() && busy.top().first < start) {
+                freeq.push(busy.top().second);
+                busy.pop();
+            }
+            int sl;
+            if (!freeq.empty()) {
+                sl = freeq.top();
+                freeq.pop();
+            } else {
+                sl = win_nslots++;
+            }
+            slot[p] = sl;
+            busy.push({lastl[p] + 2, sl});
+        }
+        for (auto& ed : edges) {
+            ed.s0 = slot[ed.p0];
+            ed.s1 = slot[ed.p1];
+        }
+        std::vector<int> load_off((size_t)nlevels + 1, 0), wb_off((size_t)nlevels + 2, 0);
+        for (auto& lp : order) load_off[lp.first + 1]++;
+        for (int p = 0; p < nv; ++p)
+            if (first[p] >= 0) wb_off[lastl[p] + 2]++;  // written back at level last + 1
+        for (int l = 0; l < nlevels; ++l) load_off[l + 1] += load_off[l];
+        for (int l = 0; l <= nlevels; ++l) wb_off[l + 1] += wb_off[l];
+        h_win_load.assign(order.size(), int2{0, 0});
+        h_win_wb.assign(order.size(), int2{0, 0});
+        std::vector<int> lc(load_off.begin(), load_off.end()), wc(wb_off.begin(), wb_off.end());
+        for (auto& lp : order) h_win_load[lc[lp.first]++] = int2{lp.second, slot[lp.second]};
+        for (int p = 0; p < nv; ++p)
+            if (first[p] >= 0) h_win_wb[wc[lastl[p] + 1]++] = int2{p, slot[p]};
+        h_win_hdr.assign(2 * (size_t)nlevels, int4{0, 0, 0, 0});
+        for (int l = 0; l < nlevels; ++l) {
+            h_win_hdr[2 * l] = int4{level_off[l], level_off[l + 1], load_off[l], load_off[l + 1]};
+            h_win_hdr[2 * l + 1] = int4{wb_off[l], wb_off[l + 1], 0, 0};
+        }
+        h_win_wb_final = int2{wb_off[nlevels], wb_off[nlevels + 1]};
+        h_win_load_off.swap(load_off);
+        h_win_wb_off.swap(wb_off);
+    }
 
     bool ok = true;
     ok &= dalloc(&d_ev, (size_t)ne * 3) == cudaSuccess;
@@ -344,6 +418,11 @@ cc_status cc_solver::assemble(const cc_mesh* m) {
     ok &= dalloc(&d_rank[0], (size_t)ne) == cudaSuccess;
     ok &= dalloc(&d_rank[1], (size_t)ne) == cudaSuccess;
     ok &= dalloc(&d_level_off, (size_t)nlevels + 1) == cudaSuccess;
+    ok &= dalloc(&d_win_load, h_win_load.size()) == cudaSuccess;
+    ok &= dalloc(&d_win_load_off, h_win_load_off.size()) == cudaSuccess;
+    ok &= dalloc(&d_win_wb, h_win_wb.size()) == cudaSuccess;
+    ok &= dalloc(&d_win_wb_off, h_win_wb_off.size()) == cudaSuccess;
+    ok &= dalloc(&d_win_hdr, h_win_hdr.size()) == cudaSuccess;
     ok &= dalloc(&d_pbox_lo, (size_t)nv) == cudaSuccess;
     ok &= dalloc(&d_pbox_hi, (size_t)nv) == cudaSuccess;
     ok &= cudaMalloc(&d_strain_step, strain_step_bytes(nedges)) == cudaSuccess;
@@ -361,6 +440,15 @@ cc_status cc_solver::assemble(const cc_mesh* m) {
     if (nedges) {
         cudaMemcpyAsync(d_edges, edges.data(), sizeof(StrainEdge) * edges.size(), cudaMemcpyHostToDevice, stream);
         cudaMemcpyAsync(d_level_off, level_off.data(), sizeof(int) * ((size_t)nlevels + 1), cudaMemcpyHostToDevice,
+                        stream);
+        cudaMemcpyAsync(d_win_load, h_win_load.data(), sizeof(int2) * h_win_load.size(), cudaMemcpyHostToDevice,
+                        stream);
+        cudaMemcpyAsync(d_win_load_off, h_win_load_off.data(), sizeof(int) * h_win_load_off.size(),
+                        cudaMemcpyHostToDevice, stream);
+        cudaMemcpyAsync(d_win_wb, h_win_wb.data(), sizeof(int2) * h_win_wb.size(), cudaMemcpyHostToDevice, stream);
+        cudaMemcpyAsync(d_win_wb_off, h_win_wb_off.data(), sizeof(int) * h_win_wb_off.size(),
+                        cudaMemcpyHostToDevice, stream);
+        cudaMemcpyAsync(d_win_hdr, h_win_hdr.data(), sizeof(int4) * h_win_hdr.size(), cudaMemcpyHostToDevice,
                         stream);
     }
     cudaMemsetAsync(d_av, 0, sizeof(double4_32a) * (size_t)(nv > 0 ? nv : 1), stream);
@@ -542,7 +630,9 @@ cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, dou
     finalize_positions(d_in_elem, d_xo, d_av, d_hc, x_cand, x_out, nv, p, lo, hi, stream);
     prof(kStFinalize, false);
     prof(kStStrain, true);
-    strain_limit(d_edges, nedges, d_level_off, nlevels, d_xo, d_av, prm.dt, d_strain_step, d_strain_passes, stream);
+    StrainWindow win{win_nslots, d_win_load, d_win_load_off, d_win_wb, d_win_wb_off, d_win_hdr, h_win_wb_final};
+    strain_limit(d_edges, nedges, d_level_off, nlevels, d_xo, d_av, nv, prm.dt, d_strain_step,
+                 strain_window ? &win : nullptr, d_strain_passes, stream);
     prof(kStStrain, false);
     final_velocity(d_in_elem, d_hc, d_av, vel, nv, stream);
     if (hc != d_hc) cudaMemcpyAsync(hc, d_hc, (size_t)nv, cudaMemcpyDeviceToDevice, stream);
@@ -732,6 +822,12 @@ cc_status cc_set_stream(cc_solver* s, void* stream) {
         if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) return CC_CUDA_ERROR;
         s->own_stream = true;
     }
+    return CC_OK;
+}
+
+cc_status cc_set_strain_window(cc_solver* s, int on) {
+    if (!s) return CC_BAD_INPUT;
+    s->strain_window = on != 0;
     return CC_OK;
 }
 

@@ -147,6 +147,10 @@ class CollisionSolver3d:
         """0: plain FP64; 1: FP32 filters in front of the same FP64 tests."""
         self._check(self._lib.cc_set_mode(self._h, int(mode)))
 
+    def setStrainWindow(self, on: bool):
+        """Shared-memory window for the strain sweep (default) or global memory."""
+        self._check(self._lib.cc_set_strain_window(self._h, int(bool(on))))
+
     def setProfiling(self, on: bool):
         self._check(self._lib.cc_set_profiling(self._h, int(bool(on))))
 

@@ -124,6 +124,11 @@ cc_status cc_resolve_device(cc_solver* s, const double* x_old, const double* x_c
  *      results are the same as mode 0's. */
 cc_status cc_set_mode(cc_solver* s, int mode);
 
+/* Strain limiting keeps each point's velocity in shared memory while the
+ * sweep uses it (default, on); off runs the same sweep on global memory.
+ * Both give the same results. */
+cc_status cc_set_strain_window(cc_solver* s, int on);
+
 /* Counters of the last step, in this order: detection passes, CCD passes,
  * impact-zone passes, candidate pairs (all passes), narrow-phase visits,
  * pairs that hit, contacts (sub-tests that applied an impulse), strain

@@ -201,3 +201,24 @@ def test_mixed_precision_equals_plain(solver_cls, make):
         x, v, hc = a
     plain.close()
     mixed.close()
+
+
+def test_strain_sweeps_agree(solver_cls):
+    """The shared-memory window sweep and the global-memory sweep of the strain
+    limiter give the same velocities (both follow the reference's order)."""
+    sc = scenes.folded_cloth(n=33, dt=5e-4, h=2e-3, seed=1, vscale=20.0)
+    a, b = solver_cls(0), solver_cls(0)
+    for s, win in ((a, True), (b, False)):
+        s.assembleFromScene(sc)
+        s.setStrainWindow(win)
+    x, v, hc = sc.x.copy(), sc.v.copy(), np.zeros(sc.nv, np.uint8)
+    for step in range(6):
+        xc = scenes.candidate(sc, x, v)
+        ra = a.resolveCollision(x, xc, v, hc)
+        rb = b.resolveCollision(x, xc, v, hc)
+        for u, w in zip(ra, rb):
+            assert np.array_equal(u, w)
+        assert a.counters()["strain_averaged"] == b.counters()["strain_averaged"] > 0 or step == 0
+        x, v, hc = ra
+    a.close()
+    b.close()
