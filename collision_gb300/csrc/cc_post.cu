@@ -583,8 +583,111 @@ __device__ __forceinline__ void strain_window_edge(const StrainEdgeHot& h, int e
 // Everything a thread needs for a level arrives kRing levels early in a
 // register ring: the level's ranges, and the thread's first edge record,
 // copy-in entry and write-back entry. Entries beyond the first per thread
-// (levels wider than the block) are read when needed.
+// (levels wider than the block) are read when needed. The level loop is
+// unrolled by kWindowAhead (a multiple of kRing) so that every ring slot has
+// a fixed register name and nothing is shifted from level to level.
 constexpr int kRing = 4;
+
+struct WinRing {
+    int4 h0[kRing], h1[kRing];
+    StrainEdgeHot hot[kRing];
+    int2 ld[kRing], wb[kRing];
+    int lslot[kWindowAhead];  // slot this thread copied in, per recent level (-1: none)
+};
+
+__device__ __forceinline__ void win_fetch(WinRing& r, int j, int lk, int nlevels, int tid,
+                                          const int4* __restrict__ hdr, const StrainEdgeHot* __restrict__ hot,
+                                          const int2* __restrict__ load_list, const int2* __restrict__ wb_list) {
+    if (lk < nlevels) {
+        int4 a = hdr[2 * lk], b = hdr[2 * lk + 1];
+        r.h0[j] = a;
+        r.h1[j] = b;
+        if (a.x + tid < a.y) r.hot[j] = hot[a.x + tid];
+        if (a.z + tid < a.w) r.ld[j] = load_list[a.z + tid];
+        if (b.x + tid < b.y) r.wb[j] = wb_list[b.x + tid];
+    }
+}
+
+struct WinArgs {
+    const StrainEdgeStep* edges;
+    const StrainEdgeHot* hot;
+    const int4* hdr;
+    int nlevels;
+    const int2* load_list;
+    const int2* wb_list;
+    double4_32a* av;
+    double dt;
+    float dt32;
+};
+
+// One level of the window sweep; J = level mod kWindowAhead.
+template <int J>
+__device__ __forceinline__ void win_level(const WinArgs& A, WinRing& r, WinSlot* s_win, int l, int tid,
+                                          int* n_avg, int* n_exact, bool* has) {
+    constexpr int R = J % kRing;
+    const int4 h0 = r.h0[R], h1 = r.h1[R];
+    const StrainEdgeHot cur = r.hot[R];
+    const int2 ld = r.ld[R], wb = r.wb[R];
+    win_fetch(r, R, l + kRing, A.nlevels, tid, A.hdr, A.hot, A.load_list, A.wb_list);
+    // copy in the points whose slot opens now
+    int my_slot = -1;
+    if (h0.z + tid < h0.w) {
+        my_slot = ld.y;
+        cp_async16(&s_win[ld.y].a, &A.av[ld.x]);
+        cp_async16(&s_win[ld.y].b, reinterpret_cast<const double2*>(&A.av[ld.x]) + 1);
+        for (int i = h0.z + tid + (int)blockDim.x; i < h0.w; i += blockDim.x) {
+            int2 ps = A.load_list[i];
+            cp_async16(&s_win[ps.y].a, &A.av[ps.x]);
+            cp_async16(&s_win[ps.y].b, reinterpret_cast<const double2*>(&A.av[ps.x]) + 1);
+        }
+    }
+    asm volatile("cp.async.commit_group;\n" ::);
+    // FP32 copies of the points whose copy has now landed (each by the thread
+    // that issued it): all of level 0's at once, then those issued
+    // kWindowAhead levels ago, before their first edge
+    const int old_slot = r.lslot[J];
+    r.lslot[J] = my_slot;
+    int cl = -1, cslot = -1;
+    if (l == 0) {
+        asm volatile("cp.async.wait_group 0;\n" ::);
+        cl = 0;
+        cslot = my_slot;
+    } else if (l < kWindowAhead) {
+        asm volatile("cp.async.wait_group 0;\n" ::);
+    } else {
+        asm volatile("cp.async.wait_group %0;\n" ::"n"(kWindowAhead));
+        if (l - kWindowAhead >= 1) {
+            cl = l - kWindowAhead;
+            cslot = old_slot;
+        }
+    }
+    if (cl >= 0 && cslot >= 0) {
+        WinSlot& w = s_win[cslot];
+        w.f = make_float4((float)w.a.x, (float)w.a.y, (float)w.b.x, 0.f);
+        int4 hc = A.hdr[2 * cl];
+        for (int i = hc.z + tid + (int)blockDim.x; i < hc.w; i += blockDim.x) {
+            WinSlot& w2 = s_win[A.load_list[i].y];
+            w2.f = make_float4((float)w2.a.x, (float)w2.a.y, (float)w2.b.x, 0.f);
+        }
+    }
+    __syncthreads();
+    // write back the points last used at the previous level
+    if (h1.x + tid < h1.y) {
+        double2 a = s_win[wb.y].a, b = s_win[wb.y].b;
+        A.av[wb.x] = make_double4_32a(a.x, a.y, b.x, 0.0);
+        for (int i = h1.x + tid + (int)blockDim.x; i < h1.y; i += blockDim.x) {
+            int2 ps = A.wb_list[i];
+            double2 a2 = s_win[ps.y].a, b2 = s_win[ps.y].b;
+            A.av[ps.x] = make_double4_32a(a2.x, a2.y, b2.x, 0.0);
+        }
+    }
+    int e = h0.x + tid;
+    if (e < h0.y) {
+        strain_window_edge(cur, e, A.edges, s_win, A.dt32, A.dt, n_avg, n_exact, has);
+        for (e += blockDim.x; e < h0.y; e += blockDim.x)
+            strain_window_edge(A.hot[e], e, A.edges, s_win, A.dt32, A.dt, n_avg, n_exact, has);
+    }
+}
 
 __global__ void __launch_bounds__(256) k_strain_window(const StrainEdgeStep* __restrict__ edges,
                                                        const StrainEdgeHot* __restrict__ hot,
@@ -601,116 +704,26 @@ __global__ void __launch_bounds__(256) k_strain_window(const StrainEdgeStep* __r
     }
     __syncthreads();
     const int tid = threadIdx.x;
-    const float dt32 = __double2float_ru(dt);
+    WinArgs A{edges, hot, hdr, nlevels, load_list, wb_list, av, dt, __double2float_ru(dt)};
     int passes = 0, n_avg = 0, n_exact = 0;
     for (int pass = 0; pass < kStrainMaxIter; ++pass) {
         const int hs = pass & 1;
         passes++;
         bool has = false;
-        // hdr[2*l] = (edge begin, edge end, load begin, load end),
-        // hdr[2*l+1] = (write-back begin, write-back end, -, -)
-        int4 rh0[kRing], rh1[kRing];
-        StrainEdgeHot rhot[kRing];
-        int2 rld[kRing], rwb[kRing];
-        int lslot[kWindowAhead];  // slot this thread copied in, per recent level (-1: none)
+        WinRing r;
 #pragma unroll
-        for (int j = 0; j < kWindowAhead; ++j) lslot[j] = -1;
+        for (int j = 0; j < kWindowAhead; ++j) r.lslot[j] = -1;
 #pragma unroll
-        for (int j = 0; j < kRing; ++j) {
-            if (j < nlevels) {
-                rh0[j] = hdr[2 * j];
-                rh1[j] = hdr[2 * j + 1];
-                if (rh0[j].x + tid < rh0[j].y) rhot[j] = hot[rh0[j].x + tid];
-                if (rh0[j].z + tid < rh0[j].w) rld[j] = load_list[rh0[j].z + tid];
-                if (rh1[j].x + tid < rh1[j].y) rwb[j] = wb_list[rh1[j].x + tid];
-            }
-        }
-        for (int l = 0; l < nlevels; ++l) {
-            const int4 h0 = rh0[0], h1 = rh1[0];
-            const StrainEdgeHot cur = rhot[0];
-            const int2 ld = rld[0], wb = rwb[0];
-#pragma unroll
-            for (int j = 0; j + 1 < kRing; ++j) {
-                rh0[j] = rh0[j + 1];
-                rh1[j] = rh1[j + 1];
-                rhot[j] = rhot[j + 1];
-                rld[j] = rld[j + 1];
-                rwb[j] = rwb[j + 1];
-            }
-            {
-                const int lk = l + kRing;
-                if (lk < nlevels) {
-                    int4 a = hdr[2 * lk], b = hdr[2 * lk + 1];
-                    rh0[kRing - 1] = a;
-                    rh1[kRing - 1] = b;
-                    if (a.x + tid < a.y) rhot[kRing - 1] = hot[a.x + tid];
-                    if (a.z + tid < a.w) rld[kRing - 1] = load_list[a.z + tid];
-                    if (b.x + tid < b.y) rwb[kRing - 1] = wb_list[b.x + tid];
-                }
-            }
-            // copy in the points whose slot opens now
-            int my_slot = -1;
-            if (h0.z + tid < h0.w) {
-                my_slot = ld.y;
-                cp_async16(&s_win[ld.y].a, &av[ld.x]);
-                cp_async16(&s_win[ld.y].b, reinterpret_cast<const double2*>(&av[ld.x]) + 1);
-                for (int i = h0.z + tid + (int)blockDim.x; i < h0.w; i += blockDim.x) {
-                    int2 ps = load_list[i];
-                    cp_async16(&s_win[ps.y].a, &av[ps.x]);
-                    cp_async16(&s_win[ps.y].b, reinterpret_cast<const double2*>(&av[ps.x]) + 1);
-                }
-            }
-            asm volatile("cp.async.commit_group;\n" ::);
-            // FP32 copies of the points whose copy has now landed (each by the
-            // thread that issued it): all of level 0's at once, then those
-            // issued kWindowAhead levels ago, before their first edge
-            const int old_slot = lslot[0];
-#pragma unroll
-            for (int j = 0; j + 1 < kWindowAhead; ++j) lslot[j] = lslot[j + 1];
-            lslot[kWindowAhead - 1] = my_slot;
-            int cl = -1, cslot = -1;
-            if (l == 0) {
-                asm volatile("cp.async.wait_group 0;\n" ::);
-                cl = 0;
-                cslot = my_slot;
-            } else if (l < kWindowAhead) {
-                asm volatile("cp.async.wait_group 0;\n" ::);
-            } else {
-                asm volatile("cp.async.wait_group %0;\n" ::"n"(kWindowAhead));
-                if (l - kWindowAhead >= 1) {
-                    cl = l - kWindowAhead;
-                    cslot = old_slot;
-                }
-            }
-            if (cl >= 0) {
-                if (cslot >= 0) {
-                    WinSlot& w = s_win[cslot];
-                    w.f = make_float4((float)w.a.x, (float)w.a.y, (float)w.b.x, 0.f);
-                    // further entries of that level (wider than the block)
-                    int4 hc = hdr[2 * cl];
-                    for (int i = hc.z + tid + (int)blockDim.x; i < hc.w; i += blockDim.x) {
-                        WinSlot& w2 = s_win[load_list[i].y];
-                        w2.f = make_float4((float)w2.a.x, (float)w2.a.y, (float)w2.b.x, 0.f);
-                    }
-                }
-            }
-            __syncthreads();
-            // write back the points last used at the previous level
-            if (h1.x + tid < h1.y) {
-                double2 a = s_win[wb.y].a, b = s_win[wb.y].b;
-                av[wb.x] = make_double4_32a(a.x, a.y, b.x, 0.0);
-                for (int i = h1.x + tid + (int)blockDim.x; i < h1.y; i += blockDim.x) {
-                    int2 ps = wb_list[i];
-                    double2 a2 = s_win[ps.y].a, b2 = s_win[ps.y].b;
-                    av[ps.x] = make_double4_32a(a2.x, a2.y, b2.x, 0.0);
-                }
-            }
-            int e = h0.x + tid;
-            if (e < h0.y) {
-                strain_window_edge(cur, e, edges, s_win, dt32, dt, &n_avg, &n_exact, &has);
-                for (e += blockDim.x; e < h0.y; e += blockDim.x)
-                    strain_window_edge(hot[e], e, edges, s_win, dt32, dt, &n_avg, &n_exact, &has);
-            }
+        for (int j = 0; j < kRing; ++j) win_fetch(r, j, j, nlevels, tid, hdr, hot, load_list, wb_list);
+        for (int lb = 0; lb < nlevels; lb += kWindowAhead) {
+            win_level<0>(A, r, s_win, lb + 0, tid, &n_avg, &n_exact, &has);
+            if (lb + 1 < nlevels) win_level<1>(A, r, s_win, lb + 1, tid, &n_avg, &n_exact, &has);
+            if (lb + 2 < nlevels) win_level<2>(A, r, s_win, lb + 2, tid, &n_avg, &n_exact, &has);
+            if (lb + 3 < nlevels) win_level<3>(A, r, s_win, lb + 3, tid, &n_avg, &n_exact, &has);
+            if (lb + 4 < nlevels) win_level<4>(A, r, s_win, lb + 4, tid, &n_avg, &n_exact, &has);
+            if (lb + 5 < nlevels) win_level<5>(A, r, s_win, lb + 5, tid, &n_avg, &n_exact, &has);
+            if (lb + 6 < nlevels) win_level<6>(A, r, s_win, lb + 6, tid, &n_avg, &n_exact, &has);
+            if (lb + 7 < nlevels) win_level<7>(A, r, s_win, lb + 7, tid, &n_avg, &n_exact, &has);
         }
         asm volatile("cp.async.wait_group 0;\n" ::);
         if (has) s_has[hs] = 1;

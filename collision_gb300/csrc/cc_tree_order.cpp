@@ -23,6 +23,7 @@ double RefTreeOrder::build(const Box6* leaf_boxes, int n) {
             L.hi[d] = leaf_boxes[e].hi[d];
         }
         L.left = L.right = -1;
+        L.vol = box_volume(L.lo, L.hi);
     }
     int next = n;
     root_ = n > 0 ? 0 : -1;
@@ -34,6 +35,15 @@ double RefTreeOrder::build(const Box6* leaf_boxes, int n) {
         while (nodes_[p].left >= 0) {
             const Node& l = nodes_[nodes_[p].left];
             const Node& r = nodes_[nodes_[p].right];
+            // the next level's nodes, whichever way this one goes
+            if (l.left >= 0) {
+                __builtin_prefetch(&nodes_[l.left]);
+                __builtin_prefetch(&nodes_[l.right]);
+            }
+            if (r.left >= 0) {
+                __builtin_prefetch(&nodes_[r.left]);
+                __builtin_prefetch(&nodes_[r.right]);
+            }
             double ml[3], Ml[3], mr[3], Mr[3];
             for (int d = 0; d < 3; ++d) {
                 ml[d] = mn(l.lo[d], nb.lo[d]);
@@ -41,8 +51,8 @@ double RefTreeOrder::build(const Box6* leaf_boxes, int n) {
                 mr[d] = mn(r.lo[d], nb.lo[d]);
                 Mr[d] = mx(r.hi[d], nb.hi[d]);
             }
-            double vdiff1 = box_volume(ml, Ml) - box_volume(l.lo, l.hi);
-            double vdiff2 = box_volume(mr, Mr) - box_volume(r.lo, r.hi);
+            double vdiff1 = box_volume(ml, Ml) - l.vol;
+            double vdiff2 = box_volume(mr, Mr) - r.vol;
             path_[depth++] = p;
             if (vdiff1 < vdiff2) {
                 slot = &nodes_[p].left;
@@ -60,6 +70,7 @@ double RefTreeOrder::build(const Box6* leaf_boxes, int n) {
             np.lo[d] = mn(nodes_[e].lo[d], nodes_[p].lo[d]);
             np.hi[d] = mx(nodes_[e].hi[d], nodes_[p].hi[d]);
         }
+        np.vol = box_volume(np.lo, np.hi);
         *slot = q;
         while (depth > 0) {
             Node& a = nodes_[path_[--depth]];
@@ -69,6 +80,7 @@ double RefTreeOrder::build(const Box6* leaf_boxes, int n) {
                 a.lo[d] = mn(l.lo[d], r.lo[d]);
                 a.hi[d] = mx(l.hi[d], r.hi[d]);
             }
+            a.vol = box_volume(a.lo, a.hi);
         }
     }
     built_ = n > 0;

@@ -31,6 +31,7 @@ public:
 private:
     struct Node {
         double lo[3], hi[3];
+        double vol;  // AABB::volume of the box, kept with it
         int left, right;
     };
     std::vector<Node> nodes_;
