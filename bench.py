@@ -1,23 +1,33 @@
 """Benchmark of the GB300 collision-handling step.
 
-Workload: the self-collision scene - one 129x129-vertex cloth (32,768
-triangles), sinusoidal start, velocity -2*grad(phi) of a seeded field,
-dt = h = 5e-4 - resolved step by step as the reference's host loop does
-(x_cand = x_old + dt*vel, then resolveCollision). A step is one
-resolveCollision() on the current state; the trajectory continues across
-warm-up and timed steps. Metric: collision-resolved scene-steps per second.
+Default workload (`batched`): 256 independent cloth-on-obstacle scenes -
+sheet resolution 16..128 vertices per side, a fixed sphere (642 points,
+r ~ U(0.1, 0.3)) or box (12 triangles) by coin flip, v = (0,0,-U(0.5,3))
++-1 %, dt = h = 1e-3 - all seeded, synthetic. One step = one
+resolveCollision() of every scene on its current state, as the reference's
+host loop does (x_cand = x_old + dt*vel, then resolve); the trajectory runs
+on across warm-up and timed steps. Metric: collision-resolved scene-steps
+per second.
 
-  value  device-resident: inputs in HBM, each step through cc_resolve_device
-  e2e    the same steps through cc_resolve with pinned host buffers, copies
-         inside the timed region
-  L2     flushed (256 MiB write) before every timed step; the working set
-         (~8 MB) would otherwise stay in the 129 MB L2
+  value       mixed precision, batched: all scenes in one solver, inputs in
+              HBM, each step through cc_resolve_batch_device
+  plain_fp64  the plain FP64 GPU path one scene at a time (one solver per
+              scene, cc_resolve_device on each) over the first steps of the
+              same trajectory; its final state must equal the batch's bit
+              for bit
+  e2e         the batched mixed path through cc_resolve_batch with pinned
+              host buffers, copies inside the timed region
+  missed_ccd  element pairs that still collide after a step, by the exact
+              FP64 CCD re-check (cc_check_ccd) after every timed step,
+              outside the timed region
+  L2          flushed (256 MiB write) before every timed step
 
---impl reference times the CPU implementation of the same path (the C
-restatement of the reference in oracle/, which is bit-exact to it; the
-reference's own sources are not available on the GPU host) on the host
-cores. Under torchrun every rank runs an independent replica (different
-seed): the path does not shard.
+--workload picks one of the other measured scenes (folded_cloth,
+cloth_on_sphere, strings, large) as a batch of one. --impl reference times
+the CPU implementation of the same path (the C restatement of the reference
+in oracle/, which is bit-exact to it; the reference's own sources are not on
+the GPU host) on all host cores, one scene per thread. Under torchrun every
+rank runs an independent replica (different seed).
 """
 from __future__ import annotations
 
@@ -28,6 +38,7 @@ import subprocess
 import sys
 import threading
 import time
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
@@ -36,13 +47,25 @@ sys.path.insert(0, ROOT)
 
 METRIC = "cloth collision steps/s: mixed-prec batched vs FP64 plain, 0 missed CCD"
 UNIT = "scene-steps/s"
-WORKLOAD = "folded_cloth"
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+NARROW_BYTES_PER_VISIT = 8 + 8 + 24 + 6 * 64  # pair, two leaf ranks, two elements' ids, x_old+avgVel of 6 points
 
 
-def make_scene(seed):
+def make_workload(name, seed):
     from collision_gb300 import scenes
-    return scenes.folded_cloth(seed=seed)
+    return scenes.workload(name, seed=seed)
+
+
+def describe(name, scs):
+    nv = sum(s.nv for s in scs)
+    nt = sum(s.nt for s in scs)
+    nb = sum(s.nb for s in scs)
+    d = {"workload": name, "scenes": len(scs), "points": nv, "tris": nt, "bonds": nb,
+         "dt": sorted({s.params["dt"] for s in scs}), "h": sorted({s.params["thickness"] for s in scs})}
+    if name == "batched":
+        d["sheet_sides"] = [16, 128]
+        d["obstacles"] = {"sphere": sum("sphere" in s.name for s in scs), "box": sum("box" in s.name for s in scs)}
+    return d
 
 
 def dist_env():
@@ -58,7 +81,6 @@ class Clocks:
     def __init__(self, device):
         self.device = device
         self.samples = []
-        self._stop = threading.Event()
         self._proc = None
 
     def __enter__(self):
@@ -99,227 +121,290 @@ class Clocks:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def cpu_oracle_rate(seed, budget_s, max_steps):
-    """Steps/s of the single-threaded CPU restatement on this workload, from
-    the start of the trajectory, within a time budget."""
+# ------------------------------------------------------------- CPU (oracle)
+def oracle_rate(scs, max_steps, budget_s, threads, skip_steps=0):
+    """Scene-steps/s of the CPU restatement over the trajectory, all scenes
+    stepped together (one scene per thread, `threads` at once); the first
+    `skip_steps` steps are run untimed. Stops after max_steps timed steps or
+    once budget_s of timed steps has passed. Returns (rate, scene-steps,
+    seconds, steps)."""
     from collision_gb300 import scenes
     from oracle.ccopy import OracleSolver
-    sc = make_scene(seed)
-    o = OracleSolver(sc, record=0)
-    x, v, hc = sc.x.copy(), sc.v.copy(), np.zeros(sc.nv, np.uint8)
-    n, t_total = 0, 0.0
-    while n < max_steps and t_total < budget_s:
-        xc = scenes.candidate(sc, x, v)
-        t0 = time.perf_counter()
-        r = o.step(x, xc, v, hc)
-        t_total += time.perf_counter() - t0
+    solvers = [OracleSolver(sc, record=0) for sc in scs]
+    state = [(sc.x.copy(), sc.v.copy(), np.zeros(sc.nv, np.uint8)) for sc in scs]
+
+    def one(i):
+        x, v, hc = state[i]
+        r = solvers[i].step(x, scenes.candidate(scs[i], x, v), v, hc)
         if r["rc"] != 0:
-            raise RuntimeError(f"oracle step failed: {r['rc']}")
-        x, v, hc = r["x"], r["v"], r["has_collsn"]
-        n += 1
-    return n / t_total, n, t_total
+            raise RuntimeError(f"oracle step failed on scene {i}: {r['rc']}")
+        state[i] = (r["x"], r["v"], r["has_collsn"])
+
+    done, t_total, steps = 0, 0.0, 0
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        for _ in range(skip_steps):
+            list(ex.map(one, range(len(scs))))
+        while steps < max_steps and t_total < budget_s:
+            t0 = time.perf_counter()
+            list(ex.map(one, range(len(scs))))
+            t_total += time.perf_counter() - t0
+            done += len(scs)
+            steps += 1
+    return done / t_total, done, t_total, steps
 
 
 def run_reference(args):
     ws, rk, _ = dist_env()
     if rk != 0:
         return
-    # warm-up steps are part of the trajectory, untimed
-    from collision_gb300 import scenes
-    from oracle.ccopy import OracleSolver
-    sc = make_scene(args.seed)
-    o = OracleSolver(sc, record=0)
-    x, v, hc = sc.x.copy(), sc.v.copy(), np.zeros(sc.nv, np.uint8)
-    times = []
-    for step in range(args.warmup + args.steps):
-        xc = scenes.candidate(sc, x, v)
-        t0 = time.perf_counter()
-        r = o.step(x, xc, v, hc)
-        dt = time.perf_counter() - t0
-        if step >= args.warmup:
-            times.append(dt)
-        x, v, hc = r["x"], r["v"], r["has_collsn"]
-    total = sum(times)
-    value = len(times) / total
-    sample = f"{WORKLOAD} 129x129, steps {args.warmup}..{args.warmup + args.steps - 1} of the trajectory"
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times), "higher_is_better": True,
+    scs = make_workload(args.workload, args.seed)
+    threads = os.cpu_count() or 1
+    rate, n, t, steps = oracle_rate(scs, args.steps, args.ref_budget, threads, skip_steps=args.warmup)
+    sample = (f"{args.workload}: {len(scs)} scenes, steps {args.warmup}..{args.warmup + steps - 1} of the "
+              f"trajectory ({n} scene-steps, {t:.1f} s), one scene per thread")
+    line = {"metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": ws, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t / max(steps, 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "grid": "129x129", "tris": 32768, "dt": 5e-4, "h": 5e-4,
-                       "parallelism": "replicas"},
+            "config": dict(describe(args.workload, scs), parallelism="replicas"),
             "impl": "reference",
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
-            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------- GPU
 def run_gpu(args):
     import torch
     ws, rk, lrk = dist_env()
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    dev = lrk if torch.cuda.is_available() else 0
+    dev = lrk
     torch.cuda.set_device(dev)
-    from collision_gb300 import scenes
-    from collision_gb300._lib import load
     from collision_gb300.solver import CollisionSolver3d
-    lib = load()
     seed = args.seed + rk
-    sc = make_scene(seed)
-    dt = sc.params["dt"]
+    scs = make_workload(args.workload, seed)
+    nsc = len(scs)
     stream = torch.cuda.Stream(device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    x0 = np.concatenate([s.x for s in scs])
+    v0 = np.concatenate([s.v for s in scs])
+    dtcol = np.concatenate([np.full((s.nv, 1), s.params["dt"]) for s in scs])
+    offs = np.cumsum([0] + [s.nv for s in scs])
+    W, K = args.warmup, args.steps
+    n_plain = min(K, args.plain_steps)
 
-    # ---------------------------------------------- device-resident runs
-    def device_run(mode):
-        """W untimed + K timed steps from the scene's start, each step
-        through cc_resolve_device; returns total timed ms and the counters."""
-        s = CollisionSolver3d(dev)
-        s.assembleFromScene(sc)
-        s.setMode(mode)
-        s.setStream(stream.cuda_stream)
+    def device_state():
         with torch.cuda.stream(stream):
-            x = torch.tensor(sc.x, dtype=torch.float64, device=dev)
-            v = torch.tensor(sc.v, dtype=torch.float64, device=dev)
-            hc = torch.zeros(sc.nv, dtype=torch.uint8, device=dev)
-            xc = torch.empty_like(x)
-            xo = torch.empty_like(x)
-        launches, counters = [], []
-        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-               for _ in range(args.steps)]
-        with torch.cuda.stream(stream):
-            for _ in range(args.warmup):
-                torch.add(x, v, alpha=dt, out=xc)
-                s.resolveCollisionDevice(x, xc, v, hc, xo)
-                x, xo = xo, x
+            st = dict(x=torch.tensor(x0, device=dev), v=torch.tensor(v0, device=dev),
+                      dt=torch.tensor(dtcol, device=dev), hc=torch.zeros(len(x0), dtype=torch.uint8, device=dev))
+            st["xc"] = torch.empty_like(st["x"])
+            st["xo"] = torch.empty_like(st["x"])
+            st["tmp"] = torch.empty_like(st["x"])
+        return st
+
+    def candidate(st):
+        # x_cand = x_old + dt*vel, two roundings as the reference's host loop
+        torch.mul(st["v"], st["dt"], out=st["tmp"])
+        torch.add(st["x"], st["tmp"], out=st["xc"])
+
+    def sync_all():
         stream.synchronize()
         if ws > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
+
+    def max_over_ranks(ms):
+        if ws == 1:
+            return ms
+        t = torch.tensor([ms], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    # ------------------------------------------- batched, device-resident
+    def batched_run(mode, check):
+        s = CollisionSolver3d(dev)
+        s.assembleBatch(scs)
+        s.setMode(mode)
+        s.setStream(stream.cuda_stream)
+        st = device_state()
+        with torch.cuda.stream(stream):
+            for _ in range(W):
+                candidate(st)
+                s.resolveCollisionBatchDevice(st["x"], st["xc"], st["v"], st["hc"], st["xo"])
+                st["x"], st["xo"] = st["xo"], st["x"]
+        sync_all()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+        counters, missed, snap = [], 0, None
         s.setProfiling(True)
         with Clocks(dev) as clk, torch.cuda.stream(stream):
-            for k in range(args.steps):
+            for k in range(K):
                 flush.fill_(float(k))
                 evs[k][0].record(stream)
-                torch.add(x, v, alpha=dt, out=xc)
-                s.resolveCollisionDevice(x, xc, v, hc, xo)
+                candidate(st)
+                s.resolveCollisionBatchDevice(st["x"], st["xc"], st["v"], st["hc"], st["xo"])
                 evs[k][1].record(stream)
-                c = s.counters()
-                counters.append(c)
-                launches.append(c["kernel_launches"] + 1)  # + the candidate update
-                x, xo = xo, x
+                counters.append(s.counters())
+                if check:
+                    hits, _ = s.checkCCD(st["x"], st["xo"])
+                    missed += hits
+                st["x"], st["xo"] = st["xo"], st["x"]
+                if k + 1 == n_plain:
+                    snap = (st["x"].cpu().numpy(), st["v"].cpu().numpy())
             stream.synchronize()
         torch.cuda.synchronize()
         step_ms = [a.elapsed_time(b) for a, b in evs]
         prof = s.profile()
         s.close()
-        total_ms = float(sum(step_ms))
-        if ws > 1:
-            t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            total_ms = float(t.item())
-            torch.distributed.barrier()
-        return total_ms, step_ms, counters, launches, prof, clk.summary()
+        return dict(total_ms=max_over_ranks(float(sum(step_ms))), step_ms=step_ms, counters=counters,
+                    missed=missed, snap=snap, prof=prof, clocks=clk.summary())
 
-    plain_ms, plain_steps, plain_ctr, _, plain_prof, _ = device_run(0)
-    total_ms, step_ms, counters, launches, prof, clocks = device_run(1)
-    value = ws * args.steps / (total_ms / 1e3)
-    plain_value = ws * args.steps / (plain_ms / 1e3)
+    mixed = batched_run(1, check=not args.no_check)
+    batch_plain = batched_run(0, check=False)
 
-    # ------------------------------------------------------ end-to-end run
+    # ------------------------------ plain FP64, one scene at a time
+    solvers = []
+    for sc in scs:
+        s = CollisionSolver3d(dev)
+        s.assembleFromScene(sc)
+        s.setMode(0)
+        s.setStream(stream.cuda_stream)
+        solvers.append(s)
+    st = device_state()
+
+    def seq_step():
+        candidate(st)
+        for i, s in enumerate(solvers):
+            a, b = int(offs[i]), int(offs[i + 1])
+            s.resolveCollisionDevice(st["x"][a:b], st["xc"][a:b], st["v"][a:b], st["hc"][a:b], st["xo"][a:b])
+        st["x"], st["xo"] = st["xo"], st["x"]
+
+    with torch.cuda.stream(stream):
+        for _ in range(W):
+            seq_step()
+    sync_all()
+    seq_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n_plain)]
+    seq_launches = 0
+    with torch.cuda.stream(stream):
+        for k in range(n_plain):
+            flush.fill_(float(k))
+            seq_ev[k][0].record(stream)
+            seq_step()
+            seq_ev[k][1].record(stream)
+            seq_launches += 2 + sum(s.counters()["kernel_launches"] for s in solvers)
+        stream.synchronize()
+    seq_ms = max_over_ranks(float(sum(a.elapsed_time(b) for a, b in seq_ev)))
+    seq_snap = (st["x"].cpu().numpy(), st["v"].cpu().numpy())
+    for s in solvers:
+        s.close()
+    del solvers
+    same = bool(np.array_equal(mixed["snap"][0], seq_snap[0]) and np.array_equal(mixed["snap"][1], seq_snap[1]))
+    diff = float(np.abs(mixed["snap"][0] - seq_snap[0]).max())
+
+    # ------------------------------------------------ end to end (host)
     s2 = CollisionSolver3d(dev)
-    s2.assembleFromScene(sc)
+    s2.assembleBatch(scs)
     s2.setMode(1)
     s2.setStream(stream.cuda_stream)
-    pin = lambda a, dtp: torch.tensor(a, dtype=dtp).pin_memory()
-    hx = pin(sc.x, torch.float64)
-    hv = pin(sc.v, torch.float64)
-    hhc = torch.zeros(sc.nv, dtype=torch.uint8).pin_memory()
-    hxc = torch.empty_like(hx).pin_memory()
-    hxo = torch.empty_like(hx).pin_memory()
+    pin = lambda a: torch.tensor(a).pin_memory()
+    hx, hv, hdt = pin(x0), pin(v0), pin(dtcol)
+    hhc = torch.zeros(len(x0), dtype=torch.uint8).pin_memory()
+    hxc, hxo = torch.empty_like(hx).pin_memory(), torch.empty_like(hx).pin_memory()
+    hcol = np.zeros(nsc, dtype=np.int32)
     import ctypes as C
-    hcol = C.c_int(0)
+    lib = s2._lib
 
-    def e2e_step():
-        torch.add(hx, hv, alpha=dt, out=hxc)
-        st = lib.cc_resolve(s2._h, hx.data_ptr(), hxc.data_ptr(), hv.data_ptr(), hhc.data_ptr(), hxo.data_ptr(),
-                            C.byref(hcol))
-        if st != 0:
-            s2._check(st)
+    def e2e_call():
+        rc = lib.cc_resolve_batch(s2._h, hx.data_ptr(), hxc.data_ptr(), hv.data_ptr(), hhc.data_ptr(),
+                                  hxo.data_ptr(), hcol.ctypes.data_as(C.POINTER(C.c_int)))
+        if rc != 0:
+            s2._check(rc)
+
+    def host_candidate():
+        np.add(hx.numpy(), hdt.numpy() * hv.numpy(), out=hxc.numpy())
+
+    for _ in range(W):
+        host_candidate()
+        e2e_call()
         hx.copy_(hxo)
-
-    for _ in range(args.warmup):
-        e2e_step()
-    e2e_ms = []
-    ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
     with torch.cuda.stream(stream):
-        for k in range(args.steps):
+        for k in range(K):
+            host_candidate()
             flush.fill_(float(k))
             stream.synchronize()
             ev2[k][0].record(stream)
-            e2e_step()
+            e2e_call()
             ev2[k][1].record(stream)
+            hx.copy_(hxo)
         stream.synchronize()
-    e2e_total = sum(a.elapsed_time(b) for a, b in ev2)
-    if ws > 1:
-        t = torch.tensor([e2e_total], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e_value = ws * args.steps / (e2e_total / 1e3)
-    h2d = sc.nv * (3 * 8 * 3 + 1)
-    d2h = sc.nv * (3 * 8 * 2 + 1)
+    e2e_ms = max_over_ranks(float(sum(a.elapsed_time(b) for a, b in ev2)))
+    s2.close()
+    nv = len(x0)
+    h2d = nv * (3 * 8 * 3 + 1)   # x_old, x_cand, vel, has_collsn
+    d2h = nv * (3 * 8 * 2 + 1) + 4 * nsc  # x_out, vel, has_collsn, has_collision
 
     if rk != 0:
         if ws > 1:
             torch.distributed.destroy_process_group()
         return
 
+    value = ws * K * nsc / (mixed["total_ms"] / 1e3)
+    plain_value = ws * n_plain * nsc / (seq_ms / 1e3)
+    batch_plain_value = ws * K * nsc / (batch_plain["total_ms"] / 1e3)
+    e2e_value = ws * K * nsc / (e2e_ms / 1e3)
+
     # ----------------------------------------------------------- roofline
     peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
     hbm = peaks.get("hbm_gbs")
     peak_src = "measured" if hbm else "fallback"
     hbm = hbm or 6800.0
-    tot = {k: sum(c[k] for c in counters) for k in counters[0]} if counters else {}
-    ptot = {k: sum(c[k] for c in plain_ctr) for k in plain_ctr[0]} if plain_ctr else {}
-    # dominant kernel: the CCD narrow phase. Algorithmic bytes per visited
-    # pair: the pair (8 B), both leaf ranks (8 B), both elements' point ids
-    # (24 B) and the x_old + avgVel records of its up to 6 points (6 x 64 B);
-    # plus 64 B per contribution written.
-    narrow_ms, narrow_calls = plain_prof.get("narrow_ccd", (0.0, 0))
-    ccd_visits = ptot.get("visits", 0)  # all passes; CCD share estimated below
-    bytes_per_visit = 8 + 8 + 24 + 6 * 64
+    tot = {k: sum(c[k] for c in mixed["counters"]) for k in mixed["counters"][0]}
+    prof = mixed["prof"]
+    kern = {}
+    ms, calls = prof.get("narrow_ccd", (0.0, 0))
+    if calls:
+        per = NARROW_BYTES_PER_VISIT * tot["moving_visits"] / calls
+        kern["narrow_ccd"] = {"kernel": "k_narrow<true> (CCD narrow phase)", "bytes_per_launch": per,
+                              "ms_per_launch": ms / calls, "achieved": per / (ms / calls / 1e3) / 1e9}
+    ms, calls = prof.get("strain", (0.0, 0))
+    if calls:
+        per = tot["strain_bytes"] / calls
+        kern["strain"] = {"kernel": "k_strain_window (strain sweep, one CTA per scene)", "bytes_per_launch": per,
+                          "ms_per_launch": ms / calls, "achieved": per / (ms / calls / 1e3) / 1e9}
     roof = None
-    if narrow_calls:
-        # visits of CCD passes: total visits minus proximity visits (one
-        # proximity pass per step visits about as many pairs as one CCD pass)
-        passes = max(ptot.get("passes", 1), 1)
-        ccd_share = (passes - args.steps) / passes
-        algo = bytes_per_visit * ccd_visits * ccd_share / narrow_calls
-        avg_s = narrow_ms / narrow_calls / 1e3
-        achieved = algo / avg_s / 1e9
-        roof = {"bound": "hbm", "kernel": "k_narrow<true> (CCD narrow phase, plain FP64)", "achieved": achieved,
-                "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_src,
-                "traffic": None, "note": "FP64-ALU bound: FP64 is ~1.25 TFLOP/s nominal on GB300"}
+    if kern:
+        top = max(kern, key=lambda k: prof[k][0])
+        kt = kern[top]
+        roof = {"bound": "hbm", "kernel": kt["kernel"], "achieved": kt["achieved"], "peak": hbm, "unit": "GB/s",
+                "frac": kt["achieved"] / hbm, "peak_source": peak_src, "traffic": None,
+                "note": "dependency-chain / FP64 bound, not bandwidth bound", "kernels": kern}
     cpu = None
     if not args.no_cpu_baseline:
-        rate, n, t = cpu_oracle_rate(seed, args.cpu_budget, args.warmup + args.steps)
-        cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"{WORKLOAD} 129x129, first {n} steps of the trajectory ({t:.1f} s)"}
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64 (f32 filters)", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "grid": "129x129", "tris": 32768, "dt": 5e-4, "h": 5e-4,
-                       "path": "mixed: FP32 sub-test filters, FP64 tests (results identical to plain FP64)",
-                       "l2": "flushed before every timed step",
-                       "parallelism": "replicas" if ws > 1 else "single"},
-            "plain_fp64": {"value": plain_value, "ms_per_step": plain_ms / args.steps,
-                           "fp64_subtests": int(sum(c.get("fp64_subtests", 0) for c in plain_ctr)),
-                           "stages_ms": {k: round(v[0], 3) for k, v in plain_prof.items()}},
-            "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
+        threads = os.cpu_count() or 1
+        rate, n, t, steps = oracle_rate(scs, W + K, args.cpu_budget, threads)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{args.workload}: {nsc} scenes, first {steps} steps of the trajectory "
+                         f"({n} scene-steps, {t:.1f} s), one scene per thread"}
+    launches = sum(c["kernel_launches"] + 2 for c in mixed["counters"])
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
+            "ms_per_step": mixed["total_ms"] / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 (f32 filters)", "data": "synthetic",
+            "config": dict(describe(args.workload, scs),
+                           path="mixed precision, batched: FP32 sub-test filters in front of unchanged FP64 "
+                                "tests, all scenes per launch",
+                           l2="flushed before every timed step",
+                           parallelism="replicas" if ws > 1 else "single"),
+            "plain_fp64": {"value": plain_value, "steps": n_plain, "ms_per_step": seq_ms / n_plain,
+                           "path": "plain FP64, one scene per call", "gpu_launches": seq_launches,
+                           "state_equal_after_steps": same, "max_abs_diff": diff},
+            "speedup_vs_plain": value / plain_value,
+            "batched_plain_fp64": {"value": batch_plain_value, "ms_per_step": batch_plain["total_ms"] / K},
+            "missed_ccd": None if args.no_check else int(mixed["missed"]),
+            "roofline": roof, "cpu_baseline": cpu, "clocks": mixed["clocks"],
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "gpu_launches": int(sum(launches)),
-            "step_ms_quantiles": [round(float(q), 3) for q in np.quantile(step_ms, [0, 0.25, 0.5, 0.75, 1.0])],
+            "gpu_launches": int(launches),
+            "step_ms_quantiles": [round(float(q), 3) for q in np.quantile(mixed["step_ms"], [0, .25, .5, .75, 1])],
             "counters": tot, "stages_ms": {k: round(v[0], 3) for k, v in prof.items()}}
     print(json.dumps(line), flush=True)
     if ws > 1:
@@ -329,12 +414,17 @@ def run_gpu(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="batched",
+                    choices=["batched", "folded_cloth", "cloth_on_sphere", "strings", "large"])
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--plain-steps", type=int, default=10, help="timed steps of the one-scene-at-a-time run")
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--ref-budget", type=float, default=120.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-check", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -63,7 +63,23 @@ def load(path: str = LIB_PATH):
     lib.cc_set_params.argtypes = [vp, C.POINTER(cc_params)]
     lib.cc_set_domain_boundary.restype = C.c_int
     lib.cc_set_domain_boundary.argtypes = [vp, dp, dp]
-    for f in ("cc_resolve", "cc_resolve_device"):
+    lib.cc_assemble_batch.restype = C.c_int
+    lib.cc_assemble_batch.argtypes = [vp, C.POINTER(cc_mesh), C.c_int]
+    lib.cc_num_scenes.restype = C.c_int
+    lib.cc_num_scenes.argtypes = [vp]
+    lib.cc_get_scene_offsets.restype = C.c_int
+    lib.cc_get_scene_offsets.argtypes = [vp, ip, ip]
+    lib.cc_set_scene_params.restype = C.c_int
+    lib.cc_set_scene_params.argtypes = [vp, C.c_int, C.POINTER(cc_params)]
+    lib.cc_set_scene_domain_boundary.restype = C.c_int
+    lib.cc_set_scene_domain_boundary.argtypes = [vp, C.c_int, dp, dp]
+    lib.cc_check_ccd.restype = C.c_int
+    lib.cc_check_ccd.argtypes = [vp, dp, dp, lp, ip]
+    lib.cc_set_host_threads.restype = C.c_int
+    lib.cc_set_host_threads.argtypes = [vp, C.c_int]
+    lib.cc_get_scene_pass_kinds.restype = C.c_int
+    lib.cc_get_scene_pass_kinds.argtypes = [vp, C.c_int, ip, C.c_int]
+    for f in ("cc_resolve", "cc_resolve_device", "cc_resolve_batch", "cc_resolve_batch_device"):
         getattr(lib, f).restype = C.c_int
         getattr(lib, f).argtypes = [vp, dp, dp, dp, up, dp, ip]
     lib.cc_get_counters.restype = C.c_int

@@ -22,21 +22,47 @@ __device__ __forceinline__ double dec_double(unsigned long long e) {
     return __longlong_as_double((long long)u);
 }
 
-__global__ void k_bbox_init(unsigned long long* bb) {
-    int t = threadIdx.x;
-    if (t < 3) bb[t] = ~0ull;
-    else if (t < 6) bb[t] = 0ull;
+__global__ void k_bbox_init(unsigned long long* bb, int n6) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n6) bb[t] = (t % 6 < 3) ? ~0ull : 0ull;
+}
+
+// Per-scene union of boxes into bb[6*scene ..]: reduced across the warp when
+// the whole warp lies in one scene (the common case: scenes are contiguous),
+// else one atomic per lane.
+__device__ __forceinline__ void scene_bbox_accumulate(unsigned long long* bb, int scene, bool valid,
+                                                      const double* lo, const double* hi) {
+    int s0 = __shfl_sync(0xffffffffu, scene, 0);
+    bool uniform = __all_sync(0xffffffffu, scene == s0);
+    for (int d = 0; d < 3; ++d) {
+        double l = valid ? lo[d] : kBig, h = valid ? hi[d] : -kBig;
+        if (uniform) {
+            for (int o = 16; o > 0; o >>= 1) {
+                l = fmin(l, __shfl_xor_sync(0xffffffffu, l, o));
+                h = fmax(h, __shfl_xor_sync(0xffffffffu, h, o));
+            }
+            if ((threadIdx.x & 31) == 0 && l <= h && s0 >= 0) {
+                atomicMin(&bb[6 * s0 + d], enc_double(l));
+                atomicMax(&bb[6 * s0 + 3 + d], enc_double(h));
+            }
+        } else if (valid) {
+            atomicMin(&bb[6 * scene + d], enc_double(l));
+            atomicMax(&bb[6 * scene + 3 + d], enc_double(h));
+        }
+    }
 }
 
 template <int MOVING>
-__global__ void k_leaf_boxes(const int* __restrict__ ev, int ne, int nt, const double4_32a* __restrict__ xo,
-                             const double4_32a* __restrict__ av, double dt, Box6* __restrict__ box,
-                             unsigned long long* bb) {
+__global__ void k_leaf_boxes(const int* __restrict__ ev, int ne, const int* __restrict__ elem_scene,
+                             const SceneDev* __restrict__ scenes, const double4_32a* __restrict__ xo,
+                             const double4_32a* __restrict__ av, Box6* __restrict__ box, unsigned long long* bb) {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
-    double lo[3] = {kBig, kBig, kBig}, hi[3] = {-kBig, -kBig, -kBig};
     bool valid = e < ne;
+    int scene = valid ? elem_scene[e] : -1;
+    double lo[3] = {kBig, kBig, kBig}, hi[3] = {-kBig, -kBig, -kBig};
     if (valid) {
-        int np = (e < nt) ? 3 : 2;
+        double dt = scenes[scene].p.dt;
+        int np = (ev[3 * e + 2] >= 0) ? 3 : 2;
         double mx[3] = {-kBig, -kBig, -kBig}, mn[3] = {kBig, kBig, kBig};
         for (int i = 0; i < np; ++i) {
             int p = ev[3 * e + i];
@@ -67,18 +93,7 @@ __global__ void k_leaf_boxes(const int* __restrict__ ev, int ne, int nt, const d
         }
         box[e] = b;
     }
-    // union of the leaf boxes (the root box of any tree over them)
-    for (int d = 0; d < 3; ++d) {
-        double l = lo[d], h = hi[d];
-        for (int o = 16; o > 0; o >>= 1) {
-            l = fmin(l, __shfl_xor_sync(0xffffffffu, l, o));
-            h = fmax(h, __shfl_xor_sync(0xffffffffu, h, o));
-        }
-        if ((threadIdx.x & 31) == 0 && l <= h) {
-            atomicMin(&bb[d], enc_double(l));
-            atomicMax(&bb[3 + d], enc_double(h));
-        }
-    }
+    scene_bbox_accumulate(bb, scene, valid, lo, hi);
 }
 
 // Union of n given boxes into bb (encoded as for k_leaf_boxes).
@@ -113,14 +128,16 @@ __device__ __forceinline__ unsigned int expand_bits10(unsigned int v) {
     return v;
 }
 
-__global__ void k_morton(const Box6* __restrict__ box, int n, const unsigned long long* bb,
-                         unsigned long long* keys, unsigned int* order) {
+__global__ void k_morton(const Box6* __restrict__ box, int n, const int* __restrict__ elem_scene,
+                         const unsigned long long* bb, unsigned long long* keys, unsigned int* order) {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n) return;
     Box6 b = box[e];
+    int sc = elem_scene ? elem_scene[e] : 0;
+    const unsigned long long* sb = bb + 6 * sc;
     unsigned int q[3];
     for (int d = 0; d < 3; ++d) {
-        double lo = dec_double(bb[d]), hi = dec_double(bb[3 + d]);
+        double lo = dec_double(sb[d]), hi = dec_double(sb[3 + d]);
         double c = 0.5 * (b.lo[d] + b.hi[d]);
         double ext = hi - lo;
         double t = ext > 0.0 ? (c - lo) / ext : 0.0;
@@ -128,7 +145,9 @@ __global__ void k_morton(const Box6* __restrict__ box, int n, const unsigned lon
         unsigned int v = (unsigned int)(t * 1023.0);
         q[d] = v > 1023u ? 1023u : v;
     }
-    keys[e] = (unsigned long long)((expand_bits10(q[0]) << 2) | (expand_bits10(q[1]) << 1) | expand_bits10(q[2]));
+    unsigned long long m = (unsigned long long)((expand_bits10(q[0]) << 2) | (expand_bits10(q[1]) << 1) |
+                                                expand_bits10(q[2]));
+    keys[e] = ((unsigned long long)sc << 30) | m;
     order[e] = (unsigned int)e;
 }
 
@@ -142,7 +161,7 @@ __device__ __forceinline__ int delta(const unsigned long long* keys, int n, int 
 // Karras, "Maximizing parallelism in the construction of BVHs, octrees and
 // k-d trees" (HPG 2012), with index tie-breaking for equal keys.
 __global__ void k_karras(const unsigned long long* __restrict__ keys, int n, int* child, int* range_hi,
-                         int* parent) {
+                         int* range_lo, int* parent) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
     int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
@@ -167,6 +186,7 @@ __global__ void k_karras(const unsigned long long* __restrict__ keys, int n, int
     child[2 * i] = left;
     child[2 * i + 1] = right;
     range_hi[i] = hi;
+    range_lo[i] = lo;
     if (left >= 0) parent[left] = i; else parent[n - 1 + ~left] = i;
     if (right >= 0) parent[right] = i; else parent[n - 1 + ~right] = i;
     if (i == 0) parent[0] = -1;
@@ -204,30 +224,65 @@ __global__ void k_refit(const Box6* __restrict__ box, const unsigned int* __rest
     }
 }
 
+// The LBVH node whose leaves are exactly scene s's (keys carry the scene id
+// in their high bits, so every scene owns one subtree).
+__global__ void k_scene_roots(const SceneDev* __restrict__ scenes, SceneRun* run, int nscenes, int n,
+                              const int* __restrict__ parent, const int* __restrict__ range_lo,
+                              const int* __restrict__ range_hi) {
+    int sc = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sc >= nscenes) return;
+    int first = scenes[sc].e0, last = scenes[sc].e0 + scenes[sc].ne - 1;
+    if (scenes[sc].ne < 2) {
+        run[sc].root = -1;
+        return;
+    }
+    int node = parent[n - 1 + first];
+    while (node >= 0 && !(range_lo[node] <= first && range_hi[node] >= last)) node = parent[node];
+    run[sc].root = node;
+}
+
 __device__ __forceinline__ bool overlap(const Box6& a, const Box6& b) {
     return (a.lo[0] <= b.hi[0] && a.hi[0] >= b.lo[0]) && (a.lo[1] <= b.hi[1] && a.hi[1] >= b.lo[1]) &&
            (a.lo[2] <= b.hi[2] && a.hi[2] >= b.lo[2]);
 }
 
 __device__ __forceinline__ void emit_pair(int a, int b, int2* pairs, int cap, PassCounters* ctr) {
-    int slot = atomicAdd(&ctr->npairs, 1);
+    int slot = aggregated_add(&ctr->npairs, 1);
     if (slot < cap)
         pairs[slot] = make_int2(a, b);
     else
         atomicOr(&ctr->err, kErrPairOverflow);
 }
 
-// One thread per sorted leaf i reports every leaf j > i whose box overlaps.
+// One thread per sorted leaf i reports every leaf j > i of its scene whose
+// box overlaps, starting from the scene's subtree root; leaves of scenes
+// idle in this pass report nothing. With ev given, pairs of elements that
+// share a point are dropped: every narrow-phase test of such a pair returns
+// false before any arithmetic (dcollid3d.cpp:493-497, 541-546, 578-582).
 __global__ void k_traverse(const Box6* __restrict__ box, const unsigned int* __restrict__ order, int n,
                            const int* __restrict__ child, const int* __restrict__ range_hi,
-                           const Box6* __restrict__ node_box, int2* pairs, int cap, PassCounters* ctr) {
+                           const Box6* __restrict__ node_box, const int* __restrict__ elem_scene,
+                           const SceneRun* __restrict__ run, const int* __restrict__ ev, int2* pairs, int cap,
+                           PassCounters* ctr) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
     int ei = (int)order[i];
+    int pi0 = -1, pi1 = -1, pi2 = -1;
+    if (ev) {
+        pi0 = ev[3 * ei];
+        pi1 = ev[3 * ei + 1];
+        pi2 = ev[3 * ei + 2];  // -1 for a bond: matches no point
+    }
+    int root = 0;
+    if (run) {
+        SceneRun r = run[elem_scene[ei]];
+        if (r.mode == kSceneIdle || r.root < 0) return;
+        root = r.root;
+    }
     Box6 q = box[ei];
     int stk[kTraversalStack];
     int sp = 0;
-    stk[sp++] = 0;
+    stk[sp++] = root;
     while (sp > 0) {
         int node = stk[--sp];
         for (int k = 0; k < 2; ++k) {
@@ -236,7 +291,15 @@ __global__ void k_traverse(const Box6* __restrict__ box, const unsigned int* __r
                 int j = ~c;
                 if (j > i) {
                     int ej = (int)order[j];
-                    if (overlap(q, box[ej])) emit_pair(ei, ej, pairs, cap, ctr);
+                    if (overlap(q, box[ej])) {
+                        bool shared = false;
+                        if (ev) {
+                            int a = ev[3 * ej], b = ev[3 * ej + 1], c3 = ev[3 * ej + 2];
+                            shared = a == pi0 || a == pi1 || a == pi2 || b == pi0 || b == pi1 || b == pi2 ||
+                                     (c3 >= 0 && (c3 == pi0 || c3 == pi1 || c3 == pi2));
+                        }
+                        if (!shared) emit_pair(ei, ej, pairs, cap, ctr);
+                    }
                 }
             } else if (range_hi[c] > i && overlap(q, node_box[c])) {
                 if (sp < kTraversalStack)
@@ -248,53 +311,64 @@ __global__ void k_traverse(const Box6* __restrict__ box, const unsigned int* __r
     }
 }
 
-__global__ void k_brute_pairs(const Box6* __restrict__ box, int n, int2* pairs, int cap, PassCounters* ctr) {
+__global__ void k_brute_pairs(const Box6* __restrict__ box, int n, const int* __restrict__ elem_scene, int2* pairs,
+                              int cap, PassCounters* ctr) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     Box6 q = box[i];
+    int si = elem_scene ? elem_scene[i] : 0;
     for (int j = i + 1; j < n; ++j)
-        if (overlap(q, box[j])) emit_pair(i, j, pairs, cap, ctr);
+        if ((!elem_scene || elem_scene[j] == si) && overlap(q, box[j])) emit_pair(i, j, pairs, cap, ctr);
 }
 
 inline int nblk(int n, int t) { return (n + t - 1) / t; }
 
 }  // namespace
 
-void leaf_boxes(const int* ev, int ne, int nt, const double4_32a* xo, const double4_32a* av, double dt, int moving,
-                Box6* box, unsigned long long* bbox_enc, cudaStream_t s) {
-    count_launch(), k_bbox_init<<<1, 32, 0, s>>>(bbox_enc);
+void leaf_boxes(const int* ev, int ne, const int* elem_scene, const SceneDev* scenes, int nscenes,
+                const double4_32a* xo, const double4_32a* av, int moving, Box6* box, unsigned long long* bbox_enc,
+                cudaStream_t s) {
+    count_launch(), k_bbox_init<<<nblk(6 * nscenes, 256), 256, 0, s>>>(bbox_enc, 6 * nscenes);
     if (ne <= 0) return;
     if (moving)
-        count_launch(), k_leaf_boxes<1><<<nblk(ne, 256), 256, 0, s>>>(ev, ne, nt, xo, av, dt, box, bbox_enc);
+        count_launch(), k_leaf_boxes<1><<<nblk(ne, 256), 256, 0, s>>>(ev, ne, elem_scene, scenes, xo, av, box, bbox_enc);
     else
-        count_launch(), k_leaf_boxes<0><<<nblk(ne, 256), 256, 0, s>>>(ev, ne, nt, xo, av, dt, box, bbox_enc);
+        count_launch(), k_leaf_boxes<0><<<nblk(ne, 256), 256, 0, s>>>(ev, ne, elem_scene, scenes, xo, av, box, bbox_enc);
 }
 
 void boxes_bbox(const Box6* box, int n, unsigned long long* bbox_enc, cudaStream_t s) {
-    count_launch(), k_bbox_init<<<1, 32, 0, s>>>(bbox_enc);
+    count_launch(), k_bbox_init<<<1, 32, 0, s>>>(bbox_enc, 6);
     if (n > 0) count_launch(), k_boxes_bbox<<<nblk(n, 256), 256, 0, s>>>(box, n, bbox_enc);
 }
 
 void bvh_build(const Box6* box, BvhBufs& b, cudaStream_t s) {
     int n = b.n;
     if (n <= 1) return;
-    count_launch(), k_morton<<<nblk(n, 256), 256, 0, s>>>(box, n, b.bbox_enc, b.keys, b.order);
-    radix_sort_pairs(b.keys, b.order, n, 30, b.sort_temp, s);
-    count_launch(), k_karras<<<nblk(n - 1, 256), 256, 0, s>>>(b.keys, n, b.child, b.range_hi, b.parent);
+    count_launch(), k_morton<<<nblk(n, 256), 256, 0, s>>>(box, n, b.elem_scene, b.bbox_enc, b.keys, b.order);
+    int bits = 30;
+    while (bits < 62 && (b.nscenes - 1) >> (bits - 30)) ++bits;
+    radix_sort_pairs(b.keys, b.order, n, bits, b.sort_temp, s);
+    count_launch(), k_karras<<<nblk(n - 1, 256), 256, 0, s>>>(b.keys, n, b.child, b.range_hi, b.range_lo, b.parent);
     cudaMemsetAsync(b.flags, 0, sizeof(int) * (size_t)(n - 1), s);
     count_launch(), k_refit<<<nblk(n, 256), 256, 0, s>>>(box, b.order, n, b.child, b.parent, b.flags, b.node_box);
+    if (b.run)
+        count_launch(), k_scene_roots<<<nblk(b.nscenes, 128), 128, 0, s>>>(b.scenes, b.run, b.nscenes, n, b.parent,
+                                                                          b.range_lo, b.range_hi);
 }
 
-void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCounters* ctr, cudaStream_t s) {
+void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCounters* ctr, cudaStream_t s,
+               const int* skip_shared_ev) {
     int n = b.n;
     if (n <= 1) return;
-    count_launch(), k_traverse<<<nblk(n - 1, 128), 128, 0, s>>>(box, b.order, n, b.child, b.range_hi, b.node_box, pairs, cap,
-                                                  ctr);
+    count_launch(), k_traverse<<<nblk(n - 1, 128), 128, 0, s>>>(box, b.order, n, b.child, b.range_hi, b.node_box,
+                                                                b.elem_scene, b.run, skip_shared_ev, pairs, cap,
+                                                                ctr);
 }
 
-void brute_pairs(const Box6* box, int ne, int2* pairs, int cap, PassCounters* ctr, cudaStream_t s) {
+void brute_pairs(const Box6* box, int ne, const int* elem_scene, int2* pairs, int cap, PassCounters* ctr,
+                 cudaStream_t s) {
     if (ne <= 1) return;
-    count_launch(), k_brute_pairs<<<nblk(ne, 128), 128, 0, s>>>(box, ne, pairs, cap, ctr);
+    count_launch(), k_brute_pairs<<<nblk(ne, 128), 128, 0, s>>>(box, ne, elem_scene, pairs, cap, ctr);
 }
 
 }  // namespace ccg

@@ -12,6 +12,11 @@
 
 #include <cmath>
 
+#ifdef __CUDACC__
+#include <cooperative_groups.h>
+#include <cooperative_groups/scan.h>
+#endif
+
 namespace ccg {
 
 // Reference constants: collid.h:17-19, AABB.cpp:10-16, dcollid.cpp:433,489,590.
@@ -49,6 +54,19 @@ enum ErrBits {
     kErrContribOverflow = 8,
     kErrRecordOverflow = 16,
     kErrMergeOverflow = 32,
+    kErrUnionOverflow = 64,
+};
+// Errors after which a pass's results are discarded (and the pass retried
+// with larger buffers, or the call fails): the impulses are not applied.
+constexpr int kErrRetry = kErrPairOverflow | kErrStack | kErrContribOverflow | kErrRecordOverflow | kErrUnionOverflow;
+
+// One createImpZone(pts, 4) call of an impact-zone pass (dcollid.cpp:473-484),
+// keyed by the reference's visiting order like a contribution: the host
+// replays the calls in key order to rebuild the reference's union-find
+// lists, whose member order fixes the summation order of the zone solve.
+struct __align__(8) UnionRec {
+    unsigned long long key;
+    int p[4];
 };
 
 // One impulse contribution to one point, keyed by the reference's visiting
@@ -72,6 +90,33 @@ struct Params {
     double dt, thickness, eps, k, m, lambda, cr;
 };
 
+// Per-scene description on the device. Scenes are concatenated: points
+// [v0, v0+nv), elements [e0, e0+ne), each scene's elements in its own order
+// (triangles, then bonds).
+// Scenes resolved together: each owns contiguous ranges of points and
+// elements (triangles first, then bonds, as in its own mesh) and has its own
+// parameters, domain box and strain-sweep schedule.
+struct SceneDev {
+    Params p;
+    double lo[3], hi[3];  // domain box
+    int v0, nv, e0, ne;   // point and element ranges
+    int strain_hdr0;      // first level of its strain schedule (index into the level headers)
+    int strain_levels;
+    int strain_slots;     // shared-memory slots of its window sweep
+    int wb_final0, wb_final1;  // write-backs after its last level
+    int pad[3];
+};
+
+// Per-pass state of a scene (written by the host before a pass, except
+// hits, which the narrow phase counts, and root, which the BVH build sets).
+enum SceneMode { kSceneIdle = 0, kSceneProx = 1, kSceneCcd = 2, kSceneZone = 3 };
+struct SceneRun {
+    int mode;  // SceneMode of the current pass
+    int hits;  // narrow-phase calls that returned true in the current pass
+    int pass;  // the scene's own pass index (for visit records)
+    int root;  // the scene's subtree root in the LBVH (-1: fewer than 2 elements)
+};
+
 struct PassCounters {
     int npairs;       // candidate pairs written by the traversal
     int ncontrib;     // contributions written by the narrow phase
@@ -81,7 +126,24 @@ struct PassCounters {
     int nvisits;      // narrow-phase calls (pairs not skipped as same-rigid-surface)
     int ncontacts;    // sub-tests that applied an impulse
     int nsub;         // sub-tests evaluated in FP64 (not rejected by a filter)
+    int ncr;          // coplanarity cubics whose roots were formed again correctly rounded
+    int nunion;       // union records written (impact-zone passes)
+    int pad[2];
 };
+
+#ifdef __CUDACC__
+// atomicAdd(p, n) for every calling thread, one atomic per group of threads
+// that arrive together (warp-aggregated); returns each thread's old value.
+__device__ __forceinline__ int aggregated_add(int* p, int n) {
+    namespace cg = cooperative_groups;
+    cg::coalesced_group g = cg::coalesced_threads();
+    int incl = cg::inclusive_scan(g, n);
+    int base = 0;
+    if (g.thread_rank() == g.size() - 1) base = atomicAdd(p, incl);
+    base = g.shfl(base, g.size() - 1);
+    return base + incl - n;
+}
+#endif
 
 __device__ __forceinline__ double dot3(const double* a, const double* b) {
     return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];

@@ -32,6 +32,11 @@ struct __align__(16) Box6 {
 
 struct BvhBufs {
     int n;                        // leaves
+    int nscenes;
+    const int* elem_scene;        // scene of every element (null: one scene)
+    const SceneDev* scenes;       // scene descriptors (null: one scene, root 0)
+    SceneRun* run;                // per-pass scene state (null: one scene, root 0)
+    int* range_lo;                // n-1: first sorted leaf covered by each internal node
     unsigned long long* keys;     // n Morton keys (sorted)
     unsigned int* order;          // n element ids in Morton order
     int* child;                   // 2*(n-1): >= 0 internal, < 0 leaf (~sorted index)
@@ -39,51 +44,62 @@ struct BvhBufs {
     int* parent;                  // 2n-1: parents of internal nodes [0,n-1) then leaves
     int* flags;                   // n-1 refit arrival counters
     Box6* node_box;               // n-1 internal boxes
-    unsigned long long* bbox_enc; // 6 encoded doubles (scene box)
+    unsigned long long* bbox_enc; // 6 encoded doubles per scene (scene boxes)
     void* sort_temp;
 };
 
 // Leaf boxes of every element (static: x_old; moving: x_old and
-// x_old + dt*avgVel), padded by 1e-6, plus their union in bbox_enc.
-void leaf_boxes(const int* ev, int ne, int nt, const double4_32a* xo, const double4_32a* av, double dt, int moving,
-                Box6* box, unsigned long long* bbox_enc, cudaStream_t s);
+// x_old + dt*avgVel with the element's scene's dt), padded by 1e-6, plus
+// each scene's union in bbox_enc[6*scene ..].
+void leaf_boxes(const int* ev, int ne, const int* elem_scene, const SceneDev* scenes, int nscenes,
+                const double4_32a* xo, const double4_32a* av, int moving, Box6* box, unsigned long long* bbox_enc,
+                cudaStream_t s);
 // Union of n given boxes in bbox_enc (the scene box the Morton keys use).
 void boxes_bbox(const Box6* box, int n, unsigned long long* bbox_enc, cudaStream_t s);
-// Morton keys, sort, Karras hierarchy, refit.
+// Morton keys (scene id above the 30 Morton bits, each scene normalised to
+// its own box), sort, Karras hierarchy, refit, per-scene subtree roots.
 void bvh_build(const Box6* box, BvhBufs& b, cudaStream_t s);
-// All leaf pairs with overlapping boxes, each unordered pair once.
-void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCounters* ctr, cudaStream_t s);
+// All leaf pairs of one scene with overlapping boxes, each unordered pair
+// once; scenes idle in this pass are skipped. With skip_shared_ev (the
+// elements' point ids), pairs of elements sharing a point are left out.
+void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCounters* ctr, cudaStream_t s,
+               const int* skip_shared_ev = nullptr);
 // The same pair set by testing every pair (for cross-checks on small meshes).
-void brute_pairs(const Box6* box, int ne, int2* pairs, int cap, PassCounters* ctr, cudaStream_t s);
+void brute_pairs(const Box6* box, int ne, const int* elem_scene, int2* pairs, int cap, PassCounters* ctr,
+                 cudaStream_t s);
 
 // ------------------------------------------------------------ narrow phase
 struct NarrowArgs {
     const double4_32a* xo;
     const double4_32a* av;
     const uint8_t* fixed;
-    const int* ev;
+    const int* ev;          // 3 point ids per element (bonds: third is -1)
     const int* esurf;
     const uint8_t* erigid;
-    const int* rank;
-    int nt;
-    int pass;
-    int zone;
-    Params p;
+    const int* rank;        // leaf rank of each element within its scene's tree (null: element ids)
+    const int* escene;      // scene of each element
+    const SceneDev* scenes; // parameters per scene
+    SceneRun* run;          // mode and pass per scene; hits counted here
     const int2* pairs;
     Contrib* contrib;
     int contrib_cap;
     PassCounters* ctr;
-    int* uf_parent;
+    UnionRec* urec;         // createImpZone records (impact-zone passes)
+    int urec_cap;
     VisitRec* rec;
     int rec_cap;
     const float4* pbox_lo;  // null: plain FP64 (no filter)
     const float4* pbox_hi;
-    float hpad, epad;
+    const float4* p32;      // x_old in FP32 (with pbox_lo)
+    const float4* v32;      // avgVel in FP32 (with pbox_lo, moving passes)
+    int check;              // hit decisions only (no impulses, contacts, zones)
 };
 void narrow_pass(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s);
-// Outward-rounded FP32 point boxes for the mixed-precision filter.
-void point_boxes(const double4_32a* xo, const double4_32a* av, double dt, int nv, int moving, float4* lo,
-                 float4* hi, cudaStream_t s);
+// Inputs of the mixed-precision filter: outward-rounded FP32 boxes of every
+// point over the pass's time window (with its scene's dt), and x_old and
+// (moving passes) avgVel rounded to FP32.
+void point_boxes(const double4_32a* xo, const double4_32a* av, const int* vscene, const SceneDev* scenes, int nv,
+                 int moving, float4* lo, float4* hi, float4* p32, float4* v32, cudaStream_t s);
 
 // ------------------------------------------------------------- post-pass
 struct ApplyBufs {
@@ -98,51 +114,46 @@ struct ApplyBufs {
 void apply_contribs(const Contrib* contrib, const PassCounters* ctr, int contrib_cap, int nv, double4_32a* av,
                     uint8_t* has_collsn, ApplyBufs& b, cudaStream_t s);
 
-struct ZoneBufs {
-    int* root;                  // nv
-    int* zcnt;                  // nv
-    unsigned long long* keys;   // nv
-    unsigned int* vals;         // nv
-    int* nmembers;              // 1
-    void* sort_temp;
-};
-void uf_init(int* parent, int nv, cudaStream_t s);
-// updateImpactZoneVelocity: rigid motion of every zone with >= 2 points.
-void zone_velocity(int* parent, const uint8_t* in_elem, const uint8_t* fixed, const double4_32a* xo, double4_32a* av,
-                   int nv, const Params& p, ZoneBufs& z, PassCounters* ctr, cudaStream_t s);
+// updateImpactZoneVelocity (dcollid.cpp:290-310): rigid motion of every
+// zone, one thread per zone over members[zone_off[z] .. zone_off[z+1]) in
+// the order of the reference's member list, with its scene's parameters.
+void zone_solve(const int* members, const int* zone_off, int nzones, const uint8_t* fixed, const double4_32a* xo,
+                double4_32a* av, const int* vscene, const SceneDev* scenes, PassCounters* ctr, cudaStream_t s);
 
-// Step set-up: pack inputs, average velocity (computeAverageVelocity).
-void step_init(const double* x_old, const double* x_cand, int nv, const uint8_t* in_elem, double dt, double4_32a* xo,
-               double4_32a* av, PassCounters* ctr, cudaStream_t s);
-// Domain clamp + final position (detectDomainBoundaryCollision, updateFinalPosition).
+// Step set-up: pack inputs, average velocity (computeAverageVelocity), each
+// point with its scene's dt.
+void step_init(const double* x_old, const double* x_cand, int nv, const uint8_t* in_elem, const int* vscene,
+               const SceneDev* scenes, double4_32a* xo, double4_32a* av, PassCounters* ctr, cudaStream_t s);
+// Domain clamp + final position (detectDomainBoundaryCollision,
+// updateFinalPosition) with each point's scene's parameters and domain box.
 void finalize_positions(const uint8_t* in_elem, const double4_32a* xo, double4_32a* av, uint8_t* has_collsn,
-                        const double* x_cand, double* x_out, int nv, const Params& p, const double* lo,
-                        const double* hi, cudaStream_t s);
-// reduceSuperelast: up to 10 Gauss-Seidel passes over the strain edges.
+                        const double* x_cand, double* x_out, int nv, const int* vscene, const SceneDev* scenes,
+                        cudaStream_t s);
+// reduceSuperelast: up to 10 Gauss-Seidel passes over each scene's strain
+// edges, one CTA per scene.
 struct StrainEdge {
     int p0, p1;
     double len0;
-    int s0, s1;  // shared-memory slots of p0, p1 in the window sweep
+    int s0, s1;  // shared-memory slots of p0, p1 in the scene's window sweep
 };
-// Shared-memory window schedule of the strain sweep (see k_strain_window):
-// per level l, load_list[load_off[l] .. load_off[l+1]) are (point, slot)
-// pairs to copy in and wb_list[wb_off[l] .. wb_off[l+1]) pairs to write back
-// (wb level nlevels: after the last level).
-struct StrainWindow {
-    int nslots;
-    const int2* load_list;
-    const int* load_off;
-    const int2* wb_list;
-    const int* wb_off;
-    const int4* hdr;  // per level: (edge begin, end, load begin, end), (write-back begin, end, 0, 0)
-    int2 wb_final;    // write-backs after the last level
+// Strain schedule of all scenes: the edges of a scene are contiguous and
+// sorted by dependency level; its levels are hdr[2*(hdr0 + l)] =
+// (edge begin, end, copy-in begin, end) and hdr[2*(hdr0 + l) + 1] =
+// (write-back begin, end, 0, 0) for l < levels, with (point, slot) entries
+// in load_list / wb_list; the write-backs after its last level are
+// wb_list[wb_final0 .. wb_final1) (SceneDev).
+struct StrainPlan {
+    bool window;           // sweep in shared memory where the scene's slots fit
+    int max_window_slots;  // largest slot count among the scenes that fit
+    bool any_global;       // some scene needs more slots than fit
 };
-// edges sorted by dependency level; level_off has nlevels+1 offsets;
-// step_buf holds strain_step_bytes(nedges).
+int strain_window_slot_cap();
+// step_buf holds strain_step_bytes(nedges); passes_out holds 3 ints per
+// scene (passes, averaged edges, exact tests).
 size_t strain_step_bytes(int nedges);
-void strain_limit(const StrainEdge* edges, int nedges, const int* level_off, int nlevels, const double4_32a* xo,
-                  double4_32a* av, int nv, double dt, void* step_buf, const StrainWindow* win, int* passes_out,
-                  cudaStream_t s);
+void strain_limit(const StrainEdge* edges, int nedges, const int4* hdr, const int2* load_list, const int2* wb_list,
+                  const SceneDev* scenes, int nscenes, const StrainPlan& plan, const double4_32a* xo,
+                  double4_32a* av, void* step_buf, int* passes_out, cudaStream_t s);
 // Correctly rounded cos/sin/acos/pow (fn 0..3) on device arrays, for self-tests.
 void math_selftest(int fn, const double* a, const double* b, double* out, int n, cudaStream_t s);
 // updateFinalVelocity.

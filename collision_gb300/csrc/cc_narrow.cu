@@ -18,19 +18,33 @@ template <bool MOVING>
 __global__ void __launch_bounds__(128) k_narrow(NarrowArgs a, int max_pairs) {
     NarrowCtx c;
     c.xo = a.xo; c.av = a.av; c.fixed = a.fixed; c.ev = a.ev; c.esurf = a.esurf; c.erigid = a.erigid;
-    c.rank = a.rank; c.nt = a.nt; c.pass = a.pass; c.zone = a.zone; c.p = a.p;
-    c.contrib = a.contrib; c.contrib_cap = a.contrib_cap; c.ctr = a.ctr; c.uf_parent = a.uf_parent;
+    c.rank = a.rank;
+    c.contrib = a.contrib; c.contrib_cap = a.contrib_cap; c.ctr = a.ctr; c.urec = a.urec;
+    c.urec_cap = a.urec_cap;
     c.rec = a.rec; c.rec_cap = a.rec_cap;
-    c.pbox_lo = a.pbox_lo; c.pbox_hi = a.pbox_hi; c.hpad = a.hpad; c.epad = a.epad;
+    c.pbox_lo = a.pbox_lo; c.pbox_hi = a.pbox_hi; c.p32 = a.p32; c.v32 = a.v32;
+    c.check = a.check;
     int np = a.ctr->npairs;
     if (np > max_pairs) np = max_pairs;
+    // counters summed per thread, added once per warp at the end
+    int t_visits = 0, t_sub = 0, t_hits = 0, t_cr = 0, t_contacts = 0;
     for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) {
         int2 pr = a.pairs[idx];
-        int ri = c.rank[pr.x], rj = c.rank[pr.y];
+        int sc = a.escene[pr.x];
+        const SceneRun run = a.run[sc];
+        c.p = a.scenes[sc].p;
+        c.zone = run.mode == kSceneZone && !a.check;
+        c.pass = run.pass;
+        // h of the sub-tests (thickness for proximity, eps for CCD) and the
+        // barycentric tolerance eps, rounded up to FP32
+        c.hpad = __double2float_ru(MOVING ? c.p.eps : c.p.thickness);
+        c.epad = __double2float_ru(c.p.eps);
+        c.dt32 = __double2float_ru(c.p.dt);
+        int ri = c.rank ? c.rank[pr.x] : pr.x, rj = c.rank ? c.rank[pr.y] : pr.y;
         int ea = ri > rj ? pr.x : pr.y;  // found leaf
         int eb = ri > rj ? pr.y : pr.x;  // query leaf
         int ra = ri > rj ? ri : rj, rb = ri > rj ? rj : ri;
-        bool ta = ea < c.nt, tb = eb < c.nt;
+        bool ta = c.ev[3 * ea + 2] >= 0, tb = c.ev[3 * eb + 2] >= 0;
         int kind = (ta && tb) ? 0 : (!ta && !tb) ? 2 : 1;
         if (kind == 0 && c.esurf[ea] == c.esurf[eb] && c.erigid[ea]) continue;  // dcollid.cpp:762-763, 805-806
         // tri-bond pairs are always handed over as (tri, bond)
@@ -40,13 +54,15 @@ __global__ void __launch_bounds__(128) k_narrow(NarrowArgs a, int max_pairs) {
         const int* P2 = c.ev + 3 * e2;
         CallState st;
         st.keybase = ((unsigned long long)rb << 26) | ((unsigned long long)ra << 4);
-        int n1 = (e1 < c.nt) ? 3 : 2, n2 = (e2 < c.nt) ? 3 : 2;
+        int n1 = (P1[2] >= 0) ? 3 : 2, n2 = (P2[2] >= 0) ? 3 : 2;
         st.np = n1 + n2;
         for (int i = 0; i < 6; ++i) { st.dcount[i] = 0; st.plist[i] = -1; }
         for (int i = 0; i < n1; ++i) st.plist[i] = P1[i];
         for (int i = 0; i < n2; ++i) st.plist[n1 + i] = P2[i];
         st.sub = 0;
         st.nsub = 0;
+        st.ncr = 0;
+        st.ncontacts = 0;
         int A[3] = {P1[0], P1[1], n1 == 3 ? P1[2] : -1};
         int B[3] = {P2[0], P2[1], n2 == 3 ? P2[2] : -1};
         bool status;
@@ -56,9 +72,14 @@ __global__ void __launch_bounds__(128) k_narrow(NarrowArgs a, int max_pairs) {
             status = tri_to_bond<MOVING>(c, st, A, B);
         else
             status = bond_to_bond<MOVING>(c, st, A, B);
-        atomicAdd(&c.ctr->nvisits, 1);
-        if (st.nsub) atomicAdd(&c.ctr->nsub, st.nsub);
-        if (status) atomicAdd(&c.ctr->nhit_pairs, 1);
+        t_visits++;
+        t_sub += st.nsub;
+        t_cr += st.ncr;
+        t_contacts += st.ncontacts;
+        if (status) {
+            t_hits++;
+            atomicAdd(&a.run[sc].hits, 1);
+        }
         if (c.rec) {
             int slot = atomicAdd(&c.ctr->nrec, 1);
             if (slot < c.rec_cap) {
@@ -71,15 +92,31 @@ __global__ void __launch_bounds__(128) k_narrow(NarrowArgs a, int max_pairs) {
             }
         }
     }
+    for (int o = 16; o > 0; o >>= 1) {
+        t_visits += __shfl_xor_sync(0xffffffffu, t_visits, o);
+        t_sub += __shfl_xor_sync(0xffffffffu, t_sub, o);
+        t_hits += __shfl_xor_sync(0xffffffffu, t_hits, o);
+        t_cr += __shfl_xor_sync(0xffffffffu, t_cr, o);
+        t_contacts += __shfl_xor_sync(0xffffffffu, t_contacts, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (t_visits) atomicAdd(&c.ctr->nvisits, t_visits);
+        if (t_sub) atomicAdd(&c.ctr->nsub, t_sub);
+        if (t_hits) atomicAdd(&c.ctr->nhit_pairs, t_hits);
+        if (t_cr) atomicAdd(&c.ctr->ncr, t_cr);
+        if (t_contacts) atomicAdd(&c.ctr->ncontacts, t_contacts);
+    }
 }
 
 // FP32 box of every point over the pass's time window, rounded outward:
 // [x_old] for proximity, [x_old, x_old + dt*avgVel] for CCD.
 template <bool MOVING>
-__global__ void k_point_boxes(const double4_32a* __restrict__ xo, const double4_32a* __restrict__ av, double dt,
-                              int nv, float4* lo, float4* hi) {
+__global__ void k_point_boxes(const double4_32a* __restrict__ xo, const double4_32a* __restrict__ av,
+                              const int* __restrict__ vscene, const SceneDev* __restrict__ scenes, int nv, float4* lo,
+                              float4* hi, float4* p32, float4* v32) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nv) return;
+    double dt = MOVING ? scenes[vscene[p]].p.dt : 0.0;
     double4_32a x = xo[p];
     double a[3] = {x.x, x.y, x.z}, b[3] = {x.x, x.y, x.z};
     if (MOVING) {
@@ -92,17 +129,24 @@ __global__ void k_point_boxes(const double4_32a* __restrict__ xo, const double4_
     }
     lo[p] = make_float4(__double2float_rd(a[0]), __double2float_rd(a[1]), __double2float_rd(a[2]), 0.f);
     hi[p] = make_float4(__double2float_ru(b[0]), __double2float_ru(b[1]), __double2float_ru(b[2]), 0.f);
+    p32[p] = make_float4((float)x.x, (float)x.y, (float)x.z, 0.f);
+    if (MOVING) {
+        double4_32a v = av[p];
+        v32[p] = make_float4((float)v.x, (float)v.y, (float)v.z, 0.f);
+    }
 }
 
 }  // namespace
 
-void point_boxes(const double4_32a* xo, const double4_32a* av, double dt, int nv, int moving, float4* lo,
-                 float4* hi, cudaStream_t s) {
+void point_boxes(const double4_32a* xo, const double4_32a* av, const int* vscene, const SceneDev* scenes, int nv,
+                 int moving, float4* lo, float4* hi, float4* p32, float4* v32, cudaStream_t s) {
     if (nv <= 0) return;
     if (moving)
-        count_launch(), k_point_boxes<true><<<(nv + 255) / 256, 256, 0, s>>>(xo, av, dt, nv, lo, hi);
+        count_launch(), k_point_boxes<true><<<(nv + 255) / 256, 256, 0, s>>>(xo, av, vscene, scenes, nv, lo, hi,
+                                                                             p32, v32);
     else
-        count_launch(), k_point_boxes<false><<<(nv + 255) / 256, 256, 0, s>>>(xo, av, dt, nv, lo, hi);
+        count_launch(), k_point_boxes<false><<<(nv + 255) / 256, 256, 0, s>>>(xo, av, vscene, scenes, nv, lo, hi,
+                                                                              p32, v32);
 }
 
 void narrow_pass(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s) {

@@ -19,23 +19,27 @@ struct NarrowCtx {
     const int* ev;           // 3 point ids per element (bonds: third is -1)
     const int* esurf;        // surface id per element (-1 for bonds)
     const uint8_t* erigid;   // element has a fixed point (isRigidBody(hse))
-    const int* rank;         // leaf rank of each element in the reference tree
-    int nt;                  // elements [0, nt) are triangles
-    int pass;
-    int zone;                // impact-zone mode (s_detImpZone)
-    Params p;
+    const int* rank;         // leaf rank of each element in its scene's reference tree
+    int pass;                // the scene's pass index
+    int zone;                // impact-zone mode (s_detImpZone) of the scene
+    Params p;                // the scene's parameters
     Contrib* contrib;
     int contrib_cap;
     PassCounters* ctr;
-    int* uf_parent;
+    UnionRec* urec;          // createImpZone calls of impact-zone passes
+    int urec_cap;
     VisitRec* rec;
     int rec_cap;
     // mixed precision: per-point FP32 boxes over the pass's time window
     // (rounded outward), used to reject sub-tests that cannot hit
     const float4* pbox_lo;
     const float4* pbox_hi;
+    const float4* p32;    // x_old rounded to FP32
+    const float4* v32;    // avgVel rounded to FP32 (moving passes)
     float hpad;   // h of the sub-tests, rounded up
     float epad;   // eps (barycentric tolerance), rounded up
+    int check;    // decide hits only: no impulses, contacts or zones
+    float dt32;   // dt rounded up to FP32
 };
 
 struct CallState {
@@ -45,6 +49,8 @@ struct CallState {
     int dcount[6];
     int sub;
     int nsub;   // sub-tests evaluated in FP64
+    int ncr;    // cubics whose roots were formed again correctly rounded
+    int ncontacts;
 };
 
 __device__ __forceinline__ bool is_static(const NarrowCtx& c, int p) { return c.fixed[p] != 0; }
@@ -53,7 +59,7 @@ __device__ __forceinline__ void emit(const NarrowCtx& c, CallState& st, int vert
                                      const double* fric, int has_fric) {
     for (int i = 0; i < st.np; ++i)
         if (st.plist[i] == vertex) { st.dcount[i]++; break; }
-    int slot = atomicAdd(&c.ctr->ncontrib, 1);
+    int slot = aggregated_add(&c.ctr->ncontrib, 1);
     if (slot >= c.contrib_cap) {
         atomicOr(&c.ctr->err, kErrContribOverflow);
         return;
@@ -66,32 +72,19 @@ __device__ __forceinline__ void emit(const NarrowCtx& c, CallState& st, int vert
 }
 
 // ---------------------------------------------------------------- unions
-__device__ __forceinline__ int uf_find(int* parent, int x) {
-    // path halving; concurrent halving writes only shorten paths
-    while (true) {
-        int p = parent[x];
-        if (p == x) return x;
-        int gp = parent[p];
-        if (gp != p) parent[x] = gp;
-        x = gp;
-    }
-}
-
-__device__ __forceinline__ void uf_union(int* parent, int a, int b) {
-    while (true) {
-        a = uf_find(parent, a);
-        b = uf_find(parent, b);
-        if (a == b) return;
-        if (a > b) { int t = a; a = b; b = t; }
-        if (atomicCAS(&parent[b], b, a) == b) return;
-    }
-}
-
 // createImpZone(pts, 4), dcollid.cpp:473-484: the four points join one zone.
-__device__ __forceinline__ void create_imp_zone(const NarrowCtx& c, const int* pts) {
-    uf_union(c.uf_parent, pts[0], pts[1]);
-    uf_union(c.uf_parent, pts[0], pts[2]);
-    uf_union(c.uf_parent, pts[0], pts[3]);
+// The call is recorded with its visiting-order key; the unions themselves
+// are replayed in that order after the pass.
+__device__ __forceinline__ void create_imp_zone(const NarrowCtx& c, const CallState& st, const int* pts) {
+    int slot = aggregated_add(&c.ctr->nunion, 1);
+    if (slot >= c.urec_cap) {
+        atomicOr(&c.ctr->err, kErrUnionOverflow);
+        return;
+    }
+    UnionRec r;
+    r.key = st.keybase | (unsigned long long)st.sub;
+    for (int i = 0; i < 4; ++i) r.p[i] = pts[i];
+    c.urec[slot] = r;
 }
 
 // -------------------------------------------------------------- impulses
@@ -265,7 +258,8 @@ static __device__ bool point_to_tri(const NarrowCtx& c, CallState& st, const int
     if (dist > h) return false;
     for (int i = 0; i < 3; ++i)
         if (w[i] > 1 + c.p.eps || w[i] < -c.p.eps) return false;
-    atomicAdd(&c.ctr->ncontacts, 1);
+    if (c.check) return true;
+    st.ncontacts++;
     point_to_tri_impulse(c, st, pts, nor, w, dist);
     return true;
 }
@@ -315,7 +309,8 @@ static __device__ bool edge_to_edge(const NarrowCtx& c, CallState& st, const int
         return false;
     }
     for (int i = 0; i < 3; ++i) nor[i] /= nor_mag;
-    atomicAdd(&c.ctr->ncontacts, 1);
+    if (c.check) return true;
+    st.ncontacts++;
     edge_to_edge_impulse(c, st, pts, nor, a, b, dist);
     return true;
 }
@@ -323,7 +318,8 @@ static __device__ bool edge_to_edge(const NarrowCtx& c, CallState& st, const int
 // ------------------------------------------------------------------- CCD
 // isCoplanar, dcollid3d.cpp:371-482: roots of the coplanarity cubic in
 // [0, dt], shifted by -MACH_EPS and sorted; roots[3] holds dt.
-static __device__ bool is_coplanar(const double (*xo4)[3], const double (*av4)[3], double dt, double* roots) {
+static __device__ bool is_coplanar(const double (*xo4)[3], const double (*av4)[3], double dt, double* roots,
+                                   int* ncr) {
     double v[4][3], x[4][3];
     for (int j = 0; j < 3; ++j) {
         v[0][j] = av4[0][j];
@@ -383,6 +379,7 @@ static __device__ bool is_coplanar(const double (*xo4)[3], const double (*av4)[3
                 any |= near_[i];
             }
             if (any) {
+                ++*ncr;
                 theta = cr::acos(z);
                 if (near_[0]) f[0] = -2 * Qsqrt * cr::cos(theta / 3) - a / 3;
                 if (near_[1]) f[1] = -2 * Qsqrt * cr::cos((theta + 2 * kPi) / 3) - a / 3;
@@ -405,6 +402,7 @@ static __device__ bool is_coplanar(const double (*xo4)[3], const double (*av4)[3
                          fabs(fabs(A) - kRoundEps) <= 1e-14 * fabs(A) + 1e-300 ||
                          fabs(fabs(A - B) - kRoundEps) <= 1e-14 * scale + 1e-300;
             if (near_) {
+                ++*ncr;
                 A = -sgn * cr::pow(base, 1.0 / 3.0);
                 B = (fabs(A) < kRoundEps) ? 0.0 : Q / A;
                 f0 = (A + B) - a / 3.0;
@@ -446,7 +444,7 @@ static __device__ bool moving_test(const NarrowCtx& c, CallState& st, const int*
     }
     double dt = c.p.dt;
     double roots[4] = {-1, -1, -1, dt};
-    if (!is_coplanar(xo4, av4, dt, roots)) return false;
+    if (!is_coplanar(xo4, av4, dt, roots, &st.ncr)) return false;
     for (int i = 0; i < 4; ++i) {
         if (roots[i] < 0) continue;
         double X[4][3];
@@ -481,7 +479,8 @@ __device__ __forceinline__ bool static_test(const NarrowCtx& c, CallState& st, c
 // When the padded boxes do not overlap, the FP64 test returns false and is
 // skipped; every other sub-test runs unchanged, so the results are the plain
 // FP64 path's.
-__device__ __forceinline__ bool mixed_may_hit(const NarrowCtx& c, const int* pts, bool ee) {
+__device__ __forceinline__ bool mixed_may_hit(const NarrowCtx& c, const int* pts, bool ee, float* ext_out,
+                                              float* extb_out) {
     float4 l0 = c.pbox_lo[pts[0]], h0 = c.pbox_hi[pts[0]];
     float4 l1 = c.pbox_lo[pts[1]], h1 = c.pbox_hi[pts[1]];
     float4 l2 = c.pbox_lo[pts[2]], h2 = c.pbox_hi[pts[2]];
@@ -502,13 +501,15 @@ __device__ __forceinline__ bool mixed_may_hit(const NarrowCtx& c, const int* pts
     }
     float ext = __fadd_ru(__fadd_ru(__fsub_ru(ahi[0], alo[0]), __fsub_ru(ahi[1], alo[1])), __fsub_ru(ahi[2], alo[2]));
     float pad;
+    float extb = 0.f;
     if (ee) {
-        float extb = __fadd_ru(__fadd_ru(__fsub_ru(bhi[0], blo[0]), __fsub_ru(bhi[1], blo[1])),
-                               __fsub_ru(bhi[2], blo[2]));
+        extb = __fadd_ru(__fadd_ru(__fsub_ru(bhi[0], blo[0]), __fsub_ru(bhi[1], blo[1])), __fsub_ru(bhi[2], blo[2]));
         pad = __fadd_ru(c.hpad, __fmul_ru(__fadd_ru(ext, extb), 0x1p-20f));
     } else {
         pad = __fadd_ru(c.hpad, __fmul_ru(ext, __fadd_ru(__fmul_ru(8.0f, c.epad), 0x1p-10f)));
     }
+    *ext_out = ext;
+    *extb_out = extb;
     for (int d = 0; d < 3; ++d) {
         if (__fsub_rd(alo[d], pad) > bhi[d]) return false;
         if (__fadd_ru(ahi[d], pad) < blo[d]) return false;
@@ -516,9 +517,145 @@ __device__ __forceinline__ bool mixed_may_hit(const NarrowCtx& c, const int* pts
     return true;
 }
 
+// Second stage of the mixed-precision filter: a lower bound on the distance
+// between the point and the triangle (PT) or between the two segments (EE)
+// over the pass's time window, from FP32 copies of the points.
+//
+// Any direction n gives a lower bound: the gap between the projections of
+// the two point sets onto n, divided by |n| (both sets are convex hulls of
+// their points, so their projections are spanned by the points'). The
+// direction is taken from FP32 closest points (Ericson, Real-Time Collision
+// Detection, 2005, 5.1.5 ClosestPtPointTriangle and 5.1.9
+// ClosestPtSegmentSegment); how well it is chosen affects only how often
+// the bound rejects, never whether the bound holds. The bound is lowered by
+//  - the rounding of its own FP32 evaluation, at most 13*u*L for dot
+//    products over difference vectors of length <= L (u = 2^-24), and of the
+//    points to FP32, at most 2*sqrt(3)*u*M for coordinates of magnitude <= M:
+//    together below 32*u*(L + M);
+//  - on moving passes, the distance the sets can close within [0, dt]: the
+//    distance between two sets changes by at most the largest displacement
+//    of a point of each relative to a common reference (a segment's or a
+//    triangle's points move by at most the largest displacement of its
+//    corners), dt*(D1 + D2) with D the largest |v - v_ref| of each side.
+// A hit needs the distance within reach: for PT the plane distance <= h and
+// barycentric coordinates >= -eps - dw (dw <= 2^-10, the solve error the
+// box stage allows too) put the point within h + 6*(eps + dw)*diam of the
+// triangle (padded to 8*(eps + 2^-10)*ext); for EE the clamped closest
+// points within h are points of the segments, so the segments are within
+// h + 2^-20*ext. Sub-tests whose bound exceeds the reach return false in
+// FP64 too and are skipped.
+struct F3 {
+    float x, y, z;
+};
+__device__ __forceinline__ F3 f3(float4 a) { return F3{a.x, a.y, a.z}; }
+__device__ __forceinline__ F3 fsub(F3 a, F3 b) { return F3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ F3 fadd(F3 a, F3 b) { return F3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ F3 fscale(F3 a, float s) { return F3{a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ float fdot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float fnorm(F3 a) { return sqrtf(fdot(a, a)); }
+__device__ __forceinline__ float fmaxabs(F3 a) { return fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fabsf(a.z)); }
+__device__ __forceinline__ float clamp01(float x) { return fminf(fmaxf(x, 0.f), 1.f); }
+
+// Closest point of triangle (a, b, c) to p (Ericson 5.1.5), as an offset
+// from a.
+__device__ __forceinline__ F3 closest_on_tri(F3 ap, F3 ab, F3 ac) {
+    float d1 = fdot(ab, ap), d2 = fdot(ac, ap);
+    if (d1 <= 0.f && d2 <= 0.f) return F3{0.f, 0.f, 0.f};
+    F3 bp = fsub(ap, ab);
+    float d3 = fdot(ab, bp), d4 = fdot(ac, bp);
+    if (d3 >= 0.f && d4 <= d3) return ab;
+    float vc = d1 * d4 - d3 * d2;
+    if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) return fscale(ab, d1 / (d1 - d3));
+    F3 cp = fsub(ap, ac);
+    float d5 = fdot(ab, cp), d6 = fdot(ac, cp);
+    if (d6 >= 0.f && d5 <= d6) return ac;
+    float vb = d5 * d2 - d1 * d6;
+    if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) return fscale(ac, d2 / (d2 - d6));
+    float va = d3 * d6 - d5 * d4;
+    if (va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f) {
+        float w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+        return fadd(ab, fscale(fsub(ac, ab), w));
+    }
+    float den = 1.f / (va + vb + vc);
+    return fadd(fscale(ab, vb * den), fscale(ac, vc * den));
+}
+
+template <bool MOVING, bool EE>
+__device__ __forceinline__ bool sat_may_hit(const NarrowCtx& c, const int* pts, float ext, float extb) {
+    F3 X[4];
+    for (int q = 0; q < 4; ++q) X[q] = f3(c.p32[pts[q]]);
+    float M = fmaxf(fmaxf(fmaxabs(X[0]), fmaxabs(X[1])), fmaxf(fmaxabs(X[2]), fmaxabs(X[3])));
+    float lb, L, reach;
+    if (!EE) {
+        // triangle X0 X1 X2, point X3; origin X0
+        F3 ab = fsub(X[1], X[0]), ac = fsub(X[2], X[0]), ap = fsub(X[3], X[0]);
+        F3 n = fsub(ap, closest_on_tri(ap, ab, ac));
+        float nn = fnorm(n);
+        if (!(nn > 0.f)) return true;
+        float gap = fdot(n, ap) - fmaxf(0.f, fmaxf(fdot(n, ab), fdot(n, ac)));
+        lb = gap / nn;
+        L = fmaxf(fmaxf(fnorm(ab), fnorm(ac)), fnorm(ap));
+        reach = __fadd_ru(c.hpad, __fmul_ru(ext, __fmul_ru(8.0f, __fadd_ru(c.epad, 0x1p-10f))));
+    } else {
+        // segments S1 = X0 X1, S2 = X2 X3; origin X2
+        F3 d1 = fsub(X[1], X[0]), d2 = fsub(X[3], X[2]), r = fsub(X[0], X[2]);
+        float a = fdot(d1, d1), e = fdot(d2, d2), f = fdot(d2, r);
+        float s = 0.f, t = 0.f;
+        if (a > 0.f && e > 0.f) {
+            float cc = fdot(d1, r), b = fdot(d1, d2), den = a * e - b * b;
+            s = den > 0.f ? clamp01((b * f - cc * e) / den) : 0.f;
+            t = (b * s + f) / e;
+            if (t < 0.f) {
+                t = 0.f;
+                s = clamp01(-cc / a);
+            } else if (t > 1.f) {
+                t = 1.f;
+                s = clamp01((b - cc) / a);
+            }
+        } else if (a > 0.f) {
+            s = clamp01(-fdot(d1, r) / a);
+        } else if (e > 0.f) {
+            t = clamp01(f / e);
+        }
+        // n from S2's closest point to S1's
+        F3 n = fsub(fadd(r, fscale(d1, s)), fscale(d2, t));
+        float nn = fnorm(n);
+        if (!(nn > 0.f)) return true;
+        F3 q1 = fadd(r, d1);  // X1 - X2
+        float gap = fminf(fdot(n, r), fdot(n, q1)) - fmaxf(0.f, fdot(n, d2));
+        lb = gap / nn;
+        L = fmaxf(fmaxf(fnorm(r), fnorm(q1)), fnorm(d2));
+        reach = __fadd_ru(c.hpad, __fmul_ru(__fadd_ru(ext, extb), 0x1p-20f));
+    }
+    float err = __fmul_ru(32.0f * 0x1p-24f, __fadd_ru(L, M));
+    float bound = __fsub_rd(lb, err);
+    if (MOVING) {
+        F3 V[4];
+        for (int q = 0; q < 4; ++q) V[q] = f3(c.v32[pts[q]]);
+        // reference velocity: the first point's
+        float D1, D2;
+        if (!EE) {
+            D1 = fmaxf(fmaxf(fnorm(fsub(V[1], V[0])), fnorm(fsub(V[2], V[0]))), 0.f);
+            D2 = fnorm(fsub(V[3], V[0]));
+        } else {
+            D1 = fnorm(fsub(V[1], V[0]));
+            D2 = fmaxf(fnorm(fsub(V[2], V[0])), fnorm(fsub(V[3], V[0])));
+        }
+        float Vm = fmaxf(fmaxf(fmaxabs(V[0]), fmaxabs(V[1])), fmaxf(fmaxabs(V[2]), fmaxabs(V[3])));
+        // FP32 rounding of the velocities and of the sums above
+        float dv = __fadd_ru(__fmul_ru(__fadd_ru(D1, D2), 1.0f + 0x1p-16f), __fmul_ru(Vm, 32.0f * 0x1p-24f));
+        bound = __fsub_rd(bound, __fmul_ru(c.dt32, dv));
+    }
+    return !(bound > reach);
+}
+
 template <bool MOVING, bool EE>
 __device__ __forceinline__ bool sub_test(const NarrowCtx& c, CallState& st, const int* pts) {
-    if (c.pbox_lo && !mixed_may_hit(c, pts, EE)) return false;
+    if (c.pbox_lo) {
+        float ext, extb;
+        if (!mixed_may_hit(c, pts, EE, &ext, &extb)) return false;
+        if (!sat_may_hit<MOVING, EE>(c, pts, ext, extb)) return false;
+    }
     st.nsub++;
     if (MOVING) return moving_test<EE>(c, st, pts);
     return static_test<EE>(c, st, pts);
@@ -544,7 +681,7 @@ static __device__ bool tri_to_tri(const NarrowCtx& c, CallState& st, const int* 
             pts[3] = pt[i];
             st.sub = sub;
             if (sub_test<MOVING, false>(c, st, pts)) status = true;
-            if (MOVING && status && c.zone) create_imp_zone(c, pts);
+            if (MOVING && status && c.zone) create_imp_zone(c, st, pts);
         }
     for (int i = 0; i < 3; ++i) {
         pts[0] = A[i];
@@ -554,7 +691,7 @@ static __device__ bool tri_to_tri(const NarrowCtx& c, CallState& st, const int* 
             pts[3] = B[(j + 1) % 3];
             st.sub = sub;
             if (sub_test<MOVING, true>(c, st, pts)) status = true;
-            if (MOVING && status && c.zone) create_imp_zone(c, pts);
+            if (MOVING && status && c.zone) create_imp_zone(c, st, pts);
         }
     }
     return status;
@@ -572,7 +709,7 @@ static __device__ bool tri_to_bond(const NarrowCtx& c, CallState& st, const int*
         pts[3] = Bd[e];
         st.sub = e;
         if (sub_test<MOVING, false>(c, st, pts)) status = true;
-        if (MOVING && status && c.zone) create_imp_zone(c, pts);
+        if (MOVING && status && c.zone) create_imp_zone(c, st, pts);
     }
     pts[2] = Bd[0];
     pts[3] = Bd[1];
@@ -581,7 +718,7 @@ static __device__ bool tri_to_bond(const NarrowCtx& c, CallState& st, const int*
         pts[1] = T[(i + 1) % 3];
         st.sub = 2 + i;
         if (sub_test<MOVING, true>(c, st, pts)) status = true;
-        if (MOVING && status && c.zone) create_imp_zone(c, pts);
+        if (MOVING && status && c.zone) create_imp_zone(c, st, pts);
     }
     return status;
 }
@@ -595,7 +732,7 @@ static __device__ bool bond_to_bond(const NarrowCtx& c, CallState& st, const int
             if (pts[i] == pts[j]) return false;
     st.sub = 0;
     bool status = sub_test<MOVING, true>(c, st, pts);
-    if (MOVING && status && c.zone) create_imp_zone(c, pts);
+    if (MOVING && status && c.zone) create_imp_zone(c, st, pts);
     return status;
 }
 

@@ -58,7 +58,7 @@ cudaError_t scratch_address(int device, void** out) {
 
 __global__ void k_clear_counters(PassCounters* c) {
     c->npairs = 0; c->ncontrib = 0; c->nhit_pairs = 0; c->nrec = 0;
-    c->nvisits = 0; c->ncontacts = 0; c->err = 0; c->nsub = 0;
+    c->nvisits = 0; c->ncontacts = 0; c->err = 0; c->nsub = 0; c->ncr = 0; c->nunion = 0;
 }
 
 cc_status static_fail(cc_status st, const char* msg) {
@@ -102,10 +102,12 @@ cc_status cc_candidate_pairs_static(int device, const double* boxes, int n, int*
     };
     BvhBufs b{};
     b.n = n;
+    b.nscenes = 1;  // one scene: no scene ids, traversal from node 0
     b.keys = (unsigned long long*)take(sizeof(unsigned long long) * (size_t)n);
     b.order = (unsigned int*)take(sizeof(unsigned int) * (size_t)n);
     b.child = (int*)take(sizeof(int) * 2 * (size_t)n);
     b.range_hi = (int*)take(sizeof(int) * (size_t)n);
+    b.range_lo = (int*)take(sizeof(int) * (size_t)n);
     b.parent = (int*)take(sizeof(int) * 2 * (size_t)n);
     b.flags = (int*)take(sizeof(int) * (size_t)n);
     b.node_box = (Box6*)take(sizeof(Box6) * (size_t)n);

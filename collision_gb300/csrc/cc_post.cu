@@ -2,12 +2,8 @@
 // a pass's impulses, impact-zone rigid motion, the domain clamp, final
 // positions, strain limiting and final velocities (dcollid.cpp:116-220,
 // 290-310, 486-624, 677-751; dcollid3d.cpp:70-200).
-#include <cooperative_groups.h>
-
 #include "cc_launch.h"
 #include "cc_narrow.cuh"
-
-namespace cg = cooperative_groups;
 
 namespace ccg {
 
@@ -17,13 +13,15 @@ inline int nblk(int n, int t) { return (n + t - 1) / t; }
 
 // computeAverageVelocity, dcollid.cpp:160-220: avgVel = (x_cand - x_old)/dt.
 __global__ void k_step_init(const double* __restrict__ x_old, const double* __restrict__ x_cand, int nv,
-                            const uint8_t* __restrict__ in_elem, double dt, double4_32a* xo, double4_32a* av,
+                            const uint8_t* __restrict__ in_elem, const int* __restrict__ vscene,
+                            const SceneDev* __restrict__ scenes, double4_32a* xo, double4_32a* av,
                             PassCounters* ctr) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nv) return;
     double o[3] = {x_old[3 * p], x_old[3 * p + 1], x_old[3 * p + 2]};
     xo[p] = make_double4_32a(o[0], o[1], o[2], 0.0);
     if (!in_elem[p]) return;
+    const double dt = scenes[vscene[p]].p.dt;
     double v[3];
     bool bad = false;
     for (int j = 0; j < 3; ++j) {
@@ -35,7 +33,7 @@ __global__ void k_step_init(const double* __restrict__ x_old, const double* __re
 }
 
 __global__ void k_contrib_count(const Contrib* __restrict__ c, const PassCounters* ctr, int cap, int* cnt) {
-    if (ctr->err & (kErrContribOverflow | kErrPairOverflow | kErrStack)) return;
+    if (ctr->err & kErrRetry) return;
     int n = ctr->ncontrib < cap ? ctr->ncontrib : cap;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         atomicAdd(&cnt[c[i].vertex], 1);
@@ -43,7 +41,7 @@ __global__ void k_contrib_count(const Contrib* __restrict__ c, const PassCounter
 
 __global__ void k_contrib_scatter(const Contrib* __restrict__ c, const PassCounters* ctr, int cap,
                                   const int* __restrict__ off, int* cur, int* idx) {
-    if (ctr->err & (kErrContribOverflow | kErrPairOverflow | kErrStack)) return;
+    if (ctr->err & kErrRetry) return;
     int n = ctr->ncontrib < cap ? ctr->ncontrib : cap;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         int v = c[i].vertex;
@@ -56,7 +54,7 @@ __global__ void k_contrib_scatter(const Contrib* __restrict__ c, const PassCount
 // as the reference accumulates collsnImpulse and friction.
 __global__ void k_apply(const Contrib* __restrict__ c, PassCounters* ctr, const int* __restrict__ cnt,
                         const int* __restrict__ off, int* idx, int nv, double4_32a* av, uint8_t* has_collsn) {
-    if (ctr->err & (kErrContribOverflow | kErrPairOverflow | kErrStack)) return;
+    if (ctr->err & kErrRetry) return;
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nv) return;
     int n = cnt[p];
@@ -92,55 +90,29 @@ __global__ void k_apply(const Contrib* __restrict__ c, PassCounters* ctr, const 
     has_collsn[p] = 1;
 }
 
-__global__ void k_uf_init(int* parent, int nv) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < nv) parent[p] = p;
-}
-
-__global__ void k_uf_flatten(int* parent, const uint8_t* in_elem, int nv, int* root, int* zcnt) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= nv) return;
-    int r = uf_find(parent, p);
-    root[p] = r;
-    if (in_elem[p]) atomicAdd(&zcnt[r], 1);
-}
-
-__global__ void k_zone_keys(const int* __restrict__ root, const int* __restrict__ zcnt,
-                            const uint8_t* __restrict__ in_elem, int nv, unsigned long long* keys,
-                            unsigned int* vals, int* nmembers) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= nv || !in_elem[p]) return;
-    int r = root[p];
-    if (zcnt[r] < 2) return;
-    int slot = atomicAdd(nmembers, 1);
-    keys[slot] = ((unsigned long long)r << 32) | (unsigned long long)p;
-    vals[slot] = (unsigned int)p;
-}
-
 __device__ __forceinline__ double det3(const double (*a)[3]) {
     return a[0][0] * (a[1][1] * a[2][2] - a[2][1] * a[1][2]) - a[0][1] * (a[1][0] * a[2][2] - a[2][0] * a[1][2]) +
            a[0][2] * (a[1][0] * a[2][1] - a[2][0] * a[1][1]);
 }
 
 // updateImpactListVelocity, dcollid3d.cpp:70-200, one thread per zone over
-// its members in point order; sin and cos correctly rounded, as the
-// reference's libm gives them.
-__global__ void k_zone_solve(const unsigned long long* __restrict__ keys, const unsigned int* __restrict__ vals,
-                             const int* nmembers_p, const uint8_t* __restrict__ fixed,
-                             const double4_32a* __restrict__ xo, double4_32a* av, Params prm, PassCounters* ctr) {
-    int nm = *nmembers_p;
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nm) return;
-    unsigned int zr = (unsigned int)(keys[i] >> 32);
-    if (i > 0 && (unsigned int)(keys[i - 1] >> 32) == zr) return;  // not the zone's first member
-    int end = i;
-    while (end < nm && (unsigned int)(keys[end] >> 32) == zr) ++end;
+// its members in the order of the reference's member list (which fixes the
+// rounding of every sum); sin and cos correctly rounded, as the reference's
+// libm gives them.
+__global__ void k_zone_solve(const int* __restrict__ members, const int* __restrict__ zone_off, int nzones,
+                             const uint8_t* __restrict__ fixed, const double4_32a* __restrict__ xo, double4_32a* av,
+                             const int* __restrict__ vscene, const SceneDev* __restrict__ scenes,
+                             PassCounters* ctr) {
+    int z = blockIdx.x * blockDim.x + threadIdx.x;
+    if (z >= nzones) return;
+    const int i = zone_off[z], end = zone_off[z + 1];
+    const Params prm = scenes[vscene[members[i]]].p;
     const double m = prm.m, dt = prm.dt;
     double x_cm[3] = {0.0, 0.0, 0.0}, v_cm[3] = {0.0, 0.0, 0.0};
     double L[3] = {0.0, 0.0, 0.0}, I[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}}, tmp[3][3];
     int num_pts = end - i;
     for (int q = i; q < end; ++q) {
-        int p = (int)vals[q];
+        int p = members[q];
         double xs[3], vs[3];
         load3(xo, p, xs);
         load3(av, p, vs);
@@ -148,7 +120,7 @@ __global__ void k_zone_solve(const unsigned long long* __restrict__ keys, const 
     }
     for (int d = 0; d < 3; ++d) { x_cm[d] /= num_pts; v_cm[d] /= num_pts; }
     for (int q = i; q < end; ++q) {
-        int p = (int)vals[q];
+        int p = members[q];
         double xs[3], vs[3], dx[3], dv[3], Li[3];
         load3(xo, p, xs);
         load3(av, p, vs);
@@ -158,7 +130,7 @@ __global__ void k_zone_solve(const unsigned long long* __restrict__ keys, const 
         for (int d = 0; d < 3; ++d) L[d] = Li[d] + L[d];
     }
     for (int q = i; q < end; ++q) {
-        int p = (int)vals[q];
+        int p = members[q];
         double xs[3], dx[3];
         load3(xo, p, xs);
         for (int d = 0; d < 3; ++d) dx[d] = xs[d] - x_cm[d];
@@ -183,7 +155,7 @@ __global__ void k_zone_solve(const unsigned long long* __restrict__ keys, const 
     double mag_w = mag3(w);
     bool bad = false;
     for (int q = i; q < end; ++q) {
-        int p = (int)vals[q];
+        int p = members[q];
         if (fixed[p]) continue;
         double xs[3], dx[3], xF[3], xR[3], wxR[3], tmpV[3], x_new[3], nv_[3];
         load3(xo, p, xs);
@@ -216,14 +188,16 @@ __global__ void k_zone_solve(const unsigned long long* __restrict__ keys, const 
 // once per point gives the same result.
 __global__ void k_finalize(const uint8_t* __restrict__ in_elem, const double4_32a* __restrict__ xo, double4_32a* av,
                            uint8_t* has_collsn, const double* __restrict__ x_cand, double* x_out, int nv,
-                           Params prm, double L0, double L1, double L2, double U0, double U1, double U2) {
+                           const int* __restrict__ vscene, const SceneDev* __restrict__ scenes) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nv) return;
     if (!in_elem[p]) {
         for (int j = 0; j < 3; ++j) x_out[3 * p + j] = x_cand[3 * p + j];
         return;
     }
-    double L[3] = {L0, L1, L2}, U[3] = {U0, U1, U2};
+    const SceneDev& sd = scenes[vscene[p]];
+    const Params prm = sd.p;
+    double L[3] = {sd.lo[0], sd.lo[1], sd.lo[2]}, U[3] = {sd.hi[0], sd.hi[1], sd.hi[2]};
     double xs[3], v[3];
     load3(xo, p, xs);
     load3(av, p, v);
@@ -374,26 +348,6 @@ __global__ void k_strain_setup(const StrainEdge* __restrict__ edges, int m, cons
     hot[e] = hh;
 }
 
-__device__ __forceinline__ bool strain_flag(const StrainEdgeStep& ed, const double4_32a* xo, const double4_32a* av,
-                                            double dt) {
-    if (!ed.exact_only) {
-        double4_32a b0 = av[ed.p0], b1 = av[ed.p1];
-        double d0 = (ed.x0[0] + dt * b0.x) - (ed.x1[0] + dt * b1.x);
-        double d1 = (ed.x0[1] + dt * b0.y) - (ed.x1[1] + dt * b1.y);
-        double d2 = (ed.x0[2] + dt * b0.z) - (ed.x1[2] + dt * b1.z);
-        double sn = 0.0;
-        sn += d0 * d0;
-        sn += d1 * d1;
-        sn += d2 * d2;
-        if (sn > 1e-18) {
-            int q0 = strain_quick(sn, ed.rest), q1 = strain_quick(sn, ed.prev);
-            if (q0 == 1 || q1 == 1) return true;
-            if (q0 == 0 && q1 == 0) return false;
-        }
-    }
-    return strain_flag_exact(ed.p0, ed.p1, ed.len0, xo, av, dt);
-}
-
 // The strain decision for given end velocities v0, v1 (bounds first, the
 // exact test of dcollid.cpp:525-530 only inside the bounds' margin).
 __device__ __forceinline__ bool strain_flag_vals(const StrainEdgeStep& ed, const double* v0, const double* v1,
@@ -422,27 +376,6 @@ __device__ __forceinline__ bool strain_flag_vals(const StrainEdgeStep& ed, const
     return true;
 }
 
-__device__ __forceinline__ bool strain_flag_counted(const StrainEdgeStep& ed, const double4_32a* xo,
-                                                    const double4_32a* av, double dt, int* n_exact) {
-    if (!ed.exact_only) {
-        double4_32a b0 = av[ed.p0], b1 = av[ed.p1];
-        double d0 = (ed.x0[0] + dt * b0.x) - (ed.x1[0] + dt * b1.x);
-        double d1 = (ed.x0[1] + dt * b0.y) - (ed.x1[1] + dt * b1.y);
-        double d2 = (ed.x0[2] + dt * b0.z) - (ed.x1[2] + dt * b1.z);
-        double sn = 0.0;
-        sn += d0 * d0;
-        sn += d1 * d1;
-        sn += d2 * d2;
-        if (sn > 1e-18) {
-            int q0 = strain_quick(sn, ed.rest), q1 = strain_quick(sn, ed.prev);
-            if (q0 == 1 || q1 == 1) return true;
-            if (q0 == 0 && q1 == 0) return false;
-        }
-    }
-    ++*n_exact;
-    return strain_flag_exact(ed.p0, ed.p1, ed.len0, xo, av, dt);
-}
-
 // reduceSuperelast, dcollid.cpp:586-596: up to 10 Gauss-Seidel passes over
 // the edges in element order, each averaging the two end velocities of an
 // over-strained edge before the next edge is tested. The edges arrive sorted
@@ -452,9 +385,15 @@ __device__ __forceinline__ bool strain_flag_counted(const StrainEdgeStep& ed, co
 // level-by-level walk below is the reference's sweep, reordered only where
 // the order cannot matter.
 __global__ void __launch_bounds__(256) k_strain(const StrainEdgeStep* __restrict__ edges,
-                                                const int* __restrict__ level_off, int nlevels,
-                                                const double4_32a* __restrict__ xo, double4_32a* av, double dt,
-                                                int* passes_out) {
+                                                const int4* __restrict__ hdr_all,
+                                                const SceneDev* __restrict__ scenes, int slot_cap,
+                                                double4_32a* av, int* passes_out_all) {
+    const SceneDev& sd = scenes[blockIdx.x];
+    if (slot_cap >= 0 && sd.strain_slots <= slot_cap) return;  // swept by k_strain_window
+    const int4* hdr = hdr_all + 2 * sd.strain_hdr0;
+    const int nlevels = sd.strain_levels;
+    const double dt = sd.p.dt;
+    int* passes_out = passes_out_all + 3 * blockIdx.x;
     __shared__ int s_has, s_avg, s_exact;
     if (threadIdx.x == 0) s_avg = s_exact = 0;
     int passes = 0, n_avg = 0, n_exact = 0;
@@ -464,13 +403,22 @@ __global__ void __launch_bounds__(256) k_strain(const StrainEdgeStep* __restrict
         passes++;
         // the records of the next level are loaded before the barrier that
         // ends the current one: they do not depend on the velocities
-        int e = level_off[0] + threadIdx.x, e1 = level_off[1];
+        int e = 0, e1 = 0;
+        if (nlevels > 0) {
+            int4 h = hdr[0];
+            e = h.x + threadIdx.x;
+            e1 = h.y;
+        }
         StrainEdgeStep cur;
         bool have = e < e1;
         if (have) cur = edges[e];
         for (int l = 0; l < nlevels; ++l) {
-            int ne = (l + 1 < nlevels) ? level_off[l + 1] + threadIdx.x : 0;
-            int ne1 = (l + 1 < nlevels) ? level_off[l + 2] : 0;
+            int ne = 0, ne1 = 0;
+            if (l + 1 < nlevels) {
+                int4 h = hdr[2 * (l + 1)];
+                ne = h.x + threadIdx.x;
+                ne1 = h.y;
+            }
             bool nhave = ne < ne1;
             StrainEdgeStep nxt;
             if (nhave) nxt = edges[ne];
@@ -524,6 +472,7 @@ __global__ void __launch_bounds__(256) k_strain(const StrainEdgeStep* __restrict
 // the outward-rounded bounds does the FP64 decision (bounds, then the exact
 // test) run. The averaging itself is FP64, as in the reference.
 constexpr int kWindowAhead = 8;
+constexpr size_t kStrainWindowBytes = 200 * 1024;  // dynamic shared memory of one sweep CTA at most
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
     unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
@@ -691,11 +640,19 @@ __device__ __forceinline__ void win_level(const WinArgs& A, WinRing& r, WinSlot*
 
 __global__ void __launch_bounds__(256) k_strain_window(const StrainEdgeStep* __restrict__ edges,
                                                        const StrainEdgeHot* __restrict__ hot,
-                                                       const int4* __restrict__ hdr, int nlevels,
+                                                       const int4* __restrict__ hdr_all,
+                                                       const SceneDev* __restrict__ scenes, int slot_cap,
                                                        const int2* __restrict__ load_list,
-                                                       const int2* __restrict__ wb_list, int2 wb_final,
-                                                       double4_32a* av, double dt, int* passes_out) {
+                                                       const int2* __restrict__ wb_list,
+                                                       double4_32a* av, int* passes_out_all) {
     extern __shared__ WinSlot s_win[];
+    const SceneDev& sd = scenes[blockIdx.x];
+    if (sd.strain_slots > slot_cap) return;  // swept by k_strain
+    const int4* hdr = hdr_all + 2 * sd.strain_hdr0;
+    const int nlevels = sd.strain_levels;
+    const int2 wb_final = make_int2(sd.wb_final0, sd.wb_final1);
+    const double dt = sd.p.dt;
+    int* passes_out = passes_out_all + 3 * blockIdx.x;
     __shared__ int s_has[2];
     __shared__ int s_avg, s_exact;
     if (threadIdx.x == 0) {
@@ -776,9 +733,11 @@ void math_selftest(int fn, const double* a, const double* b, double* out, int n,
     if (n > 0) count_launch(), k_math_selftest<<<nblk(n, 128), 128, 0, s>>>(fn, a, b, out, n);
 }
 
-void step_init(const double* x_old, const double* x_cand, int nv, const uint8_t* in_elem, double dt, double4_32a* xo,
-               double4_32a* av, PassCounters* ctr, cudaStream_t s) {
-    if (nv > 0) count_launch(), k_step_init<<<nblk(nv, 256), 256, 0, s>>>(x_old, x_cand, nv, in_elem, dt, xo, av, ctr);
+void step_init(const double* x_old, const double* x_cand, int nv, const uint8_t* in_elem, const int* vscene,
+               const SceneDev* scenes, double4_32a* xo, double4_32a* av, PassCounters* ctr, cudaStream_t s) {
+    if (nv > 0)
+        count_launch(), k_step_init<<<nblk(nv, 256), 256, 0, s>>>(x_old, x_cand, nv, in_elem, vscene, scenes, xo, av,
+                                                                  ctr);
 }
 
 void apply_contribs(const Contrib* contrib, const PassCounters* ctr, int contrib_cap, int nv, double4_32a* av,
@@ -791,37 +750,23 @@ void apply_contribs(const Contrib* contrib, const PassCounters* ctr, int contrib
     count_launch(), k_contrib_count<<<blocks, 256, 0, s>>>(contrib, ctr, contrib_cap, b.cnt);
     exclusive_scan(b.cnt, b.off, nv, nullptr, b.scan_temp, s);
     count_launch(), k_contrib_scatter<<<blocks, 256, 0, s>>>(contrib, ctr, contrib_cap, b.off, b.cur, b.idx);
-    count_launch(), k_apply<<<nblk(nv, 128), 128, 0, s>>>(contrib, const_cast<PassCounters*>(ctr), b.cnt, b.off, b.idx, nv, av,
-                                           has_collsn);
+    count_launch(), k_apply<<<nblk(nv, 128), 128, 0, s>>>(contrib, const_cast<PassCounters*>(ctr), b.cnt, b.off,
+                                                          b.idx, nv, av, has_collsn);
 }
 
-void uf_init(int* parent, int nv, cudaStream_t s) {
-    if (nv > 0) count_launch(), k_uf_init<<<nblk(nv, 256), 256, 0, s>>>(parent, nv);
-}
-
-void zone_velocity(int* parent, const uint8_t* in_elem, const uint8_t* fixed, const double4_32a* xo, double4_32a* av,
-                   int nv, const Params& p, ZoneBufs& z, PassCounters* ctr, cudaStream_t s) {
-    if (nv <= 0) return;
-    cudaMemsetAsync(z.zcnt, 0, sizeof(int) * (size_t)nv, s);
-    cudaMemsetAsync(z.nmembers, 0, sizeof(int), s);
-    count_launch(), k_uf_flatten<<<nblk(nv, 256), 256, 0, s>>>(parent, in_elem, nv, z.root, z.zcnt);
-    count_launch(), k_zone_keys<<<nblk(nv, 256), 256, 0, s>>>(z.root, z.zcnt, in_elem, nv, z.keys, z.vals, z.nmembers);
-    int nm = 0;
-    cudaMemcpyAsync(&nm, z.nmembers, sizeof(int), cudaMemcpyDeviceToHost, s);
-    cudaStreamSynchronize(s);
-    if (nm <= 0) return;
-    int bits = 32;
-    while (bits < 64 && ((unsigned long long)(nv - 1) >> (bits - 32)) != 0ull) ++bits;
-    radix_sort_pairs(z.keys, z.vals, nm, bits, z.sort_temp, s);
-    count_launch(), k_zone_solve<<<nblk(nm, 128), 128, 0, s>>>(z.keys, z.vals, z.nmembers, fixed, xo, av, p, ctr);
+void zone_solve(const int* members, const int* zone_off, int nzones, const uint8_t* fixed, const double4_32a* xo,
+                double4_32a* av, const int* vscene, const SceneDev* scenes, PassCounters* ctr, cudaStream_t s) {
+    if (nzones > 0)
+        count_launch(), k_zone_solve<<<nblk(nzones, 128), 128, 0, s>>>(members, zone_off, nzones, fixed, xo, av,
+                                                                       vscene, scenes, ctr);
 }
 
 void finalize_positions(const uint8_t* in_elem, const double4_32a* xo, double4_32a* av, uint8_t* has_collsn,
-                        const double* x_cand, double* x_out, int nv, const Params& p, const double* lo,
-                        const double* hi, cudaStream_t s) {
+                        const double* x_cand, double* x_out, int nv, const int* vscene, const SceneDev* scenes,
+                        cudaStream_t s) {
     if (nv > 0)
-        count_launch(), k_finalize<<<nblk(nv, 256), 256, 0, s>>>(in_elem, xo, av, has_collsn, x_cand, x_out, nv, p, lo[0], lo[1],
-                                                 lo[2], hi[0], hi[1], hi[2]);
+        count_launch(), k_finalize<<<nblk(nv, 256), 256, 0, s>>>(in_elem, xo, av, has_collsn, x_cand, x_out, nv,
+                                                                 vscene, scenes);
 }
 
 size_t strain_step_bytes(int nedges) {
@@ -829,24 +774,25 @@ size_t strain_step_bytes(int nedges) {
     return sizeof(StrainEdgeStep) * n + sizeof(StrainEdgeHot) * n;
 }
 
-void strain_limit(const StrainEdge* edges, int nedges, const int* level_off, int nlevels, const double4_32a* xo,
-                  double4_32a* av, int nv, double dt, void* step_buf, const StrainWindow* win, int* passes_out,
-                  cudaStream_t s) {
-    if (nlevels <= 0) {
-        cudaMemsetAsync(passes_out, 0, sizeof(int), s);
-        return;
-    }
+int strain_window_slot_cap() { return (int)(kStrainWindowBytes / sizeof(WinSlot)); }
+
+void strain_limit(const StrainEdge* edges, int nedges, const int4* hdr, const int2* load_list, const int2* wb_list,
+                  const SceneDev* scenes, int nscenes, const StrainPlan& plan, const double4_32a* xo,
+                  double4_32a* av, void* step_buf, int* passes_out, cudaStream_t s) {
+    if (nscenes <= 0) return;
     StrainEdgeStep* se = (StrainEdgeStep*)step_buf;
-    StrainEdgeHot* hot = (StrainEdgeHot*)(se + nedges);
-    count_launch(), k_strain_setup<<<nblk(nedges, 256), 256, 0, s>>>(edges, nedges, xo, se, hot);
-    if (win && win->nslots > 0 && (size_t)win->nslots * sizeof(WinSlot) <= 200 * 1024) {
-        size_t smem = (size_t)win->nslots * sizeof(WinSlot);
-        cudaFuncSetAttribute(k_strain_window, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        count_launch(), k_strain_window<<<1, 256, smem, s>>>(se, hot, win->hdr, nlevels, win->load_list,
-                                                              win->wb_list, win->wb_final, av, dt, passes_out);
-        return;
+    StrainEdgeHot* hot = (StrainEdgeHot*)(se + (nedges > 0 ? nedges : 1));
+    if (nedges > 0) count_launch(), k_strain_setup<<<nblk(nedges, 256), 256, 0, s>>>(edges, nedges, xo, se, hot);
+    // scenes with at most `cap` slots are swept in shared memory (cap -1: none)
+    int cap = plan.window ? strain_window_slot_cap() : -1;
+    if (plan.window) {
+        size_t smem = (size_t)plan.max_window_slots * sizeof(WinSlot);
+        cudaFuncSetAttribute(k_strain_window, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStrainWindowBytes);
+        count_launch(), k_strain_window<<<nscenes, 256, smem, s>>>(se, hot, hdr, scenes, cap, load_list, wb_list, av,
+                                                                   passes_out);
     }
-    count_launch(), k_strain<<<1, 256, 0, s>>>(se, level_off, nlevels, xo, av, dt, passes_out);
+    if (!plan.window || plan.any_global)
+        count_launch(), k_strain<<<nscenes, 256, 0, s>>>(se, hdr, scenes, cap, av, passes_out);
 }
 
 void final_velocity(const uint8_t* in_elem, const uint8_t* has_collsn, const double4_32a* av, double* vel, int nv,

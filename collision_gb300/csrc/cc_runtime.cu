@@ -1,12 +1,23 @@
 // Host runtime of the collision library: the solver object, the pass loop of
-// resolveCollision (dcollid.cpp:317-362) and the C ABI of
-// include/collision_gb300.h.
-#include <cstdio>
+// resolveCollision (dcollid.cpp:317-362) for a batch of independent scenes,
+// and the C ABI of include/collision_gb300.h.
+//
+// A solver holds one or more scenes. Each scene is one reference
+// CollisionSolver3d: its own mesh, parameters (the reference's class
+// statics), domain box, pair of trees with their shared volume, and pass
+// sequence (proximity, up to five CCD passes, then impact-zone passes until
+// nothing hits). All scenes advance together: every detection pass is one
+// set of launches over the points and elements of all scenes that still have
+// a pass to run, and each scene's state machine steps on the host from its
+// own hit count. A single mesh is the one-scene case of the same code.
 #include <algorithm>
-#include <queue>
+#include <atomic>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <queue>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/collision_gb300.h"
@@ -22,6 +33,10 @@ enum Stage { kStInit, kStBoxes, kStBvh, kStTraverse, kStNarrowProx, kStNarrowCcd
              kStFinalize, kStStrain, kNumStages };
 const char* kStageNames[kNumStages] = {"init", "leaf_boxes", "bvh_build", "traverse", "narrow_prox",
                                        "narrow_ccd", "apply", "zone", "finalize", "strain"};
+
+constexpr int kMaxSceneElems = (1 << 22) - 1;  // leaf ranks fill 22 bits of a contribution key
+constexpr long long kMaxTotal = 1ll << 28;     // points and elements over all scenes
+constexpr int kNumCounters = 16;
 
 template <class T>
 cudaError_t dalloc(T** p, size_t n) {
@@ -39,19 +54,151 @@ void dfree(T*& p) {
 __global__ void k_reset_counters(PassCounters* c) {
     int keep = c->err & kErrNan;
     c->npairs = 0; c->ncontrib = 0; c->nhit_pairs = 0; c->nrec = 0;
-    c->nvisits = 0; c->ncontacts = 0; c->nsub = 0; c->err = keep;
+    c->nvisits = 0; c->ncontacts = 0; c->nsub = 0; c->ncr = 0; c->nunion = 0; c->err = keep;
 }
 
-unsigned long long enc_host(double x) {
-    unsigned long long u;
-    std::memcpy(&u, &x, 8);
-    return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+// Counters and per-scene hit counts of a pass attempt.
+__global__ void k_reset_pass(PassCounters* c, SceneRun* run, int nscenes) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        int keep = c->err & kErrNan;
+        c->npairs = 0; c->ncontrib = 0; c->nhit_pairs = 0; c->nrec = 0;
+        c->nvisits = 0; c->ncontacts = 0; c->nsub = 0; c->ncr = 0; c->nunion = 0; c->err = keep;
+    }
+    if (i < nscenes) run[i].hits = 0;
 }
+
 double dec_host(unsigned long long e) {
     unsigned long long u = (e & 0x8000000000000000ull) ? (e & 0x7fffffffffffffffull) : ~e;
     double x;
     std::memcpy(&x, &u, 8);
     return x;
+}
+
+// Runs f(0..n-1) on up to `threads` host threads.
+template <class F>
+void parallel_for(int n, int threads, F f) {
+    if (threads > n) threads = n;
+    if (threads <= 1) {
+        for (int i = 0; i < n; ++i) f(i);
+        return;
+    }
+    std::atomic<int> next{0};
+    std::vector<std::thread> pool;
+    pool.reserve((size_t)threads);
+    for (int t = 0; t < threads; ++t)
+        pool.emplace_back([&] {
+            for (int i = next++; i < n; i = next++) f(i);
+        });
+    for (auto& th : pool) th.join();
+}
+
+// Where a scene is in the pass sequence of resolveCollision
+// (dcollid.cpp:323-356) during one call.
+enum HostState { kHsDone = 0, kHsProx, kHsCcd, kHsZone };
+
+struct SceneHost {
+    int v0 = 0, nv = 0, e0 = 0, ne = 0;
+    RefTreeOrder tree[2];
+    double volume = 0.0;  // shared by both trees (dcollid.cpp:381, 422)
+    int strain_edges = 0, strain_points = 0;
+    int state = kHsDone;
+    int niter = 0, cd_count = 0, zone_it = 0, hcol = 0, npass = 0;
+    std::vector<int> pass_kinds;
+};
+
+// Appends one scene's strain schedule to the batch arrays. `edges` are the
+// scene's strain edges in the reference's order (elements in order, a
+// triangle's three sides p0p1, p1p2, p2p0), with batch point ids; points
+// are [v0, v0 + nv).
+//
+// Level of an edge = 1 + the level of the last earlier edge at either of
+// its points: edges of one level share no point, so sweeping level by level
+// is the reference's sequential sweep (dcollid.cpp:586-596) reordered only
+// where the order cannot matter. For the shared-memory sweep each point gets
+// a slot for its live interval - from kAhead levels before its first edge to
+// the level after its last one - by interval colouring.
+void append_strain_schedule(const std::vector<StrainEdge>& edges, int v0, int nv, std::vector<StrainEdge>& all_edges,
+                            std::vector<int4>& hdr, std::vector<int2>& load, std::vector<int2>& wb, SceneDev& sd) {
+    const int kAhead = 8;  // kWindowAhead in cc_post.cu
+    const int m = (int)edges.size();
+    std::vector<int> lvl((size_t)m), last((size_t)nv, 0);
+    int nlevels = 0;
+    for (int i = 0; i < m; ++i) {
+        int a = edges[i].p0 - v0, b = edges[i].p1 - v0;
+        int l = 1 + std::max(last[a], last[b]);
+        lvl[i] = l;
+        last[a] = last[b] = l;
+        nlevels = std::max(nlevels, l);
+    }
+    std::vector<int> level_off((size_t)nlevels + 1, 0);
+    for (int i = 0; i < m; ++i) level_off[lvl[i]]++;
+    for (int l = 1; l <= nlevels; ++l) level_off[l] += level_off[l - 1];
+    // level_off[l] = edges of levels <= l = start of (0-based) level l
+    std::vector<StrainEdge> sorted((size_t)m);
+    {
+        std::vector<int> cur(level_off.begin(), level_off.end());
+        for (int i = 0; i < m; ++i) sorted[cur[lvl[i] - 1]++] = edges[i];
+    }
+    std::vector<int> first((size_t)nv, -1), lastl((size_t)nv, -1);
+    for (int l = 0; l < nlevels; ++l)
+        for (int i = level_off[l]; i < level_off[l + 1]; ++i)
+            for (int p : {sorted[i].p0 - v0, sorted[i].p1 - v0}) {
+                if (first[p] < 0) first[p] = l;
+                lastl[p] = l;
+            }
+    std::vector<std::pair<int, int>> order;  // (copy-in level, local point)
+    for (int p = 0; p < nv; ++p)
+        if (first[p] >= 0) order.push_back({std::max(0, first[p] - kAhead), p});
+    std::sort(order.begin(), order.end());
+    std::vector<int> slot((size_t)nv, -1);
+    std::priority_queue<std::pair<int, int>, std::vector<std::pair<int, int>>, std::greater<>> busy;  // (end, slot)
+    std::priority_queue<int, std::vector<int>, std::greater<>> freeq;
+    int nslots = 0;
+    for (auto& lp : order) {
+        while (!busy.empty() && busy.top().first < lp.first) {
+            freeq.push(busy.top().second);
+            busy.pop();
+        }
+        int sl;
+        if (!freeq.empty()) {
+            sl = freeq.top();
+            freeq.pop();
+        } else {
+            sl = nslots++;
+        }
+        slot[lp.second] = sl;
+        busy.push({lastl[lp.second] + 2, sl});
+    }
+    for (auto& ed : sorted) {
+        ed.s0 = slot[ed.p0 - v0];
+        ed.s1 = slot[ed.p1 - v0];
+    }
+    std::vector<int> load_off((size_t)nlevels + 1, 0), wb_off((size_t)nlevels + 2, 0);
+    for (auto& lp : order) load_off[lp.first + 1]++;
+    for (int p = 0; p < nv; ++p)
+        if (first[p] >= 0) wb_off[lastl[p] + 2]++;  // written back at level last + 1
+    for (int l = 0; l < nlevels; ++l) load_off[l + 1] += load_off[l];
+    for (int l = 0; l <= nlevels; ++l) wb_off[l + 1] += wb_off[l];
+    const int ebase = (int)all_edges.size(), lbase = (int)load.size(), wbase = (int)wb.size();
+    load.resize(load.size() + order.size());
+    wb.resize(wb.size() + order.size());
+    {
+        std::vector<int> lc(load_off.begin(), load_off.end()), wc(wb_off.begin(), wb_off.end());
+        for (auto& lp : order) load[lbase + lc[lp.first]++] = int2{v0 + lp.second, slot[lp.second]};
+        for (int p = 0; p < nv; ++p)
+            if (first[p] >= 0) wb[wbase + wc[lastl[p] + 1]++] = int2{v0 + p, slot[p]};
+    }
+    sd.strain_hdr0 = (int)(hdr.size() / 2);
+    sd.strain_levels = nlevels;
+    sd.strain_slots = nslots;
+    for (int l = 0; l < nlevels; ++l) {
+        hdr.push_back(int4{ebase + level_off[l], ebase + level_off[l + 1], lbase + load_off[l], lbase + load_off[l + 1]});
+        hdr.push_back(int4{wbase + wb_off[l], wbase + wb_off[l + 1], 0, 0});
+    }
+    sd.wb_final0 = wbase + wb_off[nlevels];
+    sd.wb_final1 = wbase + wb_off[nlevels + 1];
+    all_edges.insert(all_edges.end(), sorted.begin(), sorted.end());
 }
 
 }  // namespace
@@ -61,8 +208,19 @@ struct cc_solver {
     cudaStream_t stream = nullptr;
     std::string err;
 
-    // topology
-    int nv = 0, nt = 0, nb = 0, ne = 0;
+    // scenes
+    int nscenes = 0;
+    std::vector<SceneHost> scenes;
+    std::vector<SceneDev> h_scenes;
+    bool scenes_dirty = false;
+    SceneDev* d_scenes = nullptr;
+    SceneRun* d_run = nullptr;
+    SceneRun* h_run = nullptr;  // pinned, nscenes
+    int* d_vscene = nullptr;    // scene of every point
+    int* d_escene = nullptr;    // scene of every element
+
+    // topology of all scenes
+    int nv = 0, ne = 0;
     int* d_ev = nullptr;
     int* d_esurf = nullptr;
     uint8_t* d_erigid = nullptr;
@@ -70,11 +228,28 @@ struct cc_solver {
     uint8_t* d_in_elem = nullptr;
     StrainEdge* d_edges = nullptr;
     int nedges = 0;
+    int4* d_strain_hdr = nullptr;
+    int2* d_strain_load = nullptr;
+    int2* d_strain_wb = nullptr;
+    void* d_strain_step = nullptr;
+    int* d_strain_passes = nullptr;  // 3 per scene
+    std::vector<int> h_strain_passes;
 
     // state
     double4_32a* d_xo = nullptr;
     double4_32a* d_av = nullptr;
-    int* d_uf = nullptr;
+    // impact zones: the reference's union-find with member lists
+    // (dcollid.cpp:1015-1059), kept on the host and rebuilt from the
+    // recorded createImpZone calls of each impact-zone pass in visiting order
+    std::vector<int> uf_root, uf_next, uf_tail, uf_w, uf_touched;
+    std::vector<int> h_vscene;
+    UnionRec* d_urec = nullptr;
+    int urec_cap = 0;
+    std::vector<UnionRec> h_urec;
+    std::vector<int> h_members, h_zone_off;
+    int* d_members = nullptr;
+    int* d_zone_off = nullptr;
+    int members_cap = 0, zones_cap = 0;
     // staging for host-buffer calls
     double* d_xold_in = nullptr;
     double* d_xcand_in = nullptr;
@@ -90,43 +265,32 @@ struct cc_solver {
     Contrib* d_contrib = nullptr;
     int contrib_cap = 0;
     ApplyBufs apply{};
-    ZoneBufs zone{};
     PassCounters* d_ctr = nullptr;
     PassCounters* h_ctr = nullptr;
-    unsigned long long* h_bbox = nullptr;
+    unsigned long long* h_bbox = nullptr;  // pinned, 6 per scene
     int* d_rank[2] = {nullptr, nullptr};
-    RefTreeOrder tree[2];
-    double volume = 0.0;
-    int* d_level_off = nullptr;
-    int nlevels = 0;
-    int win_nslots = 0;
-    std::vector<int2> h_win_load, h_win_wb;
-    std::vector<int> h_win_load_off, h_win_wb_off;
-    std::vector<int4> h_win_hdr;
-    int2 h_win_wb_final{0, 0};
-    int4* d_win_hdr = nullptr;
-    int2* d_win_load = nullptr;
-    int* d_win_load_off = nullptr;
-    int2* d_win_wb = nullptr;
-    int* d_win_wb_off = nullptr;
-    void* d_strain_step = nullptr;
-    int* d_strain_passes = nullptr;
     std::vector<Box6> h_boxes;
     std::vector<int> h_rank;
+    float4* d_pbox_lo = nullptr;
+    float4* d_pbox_hi = nullptr;
+    float4* d_p32 = nullptr;
+    float4* d_v32 = nullptr;
 
     // recording
     bool record = false;
     VisitRec* d_rec = nullptr;
     int rec_cap = 0;
     std::vector<VisitRec> visits;
-    std::vector<int> pass_kinds;
 
-    cc_params prm{1e-3, 1e-4, 1e-6, 1000.0, 0.01, 0.02, 0.0};
+    cc_params prm{1e-3, 1e-4, 1e-6, 1000.0, 0.01, 0.02, 0.0};  // for scenes assembled later
     double lo[3] = {-1e30, -1e30, -1e30}, hi[3] = {1e30, 1e30, 1e30};
-    long long counters[13] = {0};
-    int pass_index = 0;
+    long long counters[kNumCounters] = {0};
     bool own_stream = true;
     long long launches_last = 0;
+    int zone_cap = 10000;
+    int mode = 0;  // 0 plain FP64, 1 mixed precision
+    bool strain_window = true;
+    int host_threads = 0;  // tree emulation threads (0: hardware concurrency)
 
     // per-stage GPU time, measured with events on the solver's stream
     bool profiling = false;
@@ -160,39 +324,38 @@ struct cc_solver {
         }
         ev_marks.clear();
     }
-    int zone_cap = 10000;
-    int mode = 0;  // 0 plain FP64, 1 mixed precision
-    bool strain_window = true;
-    float4* d_pbox_lo = nullptr;
-    float4* d_pbox_hi = nullptr;
 
     ~cc_solver() { release(); }
 
     void release_mesh() {
         dfree(d_ev); dfree(d_esurf); dfree(d_erigid); dfree(d_fixed); dfree(d_in_elem); dfree(d_edges);
-        dfree(d_xo); dfree(d_av); dfree(d_uf);
+        dfree(d_strain_hdr); dfree(d_strain_load); dfree(d_strain_wb); dfree(d_strain_passes);
+        if (d_strain_step) cudaFree(d_strain_step);
+        d_strain_step = nullptr;
+        dfree(d_scenes); dfree(d_run); dfree(d_vscene); dfree(d_escene);
+        if (h_run) cudaFreeHost(h_run);
+        h_run = nullptr;
+        if (h_bbox) cudaFreeHost(h_bbox);
+        h_bbox = nullptr;
+        dfree(d_xo); dfree(d_av);
+        dfree(d_urec); dfree(d_members); dfree(d_zone_off);
+        urec_cap = members_cap = zones_cap = 0;
         dfree(d_xold_in); dfree(d_xcand_in); dfree(d_vel); dfree(d_xout); dfree(d_hc);
-        dfree(d_box); dfree(bvh.keys); dfree(bvh.order); dfree(bvh.child); dfree(bvh.range_hi); dfree(bvh.parent);
-        dfree(bvh.flags); dfree(bvh.node_box); dfree(bvh.bbox_enc);
+        dfree(d_box); dfree(bvh.keys); dfree(bvh.order); dfree(bvh.child); dfree(bvh.range_hi);
+        dfree(bvh.range_lo); dfree(bvh.parent); dfree(bvh.flags); dfree(bvh.node_box); dfree(bvh.bbox_enc);
         if (bvh.sort_temp) cudaFree(bvh.sort_temp);
-        bvh.sort_temp = nullptr;
+        bvh = BvhBufs{};
         dfree(d_pairs); dfree(d_contrib);
         dfree(apply.cnt); dfree(apply.off); dfree(apply.cur); dfree(apply.idx);
         if (apply.scan_temp) cudaFree(apply.scan_temp);
         apply.scan_temp = nullptr;
-        dfree(zone.root); dfree(zone.zcnt); dfree(zone.keys); dfree(zone.vals); dfree(zone.nmembers);
-        if (zone.sort_temp) cudaFree(zone.sort_temp);
-        zone.sort_temp = nullptr;
         dfree(d_rank[0]); dfree(d_rank[1]);
-        dfree(d_level_off); dfree(d_strain_passes); dfree(d_rec); dfree(d_pbox_lo); dfree(d_pbox_hi);
-        dfree(d_win_load); dfree(d_win_load_off); dfree(d_win_wb); dfree(d_win_wb_off); dfree(d_win_hdr);
-        win_nslots = 0;
-        if (d_strain_step) cudaFree(d_strain_step);
-        d_strain_step = nullptr;
+        dfree(d_rec); dfree(d_pbox_lo); dfree(d_pbox_hi); dfree(d_p32); dfree(d_v32);
         pair_cap = contrib_cap = rec_cap = 0;
-        nv = nt = nb = ne = nedges = 0;
-        tree[0] = RefTreeOrder();
-        tree[1] = RefTreeOrder();
+        nv = ne = nedges = 0;
+        nscenes = 0;
+        scenes.clear();
+        h_scenes.clear();
     }
 
     void release() {
@@ -200,9 +363,7 @@ struct cc_solver {
         release_mesh();
         dfree(d_ctr);
         if (h_ctr) cudaFreeHost(h_ctr);
-        if (h_bbox) cudaFreeHost(h_bbox);
         h_ctr = nullptr;
-        h_bbox = nullptr;
         for (auto e : ev_pool) cudaEventDestroy(e);
         ev_pool.clear();
         if (stream && own_stream) cudaStreamDestroy(stream);
@@ -239,156 +400,198 @@ struct cc_solver {
         return CC_OK;
     }
 
-    cc_status assemble(const cc_mesh* m);
+    cc_status grow_unions(int cap) {
+        dfree(d_urec);
+        if (dalloc(&d_urec, (size_t)cap) != cudaSuccess) return fail(CC_NO_MEMORY, "union record buffer");
+        urec_cap = cap;
+        return CC_OK;
+    }
+
+    // makeSet for every point (dcollid.cpp:1015-1022), undoing the last
+    // step's unions.
+    void reset_zones() {
+        for (int p : uf_touched) {
+            uf_root[p] = uf_tail[p] = p;
+            uf_next[p] = -1;
+            uf_w[p] = 1;
+        }
+        uf_touched.clear();
+    }
+    // findSet (dcollid.cpp:1024-1031) with path compression.
+    int find_set(int p) {
+        int r = p;
+        while (uf_root[r] != r) r = uf_root[r];
+        while (uf_root[p] != r) {
+            int n = uf_root[p];
+            uf_root[p] = r;
+            p = n;
+        }
+        return r;
+    }
+    // mergePoint (dcollid.cpp:1033-1059): the lighter set joins the heavier
+    // one (the second on equal weights) and its member list is appended.
+    void merge_point(int x, int y) {
+        int px = find_set(x), py = find_set(y);
+        if (px == py) return;
+        if (uf_w[px] > uf_w[py]) std::swap(px, py);
+        // px joins py
+        uf_w[py] += uf_w[px];
+        uf_root[px] = py;
+        uf_next[uf_tail[py]] = px;
+        uf_tail[py] = uf_tail[px];
+    }
+    cc_status zone_pass_unions();
+
+    StrainPlan strain_plan() const {
+        StrainPlan pl{strain_window, 0, false};
+        int cap = strain_window_slot_cap();
+        for (const SceneDev& sd : h_scenes) {
+            if (strain_window && sd.strain_slots <= cap)
+                pl.max_window_slots = std::max(pl.max_window_slots, sd.strain_slots);
+            else
+                pl.any_global = true;
+        }
+        return pl;
+    }
+    void set_scene_params(int i, const cc_params& p) {
+        h_scenes[i].p = Params{p.dt, p.thickness, p.eps, p.k, p.m, p.lambda, p.cr};
+        scenes_dirty = true;
+    }
+    void set_scene_domain(int i, const double* l, const double* h) {
+        for (int d = 0; d < 3; ++d) {
+            h_scenes[i].lo[d] = l[d];
+            h_scenes[i].hi[d] = h[d];
+        }
+        scenes_dirty = true;
+    }
+    void upload_scenes() {
+        if (!scenes_dirty || nscenes == 0) return;
+        cudaMemcpyAsync(d_scenes, h_scenes.data(), sizeof(SceneDev) * (size_t)nscenes, cudaMemcpyHostToDevice, stream);
+        cudaStreamSynchronize(stream);  // h_scenes is pageable and may change after return
+        scenes_dirty = false;
+    }
+
+    cc_status assemble(const cc_mesh* meshes, int n);
     cc_status resolve(const double* x_old, const double* x_cand, double* vel, uint8_t* hc, double* x_out,
                       int* has_collision);
     cc_status resolve_impl(const double* x_old, const double* x_cand, double* vel, uint8_t* hc, double* x_out,
                            int* has_collision);
-    cc_status detect_pass(int moving, int zone_mode, bool* is_collision);
-    cc_status update_tree(int which);
-    Params params() const { return Params{prm.dt, prm.thickness, prm.eps, prm.k, prm.m, prm.lambda, prm.cr}; }
+    cc_status detect_pass(int moving, bool any_zone);
+    cc_status check_ccd(const double* x_old, const double* x_new, long long* hits, int* scene_hits);
+    cc_status update_trees(int which);
 };
 
-cc_status cc_solver::assemble(const cc_mesh* m) {
-    if (!m || m->n_points < 0 || m->n_tris < 0 || m->n_bonds < 0) return fail(CC_BAD_INPUT, "bad mesh sizes");
-    if ((m->n_tris && (!m->tris || !m->tri_rest_len)) || (m->n_bonds && (!m->bonds || !m->bond_rest_len)))
-        return fail(CC_BAD_INPUT, "missing element arrays");
-    long long ne_ll = (long long)m->n_tris + m->n_bonds;
-    if (ne_ll >= (1ll << 22)) return fail(CC_BAD_INPUT, "more than 2^22-1 elements");
+cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
+    if (!meshes || n <= 0) return fail(CC_BAD_INPUT, "no meshes");
+    long long tot_v = 0, tot_e = 0;
+    for (int i = 0; i < n; ++i) {
+        const cc_mesh* m = &meshes[i];
+        if (m->n_points < 0 || m->n_tris < 0 || m->n_bonds < 0) return fail(CC_BAD_INPUT, "bad mesh sizes");
+        if ((m->n_tris && (!m->tris || !m->tri_rest_len)) || (m->n_bonds && (!m->bonds || !m->bond_rest_len)))
+            return fail(CC_BAD_INPUT, "missing element arrays");
+        long long ne_s = (long long)m->n_tris + m->n_bonds;
+        if (ne_s > kMaxSceneElems) return fail(CC_BAD_INPUT, "more than 2^22-1 elements in one scene");
+        tot_v += m->n_points;
+        tot_e += ne_s;
+    }
+    if (tot_v >= kMaxTotal || tot_e >= kMaxTotal) return fail(CC_BAD_INPUT, "more than 2^28 points or elements");
     cudaSetDevice(device);
     release_mesh();
-    nv = m->n_points; nt = m->n_tris; nb = m->n_bonds; ne = nt + nb;
-    std::vector<int> ev((size_t)ne * 3, -1), esurf((size_t)ne, -1);
+    nscenes = n;
+    nv = (int)tot_v;
+    ne = (int)tot_e;
+    scenes.resize((size_t)n);
+    h_scenes.assign((size_t)n, SceneDev{});
+    std::vector<int> ev((size_t)ne * 3, -1), esurf((size_t)ne, -1), vscene((size_t)nv), escene((size_t)ne);
     std::vector<uint8_t> fixed((size_t)nv, 0), in_elem((size_t)nv, 0), erigid((size_t)ne, 0);
-    if (m->fixed)
-        for (int i = 0; i < nv; ++i) fixed[i] = m->fixed[i] ? 1 : 0;
-    for (int t = 0; t < nt; ++t) {
-        for (int k = 0; k < 3; ++k) {
-            int v = m->tris[3 * t + k];
-            if (v < 0 || v >= nv) return fail(CC_BAD_INPUT, "triangle point id out of range");
-            ev[3 * t + k] = v;
+    std::vector<StrainEdge> all_edges;
+    std::vector<int4> hdr;
+    std::vector<int2> load, wb;
+    int v0 = 0, e0 = 0;
+    for (int si = 0; si < n; ++si) {
+        const cc_mesh* m = &meshes[si];
+        const int snv = m->n_points, nt = m->n_tris, nb = m->n_bonds, sne = nt + nb;
+        SceneHost& sh = scenes[si];
+        sh.v0 = v0; sh.nv = snv; sh.e0 = e0; sh.ne = sne;
+        SceneDev& sd = h_scenes[si];
+        sd.p = Params{prm.dt, prm.thickness, prm.eps, prm.k, prm.m, prm.lambda, prm.cr};
+        for (int d = 0; d < 3; ++d) {
+            sd.lo[d] = lo[d];
+            sd.hi[d] = hi[d];
         }
-        if (ev[3 * t] == ev[3 * t + 1] || ev[3 * t] == ev[3 * t + 2] || ev[3 * t + 1] == ev[3 * t + 2])
-            return fail(CC_BAD_INPUT, "triangle with a repeated point");
-        esurf[t] = m->tri_surface ? m->tri_surface[t] : 0;
-    }
-    for (int b = 0; b < nb; ++b) {
-        for (int k = 0; k < 2; ++k) {
-            int v = m->bonds[2 * b + k];
-            if (v < 0 || v >= nv) return fail(CC_BAD_INPUT, "bond point id out of range");
-            ev[3 * (nt + b) + k] = v;
+        sd.v0 = v0; sd.nv = snv; sd.e0 = e0; sd.ne = sne;
+        for (int i = 0; i < snv; ++i) {
+            vscene[v0 + i] = si;
+            fixed[v0 + i] = (m->fixed && m->fixed[i]) ? 1 : 0;
         }
-    }
-    std::vector<StrainEdge> edges;
-    edges.reserve((size_t)3 * nt + nb);
-    for (int e = 0; e < ne; ++e) {
-        int np = e < nt ? 3 : 2;
-        bool rigid = false;
-        for (int i = 0; i < np; ++i) {
-            in_elem[ev[3 * e + i]] = 1;
-            if (fixed[ev[3 * e + i]]) rigid = true;
-        }
-        erigid[e] = rigid ? 1 : 0;
-        if (rigid) continue;  // isRigidBody(hse), dcollid.cpp:495
-        if (np == 3) {
-            for (int j = 0; j < 3; ++j)
-                edges.push_back(StrainEdge{ev[3 * e + j], ev[3 * e + (j + 1) % 3], m->tri_rest_len[3 * e + j], 0, 0});
-        } else {
-            edges.push_back(StrainEdge{ev[3 * e], ev[3 * e + 1], m->bond_rest_len[e - nt], 0, 0});
-        }
-    }
-    nedges = (int)edges.size();
-    // dependency levels of the strain sweep: an edge waits for the last
-    // earlier edge at each of its points
-    std::vector<int> lvl((size_t)nedges), last((size_t)nv, 0);
-    nlevels = 0;
-    for (int i = 0; i < nedges; ++i) {
-        int l = 1 + std::max(last[edges[i].p0], last[edges[i].p1]);
-        lvl[i] = l;
-        last[edges[i].p0] = last[edges[i].p1] = l;
-        if (l > nlevels) nlevels = l;
-    }
-    std::vector<int> level_off((size_t)nlevels + 2, 0);
-    for (int i = 0; i < nedges; ++i) level_off[lvl[i]]++;  // counts at index level (1-based)
-    for (int l = 1; l <= nlevels + 1; ++l) level_off[l] += level_off[l - 1];
-    // level_off[l] now = edges with level <= l; shift to start offsets of level l+1 (0-based)
-    std::vector<StrainEdge> sorted((size_t)nedges);
-    {
-        std::vector<int> cur(level_off.begin(), level_off.end());
-        for (int i = 0; i < nedges; ++i) sorted[cur[lvl[i] - 1]++] = edges[i];
-    }
-    edges.swap(sorted);
-    // shared-memory window of the sweep: each point lives in a slot from a few
-    // levels before its first edge to two levels after its last one
-    {
-        const int ahead = 8;  // kWindowAhead in cc_post.cu
-        std::vector<int> first((size_t)nv, -1), lastl((size_t)nv, -1);
-        for (int l = 0; l < nlevels; ++l)
-            for (int i = level_off[l]; i < level_off[l + 1]; ++i)
-                for (int p : {edges[i].p0, edges[i].p1}) {
-                    if (first[p] < 0) first[p] = l;
-                    lastl[p] = l;
-                }
-        std::vector<std::pair<int, int>> order;  // (load level, point)
-        for (int p = 0; p < nv; ++p)
-            if (first[p] >= 0) order.push_back({std::max(0, first[p] - ahead), p});
-        std::sort(order.begin(), order.end());
-        std::vector<int> slot((size_t)nv, -1);
-        std::priority_queue<std::pair<int, int>, std::vector<std::pair<int, int>>, std::greater<>> busy;  // (end, slot)
-        std::priority_queue<int, std::vector<int>, std::greater<>> freeq;
-        win_nslots = 0;
-        for (auto& lp : order) {
-            int start = lp.first, p = lp.second;
-            while (!busy.empty() && busy.top().first < start) {
-                freeq.push(busy.top().second);
-                busy.pop();
+        for (int t = 0; t < nt; ++t) {
+            int* E = &ev[3 * (size_t)(e0 + t)];
+            for (int k = 0; k < 3; ++k) {
+                int v = m->tris[3 * t + k];
+                if (v < 0 || v >= snv) return fail(CC_BAD_INPUT, "triangle point id out of range");
+                E[k] = v0 + v;
             }
-            int sl;
-            if (!freeq.empty()) {
-                sl = freeq.top();
-                freeq.pop();
+            if (E[0] == E[1] || E[0] == E[2] || E[1] == E[2])
+                return fail(CC_BAD_INPUT, "triangle with a repeated point");
+            esurf[e0 + t] = m->tri_surface ? m->tri_surface[t] : 0;
+        }
+        for (int b = 0; b < nb; ++b) {
+            for (int k = 0; k < 2; ++k) {
+                int v = m->bonds[2 * b + k];
+                if (v < 0 || v >= snv) return fail(CC_BAD_INPUT, "bond point id out of range");
+                ev[3 * (size_t)(e0 + nt + b) + k] = v0 + v;
+            }
+        }
+        std::vector<StrainEdge> edges;
+        edges.reserve((size_t)3 * nt + nb);
+        for (int e = 0; e < sne; ++e) {
+            const int* E = &ev[3 * (size_t)(e0 + e)];
+            int np = e < nt ? 3 : 2;
+            bool rigid = false;
+            escene[e0 + e] = si;
+            for (int i = 0; i < np; ++i) {
+                in_elem[E[i]] = 1;
+                if (fixed[E[i]]) rigid = true;
+            }
+            erigid[e0 + e] = rigid ? 1 : 0;
+            if (rigid) continue;  // isRigidBody(hse), dcollid.cpp:495
+            if (np == 3) {
+                for (int j = 0; j < 3; ++j)
+                    edges.push_back(StrainEdge{E[j], E[(j + 1) % 3], m->tri_rest_len[3 * e + j], 0, 0});
             } else {
-                sl = win_nslots++;
+                edges.push_back(StrainEdge{E[0], E[1], m->bond_rest_len[e - nt], 0, 0});
             }
-            slot[p] = sl;
-            busy.push({lastl[p] + 2, sl});
         }
-        for (auto& ed : edges) {
-            ed.s0 = slot[ed.p0];
-            ed.s1 = slot[ed.p1];
-        }
-        std::vector<int> load_off((size_t)nlevels + 1, 0), wb_off((size_t)nlevels + 2, 0);
-        for (auto& lp : order) load_off[lp.first + 1]++;
-        for (int p = 0; p < nv; ++p)
-            if (first[p] >= 0) wb_off[lastl[p] + 2]++;  // written back at level last + 1
-        for (int l = 0; l < nlevels; ++l) load_off[l + 1] += load_off[l];
-        for (int l = 0; l <= nlevels; ++l) wb_off[l + 1] += wb_off[l];
-        h_win_load.assign(order.size(), int2{0, 0});
-        h_win_wb.assign(order.size(), int2{0, 0});
-        std::vector<int> lc(load_off.begin(), load_off.end()), wc(wb_off.begin(), wb_off.end());
-        for (auto& lp : order) h_win_load[lc[lp.first]++] = int2{lp.second, slot[lp.second]};
-        for (int p = 0; p < nv; ++p)
-            if (first[p] >= 0) h_win_wb[wc[lastl[p] + 1]++] = int2{p, slot[p]};
-        h_win_hdr.assign(2 * (size_t)nlevels, int4{0, 0, 0, 0});
-        for (int l = 0; l < nlevels; ++l) {
-            h_win_hdr[2 * l] = int4{level_off[l], level_off[l + 1], load_off[l], load_off[l + 1]};
-            h_win_hdr[2 * l + 1] = int4{wb_off[l], wb_off[l + 1], 0, 0};
-        }
-        h_win_wb_final = int2{wb_off[nlevels], wb_off[nlevels + 1]};
-        h_win_load_off.swap(load_off);
-        h_win_wb_off.swap(wb_off);
+        size_t nload = load.size();
+        append_strain_schedule(edges, v0, snv, all_edges, hdr, load, wb, sd);
+        sh.strain_edges = (int)edges.size();
+        sh.strain_points = (int)(load.size() - nload);
+        v0 += snv;
+        e0 += sne;
     }
+    nedges = (int)all_edges.size();
 
     bool ok = true;
+    ok &= dalloc(&d_scenes, (size_t)n) == cudaSuccess;
+    ok &= dalloc(&d_run, (size_t)n) == cudaSuccess;
+    ok &= cudaMallocHost(&h_run, sizeof(SceneRun) * (size_t)n) == cudaSuccess;
+    ok &= cudaMallocHost(&h_bbox, 6 * sizeof(unsigned long long) * (size_t)n) == cudaSuccess;
+    ok &= dalloc(&d_vscene, (size_t)nv) == cudaSuccess;
+    ok &= dalloc(&d_escene, (size_t)ne) == cudaSuccess;
     ok &= dalloc(&d_ev, (size_t)ne * 3) == cudaSuccess;
     ok &= dalloc(&d_esurf, (size_t)ne) == cudaSuccess;
     ok &= dalloc(&d_erigid, (size_t)ne) == cudaSuccess;
     ok &= dalloc(&d_fixed, (size_t)nv) == cudaSuccess;
     ok &= dalloc(&d_in_elem, (size_t)nv) == cudaSuccess;
     ok &= dalloc(&d_edges, (size_t)nedges) == cudaSuccess;
+    ok &= dalloc(&d_strain_hdr, hdr.size()) == cudaSuccess;
+    ok &= dalloc(&d_strain_load, load.size()) == cudaSuccess;
+    ok &= dalloc(&d_strain_wb, wb.size()) == cudaSuccess;
+    ok &= dalloc(&d_strain_passes, 3 * (size_t)n) == cudaSuccess;
+    ok &= cudaMalloc(&d_strain_step, strain_step_bytes(nedges)) == cudaSuccess;
     ok &= dalloc(&d_xo, (size_t)nv) == cudaSuccess;
     ok &= dalloc(&d_av, (size_t)nv) == cudaSuccess;
-    ok &= dalloc(&d_uf, (size_t)nv) == cudaSuccess;
+
     ok &= dalloc(&d_xold_in, (size_t)nv * 3) == cudaSuccess;
     ok &= dalloc(&d_xcand_in, (size_t)nv * 3) == cudaSuccess;
     ok &= dalloc(&d_vel, (size_t)nv * 3) == cudaSuccess;
@@ -396,133 +599,147 @@ cc_status cc_solver::assemble(const cc_mesh* m) {
     ok &= dalloc(&d_hc, (size_t)nv) == cudaSuccess;
     ok &= dalloc(&d_box, (size_t)ne) == cudaSuccess;
     bvh.n = ne;
+    bvh.nscenes = n;
+    bvh.elem_scene = nullptr;
     ok &= dalloc(&bvh.keys, (size_t)ne) == cudaSuccess;
     ok &= dalloc(&bvh.order, (size_t)ne) == cudaSuccess;
     ok &= dalloc(&bvh.child, (size_t)2 * ne) == cudaSuccess;
     ok &= dalloc(&bvh.range_hi, (size_t)ne) == cudaSuccess;
+    ok &= dalloc(&bvh.range_lo, (size_t)ne) == cudaSuccess;
     ok &= dalloc(&bvh.parent, (size_t)2 * ne) == cudaSuccess;
     ok &= dalloc(&bvh.flags, (size_t)ne) == cudaSuccess;
     ok &= dalloc(&bvh.node_box, (size_t)ne) == cudaSuccess;
-    ok &= dalloc(&bvh.bbox_enc, 6) == cudaSuccess;
+    ok &= dalloc(&bvh.bbox_enc, 6 * (size_t)n) == cudaSuccess;
     ok &= cudaMalloc(&bvh.sort_temp, radix_sort_temp_bytes(ne > 0 ? ne : 1)) == cudaSuccess;
     ok &= dalloc(&apply.cnt, (size_t)nv) == cudaSuccess;
     ok &= dalloc(&apply.off, (size_t)nv) == cudaSuccess;
     ok &= dalloc(&apply.cur, (size_t)nv) == cudaSuccess;
     ok &= cudaMalloc(&apply.scan_temp, scan_temp_bytes(nv > 0 ? nv : 1)) == cudaSuccess;
-    ok &= dalloc(&zone.root, (size_t)nv) == cudaSuccess;
-    ok &= dalloc(&zone.zcnt, (size_t)nv) == cudaSuccess;
-    ok &= dalloc(&zone.keys, (size_t)nv) == cudaSuccess;
-    ok &= dalloc(&zone.vals, (size_t)nv) == cudaSuccess;
-    ok &= dalloc(&zone.nmembers, 1) == cudaSuccess;
-    ok &= cudaMalloc(&zone.sort_temp, radix_sort_temp_bytes(nv > 0 ? nv : 1)) == cudaSuccess;
     ok &= dalloc(&d_rank[0], (size_t)ne) == cudaSuccess;
     ok &= dalloc(&d_rank[1], (size_t)ne) == cudaSuccess;
-    ok &= dalloc(&d_level_off, (size_t)nlevels + 1) == cudaSuccess;
-    ok &= dalloc(&d_win_load, h_win_load.size()) == cudaSuccess;
-    ok &= dalloc(&d_win_load_off, h_win_load_off.size()) == cudaSuccess;
-    ok &= dalloc(&d_win_wb, h_win_wb.size()) == cudaSuccess;
-    ok &= dalloc(&d_win_wb_off, h_win_wb_off.size()) == cudaSuccess;
-    ok &= dalloc(&d_win_hdr, h_win_hdr.size()) == cudaSuccess;
     ok &= dalloc(&d_pbox_lo, (size_t)nv) == cudaSuccess;
     ok &= dalloc(&d_pbox_hi, (size_t)nv) == cudaSuccess;
-    ok &= cudaMalloc(&d_strain_step, strain_step_bytes(nedges)) == cudaSuccess;
-    ok &= dalloc(&d_strain_passes, 3) == cudaSuccess;
+    ok &= dalloc(&d_p32, (size_t)nv) == cudaSuccess;
+    ok &= dalloc(&d_v32, (size_t)nv) == cudaSuccess;
     if (!ok) return fail(CC_NO_MEMORY, "device allocation failed");
-    cc_status st = grow_pairs(16 * ne + 4096);
+    bvh.elem_scene = d_escene;
+    bvh.scenes = d_scenes;
+    bvh.run = d_run;
+    cc_status st = grow_pairs(8 * ne + 4096);
     if (st) return st;
-    st = grow_contrib(8 * ne + 4096);
+    st = grow_contrib(4 * ne + 4096);
     if (st) return st;
+    cudaMemcpyAsync(d_vscene, vscene.data(), sizeof(int) * vscene.size(), cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d_escene, escene.data(), sizeof(int) * escene.size(), cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d_ev, ev.data(), sizeof(int) * ev.size(), cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d_esurf, esurf.data(), sizeof(int) * esurf.size(), cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d_erigid, erigid.data(), erigid.size(), cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d_fixed, fixed.data(), fixed.size(), cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d_in_elem, in_elem.data(), in_elem.size(), cudaMemcpyHostToDevice, stream);
-    if (nedges) {
-        cudaMemcpyAsync(d_edges, edges.data(), sizeof(StrainEdge) * edges.size(), cudaMemcpyHostToDevice, stream);
-        cudaMemcpyAsync(d_level_off, level_off.data(), sizeof(int) * ((size_t)nlevels + 1), cudaMemcpyHostToDevice,
+    if (nedges)
+        cudaMemcpyAsync(d_edges, all_edges.data(), sizeof(StrainEdge) * all_edges.size(), cudaMemcpyHostToDevice,
                         stream);
-        cudaMemcpyAsync(d_win_load, h_win_load.data(), sizeof(int2) * h_win_load.size(), cudaMemcpyHostToDevice,
-                        stream);
-        cudaMemcpyAsync(d_win_load_off, h_win_load_off.data(), sizeof(int) * h_win_load_off.size(),
-                        cudaMemcpyHostToDevice, stream);
-        cudaMemcpyAsync(d_win_wb, h_win_wb.data(), sizeof(int2) * h_win_wb.size(), cudaMemcpyHostToDevice, stream);
-        cudaMemcpyAsync(d_win_wb_off, h_win_wb_off.data(), sizeof(int) * h_win_wb_off.size(),
-                        cudaMemcpyHostToDevice, stream);
-        cudaMemcpyAsync(d_win_hdr, h_win_hdr.data(), sizeof(int4) * h_win_hdr.size(), cudaMemcpyHostToDevice,
-                        stream);
+    if (!hdr.empty())
+        cudaMemcpyAsync(d_strain_hdr, hdr.data(), sizeof(int4) * hdr.size(), cudaMemcpyHostToDevice, stream);
+    if (!load.empty()) {
+        cudaMemcpyAsync(d_strain_load, load.data(), sizeof(int2) * load.size(), cudaMemcpyHostToDevice, stream);
+        cudaMemcpyAsync(d_strain_wb, wb.data(), sizeof(int2) * wb.size(), cudaMemcpyHostToDevice, stream);
     }
     cudaMemsetAsync(d_av, 0, sizeof(double4_32a) * (size_t)(nv > 0 ? nv : 1), stream);
+    cudaMemsetAsync(d_run, 0, sizeof(SceneRun) * (size_t)n, stream);
     h_boxes.resize((size_t)ne);
     h_rank.resize((size_t)ne);
-    volume = 0.0;
-    cudaStreamSynchronize(stream);
+    h_vscene.swap(vscene);
+    uf_root.resize((size_t)nv);
+    uf_next.assign((size_t)nv, -1);
+    uf_tail.resize((size_t)nv);
+    uf_w.assign((size_t)nv, 1);
+    for (int p = 0; p < nv; ++p) uf_root[p] = uf_tail[p] = p;
+    uf_touched.clear();
+    if (grow_unions(1024)) return CC_NO_MEMORY;
+    h_strain_passes.assign(3 * (size_t)n, 0);
+    scenes_dirty = true;
+    upload_scenes();  // synchronises: the host vectors above are pageable
     return cuda_check("assemble");
 }
 
 // Tree build / rebuild bookkeeping of aabbProximity / aabbCollision
-// (dcollid.cpp:366-428): both trees share one volume; a tree is (re)built
-// on first use or when its root volume has grown by more than 20%.
-cc_status cc_solver::update_tree(int which) {
-    cudaMemcpyAsync(h_bbox, bvh.bbox_enc, 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream);
+// (dcollid.cpp:366-428), per scene in this pass: both trees of a scene share
+// one volume; a tree is (re)built on first use or when its root volume has
+// grown by more than 20%. Rebuilds emulate the reference's insertion order
+// on the host, one scene per host thread.
+cc_status cc_solver::update_trees(int which) {
+    cudaMemcpyAsync(h_bbox, bvh.bbox_enc, 6 * sizeof(unsigned long long) * (size_t)nscenes, cudaMemcpyDeviceToHost,
+                    stream);
     if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("leaf boxes");
-    double rlo[3], rhi[3];
-    for (int d = 0; d < 3; ++d) {
-        rlo[d] = dec_host(h_bbox[d]);
-        rhi[d] = dec_host(h_bbox[3 + d]);
+    std::vector<int> todo;
+    std::vector<double> vol((size_t)nscenes, 0.0);
+    for (int s = 0; s < nscenes; ++s) {
+        if (h_run[s].mode == kSceneIdle) continue;
+        SceneHost& sh = scenes[s];
+        double rlo[3], rhi[3];
+        for (int d = 0; d < 3; ++d) {
+            rlo[d] = dec_host(h_bbox[6 * s + d]);
+            rhi[d] = dec_host(h_bbox[6 * s + 3 + d]);
+        }
+        double v = box_volume(rlo, rhi);
+        if (!sh.tree[which].built() || (v - sh.volume) > 0.2 * sh.volume) todo.push_back(s);
     }
-    double v = box_volume(rlo, rhi);
-    bool rebuild = !tree[which].built() || (v - volume) > 0.2 * volume;
-    if (!rebuild) return CC_OK;
-    cudaMemcpyAsync(h_boxes.data(), d_box, sizeof(Box6) * (size_t)ne, cudaMemcpyDeviceToHost, stream);
+    if (todo.empty()) return CC_OK;
+    for (int s : todo)
+        cudaMemcpyAsync(h_boxes.data() + scenes[s].e0, d_box + scenes[s].e0, sizeof(Box6) * (size_t)scenes[s].ne,
+                        cudaMemcpyDeviceToHost, stream);
     if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("leaf boxes to host");
-    volume = tree[which].build(h_boxes.data(), ne);
-    tree[which].ranks(h_rank.data());
-    cudaMemcpyAsync(d_rank[which], h_rank.data(), sizeof(int) * (size_t)ne, cudaMemcpyHostToDevice, stream);
-    counters[8]++;
+    // largest scenes first: they bound the time of the parallel build
+    std::sort(todo.begin(), todo.end(), [&](int a, int b) { return scenes[a].ne > scenes[b].ne; });
+    int threads = host_threads > 0 ? host_threads : (int)std::thread::hardware_concurrency();
+    if (threads <= 0) threads = 1;
+    parallel_for((int)todo.size(), threads, [&](int i) {
+        SceneHost& sh = scenes[todo[i]];
+        sh.volume = sh.tree[which].build(h_boxes.data() + sh.e0, sh.ne);
+        sh.tree[which].ranks(h_rank.data() + sh.e0);
+    });
+    for (int s : todo)
+        cudaMemcpyAsync(d_rank[which] + scenes[s].e0, h_rank.data() + scenes[s].e0, sizeof(int) * (size_t)scenes[s].ne,
+                        cudaMemcpyHostToDevice, stream);
+    counters[8] += (long long)todo.size();
     return CC_OK;
 }
 
-// One detection pass: boxes, tree bookkeeping, candidate pairs, narrow
-// phase, impulses applied (aabbProximity/aabbCollision + updateAverageVelocity,
-// dcollid.cpp:390-406, 430-468), and in zone mode the rigid zone update
-// (dcollid.cpp:236-262). Retried with larger buffers on overflow.
-cc_status cc_solver::detect_pass(int moving, int zone_mode, bool* is_collision) {
-    int pass = pass_index++;
-    pass_kinds.push_back(moving ? (zone_mode ? kPassZone : kPassCcd) : kPassProx);
-    counters[0]++;
-    if (moving) counters[zone_mode ? 2 : 1]++;
+// One detection pass of every scene that has one to run: boxes, tree
+// bookkeeping, candidate pairs, narrow phase, impulses applied
+// (aabbProximity/aabbCollision + updateAverageVelocity, dcollid.cpp:390-406,
+// 430-468), and for scenes in impact-zone mode the rigid zone update
+// (dcollid.cpp:236-262). Retried with larger buffers on overflow. Leaves
+// every scene's hit count in h_run.
+cc_status cc_solver::detect_pass(int moving, bool any_zone) {
+    cudaMemcpyAsync(d_run, h_run, sizeof(SceneRun) * (size_t)nscenes, cudaMemcpyHostToDevice, stream);
     prof(kStBoxes, true);
-    leaf_boxes(d_ev, ne, nt, d_xo, d_av, prm.dt, moving, d_box, bvh.bbox_enc, stream);
+    leaf_boxes(d_ev, ne, d_escene, d_scenes, nscenes, d_xo, d_av, moving, d_box, bvh.bbox_enc, stream);
     prof(kStBoxes, false);
-    cc_status st = update_tree(moving);
+    cc_status st = update_trees(moving);
     if (st) return st;
     prof(kStBvh, true);
     bvh_build(d_box, bvh, stream);
-    if (mode == 1) point_boxes(d_xo, d_av, prm.dt, nv, moving, d_pbox_lo, d_pbox_hi, stream);
+    if (mode == 1)
+        point_boxes(d_xo, d_av, d_vscene, d_scenes, nv, moving, d_pbox_lo, d_pbox_hi, d_p32, d_v32, stream);
     prof(kStBvh, false);
-    Params p = params();
     for (int attempt = 0; attempt < 8; ++attempt) {
-        count_launch(), k_reset_counters<<<1, 1, 0, stream>>>(d_ctr);
+        count_launch(), k_reset_pass<<<(nscenes + 255) / 256, 256, 0, stream>>>(d_ctr, d_run, nscenes);
         prof(kStTraverse, true);
-        bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream);
+        bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, record ? nullptr : d_ev);
         prof(kStTraverse, false);
         NarrowArgs a;
         a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
-        a.rank = d_rank[moving]; a.nt = nt; a.pass = pass; a.zone = zone_mode; a.p = p; a.pairs = d_pairs;
-        a.contrib = d_contrib; a.contrib_cap = contrib_cap; a.ctr = d_ctr; a.uf_parent = d_uf;
+        a.rank = d_rank[moving]; a.escene = d_escene; a.scenes = d_scenes; a.run = d_run;
+        a.pairs = d_pairs; a.contrib = d_contrib; a.contrib_cap = contrib_cap; a.ctr = d_ctr;
+        a.urec = d_urec; a.urec_cap = urec_cap;
         a.rec = record ? d_rec : nullptr; a.rec_cap = rec_cap;
         a.pbox_lo = mode == 1 ? d_pbox_lo : nullptr;
         a.pbox_hi = mode == 1 ? d_pbox_hi : nullptr;
-        {
-            // h of the sub-tests (thickness for proximity, eps for CCD) and
-            // the barycentric tolerance eps, rounded up to FP32
-            double h = moving ? prm.eps : prm.thickness;
-            float hf = (float)h, ef = (float)prm.eps;
-            if ((double)hf < h) hf = nextafterf(hf, 1e30f);
-            if ((double)ef < prm.eps) ef = nextafterf(ef, 1e30f);
-            a.hpad = hf;
-            a.epad = ef;
-        }
+        a.p32 = d_p32;
+        a.v32 = d_v32;
+        a.check = 0;
         prof(moving ? kStNarrowCcd : kStNarrowProx, true);
         narrow_pass(a, moving, pair_cap, stream);
         prof(moving ? kStNarrowCcd : kStNarrowProx, false);
@@ -530,6 +747,7 @@ cc_status cc_solver::detect_pass(int moving, int zone_mode, bool* is_collision) 
         apply_contribs(d_contrib, d_ctr, contrib_cap, nv, d_av, d_hc, apply, stream);
         prof(kStApply, false);
         cudaMemcpyAsync(h_ctr, d_ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, stream);
+        cudaMemcpyAsync(h_run, d_run, sizeof(SceneRun) * (size_t)nscenes, cudaMemcpyDeviceToHost, stream);
         if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("detection pass");
         int e = h_ctr->err;
         if (e & kErrNan) return fail(CC_NAN_DETECTED, "non-finite velocity or normal (the reference exits here)");
@@ -549,6 +767,11 @@ cc_status cc_solver::detect_pass(int moving, int zone_mode, bool* is_collision) 
             if (st) return st;
             continue;
         }
+        if (e & kErrUnionOverflow) {
+            st = grow_unions(2 * h_ctr->nunion + 1024);
+            if (st) return st;
+            continue;
+        }
         break;
     }
     if (h_ctr->err) return fail(CC_PAIR_OVERFLOW, "buffers kept overflowing");
@@ -557,21 +780,81 @@ cc_status cc_solver::detect_pass(int moving, int zone_mode, bool* is_collision) 
     counters[5] += h_ctr->nhit_pairs;
     counters[6] += h_ctr->ncontacts;
     counters[12] += h_ctr->nsub;
+    if (moving) counters[13] += h_ctr->nvisits;
+    counters[15] += h_ctr->ncr;
     if (record && h_ctr->nrec > 0) {
         size_t base = visits.size();
         visits.resize(base + (size_t)h_ctr->nrec);
         cudaMemcpyAsync(visits.data() + base, d_rec, sizeof(VisitRec) * (size_t)h_ctr->nrec,
                         cudaMemcpyDeviceToHost, stream);
     }
-    if (zone_mode) {
+    if (any_zone) {
         prof(kStZone, true);
-        zone_velocity(d_uf, d_in_elem, d_fixed, d_xo, d_av, nv, p, zone, d_ctr, stream);
+        st = zone_pass_unions();
+        if (st) return st;
         prof(kStZone, false);
         cudaMemcpyAsync(h_ctr, d_ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, stream);
     }
     if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("pass tail");
     if (h_ctr->err & kErrNan) return fail(CC_NAN_DETECTED, "non-finite zone velocity (the reference exits here)");
-    *is_collision = h_ctr->nhit_pairs > 0;
+    return CC_OK;
+}
+
+// The unions of an impact-zone pass and the zones' rigid motion
+// (computeImpactZone, dcollid.cpp:236-262). The pass's createImpZone calls
+// are replayed in the reference's visiting order of each scene - the order
+// decides which point heads each member list and how the lists are
+// concatenated - and every zone of more than one point in a scene in
+// impact-zone mode is solved over its list (updateImpactZoneVelocity,
+// dcollid.cpp:290-310).
+cc_status cc_solver::zone_pass_unions() {
+    int n = h_ctr->nunion;
+    if (n > 0) {
+        h_urec.resize((size_t)n);
+        cudaMemcpyAsync(h_urec.data(), d_urec, sizeof(UnionRec) * (size_t)n, cudaMemcpyDeviceToHost, stream);
+        if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("union records");
+        std::vector<int> ord((size_t)n);
+        for (int i = 0; i < n; ++i) ord[i] = i;
+        std::sort(ord.begin(), ord.end(), [&](int a, int b) {
+            int sa = h_vscene[h_urec[a].p[0]], sb = h_vscene[h_urec[b].p[0]];
+            return sa != sb ? sa < sb : h_urec[a].key < h_urec[b].key;
+        });
+        for (int i : ord) {
+            const int* pts = h_urec[i].p;
+            for (int a = 0; a < 4; ++a) uf_touched.push_back(pts[a]);
+            for (int a = 0; a < 4; ++a)  // createImpZone(pts, 4), dcollid.cpp:473-484
+                for (int b = 0; b < a; ++b) merge_point(pts[a], pts[b]);
+        }
+    }
+    h_members.clear();
+    h_zone_off.clear();
+    for (int p : uf_touched) {
+        if (uf_root[p] != p || uf_w[p] < 2 || uf_w[p] < 0) continue;
+        if (h_run[h_vscene[p]].mode != kSceneZone) continue;
+        uf_w[p] = -uf_w[p];  // listed (restored below)
+        h_zone_off.push_back((int)h_members.size());
+        for (int q = p; q >= 0; q = uf_next[q]) h_members.push_back(q);
+    }
+    int nz = (int)h_zone_off.size();
+    for (int z = 0; z < nz; ++z) {
+        int r = h_members[h_zone_off[z]];
+        uf_w[r] = -uf_w[r];
+    }
+    h_zone_off.push_back((int)h_members.size());
+    if (nz == 0) return CC_OK;
+    if ((int)h_members.size() > members_cap) {
+        dfree(d_members);
+        members_cap = 2 * (int)h_members.size();
+        if (dalloc(&d_members, (size_t)members_cap) != cudaSuccess) return fail(CC_NO_MEMORY, "zone members");
+    }
+    if (nz + 1 > zones_cap) {
+        dfree(d_zone_off);
+        zones_cap = 2 * (nz + 1);
+        if (dalloc(&d_zone_off, (size_t)zones_cap) != cudaSuccess) return fail(CC_NO_MEMORY, "zone offsets");
+    }
+    cudaMemcpyAsync(d_members, h_members.data(), sizeof(int) * h_members.size(), cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d_zone_off, h_zone_off.data(), sizeof(int) * h_zone_off.size(), cudaMemcpyHostToDevice, stream);
+    zone_solve(d_members, d_zone_off, nz, d_fixed, d_xo, d_av, d_vscene, d_scenes, d_ctr, stream);
     return CC_OK;
 }
 
@@ -583,117 +866,173 @@ cc_status cc_solver::resolve(const double* x_old, const double* x_cand, double* 
     return st0;
 }
 
+// resolveCollision (dcollid.cpp:317-362) for every scene: has_collision
+// receives one flag per scene.
 cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, double* vel, uint8_t* hc,
                                   double* x_out, int* has_collision) {
     std::memset(counters, 0, sizeof(counters));
-    pass_index = 0;
     visits.clear();
-    pass_kinds.clear();
-    if (has_collision) *has_collision = 0;
+    if (has_collision)
+        for (int s = 0; s < nscenes; ++s) has_collision[s] = 0;
+    for (auto& sh : scenes) {
+        sh.pass_kinds.clear();
+        sh.state = sh.ne > 0 ? kHsProx : kHsDone;
+        sh.niter = sh.cd_count = sh.zone_it = sh.hcol = sh.npass = 0;
+    }
     if (ne == 0) {
         // the reference dereferences an empty tree here; nothing collides
         if (nv) cudaMemcpyAsync(x_out, x_cand, sizeof(double) * 3 * (size_t)nv, cudaMemcpyDeviceToDevice, stream);
+        reset_zones();
         cudaStreamSynchronize(stream);
         return cuda_check("empty mesh");
     }
+    upload_scenes();
     // d_hc doubles as the device copy of has_collsn
     if (hc != d_hc) cudaMemcpyAsync(d_hc, hc, (size_t)nv, cudaMemcpyDeviceToDevice, stream);
     count_launch(), k_reset_counters<<<1, 1, 0, stream>>>(d_ctr);
     cudaMemsetAsync(&d_ctr->err, 0, sizeof(int), stream);
     ev_marks.clear();
     prof(kStInit, true);
-    step_init(x_old, x_cand, nv, d_in_elem, prm.dt, d_xo, d_av, d_ctr, stream);
-    uf_init(d_uf, nv, stream);
+    step_init(x_old, x_cand, nv, d_in_elem, d_vscene, d_scenes, d_xo, d_av, d_ctr, stream);
+    reset_zones();
     prof(kStInit, false);
-    bool is_coll = false;
-    cc_status st = detect_pass(0, 0, &is_coll);
-    if (st) return st;
-    int hcol = 0;
-    is_coll = true;
-    int niter = 1, cd_count = 0;
-    while (is_coll) {
-        st = detect_pass(1, 0, &is_coll);
+    for (bool first = true;; first = false) {
+        bool any = false, any_zone = false;
+        for (int s = 0; s < nscenes; ++s) {
+            SceneHost& sh = scenes[s];
+            int m = kSceneIdle;
+            if (sh.state == kHsProx) {
+                m = kSceneProx;
+            } else if (sh.state == kHsCcd) {
+                m = kSceneCcd;
+            } else if (sh.state == kHsZone) {
+                if (sh.zone_it++ >= zone_cap) {
+                    char buf[96];
+                    std::snprintf(buf, sizeof(buf), "impact-zone loop of scene %d did not converge", s);
+                    return fail(CC_ITER_CAP, buf);
+                }
+                m = kSceneZone;
+            }
+            h_run[s] = SceneRun{m, 0, sh.npass, -1};
+            if (m == kSceneIdle) continue;
+            any = true;
+            any_zone |= m == kSceneZone;
+            sh.npass++;
+            sh.pass_kinds.push_back(m == kSceneProx ? kPassProx : m == kSceneCcd ? kPassCcd : kPassZone);
+            counters[0]++;
+            if (m == kSceneCcd) counters[1]++;
+            if (m == kSceneZone) counters[2]++;
+        }
+        if (!any) break;
+        // proximity is every scene's first pass, so a pass is all static or all moving
+        cc_status st = detect_pass(first ? 0 : 1, any_zone);
         if (st) return st;
-        if (cd_count++ == 0 && is_coll) hcol = 1;
-        if (++niter > kMaxCcdIter) break;
-    }
-    if (is_coll) {
-        int it = 0;
-        while (is_coll) {
-            if (it++ >= zone_cap) return fail(CC_ITER_CAP, "impact-zone loop did not converge");
-            st = detect_pass(1, 1, &is_coll);
-            if (st) return st;
+        for (int s = 0; s < nscenes; ++s) {
+            SceneHost& sh = scenes[s];
+            bool is_coll = h_run[s].hits > 0;
+            switch (sh.state) {
+                case kHsProx:  // is_collision = true; niter = 1 (dcollid.cpp:333-336)
+                    sh.state = kHsCcd;
+                    sh.niter = 1;
+                    sh.cd_count = 0;
+                    break;
+                case kHsCcd:  // dcollid.cpp:337-344
+                    if (sh.cd_count++ == 0 && is_coll) sh.hcol = 1;
+                    if (!is_coll)
+                        sh.state = kHsDone;
+                    else if (++sh.niter > kMaxCcdIter)
+                        sh.state = kHsZone;  // dcollid.cpp:346-352
+                    break;
+                case kHsZone:
+                    if (!is_coll) sh.state = kHsDone;
+                    break;
+                default:
+                    break;
+            }
         }
     }
-    Params p = params();
     prof(kStFinalize, true);
-    finalize_positions(d_in_elem, d_xo, d_av, d_hc, x_cand, x_out, nv, p, lo, hi, stream);
+    finalize_positions(d_in_elem, d_xo, d_av, d_hc, x_cand, x_out, nv, d_vscene, d_scenes, stream);
     prof(kStFinalize, false);
     prof(kStStrain, true);
-    StrainWindow win{win_nslots, d_win_load, d_win_load_off, d_win_wb, d_win_wb_off, d_win_hdr, h_win_wb_final};
-    strain_limit(d_edges, nedges, d_level_off, nlevels, d_xo, d_av, nv, prm.dt, d_strain_step,
-                 strain_window ? &win : nullptr, d_strain_passes, stream);
+    strain_limit(d_edges, nedges, d_strain_hdr, d_strain_load, d_strain_wb, d_scenes, nscenes, strain_plan(), d_xo,
+                 d_av, d_strain_step, d_strain_passes, stream);
     prof(kStStrain, false);
     final_velocity(d_in_elem, d_hc, d_av, vel, nv, stream);
     if (hc != d_hc) cudaMemcpyAsync(hc, d_hc, (size_t)nv, cudaMemcpyDeviceToDevice, stream);
-    int sp[3] = {0, 0, 0};
-    if (nedges) cudaMemcpyAsync(sp, d_strain_passes, 3 * sizeof(int), cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(h_strain_passes.data(), d_strain_passes, sizeof(int) * h_strain_passes.size(),
+                    cudaMemcpyDeviceToHost, stream);
     if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("finalize");
-    counters[7] = nedges ? sp[0] : 1;
-    counters[10] = sp[1];
-    counters[11] = sp[2];
+    for (int s = 0; s < nscenes; ++s) {
+        // algorithmic bytes of the sweep: per pass, each edge's 48-byte
+        // record and one 32-byte read and write of each point it touches
+        counters[14] += (long long)h_strain_passes[3 * s] *
+                        (48ll * scenes[s].strain_edges + 64ll * scenes[s].strain_points);
+        counters[7] += h_strain_passes[3 * s];
+        counters[10] += h_strain_passes[3 * s + 1];
+        counters[11] += h_strain_passes[3 * s + 2];
+    }
     prof_collect();
-    if (has_collision) *has_collision = hcol;
+    if (has_collision)
+        for (int s = 0; s < nscenes; ++s) has_collision[s] = scenes[s].hcol;
     return cuda_check("resolve");
 }
 
-// ------------------------------------------------------------------ C ABI
-extern "C" {
-
-cc_status cc_create(int device, cc_solver** out) {
-    if (!out) return CC_BAD_INPUT;
-    *out = nullptr;
-    int n = 0;
-    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return CC_CUDA_ERROR;
-    cc_solver* s = new cc_solver;
-    s->device = device;
-    cudaSetDevice(device);
-    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        dalloc(&s->d_ctr, 1) != cudaSuccess || cudaMallocHost(&s->h_ctr, sizeof(PassCounters)) != cudaSuccess ||
-        cudaMallocHost(&s->h_bbox, 6 * sizeof(unsigned long long)) != cudaSuccess) {
-        delete s;
-        return CC_CUDA_ERROR;
+// Exact FP64 re-check of a finished step: every element pair whose swept
+// boxes over [x_old, x_new] overlap goes through the reference's CCD
+// predicate (isCoplanar, then the point-triangle / edge-edge tests with
+// h = eps at each root and at dt; dcollid3d.cpp:203-482, 643-922) with
+// avgVel = (x_new - x_old)/dt, as the next step's first CCD pass would see
+// it, without impulses or zones. A pair that still hits is a missed
+// collision. Uses the solver's pass buffers; the step's state is replaced.
+cc_status cc_solver::check_ccd(const double* x_old, const double* x_new, long long* hits, int* scene_hits) {
+    if (hits) *hits = 0;
+    if (scene_hits)
+        for (int s = 0; s < nscenes; ++s) scene_hits[s] = 0;
+    if (ne == 0) return CC_OK;
+    upload_scenes();
+    count_launch(), k_reset_counters<<<1, 1, 0, stream>>>(d_ctr);
+    cudaMemsetAsync(&d_ctr->err, 0, sizeof(int), stream);
+    step_init(x_old, x_new, nv, d_in_elem, d_vscene, d_scenes, d_xo, d_av, d_ctr, stream);
+    for (int s = 0; s < nscenes; ++s) h_run[s] = SceneRun{scenes[s].ne > 0 ? kSceneCcd : kSceneIdle, 0, 0, -1};
+    cudaMemcpyAsync(d_run, h_run, sizeof(SceneRun) * (size_t)nscenes, cudaMemcpyHostToDevice, stream);
+    leaf_boxes(d_ev, ne, d_escene, d_scenes, nscenes, d_xo, d_av, 1, d_box, bvh.bbox_enc, stream);
+    bvh_build(d_box, bvh, stream);
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        count_launch(), k_reset_pass<<<(nscenes + 255) / 256, 256, 0, stream>>>(d_ctr, d_run, nscenes);
+        bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, d_ev);
+        NarrowArgs a{};
+        a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
+        a.rank = nullptr; a.escene = d_escene; a.scenes = d_scenes; a.run = d_run;
+        a.pairs = d_pairs; a.contrib = d_contrib; a.contrib_cap = contrib_cap; a.ctr = d_ctr;
+        a.urec = nullptr; a.urec_cap = 0;
+        a.rec = nullptr; a.rec_cap = 0; a.pbox_lo = nullptr; a.pbox_hi = nullptr;
+        a.check = 1;
+        narrow_pass(a, 1, pair_cap, stream);
+        cudaMemcpyAsync(h_ctr, d_ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, stream);
+        cudaMemcpyAsync(h_run, d_run, sizeof(SceneRun) * (size_t)nscenes, cudaMemcpyDeviceToHost, stream);
+        if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("ccd check");
+        if (h_ctr->err & kErrPairOverflow) {
+            cc_status st = grow_pairs(2 * h_ctr->npairs + 1024);
+            if (st) return st;
+            continue;
+        }
+        break;
     }
-    cudaMemset(s->d_ctr, 0, sizeof(PassCounters));
-    *out = s;
-    return CC_OK;
+    int e = h_ctr->err;
+    if (e & kErrNan) return fail(CC_NAN_DETECTED, "non-finite velocity or normal in the CCD check");
+    if (e & kErrStack) return fail(CC_STACK_OVERFLOW, "BVH traversal stack overflow");
+    if (e) return fail(CC_PAIR_OVERFLOW, "buffers kept overflowing");
+    if (hits) *hits = h_ctr->nhit_pairs;
+    if (scene_hits)
+        for (int s = 0; s < nscenes; ++s) scene_hits[s] = h_run[s].hits;
+    return cuda_check("ccd check");
 }
 
-void cc_destroy(cc_solver* s) { delete s; }
+namespace {
 
-cc_status cc_assemble(cc_solver* s, const cc_mesh* mesh) {
-    if (!s) return CC_BAD_INPUT;
-    return s->assemble(mesh);
-}
-
-cc_status cc_set_params(cc_solver* s, const cc_params* p) {
-    if (!s || !p) return CC_BAD_INPUT;
-    s->prm = *p;
-    return CC_OK;
-}
-
-cc_status cc_set_domain_boundary(cc_solver* s, const double lo[3], const double hi[3]) {
-    if (!s || !lo || !hi) return CC_BAD_INPUT;
-    for (int d = 0; d < 3; ++d) {
-        s->lo[d] = lo[d];
-        s->hi[d] = hi[d];
-    }
-    return CC_OK;
-}
-
-cc_status cc_resolve(cc_solver* s, const double* x_old, const double* x_cand, double* vel, uint8_t* has_collsn,
-                     double* x_out, int* has_collision) {
-    if (!s) return CC_BAD_INPUT;
+cc_status copy_in_and_resolve(cc_solver* s, const double* x_old, const double* x_cand, double* vel,
+                              uint8_t* has_collsn, double* x_out, int* has_collision) {
     if (s->nv && (!x_old || !x_cand || !vel || !has_collsn || !x_out)) return s->fail(CC_BAD_INPUT, "null array");
     cudaSetDevice(s->device);
     size_t b3 = sizeof(double) * 3 * (size_t)s->nv;
@@ -714,17 +1053,139 @@ cc_status cc_resolve(cc_solver* s, const double* x_old, const double* x_cand, do
     return CC_OK;
 }
 
+// has_collision of a whole solver: any scene's.
+cc_status resolve_any(cc_solver* s, bool host, const double* x_old, const double* x_cand, double* vel,
+                      uint8_t* has_collsn, double* x_out, int* has_collision) {
+    std::vector<int> flags((size_t)(s->nscenes > 0 ? s->nscenes : 1), 0);
+    cc_status st = host ? copy_in_and_resolve(s, x_old, x_cand, vel, has_collsn, x_out, flags.data())
+                        : (cudaSetDevice(s->device), s->resolve(x_old, x_cand, vel, has_collsn, x_out, flags.data()));
+    if (has_collision) {
+        *has_collision = 0;
+        for (int f : flags) *has_collision |= f;
+    }
+    return st;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ C ABI
+extern "C" {
+
+cc_status cc_create(int device, cc_solver** out) {
+    if (!out) return CC_BAD_INPUT;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return CC_CUDA_ERROR;
+    cc_solver* s = new cc_solver;
+    s->device = device;
+    cudaSetDevice(device);
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        dalloc(&s->d_ctr, 1) != cudaSuccess || cudaMallocHost(&s->h_ctr, sizeof(PassCounters)) != cudaSuccess) {
+        delete s;
+        return CC_CUDA_ERROR;
+    }
+    cudaMemset(s->d_ctr, 0, sizeof(PassCounters));
+    *out = s;
+    return CC_OK;
+}
+
+void cc_destroy(cc_solver* s) { delete s; }
+
+cc_status cc_assemble(cc_solver* s, const cc_mesh* mesh) {
+    if (!s) return CC_BAD_INPUT;
+    if (!mesh) return s->fail(CC_BAD_INPUT, "no mesh");
+    return s->assemble(mesh, 1);
+}
+
+cc_status cc_assemble_batch(cc_solver* s, const cc_mesh* meshes, int n_scenes) {
+    if (!s) return CC_BAD_INPUT;
+    return s->assemble(meshes, n_scenes);
+}
+
+int cc_num_scenes(cc_solver* s) { return s ? s->nscenes : -1; }
+
+cc_status cc_get_scene_offsets(cc_solver* s, int32_t* point_off, int32_t* elem_off) {
+    if (!s) return CC_BAD_INPUT;
+    for (int i = 0; i < s->nscenes; ++i) {
+        if (point_off) point_off[i] = s->scenes[i].v0;
+        if (elem_off) elem_off[i] = s->scenes[i].e0;
+    }
+    if (point_off) point_off[s->nscenes] = s->nv;
+    if (elem_off) elem_off[s->nscenes] = s->ne;
+    return CC_OK;
+}
+
+cc_status cc_set_params(cc_solver* s, const cc_params* p) {
+    if (!s || !p) return CC_BAD_INPUT;
+    s->prm = *p;
+    for (int i = 0; i < s->nscenes; ++i) s->set_scene_params(i, *p);
+    return CC_OK;
+}
+
+cc_status cc_set_scene_params(cc_solver* s, int scene, const cc_params* p) {
+    if (!s || !p || scene < 0 || scene >= s->nscenes) return CC_BAD_INPUT;
+    s->set_scene_params(scene, *p);
+    return CC_OK;
+}
+
+cc_status cc_set_domain_boundary(cc_solver* s, const double lo[3], const double hi[3]) {
+    if (!s || !lo || !hi) return CC_BAD_INPUT;
+    for (int d = 0; d < 3; ++d) {
+        s->lo[d] = lo[d];
+        s->hi[d] = hi[d];
+    }
+    for (int i = 0; i < s->nscenes; ++i) s->set_scene_domain(i, lo, hi);
+    return CC_OK;
+}
+
+cc_status cc_set_scene_domain_boundary(cc_solver* s, int scene, const double lo[3], const double hi[3]) {
+    if (!s || !lo || !hi || scene < 0 || scene >= s->nscenes) return CC_BAD_INPUT;
+    s->set_scene_domain(scene, lo, hi);
+    return CC_OK;
+}
+
+cc_status cc_resolve(cc_solver* s, const double* x_old, const double* x_cand, double* vel, uint8_t* has_collsn,
+                     double* x_out, int* has_collision) {
+    if (!s) return CC_BAD_INPUT;
+    return resolve_any(s, true, x_old, x_cand, vel, has_collsn, x_out, has_collision);
+}
+
 cc_status cc_resolve_device(cc_solver* s, const double* x_old, const double* x_cand, double* vel,
                             uint8_t* has_collsn, double* x_out, int* has_collision) {
+    if (!s) return CC_BAD_INPUT;
+    return resolve_any(s, false, x_old, x_cand, vel, has_collsn, x_out, has_collision);
+}
+
+cc_status cc_resolve_batch(cc_solver* s, const double* x_old, const double* x_cand, double* vel,
+                           uint8_t* has_collsn, double* x_out, int* has_collision) {
+    if (!s) return CC_BAD_INPUT;
+    return copy_in_and_resolve(s, x_old, x_cand, vel, has_collsn, x_out, has_collision);
+}
+
+cc_status cc_resolve_batch_device(cc_solver* s, const double* x_old, const double* x_cand, double* vel,
+                                  uint8_t* has_collsn, double* x_out, int* has_collision) {
     if (!s) return CC_BAD_INPUT;
     cudaSetDevice(s->device);
     return s->resolve(x_old, x_cand, vel, has_collsn, x_out, has_collision);
 }
 
+cc_status cc_check_ccd(cc_solver* s, const double* x_old, const double* x_new, long long* hits, int* scene_hits) {
+    if (!s) return CC_BAD_INPUT;
+    if (s->nv && (!x_old || !x_new)) return s->fail(CC_BAD_INPUT, "null array");
+    cudaSetDevice(s->device);
+    return s->check_ccd(x_old, x_new, hits, scene_hits);
+}
+
+cc_status cc_set_host_threads(cc_solver* s, int n) {
+    if (!s || n < 0) return CC_BAD_INPUT;
+    s->host_threads = n;
+    return CC_OK;
+}
+
 int cc_get_counters(cc_solver* s, long long* out, int n) {
     if (!s || !out) return 0;
     s->counters[9] = s->launches_last;
-    int m = n < 13 ? n : 13;
+    int m = n < kNumCounters ? n : kNumCounters;
     for (int i = 0; i < m; ++i) out[i] = s->counters[i];
     return m;
 }
@@ -751,45 +1212,50 @@ int cc_get_visits(cc_solver* s, int* out, int cap) {
     return n;
 }
 
+int cc_get_scene_pass_kinds(cc_solver* s, int scene, int* out, int cap) {
+    if (!s || scene < 0 || scene >= s->nscenes) return -1;
+    const std::vector<int>& k = s->scenes[scene].pass_kinds;
+    int n = (int)k.size();
+    if (out)
+        for (int i = 0; i < n && i < cap; ++i) out[i] = k[i];
+    return n;
+}
+
 int cc_get_pass_kinds(cc_solver* s, int* out, int cap) {
     if (!s) return -1;
-    int n = (int)s->pass_kinds.size();
-    if (out)
-        for (int i = 0; i < n && i < cap; ++i) out[i] = s->pass_kinds[i];
-    return n;
+    if (s->nscenes == 0) return 0;
+    return cc_get_scene_pass_kinds(s, 0, out, cap);
 }
 
 cc_status cc_get_zone_roots(cc_solver* s, int* out) {
     if (!s || !out) return CC_BAD_INPUT;
-    cudaSetDevice(s->device);
-    if (s->nv == 0) return CC_OK;
-    std::vector<int> parent((size_t)s->nv);
-    cudaMemcpyAsync(parent.data(), s->d_uf, sizeof(int) * (size_t)s->nv, cudaMemcpyDeviceToHost, s->stream);
-    if (cudaStreamSynchronize(s->stream) != cudaSuccess) return s->cuda_check("zone roots");
-    for (int i = 0; i < s->nv; ++i) {
-        int r = i, guard = 0;
-        while (parent[r] != r && guard++ < s->nv) r = parent[r];
-        out[i] = r;
-    }
+    for (int i = 0; i < s->nv; ++i) out[i] = s->find_set(i);
     return CC_OK;
 }
 
 cc_status cc_get_leaf_ranks(cc_solver* s, int which, int* out) {
-    if (!s || !out || which < 0 || which > 1 || !s->tree[which].built()) return CC_BAD_INPUT;
-    s->tree[which].ranks(out);
+    if (!s || !out || which < 0 || which > 1) return CC_BAD_INPUT;
+    for (const SceneHost& sh : s->scenes)
+        if (sh.ne > 0 && !sh.tree[which].built()) return CC_BAD_INPUT;
+    for (const SceneHost& sh : s->scenes)
+        if (sh.ne > 0) sh.tree[which].ranks(out + sh.e0);
     return CC_OK;
 }
 
 int cc_debug_candidate_pairs(cc_solver* s, int moving, int brute_force, int* out, int cap) {
     if (!s || s->ne == 0) return 0;
     cudaSetDevice(s->device);
-    leaf_boxes(s->d_ev, s->ne, s->nt, s->d_xo, s->d_av, s->prm.dt, moving, s->d_box, s->bvh.bbox_enc, s->stream);
+    s->upload_scenes();
+    for (int i = 0; i < s->nscenes; ++i) s->h_run[i] = SceneRun{moving ? kSceneCcd : kSceneProx, 0, 0, -1};
+    cudaMemcpyAsync(s->d_run, s->h_run, sizeof(SceneRun) * (size_t)s->nscenes, cudaMemcpyHostToDevice, s->stream);
+    leaf_boxes(s->d_ev, s->ne, s->d_escene, s->d_scenes, s->nscenes, s->d_xo, s->d_av, moving, s->d_box,
+               s->bvh.bbox_enc, s->stream);
     if (!brute_force) bvh_build(s->d_box, s->bvh, s->stream);
     for (int attempt = 0; attempt < 8; ++attempt) {
         count_launch(), k_reset_counters<<<1, 1, 0, s->stream>>>(s->d_ctr);
         cudaMemsetAsync(&s->d_ctr->err, 0, sizeof(int), s->stream);
         if (brute_force)
-            brute_pairs(s->d_box, s->ne, s->d_pairs, s->pair_cap, s->d_ctr, s->stream);
+            brute_pairs(s->d_box, s->ne, s->d_escene, s->d_pairs, s->pair_cap, s->d_ctr, s->stream);
         else
             bvh_pairs(s->d_box, s->bvh, s->d_pairs, s->pair_cap, s->d_ctr, s->stream);
         cudaMemcpyAsync(s->h_ctr, s->d_ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, s->stream);

@@ -114,6 +114,115 @@ class CollisionSolver3d:
         self.setParams(scene.params)
         self.setDomainBoundary(scene.domain[:3], scene.domain[3:])
 
+    # ------------------------------------------------------------ batches
+    def assembleBatch(self, meshes):
+        """Several independent scenes in one solver. `meshes` holds dicts with
+        the keyword arguments of assembleFromMesh, or Scene objects (whose
+        parameters and domain boxes are applied per scene). Points and
+        elements are numbered scene by scene (sceneOffsets)."""
+        from .scenes import Scene
+        keep, cms, scene_objs = [], [], []
+        for m in meshes:
+            if isinstance(m, Scene):
+                scene_objs.append(m)
+                m = dict(n_points=m.nv, tris=m.tris, tri_surface=m.tri_surf, tri_rest=m.tri_rest, bonds=m.bonds,
+                         bond_rest=m.bond_rest, fixed=m.fixed)
+            else:
+                scene_objs.append(None)
+            n_points = int(m["n_points"])
+            tris = _c(m.get("tris") if m.get("tris") is not None else np.zeros((0, 3)), np.int32).reshape(-1, 3)
+            nt = tris.shape[0]
+            ts = m.get("tri_surface")
+            ts = _c(ts if ts is not None else np.zeros(nt), np.int32)
+            tr = m.get("tri_rest")
+            tr = _c(tr if tr is not None else np.zeros((nt, 3)), np.float64).reshape(-1, 3)
+            bonds = _c(m.get("bonds") if m.get("bonds") is not None else np.zeros((0, 2)), np.int32).reshape(-1, 2)
+            nb = bonds.shape[0]
+            br = m.get("bond_rest")
+            br = _c(br if br is not None else np.zeros(nb), np.float64)
+            fx = m.get("fixed")
+            fx = _c(fx if fx is not None else np.zeros(n_points), np.uint8)
+            keep.append((tris, ts, tr, bonds, br, fx))
+            cms.append(_lib.cc_mesh(n_points, nt, tris.ctypes.data, ts.ctypes.data, tr.ctypes.data, nb,
+                                    bonds.ctypes.data, br.ctypes.data, fx.ctypes.data))
+        arr = (_lib.cc_mesh * len(cms))(*cms)
+        self._check(self._lib.cc_assemble_batch(self._h, arr, len(cms)))
+        self._keep = keep
+        off_v, off_e = self.sceneOffsets()
+        self._nv = int(off_v[-1])
+        self._ne = int(off_e[-1])
+        for i, sc in enumerate(scene_objs):
+            if sc is not None:
+                self.setSceneParams(i, sc.params)
+                self.setSceneDomainBoundary(i, sc.domain[:3], sc.domain[3:])
+
+    def numScenes(self) -> int:
+        return int(self._lib.cc_num_scenes(self._h))
+
+    def sceneOffsets(self):
+        """(point offsets, element offsets), n_scenes + 1 entries each."""
+        n = self.numScenes()
+        pv = np.zeros(n + 1, dtype=np.int32)
+        pe = np.zeros(n + 1, dtype=np.int32)
+        self._check(self._lib.cc_get_scene_offsets(self._h, pv.ctypes.data_as(C.POINTER(C.c_int)),
+                                                   pe.ctypes.data_as(C.POINTER(C.c_int))))
+        return pv, pe
+
+    def setSceneParams(self, scene: int, params: dict):
+        vals = dict(self._params)
+        vals.update({k: float(v) for k, v in params.items() if k in PARAM_NAMES})
+        p = _lib.cc_params(*[float(vals[k]) for k in PARAM_NAMES])
+        self._check(self._lib.cc_set_scene_params(self._h, int(scene), C.byref(p)))
+
+    def setSceneDomainBoundary(self, scene: int, L, U):
+        lo = _c(L, np.float64)
+        hi = _c(U, np.float64)
+        self._check(self._lib.cc_set_scene_domain_boundary(self._h, int(scene), lo.ctypes.data, hi.ctypes.data))
+
+    def setHostThreads(self, n: int):
+        self._check(self._lib.cc_set_host_threads(self._h, int(n)))
+
+    def resolveCollisionBatch(self, x_old, x_cand, vel, has_collsn):
+        """resolveCollision() on every scene (host arrays over all scenes'
+        points). Returns (x_new, vel, has_collsn, has_collision per scene)."""
+        x_old = _c(x_old, np.float64)
+        x_cand = _c(x_cand, np.float64)
+        vel = np.array(vel, dtype=np.float64, copy=True, order="C")
+        hc = np.array(has_collsn, dtype=np.uint8, copy=True, order="C")
+        x_out = np.empty_like(x_old)
+        hcol = np.zeros(max(self.numScenes(), 1), dtype=np.int32)
+        self._check(self._lib.cc_resolve_batch(self._h, x_old.ctypes.data, x_cand.ctypes.data, vel.ctypes.data,
+                                               hc.ctypes.data, x_out.ctypes.data,
+                                               hcol.ctypes.data_as(C.POINTER(C.c_int))))
+        self._has_collision = bool(hcol.any())
+        return x_out, vel, hc, hcol.astype(bool)
+
+    def resolveCollisionBatchDevice(self, x_old, x_cand, vel, has_collsn, x_out):
+        """resolveCollision() on every scene, device tensors as in
+        resolveCollisionDevice. Returns has_collision per scene."""
+        hcol = np.zeros(max(self.numScenes(), 1), dtype=np.int32)
+        self._check(self._lib.cc_resolve_batch_device(self._h, x_old.data_ptr(), x_cand.data_ptr(), vel.data_ptr(),
+                                                      has_collsn.data_ptr(), x_out.data_ptr(),
+                                                      hcol.ctypes.data_as(C.POINTER(C.c_int))))
+        self._has_collision = bool(hcol.any())
+        return hcol.astype(bool)
+
+    def checkCCD(self, x_old, x_new):
+        """Exact FP64 CCD re-check of a finished step on device tensors:
+        (element pairs that still collide, per-scene counts)."""
+        hits = C.c_longlong(0)
+        per = np.zeros(max(self.numScenes(), 1), dtype=np.int32)
+        self._check(self._lib.cc_check_ccd(self._h, x_old.data_ptr(), x_new.data_ptr(), C.byref(hits),
+                                           per.ctypes.data_as(C.POINTER(C.c_int))))
+        return int(hits.value), per
+
+    def scenePassKinds(self, scene: int) -> np.ndarray:
+        n = self._lib.cc_get_scene_pass_kinds(self._h, int(scene), None, 0)
+        out = np.zeros(max(n, 0), dtype=np.int32)
+        if n > 0:
+            self._lib.cc_get_scene_pass_kinds(self._h, int(scene), out.ctypes.data_as(C.POINTER(C.c_int)), n)
+        return out
+
     # -------------------------------------------------------------- step
     def resolveCollision(self, x_old, x_cand, vel, has_collsn):
         """One resolveCollision() on host arrays. Returns (x_new, vel, has_collsn)."""
@@ -166,11 +275,12 @@ class CollisionSolver3d:
     # ------------------------------------------------------- inspection
     COUNTER_NAMES = ("passes", "ccd_passes", "zone_passes", "candidate_pairs", "visits", "hit_pairs",
                      "contacts", "strain_passes", "tree_builds", "kernel_launches", "strain_averaged",
-                     "strain_exact", "fp64_subtests")
+                     "strain_exact", "fp64_subtests", "moving_visits", "strain_bytes", "cr_roots")
 
     def counters(self) -> dict:
-        out = (C.c_longlong * 13)()
-        n = self._lib.cc_get_counters(self._h, out, 13)
+        n_all = len(self.COUNTER_NAMES)
+        out = (C.c_longlong * n_all)()
+        n = self._lib.cc_get_counters(self._h, out, n_all)
         return dict(zip(self.COUNTER_NAMES[:n], list(out)[:n]))
 
     def setRecording(self, on: bool):

@@ -116,6 +116,54 @@ cc_status cc_resolve(cc_solver* s, const double* x_old, const double* x_cand, do
 cc_status cc_resolve_device(cc_solver* s, const double* x_old, const double* x_cand, double* vel,
                             uint8_t* has_collsn, double* x_out, int* has_collision);
 
+/*
+ * Batches: several independent scenes resolved together, each with its own
+ * mesh, parameters, domain box, trees and pass sequence - as if each were
+ * its own CollisionSolver3d and resolveCollision() were called on each.
+ * No counterpart in the reference, whose solver state is static
+ * (collid.h:134-140) and so holds one scene per process.
+ *
+ * cc_assemble_batch replaces the solver's mesh by n_scenes meshes. Points
+ * and elements of all scenes are numbered scene by scene: the arrays of the
+ * resolve calls hold scene 0's points, then scene 1's, and so on;
+ * cc_get_scene_offsets gives the first point and first element of each
+ * scene (n_scenes + 1 entries each, the last being the totals; either
+ * pointer may be NULL). Every scene starts with the solver's current
+ * parameters and domain box; cc_set_params and cc_set_domain_boundary set
+ * all scenes, the _scene_ forms one. cc_assemble is cc_assemble_batch with
+ * one mesh.
+ */
+cc_status cc_assemble_batch(cc_solver* s, const cc_mesh* meshes, int n_scenes);
+int cc_num_scenes(cc_solver* s);
+cc_status cc_get_scene_offsets(cc_solver* s, int32_t* point_off, int32_t* elem_off);
+cc_status cc_set_scene_params(cc_solver* s, int scene, const cc_params* p);
+cc_status cc_set_scene_domain_boundary(cc_solver* s, int scene, const double lo[3], const double hi[3]);
+
+/* resolveCollision on every scene of the batch, as cc_resolve (host
+ * buffers) and cc_resolve_device (device buffers), with has_collision
+ * holding one flag per scene (may be NULL). cc_resolve and
+ * cc_resolve_device on a batch report whether any scene collided. */
+cc_status cc_resolve_batch(cc_solver* s, const double* x_old, const double* x_cand, double* vel,
+                           uint8_t* has_collsn, double* x_out, int* has_collision);
+cc_status cc_resolve_batch_device(cc_solver* s, const double* x_old, const double* x_cand, double* vel,
+                                  uint8_t* has_collsn, double* x_out, int* has_collision);
+
+/* Exact FP64 re-check of a finished step (device arrays, all scenes): every
+ * element pair whose swept boxes over [x_old, x_new] overlap goes through
+ * the reference's CCD predicate (isCoplanar and the point-triangle /
+ * edge-edge tests with h = eps, dcollid3d.cpp:203-482, 643-922) with
+ * avgVel = (x_new - x_old)/dt, without impulses. *hits receives the number
+ * of element pairs that still collide (0 for a fully resolved step),
+ * scene_hits (may be NULL) the count per scene. No counterpart in the
+ * reference. Replaces the solver's per-step device state (zone roots and
+ * recorded visits are kept). */
+cc_status cc_check_ccd(cc_solver* s, const double* x_old, const double* x_new, long long* hits, int* scene_hits);
+
+/* Host threads that emulate the reference's tree insertion order when a
+ * scene's tree is (re)built, one scene per thread (0 = one per hardware
+ * thread, the default). */
+cc_status cc_set_host_threads(cc_solver* s, int n);
+
 /* Arithmetic of the narrow phase:
  *   0  plain FP64 (default): every sub-test evaluated in FP64 as the reference
  *   1  mixed precision: FP32 swept boxes of each sub-test's points, rounded
@@ -129,11 +177,16 @@ cc_status cc_set_mode(cc_solver* s, int mode);
  * Both give the same results. */
 cc_status cc_set_strain_window(cc_solver* s, int on);
 
-/* Counters of the last step, in this order: detection passes, CCD passes,
- * impact-zone passes, candidate pairs (all passes), narrow-phase visits,
- * pairs that hit, contacts (sub-tests that applied an impulse), strain
- * passes, tree builds, kernel launches, strain edges averaged, strain tests
- * taken the exact way, sub-tests evaluated in FP64. Returns how many were
+/* Counters of the last step, summed over the scenes of a batch, in this
+ * order: detection passes, CCD passes, impact-zone passes, candidate pairs
+ * (all passes), narrow-phase visits, pairs that hit, contacts (sub-tests
+ * that applied an impulse), strain passes, tree builds, kernel launches,
+ * strain edges averaged, strain tests taken the exact way, sub-tests
+ * evaluated in FP64, narrow-phase visits of CCD and impact-zone passes,
+ * algorithmic bytes of the strain sweeps, coplanarity cubics whose roots
+ * were formed again with correctly rounded functions. Candidate pairs and
+ * visits leave out pairs of elements that share a point (their tests
+ * return false at once) unless recording is on. Returns how many were
  * written. */
 int cc_get_counters(cc_solver* s, long long* out, int n);
 
@@ -142,11 +195,15 @@ int cc_get_counters(cc_solver* s, long long* out, int n);
  * rank_b, rank_a; a/b as the reference calls TriToTri/TriToBond/BondToBond). */
 cc_status cc_set_recording(cc_solver* s, int on);
 int cc_get_visits(cc_solver* s, int* out, int cap);
+/* Kinds (0 proximity, 1 CCD, 2 impact zone) of the last step's passes of
+ * scene 0, or of the given scene; returns the number of passes. Visit
+ * records carry their scene's pass index and batch element ids. */
 int cc_get_pass_kinds(cc_solver* s, int* out, int cap);
+int cc_get_scene_pass_kinds(cc_solver* s, int scene, int* out, int cap);
 /* Impact-zone root of every point after the last step. */
 cc_status cc_get_zone_roots(cc_solver* s, int* out);
-/* Leaf rank of every element in the proximity (which=0) or collision
- * (which=1) tree; CC_BAD_INPUT while that tree is unbuilt. */
+/* Leaf rank of every element in its scene's proximity (which=0) or
+ * collision (which=1) tree; CC_BAD_INPUT while one of them is unbuilt. */
 cc_status cc_get_leaf_ranks(cc_solver* s, int which, int* out);
 
 /* Candidate pairs of the current state (after cc_resolve: the final x_old

@@ -1,0 +1,215 @@
+"""Batched path: several independent scenes resolved together.
+
+A batch must give every scene exactly what a solver holding that scene alone
+gives it (same bits: the per-scene arithmetic, trees, pass sequence and
+summation order do not depend on the other scenes), and so, through the
+single-scene parity tests, what the reference gives it. Checked here on a
+mix of sizes, element kinds and parameters, with scenes that finish after
+one CCD pass next to scenes that need impact zones, plus an empty scene.
+"""
+import numpy as np
+import pytest
+
+from collision_gb300 import scenes
+from tests.gpu_util import record_sha, rel_err, zone_labels
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12
+
+
+def _points_only(n=7, seed=3):
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-1, 1, size=(n, 3))
+    return scenes.Scene("points_only", x, rng.uniform(-1, 1, size=(n, 3)), np.zeros(n, np.uint8),
+                        np.zeros((0, 3), np.int32), np.zeros(0, np.int32), np.zeros((0, 3)),
+                        np.zeros((0, 2), np.int32), np.zeros(0, np.int32), np.zeros(0),
+                        np.array([-10, -10, -10, 10, 10, 10], np.float64), dict(scenes.DEFAULTS))
+
+
+def _mix():
+    out = [
+        scenes.cloth_on_obstacle(10, "sphere", 0.2, 1.5, seed=1),
+        scenes.folded_cloth(n=17, seed=1),
+        scenes.cloth_on_obstacle(14, "box", 0.2, 2.5, seed=2),
+        _points_only(),
+        scenes.strings(nstr=4, nseg=32, seed=4),
+        scenes.cloth_on_sphere(n=12, speed=3.0, seed=5),
+    ]
+    # a tight domain box on one scene exercises the per-scene clamp
+    out[2].domain = np.array([-0.6, -0.6, -0.01, 0.6, 0.6, 1.0])
+    return out
+
+
+@pytest.fixture(scope="module")
+def solver_cls():
+    import torch
+    assert torch.cuda.is_available()
+    from collision_gb300.solver import CollisionSolver3d
+    return CollisionSolver3d
+
+
+def _split(a, off, i):
+    return a[off[i]:off[i + 1]]
+
+
+def _run_batch(solver_cls, mix, nsteps, mode=0, window=True, record=False):
+    b = solver_cls(0)
+    b.assembleBatch(mix)
+    b.setMode(mode)
+    b.setStrainWindow(window)
+    b.setRecording(record)
+    pv, pe = b.sceneOffsets()
+    x = np.concatenate([s.x for s in mix])
+    v = np.concatenate([s.v for s in mix])
+    hc = np.zeros(len(x), np.uint8)
+    dt = np.concatenate([np.full(s.nv, s.params["dt"]) for s in mix])[:, None]
+    steps = []
+    for _ in range(nsteps):
+        xc = x + dt * v
+        xo, vo, ho, hcol = b.resolveCollisionBatch(x, xc, v, hc)
+        info = dict(x_in=x, xc=xc, v_in=v, hc_in=hc, x=xo, v=vo, hc=ho, hcol=hcol,
+                    kinds=[b.scenePassKinds(i) for i in range(len(mix))],
+                    zones=b.zoneRoots(), visits=b.visits() if record else None)
+        steps.append(info)
+        x, v, hc = xo, vo, ho
+    b.close()
+    return steps, pv, pe
+
+
+def test_batch_equals_single_scenes(solver_cls):
+    from collision_gb300.solver import ordered_visits
+    mix = _mix()
+    steps, pv, pe = _run_batch(solver_cls, mix, 12, record=True)
+    for i, sc in enumerate(mix):
+        s = solver_cls(0)
+        s.assembleFromScene(sc)
+        s.setRecording(True)
+        for k, st in enumerate(steps):
+            xs, vs, hs = s.resolveCollision(_split(st["x_in"], pv, i), _split(st["xc"], pv, i),
+                                            _split(st["v_in"], pv, i), _split(st["hc_in"], pv, i))
+            tag = f"scene {i} ({sc.name}) step {k}"
+            assert np.array_equal(xs, _split(st["x"], pv, i)), tag
+            assert np.array_equal(vs, _split(st["v"], pv, i)), tag
+            assert np.array_equal(hs, _split(st["hc"], pv, i)), tag
+            assert s.hasCollision() == bool(st["hcol"][i]), tag
+            assert np.array_equal(s.passKinds(), st["kinds"][i]), tag
+            assert np.array_equal(zone_labels(_split(st["zones"], pv, i) - pv[i]), zone_labels(s.zoneRoots())), tag
+            bv = st["visits"]
+            mine = bv[(bv[:, 2] >= pe[i]) & (bv[:, 2] < pe[i + 1])].copy()
+            mine[:, 2:4] -= pe[i]
+            assert record_sha(ordered_visits(mine)) == record_sha(ordered_visits(s.visits())), tag
+        s.close()
+
+
+def test_batch_matches_oracle(solver_cls):
+    from oracle.ccopy import OracleSolver
+    mix = _mix()
+    steps, pv, pe = _run_batch(solver_cls, mix, 6)
+    for i, sc in enumerate(mix):
+        if sc.ne == 0:
+            for st in steps:  # nothing to collide: candidates pass through
+                assert np.array_equal(_split(st["x"], pv, i), _split(st["xc"], pv, i))
+                assert np.array_equal(_split(st["v"], pv, i), _split(st["v_in"], pv, i))
+            continue
+        o = OracleSolver(sc)
+        for k, st in enumerate(steps):
+            r = o.step(_split(st["x_in"], pv, i), _split(st["xc"], pv, i), _split(st["v_in"], pv, i),
+                       _split(st["hc_in"], pv, i))
+            assert r["rc"] == 0
+            tag = f"scene {i} ({sc.name}) step {k}"
+            assert np.array_equal(o.passes(), st["kinds"][i]), tag
+            assert np.array_equal(_split(st["hc"], pv, i), r["has_collsn"]), tag
+            assert rel_err(_split(st["x"], pv, i), r["x"]) <= RTOL, tag
+            assert rel_err(_split(st["v"], pv, i), r["v"]) <= RTOL, tag
+
+
+def test_batch_mixed_and_global_strain_equal_plain(solver_cls):
+    mix = _mix()
+    ref, _, _ = _run_batch(solver_cls, mix, 8)
+    for mode, window in ((1, True), (0, False), (1, False)):
+        got, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, window=window)
+        for k, (a, b) in enumerate(zip(ref, got)):
+            assert np.array_equal(a["x"], b["x"]), (mode, window, k)
+            assert np.array_equal(a["v"], b["v"]), (mode, window, k)
+            assert np.array_equal(a["hc"], b["hc"]), (mode, window, k)
+            assert np.array_equal(a["hcol"], b["hcol"]), (mode, window, k)
+
+
+def test_batch_per_scene_params(solver_cls):
+    """Changing one scene's parameters changes that scene only."""
+    mix = [scenes.cloth_on_obstacle(12, "sphere", 0.2, 2.0, seed=7) for _ in range(3)]
+    b = solver_cls(0)
+    b.assembleBatch(mix)
+    # the sheets start 0.05 above the sphere at 2 m/s: within 2e-2 (the
+    # thicker scene's repulsion reach) after about 15 steps
+    thick = dict(mix[1].params, thickness=2e-2)
+    b.setSceneParams(1, thick)
+    pv, _ = b.sceneOffsets()
+    x = np.concatenate([s.x for s in mix])
+    v = np.concatenate([s.v for s in mix])
+    hc = np.zeros(len(x), np.uint8)
+    xc = x + 1e-3 * v
+    for _ in range(30):
+        xo, vo, ho, _ = b.resolveCollisionBatch(x, xc, v, hc)
+        x, v, hc = xo, vo, ho
+        xc = x + 1e-3 * v
+    assert np.array_equal(_split(x, pv, 0), _split(x, pv, 2))
+    assert not np.array_equal(_split(x, pv, 0), _split(x, pv, 1))
+    s = solver_cls(0)
+    sc = mix[1].copy()
+    sc.params = thick
+    s.assembleFromScene(sc)
+    xs, vs, hs = sc.x, sc.v, np.zeros(sc.nv, np.uint8)
+    for _ in range(30):
+        xs, vs, hs = s.resolveCollision(xs, xs + 1e-3 * vs, vs, hs)
+    assert np.array_equal(xs, _split(x, pv, 1))
+    b.close()
+    s.close()
+
+
+def test_batch_device_entry(solver_cls):
+    import torch
+    mix = _mix()[:3]
+    steps, pv, _ = _run_batch(solver_cls, mix, 3)
+    b = solver_cls(0)
+    b.assembleBatch(mix)
+    dev = torch.device("cuda:0")
+    for st in steps:
+        xo = torch.from_numpy(st["x_in"]).to(dev)
+        xc = torch.from_numpy(st["xc"]).to(dev)
+        v = torch.from_numpy(st["v_in"]).to(dev)
+        hc = torch.from_numpy(st["hc_in"]).to(dev)
+        out = torch.empty_like(xo)
+        hcol = b.resolveCollisionBatchDevice(xo, xc, v, hc, out)
+        assert np.array_equal(out.cpu().numpy(), st["x"])
+        assert np.array_equal(v.cpu().numpy(), st["v"])
+        assert np.array_equal(hcol, st["hcol"])
+    b.close()
+
+
+def test_ccd_recheck_after_resolved_steps(solver_cls):
+    """The exact CCD re-check finds nothing after a resolved step and finds
+    the collisions of the unresolved candidate positions."""
+    import torch
+    mix = [scenes.cloth_on_obstacle(12, "sphere", 0.2, 3.0, seed=11), scenes.folded_cloth(n=17, seed=2),
+           scenes.strings(nstr=4, nseg=32, seed=4)]
+    b = solver_cls(0)
+    b.assembleBatch(mix)
+    dev = torch.device("cuda:0")
+    x = torch.tensor(np.concatenate([s.x for s in mix]), device=dev)
+    v = torch.tensor(np.concatenate([s.v for s in mix]), device=dev)
+    dt = torch.tensor(np.concatenate([np.full((s.nv, 1), s.params["dt"]) for s in mix]), device=dev)
+    hc = torch.zeros(len(x), dtype=torch.uint8, device=dev)
+    unresolved = 0
+    for step in range(25):
+        xc = x + dt * v
+        xo = torch.empty_like(x)
+        b.resolveCollisionBatchDevice(x, xc, v, hc, xo)
+        hits, per = b.checkCCD(x, xo)
+        assert hits == 0 and not per.any(), (step, hits, per)
+        h2, _ = b.checkCCD(x, xc)
+        unresolved += h2
+        x = xo
+    assert unresolved > 0
+    b.close()
