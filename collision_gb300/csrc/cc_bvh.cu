@@ -160,7 +160,7 @@ __device__ __forceinline__ int delta(const unsigned long long* keys, int n, int 
 
 // Karras, "Maximizing parallelism in the construction of BVHs, octrees and
 // k-d trees" (HPG 2012), with index tie-breaking for equal keys.
-__global__ void k_karras(const unsigned long long* __restrict__ keys, int n, int* child, int* range_hi,
+__global__ void k_karras(const unsigned long long* __restrict__ keys, int n, BvhNode32* node, int* range_hi,
                          int* range_lo, int* parent) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
@@ -183,8 +183,8 @@ __global__ void k_karras(const unsigned long long* __restrict__ keys, int n, int
     int lo = i < j ? i : j, hi = i < j ? j : i;
     int left = (lo == gamma) ? ~gamma : gamma;
     int right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
-    child[2 * i] = left;
-    child[2 * i + 1] = right;
+    // children cover [lo, gamma] and [gamma + 1, hi]
+    node[i].meta = make_int4(left, right, gamma, hi);
     range_hi[i] = hi;
     range_lo[i] = lo;
     if (left >= 0) parent[left] = i; else parent[n - 1 + ~left] = i;
@@ -192,35 +192,58 @@ __global__ void k_karras(const unsigned long long* __restrict__ keys, int n, int
     if (i == 0) parent[0] = -1;
 }
 
-__device__ __forceinline__ Box6 load_box_cg(const Box6* p) {
-    const double2* q = reinterpret_cast<const double2*>(p);
-    double2 a = __ldcg(q), b = __ldcg(q + 1), c = __ldcg(q + 2);
-    Box6 r;
-    r.lo[0] = a.x; r.lo[1] = a.y; r.lo[2] = b.x;
-    r.hi[0] = b.y; r.hi[1] = c.x; r.hi[2] = c.y;
+struct Box32 {
+    float lo[3], hi[3];
+};
+
+__device__ __forceinline__ Box32 box32_out(const Box6& b) {
+    Box32 r;
+    for (int d = 0; d < 3; ++d) {
+        r.lo[d] = __double2float_rd(b.lo[d]);
+        r.hi[d] = __double2float_ru(b.hi[d]);
+    }
     return r;
 }
 
+__device__ __forceinline__ void unpack(const float4& b0, const float4& b1, const float4& b2, Box32& c0, Box32& c1) {
+    c0.lo[0] = b0.x; c0.lo[1] = b0.y; c0.lo[2] = b0.z; c0.hi[0] = b0.w;
+    c0.hi[1] = b1.x; c0.hi[2] = b1.y; c1.lo[0] = b1.z; c1.lo[1] = b1.w;
+    c1.lo[2] = b2.x; c1.hi[0] = b2.y; c1.hi[1] = b2.z; c1.hi[2] = b2.w;
+}
+
+// Box of an internal node: the union of its record's two child boxes,
+// written by another thread of the refit (read through L2).
+__device__ __forceinline__ Box32 node_union_cg(const BvhNode32* nd) {
+    const float4* q = reinterpret_cast<const float4*>(nd);
+    Box32 a, b, m;
+    unpack(__ldcg(q), __ldcg(q + 1), __ldcg(q + 2), a, b);
+    for (int d = 0; d < 3; ++d) {
+        m.lo[d] = fminf(a.lo[d], b.lo[d]);
+        m.hi[d] = fmaxf(a.hi[d], b.hi[d]);
+    }
+    return m;
+}
+
+// Bottom-up refit: the second child to arrive at a node writes the node's
+// two child boxes (leaf boxes rounded outward to FP32, internal children as
+// the union of their own records).
 __global__ void k_refit(const Box6* __restrict__ box, const unsigned int* __restrict__ order, int n,
-                        const int* __restrict__ child, const int* __restrict__ parent, int* flags,
-                        Box6* node_box) {
+                        const int* __restrict__ parent, int* flags, BvhNode32* node) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    int node = parent[n - 1 + i];
-    while (node >= 0) {
+    int nd = parent[n - 1 + i];
+    while (nd >= 0) {
         __threadfence();
-        if (atomicAdd(&flags[node], 1) == 0) return;
+        if (atomicAdd(&flags[nd], 1) == 0) return;
         __threadfence();
-        int c0 = child[2 * node], c1 = child[2 * node + 1];
-        Box6 a = c0 >= 0 ? load_box_cg(&node_box[c0]) : box[order[~c0]];
-        Box6 b = c1 >= 0 ? load_box_cg(&node_box[c1]) : box[order[~c1]];
-        Box6 m;
-        for (int d = 0; d < 3; ++d) {
-            m.lo[d] = smin(a.lo[d], b.lo[d]);
-            m.hi[d] = smax(a.hi[d], b.hi[d]);
-        }
-        node_box[node] = m;
-        node = parent[node];
+        int4 meta = node[nd].meta;
+        Box32 a = meta.x >= 0 ? node_union_cg(&node[meta.x]) : box32_out(box[order[~meta.x]]);
+        Box32 b = meta.y >= 0 ? node_union_cg(&node[meta.y]) : box32_out(box[order[~meta.y]]);
+        float4* q = reinterpret_cast<float4*>(&node[nd]);
+        q[0] = make_float4(a.lo[0], a.lo[1], a.lo[2], a.hi[0]);
+        q[1] = make_float4(a.hi[1], a.hi[2], b.lo[0], b.lo[1]);
+        q[2] = make_float4(b.lo[2], b.hi[0], b.hi[1], b.hi[2]);
+        nd = parent[nd];
     }
 }
 
@@ -239,6 +262,11 @@ __global__ void k_scene_roots(const SceneDev* __restrict__ scenes, SceneRun* run
     int node = parent[n - 1 + first];
     while (node >= 0 && !(range_lo[node] <= first && range_hi[node] >= last)) node = parent[node];
     run[sc].root = node;
+}
+
+__device__ __forceinline__ bool overlap32(const Box32& a, const Box32& b) {
+    return (a.lo[0] <= b.hi[0] && a.hi[0] >= b.lo[0]) && (a.lo[1] <= b.hi[1] && a.hi[1] >= b.lo[1]) &&
+           (a.lo[2] <= b.hi[2] && a.hi[2] >= b.lo[2]);
 }
 
 __device__ __forceinline__ bool overlap(const Box6& a, const Box6& b) {
@@ -260,52 +288,54 @@ __device__ __forceinline__ void emit_pair(int a, int b, int2* pairs, int cap, Pa
 // share a point are dropped: every narrow-phase test of such a pair returns
 // false before any arithmetic (dcollid3d.cpp:493-497, 541-546, 578-582).
 __global__ void k_traverse(const Box6* __restrict__ box, const unsigned int* __restrict__ order, int n,
-                           const int* __restrict__ child, const int* __restrict__ range_hi,
-                           const Box6* __restrict__ node_box, const int* __restrict__ elem_scene,
+                           const BvhNode32* __restrict__ node, const int* __restrict__ elem_scene,
                            const SceneRun* __restrict__ run, const int* __restrict__ ev, int2* pairs, int cap,
                            PassCounters* ctr) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
     int ei = (int)order[i];
-    int pi0 = -1, pi1 = -1, pi2 = -1;
-    if (ev) {
-        pi0 = ev[3 * ei];
-        pi1 = ev[3 * ei + 1];
-        pi2 = ev[3 * ei + 2];  // -1 for a bond: matches no point
-    }
     int root = 0;
     if (run) {
         SceneRun r = run[elem_scene[ei]];
         if (r.mode == kSceneIdle || r.root < 0) return;
         root = r.root;
     }
-    Box6 q = box[ei];
+    int pi0 = -1, pi1 = -1, pi2 = -1;
+    if (ev) {
+        pi0 = ev[3 * ei];
+        pi1 = ev[3 * ei + 1];
+        pi2 = ev[3 * ei + 2];  // -1 for a bond: matches no point
+    }
+    const Box6 q = box[ei];
+    const Box32 q32 = box32_out(q);
     int stk[kTraversalStack];
     int sp = 0;
     stk[sp++] = root;
     while (sp > 0) {
-        int node = stk[--sp];
+        const BvhNode32* nd = &node[stk[--sp]];
+        const float4* r4 = reinterpret_cast<const float4*>(nd);
+        Box32 cb[2];
+        unpack(__ldg(r4), __ldg(r4 + 1), __ldg(r4 + 2), cb[0], cb[1]);
+        const int4 meta = __ldg(reinterpret_cast<const int4*>(r4 + 3));
+        const int cs[2] = {meta.x, meta.y}, last[2] = {meta.z, meta.w};
         for (int k = 0; k < 2; ++k) {
-            int c = child[2 * node + k];
+            // nothing under this child lies after leaf i
+            if (last[k] <= i || !overlap32(q32, cb[k])) continue;
+            int c = cs[k];
             if (c < 0) {
-                int j = ~c;
-                if (j > i) {
-                    int ej = (int)order[j];
-                    if (overlap(q, box[ej])) {
-                        bool shared = false;
-                        if (ev) {
-                            int a = ev[3 * ej], b = ev[3 * ej + 1], c3 = ev[3 * ej + 2];
-                            shared = a == pi0 || a == pi1 || a == pi2 || b == pi0 || b == pi1 || b == pi2 ||
-                                     (c3 >= 0 && (c3 == pi0 || c3 == pi1 || c3 == pi2));
-                        }
-                        if (!shared) emit_pair(ei, ej, pairs, cap, ctr);
-                    }
+                int ej = (int)order[~c];
+                if (!overlap(q, box[ej])) continue;  // the exact test
+                bool shared = false;
+                if (ev) {
+                    int a = ev[3 * ej], b = ev[3 * ej + 1], c3 = ev[3 * ej + 2];
+                    shared = a == pi0 || a == pi1 || a == pi2 || b == pi0 || b == pi1 || b == pi2 ||
+                             (c3 >= 0 && (c3 == pi0 || c3 == pi1 || c3 == pi2));
                 }
-            } else if (range_hi[c] > i && overlap(q, node_box[c])) {
-                if (sp < kTraversalStack)
-                    stk[sp++] = c;
-                else
-                    atomicOr(&ctr->err, kErrStack);
+                if (!shared) emit_pair(ei, ej, pairs, cap, ctr);
+            } else if (sp < kTraversalStack) {
+                stk[sp++] = c;
+            } else {
+                atomicOr(&ctr->err, kErrStack);
             }
         }
     }
@@ -348,9 +378,9 @@ void bvh_build(const Box6* box, BvhBufs& b, cudaStream_t s) {
     int bits = 30;
     while (bits < 62 && (b.nscenes - 1) >> (bits - 30)) ++bits;
     radix_sort_pairs(b.keys, b.order, n, bits, b.sort_temp, s);
-    count_launch(), k_karras<<<nblk(n - 1, 256), 256, 0, s>>>(b.keys, n, b.child, b.range_hi, b.range_lo, b.parent);
+    count_launch(), k_karras<<<nblk(n - 1, 256), 256, 0, s>>>(b.keys, n, b.node, b.range_hi, b.range_lo, b.parent);
     cudaMemsetAsync(b.flags, 0, sizeof(int) * (size_t)(n - 1), s);
-    count_launch(), k_refit<<<nblk(n, 256), 256, 0, s>>>(box, b.order, n, b.child, b.parent, b.flags, b.node_box);
+    count_launch(), k_refit<<<nblk(n, 256), 256, 0, s>>>(box, b.order, n, b.parent, b.flags, b.node);
     if (b.run)
         count_launch(), k_scene_roots<<<nblk(b.nscenes, 128), 128, 0, s>>>(b.scenes, b.run, b.nscenes, n, b.parent,
                                                                           b.range_lo, b.range_hi);
@@ -360,9 +390,8 @@ void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCoun
                const int* skip_shared_ev) {
     int n = b.n;
     if (n <= 1) return;
-    count_launch(), k_traverse<<<nblk(n - 1, 128), 128, 0, s>>>(box, b.order, n, b.child, b.range_hi, b.node_box,
-                                                                b.elem_scene, b.run, skip_shared_ev, pairs, cap,
-                                                                ctr);
+    count_launch(), k_traverse<<<nblk(n - 1, 128), 128, 0, s>>>(box, b.order, n, b.node, b.elem_scene, b.run,
+                                                                skip_shared_ev, pairs, cap, ctr);
 }
 
 void brute_pairs(const Box6* box, int ne, const int* elem_scene, int2* pairs, int cap, PassCounters* ctr,

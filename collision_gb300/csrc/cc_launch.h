@@ -30,6 +30,17 @@ struct __align__(16) Box6 {
     double hi[3];
 };
 
+// An internal LBVH node as the traversal reads it: both children's boxes in
+// FP32, rounded outward (so a test against them never rejects what the
+// exact boxes would accept), the children (>= 0 internal, < 0 ~leaf), and
+// the last sorted leaf under each child.
+struct __align__(16) BvhNode32 {
+    float4 b0;  // child 0: lo.x lo.y lo.z hi.x
+    float4 b1;  // child 0: hi.y hi.z, child 1: lo.x lo.y
+    float4 b2;  // child 1: lo.z hi.x hi.y hi.z
+    int4 meta;  // child 0, child 1, last leaf under child 0, under child 1
+};
+
 struct BvhBufs {
     int n;                        // leaves
     int nscenes;
@@ -39,11 +50,10 @@ struct BvhBufs {
     int* range_lo;                // n-1: first sorted leaf covered by each internal node
     unsigned long long* keys;     // n Morton keys (sorted)
     unsigned int* order;          // n element ids in Morton order
-    int* child;                   // 2*(n-1): >= 0 internal, < 0 leaf (~sorted index)
     int* range_hi;                // n-1: last sorted leaf covered by each internal node
     int* parent;                  // 2n-1: parents of internal nodes [0,n-1) then leaves
     int* flags;                   // n-1 refit arrival counters
-    Box6* node_box;               // n-1 internal boxes
+    BvhNode32* node;              // n-1 internal nodes
     unsigned long long* bbox_enc; // 6 encoded doubles per scene (scene boxes)
     void* sort_temp;
 };

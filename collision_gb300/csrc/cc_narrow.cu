@@ -66,7 +66,9 @@ __global__ void __launch_bounds__(128) k_narrow(NarrowArgs a, int max_pairs) {
         int A[3] = {P1[0], P1[1], n1 == 3 ? P1[2] : -1};
         int B[3] = {P2[0], P2[1], n2 == 3 ? P2[2] : -1};
         bool status;
-        if (kind == 0)
+        if (c.pbox_lo && !pair_may_hit<MOVING>(c, A, n1, B, n2))
+            status = false;  // no sub-test of the pair can hit
+        else if (kind == 0)
             status = tri_to_tri<MOVING>(c, st, A, B);
         else if (kind == 1)
             status = tri_to_bond<MOVING>(c, st, A, B);

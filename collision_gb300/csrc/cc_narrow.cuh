@@ -649,6 +649,118 @@ __device__ __forceinline__ bool sat_may_hit(const NarrowCtx& c, const int* pts, 
     return !(bound > reach);
 }
 
+__device__ __forceinline__ F3 fcross(F3 a, F3 b) {
+    return F3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+
+// Element-pair stage of the mixed-precision filter: one lower bound on the
+// distance between the two elements (as point sets) over the pass's time
+// window. Every sub-test of the pair involves a point or an edge of each
+// element, so its distance is at least this one, and when the bound exceeds
+// the largest reach of the pair's sub-tests none of them can hit. The bound
+// is the separating-axis gap (as in sat_may_hit, with the same rounding and
+// motion allowances) maximised over a few axes: each triangle's normal and
+// its three in-plane edge normals (for two disjoint coplanar triangles one of
+// those separates them), for two segments their common normal and the
+// in-plane normals of each, and the line between the centroids.
+template <bool MOVING>
+__device__ __forceinline__ bool pair_may_hit(const NarrowCtx& c, const int* A, int na, const int* B, int nb) {
+    F3 X[6];
+    int n = na + nb;
+    for (int q = 0; q < na; ++q) X[q] = f3(c.p32[A[q]]);
+    for (int q = 0; q < nb; ++q) X[na + q] = f3(c.p32[B[q]]);
+    float M = 0.f, L = 0.f;
+    F3 R[6];
+    for (int q = 0; q < n; ++q) {
+        M = fmaxf(M, fmaxabs(X[q]));
+        R[q] = fsub(X[q], X[0]);
+        L = fmaxf(L, fnorm(R[q]));
+    }
+    F3 ax[10];
+    int nax = 0;
+    F3 cA = F3{0.f, 0.f, 0.f}, cB = F3{0.f, 0.f, 0.f};
+    for (int q = 0; q < na; ++q) cA = fadd(cA, R[q]);
+    for (int q = 0; q < nb; ++q) cB = fadd(cB, R[na + q]);
+    ax[nax++] = fsub(fscale(cB, 1.f / nb), fscale(cA, 1.f / na));
+    for (int side = 0; side < 2; ++side) {
+        const F3* P = side ? R + na : R;
+        int np = side ? nb : na;
+        if (np == 3) {
+            F3 e0 = fsub(P[1], P[0]), e1 = fsub(P[2], P[1]), e2 = fsub(P[0], P[2]);
+            F3 nrm = fcross(e0, fsub(P[2], P[0]));
+            ax[nax++] = nrm;
+            ax[nax++] = fcross(nrm, e0);
+            ax[nax++] = fcross(nrm, e1);
+            ax[nax++] = fcross(nrm, e2);
+        }
+    }
+    if (na == 2 && nb == 2) {
+        F3 d1 = fsub(R[1], R[0]), d2 = fsub(R[3], R[2]);
+        F3 nrm = fcross(d1, d2);
+        ax[nax++] = nrm;
+        ax[nax++] = fcross(nrm, d1);
+        ax[nax++] = fcross(nrm, d2);
+    }
+    float lb = -1.f;
+    for (int k = 0; k < nax; ++k) {
+        float an = fnorm(ax[k]);
+        if (!(an > 0.f)) continue;
+        float amin = 3.0e38f, amax = -3.0e38f, bmin = 3.0e38f, bmax = -3.0e38f;
+        for (int q = 0; q < na; ++q) {
+            float t = fdot(ax[k], R[q]);
+            amin = fminf(amin, t);
+            amax = fmaxf(amax, t);
+        }
+        for (int q = 0; q < nb; ++q) {
+            float t = fdot(ax[k], R[na + q]);
+            bmin = fminf(bmin, t);
+            bmax = fmaxf(bmax, t);
+        }
+        lb = fmaxf(lb, fmaxf(bmin - amax, amin - bmax) / an);
+    }
+    // the largest reach of the pair's sub-tests, with the boxes' extents
+    float extA = 0.f, extB = 0.f;
+    {
+        float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+        for (int q = 0; q < na; ++q) {
+            float4 l = c.pbox_lo[A[q]], h = c.pbox_hi[A[q]];
+            lo[0] = fminf(lo[0], l.x); lo[1] = fminf(lo[1], l.y); lo[2] = fminf(lo[2], l.z);
+            hi[0] = fmaxf(hi[0], h.x); hi[1] = fmaxf(hi[1], h.y); hi[2] = fmaxf(hi[2], h.z);
+        }
+        extA = __fadd_ru(__fadd_ru(__fsub_ru(hi[0], lo[0]), __fsub_ru(hi[1], lo[1])), __fsub_ru(hi[2], lo[2]));
+        float lo2[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi2[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+        for (int q = 0; q < nb; ++q) {
+            float4 l = c.pbox_lo[B[q]], h = c.pbox_hi[B[q]];
+            lo2[0] = fminf(lo2[0], l.x); lo2[1] = fminf(lo2[1], l.y); lo2[2] = fminf(lo2[2], l.z);
+            hi2[0] = fmaxf(hi2[0], h.x); hi2[1] = fmaxf(hi2[1], h.y); hi2[2] = fmaxf(hi2[2], h.z);
+        }
+        extB = __fadd_ru(__fadd_ru(__fsub_ru(hi2[0], lo2[0]), __fsub_ru(hi2[1], lo2[1])), __fsub_ru(hi2[2], lo2[2]));
+    }
+    float ext_tri = fmaxf(na == 3 ? extA : 0.f, nb == 3 ? extB : 0.f);
+    float reach_pt = __fmul_ru(ext_tri, __fmul_ru(8.0f, __fadd_ru(c.epad, 0x1p-10f)));
+    float reach_ee = __fmul_ru(__fadd_ru(extA, extB), 0x1p-20f);
+    float reach = __fadd_ru(c.hpad, fmaxf(reach_pt, reach_ee));
+    float err = __fmul_ru(32.0f * 0x1p-24f, __fadd_ru(L, M));
+    float bound = __fsub_rd(lb, err);
+    if (MOVING) {
+        F3 v0 = f3(c.v32[A[0]]);
+        float DA = 0.f, DB = 0.f, Vm = fmaxabs(v0);
+        for (int q = 1; q < na; ++q) {
+            F3 v = f3(c.v32[A[q]]);
+            DA = fmaxf(DA, fnorm(fsub(v, v0)));
+            Vm = fmaxf(Vm, fmaxabs(v));
+        }
+        for (int q = 0; q < nb; ++q) {
+            F3 v = f3(c.v32[B[q]]);
+            DB = fmaxf(DB, fnorm(fsub(v, v0)));
+            Vm = fmaxf(Vm, fmaxabs(v));
+        }
+        float dv = __fadd_ru(__fmul_ru(__fadd_ru(DA, DB), 1.0f + 0x1p-16f), __fmul_ru(Vm, 32.0f * 0x1p-24f));
+        bound = __fsub_rd(bound, __fmul_ru(c.dt32, dv));
+    }
+    return !(bound > reach);
+}
+
 template <bool MOVING, bool EE>
 __device__ __forceinline__ bool sub_test(const NarrowCtx& c, CallState& st, const int* pts) {
     if (c.pbox_lo) {

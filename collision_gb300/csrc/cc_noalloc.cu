@@ -105,12 +105,11 @@ cc_status cc_candidate_pairs_static(int device, const double* boxes, int n, int*
     b.nscenes = 1;  // one scene: no scene ids, traversal from node 0
     b.keys = (unsigned long long*)take(sizeof(unsigned long long) * (size_t)n);
     b.order = (unsigned int*)take(sizeof(unsigned int) * (size_t)n);
-    b.child = (int*)take(sizeof(int) * 2 * (size_t)n);
     b.range_hi = (int*)take(sizeof(int) * (size_t)n);
     b.range_lo = (int*)take(sizeof(int) * (size_t)n);
     b.parent = (int*)take(sizeof(int) * 2 * (size_t)n);
     b.flags = (int*)take(sizeof(int) * (size_t)n);
-    b.node_box = (Box6*)take(sizeof(Box6) * (size_t)n);
+    b.node = (BvhNode32*)take(sizeof(BvhNode32) * (size_t)n);
     b.bbox_enc = (unsigned long long*)take(6 * sizeof(unsigned long long));
     PassCounters* ctr = (PassCounters*)take(sizeof(PassCounters));
     b.sort_temp = take(radix_sort_temp_bytes(n));

@@ -341,8 +341,8 @@ struct cc_solver {
         dfree(d_urec); dfree(d_members); dfree(d_zone_off);
         urec_cap = members_cap = zones_cap = 0;
         dfree(d_xold_in); dfree(d_xcand_in); dfree(d_vel); dfree(d_xout); dfree(d_hc);
-        dfree(d_box); dfree(bvh.keys); dfree(bvh.order); dfree(bvh.child); dfree(bvh.range_hi);
-        dfree(bvh.range_lo); dfree(bvh.parent); dfree(bvh.flags); dfree(bvh.node_box); dfree(bvh.bbox_enc);
+        dfree(d_box); dfree(bvh.keys); dfree(bvh.order); dfree(bvh.range_hi);
+        dfree(bvh.range_lo); dfree(bvh.parent); dfree(bvh.flags); dfree(bvh.node); dfree(bvh.bbox_enc);
         if (bvh.sort_temp) cudaFree(bvh.sort_temp);
         bvh = BvhBufs{};
         dfree(d_pairs); dfree(d_contrib);
@@ -603,12 +603,11 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     bvh.elem_scene = nullptr;
     ok &= dalloc(&bvh.keys, (size_t)ne) == cudaSuccess;
     ok &= dalloc(&bvh.order, (size_t)ne) == cudaSuccess;
-    ok &= dalloc(&bvh.child, (size_t)2 * ne) == cudaSuccess;
     ok &= dalloc(&bvh.range_hi, (size_t)ne) == cudaSuccess;
     ok &= dalloc(&bvh.range_lo, (size_t)ne) == cudaSuccess;
     ok &= dalloc(&bvh.parent, (size_t)2 * ne) == cudaSuccess;
     ok &= dalloc(&bvh.flags, (size_t)ne) == cudaSuccess;
-    ok &= dalloc(&bvh.node_box, (size_t)ne) == cudaSuccess;
+    ok &= dalloc(&bvh.node, (size_t)ne) == cudaSuccess;
     ok &= dalloc(&bvh.bbox_enc, 6 * (size_t)n) == cudaSuccess;
     ok &= cudaMalloc(&bvh.sort_temp, radix_sort_temp_bytes(ne > 0 ? ne : 1)) == cudaSuccess;
     ok &= dalloc(&apply.cnt, (size_t)nv) == cudaSuccess;
