@@ -75,6 +75,12 @@ def load(path: str = LIB_PATH):
     lib.cc_set_scene_domain_boundary.argtypes = [vp, C.c_int, dp, dp]
     lib.cc_check_ccd.restype = C.c_int
     lib.cc_check_ccd.argtypes = [vp, dp, dp, lp, ip]
+    lib.cc_set_zone_cap.restype = C.c_int
+    lib.cc_set_zone_cap.argtypes = [vp, C.c_int]
+    lib.cc_get_scene_status.restype = C.c_int
+    lib.cc_get_scene_status.argtypes = [vp, ip]
+    lib.cc_set_scene_enabled.restype = C.c_int
+    lib.cc_set_scene_enabled.argtypes = [vp, C.c_int, C.c_int]
     lib.cc_set_host_threads.restype = C.c_int
     lib.cc_set_host_threads.argtypes = [vp, C.c_int]
     lib.cc_get_scene_pass_kinds.restype = C.c_int

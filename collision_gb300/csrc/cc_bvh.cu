@@ -53,11 +53,13 @@ __device__ __forceinline__ void scene_bbox_accumulate(unsigned long long* bb, in
 }
 
 template <int MOVING>
-__global__ void k_leaf_boxes(const int* __restrict__ ev, int ne, const int* __restrict__ elem_scene,
-                             const SceneDev* __restrict__ scenes, const double4_32a* __restrict__ xo,
-                             const double4_32a* __restrict__ av, Box6* __restrict__ box, unsigned long long* bb) {
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
-    bool valid = e < ne;
+__global__ void k_leaf_boxes(const int* __restrict__ ev, const int* __restrict__ act, int n,
+                             const int* __restrict__ elem_scene, const SceneDev* __restrict__ scenes,
+                             const double4_32a* __restrict__ xo, const double4_32a* __restrict__ av,
+                             Box6* __restrict__ box, unsigned long long* bb) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    bool valid = k < n;
+    int e = valid ? (act ? act[k] : k) : 0;
     int scene = valid ? elem_scene[e] : -1;
     double lo[3] = {kBig, kBig, kBig}, hi[3] = {-kBig, -kBig, -kBig};
     if (valid) {
@@ -128,10 +130,12 @@ __device__ __forceinline__ unsigned int expand_bits10(unsigned int v) {
     return v;
 }
 
-__global__ void k_morton(const Box6* __restrict__ box, int n, const int* __restrict__ elem_scene,
-                         const unsigned long long* bb, unsigned long long* keys, unsigned int* order) {
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= n) return;
+__global__ void k_morton(const Box6* __restrict__ box, const int* __restrict__ act, int n,
+                         const int* __restrict__ elem_scene, const unsigned long long* bb, unsigned long long* keys,
+                         unsigned int* order) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int e = act ? act[k] : k;
     Box6 b = box[e];
     int sc = elem_scene ? elem_scene[e] : 0;
     const unsigned long long* sb = bb + 6 * sc;
@@ -147,8 +151,8 @@ __global__ void k_morton(const Box6* __restrict__ box, int n, const int* __restr
     }
     unsigned long long m = (unsigned long long)((expand_bits10(q[0]) << 2) | (expand_bits10(q[1]) << 1) |
                                                 expand_bits10(q[2]));
-    keys[e] = ((unsigned long long)sc << 30) | m;
-    order[e] = (unsigned int)e;
+    keys[k] = ((unsigned long long)sc << 30) | m;
+    order[k] = (unsigned int)e;
 }
 
 __device__ __forceinline__ int delta(const unsigned long long* keys, int n, int i, int j) {
@@ -254,8 +258,8 @@ __global__ void k_scene_roots(const SceneDev* __restrict__ scenes, SceneRun* run
                               const int* __restrict__ range_hi) {
     int sc = blockIdx.x * blockDim.x + threadIdx.x;
     if (sc >= nscenes) return;
-    int first = scenes[sc].e0, last = scenes[sc].e0 + scenes[sc].ne - 1;
-    if (scenes[sc].ne < 2) {
+    int first = run[sc].leaf0, last = first + scenes[sc].ne - 1;
+    if (scenes[sc].ne < 2 || first < 0) {
         run[sc].root = -1;
         return;
     }
@@ -355,15 +359,41 @@ inline int nblk(int n, int t) { return (n + t - 1) / t; }
 
 }  // namespace
 
-void leaf_boxes(const int* ev, int ne, const int* elem_scene, const SceneDev* scenes, int nscenes,
+void leaf_boxes(const int* ev, const int* act, int n, const int* elem_scene, const SceneDev* scenes, int nscenes,
                 const double4_32a* xo, const double4_32a* av, int moving, Box6* box, unsigned long long* bbox_enc,
                 cudaStream_t s) {
     count_launch(), k_bbox_init<<<nblk(6 * nscenes, 256), 256, 0, s>>>(bbox_enc, 6 * nscenes);
-    if (ne <= 0) return;
+    if (n <= 0) return;
     if (moving)
-        count_launch(), k_leaf_boxes<1><<<nblk(ne, 256), 256, 0, s>>>(ev, ne, elem_scene, scenes, xo, av, box, bbox_enc);
+        count_launch(), k_leaf_boxes<1><<<nblk(n, 256), 256, 0, s>>>(ev, act, n, elem_scene, scenes, xo, av, box,
+                                                                     bbox_enc);
     else
-        count_launch(), k_leaf_boxes<0><<<nblk(ne, 256), 256, 0, s>>>(ev, ne, elem_scene, scenes, xo, av, box, bbox_enc);
+        count_launch(), k_leaf_boxes<0><<<nblk(n, 256), 256, 0, s>>>(ev, act, n, elem_scene, scenes, xo, av, box,
+                                                                     bbox_enc);
+}
+
+// Element / point k of the selection: scene j with off[j] <= k < off[j+1].
+__global__ void k_expand(const int* __restrict__ scene_ids, const int* __restrict__ off, int nsel, int n,
+                         const SceneDev* __restrict__ scenes, int points, int* out) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int lo = 0, hi = nsel - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= k) lo = mid; else hi = mid - 1;
+    }
+    const SceneDev& sd = scenes[scene_ids[lo]];
+    out[k] = (points ? sd.v0 : sd.e0) + (k - off[lo]);
+}
+
+void expand_scenes(const int* scene_ids, const int* elem_off, const int* pt_off, int nsel, int n_elems, int n_pts,
+                   const SceneDev* scenes, int* elems, int* pts, cudaStream_t s) {
+    if (nsel <= 0) return;
+    if (n_elems > 0)
+        count_launch(), k_expand<<<nblk(n_elems, 256), 256, 0, s>>>(scene_ids, elem_off, nsel, n_elems, scenes, 0,
+                                                                    elems);
+    if (n_pts > 0)
+        count_launch(), k_expand<<<nblk(n_pts, 256), 256, 0, s>>>(scene_ids, pt_off, nsel, n_pts, scenes, 1, pts);
 }
 
 void boxes_bbox(const Box6* box, int n, unsigned long long* bbox_enc, cudaStream_t s) {
@@ -374,7 +404,7 @@ void boxes_bbox(const Box6* box, int n, unsigned long long* bbox_enc, cudaStream
 void bvh_build(const Box6* box, BvhBufs& b, cudaStream_t s) {
     int n = b.n;
     if (n <= 1) return;
-    count_launch(), k_morton<<<nblk(n, 256), 256, 0, s>>>(box, n, b.elem_scene, b.bbox_enc, b.keys, b.order);
+    count_launch(), k_morton<<<nblk(n, 256), 256, 0, s>>>(box, b.act, n, b.elem_scene, b.bbox_enc, b.keys, b.order);
     int bits = 30;
     while (bits < 62 && (b.nscenes - 1) >> (bits - 30)) ++bits;
     radix_sort_pairs(b.keys, b.order, n, bits, b.sort_temp, s);

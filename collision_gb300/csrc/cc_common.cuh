@@ -104,17 +104,20 @@ struct SceneDev {
     int strain_levels;
     int strain_slots;     // shared-memory slots of its window sweep
     int wb_final0, wb_final1;  // write-backs after its last level
-    int pad[3];
+    int enabled;          // 0: left out of resolve calls (candidates pass through)
+    int pad[2];
 };
 
 // Per-pass state of a scene (written by the host before a pass, except
 // hits, which the narrow phase counts, and root, which the BVH build sets).
 enum SceneMode { kSceneIdle = 0, kSceneProx = 1, kSceneCcd = 2, kSceneZone = 3 };
 struct SceneRun {
-    int mode;  // SceneMode of the current pass
-    int hits;  // narrow-phase calls that returned true in the current pass
-    int pass;  // the scene's own pass index (for visit records)
-    int root;  // the scene's subtree root in the LBVH (-1: fewer than 2 elements)
+    int mode;   // SceneMode of the current pass
+    int hits;   // narrow-phase calls that returned true in the current pass
+    int pass;   // the scene's own pass index (for visit records)
+    int root;   // the scene's subtree root in the LBVH (-1: fewer than 2 elements)
+    int leaf0;  // first sorted leaf of the scene in this pass's LBVH (-1: not in it)
+    int pad[3];
 };
 
 struct PassCounters {

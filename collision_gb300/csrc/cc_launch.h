@@ -42,7 +42,8 @@ struct __align__(16) BvhNode32 {
 };
 
 struct BvhBufs {
-    int n;                        // leaves
+    int n;                        // leaves of this pass's hierarchy
+    const int* act;               // their element ids (null: elements 0..n-1)
     int nscenes;
     const int* elem_scene;        // scene of every element (null: one scene)
     const SceneDev* scenes;       // scene descriptors (null: one scene, root 0)
@@ -61,9 +62,15 @@ struct BvhBufs {
 // Leaf boxes of every element (static: x_old; moving: x_old and
 // x_old + dt*avgVel with the element's scene's dt), padded by 1e-6, plus
 // each scene's union in bbox_enc[6*scene ..].
-void leaf_boxes(const int* ev, int ne, const int* elem_scene, const SceneDev* scenes, int nscenes,
+// Only the n elements listed in act (null: elements 0..n-1) are boxed; box
+// is indexed by element id.
+void leaf_boxes(const int* ev, const int* act, int n, const int* elem_scene, const SceneDev* scenes, int nscenes,
                 const double4_32a* xo, const double4_32a* av, int moving, Box6* box, unsigned long long* bbox_enc,
                 cudaStream_t s);
+// The elements and points of the given scenes, in scene order:
+// elem_off / pt_off are the exclusive prefix sums of their counts.
+void expand_scenes(const int* scene_ids, const int* elem_off, const int* pt_off, int nsel, int n_elems, int n_pts,
+                   const SceneDev* scenes, int* elems, int* pts, cudaStream_t s);
 // Union of n given boxes in bbox_enc (the scene box the Morton keys use).
 void boxes_bbox(const Box6* box, int n, unsigned long long* bbox_enc, cudaStream_t s);
 // Morton keys (scene id above the 30 Morton bits, each scene normalised to
@@ -108,8 +115,9 @@ void narrow_pass(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s)
 // Inputs of the mixed-precision filter: outward-rounded FP32 boxes of every
 // point over the pass's time window (with its scene's dt), and x_old and
 // (moving passes) avgVel rounded to FP32.
-void point_boxes(const double4_32a* xo, const double4_32a* av, const int* vscene, const SceneDev* scenes, int nv,
-                 int moving, float4* lo, float4* hi, float4* p32, float4* v32, cudaStream_t s);
+void point_boxes(const double4_32a* xo, const double4_32a* av, const int* vscene, const SceneDev* scenes,
+                 const int* act_pts, int n, int moving, float4* lo, float4* hi, float4* p32, float4* v32,
+                 cudaStream_t s);
 
 // ------------------------------------------------------------- post-pass
 struct ApplyBufs {
@@ -167,7 +175,7 @@ void strain_limit(const StrainEdge* edges, int nedges, const int4* hdr, const in
 // Correctly rounded cos/sin/acos/pow (fn 0..3) on device arrays, for self-tests.
 void math_selftest(int fn, const double* a, const double* b, double* out, int n, cudaStream_t s);
 // updateFinalVelocity.
-void final_velocity(const uint8_t* in_elem, const uint8_t* has_collsn, const double4_32a* av, double* vel, int nv,
-                    cudaStream_t s);
+void final_velocity(const uint8_t* in_elem, const uint8_t* has_collsn, const double4_32a* av, const int* vscene,
+                    const SceneDev* scenes, double* vel, int nv, cudaStream_t s);
 
 }  // namespace ccg

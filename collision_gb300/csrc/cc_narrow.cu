@@ -114,10 +114,11 @@ __global__ void __launch_bounds__(128) k_narrow(NarrowArgs a, int max_pairs) {
 // [x_old] for proximity, [x_old, x_old + dt*avgVel] for CCD.
 template <bool MOVING>
 __global__ void k_point_boxes(const double4_32a* __restrict__ xo, const double4_32a* __restrict__ av,
-                              const int* __restrict__ vscene, const SceneDev* __restrict__ scenes, int nv, float4* lo,
-                              float4* hi, float4* p32, float4* v32) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= nv) return;
+                              const int* __restrict__ vscene, const SceneDev* __restrict__ scenes,
+                              const int* __restrict__ act, int n, float4* lo, float4* hi, float4* p32, float4* v32) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int p = act ? act[k] : k;
     double dt = MOVING ? scenes[vscene[p]].p.dt : 0.0;
     double4_32a x = xo[p];
     double a[3] = {x.x, x.y, x.z}, b[3] = {x.x, x.y, x.z};
@@ -140,15 +141,16 @@ __global__ void k_point_boxes(const double4_32a* __restrict__ xo, const double4_
 
 }  // namespace
 
-void point_boxes(const double4_32a* xo, const double4_32a* av, const int* vscene, const SceneDev* scenes, int nv,
-                 int moving, float4* lo, float4* hi, float4* p32, float4* v32, cudaStream_t s) {
-    if (nv <= 0) return;
+void point_boxes(const double4_32a* xo, const double4_32a* av, const int* vscene, const SceneDev* scenes,
+                 const int* act_pts, int n, int moving, float4* lo, float4* hi, float4* p32, float4* v32,
+                 cudaStream_t s) {
+    if (n <= 0) return;
     if (moving)
-        count_launch(), k_point_boxes<true><<<(nv + 255) / 256, 256, 0, s>>>(xo, av, vscene, scenes, nv, lo, hi,
-                                                                             p32, v32);
+        count_launch(), k_point_boxes<true><<<(n + 255) / 256, 256, 0, s>>>(xo, av, vscene, scenes, act_pts, n, lo,
+                                                                            hi, p32, v32);
     else
-        count_launch(), k_point_boxes<false><<<(nv + 255) / 256, 256, 0, s>>>(xo, av, vscene, scenes, nv, lo, hi,
-                                                                              p32, v32);
+        count_launch(), k_point_boxes<false><<<(n + 255) / 256, 256, 0, s>>>(xo, av, vscene, scenes, act_pts, n, lo,
+                                                                             hi, p32, v32);
 }
 
 void narrow_pass(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s) {

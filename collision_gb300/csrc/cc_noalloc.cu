@@ -102,6 +102,7 @@ cc_status cc_candidate_pairs_static(int device, const double* boxes, int n, int*
     };
     BvhBufs b{};
     b.n = n;
+    b.act = nullptr;
     b.nscenes = 1;  // one scene: no scene ids, traversal from node 0
     b.keys = (unsigned long long*)take(sizeof(unsigned long long) * (size_t)n);
     b.order = (unsigned int*)take(sizeof(unsigned int) * (size_t)n);

@@ -196,6 +196,10 @@ __global__ void k_finalize(const uint8_t* __restrict__ in_elem, const double4_32
         return;
     }
     const SceneDev& sd = scenes[vscene[p]];
+    if (!sd.enabled) {
+        for (int j = 0; j < 3; ++j) x_out[3 * p + j] = x_cand[3 * p + j];
+        return;
+    }
     const Params prm = sd.p;
     double L[3] = {sd.lo[0], sd.lo[1], sd.lo[2]}, U[3] = {sd.hi[0], sd.hi[1], sd.hi[2]};
     double xs[3], v[3];
@@ -390,6 +394,11 @@ __global__ void __launch_bounds__(256) k_strain(const StrainEdgeStep* __restrict
                                                 double4_32a* av, int* passes_out_all) {
     const SceneDev& sd = scenes[blockIdx.x];
     if (slot_cap >= 0 && sd.strain_slots <= slot_cap) return;  // swept by k_strain_window
+    if (!sd.enabled) {
+        if (threadIdx.x == 0) passes_out_all[3 * blockIdx.x] = passes_out_all[3 * blockIdx.x + 1] =
+                                  passes_out_all[3 * blockIdx.x + 2] = 0;
+        return;
+    }
     const int4* hdr = hdr_all + 2 * sd.strain_hdr0;
     const int nlevels = sd.strain_levels;
     const double dt = sd.p.dt;
@@ -648,6 +657,11 @@ __global__ void __launch_bounds__(256) k_strain_window(const StrainEdgeStep* __r
     extern __shared__ WinSlot s_win[];
     const SceneDev& sd = scenes[blockIdx.x];
     if (sd.strain_slots > slot_cap) return;  // swept by k_strain
+    if (!sd.enabled) {
+        if (threadIdx.x == 0) passes_out_all[3 * blockIdx.x] = passes_out_all[3 * blockIdx.x + 1] =
+                                  passes_out_all[3 * blockIdx.x + 2] = 0;
+        return;
+    }
     const int4* hdr = hdr_all + 2 * sd.strain_hdr0;
     const int nlevels = sd.strain_levels;
     const int2 wb_final = make_int2(sd.wb_final0, sd.wb_final1);
@@ -705,9 +719,10 @@ __global__ void __launch_bounds__(256) k_strain_window(const StrainEdgeStep* __r
 }
 
 __global__ void k_final_velocity(const uint8_t* __restrict__ in_elem, const uint8_t* __restrict__ has_collsn,
-                                 const double4_32a* __restrict__ av, double* vel, int nv) {
+                                 const double4_32a* __restrict__ av, const int* __restrict__ vscene,
+                                 const SceneDev* __restrict__ scenes, double* vel, int nv) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= nv || !in_elem[p] || !has_collsn[p]) return;
+    if (p >= nv || !in_elem[p] || !has_collsn[p] || !scenes[vscene[p]].enabled) return;
     double4_32a a = av[p];
     vel[3 * p] = a.x;
     vel[3 * p + 1] = a.y;
@@ -795,9 +810,11 @@ void strain_limit(const StrainEdge* edges, int nedges, const int4* hdr, const in
         count_launch(), k_strain<<<nscenes, 256, 0, s>>>(se, hdr, scenes, cap, av, passes_out);
 }
 
-void final_velocity(const uint8_t* in_elem, const uint8_t* has_collsn, const double4_32a* av, double* vel, int nv,
-                    cudaStream_t s) {
-    if (nv > 0) count_launch(), k_final_velocity<<<nblk(nv, 256), 256, 0, s>>>(in_elem, has_collsn, av, vel, nv);
+void final_velocity(const uint8_t* in_elem, const uint8_t* has_collsn, const double4_32a* av, const int* vscene,
+                    const SceneDev* scenes, double* vel, int nv, cudaStream_t s) {
+    if (nv > 0)
+        count_launch(), k_final_velocity<<<nblk(nv, 256), 256, 0, s>>>(in_elem, has_collsn, av, vscene, scenes, vel,
+                                                                       nv);
 }
 
 }  // namespace ccg

@@ -102,6 +102,8 @@ struct SceneHost {
     RefTreeOrder tree[2];
     double volume = 0.0;  // shared by both trees (dcollid.cpp:381, 422)
     int strain_edges = 0, strain_points = 0;
+    bool enabled = true;
+    int status = CC_OK;  // of the last resolve call
     int state = kHsDone;
     int niter = 0, cd_count = 0, zone_it = 0, hcol = 0, npass = 0;
     std::vector<int> pass_kinds;
@@ -275,6 +277,14 @@ struct cc_solver {
     float4* d_pbox_hi = nullptr;
     float4* d_p32 = nullptr;
     float4* d_v32 = nullptr;
+    // the scenes of a pass, when not all of them have one: their elements
+    // and points (expanded on the device from per-scene ranges)
+    int* d_act_e = nullptr;
+    int* d_act_p = nullptr;
+    int* d_sel = nullptr;        // 3 * nscenes: scene ids, element offsets, point offsets
+    int* h_sel = nullptr;        // pinned staging of d_sel
+    std::vector<int> sel_prev;   // scene ids of the last expanded selection
+    int n_act_e = 0, n_act_p = 0;
 
     // recording
     bool record = false;
@@ -351,6 +361,10 @@ struct cc_solver {
         apply.scan_temp = nullptr;
         dfree(d_rank[0]); dfree(d_rank[1]);
         dfree(d_rec); dfree(d_pbox_lo); dfree(d_pbox_hi); dfree(d_p32); dfree(d_v32);
+        dfree(d_act_e); dfree(d_act_p); dfree(d_sel);
+        if (h_sel) cudaFreeHost(h_sel);
+        h_sel = nullptr;
+        sel_prev.clear();
         pair_cap = contrib_cap = rec_cap = 0;
         nv = ne = nedges = 0;
         nscenes = 0;
@@ -441,6 +455,53 @@ struct cc_solver {
         uf_tail[py] = uf_tail[px];
     }
     cc_status zone_pass_unions();
+    // Elements and points of the scenes whose h_run mode is not idle, and
+    // each one's first leaf in the pass's hierarchy (sets h_run[].leaf0 and
+    // bvh.n / bvh.act; the lists are rebuilt only when the set changes).
+    void select_active() {
+        std::vector<int> ids;
+        int with_elems = 0;
+        int ae = 0, ap = 0;
+        for (int s = 0; s < nscenes; ++s) {
+            if (scenes[s].ne > 0) ++with_elems;
+            if (h_run[s].mode == kSceneIdle) {
+                h_run[s].leaf0 = -1;
+                continue;
+            }
+            h_run[s].leaf0 = ae;
+            ids.push_back(s);
+            ae += scenes[s].ne;
+            ap += scenes[s].nv;
+        }
+        if ((int)ids.size() == with_elems) {  // every scene: no lists needed
+            bvh.act = nullptr;
+            bvh.n = ne;
+            n_act_e = ne;
+            n_act_p = nv;
+            return;
+        }
+        bvh.act = d_act_e;
+        bvh.n = ae;
+        n_act_e = ae;
+        n_act_p = ap;
+        if (ids == sel_prev) return;
+        int k = (int)ids.size();
+        int* eoff = h_sel + k;
+        int* poff = h_sel + 2 * k + 1;
+        int e = 0, p = 0;
+        for (int j = 0; j < k; ++j) {
+            h_sel[j] = ids[j];
+            eoff[j] = e;
+            poff[j] = p;
+            e += scenes[ids[j]].ne;
+            p += scenes[ids[j]].nv;
+        }
+        eoff[k] = e;
+        poff[k] = p;
+        cudaMemcpyAsync(d_sel, h_sel, sizeof(int) * (3 * (size_t)k + 2), cudaMemcpyHostToDevice, stream);
+        expand_scenes(d_sel, d_sel + k, d_sel + 2 * k + 1, k, ae, ap, d_scenes, d_act_e, d_act_p, stream);
+        sel_prev.swap(ids);
+    }
 
     StrainPlan strain_plan() const {
         StrainPlan pl{strain_window, 0, false};
@@ -520,6 +581,7 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
             sd.hi[d] = hi[d];
         }
         sd.v0 = v0; sd.nv = snv; sd.e0 = e0; sd.ne = sne;
+        sd.enabled = 1;
         for (int i = 0; i < snv; ++i) {
             vscene[v0 + i] = si;
             fixed[v0 + i] = (m->fixed && m->fixed[i]) ? 1 : 0;
@@ -620,6 +682,10 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     ok &= dalloc(&d_pbox_hi, (size_t)nv) == cudaSuccess;
     ok &= dalloc(&d_p32, (size_t)nv) == cudaSuccess;
     ok &= dalloc(&d_v32, (size_t)nv) == cudaSuccess;
+    ok &= dalloc(&d_act_e, (size_t)ne) == cudaSuccess;
+    ok &= dalloc(&d_act_p, (size_t)nv) == cudaSuccess;
+    ok &= dalloc(&d_sel, 3 * (size_t)n + 2) == cudaSuccess;
+    ok &= cudaMallocHost(&h_sel, sizeof(int) * (3 * (size_t)n + 2)) == cudaSuccess;
     if (!ok) return fail(CC_NO_MEMORY, "device allocation failed");
     bvh.elem_scene = d_escene;
     bvh.scenes = d_scenes;
@@ -712,16 +778,18 @@ cc_status cc_solver::update_trees(int which) {
 // (dcollid.cpp:236-262). Retried with larger buffers on overflow. Leaves
 // every scene's hit count in h_run.
 cc_status cc_solver::detect_pass(int moving, bool any_zone) {
+    select_active();
     cudaMemcpyAsync(d_run, h_run, sizeof(SceneRun) * (size_t)nscenes, cudaMemcpyHostToDevice, stream);
     prof(kStBoxes, true);
-    leaf_boxes(d_ev, ne, d_escene, d_scenes, nscenes, d_xo, d_av, moving, d_box, bvh.bbox_enc, stream);
+    leaf_boxes(d_ev, bvh.act, bvh.n, d_escene, d_scenes, nscenes, d_xo, d_av, moving, d_box, bvh.bbox_enc, stream);
     prof(kStBoxes, false);
     cc_status st = update_trees(moving);
     if (st) return st;
     prof(kStBvh, true);
     bvh_build(d_box, bvh, stream);
     if (mode == 1)
-        point_boxes(d_xo, d_av, d_vscene, d_scenes, nv, moving, d_pbox_lo, d_pbox_hi, d_p32, d_v32, stream);
+        point_boxes(d_xo, d_av, d_vscene, d_scenes, bvh.act ? d_act_p : nullptr, n_act_p, moving, d_pbox_lo,
+                    d_pbox_hi, d_p32, d_v32, stream);
     prof(kStBvh, false);
     for (int attempt = 0; attempt < 8; ++attempt) {
         count_launch(), k_reset_pass<<<(nscenes + 255) / 256, 256, 0, stream>>>(d_ctr, d_run, nscenes);
@@ -875,9 +943,11 @@ cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, dou
         for (int s = 0; s < nscenes; ++s) has_collision[s] = 0;
     for (auto& sh : scenes) {
         sh.pass_kinds.clear();
-        sh.state = sh.ne > 0 ? kHsProx : kHsDone;
+        sh.state = (sh.ne > 0 && sh.enabled) ? kHsProx : kHsDone;
         sh.niter = sh.cd_count = sh.zone_it = sh.hcol = sh.npass = 0;
+        sh.status = CC_OK;
     }
+    std::string capped;
     if (ne == 0) {
         // the reference dereferences an empty tree here; nothing collides
         if (nv) cudaMemcpyAsync(x_out, x_cand, sizeof(double) * 3 * (size_t)nv, cudaMemcpyDeviceToDevice, stream);
@@ -906,13 +976,16 @@ cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, dou
                 m = kSceneCcd;
             } else if (sh.state == kHsZone) {
                 if (sh.zone_it++ >= zone_cap) {
-                    char buf[96];
-                    std::snprintf(buf, sizeof(buf), "impact-zone loop of scene %d did not converge", s);
-                    return fail(CC_ITER_CAP, buf);
+                    // the reference would loop on; this scene stops here and
+                    // is finished with its current velocities
+                    sh.status = CC_ITER_CAP;
+                    sh.state = kHsDone;
+                    capped += (capped.empty() ? "" : " ") + std::to_string(s);
+                } else {
+                    m = kSceneZone;
                 }
-                m = kSceneZone;
             }
-            h_run[s] = SceneRun{m, 0, sh.npass, -1};
+            h_run[s] = SceneRun{m, 0, sh.npass, -1, -1, {0, 0, 0}};
             if (m == kSceneIdle) continue;
             any = true;
             any_zone |= m == kSceneZone;
@@ -957,7 +1030,7 @@ cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, dou
     strain_limit(d_edges, nedges, d_strain_hdr, d_strain_load, d_strain_wb, d_scenes, nscenes, strain_plan(), d_xo,
                  d_av, d_strain_step, d_strain_passes, stream);
     prof(kStStrain, false);
-    final_velocity(d_in_elem, d_hc, d_av, vel, nv, stream);
+    final_velocity(d_in_elem, d_hc, d_av, d_vscene, d_scenes, vel, nv, stream);
     if (hc != d_hc) cudaMemcpyAsync(hc, d_hc, (size_t)nv, cudaMemcpyDeviceToDevice, stream);
     cudaMemcpyAsync(h_strain_passes.data(), d_strain_passes, sizeof(int) * h_strain_passes.size(),
                     cudaMemcpyDeviceToHost, stream);
@@ -974,7 +1047,12 @@ cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, dou
     prof_collect();
     if (has_collision)
         for (int s = 0; s < nscenes; ++s) has_collision[s] = scenes[s].hcol;
-    return cuda_check("resolve");
+    cc_status st = cuda_check("resolve");
+    if (st) return st;
+    if (!capped.empty())
+        return fail(CC_ITER_CAP, "impact-zone loop did not converge within the cap in scene(s) " + capped +
+                                     "; their step was finished with the last velocities");
+    return CC_OK;
 }
 
 // Exact FP64 re-check of a finished step: every element pair whose swept
@@ -993,9 +1071,11 @@ cc_status cc_solver::check_ccd(const double* x_old, const double* x_new, long lo
     count_launch(), k_reset_counters<<<1, 1, 0, stream>>>(d_ctr);
     cudaMemsetAsync(&d_ctr->err, 0, sizeof(int), stream);
     step_init(x_old, x_new, nv, d_in_elem, d_vscene, d_scenes, d_xo, d_av, d_ctr, stream);
-    for (int s = 0; s < nscenes; ++s) h_run[s] = SceneRun{scenes[s].ne > 0 ? kSceneCcd : kSceneIdle, 0, 0, -1};
+    for (int s = 0; s < nscenes; ++s)
+        h_run[s] = SceneRun{scenes[s].ne > 0 ? kSceneCcd : kSceneIdle, 0, 0, -1, -1, {0, 0, 0}};
+    select_active();
     cudaMemcpyAsync(d_run, h_run, sizeof(SceneRun) * (size_t)nscenes, cudaMemcpyHostToDevice, stream);
-    leaf_boxes(d_ev, ne, d_escene, d_scenes, nscenes, d_xo, d_av, 1, d_box, bvh.bbox_enc, stream);
+    leaf_boxes(d_ev, bvh.act, bvh.n, d_escene, d_scenes, nscenes, d_xo, d_av, 1, d_box, bvh.bbox_enc, stream);
     bvh_build(d_box, bvh, stream);
     for (int attempt = 0; attempt < 8; ++attempt) {
         count_launch(), k_reset_pass<<<(nscenes + 255) / 256, 256, 0, stream>>>(d_ctr, d_run, nscenes);
@@ -1042,14 +1122,15 @@ cc_status copy_in_and_resolve(cc_solver* s, const double* x_old, const double* x
         cudaMemcpyAsync(s->d_hc, has_collsn, (size_t)s->nv, cudaMemcpyHostToDevice, s->stream);
     }
     cc_status st = s->resolve(s->d_xold_in, s->d_xcand_in, s->d_vel, s->d_hc, s->d_xout, has_collision);
-    if (st) return st;
+    // a scene stopped at the zone cap still completes the call's outputs
+    if (st != CC_OK && st != CC_ITER_CAP) return st;
     if (s->nv) {
         cudaMemcpyAsync(x_out, s->d_xout, b3, cudaMemcpyDeviceToHost, s->stream);
         cudaMemcpyAsync(vel, s->d_vel, b3, cudaMemcpyDeviceToHost, s->stream);
         cudaMemcpyAsync(has_collsn, s->d_hc, (size_t)s->nv, cudaMemcpyDeviceToHost, s->stream);
     }
     if (cudaStreamSynchronize(s->stream) != cudaSuccess) return s->cuda_check("read back");
-    return CC_OK;
+    return st;
 }
 
 // has_collision of a whole solver: any scene's.
@@ -1175,6 +1256,26 @@ cc_status cc_check_ccd(cc_solver* s, const double* x_old, const double* x_new, l
     return s->check_ccd(x_old, x_new, hits, scene_hits);
 }
 
+cc_status cc_set_zone_cap(cc_solver* s, int cap) {
+    if (!s || cap < 0) return CC_BAD_INPUT;
+    s->zone_cap = cap;
+    return CC_OK;
+}
+
+cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on) {
+    if (!s || scene < 0 || scene >= s->nscenes) return CC_BAD_INPUT;
+    s->scenes[scene].enabled = on != 0;
+    s->h_scenes[scene].enabled = on != 0;
+    s->scenes_dirty = true;
+    return CC_OK;
+}
+
+cc_status cc_get_scene_status(cc_solver* s, int* out) {
+    if (!s || !out) return CC_BAD_INPUT;
+    for (int i = 0; i < s->nscenes; ++i) out[i] = s->scenes[i].status;
+    return CC_OK;
+}
+
 cc_status cc_set_host_threads(cc_solver* s, int n) {
     if (!s || n < 0) return CC_BAD_INPUT;
     s->host_threads = n;
@@ -1245,10 +1346,13 @@ int cc_debug_candidate_pairs(cc_solver* s, int moving, int brute_force, int* out
     if (!s || s->ne == 0) return 0;
     cudaSetDevice(s->device);
     s->upload_scenes();
-    for (int i = 0; i < s->nscenes; ++i) s->h_run[i] = SceneRun{moving ? kSceneCcd : kSceneProx, 0, 0, -1};
+    for (int i = 0; i < s->nscenes; ++i)
+        s->h_run[i] = SceneRun{s->scenes[i].ne > 0 ? (moving ? kSceneCcd : kSceneProx) : kSceneIdle, 0, 0, -1, -1,
+                               {0, 0, 0}};
+    s->select_active();
     cudaMemcpyAsync(s->d_run, s->h_run, sizeof(SceneRun) * (size_t)s->nscenes, cudaMemcpyHostToDevice, s->stream);
-    leaf_boxes(s->d_ev, s->ne, s->d_escene, s->d_scenes, s->nscenes, s->d_xo, s->d_av, moving, s->d_box,
-               s->bvh.bbox_enc, s->stream);
+    leaf_boxes(s->d_ev, s->bvh.act, s->bvh.n, s->d_escene, s->d_scenes, s->nscenes, s->d_xo, s->d_av, moving,
+               s->d_box, s->bvh.bbox_enc, s->stream);
     if (!brute_force) bvh_build(s->d_box, s->bvh, s->stream);
     for (int attempt = 0; attempt < 8; ++attempt) {
         count_launch(), k_reset_counters<<<1, 1, 0, s->stream>>>(s->d_ctr);

@@ -179,6 +179,19 @@ class CollisionSolver3d:
         hi = _c(U, np.float64)
         self._check(self._lib.cc_set_scene_domain_boundary(self._h, int(scene), lo.ctypes.data, hi.ctypes.data))
 
+    def setZoneCap(self, cap: int):
+        """Impact-zone passes per scene and step before the loop is stopped."""
+        self._check(self._lib.cc_set_zone_cap(self._h, int(cap)))
+
+    def setSceneEnabled(self, scene: int, on: bool):
+        self._check(self._lib.cc_set_scene_enabled(self._h, int(scene), int(bool(on))))
+
+    def sceneStatus(self) -> np.ndarray:
+        """Status of every scene in the last resolve call (0, or 4 = CC_ITER_CAP)."""
+        out = np.zeros(max(self.numScenes(), 1), dtype=np.int32)
+        self._check(self._lib.cc_get_scene_status(self._h, out.ctypes.data_as(C.POINTER(C.c_int))))
+        return out[:self.numScenes()]
+
     def setHostThreads(self, n: int):
         self._check(self._lib.cc_set_host_threads(self._h, int(n)))
 
@@ -191,9 +204,10 @@ class CollisionSolver3d:
         hc = np.array(has_collsn, dtype=np.uint8, copy=True, order="C")
         x_out = np.empty_like(x_old)
         hcol = np.zeros(max(self.numScenes(), 1), dtype=np.int32)
-        self._check(self._lib.cc_resolve_batch(self._h, x_old.ctypes.data, x_cand.ctypes.data, vel.ctypes.data,
-                                               hc.ctypes.data, x_out.ctypes.data,
-                                               hcol.ctypes.data_as(C.POINTER(C.c_int))))
+        st = self._lib.cc_resolve_batch(self._h, x_old.ctypes.data, x_cand.ctypes.data, vel.ctypes.data,
+                                        hc.ctypes.data, x_out.ctypes.data, hcol.ctypes.data_as(C.POINTER(C.c_int)))
+        if st != self.ITER_CAP:  # scenes that reached the zone cap: see sceneStatus()
+            self._check(st)
         self._has_collision = bool(hcol.any())
         return x_out, vel, hc, hcol.astype(bool)
 
@@ -201,9 +215,11 @@ class CollisionSolver3d:
         """resolveCollision() on every scene, device tensors as in
         resolveCollisionDevice. Returns has_collision per scene."""
         hcol = np.zeros(max(self.numScenes(), 1), dtype=np.int32)
-        self._check(self._lib.cc_resolve_batch_device(self._h, x_old.data_ptr(), x_cand.data_ptr(), vel.data_ptr(),
-                                                      has_collsn.data_ptr(), x_out.data_ptr(),
-                                                      hcol.ctypes.data_as(C.POINTER(C.c_int))))
+        st = self._lib.cc_resolve_batch_device(self._h, x_old.data_ptr(), x_cand.data_ptr(), vel.data_ptr(),
+                                               has_collsn.data_ptr(), x_out.data_ptr(),
+                                               hcol.ctypes.data_as(C.POINTER(C.c_int)))
+        if st != self.ITER_CAP:
+            self._check(st)
         self._has_collision = bool(hcol.any())
         return hcol.astype(bool)
 
@@ -251,6 +267,7 @@ class CollisionSolver3d:
         self._check(self._lib.cc_set_stream(self._h, stream_handle))
 
     PLAIN_FP64, MIXED = 0, 1
+    ITER_CAP = 4
 
     def setMode(self, mode: int):
         """0: plain FP64; 1: FP32 filters in front of the same FP64 tests."""

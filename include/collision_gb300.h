@@ -159,6 +159,19 @@ cc_status cc_resolve_batch_device(cc_solver* s, const double* x_old, const doubl
  * recorded visits are kept). */
 cc_status cc_check_ccd(cc_solver* s, const double* x_old, const double* x_new, long long* hits, int* scene_hits);
 
+/* Impact-zone passes per scene and step before the loop is stopped
+ * (default 10000). The reference's loop (dcollid.cpp:346-352) has no bound
+ * and does not end for some configurations; a scene that reaches the cap is
+ * finished with its current velocities, its status becomes CC_ITER_CAP
+ * (cc_get_scene_status, one int per scene) and the call returns CC_ITER_CAP
+ * after completing every other scene. */
+cc_status cc_set_zone_cap(cc_solver* s, int cap);
+cc_status cc_get_scene_status(cc_solver* s, int* out);
+/* Leave a scene out of the following resolve calls (on = 0) or take it
+ * back: a disabled scene's points get x_out = x_cand and keep their
+ * velocities and flags. */
+cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
+
 /* Host threads that emulate the reference's tree insertion order when a
  * scene's tree is (re)built, one scene per thread (0 = one per hardware
  * thread, the default). */

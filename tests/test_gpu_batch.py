@@ -213,3 +213,47 @@ def test_ccd_recheck_after_resolved_steps(solver_cls):
         x = xo
     assert unresolved > 0
     b.close()
+
+
+def test_zone_cap_stops_one_scene_only(solver_cls):
+    """Scene 186 of the 256-scene workload (an 80x80 cloth on a box) reaches
+    an impact-zone loop that the reference never leaves (the oracle runs
+    into its cap there too). In a batch, that scene stops at the cap and the
+    others finish exactly as they do alone; disabled afterwards, its points
+    pass through."""
+    stuck = scenes.batched(nscenes=256, seed=0)[186]
+    other = scenes.cloth_on_obstacle(20, "sphere", 0.2, 2.0, seed=3)
+    mix = [stuck, other]
+    b = solver_cls(0)
+    b.assembleBatch(mix)
+    b.setMode(1)
+    b.setZoneCap(40)
+    s = solver_cls(0)
+    s.assembleFromScene(other)
+    pv, _ = b.sceneOffsets()
+    x = np.concatenate([q.x for q in mix])
+    v = np.concatenate([q.v for q in mix])
+    hc = np.zeros(len(x), np.uint8)
+    xs, vs, hs = other.x, other.v, np.zeros(other.nv, np.uint8)
+    capped_at = None
+    for step in range(70):
+        xc = x + 1e-3 * v
+        xo, vo, ho, _ = b.resolveCollisionBatch(x, xc, v, hc)
+        status = b.sceneStatus()
+        xs, vs, hs = s.resolveCollision(xs, xs + 1e-3 * vs, vs, hs)
+        assert status[1] == 0
+        assert np.array_equal(_split(xo, pv, 1), xs) and np.array_equal(_split(vo, pv, 1), vs), step
+        if status[0] != 0:
+            assert status[0] == solver_cls.ITER_CAP
+            capped_at = step
+            b.setSceneEnabled(0, False)
+            x, v, hc = xo, vo, ho
+            xc = x + 1e-3 * v
+            xo, vo, ho, _ = b.resolveCollisionBatch(x, xc, v, hc)
+            assert np.array_equal(_split(xo, pv, 0), _split(xc, pv, 0))
+            assert np.array_equal(_split(vo, pv, 0), _split(v, pv, 0))
+            break
+        x, v, hc = xo, vo, ho
+    assert capped_at is not None
+    b.close()
+    s.close()
