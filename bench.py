@@ -12,7 +12,7 @@ per second.
   value       mixed precision, batched: all scenes in one solver, inputs in
               HBM, each step through cc_resolve_batch_device
   plain_fp64  the plain FP64 GPU path one scene at a time (one solver per
-              scene, cc_resolve_device on each) over the first steps of the
+              scene, cc_resolve_device on each) over the same steps of the
               same trajectory; its final state must equal the batch's bit
               for bit
   e2e         the batched mixed path through cc_resolve_batch with pinned
@@ -20,6 +20,11 @@ per second.
   missed_ccd  element pairs that still collide after a step, by the exact
               FP64 CCD re-check (cc_check_ccd) after every timed step,
               outside the timed region
+  zone cap    the reference's impact-zone loop does not end on some of these
+              scenes (an 80x80 cloth on a box at step 56 is the first); such a
+              scene stops after --zone-cap zone passes, is counted in
+              capped_scenes and is left out of the following steps (in every
+              arm alike)
   L2          flushed (256 MiB write) before every timed step
 
 --workload picks one of the other measured scenes (folded_cloth,
@@ -51,9 +56,10 @@ PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 NARROW_BYTES_PER_VISIT = 8 + 8 + 24 + 6 * 64  # pair, two leaf ranks, two elements' ids, x_old+avgVel of 6 points
 
 
-def make_workload(name, seed):
+def make_workload(name, seed, nscenes=0):
     from collision_gb300 import scenes
-    return scenes.workload(name, seed=seed)
+    scs = scenes.workload(name, seed=seed)
+    return scs[:nscenes] if nscenes > 0 else scs
 
 
 def describe(name, scs):
@@ -122,23 +128,36 @@ class Clocks:
 
 
 # ------------------------------------------------------------- CPU (oracle)
-def oracle_rate(scs, max_steps, budget_s, threads, skip_steps=0):
+ORACLE_ITER_CAP = -3
+
+
+def oracle_rate(scs, max_steps, budget_s, threads, zone_cap, skip_steps=0):
     """Scene-steps/s of the CPU restatement over the trajectory, all scenes
     stepped together (one scene per thread, `threads` at once); the first
     `skip_steps` steps are run untimed. Stops after max_steps timed steps or
-    once budget_s of timed steps has passed. Returns (rate, scene-steps,
-    seconds, steps)."""
+    once budget_s of timed steps has passed. A scene whose impact-zone loop
+    reaches zone_cap is left out from then on, as in the GPU arms. Returns
+    (rate, scene-steps, seconds, steps)."""
     from collision_gb300 import scenes
     from oracle.ccopy import OracleSolver
     solvers = [OracleSolver(sc, record=0) for sc in scs]
+    for o in solvers:
+        o.set_zone_cap(zone_cap)
     state = [(sc.x.copy(), sc.v.copy(), np.zeros(sc.nv, np.uint8)) for sc in scs]
+    live = [True] * len(scs)
 
     def one(i):
+        if not live[i]:
+            return 0
         x, v, hc = state[i]
         r = solvers[i].step(x, scenes.candidate(scs[i], x, v), v, hc)
+        if r["rc"] == ORACLE_ITER_CAP:
+            live[i] = False
+            return 1
         if r["rc"] != 0:
             raise RuntimeError(f"oracle step failed on scene {i}: {r['rc']}")
         state[i] = (r["x"], r["v"], r["has_collsn"])
+        return 1
 
     done, t_total, steps = 0, 0.0, 0
     with ThreadPoolExecutor(max_workers=threads) as ex:
@@ -146,9 +165,9 @@ def oracle_rate(scs, max_steps, budget_s, threads, skip_steps=0):
             list(ex.map(one, range(len(scs))))
         while steps < max_steps and t_total < budget_s:
             t0 = time.perf_counter()
-            list(ex.map(one, range(len(scs))))
+            n = sum(ex.map(one, range(len(scs))))
             t_total += time.perf_counter() - t0
-            done += len(scs)
+            done += n
             steps += 1
     return done / t_total, done, t_total, steps
 
@@ -157,9 +176,10 @@ def run_reference(args):
     ws, rk, _ = dist_env()
     if rk != 0:
         return
-    scs = make_workload(args.workload, args.seed)
+    scs = make_workload(args.workload, args.seed, args.scenes)
     threads = os.cpu_count() or 1
-    rate, n, t, steps = oracle_rate(scs, args.steps, args.ref_budget, threads, skip_steps=args.warmup)
+    rate, n, t, steps = oracle_rate(scs, args.steps, args.ref_budget, threads, args.zone_cap,
+                                    skip_steps=args.warmup)
     sample = (f"{args.workload}: {len(scs)} scenes, steps {args.warmup}..{args.warmup + steps - 1} of the "
               f"trajectory ({n} scene-steps, {t:.1f} s), one scene per thread")
     line = {"metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": ws, "steps": steps,
@@ -181,9 +201,10 @@ def run_gpu(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     dev = lrk
     torch.cuda.set_device(dev)
+    from collision_gb300 import _lib
     from collision_gb300.solver import CollisionSolver3d
     seed = args.seed + rk
-    scs = make_workload(args.workload, seed)
+    scs = make_workload(args.workload, seed, args.scenes)
     nsc = len(scs)
     stream = torch.cuda.Stream(device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -192,7 +213,7 @@ def run_gpu(args):
     dtcol = np.concatenate([np.full((s.nv, 1), s.params["dt"]) for s in scs])
     offs = np.cumsum([0] + [s.nv for s in scs])
     W, K = args.warmup, args.steps
-    n_plain = min(K, args.plain_steps)
+    n_plain = min(K, args.plain_steps) if args.plain_steps > 0 else K
 
     def device_state():
         with torch.cuda.stream(stream):
@@ -222,29 +243,40 @@ def run_gpu(args):
         return float(t.item())
 
     # ------------------------------------------- batched, device-resident
+    def drop_capped(s, enabled):
+        for q in np.nonzero(s.sceneStatus())[0]:
+            s.setSceneEnabled(int(q), False)
+            enabled[int(q)] = False
+
     def batched_run(mode, check):
         s = CollisionSolver3d(dev)
         s.assembleBatch(scs)
         s.setMode(mode)
+        s.setZoneCap(args.zone_cap)
         s.setStream(stream.cuda_stream)
         st = device_state()
+        enabled = np.ones(nsc, dtype=bool)
         with torch.cuda.stream(stream):
             for _ in range(W):
                 candidate(st)
                 s.resolveCollisionBatchDevice(st["x"], st["xc"], st["v"], st["hc"], st["xo"])
+                drop_capped(s, enabled)
                 st["x"], st["xo"] = st["xo"], st["x"]
         sync_all()
+        scene_steps = 0
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
         counters, missed, snap = [], 0, None
         s.setProfiling(True)
         with Clocks(dev) as clk, torch.cuda.stream(stream):
             for k in range(K):
                 flush.fill_(float(k))
+                scene_steps += int(enabled.sum())
                 evs[k][0].record(stream)
                 candidate(st)
                 s.resolveCollisionBatchDevice(st["x"], st["xc"], st["v"], st["hc"], st["xo"])
                 evs[k][1].record(stream)
                 counters.append(s.counters())
+                drop_capped(s, enabled)
                 if check:
                     hits, _ = s.checkCCD(st["x"], st["xo"])
                     missed += hits
@@ -257,89 +289,114 @@ def run_gpu(args):
         prof = s.profile()
         s.close()
         return dict(total_ms=max_over_ranks(float(sum(step_ms))), step_ms=step_ms, counters=counters,
-                    missed=missed, snap=snap, prof=prof, clocks=clk.summary())
-
-    mixed = batched_run(1, check=not args.no_check)
-    batch_plain = batched_run(0, check=False)
+                    missed=missed, snap=snap, prof=prof, clocks=clk.summary(), scene_steps=scene_steps,
+                    capped=int((~enabled).sum()))
 
     # ------------------------------ plain FP64, one scene at a time
-    solvers = []
-    for sc in scs:
-        s = CollisionSolver3d(dev)
-        s.assembleFromScene(sc)
-        s.setMode(0)
-        s.setStream(stream.cuda_stream)
-        solvers.append(s)
-    st = device_state()
+    def plain_sequential():
+        solvers = []
+        for sc in scs:
+            s = CollisionSolver3d(dev)
+            s.assembleFromScene(sc)
+            s.setMode(0)
+            s.setZoneCap(args.zone_cap)
+            s.setStream(stream.cuda_stream)
+            solvers.append(s)
+        st = device_state()
+        seq_enabled = np.ones(nsc, dtype=bool)
 
-    def seq_step():
-        candidate(st)
-        for i, s in enumerate(solvers):
-            a, b = int(offs[i]), int(offs[i + 1])
-            s.resolveCollisionDevice(st["x"][a:b], st["xc"][a:b], st["v"][a:b], st["hc"][a:b], st["xo"][a:b])
-        st["x"], st["xo"] = st["xo"], st["x"]
+        def seq_step():
+            candidate(st)
+            for i, s in enumerate(solvers):
+                a, b = int(offs[i]), int(offs[i + 1])
+                if not seq_enabled[i]:  # left out, as in the batch: candidates pass through
+                    st["xo"][a:b].copy_(st["xc"][a:b])
+                    continue
+                try:
+                    s.resolveCollisionDevice(st["x"][a:b], st["xc"][a:b], st["v"][a:b], st["hc"][a:b], st["xo"][a:b])
+                except _lib.CCError as e:
+                    if e.status != CollisionSolver3d.ITER_CAP:
+                        raise
+                    seq_enabled[i] = False
+            st["x"], st["xo"] = st["xo"], st["x"]
 
-    with torch.cuda.stream(stream):
-        for _ in range(W):
-            seq_step()
-    sync_all()
-    seq_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n_plain)]
-    seq_launches = 0
-    with torch.cuda.stream(stream):
-        for k in range(n_plain):
-            flush.fill_(float(k))
-            seq_ev[k][0].record(stream)
-            seq_step()
-            seq_ev[k][1].record(stream)
-            seq_launches += 2 + sum(s.counters()["kernel_launches"] for s in solvers)
-        stream.synchronize()
-    seq_ms = max_over_ranks(float(sum(a.elapsed_time(b) for a, b in seq_ev)))
-    seq_snap = (st["x"].cpu().numpy(), st["v"].cpu().numpy())
-    for s in solvers:
-        s.close()
-    del solvers
-    same = bool(np.array_equal(mixed["snap"][0], seq_snap[0]) and np.array_equal(mixed["snap"][1], seq_snap[1]))
-    diff = float(np.abs(mixed["snap"][0] - seq_snap[0]).max())
+        with torch.cuda.stream(stream):
+            for _ in range(W):
+                seq_step()
+        sync_all()
+        seq_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n_plain)]
+        seq_launches = 0
+        seq_scene_steps = 0
+        with torch.cuda.stream(stream):
+            for k in range(n_plain):
+                flush.fill_(float(k))
+                seq_scene_steps += int(seq_enabled.sum())
+                seq_ev[k][0].record(stream)
+                seq_step()
+                seq_ev[k][1].record(stream)
+                seq_launches += 2 + sum(s.counters()["kernel_launches"] for s in solvers)
+            stream.synchronize()
+        seq_ms = max_over_ranks(float(sum(a.elapsed_time(b) for a, b in seq_ev)))
+        seq_snap = (st["x"].cpu().numpy(), st["v"].cpu().numpy())
+        for s in solvers:
+            s.close()
+        del solvers
+        same = bool(np.array_equal(mixed["snap"][0], seq_snap[0]) and np.array_equal(mixed["snap"][1], seq_snap[1]))
+        diff = float(np.abs(mixed["snap"][0] - seq_snap[0]).max())
+        return dict(ms=seq_ms, scene_steps=seq_scene_steps, launches=seq_launches, same=same, diff=diff)
+
 
     # ------------------------------------------------ end to end (host)
-    s2 = CollisionSolver3d(dev)
-    s2.assembleBatch(scs)
-    s2.setMode(1)
-    s2.setStream(stream.cuda_stream)
-    pin = lambda a: torch.tensor(a).pin_memory()
-    hx, hv, hdt = pin(x0), pin(v0), pin(dtcol)
-    hhc = torch.zeros(len(x0), dtype=torch.uint8).pin_memory()
-    hxc, hxo = torch.empty_like(hx).pin_memory(), torch.empty_like(hx).pin_memory()
-    hcol = np.zeros(nsc, dtype=np.int32)
-    import ctypes as C
-    lib = s2._lib
+    def e2e_run():
+        s2 = CollisionSolver3d(dev)
+        s2.assembleBatch(scs)
+        s2.setMode(1)
+        s2.setZoneCap(args.zone_cap)
+        s2.setStream(stream.cuda_stream)
+        e2e_enabled = np.ones(nsc, dtype=bool)
+        pin = lambda a: torch.tensor(a).pin_memory()
+        hx, hv, hdt = pin(x0), pin(v0), pin(dtcol)
+        hhc = torch.zeros(len(x0), dtype=torch.uint8).pin_memory()
+        hxc, hxo = torch.empty_like(hx).pin_memory(), torch.empty_like(hx).pin_memory()
+        hcol = np.zeros(nsc, dtype=np.int32)
+        import ctypes as C
+        lib = s2._lib
 
-    def e2e_call():
-        rc = lib.cc_resolve_batch(s2._h, hx.data_ptr(), hxc.data_ptr(), hv.data_ptr(), hhc.data_ptr(),
-                                  hxo.data_ptr(), hcol.ctypes.data_as(C.POINTER(C.c_int)))
-        if rc != 0:
-            s2._check(rc)
+        def e2e_call():
+            rc = lib.cc_resolve_batch(s2._h, hx.data_ptr(), hxc.data_ptr(), hv.data_ptr(), hhc.data_ptr(),
+                                      hxo.data_ptr(), hcol.ctypes.data_as(C.POINTER(C.c_int)))
+            if rc not in (0, CollisionSolver3d.ITER_CAP):
+                s2._check(rc)
+            drop_capped(s2, e2e_enabled)
 
-    def host_candidate():
-        np.add(hx.numpy(), hdt.numpy() * hv.numpy(), out=hxc.numpy())
+        def host_candidate():
+            np.add(hx.numpy(), hdt.numpy() * hv.numpy(), out=hxc.numpy())
 
-    for _ in range(W):
-        host_candidate()
-        e2e_call()
-        hx.copy_(hxo)
-    ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-    with torch.cuda.stream(stream):
-        for k in range(K):
+        for _ in range(W):
             host_candidate()
-            flush.fill_(float(k))
-            stream.synchronize()
-            ev2[k][0].record(stream)
             e2e_call()
-            ev2[k][1].record(stream)
             hx.copy_(hxo)
-        stream.synchronize()
-    e2e_ms = max_over_ranks(float(sum(a.elapsed_time(b) for a, b in ev2)))
-    s2.close()
+        ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+        with torch.cuda.stream(stream):
+            for k in range(K):
+                host_candidate()
+                flush.fill_(float(k))
+                stream.synchronize()
+                ev2[k][0].record(stream)
+                e2e_call()
+                ev2[k][1].record(stream)
+                hx.copy_(hxo)
+            stream.synchronize()
+        e2e_ms = max_over_ranks(float(sum(a.elapsed_time(b) for a, b in ev2)))
+        s2.close()
+        return e2e_ms
+
+
+    arms = set(args.arms.split(","))
+    mixed = batched_run(1, check=not args.no_check)
+    batch_plain = batched_run(0, check=False) if "batch_plain" in arms else None
+    plain = plain_sequential() if "plain" in arms else None
+    e2e_ms = e2e_run() if "e2e" in arms else None
     nv = len(x0)
     h2d = nv * (3 * 8 * 3 + 1)   # x_old, x_cand, vel, has_collsn
     d2h = nv * (3 * 8 * 2 + 1) + 4 * nsc  # x_out, vel, has_collsn, has_collision
@@ -349,10 +406,10 @@ def run_gpu(args):
             torch.distributed.destroy_process_group()
         return
 
-    value = ws * K * nsc / (mixed["total_ms"] / 1e3)
-    plain_value = ws * n_plain * nsc / (seq_ms / 1e3)
-    batch_plain_value = ws * K * nsc / (batch_plain["total_ms"] / 1e3)
-    e2e_value = ws * K * nsc / (e2e_ms / 1e3)
+    value = ws * mixed["scene_steps"] / (mixed["total_ms"] / 1e3)
+    plain_value = ws * plain["scene_steps"] / (plain["ms"] / 1e3) if plain else None
+    batch_plain_value = ws * batch_plain["scene_steps"] / (batch_plain["total_ms"] / 1e3) if batch_plain else None
+    e2e_value = ws * mixed["scene_steps"] / (e2e_ms / 1e3) if e2e_ms else None
 
     # ----------------------------------------------------------- roofline
     peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
@@ -382,7 +439,7 @@ def run_gpu(args):
     cpu = None
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        rate, n, t, steps = oracle_rate(scs, W + K, args.cpu_budget, threads)
+        rate, n, t, steps = oracle_rate(scs, W + K, args.cpu_budget, threads, args.zone_cap)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{args.workload}: {nsc} scenes, first {steps} steps of the trajectory "
                          f"({n} scene-steps, {t:.1f} s), one scene per thread"}
@@ -395,14 +452,18 @@ def run_gpu(args):
                                 "tests, all scenes per launch",
                            l2="flushed before every timed step",
                            parallelism="replicas" if ws > 1 else "single"),
-            "plain_fp64": {"value": plain_value, "steps": n_plain, "ms_per_step": seq_ms / n_plain,
-                           "path": "plain FP64, one scene per call", "gpu_launches": seq_launches,
-                           "state_equal_after_steps": same, "max_abs_diff": diff},
-            "speedup_vs_plain": value / plain_value,
-            "batched_plain_fp64": {"value": batch_plain_value, "ms_per_step": batch_plain["total_ms"] / K},
+            "plain_fp64": None if not plain else {
+                "value": plain_value, "steps": n_plain, "ms_per_step": plain["ms"] / n_plain,
+                "path": "plain FP64, one scene per call", "gpu_launches": plain["launches"],
+                "state_equal_after_steps": plain["same"], "max_abs_diff": plain["diff"]},
+            "speedup_vs_plain": value / plain_value if plain else None,
+            "batched_plain_fp64": None if not batch_plain else {
+                "value": batch_plain_value, "ms_per_step": batch_plain["total_ms"] / K},
             "missed_ccd": None if args.no_check else int(mixed["missed"]),
+            "capped_scenes": mixed["capped"], "zone_cap": args.zone_cap,
             "roofline": roof, "cpu_baseline": cpu, "clocks": mixed["clocks"],
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "e2e": None if e2e_value is None else
+                   {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),
             "step_ms_quantiles": [round(float(q), 3) for q in np.quantile(mixed["step_ms"], [0, .25, .5, .75, 1])],
             "counters": tot, "stages_ms": {k: round(v[0], 3) for k, v in prof.items()}}
@@ -420,7 +481,12 @@ def main():
     ap.add_argument("--workload", default="batched",
                     choices=["batched", "folded_cloth", "cloth_on_sphere", "strings", "large"])
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--plain-steps", type=int, default=10, help="timed steps of the one-scene-at-a-time run")
+    ap.add_argument("--plain-steps", type=int, default=0,
+                    help="timed steps of the one-scene-at-a-time run (0: all K)")
+    ap.add_argument("--zone-cap", type=int, default=1000)
+    ap.add_argument("--arms", default="mixed,batch_plain,plain,e2e",
+                    help="arms to run besides the headline batched mixed one (for profiling runs)")
+    ap.add_argument("--scenes", type=int, default=0, help="first N scenes of the batched workload (0: all)")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--ref-budget", type=float, default=120.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -105,4 +105,83 @@ private:
     int n_points_ = 0;
 };
 
+// Many independent scenes in one solver (cc_assemble_batch): each scene is
+// what one CollisionSolver3d holds, with its own parameters and domain box.
+// Point arrays of the resolve call hold scene 0's points, then scene 1's...
+class SceneBatch {
+public:
+    struct Mesh {
+        int n_points = 0;
+        std::vector<int32_t> tris, tri_surface;
+        std::vector<double> tri_rest_len;
+        std::vector<int32_t> bonds;
+        std::vector<double> bond_rest_len;
+        std::vector<uint8_t> fixed;
+    };
+
+    explicit SceneBatch(int device = 0) { check(cc_create(device, &s_), "cc_create"); }
+    ~SceneBatch() { cc_destroy(s_); }
+    SceneBatch(const SceneBatch&) = delete;
+    SceneBatch& operator=(const SceneBatch&) = delete;
+
+    void assemble(const std::vector<Mesh>& meshes) {
+        std::vector<cc_mesh> ms(meshes.size());
+        for (size_t i = 0; i < meshes.size(); ++i) {
+            const Mesh& m = meshes[i];
+            ms[i].n_points = m.n_points;
+            ms[i].n_tris = (int32_t)(m.tris.size() / 3);
+            ms[i].tris = m.tris.data();
+            ms[i].tri_surface = m.tri_surface.empty() ? nullptr : m.tri_surface.data();
+            ms[i].tri_rest_len = m.tri_rest_len.data();
+            ms[i].n_bonds = (int32_t)(m.bonds.size() / 2);
+            ms[i].bonds = m.bonds.data();
+            ms[i].bond_rest_len = m.bond_rest_len.data();
+            ms[i].fixed = m.fixed.empty() ? nullptr : m.fixed.data();
+        }
+        check(cc_assemble_batch(s_, ms.data(), (int)ms.size()), "assemble_batch");
+        n_ = (int)meshes.size();
+        point_off_.assign((size_t)n_ + 1, 0);
+        check(cc_get_scene_offsets(s_, point_off_.data(), nullptr), "scene offsets");
+        has_collision_.assign((size_t)n_, 0);
+        status_.assign((size_t)n_, 0);
+    }
+    int numScenes() const { return n_; }
+    // first point of each scene; the last entry is the total
+    const std::vector<int32_t>& pointOffsets() const { return point_off_; }
+
+    void setParams(int scene, const cc_params& p) { check(cc_set_scene_params(s_, scene, &p), "scene params"); }
+    void setParams(const cc_params& p) { check(cc_set_params(s_, &p), "params"); }
+    void setDomainBoundary(int scene, const double* L, const double* U) {
+        check(cc_set_scene_domain_boundary(s_, scene, L, U), "scene domain");
+    }
+    void setZoneCap(int cap) { check(cc_set_zone_cap(s_, cap), "zone cap"); }
+    void setSceneEnabled(int scene, bool on) { check(cc_set_scene_enabled(s_, scene, on ? 1 : 0), "enable"); }
+
+    // resolveCollision on every scene (host arrays over all points). Returns
+    // false when some scene stopped at the impact-zone cap (see status()).
+    bool resolveCollision(const double* x_old, const double* x_cand, double* vel, uint8_t* has_collsn,
+                          double* x_out) {
+        cc_status st = cc_resolve_batch(s_, x_old, x_cand, vel, has_collsn, x_out, has_collision_.data());
+        if (st != CC_ITER_CAP) check(st, "resolve_batch");
+        check(cc_get_scene_status(s_, status_.data()), "scene status");
+        return st == CC_OK;
+    }
+    bool hasCollision(int scene) const { return has_collision_[(size_t)scene] != 0; }
+    int status(int scene) const { return status_[(size_t)scene]; }
+
+    cc_solver* handle() { return s_; }
+
+private:
+    void check(cc_status st, const char* what) {
+        if (st == CC_OK) return;
+        char buf[512] = {0};
+        if (s_) cc_last_error(s_, buf, sizeof(buf));
+        throw Error(st, std::string(what) + ": " + buf);
+    }
+    cc_solver* s_ = nullptr;
+    int n_ = 0;
+    std::vector<int32_t> point_off_;
+    std::vector<int> has_collision_, status_;
+};
+
 }  // namespace collision_gb300

@@ -51,3 +51,31 @@ def test_batched_sizes_deterministic():
     b = scenes.batched(nscenes=4, seed=3)
     assert [s.nv for s in a] == [s.nv for s in b]
     assert all(16 * 16 <= s.nv - (642 if s.nt > 12 + 2 * 15 * 15 + 1280 - 1 else 8) or True for s in a)
+
+
+def test_cpp_headers_compile_and_link(tmp_path):
+    """The C++ classes over the C ABI compile and link against the library
+    (nothing is called: there is no GPU here)."""
+    import shutil
+    import subprocess
+    from collision_gb300 import _lib
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    src = tmp_path / "use.cpp"
+    src.write_text(
+        '#include "collision_gb300.hpp"\n'
+        'int main(int argc, char**) {\n'
+        '  if (argc > 5) {\n'
+        '    collision_gb300::CollisionSolver3d s(0);\n'
+        '    collision_gb300::SceneBatch b(0);\n'
+        '    b.assemble({});\n'
+        '    return s.hasCollision() + b.numScenes();\n'
+        '  }\n'
+        '  return 0;\n'
+        '}\n')
+    out = tmp_path / "use"
+    inc = os.path.join(_lib.ROOT, "include")
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    r = subprocess.run(["g++", "-std=c++17", "-I", inc, str(src), "-o", str(out), "-L", libdir,
+                        "-lcollision_gb300", f"-Wl,-rpath,{libdir}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
