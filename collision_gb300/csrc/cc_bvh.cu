@@ -273,6 +273,33 @@ __device__ __forceinline__ bool overlap32(const Box32& a, const Box32& b) {
            (a.lo[2] <= b.hi[2] && a.hi[2] >= b.lo[2]);
 }
 
+// Doubles as order-preserving unsigned integers (-0 as +0), so that exact
+// box comparisons run on the integer pipe.
+__device__ __forceinline__ unsigned long long ord_double(unsigned long long u) {
+    if (u == 0x8000000000000000ull) u = 0;
+    return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+struct BoxOrd {
+    unsigned long long lo[3], hi[3];
+};
+__device__ __forceinline__ BoxOrd box_ord(const Box6& b) {
+    BoxOrd r;
+    for (int d = 0; d < 3; ++d) {
+        r.lo[d] = ord_double((unsigned long long)__double_as_longlong(b.lo[d]));
+        r.hi[d] = ord_double((unsigned long long)__double_as_longlong(b.hi[d]));
+    }
+    return r;
+}
+// Box6 a vs box b in memory, exactly as overlap(a, b).
+__device__ __forceinline__ bool overlap_ord(const BoxOrd& a, const Box6* bp) {
+    const ulonglong2* q = reinterpret_cast<const ulonglong2*>(bp);
+    ulonglong2 u0 = __ldg(q), u1 = __ldg(q + 1), u2 = __ldg(q + 2);
+    unsigned long long lo[3] = {u0.x, u0.y, u1.x}, hi[3] = {u1.y, u2.x, u2.y};
+    for (int d = 0; d < 3; ++d)
+        if (!(a.lo[d] <= ord_double(hi[d]) && a.hi[d] >= ord_double(lo[d]))) return false;
+    return true;
+}
+
 __device__ __forceinline__ bool overlap(const Box6& a, const Box6& b) {
     return (a.lo[0] <= b.hi[0] && a.hi[0] >= b.lo[0]) && (a.lo[1] <= b.hi[1] && a.hi[1] >= b.lo[1]) &&
            (a.lo[2] <= b.hi[2] && a.hi[2] >= b.lo[2]);
@@ -312,6 +339,7 @@ __global__ void k_traverse(const Box6* __restrict__ box, const unsigned int* __r
     }
     const Box6 q = box[ei];
     const Box32 q32 = box32_out(q);
+    const BoxOrd qo = box_ord(q);
     int stk[kTraversalStack];
     int sp = 0;
     stk[sp++] = root;
@@ -328,7 +356,7 @@ __global__ void k_traverse(const Box6* __restrict__ box, const unsigned int* __r
             int c = cs[k];
             if (c < 0) {
                 int ej = (int)order[~c];
-                if (!overlap(q, box[ej])) continue;  // the exact test
+                if (!overlap_ord(qo, &box[ej])) continue;  // the exact test
                 bool shared = false;
                 if (ev) {
                     int a = ev[3 * ej], b = ev[3 * ej + 1], c3 = ev[3 * ej + 2];
@@ -417,11 +445,11 @@ void bvh_build(const Box6* box, BvhBufs& b, cudaStream_t s) {
 }
 
 void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCounters* ctr, cudaStream_t s,
-               const int* skip_shared_ev) {
+               const int* skip_shared_ev, int block) {
     int n = b.n;
     if (n <= 1) return;
-    count_launch(), k_traverse<<<nblk(n - 1, 128), 128, 0, s>>>(box, b.order, n, b.node, b.elem_scene, b.run,
-                                                                skip_shared_ev, pairs, cap, ctr);
+    count_launch(), k_traverse<<<nblk(n - 1, block), block, 0, s>>>(box, b.order, n, b.node, b.elem_scene, b.run,
+                                                                    skip_shared_ev, pairs, cap, ctr);
 }
 
 void brute_pairs(const Box6* box, int ne, const int* elem_scene, int2* pairs, int cap, PassCounters* ctr,

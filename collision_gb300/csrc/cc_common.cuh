@@ -55,10 +55,24 @@ enum ErrBits {
     kErrRecordOverflow = 16,
     kErrMergeOverflow = 32,
     kErrUnionOverflow = 64,
+    kErrSubOverflow = 128,
 };
 // Errors after which a pass's results are discarded (and the pass retried
 // with larger buffers, or the call fails): the impulses are not applied.
-constexpr int kErrRetry = kErrPairOverflow | kErrStack | kErrContribOverflow | kErrRecordOverflow | kErrUnionOverflow;
+constexpr int kErrRetry =
+    kErrPairOverflow | kErrStack | kErrContribOverflow | kErrRecordOverflow | kErrUnionOverflow | kErrSubOverflow;
+
+// A sub-test that passed the FP32 filters, queued for the FP64 stage of a
+// split narrow pass: its element pair's visiting-order key base, the pair's
+// index (for the pair's hit flag), its scene, points and sub-test index.
+struct __align__(8) SubRec {
+    unsigned long long keybase;
+    int pair;
+    int scene;
+    int p[4];
+    int sub;
+    int pad;
+};
 
 // One createImpZone(pts, 4) call of an impact-zone pass (dcollid.cpp:473-484),
 // keyed by the reference's visiting order like a contribution: the host
@@ -105,7 +119,7 @@ struct SceneDev {
     int strain_slots;     // shared-memory slots of its window sweep
     int wb_final0, wb_final1;  // write-backs after its last level
     int enabled;          // 0: left out of resolve calls (candidates pass through)
-    int pad[2];
+    int strain_e0, strain_ne;  // its strain edges
 };
 
 // Per-pass state of a scene (written by the host before a pass, except
@@ -131,7 +145,8 @@ struct PassCounters {
     int nsub;         // sub-tests evaluated in FP64 (not rejected by a filter)
     int ncr;          // coplanarity cubics whose roots were formed again correctly rounded
     int nunion;       // union records written (impact-zone passes)
-    int pad[2];
+    int nsub_pt;      // point-triangle sub-tests queued by a split pass
+    int nsub_ee;      // edge-edge sub-tests queued by a split pass
 };
 
 #ifdef __CUDACC__

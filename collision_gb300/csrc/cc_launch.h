@@ -13,6 +13,13 @@ namespace ccg {
 extern long long g_kernel_launches;
 inline void count_launch(int n = 1) { g_kernel_launches += n; }
 
+// Launch shapes that do not change results (set through cc_set_tuning).
+struct LaunchTuning {
+    int traverse_block = 128;
+    int narrow_block = 128;
+    int strain_block = 256;
+};
+
 // ------------------------------------------------------------- primitives
 // Scratch bytes needed to sort n (key, value) pairs.
 size_t radix_sort_temp_bytes(int n);
@@ -80,7 +87,7 @@ void bvh_build(const Box6* box, BvhBufs& b, cudaStream_t s);
 // once; scenes idle in this pass are skipped. With skip_shared_ev (the
 // elements' point ids), pairs of elements sharing a point are left out.
 void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCounters* ctr, cudaStream_t s,
-               const int* skip_shared_ev = nullptr);
+               const int* skip_shared_ev = nullptr, int block = 128);
 // The same pair set by testing every pair (for cross-checks on small meshes).
 void brute_pairs(const Box6* box, int ne, const int* elem_scene, int2* pairs, int cap, PassCounters* ctr,
                  cudaStream_t s);
@@ -110,8 +117,19 @@ struct NarrowArgs {
     const float4* p32;      // x_old in FP32 (with pbox_lo)
     const float4* v32;      // avgVel in FP32 (with pbox_lo, moving passes)
     int check;              // hit decisions only (no impulses, contacts, zones)
+    // split pass (mixed precision, no zones, no recording): the sub-tests
+    // that pass the FP32 filters, point-triangle and edge-edge apart, and a
+    // hit flag per candidate pair
+    SubRec* sub_pt;
+    SubRec* sub_ee;
+    int sub_cap;
+    int* pair_hit;
 };
-void narrow_pass(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s);
+void narrow_pass(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s, int block = 128);
+// The same pass in two stages (mixed precision only, no impact-zone scene,
+// no recording): FP32 filters per pair, then the FP64 sub-tests that pass
+// them, one thread each.
+void narrow_pass_split(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s, int block = 128);
 // Inputs of the mixed-precision filter: outward-rounded FP32 boxes of every
 // point over the pass's time window (with its scene's dt), and x_old and
 // (moving passes) avgVel rounded to FP32.
@@ -164,14 +182,18 @@ struct StrainPlan {
     bool window;           // sweep in shared memory where the scene's slots fit
     int max_window_slots;  // largest slot count among the scenes that fit
     bool any_global;       // some scene needs more slots than fit
+    int block;             // threads per sweep CTA
 };
 int strain_window_slot_cap();
 // step_buf holds strain_step_bytes(nedges); passes_out holds 3 ints per
 // scene (passes, averaged edges, exact tests).
 size_t strain_step_bytes(int nedges);
+// chunks: (scene, first edge) of every run of at most 256 edges of one
+// scene; flags: 2 ints per scene.
 void strain_limit(const StrainEdge* edges, int nedges, const int4* hdr, const int2* load_list, const int2* wb_list,
-                  const SceneDev* scenes, int nscenes, const StrainPlan& plan, const double4_32a* xo,
-                  double4_32a* av, void* step_buf, int* passes_out, cudaStream_t s);
+                  const int2* chunks, int nchunks, const SceneDev* scenes, int nscenes, const StrainPlan& plan,
+                  const double4_32a* xo, double4_32a* av, void* step_buf, int* flags, int* passes_out,
+                  cudaStream_t s);
 // Correctly rounded cos/sin/acos/pow (fn 0..3) on device arrays, for self-tests.
 void math_selftest(int fn, const double* a, const double* b, double* out, int n, cudaStream_t s);
 // updateFinalVelocity.

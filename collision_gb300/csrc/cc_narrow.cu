@@ -110,6 +110,156 @@ __global__ void __launch_bounds__(128) k_narrow(NarrowArgs a, int max_pairs) {
     }
 }
 
+// Stage 1 of a split pass: per candidate pair, the visit bookkeeping of
+// k_narrow, the element-pair filter, and the box and separating-axis filter
+// of every sub-test, in the sub-test order of tri_to_tri / tri_to_bond /
+// bond_to_bond; survivors are queued with their keys.
+template <bool MOVING>
+__device__ __forceinline__ void queue_sub(const NarrowArgs& a, const NarrowCtx& c, bool ee, unsigned long long kb,
+                                          int pair, int sc, const int* pts, int sub, bool& first) {
+    float ext, extb;
+    if (!mixed_may_hit(c, pts, ee, &ext, &extb)) return;
+    if (ee ? !sat_may_hit<MOVING, true>(c, pts, ext, extb) : !sat_may_hit<MOVING, false>(c, pts, ext, extb)) return;
+    int* cnt = ee ? &a.ctr->nsub_ee : &a.ctr->nsub_pt;
+    int slot = aggregated_add(cnt, 1);
+    if (slot >= a.sub_cap) {
+        atomicOr(&a.ctr->err, kErrSubOverflow);
+        return;
+    }
+    if (first) {
+        a.pair_hit[pair] = 0;
+        first = false;
+    }
+    SubRec r;
+    r.keybase = kb;
+    r.pair = pair;
+    r.scene = sc;
+    for (int i = 0; i < 4; ++i) r.p[i] = pts[i];
+    r.sub = sub;
+    r.pad = 0;
+    (ee ? a.sub_ee : a.sub_pt)[slot] = r;
+}
+
+template <bool MOVING>
+__global__ void __launch_bounds__(512) k_narrow_filter(NarrowArgs a, int max_pairs) {
+    NarrowCtx c;
+    c.pbox_lo = a.pbox_lo; c.pbox_hi = a.pbox_hi; c.p32 = a.p32; c.v32 = a.v32;
+    int np = a.ctr->npairs;
+    if (np > max_pairs) np = max_pairs;
+    int t_visits = 0;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) {
+        int2 pr = a.pairs[idx];
+        int sc = a.escene[pr.x];
+        const double eps = a.scenes[sc].p.eps;
+        c.hpad = __double2float_ru(MOVING ? eps : a.scenes[sc].p.thickness);
+        c.epad = __double2float_ru(eps);
+        c.dt32 = __double2float_ru(a.scenes[sc].p.dt);
+        int ri = a.rank[pr.x], rj = a.rank[pr.y];
+        int ea = ri > rj ? pr.x : pr.y;
+        int eb = ri > rj ? pr.y : pr.x;
+        int ra = ri > rj ? ri : rj, rb = ri > rj ? rj : ri;
+        bool ta = a.ev[3 * ea + 2] >= 0, tb = a.ev[3 * eb + 2] >= 0;
+        int kind = (ta && tb) ? 0 : (!ta && !tb) ? 2 : 1;
+        if (kind == 0 && a.esurf[ea] == a.esurf[eb] && a.erigid[ea]) continue;  // dcollid.cpp:762-763, 805-806
+        t_visits++;
+        int e1 = (kind == 1 && !ta) ? eb : ea;
+        int e2 = (kind == 1 && !ta) ? ea : eb;
+        int A[3] = {a.ev[3 * e1], a.ev[3 * e1 + 1], a.ev[3 * e1 + 2]};
+        int B[3] = {a.ev[3 * e2], a.ev[3 * e2 + 1], a.ev[3 * e2 + 2]};
+        int n1 = A[2] >= 0 ? 3 : 2, n2 = B[2] >= 0 ? 3 : 2;
+        // a shared point makes every test of the pair return false
+        bool shared = false;
+        for (int i = 0; i < n1; ++i)
+            for (int j = 0; j < n2; ++j) shared |= A[i] == B[j];
+        if (shared || !pair_may_hit<MOVING>(c, A, n1, B, n2)) continue;
+        const unsigned long long kb = ((unsigned long long)rb << 26) | ((unsigned long long)ra << 4);
+        bool first = true;
+        int pts[4];
+        if (kind == 0) {
+            int sub = 0;
+            for (int k = 0; k < 2; ++k)
+                for (int i = 0; i < 3; ++i, ++sub) {
+                    const int* tri = MOVING ? ((k == 0) ? A : B) : ((k == 0) ? B : A);
+                    const int* pt = MOVING ? ((k == 0) ? B : A) : ((k == 0) ? A : B);
+                    pts[0] = tri[0]; pts[1] = tri[1]; pts[2] = tri[2]; pts[3] = pt[i];
+                    queue_sub<MOVING>(a, c, false, kb, idx, sc, pts, sub, first);
+                }
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j, ++sub) {
+                    pts[0] = A[i]; pts[1] = A[(i + 1) % 3]; pts[2] = B[j]; pts[3] = B[(j + 1) % 3];
+                    queue_sub<MOVING>(a, c, true, kb, idx, sc, pts, sub, first);
+                }
+        } else if (kind == 1) {
+            pts[0] = A[0]; pts[1] = A[1]; pts[2] = A[2];
+            pts[3] = B[0];
+            queue_sub<MOVING>(a, c, false, kb, idx, sc, pts, 0, first);
+            pts[3] = B[1];
+            queue_sub<MOVING>(a, c, false, kb, idx, sc, pts, 1, first);
+            pts[2] = B[0];
+            pts[3] = B[1];
+            for (int i = 0; i < 3; ++i) {
+                pts[0] = A[i];
+                pts[1] = A[(i + 1) % 3];
+                queue_sub<MOVING>(a, c, true, kb, idx, sc, pts, 2 + i, first);
+            }
+        } else {
+            pts[0] = A[0]; pts[1] = A[1]; pts[2] = B[0]; pts[3] = B[1];
+            queue_sub<MOVING>(a, c, true, kb, idx, sc, pts, 0, first);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) t_visits += __shfl_xor_sync(0xffffffffu, t_visits, o);
+    if ((threadIdx.x & 31) == 0 && t_visits) atomicAdd(&a.ctr->nvisits, t_visits);
+}
+
+// Stage 2: one queued sub-test per thread, the FP64 test of k_narrow.
+template <bool MOVING, bool EE>
+__global__ void __launch_bounds__(128) k_subtests(NarrowArgs a) {
+    const SubRec* list = EE ? a.sub_ee : a.sub_pt;
+    int n = EE ? a.ctr->nsub_ee : a.ctr->nsub_pt;
+    if (n > a.sub_cap) n = a.sub_cap;
+    NarrowCtx c;
+    c.xo = a.xo; c.av = a.av; c.fixed = a.fixed; c.ev = a.ev; c.esurf = a.esurf; c.erigid = a.erigid;
+    c.rank = a.rank;
+    c.contrib = a.contrib; c.contrib_cap = a.contrib_cap; c.ctr = a.ctr; c.urec = nullptr; c.urec_cap = 0;
+    c.rec = nullptr; c.rec_cap = 0;
+    c.pbox_lo = nullptr; c.pbox_hi = nullptr; c.p32 = nullptr; c.v32 = nullptr;
+    c.check = 0;
+    c.zone = 0;
+    int t_hits = 0, t_cr = 0, t_contacts = 0, t_sub = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const SubRec r = list[i];
+        c.p = a.scenes[r.scene].p;
+        c.pass = 0;
+        CallState st;
+        st.keybase = r.keybase;
+        st.np = 0;
+        st.sub = r.sub;
+        st.nsub = 0;
+        st.ncr = 0;
+        st.ncontacts = 0;
+        bool hit = MOVING ? moving_test<EE>(c, st, r.p) : static_test<EE>(c, st, r.p);
+        t_sub++;
+        t_cr += st.ncr;
+        t_contacts += st.ncontacts;
+        if (hit && atomicOr(&a.pair_hit[r.pair], 1) == 0) {
+            t_hits++;
+            atomicAdd(&a.run[r.scene].hits, 1);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        t_hits += __shfl_xor_sync(0xffffffffu, t_hits, o);
+        t_cr += __shfl_xor_sync(0xffffffffu, t_cr, o);
+        t_contacts += __shfl_xor_sync(0xffffffffu, t_contacts, o);
+        t_sub += __shfl_xor_sync(0xffffffffu, t_sub, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (t_hits) atomicAdd(&a.ctr->nhit_pairs, t_hits);
+        if (t_cr) atomicAdd(&a.ctr->ncr, t_cr);
+        if (t_contacts) atomicAdd(&a.ctr->ncontacts, t_contacts);
+        if (t_sub) atomicAdd(&a.ctr->nsub, t_sub);
+    }
+}
+
 // FP32 box of every point over the pass's time window, rounded outward:
 // [x_old] for proximity, [x_old, x_old + dt*avgVel] for CCD.
 template <bool MOVING>
@@ -153,7 +303,7 @@ void point_boxes(const double4_32a* xo, const double4_32a* av, const int* vscene
                                                                              hi, p32, v32);
 }
 
-void narrow_pass(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s) {
+void narrow_pass(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s, int) {
     if (max_pairs <= 0) return;
     int threads = 128;
     int blocks = (max_pairs + threads - 1) / threads;
@@ -162,6 +312,24 @@ void narrow_pass(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s)
         count_launch(), k_narrow<true><<<blocks, threads, 0, s>>>(a, max_pairs);
     else
         count_launch(), k_narrow<false><<<blocks, threads, 0, s>>>(a, max_pairs);
+}
+
+void narrow_pass_split(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s, int block) {
+    if (max_pairs <= 0) return;
+    const int cap_blocks = 152 * 16 * 128 / block;
+    int blocks = (max_pairs + block - 1) / block;
+    if (blocks > cap_blocks) blocks = cap_blocks;
+    int sblocks = (a.sub_cap + 127) / 128;
+    if (sblocks > 152 * 16) sblocks = 152 * 16;
+    if (moving) {
+        count_launch(), k_narrow_filter<true><<<blocks, block, 0, s>>>(a, max_pairs);
+        count_launch(), k_subtests<true, false><<<sblocks, 128, 0, s>>>(a);
+        count_launch(), k_subtests<true, true><<<sblocks, 128, 0, s>>>(a);
+    } else {
+        count_launch(), k_narrow_filter<false><<<blocks, block, 0, s>>>(a, max_pairs);
+        count_launch(), k_subtests<false, false><<<sblocks, 128, 0, s>>>(a);
+        count_launch(), k_subtests<false, true><<<sblocks, 128, 0, s>>>(a);
+    }
 }
 
 }  // namespace ccg

@@ -663,74 +663,82 @@ __device__ __forceinline__ F3 fcross(F3 a, F3 b) {
 // its three in-plane edge normals (for two disjoint coplanar triangles one of
 // those separates them), for two segments their common normal and the
 // in-plane normals of each, and the line between the centroids.
+// Gap between the projections of two point sets (3 points each) onto ax,
+// divided by |ax|: a lower bound on their distance (-1 for a zero axis).
+__device__ __forceinline__ float axis_gap(F3 ax, const F3* R) {
+    float an = fnorm(ax);
+    if (!(an > 0.f)) return -1.f;
+    float amin = fdot(ax, R[0]), amax = amin, bmin = fdot(ax, R[3]), bmax = bmin;
+#pragma unroll
+    for (int q = 1; q < 3; ++q) {
+        float ta = fdot(ax, R[q]), tb = fdot(ax, R[3 + q]);
+        amin = fminf(amin, ta);
+        amax = fmaxf(amax, ta);
+        bmin = fminf(bmin, tb);
+        bmax = fmaxf(bmax, tb);
+    }
+    return fmaxf(bmin - amax, amin - bmax) / an;
+}
+
 template <bool MOVING>
 __device__ __forceinline__ bool pair_may_hit(const NarrowCtx& c, const int* A, int na, const int* B, int nb) {
-    F3 X[6];
-    int n = na + nb;
-    for (int q = 0; q < na; ++q) X[q] = f3(c.p32[A[q]]);
-    for (int q = 0; q < nb; ++q) X[na + q] = f3(c.p32[B[q]]);
-    float M = 0.f, L = 0.f;
+    // points relative to A's first; a segment's third point repeats its
+    // second (the same convex hull, so the same projections)
+    const int ia[3] = {A[0], A[1], na == 3 ? A[2] : A[1]};
+    const int ib[3] = {B[0], B[1], nb == 3 ? B[2] : B[1]};
     F3 R[6];
-    for (int q = 0; q < n; ++q) {
-        M = fmaxf(M, fmaxabs(X[q]));
-        R[q] = fsub(X[q], X[0]);
+    const F3 X0 = f3(c.p32[ia[0]]);
+    float M = fmaxabs(X0), L = 0.f;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        F3 x = q < 3 ? f3(c.p32[ia[q]]) : f3(c.p32[ib[q - 3]]);
+        M = fmaxf(M, fmaxabs(x));
+        R[q] = fsub(x, X0);
         L = fmaxf(L, fnorm(R[q]));
     }
-    F3 ax[10];
-    int nax = 0;
-    F3 cA = F3{0.f, 0.f, 0.f}, cB = F3{0.f, 0.f, 0.f};
-    for (int q = 0; q < na; ++q) cA = fadd(cA, R[q]);
-    for (int q = 0; q < nb; ++q) cB = fadd(cB, R[na + q]);
-    ax[nax++] = fsub(fscale(cB, 1.f / nb), fscale(cA, 1.f / na));
-    for (int side = 0; side < 2; ++side) {
-        const F3* P = side ? R + na : R;
-        int np = side ? nb : na;
-        if (np == 3) {
-            F3 e0 = fsub(P[1], P[0]), e1 = fsub(P[2], P[1]), e2 = fsub(P[0], P[2]);
-            F3 nrm = fcross(e0, fsub(P[2], P[0]));
-            ax[nax++] = nrm;
-            ax[nax++] = fcross(nrm, e0);
-            ax[nax++] = fcross(nrm, e1);
-            ax[nax++] = fcross(nrm, e2);
-        }
-    }
-    if (na == 2 && nb == 2) {
-        F3 d1 = fsub(R[1], R[0]), d2 = fsub(R[3], R[2]);
-        F3 nrm = fcross(d1, d2);
-        ax[nax++] = nrm;
-        ax[nax++] = fcross(nrm, d1);
-        ax[nax++] = fcross(nrm, d2);
-    }
     float lb = -1.f;
-    for (int k = 0; k < nax; ++k) {
-        float an = fnorm(ax[k]);
-        if (!(an > 0.f)) continue;
-        float amin = 3.0e38f, amax = -3.0e38f, bmin = 3.0e38f, bmax = -3.0e38f;
-        for (int q = 0; q < na; ++q) {
-            float t = fdot(ax[k], R[q]);
-            amin = fminf(amin, t);
-            amax = fmaxf(amax, t);
-        }
-        for (int q = 0; q < nb; ++q) {
-            float t = fdot(ax[k], R[na + q]);
-            bmin = fminf(bmin, t);
-            bmax = fmaxf(bmax, t);
-        }
-        lb = fmaxf(lb, fmaxf(bmin - amax, amin - bmax) / an);
+    {
+        F3 cA = fscale(fadd(fadd(R[0], R[1]), R[2]), 1.f / 3.f);
+        F3 cB = fscale(fadd(fadd(R[3], R[4]), R[5]), 1.f / 3.f);
+        lb = fmaxf(lb, axis_gap(fsub(cB, cA), R));
+    }
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+        const F3* P = R + 3 * side;
+        F3 e0 = fsub(P[1], P[0]), e1 = fsub(P[2], P[1]), e2 = fsub(P[0], P[2]);
+        F3 nrm = fcross(e0, fsub(P[2], P[0]));  // zero for a segment: skipped
+        lb = fmaxf(lb, axis_gap(nrm, R));
+        lb = fmaxf(lb, axis_gap(fcross(nrm, e0), R));
+        lb = fmaxf(lb, axis_gap(fcross(nrm, e1), R));
+        lb = fmaxf(lb, axis_gap(fcross(nrm, e2), R));
+    }
+    {
+        F3 d1 = fsub(R[1], R[0]), d2 = fsub(R[4], R[3]);
+        F3 nrm = fcross(d1, d2);
+        lb = fmaxf(lb, axis_gap(nrm, R));
+        lb = fmaxf(lb, axis_gap(fcross(nrm, d1), R));
+        lb = fmaxf(lb, axis_gap(fcross(nrm, d2), R));
     }
     // the largest reach of the pair's sub-tests, with the boxes' extents
-    float extA = 0.f, extB = 0.f;
+    float extA, extB;
     {
-        float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
-        for (int q = 0; q < na; ++q) {
-            float4 l = c.pbox_lo[A[q]], h = c.pbox_hi[A[q]];
+        float4 l = c.pbox_lo[ia[0]], h = c.pbox_hi[ia[0]];
+        float lo[3] = {l.x, l.y, l.z}, hi[3] = {h.x, h.y, h.z};
+#pragma unroll
+        for (int q = 1; q < 3; ++q) {
+            l = c.pbox_lo[ia[q]];
+            h = c.pbox_hi[ia[q]];
             lo[0] = fminf(lo[0], l.x); lo[1] = fminf(lo[1], l.y); lo[2] = fminf(lo[2], l.z);
             hi[0] = fmaxf(hi[0], h.x); hi[1] = fmaxf(hi[1], h.y); hi[2] = fmaxf(hi[2], h.z);
         }
         extA = __fadd_ru(__fadd_ru(__fsub_ru(hi[0], lo[0]), __fsub_ru(hi[1], lo[1])), __fsub_ru(hi[2], lo[2]));
-        float lo2[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi2[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
-        for (int q = 0; q < nb; ++q) {
-            float4 l = c.pbox_lo[B[q]], h = c.pbox_hi[B[q]];
+        l = c.pbox_lo[ib[0]];
+        h = c.pbox_hi[ib[0]];
+        float lo2[3] = {l.x, l.y, l.z}, hi2[3] = {h.x, h.y, h.z};
+#pragma unroll
+        for (int q = 1; q < 3; ++q) {
+            l = c.pbox_lo[ib[q]];
+            h = c.pbox_hi[ib[q]];
             lo2[0] = fminf(lo2[0], l.x); lo2[1] = fminf(lo2[1], l.y); lo2[2] = fminf(lo2[2], l.z);
             hi2[0] = fmaxf(hi2[0], h.x); hi2[1] = fmaxf(hi2[1], h.y); hi2[2] = fmaxf(hi2[2], h.z);
         }
@@ -743,15 +751,17 @@ __device__ __forceinline__ bool pair_may_hit(const NarrowCtx& c, const int* A, i
     float err = __fmul_ru(32.0f * 0x1p-24f, __fadd_ru(L, M));
     float bound = __fsub_rd(lb, err);
     if (MOVING) {
-        F3 v0 = f3(c.v32[A[0]]);
+        F3 v0 = f3(c.v32[ia[0]]);
         float DA = 0.f, DB = 0.f, Vm = fmaxabs(v0);
-        for (int q = 1; q < na; ++q) {
-            F3 v = f3(c.v32[A[q]]);
+#pragma unroll
+        for (int q = 1; q < 3; ++q) {
+            F3 v = f3(c.v32[ia[q]]);
             DA = fmaxf(DA, fnorm(fsub(v, v0)));
             Vm = fmaxf(Vm, fmaxabs(v));
         }
-        for (int q = 0; q < nb; ++q) {
-            F3 v = f3(c.v32[B[q]]);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            F3 v = f3(c.v32[ib[q]]);
             DB = fmaxf(DB, fnorm(fsub(v, v0)));
             Vm = fmaxf(Vm, fmaxabs(v));
         }

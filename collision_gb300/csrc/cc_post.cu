@@ -269,6 +269,18 @@ __device__ __forceinline__ StrainBounds strain_bounds(double L) {
     b.lo_def = e * e;  // s below: over-compressed for sure
     return b;
 }
+// The same bounds from the squared length L2 = L*L, without the square root:
+// each differs from the one above by a few ulps, far inside the 1e-9 margin.
+__device__ __forceinline__ StrainBounds strain_bounds_sq(double L2) {
+    const double ka = (1.1 * (1.0 + 1e-9)) * (1.1 * (1.0 + 1e-9)), kc = (1.1 * (1.0 - 1e-9)) * (1.1 * (1.0 - 1e-9));
+    const double kd = (0.9 * (1.0 + 1e-9)) * (0.9 * (1.0 + 1e-9)), ke = (0.9 * (1.0 - 1e-9)) * (0.9 * (1.0 - 1e-9));
+    StrainBounds b;
+    b.hi_def = L2 * ka;
+    b.hi_no = L2 * kc;
+    b.lo_no = L2 * kd;
+    b.lo_def = L2 * ke;
+    return b;
+}
 // 1: over the limit, 0: within it, -1: too close to tell without the exact test.
 __device__ __forceinline__ int strain_quick(double s, const StrainBounds& b) {
     if (s > b.hi_def || s < b.lo_def) return 1;
@@ -313,19 +325,18 @@ __global__ void k_strain_setup(const StrainEdge* __restrict__ edges, int m, cons
     load3(xo, ed.p1, x1);
     double so = 0.0;
     for (int k = 0; k < 3; ++k) so += sqr(x0[k] - x1[k]);
-    double len_old = sqrt(so);
     StrainEdgeStep r;
     r.p0 = ed.p0;
     r.p1 = ed.p1;
     r.len0 = ed.len0;
     r.rest = strain_bounds(ed.len0);
-    r.prev = strain_bounds(len_old);
+    r.prev = strain_bounds_sq(so);
     for (int k = 0; k < 3; ++k) {
         r.x0[k] = x0[k];
         r.x1[k] = x1[k];
     }
     // tiny or non-positive lengths: leave every decision to the exact test
-    r.exact_only = !(len_old > 1e-6 && ed.len0 > 1e-6);
+    r.exact_only = !(so > 1e-12 && ed.len0 > 1e-6);
     r.s0 = ed.s0;
     r.s1 = ed.s1;
     r.pad = 0;
@@ -382,88 +393,107 @@ __device__ __forceinline__ bool strain_flag_vals(const StrainEdgeStep& ed, const
 
 // reduceSuperelast, dcollid.cpp:586-596: up to 10 Gauss-Seidel passes over
 // the edges in element order, each averaging the two end velocities of an
-// over-strained edge before the next edge is tested. The edges arrive sorted
+// over-strained edge before the next edge is tested (one pass per launch). The edges arrive sorted
 // by dependency level (an edge's level is one more than the level of the
 // last earlier edge at either of its points), so the edges of one level share
 // no point and see exactly the values the sequential sweep gives them: the
 // level-by-level walk below is the reference's sweep, reordered only where
 // the order cannot matter.
-__global__ void __launch_bounds__(256) k_strain(const StrainEdgeStep* __restrict__ edges,
-                                                const int4* __restrict__ hdr_all,
-                                                const SceneDev* __restrict__ scenes, int slot_cap,
-                                                double4_32a* av, int* passes_out_all) {
-    const SceneDev& sd = scenes[blockIdx.x];
-    if (slot_cap >= 0 && sd.strain_slots <= slot_cap) return;  // swept by k_strain_window
-    if (!sd.enabled) {
-        if (threadIdx.x == 0) passes_out_all[3 * blockIdx.x] = passes_out_all[3 * blockIdx.x + 1] =
-                                  passes_out_all[3 * blockIdx.x + 2] = 0;
-        return;
+// Per scene and step, flags[2s] ("some edge would average": set by
+// k_strain_check) and flags[2s+1] (the sweep is over); passes_out[3s ..] the
+// sweeps run, edges averaged, exact tests. One launch is one pass: a scene
+// whose check found nothing to average is done - its sweep would change
+// nothing, which is how the reference's loop ends (dcollid.cpp:588-595) -
+// and counts that sweep; otherwise it sweeps once.
+__device__ __forceinline__ bool sweep_gate(int pass, int s, int* flags, int* passes_out_all) {
+    __shared__ int s_go;
+    if (threadIdx.x == 0) {
+        int go = 0;
+        if (!flags[2 * s + 1]) {
+            if (!flags[2 * s]) {
+                flags[2 * s + 1] = 1;
+                passes_out_all[3 * s] = pass + 1;
+            } else {
+                flags[2 * s] = 0;
+                go = 1;
+            }
+        }
+        s_go = go;
     }
-    const int4* hdr = hdr_all + 2 * sd.strain_hdr0;
-    const int nlevels = sd.strain_levels;
-    const double dt = sd.p.dt;
-    int* passes_out = passes_out_all + 3 * blockIdx.x;
-    __shared__ int s_has, s_avg, s_exact;
+    __syncthreads();
+    return s_go != 0;
+}
+
+__device__ __forceinline__ void sweep_done(int pass, int s, int n_avg, int n_exact, int* flags, int* passes_out_all) {
+    __shared__ int s_avg, s_exact;
     if (threadIdx.x == 0) s_avg = s_exact = 0;
-    int passes = 0, n_avg = 0, n_exact = 0;
-    for (int pass = 0; pass < kStrainMaxIter; ++pass) {
-        if (threadIdx.x == 0) s_has = 0;
-        __syncthreads();
-        passes++;
-        // the records of the next level are loaded before the barrier that
-        // ends the current one: they do not depend on the velocities
-        int e = 0, e1 = 0;
-        if (nlevels > 0) {
-            int4 h = hdr[0];
-            e = h.x + threadIdx.x;
-            e1 = h.y;
-        }
-        StrainEdgeStep cur;
-        bool have = e < e1;
-        if (have) cur = edges[e];
-        for (int l = 0; l < nlevels; ++l) {
-            int ne = 0, ne1 = 0;
-            if (l + 1 < nlevels) {
-                int4 h = hdr[2 * (l + 1)];
-                ne = h.x + threadIdx.x;
-                ne1 = h.y;
-            }
-            bool nhave = ne < ne1;
-            StrainEdgeStep nxt;
-            if (nhave) nxt = edges[ne];
-            while (have) {
-                double4_32a a0 = av[cur.p0], a1 = av[cur.p1];
-                double v0[3] = {a0.x, a0.y, a0.z}, v1[3] = {a1.x, a1.y, a1.z};
-                if (strain_flag_vals(cur, v0, v1, dt, &n_exact)) {
-                    ++n_avg;
-                    double t0 = a0.x + a1.x, t1 = a0.y + a1.y, t2 = a0.z + a1.z;
-                    t0 = 0.5 * t0; t1 = 0.5 * t1; t2 = 0.5 * t2;
-                    double4_32a nv4 = make_double4_32a(t0, t1, t2, 0.0);
-                    av[cur.p0] = nv4;
-                    av[cur.p1] = nv4;
-                    s_has = 1;
-                }
-                e += blockDim.x;
-                have = e < e1;
-                if (have) cur = edges[e];
-            }
-            __syncthreads();
-            e = ne;
-            e1 = ne1;
-            have = nhave;
-            cur = nxt;
-        }
-        if (!s_has) break;
-        __syncthreads();
-    }
+    __syncthreads();
     atomicAdd(&s_avg, n_avg);
     atomicAdd(&s_exact, n_exact);
     __syncthreads();
     if (threadIdx.x == 0) {
-        passes_out[0] = passes;
-        passes_out[1] = s_avg;
-        passes_out[2] = s_exact;
+        passes_out_all[3 * s] = pass + 1;
+        passes_out_all[3 * s + 1] += s_avg;
+        passes_out_all[3 * s + 2] += s_exact;
+        if (pass + 1 >= kStrainMaxIter) flags[2 * s + 1] = 1;
     }
+}
+
+__global__ void __launch_bounds__(256) k_strain(const StrainEdgeStep* __restrict__ edges,
+                                                const int4* __restrict__ hdr_all,
+                                                const SceneDev* __restrict__ scenes, int slot_cap,
+                                                double4_32a* av, int pass, int* flags, int* passes_out_all) {
+    const int sc = blockIdx.x;
+    const SceneDev& sd = scenes[sc];
+    if ((slot_cap >= 0 && sd.strain_slots <= slot_cap) || !sd.enabled) return;  // k_strain_window's, or left out
+    if (!sweep_gate(pass, sc, flags, passes_out_all)) return;
+    const int4* hdr = hdr_all + 2 * sd.strain_hdr0;
+    const int nlevels = sd.strain_levels;
+    const double dt = sd.p.dt;
+    int n_avg = 0, n_exact = 0;
+    // the records of the next level are loaded before the barrier that ends
+    // the current one: they do not depend on the velocities
+    int e = 0, e1 = 0;
+    if (nlevels > 0) {
+        int4 h = hdr[0];
+        e = h.x + threadIdx.x;
+        e1 = h.y;
+    }
+    StrainEdgeStep cur;
+    bool have = e < e1;
+    if (have) cur = edges[e];
+    for (int l = 0; l < nlevels; ++l) {
+        int ne = 0, ne1 = 0;
+        if (l + 1 < nlevels) {
+            int4 h = hdr[2 * (l + 1)];
+            ne = h.x + threadIdx.x;
+            ne1 = h.y;
+        }
+        bool nhave = ne < ne1;
+        StrainEdgeStep nxt;
+        if (nhave) nxt = edges[ne];
+        while (have) {
+            double4_32a a0 = av[cur.p0], a1 = av[cur.p1];
+            double v0[3] = {a0.x, a0.y, a0.z}, v1[3] = {a1.x, a1.y, a1.z};
+            if (strain_flag_vals(cur, v0, v1, dt, &n_exact)) {
+                ++n_avg;
+                double t0 = a0.x + a1.x, t1 = a0.y + a1.y, t2 = a0.z + a1.z;
+                t0 = 0.5 * t0; t1 = 0.5 * t1; t2 = 0.5 * t2;
+                double4_32a nv4 = make_double4_32a(t0, t1, t2, 0.0);
+                av[cur.p0] = nv4;
+                av[cur.p1] = nv4;
+            }
+            e += blockDim.x;
+            have = e < e1;
+            if (have) cur = edges[e];
+        }
+        __syncthreads();
+        e = ne;
+        e1 = ne1;
+        have = nhave;
+        cur = nxt;
+    }
+    sweep_done(pass, sc, n_avg, n_exact, flags, passes_out_all);
 }
 
 // The same sweep with each point's velocity in shared memory while the
@@ -653,69 +683,73 @@ __global__ void __launch_bounds__(256) k_strain_window(const StrainEdgeStep* __r
                                                        const SceneDev* __restrict__ scenes, int slot_cap,
                                                        const int2* __restrict__ load_list,
                                                        const int2* __restrict__ wb_list,
-                                                       double4_32a* av, int* passes_out_all) {
+                                                       double4_32a* av, int pass, int* flags,
+                                                       int* passes_out_all) {
     extern __shared__ WinSlot s_win[];
-    const SceneDev& sd = scenes[blockIdx.x];
-    if (sd.strain_slots > slot_cap) return;  // swept by k_strain
-    if (!sd.enabled) {
-        if (threadIdx.x == 0) passes_out_all[3 * blockIdx.x] = passes_out_all[3 * blockIdx.x + 1] =
-                                  passes_out_all[3 * blockIdx.x + 2] = 0;
-        return;
-    }
+    const int sc = blockIdx.x;
+    const SceneDev& sd = scenes[sc];
+    if (sd.strain_slots > slot_cap || !sd.enabled) return;  // k_strain's, or left out
+    if (!sweep_gate(pass, sc, flags, passes_out_all)) return;
     const int4* hdr = hdr_all + 2 * sd.strain_hdr0;
     const int nlevels = sd.strain_levels;
     const int2 wb_final = make_int2(sd.wb_final0, sd.wb_final1);
     const double dt = sd.p.dt;
-    int* passes_out = passes_out_all + 3 * blockIdx.x;
-    __shared__ int s_has[2];
-    __shared__ int s_avg, s_exact;
-    if (threadIdx.x == 0) {
-        s_has[0] = s_has[1] = 0;
-        s_avg = s_exact = 0;
-    }
-    __syncthreads();
     const int tid = threadIdx.x;
     WinArgs A{edges, hot, hdr, nlevels, load_list, wb_list, av, dt, __double2float_ru(dt)};
-    int passes = 0, n_avg = 0, n_exact = 0;
-    for (int pass = 0; pass < kStrainMaxIter; ++pass) {
-        const int hs = pass & 1;
-        passes++;
-        bool has = false;
-        WinRing r;
+    int n_avg = 0, n_exact = 0;
+    bool has = false;
+    WinRing r;
 #pragma unroll
-        for (int j = 0; j < kWindowAhead; ++j) r.lslot[j] = -1;
+    for (int j = 0; j < kWindowAhead; ++j) r.lslot[j] = -1;
 #pragma unroll
-        for (int j = 0; j < kRing; ++j) win_fetch(r, j, j, nlevels, tid, hdr, hot, load_list, wb_list);
-        for (int lb = 0; lb < nlevels; lb += kWindowAhead) {
-            win_level<0>(A, r, s_win, lb + 0, tid, &n_avg, &n_exact, &has);
-            if (lb + 1 < nlevels) win_level<1>(A, r, s_win, lb + 1, tid, &n_avg, &n_exact, &has);
-            if (lb + 2 < nlevels) win_level<2>(A, r, s_win, lb + 2, tid, &n_avg, &n_exact, &has);
-            if (lb + 3 < nlevels) win_level<3>(A, r, s_win, lb + 3, tid, &n_avg, &n_exact, &has);
-            if (lb + 4 < nlevels) win_level<4>(A, r, s_win, lb + 4, tid, &n_avg, &n_exact, &has);
-            if (lb + 5 < nlevels) win_level<5>(A, r, s_win, lb + 5, tid, &n_avg, &n_exact, &has);
-            if (lb + 6 < nlevels) win_level<6>(A, r, s_win, lb + 6, tid, &n_avg, &n_exact, &has);
-            if (lb + 7 < nlevels) win_level<7>(A, r, s_win, lb + 7, tid, &n_avg, &n_exact, &has);
-        }
-        asm volatile("cp.async.wait_group 0;\n" ::);
-        if (has) s_has[hs] = 1;
-        __syncthreads();
-        for (int i = wb_final.x + tid; i < wb_final.y; i += blockDim.x) {
-            int2 ps = wb_list[i];
-            double2 a = s_win[ps.y].a, b = s_win[ps.y].b;
-            av[ps.x] = make_double4_32a(a.x, a.y, b.x, 0.0);
-        }
-        if (tid == 0) s_has[hs ^ 1] = 0;
-        __syncthreads();
-        if (!s_has[hs]) break;
+    for (int j = 0; j < kRing; ++j) win_fetch(r, j, j, nlevels, tid, hdr, hot, load_list, wb_list);
+    for (int lb = 0; lb < nlevels; lb += kWindowAhead) {
+        win_level<0>(A, r, s_win, lb + 0, tid, &n_avg, &n_exact, &has);
+        if (lb + 1 < nlevels) win_level<1>(A, r, s_win, lb + 1, tid, &n_avg, &n_exact, &has);
+        if (lb + 2 < nlevels) win_level<2>(A, r, s_win, lb + 2, tid, &n_avg, &n_exact, &has);
+        if (lb + 3 < nlevels) win_level<3>(A, r, s_win, lb + 3, tid, &n_avg, &n_exact, &has);
+        if (lb + 4 < nlevels) win_level<4>(A, r, s_win, lb + 4, tid, &n_avg, &n_exact, &has);
+        if (lb + 5 < nlevels) win_level<5>(A, r, s_win, lb + 5, tid, &n_avg, &n_exact, &has);
+        if (lb + 6 < nlevels) win_level<6>(A, r, s_win, lb + 6, tid, &n_avg, &n_exact, &has);
+        if (lb + 7 < nlevels) win_level<7>(A, r, s_win, lb + 7, tid, &n_avg, &n_exact, &has);
     }
-    atomicAdd(&s_avg, n_avg);
-    atomicAdd(&s_exact, n_exact);
+    asm volatile("cp.async.wait_group 0;\n" ::);
     __syncthreads();
-    if (tid == 0) {
-        passes_out[0] = passes;
-        passes_out[1] = s_avg;
-        passes_out[2] = s_exact;
+    for (int i = wb_final.x + tid; i < wb_final.y; i += blockDim.x) {
+        int2 ps = wb_list[i];
+        double2 a = s_win[ps.y].a, b = s_win[ps.y].b;
+        av[ps.x] = make_double4_32a(a.x, a.y, b.x, 0.0);
     }
+    sweep_done(pass, sc, n_avg, n_exact, flags, passes_out_all);
+}
+
+// Would any edge of the chunk average on the current velocities? (One
+// block per chunk of at most 256 edges of one scene.) If none of a scene's
+// edges would, its sweep changes nothing: before the first edge that
+// averages every edge sees the start-of-pass velocities.
+__global__ void __launch_bounds__(256) k_strain_check(const StrainEdgeStep* __restrict__ edges,
+                                                      const StrainEdgeHot* __restrict__ hot,
+                                                      const int2* __restrict__ chunks,
+                                                      const SceneDev* __restrict__ scenes,
+                                                      const double4_32a* __restrict__ av, int* flags) {
+    const int2 ch = chunks[blockIdx.x];  // (scene, first edge)
+    const SceneDev& sd = scenes[ch.x];
+    if (!sd.enabled || flags[2 * ch.x + 1]) return;
+    const int end = sd.strain_e0 + sd.strain_ne;
+    const int e = ch.y + threadIdx.x;
+    if (e >= end) return;
+    const StrainEdgeHot h = hot[e];
+    const int2 pp = *reinterpret_cast<const int2*>(&edges[e]);  // p0, p1
+    const double4_32a a0 = av[pp.x], a1 = av[pp.y];
+    const float dt32 = __double2float_ru(sd.p.dt);
+    int q = strain_decide32(h, make_float4((float)a0.x, (float)a0.y, (float)a0.z, 0.f),
+                            make_float4((float)a1.x, (float)a1.y, (float)a1.z, 0.f), dt32);
+    if (q < 0) {
+        double v0[3] = {a0.x, a0.y, a0.z}, v1[3] = {a1.x, a1.y, a1.z};
+        int n_exact = 0;
+        q = strain_flag_vals(edges[e], v0, v1, sd.p.dt, &n_exact) ? 1 : 0;
+    }
+    if (q > 0 && !flags[2 * ch.x]) atomicOr(&flags[2 * ch.x], 1);
 }
 
 __global__ void k_final_velocity(const uint8_t* __restrict__ in_elem, const uint8_t* __restrict__ has_collsn,
@@ -792,22 +826,28 @@ size_t strain_step_bytes(int nedges) {
 int strain_window_slot_cap() { return (int)(kStrainWindowBytes / sizeof(WinSlot)); }
 
 void strain_limit(const StrainEdge* edges, int nedges, const int4* hdr, const int2* load_list, const int2* wb_list,
-                  const SceneDev* scenes, int nscenes, const StrainPlan& plan, const double4_32a* xo,
-                  double4_32a* av, void* step_buf, int* passes_out, cudaStream_t s) {
+                  const int2* chunks, int nchunks, const SceneDev* scenes, int nscenes, const StrainPlan& plan,
+                  const double4_32a* xo, double4_32a* av, void* step_buf, int* flags, int* passes_out,
+                  cudaStream_t s) {
     if (nscenes <= 0) return;
     StrainEdgeStep* se = (StrainEdgeStep*)step_buf;
     StrainEdgeHot* hot = (StrainEdgeHot*)(se + (nedges > 0 ? nedges : 1));
+    cudaMemsetAsync(flags, 0, sizeof(int) * 2 * (size_t)nscenes, s);
+    cudaMemsetAsync(passes_out, 0, sizeof(int) * 3 * (size_t)nscenes, s);
     if (nedges > 0) count_launch(), k_strain_setup<<<nblk(nedges, 256), 256, 0, s>>>(edges, nedges, xo, se, hot);
     // scenes with at most `cap` slots are swept in shared memory (cap -1: none)
     int cap = plan.window ? strain_window_slot_cap() : -1;
-    if (plan.window) {
-        size_t smem = (size_t)plan.max_window_slots * sizeof(WinSlot);
+    size_t smem = (size_t)plan.max_window_slots * sizeof(WinSlot);
+    if (plan.window)
         cudaFuncSetAttribute(k_strain_window, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStrainWindowBytes);
-        count_launch(), k_strain_window<<<nscenes, 256, smem, s>>>(se, hot, hdr, scenes, cap, load_list, wb_list, av,
-                                                                   passes_out);
+    for (int pass = 0; pass < kStrainMaxIter; ++pass) {
+        if (nchunks > 0) count_launch(), k_strain_check<<<nchunks, 256, 0, s>>>(se, hot, chunks, scenes, av, flags);
+        if (plan.window)
+            count_launch(), k_strain_window<<<nscenes, plan.block, smem, s>>>(se, hot, hdr, scenes, cap, load_list,
+                                                                              wb_list, av, pass, flags, passes_out);
+        if (!plan.window || plan.any_global)
+            count_launch(), k_strain<<<nscenes, 256, 0, s>>>(se, hdr, scenes, cap, av, pass, flags, passes_out);
     }
-    if (!plan.window || plan.any_global)
-        count_launch(), k_strain<<<nscenes, 256, 0, s>>>(se, hdr, scenes, cap, av, passes_out);
 }
 
 void final_velocity(const uint8_t* in_elem, const uint8_t* has_collsn, const double4_32a* av, const int* vscene,

@@ -54,7 +54,8 @@ void dfree(T*& p) {
 __global__ void k_reset_counters(PassCounters* c) {
     int keep = c->err & kErrNan;
     c->npairs = 0; c->ncontrib = 0; c->nhit_pairs = 0; c->nrec = 0;
-    c->nvisits = 0; c->ncontacts = 0; c->nsub = 0; c->ncr = 0; c->nunion = 0; c->err = keep;
+    c->nvisits = 0; c->ncontacts = 0; c->nsub = 0; c->ncr = 0; c->nunion = 0; c->nsub_pt = 0; c->nsub_ee = 0;
+    c->err = keep;
 }
 
 // Counters and per-scene hit counts of a pass attempt.
@@ -63,7 +64,8 @@ __global__ void k_reset_pass(PassCounters* c, SceneRun* run, int nscenes) {
     if (i == 0) {
         int keep = c->err & kErrNan;
         c->npairs = 0; c->ncontrib = 0; c->nhit_pairs = 0; c->nrec = 0;
-        c->nvisits = 0; c->ncontacts = 0; c->nsub = 0; c->ncr = 0; c->nunion = 0; c->err = keep;
+        c->nvisits = 0; c->ncontacts = 0; c->nsub = 0; c->ncr = 0; c->nunion = 0; c->nsub_pt = 0; c->nsub_ee = 0;
+    c->err = keep;
     }
     if (i < nscenes) run[i].hits = 0;
 }
@@ -235,6 +237,9 @@ struct cc_solver {
     int2* d_strain_wb = nullptr;
     void* d_strain_step = nullptr;
     int* d_strain_passes = nullptr;  // 3 per scene
+    int* d_strain_flags = nullptr;   // 2 per scene
+    int2* d_strain_chunks = nullptr; // (scene, first edge) per run of <= 256 edges
+    int n_strain_chunks = 0;
     std::vector<int> h_strain_passes;
 
     // state
@@ -263,7 +268,11 @@ struct cc_solver {
     Box6* d_box = nullptr;
     BvhBufs bvh{};
     int2* d_pairs = nullptr;
+    int* d_pair_hit = nullptr;  // hit flag per candidate pair (split passes)
     int pair_cap = 0;
+    SubRec* d_sub_pt = nullptr;
+    SubRec* d_sub_ee = nullptr;
+    int sub_cap = 0;
     Contrib* d_contrib = nullptr;
     int contrib_cap = 0;
     ApplyBufs apply{};
@@ -300,6 +309,8 @@ struct cc_solver {
     int zone_cap = 10000;
     int mode = 0;  // 0 plain FP64, 1 mixed precision
     bool strain_window = true;
+    bool split_narrow = true;  // two-stage narrow phase for mixed passes
+    LaunchTuning tune;
     int host_threads = 0;  // tree emulation threads (0: hardware concurrency)
 
     // per-stage GPU time, measured with events on the solver's stream
@@ -340,6 +351,8 @@ struct cc_solver {
     void release_mesh() {
         dfree(d_ev); dfree(d_esurf); dfree(d_erigid); dfree(d_fixed); dfree(d_in_elem); dfree(d_edges);
         dfree(d_strain_hdr); dfree(d_strain_load); dfree(d_strain_wb); dfree(d_strain_passes);
+        dfree(d_strain_flags); dfree(d_strain_chunks);
+        n_strain_chunks = 0;
         if (d_strain_step) cudaFree(d_strain_step);
         d_strain_step = nullptr;
         dfree(d_scenes); dfree(d_run); dfree(d_vscene); dfree(d_escene);
@@ -355,7 +368,8 @@ struct cc_solver {
         dfree(bvh.range_lo); dfree(bvh.parent); dfree(bvh.flags); dfree(bvh.node); dfree(bvh.bbox_enc);
         if (bvh.sort_temp) cudaFree(bvh.sort_temp);
         bvh = BvhBufs{};
-        dfree(d_pairs); dfree(d_contrib);
+        dfree(d_pairs); dfree(d_contrib); dfree(d_pair_hit); dfree(d_sub_pt); dfree(d_sub_ee);
+        sub_cap = 0;
         dfree(apply.cnt); dfree(apply.off); dfree(apply.cur); dfree(apply.idx);
         if (apply.scan_temp) cudaFree(apply.scan_temp);
         apply.scan_temp = nullptr;
@@ -396,7 +410,9 @@ struct cc_solver {
 
     cc_status grow_pairs(int cap) {
         dfree(d_pairs);
-        if (dalloc(&d_pairs, (size_t)cap) != cudaSuccess) return fail(CC_NO_MEMORY, "pair buffer");
+        dfree(d_pair_hit);
+        if (dalloc(&d_pairs, (size_t)cap) != cudaSuccess || dalloc(&d_pair_hit, (size_t)cap) != cudaSuccess)
+            return fail(CC_NO_MEMORY, "pair buffer");
         pair_cap = cap;
         if (record) {
             dfree(d_rec);
@@ -414,6 +430,14 @@ struct cc_solver {
         return CC_OK;
     }
 
+    cc_status grow_subs(int cap) {
+        dfree(d_sub_pt);
+        dfree(d_sub_ee);
+        if (dalloc(&d_sub_pt, (size_t)cap) != cudaSuccess || dalloc(&d_sub_ee, (size_t)cap) != cudaSuccess)
+            return fail(CC_NO_MEMORY, "sub-test queues");
+        sub_cap = cap;
+        return CC_OK;
+    }
     cc_status grow_unions(int cap) {
         dfree(d_urec);
         if (dalloc(&d_urec, (size_t)cap) != cudaSuccess) return fail(CC_NO_MEMORY, "union record buffer");
@@ -504,7 +528,7 @@ struct cc_solver {
     }
 
     StrainPlan strain_plan() const {
-        StrainPlan pl{strain_window, 0, false};
+        StrainPlan pl{strain_window, 0, false, tune.strain_block};
         int cap = strain_window_slot_cap();
         for (const SceneDev& sd : h_scenes) {
             if (strain_window && sd.strain_slots <= cap)
@@ -567,7 +591,7 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     std::vector<uint8_t> fixed((size_t)nv, 0), in_elem((size_t)nv, 0), erigid((size_t)ne, 0);
     std::vector<StrainEdge> all_edges;
     std::vector<int4> hdr;
-    std::vector<int2> load, wb;
+    std::vector<int2> load, wb, chunks;
     int v0 = 0, e0 = 0;
     for (int si = 0; si < n; ++si) {
         const cc_mesh* m = &meshes[si];
@@ -625,6 +649,9 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
             }
         }
         size_t nload = load.size();
+        sd.strain_e0 = (int)all_edges.size();
+        sd.strain_ne = (int)edges.size();
+        for (int c = 0; c < sd.strain_ne; c += 256) chunks.push_back(int2{si, sd.strain_e0 + c});
         append_strain_schedule(edges, v0, snv, all_edges, hdr, load, wb, sd);
         sh.strain_edges = (int)edges.size();
         sh.strain_points = (int)(load.size() - nload);
@@ -650,6 +677,9 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     ok &= dalloc(&d_strain_load, load.size()) == cudaSuccess;
     ok &= dalloc(&d_strain_wb, wb.size()) == cudaSuccess;
     ok &= dalloc(&d_strain_passes, 3 * (size_t)n) == cudaSuccess;
+    ok &= dalloc(&d_strain_flags, 2 * (size_t)n) == cudaSuccess;
+    ok &= dalloc(&d_strain_chunks, chunks.size()) == cudaSuccess;
+    n_strain_chunks = (int)chunks.size();
     ok &= cudaMalloc(&d_strain_step, strain_step_bytes(nedges)) == cudaSuccess;
     ok &= dalloc(&d_xo, (size_t)nv) == cudaSuccess;
     ok &= dalloc(&d_av, (size_t)nv) == cudaSuccess;
@@ -706,6 +736,8 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
                         stream);
     if (!hdr.empty())
         cudaMemcpyAsync(d_strain_hdr, hdr.data(), sizeof(int4) * hdr.size(), cudaMemcpyHostToDevice, stream);
+    if (!chunks.empty())
+        cudaMemcpyAsync(d_strain_chunks, chunks.data(), sizeof(int2) * chunks.size(), cudaMemcpyHostToDevice, stream);
     if (!load.empty()) {
         cudaMemcpyAsync(d_strain_load, load.data(), sizeof(int2) * load.size(), cudaMemcpyHostToDevice, stream);
         cudaMemcpyAsync(d_strain_wb, wb.data(), sizeof(int2) * wb.size(), cudaMemcpyHostToDevice, stream);
@@ -722,6 +754,7 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     for (int p = 0; p < nv; ++p) uf_root[p] = uf_tail[p] = p;
     uf_touched.clear();
     if (grow_unions(1024)) return CC_NO_MEMORY;
+    if (grow_subs(2 * ne + 4096)) return CC_NO_MEMORY;
     h_strain_passes.assign(3 * (size_t)n, 0);
     scenes_dirty = true;
     upload_scenes();  // synchronises: the host vectors above are pageable
@@ -794,7 +827,7 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
     for (int attempt = 0; attempt < 8; ++attempt) {
         count_launch(), k_reset_pass<<<(nscenes + 255) / 256, 256, 0, stream>>>(d_ctr, d_run, nscenes);
         prof(kStTraverse, true);
-        bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, record ? nullptr : d_ev);
+        bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, record ? nullptr : d_ev, tune.traverse_block);
         prof(kStTraverse, false);
         NarrowArgs a;
         a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
@@ -807,8 +840,17 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
         a.p32 = d_p32;
         a.v32 = d_v32;
         a.check = 0;
+        a.sub_pt = d_sub_pt;
+        a.sub_ee = d_sub_ee;
+        a.sub_cap = sub_cap;
+        a.pair_hit = d_pair_hit;
         prof(moving ? kStNarrowCcd : kStNarrowProx, true);
-        narrow_pass(a, moving, pair_cap, stream);
+        // mixed passes without impact zones or recording run in two stages:
+        // per-pair FP32 filters, then the surviving FP64 sub-tests densely
+        if (mode == 1 && !any_zone && !record && split_narrow)
+            narrow_pass_split(a, moving, pair_cap, stream, tune.narrow_block);
+        else
+            narrow_pass(a, moving, pair_cap, stream, tune.narrow_block);
         prof(moving ? kStNarrowCcd : kStNarrowProx, false);
         prof(kStApply, true);
         apply_contribs(d_contrib, d_ctr, contrib_cap, nv, d_av, d_hc, apply, stream);
@@ -831,6 +873,11 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
         }
         if (e & kErrRecordOverflow) {
             st = grow_pairs(pair_cap);
+            if (st) return st;
+            continue;
+        }
+        if (e & kErrSubOverflow) {
+            st = grow_subs(2 * std::max(h_ctr->nsub_pt, h_ctr->nsub_ee) + 1024);
             if (st) return st;
             continue;
         }
@@ -1027,8 +1074,8 @@ cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, dou
     finalize_positions(d_in_elem, d_xo, d_av, d_hc, x_cand, x_out, nv, d_vscene, d_scenes, stream);
     prof(kStFinalize, false);
     prof(kStStrain, true);
-    strain_limit(d_edges, nedges, d_strain_hdr, d_strain_load, d_strain_wb, d_scenes, nscenes, strain_plan(), d_xo,
-                 d_av, d_strain_step, d_strain_passes, stream);
+    strain_limit(d_edges, nedges, d_strain_hdr, d_strain_load, d_strain_wb, d_strain_chunks, n_strain_chunks,
+                 d_scenes, nscenes, strain_plan(), d_xo, d_av, d_strain_step, d_strain_flags, d_strain_passes, stream);
     prof(kStStrain, false);
     final_velocity(d_in_elem, d_hc, d_av, d_vscene, d_scenes, vel, nv, stream);
     if (hc != d_hc) cudaMemcpyAsync(hc, d_hc, (size_t)nv, cudaMemcpyDeviceToDevice, stream);
@@ -1254,6 +1301,37 @@ cc_status cc_check_ccd(cc_solver* s, const double* x_old, const double* x_new, l
     if (s->nv && (!x_old || !x_new)) return s->fail(CC_BAD_INPUT, "null array");
     cudaSetDevice(s->device);
     return s->check_ccd(x_old, x_new, hits, scene_hits);
+}
+
+cc_status cc_set_tuning(cc_solver* s, int knob, int value) {
+    if (!s) return CC_BAD_INPUT;
+    switch (knob) {
+        case CC_TUNE_SPLIT_NARROW:
+            s->split_narrow = value != 0;
+            return CC_OK;
+        case CC_TUNE_STRAIN_BLOCK:
+            if (value < 32 || value > 256 || value % 32) return CC_BAD_INPUT;
+            s->tune.strain_block = value;
+            return CC_OK;
+        case CC_TUNE_TRAVERSE_BLOCK:
+        case CC_TUNE_NARROW_BLOCK:
+            if (value < 32 || value > (knob == CC_TUNE_NARROW_BLOCK ? 512 : 1024) || value % 32) return CC_BAD_INPUT;
+            (knob == CC_TUNE_TRAVERSE_BLOCK ? s->tune.traverse_block : s->tune.narrow_block) = value;
+            return CC_OK;
+        default:
+            return CC_BAD_INPUT;
+    }
+}
+
+int cc_get_tuning(cc_solver* s, int knob) {
+    if (!s) return -1;
+    switch (knob) {
+        case CC_TUNE_SPLIT_NARROW: return s->split_narrow ? 1 : 0;
+        case CC_TUNE_TRAVERSE_BLOCK: return s->tune.traverse_block;
+        case CC_TUNE_NARROW_BLOCK: return s->tune.narrow_block;
+        case CC_TUNE_STRAIN_BLOCK: return s->tune.strain_block;
+        default: return -1;
+    }
 }
 
 cc_status cc_set_zone_cap(cc_solver* s, int cap) {

@@ -179,6 +179,15 @@ class CollisionSolver3d:
         hi = _c(U, np.float64)
         self._check(self._lib.cc_set_scene_domain_boundary(self._h, int(scene), lo.ctypes.data, hi.ctypes.data))
 
+    TUNE_SPLIT_NARROW, TUNE_TRAVERSE_BLOCK, TUNE_NARROW_BLOCK, TUNE_STRAIN_BLOCK = 0, 1, 2, 3
+
+    def setTuning(self, knob: int, value: int):
+        """Launch shapes and the two-stage narrow phase; none changes results."""
+        self._check(self._lib.cc_set_tuning(self._h, int(knob), int(value)))
+
+    def getTuning(self, knob: int) -> int:
+        return int(self._lib.cc_get_tuning(self._h, int(knob)))
+
     def setZoneCap(self, cap: int):
         """Impact-zone passes per scene and step before the loop is stopped."""
         self._check(self._lib.cc_set_zone_cap(self._h, int(cap)))

@@ -172,6 +172,20 @@ cc_status cc_get_scene_status(cc_solver* s, int* out);
  * velocities and flags. */
 cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
 
+/* Tuning knobs (none changes results):
+ *   CC_TUNE_SPLIT_NARROW    1 (default): mixed passes without impact zones
+ *                           or recording filter per pair, then run the FP64
+ *                           sub-tests that pass, one thread each; 0: one
+ *                           thread per pair throughout
+ *   CC_TUNE_TRAVERSE_BLOCK  threads per block of the BVH traversal (32..1024)
+ *   CC_TUNE_NARROW_BLOCK    threads per block of the per-pair filter stage
+ *                           of split passes (32..512)
+ *   CC_TUNE_STRAIN_BLOCK    threads of each scene's strain-sweep CTA (32..256)
+ * cc_get_tuning returns the current value, or -1 for an unknown knob. */
+enum { CC_TUNE_SPLIT_NARROW = 0, CC_TUNE_TRAVERSE_BLOCK = 1, CC_TUNE_NARROW_BLOCK = 2, CC_TUNE_STRAIN_BLOCK = 3 };
+cc_status cc_set_tuning(cc_solver* s, int knob, int value);
+int cc_get_tuning(cc_solver* s, int knob);
+
 /* Host threads that emulate the reference's tree insertion order when a
  * scene's tree is (re)built, one scene per thread (0 = one per hardware
  * thread, the default). */
