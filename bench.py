@@ -25,6 +25,9 @@ per second.
               scene stops after --zone-cap zone passes, is counted in
               capped_scenes and is left out of the following steps (in every
               arm alike)
+  autotune    after the warm-up steps, cc_autotune picks the traversal and
+              narrow-phase launch shapes on the state reached (outside the
+              timed region); the chosen settings are reported
   L2          flushed (256 MiB write) before every timed step
 
 --workload picks one of the other measured scenes (folded_cloth,
@@ -263,6 +266,8 @@ def run_gpu(args):
                 drop_capped(s, enabled)
                 st["x"], st["xo"] = st["xo"], st["x"]
         sync_all()
+        tuned = s.autotune() if not args.no_autotune else None
+        sync_all()
         scene_steps = 0
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
         counters, missed, snap = [], 0, None
@@ -290,7 +295,7 @@ def run_gpu(args):
         s.close()
         return dict(total_ms=max_over_ranks(float(sum(step_ms))), step_ms=step_ms, counters=counters,
                     missed=missed, snap=snap, prof=prof, clocks=clk.summary(), scene_steps=scene_steps,
-                    capped=int((~enabled).sum()))
+                    capped=int((~enabled).sum()), tuned=tuned)
 
     # ------------------------------ plain FP64, one scene at a time
     def plain_sequential():
@@ -376,6 +381,8 @@ def run_gpu(args):
             host_candidate()
             e2e_call()
             hx.copy_(hxo)
+        if not args.no_autotune:
+            s2.autotune()
         ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
         with torch.cuda.stream(stream):
             for k in range(K):
@@ -461,6 +468,7 @@ def run_gpu(args):
                 "value": batch_plain_value, "ms_per_step": batch_plain["total_ms"] / K},
             "missed_ccd": None if args.no_check else int(mixed["missed"]),
             "capped_scenes": mixed["capped"], "zone_cap": args.zone_cap,
+            "autotune": mixed["tuned"],
             "roofline": roof, "cpu_baseline": cpu, "clocks": mixed["clocks"],
             "e2e": None if e2e_value is None else
                    {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -491,6 +499,7 @@ def main():
     ap.add_argument("--ref-budget", type=float, default=120.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-check", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -75,6 +75,8 @@ def load(path: str = LIB_PATH):
     lib.cc_set_scene_domain_boundary.argtypes = [vp, C.c_int, dp, dp]
     lib.cc_check_ccd.restype = C.c_int
     lib.cc_check_ccd.argtypes = [vp, dp, dp, lp, ip]
+    lib.cc_autotune.restype = C.c_int
+    lib.cc_autotune.argtypes = [vp, C.POINTER(C.c_double)]
     lib.cc_set_tuning.restype = C.c_int
     lib.cc_set_tuning.argtypes = [vp, C.c_int, C.c_int]
     lib.cc_get_tuning.restype = C.c_int

@@ -444,6 +444,16 @@ void bvh_build(const Box6* box, BvhBufs& b, cudaStream_t s) {
                                                                           b.range_lo, b.range_hi);
 }
 
+void bvh_refit(const Box6* box, BvhBufs& b, cudaStream_t s) {
+    int n = b.n;
+    if (n <= 1) return;
+    cudaMemsetAsync(b.flags, 0, sizeof(int) * (size_t)(n - 1), s);
+    count_launch(), k_refit<<<nblk(n, 256), 256, 0, s>>>(box, b.order, n, b.parent, b.flags, b.node);
+    if (b.run)
+        count_launch(), k_scene_roots<<<nblk(b.nscenes, 128), 128, 0, s>>>(b.scenes, b.run, b.nscenes, n, b.parent,
+                                                                          b.range_lo, b.range_hi);
+}
+
 void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCounters* ctr, cudaStream_t s,
                const int* skip_shared_ev, int block) {
     int n = b.n;

@@ -83,6 +83,9 @@ void boxes_bbox(const Box6* box, int n, unsigned long long* bbox_enc, cudaStream
 // Morton keys (scene id above the 30 Morton bits, each scene normalised to
 // its own box), sort, Karras hierarchy, refit, per-scene subtree roots.
 void bvh_build(const Box6* box, BvhBufs& b, cudaStream_t s);
+// New boxes for the same leaves in the same hierarchy (refit and scene
+// roots only): the pairs found are the same, the tree is only less tight.
+void bvh_refit(const Box6* box, BvhBufs& b, cudaStream_t s);
 // All leaf pairs of one scene with overlapping boxes, each unordered pair
 // once; scenes idle in this pass are skipped. With skip_shared_ev (the
 // elements' point ids), pairs of elements sharing a point are left out.

@@ -294,6 +294,10 @@ struct cc_solver {
     int* h_sel = nullptr;        // pinned staging of d_sel
     std::vector<int> sel_prev;   // scene ids of the last expanded selection
     int n_act_e = 0, n_act_p = 0;
+    // the LBVH built this step and for which scenes: later passes of the
+    // step over the same scenes refit it instead of building anew
+    bool bvh_this_step = false;
+    std::vector<int> bvh_set, cur_set;
 
     // recording
     bool record = false;
@@ -483,7 +487,8 @@ struct cc_solver {
     // each one's first leaf in the pass's hierarchy (sets h_run[].leaf0 and
     // bvh.n / bvh.act; the lists are rebuilt only when the set changes).
     void select_active() {
-        std::vector<int> ids;
+        std::vector<int>& ids = cur_set;
+        ids.clear();
         int with_elems = 0;
         int ae = 0, ap = 0;
         for (int s = 0; s < nscenes; ++s) {
@@ -524,7 +529,7 @@ struct cc_solver {
         poff[k] = p;
         cudaMemcpyAsync(d_sel, h_sel, sizeof(int) * (3 * (size_t)k + 2), cudaMemcpyHostToDevice, stream);
         expand_scenes(d_sel, d_sel + k, d_sel + 2 * k + 1, k, ae, ap, d_scenes, d_act_e, d_act_p, stream);
-        sel_prev.swap(ids);
+        sel_prev = ids;
     }
 
     StrainPlan strain_plan() const {
@@ -563,6 +568,7 @@ struct cc_solver {
                            int* has_collision);
     cc_status detect_pass(int moving, bool any_zone);
     cc_status check_ccd(const double* x_old, const double* x_new, long long* hits, int* scene_hits);
+    cc_status autotune(double* best_ms);
     cc_status update_trees(int which);
 };
 
@@ -819,7 +825,13 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
     cc_status st = update_trees(moving);
     if (st) return st;
     prof(kStBvh, true);
-    bvh_build(d_box, bvh, stream);
+    if (bvh_this_step && cur_set == bvh_set) {
+        bvh_refit(d_box, bvh, stream);
+    } else {
+        bvh_build(d_box, bvh, stream);
+        bvh_this_step = true;
+        bvh_set = cur_set;
+    }
     if (mode == 1)
         point_boxes(d_xo, d_av, d_vscene, d_scenes, bvh.act ? d_act_p : nullptr, n_act_p, moving, d_pbox_lo,
                     d_pbox_hi, d_p32, d_v32, stream);
@@ -1011,6 +1023,7 @@ cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, dou
     prof(kStInit, true);
     step_init(x_old, x_cand, nv, d_in_elem, d_vscene, d_scenes, d_xo, d_av, d_ctr, stream);
     reset_zones();
+    bvh_this_step = false;
     prof(kStInit, false);
     for (bool first = true;; first = false) {
         bool any = false, any_zone = false;
@@ -1123,6 +1136,7 @@ cc_status cc_solver::check_ccd(const double* x_old, const double* x_new, long lo
     select_active();
     cudaMemcpyAsync(d_run, h_run, sizeof(SceneRun) * (size_t)nscenes, cudaMemcpyHostToDevice, stream);
     leaf_boxes(d_ev, bvh.act, bvh.n, d_escene, d_scenes, nscenes, d_xo, d_av, 1, d_box, bvh.bbox_enc, stream);
+    bvh_this_step = false;  // the pass hierarchy is replaced
     bvh_build(d_box, bvh, stream);
     for (int attempt = 0; attempt < 8; ++attempt) {
         count_launch(), k_reset_pass<<<(nscenes + 255) / 256, 256, 0, stream>>>(d_ctr, d_run, nscenes);
@@ -1153,6 +1167,125 @@ cc_status cc_solver::check_ccd(const double* x_old, const double* x_new, long lo
     if (scene_hits)
         for (int s = 0; s < nscenes; ++s) scene_hits[s] = h_run[s].hits;
     return cuda_check("ccd check");
+}
+
+// Launch-shape autotuner. On the state of the last step (x_old and the
+// final average velocities), one moving pass of every scene - leaf boxes,
+// a full LBVH build, then the traversal and the narrow phase - is timed for
+// each candidate traversal block size, narrow-phase variant (two-stage or
+// one kernel, mixed precision only) and filter block size; impulses are not
+// applied, so the state is unchanged. The fastest setting is kept, and the
+// pair and sub-test buffers are grown to what the pass needed plus a
+// quarter, so that the passes that follow do not overflow and retry.
+cc_status cc_solver::autotune(double* best_ms) {
+    if (best_ms) *best_ms = 0.0;
+    if (ne == 0) return CC_OK;
+    upload_scenes();
+    for (int s = 0; s < nscenes; ++s)
+        h_run[s] = SceneRun{scenes[s].ne > 0 && scenes[s].enabled ? kSceneCcd : kSceneIdle, 0, 0, -1, -1, {0, 0, 0}};
+    select_active();
+    cudaMemcpyAsync(d_run, h_run, sizeof(SceneRun) * (size_t)nscenes, cudaMemcpyHostToDevice, stream);
+    leaf_boxes(d_ev, bvh.act, bvh.n, d_escene, d_scenes, nscenes, d_xo, d_av, 1, d_box, bvh.bbox_enc, stream);
+    bvh_this_step = false;
+    bvh_build(d_box, bvh, stream);
+    if (mode == 1)
+        point_boxes(d_xo, d_av, d_vscene, d_scenes, bvh.act ? d_act_p : nullptr, n_act_p, 1, d_pbox_lo, d_pbox_hi,
+                    d_p32, d_v32, stream);
+    // ranks only orient pairs here; any tree's will do for timing
+    const int* rank = d_rank[1];
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    auto run_once = [&](const LaunchTuning& t, bool split, float* ms) -> cc_status {
+        for (int attempt = 0; attempt < 8; ++attempt) {
+            count_launch(), k_reset_pass<<<(nscenes + 255) / 256, 256, 0, stream>>>(d_ctr, d_run, nscenes);
+            cudaEventRecord(e0, stream);
+            bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, d_ev, t.traverse_block);
+            NarrowArgs a{};
+            a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
+            a.rank = rank; a.escene = d_escene; a.scenes = d_scenes; a.run = d_run;
+            a.pairs = d_pairs; a.contrib = d_contrib; a.contrib_cap = contrib_cap; a.ctr = d_ctr;
+            a.urec = d_urec; a.urec_cap = urec_cap;
+            a.pbox_lo = mode == 1 ? d_pbox_lo : nullptr;
+            a.pbox_hi = mode == 1 ? d_pbox_hi : nullptr;
+            a.p32 = d_p32; a.v32 = d_v32;
+            a.sub_pt = d_sub_pt; a.sub_ee = d_sub_ee; a.sub_cap = sub_cap; a.pair_hit = d_pair_hit;
+            if (split)
+                narrow_pass_split(a, 1, pair_cap, stream, t.narrow_block);
+            else
+                narrow_pass(a, 1, pair_cap, stream, t.narrow_block);
+            cudaEventRecord(e1, stream);
+            cudaMemcpyAsync(h_ctr, d_ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, stream);
+            if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("autotune");
+            int e = h_ctr->err;
+            if (e & kErrPairOverflow) {
+                cc_status st = grow_pairs(h_ctr->npairs + h_ctr->npairs / 4 + 1024);
+                if (st) return st;
+                continue;
+            }
+            if (e & kErrContribOverflow) {
+                cc_status st = grow_contrib(h_ctr->ncontrib + h_ctr->ncontrib / 4 + 1024);
+                if (st) return st;
+                continue;
+            }
+            if (e & kErrSubOverflow) {
+                int need = std::max(h_ctr->nsub_pt, h_ctr->nsub_ee);
+                cc_status st = grow_subs(need + need / 4 + 1024);
+                if (st) return st;
+                continue;
+            }
+            if (e & kErrUnionOverflow) {
+                cc_status st = grow_unions(h_ctr->nunion + h_ctr->nunion / 4 + 1024);
+                if (st) return st;
+                continue;
+            }
+            if (e & (kErrStack | kErrNan)) return fail(CC_STACK_OVERFLOW, "autotune pass failed");
+            cudaEventElapsedTime(ms, e0, e1);
+            return CC_OK;
+        }
+        return fail(CC_PAIR_OVERFLOW, "autotune: buffers kept overflowing");
+    };
+    auto time_it = [&](const LaunchTuning& t, bool split, float* best) -> cc_status {
+        float m = 0.f, b = 1e30f;
+        for (int r = 0; r < 3; ++r) {
+            cc_status st = run_once(t, split, &m);
+            if (st) return st;
+            b = std::min(b, m);
+        }
+        *best = b;
+        return CC_OK;
+    };
+    LaunchTuning best_t = tune;
+    bool best_split = split_narrow;
+    float best = 1e30f;
+    cc_status st = time_it(best_t, best_split, &best);  // the current setting, which also sizes the buffers
+    const int tb[] = {64, 128, 256, 512};
+    const int nb[] = {64, 128, 256};
+    for (int a : tb) {
+        LaunchTuning t = best_t;
+        t.traverse_block = a;
+        float m;
+        if (!st) st = time_it(t, best_split, &m);
+        if (!st && m < best) { best = m; best_t = t; }
+    }
+    for (int split = (mode == 1 ? 0 : 1); split <= (mode == 1 ? 1 : 0) && !st; ++split) {
+        for (int b : nb) {
+            LaunchTuning t = best_t;
+            t.narrow_block = b;
+            float m;
+            st = time_it(t, split != 0, &m);
+            if (st) break;
+            if (m < best) { best = m; best_t = t; best_split = split != 0; }
+            if (!split) break;  // the one-kernel pass has a fixed block
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st) return st;
+    tune = best_t;
+    split_narrow = best_split;
+    if (best_ms) *best_ms = best;
+    return cuda_check("autotune");
 }
 
 namespace {
@@ -1303,6 +1436,12 @@ cc_status cc_check_ccd(cc_solver* s, const double* x_old, const double* x_new, l
     return s->check_ccd(x_old, x_new, hits, scene_hits);
 }
 
+cc_status cc_autotune(cc_solver* s, double* best_ms) {
+    if (!s) return CC_BAD_INPUT;
+    cudaSetDevice(s->device);
+    return s->autotune(best_ms);
+}
+
 cc_status cc_set_tuning(cc_solver* s, int knob, int value) {
     if (!s) return CC_BAD_INPUT;
     switch (knob) {
@@ -1431,6 +1570,7 @@ int cc_debug_candidate_pairs(cc_solver* s, int moving, int brute_force, int* out
     cudaMemcpyAsync(s->d_run, s->h_run, sizeof(SceneRun) * (size_t)s->nscenes, cudaMemcpyHostToDevice, s->stream);
     leaf_boxes(s->d_ev, s->bvh.act, s->bvh.n, s->d_escene, s->d_scenes, s->nscenes, s->d_xo, s->d_av, moving,
                s->d_box, s->bvh.bbox_enc, s->stream);
+    s->bvh_this_step = false;
     if (!brute_force) bvh_build(s->d_box, s->bvh, s->stream);
     for (int attempt = 0; attempt < 8; ++attempt) {
         count_launch(), k_reset_counters<<<1, 1, 0, s->stream>>>(s->d_ctr);

@@ -188,6 +188,15 @@ class CollisionSolver3d:
     def getTuning(self, knob: int) -> int:
         return int(self._lib.cc_get_tuning(self._h, int(knob)))
 
+    def autotune(self) -> dict:
+        """Pick launch shapes on the current state (after a resolve call);
+        returns the chosen settings and the best timed pass in ms."""
+        ms = C.c_double(0.0)
+        self._check(self._lib.cc_autotune(self._h, C.byref(ms)))
+        return {"traverse_block": self.getTuning(self.TUNE_TRAVERSE_BLOCK),
+                "split_narrow": self.getTuning(self.TUNE_SPLIT_NARROW),
+                "narrow_block": self.getTuning(self.TUNE_NARROW_BLOCK), "pass_ms": ms.value}
+
     def setZoneCap(self, cap: int):
         """Impact-zone passes per scene and step before the loop is stopped."""
         self._check(self._lib.cc_set_zone_cap(self._h, int(cap)))

@@ -185,6 +185,13 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
 enum { CC_TUNE_SPLIT_NARROW = 0, CC_TUNE_TRAVERSE_BLOCK = 1, CC_TUNE_NARROW_BLOCK = 2, CC_TUNE_STRAIN_BLOCK = 3 };
 cc_status cc_set_tuning(cc_solver* s, int knob, int value);
 int cc_get_tuning(cc_solver* s, int knob);
+/* Autotuner: on the state of the last resolve call, times one moving pass
+ * of every scene (traversal and narrow phase, no impulses applied) for
+ * candidate CC_TUNE_TRAVERSE_BLOCK, CC_TUNE_SPLIT_NARROW and
+ * CC_TUNE_NARROW_BLOCK settings, keeps the fastest, and grows the pair and
+ * sub-test buffers to that pass's needs plus a quarter. The solver's state
+ * is unchanged. *best_ms (may be NULL) receives the best time. */
+cc_status cc_autotune(cc_solver* s, double* best_ms);
 
 /* Host threads that emulate the reference's tree insertion order when a
  * scene's tree is (re)built, one scene per thread (0 = one per hardware

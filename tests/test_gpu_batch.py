@@ -258,3 +258,25 @@ def test_zone_cap_stops_one_scene_only(solver_cls):
     assert capped_at is not None
     b.close()
     s.close()
+
+
+def test_autotune_keeps_results(solver_cls):
+    """The autotuner changes launch shapes and buffer sizes only: a solver
+    tuned after its second step produces the same bits as one that is not."""
+    mix = _mix()
+    ref, pv, _ = _run_batch(solver_cls, mix, 6, mode=1)
+    b = solver_cls(0)
+    b.assembleBatch(mix)
+    b.setMode(1)
+    x = np.concatenate([s.x for s in mix])
+    v = np.concatenate([s.v for s in mix])
+    hc = np.zeros(len(x), np.uint8)
+    dt = np.concatenate([np.full(s.nv, s.params["dt"]) for s in mix])[:, None]
+    for k in range(6):
+        xo, vo, ho, hcol = b.resolveCollisionBatch(x, x + dt * v, v, hc)
+        assert np.array_equal(xo, ref[k]["x"]) and np.array_equal(vo, ref[k]["v"]), k
+        if k == 1:
+            got = b.autotune()
+            assert got["traverse_block"] in (64, 128, 256, 512) and got["pass_ms"] > 0
+        x, v, hc = xo, vo, ho
+    b.close()
