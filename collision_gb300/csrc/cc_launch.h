@@ -188,6 +188,9 @@ struct StrainPlan {
     int block;             // threads per sweep CTA
 };
 int strain_window_slot_cap();
+// Once per device before any strain_limit (not a stream operation, so it
+// stays out of captured graphs).
+void strain_configure();
 // step_buf holds strain_step_bytes(nedges); passes_out holds 3 ints per
 // scene (passes, averaged edges, exact tests).
 size_t strain_step_bytes(int nedges);

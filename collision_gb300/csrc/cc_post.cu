@@ -825,6 +825,10 @@ size_t strain_step_bytes(int nedges) {
 
 int strain_window_slot_cap() { return (int)(kStrainWindowBytes / sizeof(WinSlot)); }
 
+void strain_configure() {
+    cudaFuncSetAttribute(k_strain_window, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStrainWindowBytes);
+}
+
 void strain_limit(const StrainEdge* edges, int nedges, const int4* hdr, const int2* load_list, const int2* wb_list,
                   const int2* chunks, int nchunks, const SceneDev* scenes, int nscenes, const StrainPlan& plan,
                   const double4_32a* xo, double4_32a* av, void* step_buf, int* flags, int* passes_out,
@@ -838,8 +842,6 @@ void strain_limit(const StrainEdge* edges, int nedges, const int4* hdr, const in
     // scenes with at most `cap` slots are swept in shared memory (cap -1: none)
     int cap = plan.window ? strain_window_slot_cap() : -1;
     size_t smem = (size_t)plan.max_window_slots * sizeof(WinSlot);
-    if (plan.window)
-        cudaFuncSetAttribute(k_strain_window, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStrainWindowBytes);
     for (int pass = 0; pass < kStrainMaxIter; ++pass) {
         if (nchunks > 0) count_launch(), k_strain_check<<<nchunks, 256, 0, s>>>(se, hot, chunks, scenes, av, flags);
         if (plan.window)

@@ -353,6 +353,7 @@ struct cc_solver {
     ~cc_solver() { release(); }
 
     void release_mesh() {
+        clear_tail_graphs();
         dfree(d_ev); dfree(d_esurf); dfree(d_erigid); dfree(d_fixed); dfree(d_in_elem); dfree(d_edges);
         dfree(d_strain_hdr); dfree(d_strain_load); dfree(d_strain_wb); dfree(d_strain_passes);
         dfree(d_strain_flags); dfree(d_strain_chunks);
@@ -483,6 +484,68 @@ struct cc_solver {
         uf_tail[py] = uf_tail[px];
     }
     cc_status zone_pass_unions();
+
+    // The end of a step: strain limiting and final velocities (after
+    // finalize_positions).
+    void tail_after_finalize(double* vel, uint8_t* hc) {
+        strain_limit(d_edges, nedges, d_strain_hdr, d_strain_load, d_strain_wb, d_strain_chunks, n_strain_chunks,
+                     d_scenes, nscenes, strain_plan(), d_xo, d_av, d_strain_step, d_strain_flags, d_strain_passes,
+                     stream);
+        final_velocity(d_in_elem, d_hc, d_av, d_vscene, d_scenes, vel, nv, stream);
+        if (hc != d_hc) cudaMemcpyAsync(hc, d_hc, (size_t)nv, cudaMemcpyDeviceToDevice, stream);
+    }
+    // The whole end of a step captured once per set of caller pointers and
+    // strain settings, then replayed.
+    struct TailGraph {
+        const void* key[4];
+        int block, window;
+        cudaGraphExec_t exec;
+        long long launches;
+    };
+    std::vector<TailGraph> tail_graphs;
+    bool tail_graphs_on = true;
+    void clear_tail_graphs() {
+        for (auto& g : tail_graphs) cudaGraphExecDestroy(g.exec);
+        tail_graphs.clear();
+    }
+    cc_status run_tail_graph(const double* x_cand, double* x_out, double* vel, uint8_t* hc) {
+        const void* key[4] = {x_cand, x_out, vel, hc};
+        TailGraph* hit = nullptr;
+        for (auto& g : tail_graphs)
+            if (std::equal(key, key + 4, g.key) && g.block == tune.strain_block && g.window == (int)strain_window) {
+                hit = &g;
+                break;
+            }
+        if (!hit) {
+            if (tail_graphs.size() >= 4) {
+                cudaGraphExecDestroy(tail_graphs.front().exec);
+                tail_graphs.erase(tail_graphs.begin());
+            }
+            cudaGraph_t g = nullptr;
+            long long l0 = g_kernel_launches;
+            if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+                return cuda_check("tail capture");
+            finalize_positions(d_in_elem, d_xo, d_av, d_hc, x_cand, x_out, nv, d_vscene, d_scenes, stream);
+            tail_after_finalize(vel, hc);
+            cudaError_t e = cudaStreamEndCapture(stream, &g);
+            long long n = g_kernel_launches - l0;
+            g_kernel_launches = l0;
+            if (e != cudaSuccess || !g) return fail(CC_CUDA_ERROR, std::string("tail capture: ") + cudaGetErrorString(e));
+            TailGraph tg;
+            std::copy(key, key + 4, tg.key);
+            tg.block = tune.strain_block;
+            tg.window = (int)strain_window;
+            tg.launches = n;
+            e = cudaGraphInstantiate(&tg.exec, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return fail(CC_CUDA_ERROR, std::string("tail graph: ") + cudaGetErrorString(e));
+            tail_graphs.push_back(tg);
+            hit = &tail_graphs.back();
+        }
+        if (cudaGraphLaunch(hit->exec, stream) != cudaSuccess) return cuda_check("tail graph launch");
+        count_launch((int)hit->launches);
+        return CC_OK;
+    }
     // Elements and points of the scenes whose h_run mode is not idle, and
     // each one's first leaf in the pass's hierarchy (sets h_run[].leaf0 and
     // bvh.n / bvh.act; the lists are rebuilt only when the set changes).
@@ -763,6 +826,7 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     if (grow_subs(2 * ne + 4096)) return CC_NO_MEMORY;
     h_strain_passes.assign(3 * (size_t)n, 0);
     scenes_dirty = true;
+    strain_configure();
     upload_scenes();  // synchronises: the host vectors above are pageable
     return cuda_check("assemble");
 }
@@ -1083,15 +1147,21 @@ cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, dou
             }
         }
     }
-    prof(kStFinalize, true);
-    finalize_positions(d_in_elem, d_xo, d_av, d_hc, x_cand, x_out, nv, d_vscene, d_scenes, stream);
-    prof(kStFinalize, false);
-    prof(kStStrain, true);
-    strain_limit(d_edges, nedges, d_strain_hdr, d_strain_load, d_strain_wb, d_strain_chunks, n_strain_chunks,
-                 d_scenes, nscenes, strain_plan(), d_xo, d_av, d_strain_step, d_strain_flags, d_strain_passes, stream);
-    prof(kStStrain, false);
-    final_velocity(d_in_elem, d_hc, d_av, d_vscene, d_scenes, vel, nv, stream);
-    if (hc != d_hc) cudaMemcpyAsync(hc, d_hc, (size_t)nv, cudaMemcpyDeviceToDevice, stream);
+    if (tail_graphs_on) {
+        // finalize, strain limiting and final velocities as one graph
+        // (the strain loop ends on the device); profiled as "strain"
+        prof(kStStrain, true);
+        cc_status st = run_tail_graph(x_cand, x_out, vel, hc);
+        if (st) return st;
+        prof(kStStrain, false);
+    } else {
+        prof(kStFinalize, true);
+        finalize_positions(d_in_elem, d_xo, d_av, d_hc, x_cand, x_out, nv, d_vscene, d_scenes, stream);
+        prof(kStFinalize, false);
+        prof(kStStrain, true);
+        tail_after_finalize(vel, hc);
+        prof(kStStrain, false);
+    }
     cudaMemcpyAsync(h_strain_passes.data(), d_strain_passes, sizeof(int) * h_strain_passes.size(),
                     cudaMemcpyDeviceToHost, stream);
     if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("finalize");
@@ -1448,6 +1518,9 @@ cc_status cc_set_tuning(cc_solver* s, int knob, int value) {
         case CC_TUNE_SPLIT_NARROW:
             s->split_narrow = value != 0;
             return CC_OK;
+        case CC_TUNE_TAIL_GRAPH:
+            s->tail_graphs_on = value != 0;
+            return CC_OK;
         case CC_TUNE_STRAIN_BLOCK:
             if (value < 32 || value > 256 || value % 32) return CC_BAD_INPUT;
             s->tune.strain_block = value;
@@ -1469,6 +1542,7 @@ int cc_get_tuning(cc_solver* s, int knob) {
         case CC_TUNE_TRAVERSE_BLOCK: return s->tune.traverse_block;
         case CC_TUNE_NARROW_BLOCK: return s->tune.narrow_block;
         case CC_TUNE_STRAIN_BLOCK: return s->tune.strain_block;
+        case CC_TUNE_TAIL_GRAPH: return s->tail_graphs_on ? 1 : 0;
         default: return -1;
     }
 }

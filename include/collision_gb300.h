@@ -181,8 +181,19 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
  *   CC_TUNE_NARROW_BLOCK    threads per block of the per-pair filter stage
  *                           of split passes (32..512)
  *   CC_TUNE_STRAIN_BLOCK    threads of each scene's strain-sweep CTA (32..256)
+ *   CC_TUNE_TAIL_GRAPH      1 (default): the end of a step (domain clamp and
+ *                           final positions, the strain-limiting loop, whose
+ *                           end is decided on the device, final velocities)
+ *                           runs as one captured CUDA graph, replayed every
+ *                           step; 0: launched kernel by kernel
  * cc_get_tuning returns the current value, or -1 for an unknown knob. */
-enum { CC_TUNE_SPLIT_NARROW = 0, CC_TUNE_TRAVERSE_BLOCK = 1, CC_TUNE_NARROW_BLOCK = 2, CC_TUNE_STRAIN_BLOCK = 3 };
+enum {
+    CC_TUNE_SPLIT_NARROW = 0,
+    CC_TUNE_TRAVERSE_BLOCK = 1,
+    CC_TUNE_NARROW_BLOCK = 2,
+    CC_TUNE_STRAIN_BLOCK = 3,
+    CC_TUNE_TAIL_GRAPH = 4
+};
 cc_status cc_set_tuning(cc_solver* s, int knob, int value);
 int cc_get_tuning(cc_solver* s, int knob);
 /* Autotuner: on the state of the last resolve call, times one moving pass
