@@ -59,8 +59,10 @@ PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 NARROW_BYTES_PER_VISIT = 8 + 8 + 24 + 6 * 64  # pair, two leaf ranks, two elements' ids, x_old+avgVel of 6 points
 
 
-def make_workload(name, seed, nscenes=0):
+def make_workload(name, seed, nscenes=0, large_n=1025):
     from collision_gb300 import scenes
+    if name == "large":
+        return [scenes.large(n=large_n, seed=seed)]
     scs = scenes.workload(name, seed=seed)
     return scs[:nscenes] if nscenes > 0 else scs
 
@@ -78,10 +80,8 @@ def describe(name, scs):
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rk = int(os.environ.get("RANK", "0"))
-    lrk = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rk, lrk
+    from collision_gb300.replicas import dist_env as env
+    return env()
 
 
 class Clocks:
@@ -179,7 +179,7 @@ def run_reference(args):
     ws, rk, _ = dist_env()
     if rk != 0:
         return
-    scs = make_workload(args.workload, args.seed, args.scenes)
+    scs = make_workload(args.workload, args.seed, args.scenes, args.large_n)
     threads = os.cpu_count() or 1
     rate, n, t, steps = oracle_rate(scs, args.steps, args.ref_budget, threads, args.zone_cap,
                                     skip_steps=args.warmup)
@@ -206,8 +206,9 @@ def run_gpu(args):
     torch.cuda.set_device(dev)
     from collision_gb300 import _lib
     from collision_gb300.solver import CollisionSolver3d
-    seed = args.seed + rk
-    scs = make_workload(args.workload, seed, args.scenes)
+    from collision_gb300.replicas import max_over_ranks as mor, rank_seed
+    seed = rank_seed(args.seed, rk)
+    scs = make_workload(args.workload, seed, args.scenes, args.large_n)
     nsc = len(scs)
     stream = torch.cuda.Stream(device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -239,11 +240,7 @@ def run_gpu(args):
         torch.cuda.synchronize()
 
     def max_over_ranks(ms):
-        if ws == 1:
-            return ms
-        t = torch.tensor([ms], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+        return mor(ms, device=dev)
 
     # ------------------------------------------- batched, device-resident
     def drop_capped(s, enabled):
@@ -399,7 +396,80 @@ def run_gpu(args):
         return e2e_ms
 
 
+    # ------------- one scene: both arithmetic modes on the same solver
+    def single_scene_pair():
+        """Each timed step runs once in plain FP64 and once in mixed
+        precision from the same inputs (in alternating order), in one
+        solver, so the host's tree emulation is paid once; the two results
+        must be equal bit for bit."""
+        s = CollisionSolver3d(dev)
+        s.assembleFromScene(scs[0])
+        s.setZoneCap(args.zone_cap)
+        s.setStream(stream.cuda_stream)
+        s.setMode(1)
+        st = device_state()
+        with torch.cuda.stream(stream):
+            for _ in range(W):
+                candidate(st)
+                s.resolveCollisionBatchDevice(st["x"], st["xc"], st["v"], st["hc"], st["xo"])
+                st["x"], st["xo"] = st["xo"], st["x"]
+        sync_all()
+        tuned = s.autotune() if not args.no_autotune else None
+        ms = {0: 0.0, 1: 0.0}
+        same = True
+        counters = []
+        s.setProfiling(True)
+        with Clocks(dev) as clk, torch.cuda.stream(stream):
+            for k in range(K):
+                candidate(st)
+                v0, hc0 = st["v"].clone(), st["hc"].clone()
+                outs = {}
+                for mode in ((0, 1) if k % 2 == 0 else (1, 0)):
+                    st["v"].copy_(v0)
+                    st["hc"].copy_(hc0)
+                    s.setMode(mode)
+                    flush.fill_(float(k))
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    s.resolveCollisionBatchDevice(st["x"], st["xc"], st["v"], st["hc"], st["xo"])
+                    e1.record(stream)
+                    stream.synchronize()
+                    ms[mode] += e0.elapsed_time(e1)
+                    outs[mode] = (st["xo"].clone(), st["v"].clone(), st["hc"].clone())
+                    if mode == 1:
+                        counters.append(s.counters())
+                same &= all(bool(torch.equal(a, b)) for a, b in zip(outs[0], outs[1]))
+                st["xo"].copy_(outs[1][0])
+                st["v"].copy_(outs[1][1])
+                st["hc"].copy_(outs[1][2])
+                st["x"], st["xo"] = st["xo"], st["x"]
+            stream.synchronize()
+        prof = s.profile()
+        s.close()
+        return dict(mixed_ms=max_over_ranks(ms[1]), plain_ms=max_over_ranks(ms[0]), same=same, tuned=tuned,
+                    counters=counters, prof=prof, clocks=clk.summary())
+
     arms = set(args.arms.split(","))
+    if nsc == 1 and "plain" in arms:
+        pair = single_scene_pair()
+        tot = {k: sum(c[k] for c in pair["counters"]) for k in pair["counters"][0]}
+        if rk == 0:
+            value = ws * K / (pair["mixed_ms"] / 1e3)
+            plain_value = ws * K / (pair["plain_ms"] / 1e3)
+            line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
+                    "ms_per_step": pair["mixed_ms"] / K, "higher_is_better": True, "scaling": "weak",
+                    "vs_baseline": None, "dtype": "f64 (f32 filters)", "data": "synthetic",
+                    "config": dict(describe(args.workload, scs), l2="flushed before every timed step",
+                                   path="one scene: mixed precision and plain FP64 on the same inputs"),
+                    "plain_fp64": {"value": plain_value, "ms_per_step": pair["plain_ms"] / K,
+                                   "state_equal_every_step": pair["same"]},
+                    "speedup_vs_plain": value / plain_value, "autotune": pair["tuned"],
+                    "zone_cap": args.zone_cap, "clocks": pair["clocks"], "counters": tot,
+                    "stages_ms": {k: round(v[0], 3) for k, v in pair["prof"].items()}}
+            print(json.dumps(line), flush=True)
+        if ws > 1:
+            torch.distributed.destroy_process_group()
+        return
     mixed = batched_run(1, check=not args.no_check)
     batch_plain = batched_run(0, check=False) if "batch_plain" in arms else None
     plain = plain_sequential() if "plain" in arms else None
@@ -495,6 +565,7 @@ def main():
     ap.add_argument("--arms", default="mixed,batch_plain,plain,e2e",
                     help="arms to run besides the headline batched mixed one (for profiling runs)")
     ap.add_argument("--scenes", type=int, default=0, help="first N scenes of the batched workload (0: all)")
+    ap.add_argument("--large-n", type=int, default=1025, help="cloth vertices per side of the large workload")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--ref-budget", type=float, default=120.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
