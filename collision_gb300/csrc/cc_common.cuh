@@ -147,6 +147,8 @@ struct PassCounters {
     int nunion;       // union records written (impact-zone passes)
     int nsub_pt;      // point-triangle sub-tests queued by a split pass
     int nsub_ee;      // edge-edge sub-tests queued by a split pass
+    int npairq;       // pairs with a queued sub-test (split passes)
+    int pad[3];
 };
 
 #ifdef __CUDACC__

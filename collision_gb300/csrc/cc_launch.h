@@ -126,13 +126,16 @@ struct NarrowArgs {
     SubRec* sub_pt;
     SubRec* sub_ee;
     int sub_cap;
-    int* pair_hit;
+    int* pair_hit;  // per candidate pair: bit s set when sub-test s hit
+    int* pairq;     // candidate pairs with a queued sub-test (capacity: the pair buffer's)
 };
 void narrow_pass(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s, int block = 128);
-// The same pass in two stages (mixed precision only, no impact-zone scene,
-// no recording): FP32 filters per pair, then the FP64 sub-tests that pass
-// them, one thread each.
-void narrow_pass_split(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s, int block = 128);
+// The same pass in stages (mixed precision only, no recording): FP32
+// filters per pair, then the FP64 sub-tests that pass them, one thread
+// each, then - for scenes in impact-zone mode - the createImpZone calls of
+// every pair that hit.
+void narrow_pass_split(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s, int block = 128,
+                       bool zone = false);
 // Inputs of the mixed-precision filter: outward-rounded FP32 boxes of every
 // point over the pass's time window (with its scene's dt), and x_old and
 // (moving passes) avgVel rounded to FP32.

@@ -110,10 +110,79 @@ __global__ void __launch_bounds__(128) k_narrow(NarrowArgs a, int max_pairs) {
     }
 }
 
+// The sub-tests of an element pair in the order of tri_to_tri /
+// tri_to_bond / bond_to_bond (A the found element, B the query element):
+// f(sub, pts, ee) for each.
+template <bool MOVING, class F>
+__device__ __forceinline__ void for_each_subtest(int kind, const int* A, const int* B, F&& f) {
+    int pts[4];
+    if (kind == 0) {
+        int sub = 0;
+        for (int k = 0; k < 2; ++k)
+            for (int i = 0; i < 3; ++i, ++sub) {
+                // proximity tests B's triangle against A's points first; CCD the reverse
+                const int* tri = MOVING ? ((k == 0) ? A : B) : ((k == 0) ? B : A);
+                const int* pt = MOVING ? ((k == 0) ? B : A) : ((k == 0) ? A : B);
+                pts[0] = tri[0]; pts[1] = tri[1]; pts[2] = tri[2]; pts[3] = pt[i];
+                f(sub, pts, false);
+            }
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j, ++sub) {
+                pts[0] = A[i]; pts[1] = A[(i + 1) % 3]; pts[2] = B[j]; pts[3] = B[(j + 1) % 3];
+                f(sub, pts, true);
+            }
+    } else if (kind == 1) {
+        pts[0] = A[0]; pts[1] = A[1]; pts[2] = A[2];
+        pts[3] = B[0];
+        f(0, pts, false);
+        pts[3] = B[1];
+        f(1, pts, false);
+        pts[2] = B[0];
+        pts[3] = B[1];
+        for (int i = 0; i < 3; ++i) {
+            pts[0] = A[i];
+            pts[1] = A[(i + 1) % 3];
+            f(2 + i, pts, true);
+        }
+    } else {
+        pts[0] = A[0]; pts[1] = A[1]; pts[2] = B[0]; pts[3] = B[1];
+        f(0, pts, true);
+    }
+}
+
+// A candidate pair as k_narrow orients it: kind (0 tri-tri, 1 tri-bond,
+// 2 bond-bond), the points of the element handed over first (A) and second
+// (B), and the visiting-order key base (rank of the query leaf, rank of the
+// found leaf). False for a same-rigid-surface pair, which is not visited.
+struct OrientedPair {
+    int kind, n1, n2;
+    int A[3], B[3];
+    unsigned long long keybase;
+};
+__device__ __forceinline__ bool orient_pair(const NarrowArgs& a, int2 pr, OrientedPair& o) {
+    int ri = a.rank[pr.x], rj = a.rank[pr.y];
+    int ea = ri > rj ? pr.x : pr.y;  // found leaf
+    int eb = ri > rj ? pr.y : pr.x;  // query leaf
+    int ra = ri > rj ? ri : rj, rb = ri > rj ? rj : ri;
+    bool ta = a.ev[3 * ea + 2] >= 0, tb = a.ev[3 * eb + 2] >= 0;
+    o.kind = (ta && tb) ? 0 : (!ta && !tb) ? 2 : 1;
+    if (o.kind == 0 && a.esurf[ea] == a.esurf[eb] && a.erigid[ea]) return false;  // dcollid.cpp:762-763, 805-806
+    int e1 = (o.kind == 1 && !ta) ? eb : ea;  // tri-bond pairs are handed over as (tri, bond)
+    int e2 = (o.kind == 1 && !ta) ? ea : eb;
+    for (int i = 0; i < 3; ++i) {
+        o.A[i] = a.ev[3 * e1 + i];
+        o.B[i] = a.ev[3 * e2 + i];
+    }
+    o.n1 = o.A[2] >= 0 ? 3 : 2;
+    o.n2 = o.B[2] >= 0 ? 3 : 2;
+    o.keybase = ((unsigned long long)rb << 26) | ((unsigned long long)ra << 4);
+    return true;
+}
+
 // Stage 1 of a split pass: per candidate pair, the visit bookkeeping of
 // k_narrow, the element-pair filter, and the box and separating-axis filter
-// of every sub-test, in the sub-test order of tri_to_tri / tri_to_bond /
-// bond_to_bond; survivors are queued with their keys.
+// of every sub-test, in sub-test order; survivors are queued with their keys,
+// and a pair with survivors is queued for stage 3.
 template <bool MOVING>
 __device__ __forceinline__ void queue_sub(const NarrowArgs& a, const NarrowCtx& c, bool ee, unsigned long long kb,
                                           int pair, int sc, const int* pts, int sub, bool& first) {
@@ -128,6 +197,8 @@ __device__ __forceinline__ void queue_sub(const NarrowArgs& a, const NarrowCtx& 
     }
     if (first) {
         a.pair_hit[pair] = 0;
+        int q = aggregated_add(&a.ctr->npairq, 1);
+        a.pairq[q] = pair;  // at most one entry per candidate pair: fits the pair buffer
         first = false;
     }
     SubRec r;
@@ -149,66 +220,57 @@ __global__ void __launch_bounds__(512) k_narrow_filter(NarrowArgs a, int max_pai
     int t_visits = 0;
     for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) {
         int2 pr = a.pairs[idx];
+        OrientedPair o;
+        if (!orient_pair(a, pr, o)) continue;
+        t_visits++;
         int sc = a.escene[pr.x];
         const double eps = a.scenes[sc].p.eps;
         c.hpad = __double2float_ru(MOVING ? eps : a.scenes[sc].p.thickness);
         c.epad = __double2float_ru(eps);
         c.dt32 = __double2float_ru(a.scenes[sc].p.dt);
-        int ri = a.rank[pr.x], rj = a.rank[pr.y];
-        int ea = ri > rj ? pr.x : pr.y;
-        int eb = ri > rj ? pr.y : pr.x;
-        int ra = ri > rj ? ri : rj, rb = ri > rj ? rj : ri;
-        bool ta = a.ev[3 * ea + 2] >= 0, tb = a.ev[3 * eb + 2] >= 0;
-        int kind = (ta && tb) ? 0 : (!ta && !tb) ? 2 : 1;
-        if (kind == 0 && a.esurf[ea] == a.esurf[eb] && a.erigid[ea]) continue;  // dcollid.cpp:762-763, 805-806
-        t_visits++;
-        int e1 = (kind == 1 && !ta) ? eb : ea;
-        int e2 = (kind == 1 && !ta) ? ea : eb;
-        int A[3] = {a.ev[3 * e1], a.ev[3 * e1 + 1], a.ev[3 * e1 + 2]};
-        int B[3] = {a.ev[3 * e2], a.ev[3 * e2 + 1], a.ev[3 * e2 + 2]};
-        int n1 = A[2] >= 0 ? 3 : 2, n2 = B[2] >= 0 ? 3 : 2;
         // a shared point makes every test of the pair return false
         bool shared = false;
-        for (int i = 0; i < n1; ++i)
-            for (int j = 0; j < n2; ++j) shared |= A[i] == B[j];
-        if (shared || !pair_may_hit<MOVING>(c, A, n1, B, n2)) continue;
-        const unsigned long long kb = ((unsigned long long)rb << 26) | ((unsigned long long)ra << 4);
+        for (int i = 0; i < o.n1; ++i)
+            for (int j = 0; j < o.n2; ++j) shared |= o.A[i] == o.B[j];
+        if (shared || !pair_may_hit<MOVING>(c, o.A, o.n1, o.B, o.n2)) continue;
         bool first = true;
-        int pts[4];
-        if (kind == 0) {
-            int sub = 0;
-            for (int k = 0; k < 2; ++k)
-                for (int i = 0; i < 3; ++i, ++sub) {
-                    const int* tri = MOVING ? ((k == 0) ? A : B) : ((k == 0) ? B : A);
-                    const int* pt = MOVING ? ((k == 0) ? B : A) : ((k == 0) ? A : B);
-                    pts[0] = tri[0]; pts[1] = tri[1]; pts[2] = tri[2]; pts[3] = pt[i];
-                    queue_sub<MOVING>(a, c, false, kb, idx, sc, pts, sub, first);
-                }
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j, ++sub) {
-                    pts[0] = A[i]; pts[1] = A[(i + 1) % 3]; pts[2] = B[j]; pts[3] = B[(j + 1) % 3];
-                    queue_sub<MOVING>(a, c, true, kb, idx, sc, pts, sub, first);
-                }
-        } else if (kind == 1) {
-            pts[0] = A[0]; pts[1] = A[1]; pts[2] = A[2];
-            pts[3] = B[0];
-            queue_sub<MOVING>(a, c, false, kb, idx, sc, pts, 0, first);
-            pts[3] = B[1];
-            queue_sub<MOVING>(a, c, false, kb, idx, sc, pts, 1, first);
-            pts[2] = B[0];
-            pts[3] = B[1];
-            for (int i = 0; i < 3; ++i) {
-                pts[0] = A[i];
-                pts[1] = A[(i + 1) % 3];
-                queue_sub<MOVING>(a, c, true, kb, idx, sc, pts, 2 + i, first);
-            }
-        } else {
-            pts[0] = A[0]; pts[1] = A[1]; pts[2] = B[0]; pts[3] = B[1];
-            queue_sub<MOVING>(a, c, true, kb, idx, sc, pts, 0, first);
-        }
+        for_each_subtest<MOVING>(o.kind, o.A, o.B, [&](int sub, const int* pts, bool ee) {
+            queue_sub<MOVING>(a, c, ee, o.keybase, idx, sc, pts, sub, first);
+        });
     }
     for (int o = 16; o > 0; o >>= 1) t_visits += __shfl_xor_sync(0xffffffffu, t_visits, o);
     if ((threadIdx.x & 31) == 0 && t_visits) atomicAdd(&a.ctr->nvisits, t_visits);
+}
+
+// Stage 3 (impact-zone scenes): createImpZone for every sub-test of a pair
+// from its first hit on, in sub-test order - the reference's status stays
+// true after the first hit (dcollid3d.cpp:300-321), whether or not the
+// later sub-tests ran in FP64.
+__global__ void __launch_bounds__(128) k_zone_unions(NarrowArgs a) {
+    int n = a.ctr->npairq;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int pi = a.pairq[i];
+        const int mask = a.pair_hit[pi];
+        if (!mask) continue;
+        const int2 pr = a.pairs[pi];
+        const int sc = a.escene[pr.x];
+        if (a.run[sc].mode != kSceneZone) continue;
+        OrientedPair o;
+        if (!orient_pair(a, pr, o)) continue;
+        const int kfirst = __ffs(mask) - 1;
+        for_each_subtest<true>(o.kind, o.A, o.B, [&](int sub, const int* pts, bool) {
+            if (sub < kfirst) return;
+            int slot = aggregated_add(&a.ctr->nunion, 1);
+            if (slot >= a.urec_cap) {
+                atomicOr(&a.ctr->err, kErrUnionOverflow);
+                return;
+            }
+            UnionRec r;
+            r.key = o.keybase | (unsigned long long)sub;
+            for (int q = 0; q < 4; ++q) r.p[q] = pts[q];
+            a.urec[slot] = r;
+        });
+    }
 }
 
 // Stage 2: one queued sub-test per thread, the FP64 test of k_narrow.
@@ -241,7 +303,7 @@ __global__ void __launch_bounds__(128) k_subtests(NarrowArgs a) {
         t_sub++;
         t_cr += st.ncr;
         t_contacts += st.ncontacts;
-        if (hit && atomicOr(&a.pair_hit[r.pair], 1) == 0) {
+        if (hit && atomicOr(&a.pair_hit[r.pair], 1 << r.sub) == 0) {
             t_hits++;
             atomicAdd(&a.run[r.scene].hits, 1);
         }
@@ -314,7 +376,7 @@ void narrow_pass(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s,
         count_launch(), k_narrow<false><<<blocks, threads, 0, s>>>(a, max_pairs);
 }
 
-void narrow_pass_split(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s, int block) {
+void narrow_pass_split(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s, int block, bool zone) {
     if (max_pairs <= 0) return;
     const int cap_blocks = 152 * 16 * 128 / block;
     int blocks = (max_pairs + block - 1) / block;
@@ -325,6 +387,7 @@ void narrow_pass_split(const NarrowArgs& a, int moving, int max_pairs, cudaStrea
         count_launch(), k_narrow_filter<true><<<blocks, block, 0, s>>>(a, max_pairs);
         count_launch(), k_subtests<true, false><<<sblocks, 128, 0, s>>>(a);
         count_launch(), k_subtests<true, true><<<sblocks, 128, 0, s>>>(a);
+        if (zone) count_launch(), k_zone_unions<<<blocks, 128, 0, s>>>(a);
     } else {
         count_launch(), k_narrow_filter<false><<<blocks, block, 0, s>>>(a, max_pairs);
         count_launch(), k_subtests<false, false><<<sblocks, 128, 0, s>>>(a);

@@ -59,7 +59,7 @@ cudaError_t scratch_address(int device, void** out) {
 __global__ void k_clear_counters(PassCounters* c) {
     c->npairs = 0; c->ncontrib = 0; c->nhit_pairs = 0; c->nrec = 0;
     c->nvisits = 0; c->ncontacts = 0; c->err = 0; c->nsub = 0; c->ncr = 0; c->nunion = 0;
-    c->nsub_pt = 0; c->nsub_ee = 0;
+    c->nsub_pt = 0; c->nsub_ee = 0; c->npairq = 0;
 }
 
 cc_status static_fail(cc_status st, const char* msg) {

@@ -54,7 +54,7 @@ void dfree(T*& p) {
 __global__ void k_reset_counters(PassCounters* c) {
     int keep = c->err & kErrNan;
     c->npairs = 0; c->ncontrib = 0; c->nhit_pairs = 0; c->nrec = 0;
-    c->nvisits = 0; c->ncontacts = 0; c->nsub = 0; c->ncr = 0; c->nunion = 0; c->nsub_pt = 0; c->nsub_ee = 0;
+    c->nvisits = 0; c->ncontacts = 0; c->nsub = 0; c->ncr = 0; c->nunion = 0; c->nsub_pt = 0; c->nsub_ee = 0; c->npairq = 0;
     c->err = keep;
 }
 
@@ -64,7 +64,7 @@ __global__ void k_reset_pass(PassCounters* c, SceneRun* run, int nscenes) {
     if (i == 0) {
         int keep = c->err & kErrNan;
         c->npairs = 0; c->ncontrib = 0; c->nhit_pairs = 0; c->nrec = 0;
-        c->nvisits = 0; c->ncontacts = 0; c->nsub = 0; c->ncr = 0; c->nunion = 0; c->nsub_pt = 0; c->nsub_ee = 0;
+        c->nvisits = 0; c->ncontacts = 0; c->nsub = 0; c->ncr = 0; c->nunion = 0; c->nsub_pt = 0; c->nsub_ee = 0; c->npairq = 0;
     c->err = keep;
     }
     if (i < nscenes) run[i].hits = 0;
@@ -269,6 +269,7 @@ struct cc_solver {
     BvhBufs bvh{};
     int2* d_pairs = nullptr;
     int* d_pair_hit = nullptr;  // hit flag per candidate pair (split passes)
+    int* d_pairq = nullptr;     // pairs with queued sub-tests (split passes)
     int pair_cap = 0;
     SubRec* d_sub_pt = nullptr;
     SubRec* d_sub_ee = nullptr;
@@ -373,7 +374,7 @@ struct cc_solver {
         dfree(bvh.range_lo); dfree(bvh.parent); dfree(bvh.flags); dfree(bvh.node); dfree(bvh.bbox_enc);
         if (bvh.sort_temp) cudaFree(bvh.sort_temp);
         bvh = BvhBufs{};
-        dfree(d_pairs); dfree(d_contrib); dfree(d_pair_hit); dfree(d_sub_pt); dfree(d_sub_ee);
+        dfree(d_pairs); dfree(d_contrib); dfree(d_pair_hit); dfree(d_pairq); dfree(d_sub_pt); dfree(d_sub_ee);
         sub_cap = 0;
         dfree(apply.cnt); dfree(apply.off); dfree(apply.cur); dfree(apply.idx);
         if (apply.scan_temp) cudaFree(apply.scan_temp);
@@ -416,7 +417,9 @@ struct cc_solver {
     cc_status grow_pairs(int cap) {
         dfree(d_pairs);
         dfree(d_pair_hit);
-        if (dalloc(&d_pairs, (size_t)cap) != cudaSuccess || dalloc(&d_pair_hit, (size_t)cap) != cudaSuccess)
+        dfree(d_pairq);
+        if (dalloc(&d_pairs, (size_t)cap) != cudaSuccess || dalloc(&d_pair_hit, (size_t)cap) != cudaSuccess ||
+            dalloc(&d_pairq, (size_t)cap) != cudaSuccess)
             return fail(CC_NO_MEMORY, "pair buffer");
         pair_cap = cap;
         if (record) {
@@ -920,11 +923,12 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
         a.sub_ee = d_sub_ee;
         a.sub_cap = sub_cap;
         a.pair_hit = d_pair_hit;
+        a.pairq = d_pairq;
         prof(moving ? kStNarrowCcd : kStNarrowProx, true);
-        // mixed passes without impact zones or recording run in two stages:
-        // per-pair FP32 filters, then the surviving FP64 sub-tests densely
-        if (mode == 1 && !any_zone && !record && split_narrow)
-            narrow_pass_split(a, moving, pair_cap, stream, tune.narrow_block);
+        // mixed passes without recording run in stages: per-pair FP32
+        // filters, the surviving FP64 sub-tests densely, then the zone unions
+        if (mode == 1 && !record && split_narrow)
+            narrow_pass_split(a, moving, pair_cap, stream, tune.narrow_block, any_zone);
         else
             narrow_pass(a, moving, pair_cap, stream, tune.narrow_block);
         prof(moving ? kStNarrowCcd : kStNarrowProx, false);
@@ -1280,6 +1284,7 @@ cc_status cc_solver::autotune(double* best_ms) {
             a.pbox_hi = mode == 1 ? d_pbox_hi : nullptr;
             a.p32 = d_p32; a.v32 = d_v32;
             a.sub_pt = d_sub_pt; a.sub_ee = d_sub_ee; a.sub_cap = sub_cap; a.pair_hit = d_pair_hit;
+            a.pairq = d_pairq;
             if (split)
                 narrow_pass_split(a, 1, pair_cap, stream, t.narrow_block);
             else
