@@ -81,6 +81,8 @@ def load(path: str = LIB_PATH):
     lib.cc_set_tuning.argtypes = [vp, C.c_int, C.c_int]
     lib.cc_get_tuning.restype = C.c_int
     lib.cc_get_tuning.argtypes = [vp, C.c_int]
+    lib.cc_set_vtk_dump.restype = C.c_int
+    lib.cc_set_vtk_dump.argtypes = [vp, C.c_char_p]
     lib.cc_set_zone_cap.restype = C.c_int
     lib.cc_set_zone_cap.argtypes = [vp, C.c_int]
     lib.cc_get_scene_status.restype = C.c_int

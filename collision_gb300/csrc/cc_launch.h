@@ -153,8 +153,10 @@ struct ApplyBufs {
 };
 // Per-point sums of the pass's contributions in visiting order, then
 // avgVel += (impulse + friction) / n and has_collsn (updateAverageVelocity).
+// dump (may be null): per point, the pass's summed impulse and the number
+// of contributions (zero for points without any).
 void apply_contribs(const Contrib* contrib, const PassCounters* ctr, int contrib_cap, int nv, double4_32a* av,
-                    uint8_t* has_collsn, ApplyBufs& b, cudaStream_t s);
+                    uint8_t* has_collsn, ApplyBufs& b, cudaStream_t s, double4_32a* dump = nullptr);
 
 // updateImpactZoneVelocity (dcollid.cpp:290-310): rigid motion of every
 // zone, one thread per zone over members[zone_off[z] .. zone_off[z+1]) in

@@ -53,7 +53,8 @@ __global__ void k_contrib_scatter(const Contrib* __restrict__ c, const PassCount
 // contributions are put in visiting order and summed one by one from zero,
 // as the reference accumulates collsnImpulse and friction.
 __global__ void k_apply(const Contrib* __restrict__ c, PassCounters* ctr, const int* __restrict__ cnt,
-                        const int* __restrict__ off, int* idx, int nv, double4_32a* av, uint8_t* has_collsn) {
+                        const int* __restrict__ off, int* idx, int nv, double4_32a* av, uint8_t* has_collsn,
+                        double4_32a* dump) {
     if (ctr->err & kErrRetry) return;
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nv) return;
@@ -88,6 +89,7 @@ __global__ void k_apply(const Contrib* __restrict__ c, PassCounters* ctr, const 
     if (bad) atomicOr(&ctr->err, kErrNan);
     av[p] = make_double4_32a(v[0], v[1], v[2], 0.0);
     has_collsn[p] = 1;
+    if (dump) dump[p] = make_double4_32a(imp[0], imp[1], imp[2], (double)n);  // collsnImpulse, collsn_num
 }
 
 __device__ __forceinline__ double det3(const double (*a)[3]) {
@@ -790,7 +792,8 @@ void step_init(const double* x_old, const double* x_cand, int nv, const uint8_t*
 }
 
 void apply_contribs(const Contrib* contrib, const PassCounters* ctr, int contrib_cap, int nv, double4_32a* av,
-                    uint8_t* has_collsn, ApplyBufs& b, cudaStream_t s) {
+                    uint8_t* has_collsn, ApplyBufs& b, cudaStream_t s, double4_32a* dump) {
+    if (dump && nv > 0) cudaMemsetAsync(dump, 0, sizeof(double4_32a) * (size_t)nv, s);
     if (nv <= 0) return;
     cudaMemsetAsync(b.cnt, 0, sizeof(int) * (size_t)nv, s);
     cudaMemsetAsync(b.cur, 0, sizeof(int) * (size_t)nv, s);
@@ -800,7 +803,7 @@ void apply_contribs(const Contrib* contrib, const PassCounters* ctr, int contrib
     exclusive_scan(b.cnt, b.off, nv, nullptr, b.scan_temp, s);
     count_launch(), k_contrib_scatter<<<blocks, 256, 0, s>>>(contrib, ctr, contrib_cap, b.off, b.cur, b.idx);
     count_launch(), k_apply<<<nblk(nv, 128), 128, 0, s>>>(contrib, const_cast<PassCounters*>(ctr), b.cnt, b.off,
-                                                          b.idx, nv, av, has_collsn);
+                                                          b.idx, nv, av, has_collsn, dump);
 }
 
 void zone_solve(const int* members, const int* zone_off, int nzones, const uint8_t* fixed, const double4_32a* xo,

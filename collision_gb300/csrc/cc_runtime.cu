@@ -21,8 +21,11 @@
 #include <vector>
 
 #include "../../include/collision_gb300.h"
+#include <sys/stat.h>
+
 #include "cc_launch.h"
 #include "cc_tree_order.h"
+#include "cc_vtk.h"
 
 using namespace ccg;
 
@@ -300,6 +303,12 @@ struct cc_solver {
     bool bvh_this_step = false;
     std::vector<int> bvh_set, cur_set;
 
+    // VTK dumps of every pass (empty: off)
+    std::string vtk_dir;
+    std::vector<int> vtk_count, h_ev;
+    double4_32a* d_dump = nullptr;
+    double4_32a* d_av_pre = nullptr;
+
     // recording
     bool record = false;
     VisitRec* d_rec = nullptr;
@@ -381,7 +390,7 @@ struct cc_solver {
         apply.scan_temp = nullptr;
         dfree(d_rank[0]); dfree(d_rank[1]);
         dfree(d_rec); dfree(d_pbox_lo); dfree(d_pbox_hi); dfree(d_p32); dfree(d_v32);
-        dfree(d_act_e); dfree(d_act_p); dfree(d_sel);
+        dfree(d_act_e); dfree(d_act_p); dfree(d_sel); dfree(d_dump); dfree(d_av_pre);
         if (h_sel) cudaFreeHost(h_sel);
         h_sel = nullptr;
         sel_prev.clear();
@@ -487,6 +496,39 @@ struct cc_solver {
         uf_tail[py] = uf_tail[px];
     }
     cc_status zone_pass_unions();
+
+    // One .vtp per scene of the pass just applied (cc_vtk.cpp).
+    cc_status write_vtk_pass() {
+        std::vector<double4_32a> xo((size_t)nv), av((size_t)nv), dump((size_t)nv);
+        cudaMemcpyAsync(xo.data(), d_xo, sizeof(double4_32a) * (size_t)nv, cudaMemcpyDeviceToHost, stream);
+        cudaMemcpyAsync(av.data(), d_av_pre, sizeof(double4_32a) * (size_t)nv, cudaMemcpyDeviceToHost, stream);
+        cudaMemcpyAsync(dump.data(), d_dump, sizeof(double4_32a) * (size_t)nv, cudaMemcpyDeviceToHost, stream);
+        if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("vtk dump");
+        std::vector<double> pos((size_t)nv * 3), imp((size_t)nv * 3), num((size_t)nv);
+        for (int p = 0; p < nv; ++p) {
+            double dt = h_scenes[h_vscene[p]].p.dt;  // updateFinalPosition before the impulses
+            pos[3 * p] = xo[p].x + dt * av[p].x;
+            pos[3 * p + 1] = xo[p].y + dt * av[p].y;
+            pos[3 * p + 2] = xo[p].z + dt * av[p].z;
+            imp[3 * p] = dump[p].x;
+            imp[3 * p + 1] = dump[p].y;
+            imp[3 * p + 2] = dump[p].z;
+            num[p] = dump[p].w;
+        }
+        for (int s = 0; s < nscenes; ++s) {
+            if (h_run[s].mode == kSceneIdle || scenes[s].ne == 0) continue;
+            char name[64];
+            if (nscenes == 1)
+                std::snprintf(name, sizeof(name), "/surf-%03d.vtp", vtk_count[s]++);
+            else
+                std::snprintf(name, sizeof(name), "/surf-s%03d-%03d.vtp", s, vtk_count[s]++);
+            std::string path = vtk_dir + name;
+            if (!write_vtp(path.c_str(), scenes[s].ne, h_ev.data() + 3 * (size_t)scenes[s].e0, pos.data(), imp.data(),
+                           num.data()))
+                return fail(CC_BAD_INPUT, "cannot write " + path);
+        }
+        return CC_OK;
+    }
 
     // The end of a step: strain limiting and final velocities (after
     // finalize_positions).
@@ -819,6 +861,8 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     h_boxes.resize((size_t)ne);
     h_rank.resize((size_t)ne);
     h_vscene.swap(vscene);
+    h_ev = ev;
+    vtk_count.assign((size_t)n, 0);
     uf_root.resize((size_t)nv);
     uf_next.assign((size_t)nv, -1);
     uf_tail.resize((size_t)nv);
@@ -903,6 +947,9 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
         point_boxes(d_xo, d_av, d_vscene, d_scenes, bvh.act ? d_act_p : nullptr, n_act_p, moving, d_pbox_lo,
                     d_pbox_hi, d_p32, d_v32, stream);
     prof(kStBvh, false);
+    const bool dump = !vtk_dir.empty();
+    if (dump)
+        cudaMemcpyAsync(d_av_pre, d_av, sizeof(double4_32a) * (size_t)nv, cudaMemcpyDeviceToDevice, stream);
     for (int attempt = 0; attempt < 8; ++attempt) {
         count_launch(), k_reset_pass<<<(nscenes + 255) / 256, 256, 0, stream>>>(d_ctr, d_run, nscenes);
         prof(kStTraverse, true);
@@ -933,7 +980,7 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
             narrow_pass(a, moving, pair_cap, stream, tune.narrow_block);
         prof(moving ? kStNarrowCcd : kStNarrowProx, false);
         prof(kStApply, true);
-        apply_contribs(d_contrib, d_ctr, contrib_cap, nv, d_av, d_hc, apply, stream);
+        apply_contribs(d_contrib, d_ctr, contrib_cap, nv, d_av, d_hc, apply, stream, dump ? d_dump : nullptr);
         prof(kStApply, false);
         cudaMemcpyAsync(h_ctr, d_ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, stream);
         cudaMemcpyAsync(h_run, d_run, sizeof(SceneRun) * (size_t)nscenes, cudaMemcpyDeviceToHost, stream);
@@ -969,6 +1016,10 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
         break;
     }
     if (h_ctr->err) return fail(CC_PAIR_OVERFLOW, "buffers kept overflowing");
+    if (dump) {
+        st = write_vtk_pass();
+        if (st) return st;
+    }
     counters[3] += h_ctr->npairs;
     counters[4] += h_ctr->nvisits;
     counters[5] += h_ctr->nhit_pairs;
@@ -1550,6 +1601,24 @@ int cc_get_tuning(cc_solver* s, int knob) {
         case CC_TUNE_TAIL_GRAPH: return s->tail_graphs_on ? 1 : 0;
         default: return -1;
     }
+}
+
+cc_status cc_set_vtk_dump(cc_solver* s, const char* dir) {
+    if (!s) return CC_BAD_INPUT;
+    cudaSetDevice(s->device);
+    s->vtk_dir = dir ? dir : "";
+    if (s->vtk_dir.empty()) return CC_OK;
+    mkdir(s->vtk_dir.c_str(), 0755);  // as create_directory(fname, NO), dcollid.cpp:689
+    struct stat sb;
+    if (stat(s->vtk_dir.c_str(), &sb) != 0 || !S_ISDIR(sb.st_mode)) {
+        s->vtk_dir.clear();
+        return s->fail(CC_BAD_INPUT, "cannot create the dump directory");
+    }
+    bool ok = true;
+    if (!s->d_dump) ok &= dalloc(&s->d_dump, (size_t)s->nv) == cudaSuccess;
+    if (!s->d_av_pre) ok &= dalloc(&s->d_av_pre, (size_t)s->nv) == cudaSuccess;
+    if (!ok) return s->fail(CC_NO_MEMORY, "dump buffers");
+    return CC_OK;
 }
 
 cc_status cc_set_zone_cap(cc_solver* s, int cap) {

@@ -197,6 +197,11 @@ class CollisionSolver3d:
                 "split_narrow": self.getTuning(self.TUNE_SPLIT_NARROW),
                 "narrow_block": self.getTuning(self.TUNE_NARROW_BLOCK), "pass_ms": ms.value}
 
+    def setVtkDump(self, directory):
+        """Write a .vtp of every detection pass into `directory` (None: off)."""
+        d = None if directory is None else str(directory).encode()
+        self._check(self._lib.cc_set_vtk_dump(self._h, d))
+
     def setZoneCap(self, cap: int):
         """Impact-zone passes per scene and step before the loop is stopped."""
         self._check(self._lib.cc_set_zone_cap(self._h, int(cap)))

@@ -204,6 +204,16 @@ int cc_get_tuning(cc_solver* s, int knob);
  * is unchanged. *best_ms (may be NULL) receives the best time. */
 cc_status cc_autotune(cc_solver* s, double* best_ms);
 
+/* Debugging dumps, as the reference writes under its "CollisionImpulse"
+ * flag (dcollid.cpp:684-693, vtk.cpp:14-93): after every detection pass, one
+ * VTK XML PolyData file per scene in dir (created if missing) - surf-NNN.vtp
+ * for a single scene, surf-sSSS-NNN.vtp in a batch - with the surface at
+ * x_old + dt*avgVel before the pass's impulses, each point's accumulated
+ * impulse (CollsnImpulse) and each element red if a point of it was hit in
+ * the pass, green otherwise (CollsnRegion). NULL or "" turns dumps off.
+ * Call after cc_assemble. Slow (host copies each pass). */
+cc_status cc_set_vtk_dump(cc_solver* s, const char* dir);
+
 /* Host threads that emulate the reference's tree insertion order when a
  * scene's tree is (re)built, one scene per thread (0 = one per hardware
  * thread, the default). */

@@ -282,3 +282,47 @@ def test_autotune_keeps_results(solver_cls):
             assert got["traverse_block"] in (64, 128, 256, 512) and got["pass_ms"] > 0
         x, v, hc = xo, vo, ho
     b.close()
+
+
+def test_vtk_dumps(solver_cls, tmp_path):
+    """Every pass writes a .vtp per scene: element points numbered by first
+    appearance, positions x_old + dt*avgVel before the pass's impulses (the
+    first pass's are the candidates), red elements exactly where a point
+    received an impulse."""
+    import xml.etree.ElementTree as ET
+    sc = scenes.cloth_on_sphere(n=12, z=0.252, radius=0.25, sub=2, side=0.4, mu=0.3, speed=3.0, seed=2)
+    s = solver_cls(0)
+    s.assembleFromScene(sc)
+    s.setVtkDump(tmp_path)
+    x, v, hc = sc.x, sc.v, np.zeros(sc.nv, np.uint8)
+    nfiles = 0
+    for step in range(3):
+        xc = x + sc.params["dt"] * v
+        x1, v1, hc1 = s.resolveCollision(x, xc, v, hc)
+        npass = len(s.passKinds())
+        files = sorted(tmp_path.glob("surf-*.vtp"))
+        assert len(files) == nfiles + npass
+        first = ET.parse(files[nfiles]).getroot()
+        nfiles = len(files)
+        piece = first.find("PolyData/Piece")
+        assert int(piece.get("NumberOfPolys")) == sc.ne
+        conn = np.array(piece.find("Polys/DataArray[@Name='connectivity']").text.split(), dtype=int)
+        order, seen = [], set()
+        for t in sc.tris:
+            for p in t:
+                if p not in seen:
+                    seen.add(p)
+                    order.append(p)
+        assert int(piece.get("NumberOfPoints")) == len(order)
+        assert np.array_equal(np.array(order)[conn.reshape(-1, 3)], sc.tris)
+        pts = np.array(piece.find("Points/DataArray").text.split(), dtype=float).reshape(-1, 3)
+        assert np.allclose(pts, xc[order], rtol=0, atol=1e-6 * max(1.0, np.abs(xc).max()))
+        imp = np.array(piece.find("PointData/DataArray").text.split(), dtype=float).reshape(-1, 3)
+        col = np.array(piece.find("CellData/DataArray").text.split(), dtype=int).reshape(-1, 3)
+        hit_pt = np.zeros(sc.nv, bool)
+        hit_pt[np.array(order)[np.abs(imp).sum(1) > 0]] = True
+        red = col[:, 0] == 255
+        assert np.array_equal(red, hit_pt[sc.tris].any(1))
+        x, v, hc = x1, v1, hc1
+    s.setVtkDump(None)
+    s.close()
