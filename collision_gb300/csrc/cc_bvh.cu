@@ -321,7 +321,7 @@ __device__ __forceinline__ void emit_pair(int a, int b, int2* pairs, int cap, Pa
 __global__ void k_traverse(const Box6* __restrict__ box, const unsigned int* __restrict__ order, int n,
                            const BvhNode32* __restrict__ node, const int* __restrict__ elem_scene,
                            const SceneRun* __restrict__ run, const int* __restrict__ ev, int2* pairs, int cap,
-                           PassCounters* ctr) {
+                           PassCounters* ctr, const Box6* __restrict__ box_static) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
     int ei = (int)order[i];
@@ -340,6 +340,8 @@ __global__ void k_traverse(const Box6* __restrict__ box, const unsigned int* __r
     const Box6 q = box[ei];
     const Box32 q32 = box32_out(q);
     const BoxOrd qo = box_ord(q);
+    BoxOrd qs;
+    if (box_static) qs = box_ord(box_static[ei]);
     int stk[kTraversalStack];
     int sp = 0;
     stk[sp++] = root;
@@ -363,7 +365,9 @@ __global__ void k_traverse(const Box6* __restrict__ box, const unsigned int* __r
                     shared = a == pi0 || a == pi1 || a == pi2 || b == pi0 || b == pi1 || b == pi2 ||
                              (c3 >= 0 && (c3 == pi0 || c3 == pi1 || c3 == pi2));
                 }
-                if (!shared) emit_pair(ei, ej, pairs, cap, ctr);
+                if (!shared)
+                    emit_pair(ei, (box_static && overlap_ord(qs, &box_static[ej])) ? (ej | kPairStatic) : ej, pairs,
+                              cap, ctr);
             } else if (sp < kTraversalStack) {
                 stk[sp++] = c;
             } else {
@@ -455,11 +459,11 @@ void bvh_refit(const Box6* box, BvhBufs& b, cudaStream_t s) {
 }
 
 void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCounters* ctr, cudaStream_t s,
-               const int* skip_shared_ev, int block) {
+               const int* skip_shared_ev, int block, const Box6* box_static) {
     int n = b.n;
     if (n <= 1) return;
     count_launch(), k_traverse<<<nblk(n - 1, block), block, 0, s>>>(box, b.order, n, b.node, b.elem_scene, b.run,
-                                                                    skip_shared_ev, pairs, cap, ctr);
+                                                                    skip_shared_ev, pairs, cap, ctr, box_static);
 }
 
 void brute_pairs(const Box6* box, int ne, const int* elem_scene, int2* pairs, int cap, PassCounters* ctr,

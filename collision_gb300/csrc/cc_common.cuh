@@ -62,6 +62,11 @@ enum ErrBits {
 constexpr int kErrRetry =
     kErrPairOverflow | kErrStack | kErrContribOverflow | kErrRecordOverflow | kErrUnionOverflow | kErrSubOverflow;
 
+// Candidate pairs found on swept boxes carry this bit in .y when the two
+// elements' static boxes overlap too (the proximity pass's pairs).
+constexpr int kPairStatic = (int)0x80000000u;
+constexpr int kPairIdMask = 0x7fffffff;
+
 // A sub-test that passed the FP32 filters, queued for the FP64 stage of a
 // split narrow pass: its element pair's visiting-order key base, the pair's
 // index (for the pair's hit flag), its scene, points and sub-test index.

@@ -89,8 +89,10 @@ void bvh_refit(const Box6* box, BvhBufs& b, cudaStream_t s);
 // All leaf pairs of one scene with overlapping boxes, each unordered pair
 // once; scenes idle in this pass are skipped. With skip_shared_ev (the
 // elements' point ids), pairs of elements sharing a point are left out.
+// With box_static, every pair is found on `box` (swept boxes) and carries
+// kPairStatic when the elements' static boxes overlap as well.
 void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCounters* ctr, cudaStream_t s,
-               const int* skip_shared_ev = nullptr, int block = 128);
+               const int* skip_shared_ev = nullptr, int block = 128, const Box6* box_static = nullptr);
 // The same pair set by testing every pair (for cross-checks on small meshes).
 void brute_pairs(const Box6* box, int ne, const int* elem_scene, int2* pairs, int cap, PassCounters* ctr,
                  cudaStream_t s);
@@ -128,6 +130,7 @@ struct NarrowArgs {
     int sub_cap;
     int* pair_hit;  // per candidate pair: bit s set when sub-test s hit
     int* pairq;     // candidate pairs with a queued sub-test (capacity: the pair buffer's)
+    int static_only;  // proximity pass over swept-box pairs: only those with kPairStatic
 };
 void narrow_pass(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s, int block = 128);
 // The same pass in stages (mixed precision only, no recording): FP32

@@ -30,6 +30,8 @@ __global__ void __launch_bounds__(128) k_narrow(NarrowArgs a, int max_pairs) {
     int t_visits = 0, t_sub = 0, t_hits = 0, t_cr = 0, t_contacts = 0;
     for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) {
         int2 pr = a.pairs[idx];
+        if (!MOVING && a.static_only && !(pr.y & kPairStatic)) continue;
+        pr.y &= kPairIdMask;
         int sc = a.escene[pr.x];
         const SceneRun run = a.run[sc];
         c.p = a.scenes[sc].p;
@@ -220,6 +222,8 @@ __global__ void __launch_bounds__(512) k_narrow_filter(NarrowArgs a, int max_pai
     int t_visits = 0;
     for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < np; idx += gridDim.x * blockDim.x) {
         int2 pr = a.pairs[idx];
+        if (!MOVING && a.static_only && !(pr.y & kPairStatic)) continue;
+        pr.y &= kPairIdMask;
         OrientedPair o;
         if (!orient_pair(a, pr, o)) continue;
         t_visits++;
@@ -252,7 +256,8 @@ __global__ void __launch_bounds__(128) k_zone_unions(NarrowArgs a) {
         const int pi = a.pairq[i];
         const int mask = a.pair_hit[pi];
         if (!mask) continue;
-        const int2 pr = a.pairs[pi];
+        int2 pr = a.pairs[pi];
+        pr.y &= kPairIdMask;
         const int sc = a.escene[pr.x];
         if (a.run[sc].mode != kSceneZone) continue;
         OrientedPair o;

@@ -62,11 +62,13 @@ __global__ void k_reset_counters(PassCounters* c) {
 }
 
 // Counters and per-scene hit counts of a pass attempt.
-__global__ void k_reset_pass(PassCounters* c, SceneRun* run, int nscenes) {
+// npairs_keep >= 0: the pair buffer holds this many pairs from an earlier
+// pass that this one reuses.
+__global__ void k_reset_pass(PassCounters* c, SceneRun* run, int nscenes, int npairs_keep = -1) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) {
         int keep = c->err & kErrNan;
-        c->npairs = 0; c->ncontrib = 0; c->nhit_pairs = 0; c->nrec = 0;
+        c->npairs = npairs_keep >= 0 ? npairs_keep : 0; c->ncontrib = 0; c->nhit_pairs = 0; c->nrec = 0;
         c->nvisits = 0; c->ncontacts = 0; c->nsub = 0; c->ncr = 0; c->nunion = 0; c->nsub_pt = 0; c->nsub_ee = 0; c->npairq = 0;
     c->err = keep;
     }
@@ -269,6 +271,14 @@ struct cc_solver {
 
     // pass buffers
     Box6* d_box = nullptr;
+    // The proximity pass finds its pairs on swept boxes, flagging those whose
+    // static boxes (d_box_st) overlap too; when it applies no impulse, the
+    // first CCD pass over the same scenes reuses the list as it is.
+    Box6* d_box_st = nullptr;
+    bool combined_broad = true;
+    bool reuse_pairs = false;
+    int reuse_npairs = 0;
+    std::vector<int> reuse_set;
     BvhBufs bvh{};
     int2* d_pairs = nullptr;
     int* d_pair_hit = nullptr;  // hit flag per candidate pair (split passes)
@@ -379,7 +389,7 @@ struct cc_solver {
         dfree(d_urec); dfree(d_members); dfree(d_zone_off);
         urec_cap = members_cap = zones_cap = 0;
         dfree(d_xold_in); dfree(d_xcand_in); dfree(d_vel); dfree(d_xout); dfree(d_hc);
-        dfree(d_box); dfree(bvh.keys); dfree(bvh.order); dfree(bvh.range_hi);
+        dfree(d_box); dfree(d_box_st); dfree(bvh.keys); dfree(bvh.order); dfree(bvh.range_hi);
         dfree(bvh.range_lo); dfree(bvh.parent); dfree(bvh.flags); dfree(bvh.node); dfree(bvh.bbox_enc);
         if (bvh.sort_temp) cudaFree(bvh.sort_temp);
         bvh = BvhBufs{};
@@ -677,7 +687,7 @@ struct cc_solver {
     cc_status detect_pass(int moving, bool any_zone);
     cc_status check_ccd(const double* x_old, const double* x_new, long long* hits, int* scene_hits);
     cc_status autotune(double* best_ms);
-    cc_status update_trees(int which);
+    cc_status update_trees(int which, const Box6* boxes);
 };
 
 cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
@@ -804,6 +814,7 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     ok &= dalloc(&d_xout, (size_t)nv * 3) == cudaSuccess;
     ok &= dalloc(&d_hc, (size_t)nv) == cudaSuccess;
     ok &= dalloc(&d_box, (size_t)ne) == cudaSuccess;
+    ok &= dalloc(&d_box_st, (size_t)ne) == cudaSuccess;
     bvh.n = ne;
     bvh.nscenes = n;
     bvh.elem_scene = nullptr;
@@ -883,7 +894,7 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
 // one volume; a tree is (re)built on first use or when its root volume has
 // grown by more than 20%. Rebuilds emulate the reference's insertion order
 // on the host, one scene per host thread.
-cc_status cc_solver::update_trees(int which) {
+cc_status cc_solver::update_trees(int which, const Box6* boxes) {
     cudaMemcpyAsync(h_bbox, bvh.bbox_enc, 6 * sizeof(unsigned long long) * (size_t)nscenes, cudaMemcpyDeviceToHost,
                     stream);
     if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("leaf boxes");
@@ -902,7 +913,7 @@ cc_status cc_solver::update_trees(int which) {
     }
     if (todo.empty()) return CC_OK;
     for (int s : todo)
-        cudaMemcpyAsync(h_boxes.data() + scenes[s].e0, d_box + scenes[s].e0, sizeof(Box6) * (size_t)scenes[s].ne,
+        cudaMemcpyAsync(h_boxes.data() + scenes[s].e0, boxes + scenes[s].e0, sizeof(Box6) * (size_t)scenes[s].ne,
                         cudaMemcpyDeviceToHost, stream);
     if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("leaf boxes to host");
     // largest scenes first: they bound the time of the parallel build
@@ -930,13 +941,30 @@ cc_status cc_solver::update_trees(int which) {
 cc_status cc_solver::detect_pass(int moving, bool any_zone) {
     select_active();
     cudaMemcpyAsync(d_run, h_run, sizeof(SceneRun) * (size_t)nscenes, cudaMemcpyHostToDevice, stream);
+    // proximity pass: pairs on swept boxes with the static-overlap flag;
+    // first CCD pass after a proximity pass without impulses: those pairs
+    const bool combined = combined_broad && !moving;
+    const bool reuse = moving && reuse_pairs && cur_set == reuse_set;
+    reuse_pairs = false;
+    cc_status st = CC_OK;
     prof(kStBoxes, true);
-    leaf_boxes(d_ev, bvh.act, bvh.n, d_escene, d_scenes, nscenes, d_xo, d_av, moving, d_box, bvh.bbox_enc, stream);
+    if (combined) {
+        leaf_boxes(d_ev, bvh.act, bvh.n, d_escene, d_scenes, nscenes, d_xo, d_av, 0, d_box_st, bvh.bbox_enc, stream);
+        st = update_trees(0, d_box_st);
+        if (st) return st;
+        leaf_boxes(d_ev, bvh.act, bvh.n, d_escene, d_scenes, nscenes, d_xo, d_av, 1, d_box, bvh.bbox_enc, stream);
+    } else if (!reuse) {
+        leaf_boxes(d_ev, bvh.act, bvh.n, d_escene, d_scenes, nscenes, d_xo, d_av, moving, d_box, bvh.bbox_enc, stream);
+    }
     prof(kStBoxes, false);
-    cc_status st = update_trees(moving);
-    if (st) return st;
+    if (!combined) {
+        st = update_trees(moving, d_box);
+        if (st) return st;
+    }
     prof(kStBvh, true);
-    if (bvh_this_step && cur_set == bvh_set) {
+    if (reuse) {
+        // the hierarchy and the pairs of the proximity pass stand
+    } else if (bvh_this_step && cur_set == bvh_set) {
         bvh_refit(d_box, bvh, stream);
     } else {
         bvh_build(d_box, bvh, stream);
@@ -951,9 +979,12 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
     if (dump)
         cudaMemcpyAsync(d_av_pre, d_av, sizeof(double4_32a) * (size_t)nv, cudaMemcpyDeviceToDevice, stream);
     for (int attempt = 0; attempt < 8; ++attempt) {
-        count_launch(), k_reset_pass<<<(nscenes + 255) / 256, 256, 0, stream>>>(d_ctr, d_run, nscenes);
+        count_launch(), k_reset_pass<<<(nscenes + 255) / 256, 256, 0, stream>>>(d_ctr, d_run, nscenes,
+                                                                                reuse ? reuse_npairs : -1);
         prof(kStTraverse, true);
-        bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, record ? nullptr : d_ev, tune.traverse_block);
+        if (!reuse)
+            bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, record ? nullptr : d_ev, tune.traverse_block,
+                      combined ? d_box_st : nullptr);
         prof(kStTraverse, false);
         NarrowArgs a;
         a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
@@ -971,6 +1002,7 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
         a.sub_cap = sub_cap;
         a.pair_hit = d_pair_hit;
         a.pairq = d_pairq;
+        a.static_only = combined ? 1 : 0;
         prof(moving ? kStNarrowCcd : kStNarrowProx, true);
         // mixed passes without recording run in stages: per-pair FP32
         // filters, the surviving FP64 sub-tests densely, then the zone unions
@@ -1016,6 +1048,11 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
         break;
     }
     if (h_ctr->err) return fail(CC_PAIR_OVERFLOW, "buffers kept overflowing");
+    if (combined && h_ctr->ncontrib == 0) {  // velocities unchanged: the swept pairs hold for the next pass
+        reuse_pairs = true;
+        reuse_npairs = h_ctr->npairs;
+        reuse_set = cur_set;
+    }
     if (dump) {
         st = write_vtk_pass();
         if (st) return st;
@@ -1143,6 +1180,7 @@ cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, dou
     step_init(x_old, x_cand, nv, d_in_elem, d_vscene, d_scenes, d_xo, d_av, d_ctr, stream);
     reset_zones();
     bvh_this_step = false;
+    reuse_pairs = false;
     prof(kStInit, false);
     for (bool first = true;; first = false) {
         bool any = false, any_zone = false;
@@ -1261,7 +1299,8 @@ cc_status cc_solver::check_ccd(const double* x_old, const double* x_new, long lo
     select_active();
     cudaMemcpyAsync(d_run, h_run, sizeof(SceneRun) * (size_t)nscenes, cudaMemcpyHostToDevice, stream);
     leaf_boxes(d_ev, bvh.act, bvh.n, d_escene, d_scenes, nscenes, d_xo, d_av, 1, d_box, bvh.bbox_enc, stream);
-    bvh_this_step = false;  // the pass hierarchy is replaced
+    bvh_this_step = false;  // the pass hierarchy and pairs are replaced
+    reuse_pairs = false;
     bvh_build(d_box, bvh, stream);
     for (int attempt = 0; attempt < 8; ++attempt) {
         count_launch(), k_reset_pass<<<(nscenes + 255) / 256, 256, 0, stream>>>(d_ctr, d_run, nscenes);
@@ -1312,6 +1351,7 @@ cc_status cc_solver::autotune(double* best_ms) {
     cudaMemcpyAsync(d_run, h_run, sizeof(SceneRun) * (size_t)nscenes, cudaMemcpyHostToDevice, stream);
     leaf_boxes(d_ev, bvh.act, bvh.n, d_escene, d_scenes, nscenes, d_xo, d_av, 1, d_box, bvh.bbox_enc, stream);
     bvh_this_step = false;
+    reuse_pairs = false;
     bvh_build(d_box, bvh, stream);
     if (mode == 1)
         point_boxes(d_xo, d_av, d_vscene, d_scenes, bvh.act ? d_act_p : nullptr, n_act_p, 1, d_pbox_lo, d_pbox_hi,
@@ -1577,6 +1617,9 @@ cc_status cc_set_tuning(cc_solver* s, int knob, int value) {
         case CC_TUNE_TAIL_GRAPH:
             s->tail_graphs_on = value != 0;
             return CC_OK;
+        case CC_TUNE_COMBINED_BROAD:
+            s->combined_broad = value != 0;
+            return CC_OK;
         case CC_TUNE_STRAIN_BLOCK:
             if (value < 32 || value > 256 || value % 32) return CC_BAD_INPUT;
             s->tune.strain_block = value;
@@ -1599,6 +1642,7 @@ int cc_get_tuning(cc_solver* s, int knob) {
         case CC_TUNE_NARROW_BLOCK: return s->tune.narrow_block;
         case CC_TUNE_STRAIN_BLOCK: return s->tune.strain_block;
         case CC_TUNE_TAIL_GRAPH: return s->tail_graphs_on ? 1 : 0;
+        case CC_TUNE_COMBINED_BROAD: return s->combined_broad ? 1 : 0;
         default: return -1;
     }
 }
@@ -1719,6 +1763,7 @@ int cc_debug_candidate_pairs(cc_solver* s, int moving, int brute_force, int* out
     leaf_boxes(s->d_ev, s->bvh.act, s->bvh.n, s->d_escene, s->d_scenes, s->nscenes, s->d_xo, s->d_av, moving,
                s->d_box, s->bvh.bbox_enc, s->stream);
     s->bvh_this_step = false;
+    s->reuse_pairs = false;
     if (!brute_force) bvh_build(s->d_box, s->bvh, s->stream);
     for (int attempt = 0; attempt < 8; ++attempt) {
         count_launch(), k_reset_counters<<<1, 1, 0, s->stream>>>(s->d_ctr);

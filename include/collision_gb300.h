@@ -186,13 +186,19 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
  *                           end is decided on the device, final velocities)
  *                           runs as one captured CUDA graph, replayed every
  *                           step; 0: launched kernel by kernel
+ *   CC_TUNE_COMBINED_BROAD  1 (default): the proximity pass finds its pairs
+ *                           on swept boxes, flagged where the static boxes
+ *                           overlap, and the first CCD pass reuses them when
+ *                           the proximity pass applied no impulse; 0: a
+ *                           broad phase per pass
  * cc_get_tuning returns the current value, or -1 for an unknown knob. */
 enum {
     CC_TUNE_SPLIT_NARROW = 0,
     CC_TUNE_TRAVERSE_BLOCK = 1,
     CC_TUNE_NARROW_BLOCK = 2,
     CC_TUNE_STRAIN_BLOCK = 3,
-    CC_TUNE_TAIL_GRAPH = 4
+    CC_TUNE_TAIL_GRAPH = 4,
+    CC_TUNE_COMBINED_BROAD = 5
 };
 cc_status cc_set_tuning(cc_solver* s, int knob, int value);
 int cc_get_tuning(cc_solver* s, int knob);

@@ -53,13 +53,14 @@ def _split(a, off, i):
     return a[off[i]:off[i + 1]]
 
 
-def _run_batch(solver_cls, mix, nsteps, mode=0, window=True, record=False, split=True, graph=True):
+def _run_batch(solver_cls, mix, nsteps, mode=0, window=True, record=False, split=True, graph=True, combined=True):
     b = solver_cls(0)
     b.assembleBatch(mix)
     b.setMode(mode)
     b.setStrainWindow(window)
     b.setTuning(solver_cls.TUNE_SPLIT_NARROW, int(split))
     b.setTuning(solver_cls.TUNE_TAIL_GRAPH, int(graph))
+    b.setTuning(solver_cls.TUNE_COMBINED_BROAD, int(combined))
     b.setRecording(record)
     pv, pe = b.sceneOffsets()
     x = np.concatenate([s.x for s in mix])
@@ -129,9 +130,12 @@ def test_batch_matches_oracle(solver_cls):
 def test_batch_mixed_and_global_strain_equal_plain(solver_cls):
     mix = _mix()
     ref, _, _ = _run_batch(solver_cls, mix, 8)
-    for mode, window, split, graph in ((1, True, True, True), (1, True, False, True), (0, False, True, True),
-                                       (1, False, True, True), (0, True, True, False), (1, True, True, False)):
-        got, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, window=window, split=split, graph=graph)
+    for mode, window, split, graph, comb in ((1, True, True, True, True), (1, True, False, True, True),
+                                             (0, False, True, True, True), (1, False, True, True, True),
+                                             (0, True, True, False, True), (1, True, True, False, True),
+                                             (0, True, True, True, False), (1, True, True, True, False)):
+        got, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, window=window, split=split, graph=graph,
+                               combined=comb)
         for k, (a, b) in enumerate(zip(ref, got)):
             assert np.array_equal(a["x"], b["x"]), (mode, window, split, k)
             assert np.array_equal(a["v"], b["v"]), (mode, window, split, k)
