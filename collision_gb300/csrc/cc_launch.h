@@ -194,7 +194,12 @@ struct StrainPlan {
     int max_window_slots;  // largest slot count among the scenes that fit
     bool any_global;       // some scene needs more slots than fit
     int block;             // threads per sweep CTA
+    bool warp;             // one warp per scene with staged levels (k_strain_warp)
+    int ecap, lcap, wcap;  // most edges, copy-ins, write-backs of one level (scenes that fit)
+    size_t warp_smem;      // its dynamic shared memory
 };
+// Dynamic shared memory of the one-warp sweep for these sizes.
+size_t strain_warp_smem(int max_slots, int ecap, int lcap, int wcap);
 int strain_window_slot_cap();
 // Once per device before any strain_limit (not a stream operation, so it
 // stays out of captured graphs).

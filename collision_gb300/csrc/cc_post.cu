@@ -514,6 +514,7 @@ __global__ void __launch_bounds__(256) k_strain(const StrainEdgeStep* __restrict
 // test) run. The averaging itself is FP64, as in the reference.
 constexpr int kWindowAhead = 8;
 constexpr size_t kStrainWindowBytes = 200 * 1024;  // dynamic shared memory of one sweep CTA at most
+constexpr size_t kStrainWarpBytes = 200 * 1024;
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
     unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
@@ -725,6 +726,132 @@ __global__ void __launch_bounds__(256) k_strain_window(const StrainEdgeStep* __r
     sweep_done(pass, sc, n_avg, n_exact, flags, passes_out_all);
 }
 
+// The sweep of one scene by a single warp. The block barrier of
+// k_strain_window costs most of a level there; here a level needs only
+// __syncwarp. Each level's edge records and its copy-in and write-back
+// lists are staged into a shared-memory ring kWarpAhead levels ahead with
+// cp.async, and velocities are copied into their slots (the same interval
+// schedule) kWindowAhead levels before their first edge, so a level touches
+// only shared memory. Slots hold the FP64 velocities; the FP32 values of the
+// first decision are converted from them as needed.
+constexpr int kWarpAhead = kWindowAhead;   // the copy-in distance of the schedule
+constexpr int kWarpRing = kWarpAhead + 1;  // level L+K goes where level L-1 was
+
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem));
+}
+
+struct WarpSlot {
+    double2 a, b;  // x y | z -
+};
+
+__global__ void __launch_bounds__(32) k_strain_warp(const StrainEdgeStep* __restrict__ edges,
+                                                    const StrainEdgeHot* __restrict__ hot,
+                                                    const int4* __restrict__ hdr_all,
+                                                    const SceneDev* __restrict__ scenes, int slot_cap,
+                                                    const int2* __restrict__ load_list,
+                                                    const int2* __restrict__ wb_list, double4_32a* av, int pass,
+                                                    int* flags, int* passes_out_all, int max_slots, int ecap,
+                                                    int lcap, int wcap) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int sc = blockIdx.x;
+    const SceneDev& sd = scenes[sc];
+    if (sd.strain_slots > slot_cap || !sd.enabled) return;  // k_strain's, or left out
+    if (!sweep_gate(pass, sc, flags, passes_out_all)) return;
+    WarpSlot* s_win = reinterpret_cast<WarpSlot*>(smem_raw);
+    size_t off = (size_t)max_slots * sizeof(WarpSlot);
+    StrainEdgeHot* s_hot = reinterpret_cast<StrainEdgeHot*>(smem_raw + off);
+    off += (size_t)kWarpRing * ecap * sizeof(StrainEdgeHot);
+    int2* s_ld = reinterpret_cast<int2*>(smem_raw + off);
+    off += (size_t)kWarpRing * lcap * 8;
+    int2* s_wb = reinterpret_cast<int2*>(smem_raw + off);
+    off += (size_t)kWarpRing * wcap * 8;
+    off = (off + 15) & ~(size_t)15;  // the headers are int4
+    int4* s_h = reinterpret_cast<int4*>(smem_raw + off);
+    const int lane = threadIdx.x;
+    const int4* hdr = hdr_all + 2 * sd.strain_hdr0;
+    const int nlevels = sd.strain_levels;
+    const double dt = sd.p.dt;
+    const float dt32 = __double2float_ru(dt);
+    // level L's records and lists into ring slot L % kWarpRing
+    auto stage = [&](int L) {
+        if (L >= nlevels) return;
+        const int r = L % kWarpRing;
+        const int4 h0 = hdr[2 * L], h1 = hdr[2 * L + 1];
+        if (lane == 0) {
+            s_h[2 * r] = h0;
+            s_h[2 * r + 1] = h1;
+        }
+        const float4* src = reinterpret_cast<const float4*>(hot + h0.x);
+        float4* dst = reinterpret_cast<float4*>(s_hot + (size_t)r * ecap);
+        const int nchunk = 3 * (h0.y - h0.x);  // 48-byte records, three 16-byte chunks each
+        for (int c = lane; c < nchunk; c += 32) cp_async16(dst + c, src + c);
+        for (int c = lane; c < h0.w - h0.z; c += 32) cp_async8(s_ld + (size_t)r * lcap + c, load_list + h0.z + c);
+        for (int c = lane; c < h1.y - h1.x; c += 32) cp_async8(s_wb + (size_t)r * wcap + c, wb_list + h1.x + c);
+    };
+    for (int L = 0; L < kWarpAhead; ++L) {
+        stage(L);
+        asm volatile("cp.async.commit_group;\n" ::);
+    }
+    int n_avg = 0, n_exact = 0;
+    for (int L = 0; L < nlevels; ++L) {
+        // level L's stage: the (L+1)-th group committed
+        if (L < kWarpAhead)
+            asm volatile("cp.async.wait_group 0;\n" ::);
+        else
+            asm volatile("cp.async.wait_group %0;\n" ::"n"(kWarpAhead - 1));
+        __syncwarp();
+        const int r = L % kWarpRing;
+        const int4 h0 = s_h[2 * r], h1 = s_h[2 * r + 1];
+        // velocities whose slots open now (first used kWindowAhead levels on)
+        for (int c = lane; c < h0.w - h0.z; c += 32) {
+            const int2 ps = s_ld[(size_t)r * lcap + c];
+            cp_async16(&s_win[ps.y].a, &av[ps.x]);
+            cp_async16(&s_win[ps.y].b, reinterpret_cast<const double2*>(&av[ps.x]) + 1);
+        }
+        stage(L + kWarpAhead);
+        asm volatile("cp.async.commit_group;\n" ::);
+        if (L < kWarpAhead) asm volatile("cp.async.wait_group 0;\n" ::);  // first levels use them at once
+        __syncwarp();
+        // write back the points last used at the previous level
+        for (int c = lane; c < h1.y - h1.x; c += 32) {
+            const int2 ps = s_wb[(size_t)r * wcap + c];
+            const double2 a = s_win[ps.y].a, b = s_win[ps.y].b;
+            av[ps.x] = make_double4_32a(a.x, a.y, b.x, 0.0);
+        }
+        for (int i = lane; i < h0.y - h0.x; i += 32) {
+            const StrainEdgeHot h = s_hot[(size_t)r * ecap + i];
+            WarpSlot& w0 = s_win[h.s0];
+            WarpSlot& w1 = s_win[h.s1];
+            const double2 a0 = w0.a, a1 = w0.b, b0 = w1.a, b1 = w1.b;
+            int q = strain_decide32(h, make_float4((float)a0.x, (float)a0.y, (float)a1.x, 0.f),
+                                    make_float4((float)b0.x, (float)b0.y, (float)b1.x, 0.f), dt32);
+            if (q == 0) continue;
+            double v0[3] = {a0.x, a0.y, a1.x}, v1[3] = {b0.x, b0.y, b1.x};
+            if (q < 0 && !strain_flag_vals(edges[h0.x + i], v0, v1, dt, &n_exact)) continue;
+            ++n_avg;
+            double t[3];
+            for (int k = 0; k < 3; ++k) {
+                t[k] = v0[k] + v1[k];
+                t[k] = 0.5 * t[k];
+            }
+            const double2 na = make_double2(t[0], t[1]), nb = make_double2(t[2], 0.0);
+            w0.a = na; w0.b = nb;
+            w1.a = na; w1.b = nb;
+        }
+        __syncwarp();
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::);
+    __syncwarp();
+    for (int i = sd.wb_final0 + lane; i < sd.wb_final1; i += 32) {
+        const int2 ps = wb_list[i];
+        const double2 a = s_win[ps.y].a, b = s_win[ps.y].b;
+        av[ps.x] = make_double4_32a(a.x, a.y, b.x, 0.0);
+    }
+    sweep_done(pass, sc, n_avg, n_exact, flags, passes_out_all);
+}
+
 // Would any edge of the chunk average on the current velocities? (One
 // block per chunk of at most 256 edges of one scene.) If none of a scene's
 // edges would, its sweep changes nothing: before the first edge that
@@ -780,6 +907,12 @@ __global__ void k_math_selftest(int fn, const double* a, const double* b, double
 
 }  // namespace
 
+size_t strain_warp_smem(int max_slots, int ecap, int lcap, int wcap) {
+    size_t b = (size_t)max_slots * sizeof(WarpSlot) +
+               (size_t)kWarpRing * ((size_t)ecap * sizeof(StrainEdgeHot) + (size_t)lcap * 8 + (size_t)wcap * 8);
+    return ((b + 15) & ~(size_t)15) + (size_t)kWarpRing * 32;
+}
+
 void math_selftest(int fn, const double* a, const double* b, double* out, int n, cudaStream_t s) {
     if (n > 0) count_launch(), k_math_selftest<<<nblk(n, 128), 128, 0, s>>>(fn, a, b, out, n);
 }
@@ -830,6 +963,7 @@ int strain_window_slot_cap() { return (int)(kStrainWindowBytes / sizeof(WinSlot)
 
 void strain_configure() {
     cudaFuncSetAttribute(k_strain_window, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStrainWindowBytes);
+    cudaFuncSetAttribute(k_strain_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStrainWarpBytes);
 }
 
 void strain_limit(const StrainEdge* edges, int nedges, const int4* hdr, const int2* load_list, const int2* wb_list,
@@ -847,7 +981,11 @@ void strain_limit(const StrainEdge* edges, int nedges, const int4* hdr, const in
     size_t smem = (size_t)plan.max_window_slots * sizeof(WinSlot);
     for (int pass = 0; pass < kStrainMaxIter; ++pass) {
         if (nchunks > 0) count_launch(), k_strain_check<<<nchunks, 256, 0, s>>>(se, hot, chunks, scenes, av, flags);
-        if (plan.window)
+        if (plan.window && plan.warp)
+            count_launch(), k_strain_warp<<<nscenes, 32, plan.warp_smem, s>>>(
+                se, hot, hdr, scenes, cap, load_list, wb_list, av, pass, flags, passes_out, plan.max_window_slots,
+                plan.ecap, plan.lcap, plan.wcap);
+        else if (plan.window)
             count_launch(), k_strain_window<<<nscenes, plan.block, smem, s>>>(se, hot, hdr, scenes, cap, load_list,
                                                                               wb_list, av, pass, flags, passes_out);
         if (!plan.window || plan.any_global)

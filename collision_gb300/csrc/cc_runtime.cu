@@ -109,6 +109,7 @@ struct SceneHost {
     RefTreeOrder tree[2];
     double volume = 0.0;  // shared by both trees (dcollid.cpp:381, 422)
     int strain_edges = 0, strain_points = 0;
+    int strain_caps[3] = {0, 0, 0};
     bool enabled = true;
     int status = CC_OK;  // of the last resolve call
     int state = kHsDone;
@@ -128,7 +129,8 @@ struct SceneHost {
 // a slot for its live interval - from kAhead levels before its first edge to
 // the level after its last one - by interval colouring.
 void append_strain_schedule(const std::vector<StrainEdge>& edges, int v0, int nv, std::vector<StrainEdge>& all_edges,
-                            std::vector<int4>& hdr, std::vector<int2>& load, std::vector<int2>& wb, SceneDev& sd) {
+                            std::vector<int4>& hdr, std::vector<int2>& load, std::vector<int2>& wb, SceneDev& sd,
+                            int caps[3]) {
     const int kAhead = 8;  // kWindowAhead in cc_post.cu
     const int m = (int)edges.size();
     std::vector<int> lvl((size_t)m), last((size_t)nv, 0);
@@ -201,6 +203,12 @@ void append_strain_schedule(const std::vector<StrainEdge>& edges, int v0, int nv
     sd.strain_hdr0 = (int)(hdr.size() / 2);
     sd.strain_levels = nlevels;
     sd.strain_slots = nslots;
+    caps[0] = caps[1] = caps[2] = 0;  // most edges, copy-ins, write-backs of one level
+    for (int l = 0; l < nlevels; ++l) {
+        caps[0] = std::max(caps[0], level_off[l + 1] - level_off[l]);
+        caps[1] = std::max(caps[1], load_off[l + 1] - load_off[l]);
+        caps[2] = std::max(caps[2], wb_off[l + 1] - wb_off[l]);
+    }
     for (int l = 0; l < nlevels; ++l) {
         hdr.push_back(int4{ebase + level_off[l], ebase + level_off[l + 1], lbase + load_off[l], lbase + load_off[l + 1]});
         hdr.push_back(int4{wbase + wb_off[l], wbase + wb_off[l + 1], 0, 0});
@@ -334,6 +342,7 @@ struct cc_solver {
     int mode = 0;  // 0 plain FP64, 1 mixed precision
     bool strain_window = true;
     bool split_narrow = true;  // two-stage narrow phase for mixed passes
+    bool strain_warp = false;  // one-warp strain sweep with staged levels
     LaunchTuning tune;
     int host_threads = 0;  // tree emulation threads (0: hardware concurrency)
 
@@ -553,7 +562,7 @@ struct cc_solver {
     // strain settings, then replayed.
     struct TailGraph {
         const void* key[4];
-        int block, window;
+        int block, window, warp;
         cudaGraphExec_t exec;
         long long launches;
     };
@@ -567,7 +576,8 @@ struct cc_solver {
         const void* key[4] = {x_cand, x_out, vel, hc};
         TailGraph* hit = nullptr;
         for (auto& g : tail_graphs)
-            if (std::equal(key, key + 4, g.key) && g.block == tune.strain_block && g.window == (int)strain_window) {
+            if (std::equal(key, key + 4, g.key) && g.block == tune.strain_block && g.window == (int)strain_window &&
+                g.warp == (int)strain_warp) {
                 hit = &g;
                 break;
             }
@@ -590,6 +600,7 @@ struct cc_solver {
             std::copy(key, key + 4, tg.key);
             tg.block = tune.strain_block;
             tg.window = (int)strain_window;
+            tg.warp = (int)strain_warp;
             tg.launches = n;
             e = cudaGraphInstantiate(&tg.exec, g, 0);
             cudaGraphDestroy(g);
@@ -651,14 +662,21 @@ struct cc_solver {
     }
 
     StrainPlan strain_plan() const {
-        StrainPlan pl{strain_window, 0, false, tune.strain_block};
+        StrainPlan pl{strain_window, 0, false, tune.strain_block, false, 0, 0, 0, 0};
         int cap = strain_window_slot_cap();
-        for (const SceneDev& sd : h_scenes) {
-            if (strain_window && sd.strain_slots <= cap)
+        for (int s = 0; s < nscenes; ++s) {
+            const SceneDev& sd = h_scenes[s];
+            if (strain_window && sd.strain_slots <= cap) {
                 pl.max_window_slots = std::max(pl.max_window_slots, sd.strain_slots);
-            else
+                pl.ecap = std::max(pl.ecap, scenes[s].strain_caps[0]);
+                pl.lcap = std::max(pl.lcap, scenes[s].strain_caps[1]);
+                pl.wcap = std::max(pl.wcap, scenes[s].strain_caps[2]);
+            } else {
                 pl.any_global = true;
+            }
         }
+        pl.warp_smem = strain_warp_smem(pl.max_window_slots, pl.ecap, pl.lcap, pl.wcap);
+        pl.warp = strain_window && strain_warp && pl.warp_smem <= 200 * 1024;
         return pl;
     }
     void set_scene_params(int i, const cc_params& p) {
@@ -776,7 +794,7 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
         sd.strain_e0 = (int)all_edges.size();
         sd.strain_ne = (int)edges.size();
         for (int c = 0; c < sd.strain_ne; c += 256) chunks.push_back(int2{si, sd.strain_e0 + c});
-        append_strain_schedule(edges, v0, snv, all_edges, hdr, load, wb, sd);
+        append_strain_schedule(edges, v0, snv, all_edges, hdr, load, wb, sd, sh.strain_caps);
         sh.strain_edges = (int)edges.size();
         sh.strain_points = (int)(load.size() - nload);
         v0 += snv;
@@ -1620,6 +1638,9 @@ cc_status cc_set_tuning(cc_solver* s, int knob, int value) {
         case CC_TUNE_COMBINED_BROAD:
             s->combined_broad = value != 0;
             return CC_OK;
+        case CC_TUNE_STRAIN_WARP:
+            s->strain_warp = value != 0;
+            return CC_OK;
         case CC_TUNE_STRAIN_BLOCK:
             if (value < 32 || value > 256 || value % 32) return CC_BAD_INPUT;
             s->tune.strain_block = value;
@@ -1643,6 +1664,7 @@ int cc_get_tuning(cc_solver* s, int knob) {
         case CC_TUNE_STRAIN_BLOCK: return s->tune.strain_block;
         case CC_TUNE_TAIL_GRAPH: return s->tail_graphs_on ? 1 : 0;
         case CC_TUNE_COMBINED_BROAD: return s->combined_broad ? 1 : 0;
+        case CC_TUNE_STRAIN_WARP: return s->strain_warp ? 1 : 0;
         default: return -1;
     }
 }

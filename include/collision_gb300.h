@@ -191,6 +191,11 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
  *                           overlap, and the first CCD pass reuses them when
  *                           the proximity pass applied no impulse; 0: a
  *                           broad phase per pass
+ *   CC_TUNE_STRAIN_WARP     1: each scene's strain sweep runs on one warp
+ *                           with its levels staged in shared memory;
+ *                           0 (default): on a CTA of CC_TUNE_STRAIN_BLOCK
+ *                           threads. Same results; the CTA sweep is faster
+ *                           for sheets whose levels hold more than ~32 edges
  * cc_get_tuning returns the current value, or -1 for an unknown knob. */
 enum {
     CC_TUNE_SPLIT_NARROW = 0,
@@ -198,7 +203,8 @@ enum {
     CC_TUNE_NARROW_BLOCK = 2,
     CC_TUNE_STRAIN_BLOCK = 3,
     CC_TUNE_TAIL_GRAPH = 4,
-    CC_TUNE_COMBINED_BROAD = 5
+    CC_TUNE_COMBINED_BROAD = 5,
+    CC_TUNE_STRAIN_WARP = 6
 };
 cc_status cc_set_tuning(cc_solver* s, int knob, int value);
 int cc_get_tuning(cc_solver* s, int knob);

@@ -53,7 +53,8 @@ def _split(a, off, i):
     return a[off[i]:off[i + 1]]
 
 
-def _run_batch(solver_cls, mix, nsteps, mode=0, window=True, record=False, split=True, graph=True, combined=True):
+def _run_batch(solver_cls, mix, nsteps, mode=0, window=True, record=False, split=True, graph=True, combined=True,
+               warp=False):
     b = solver_cls(0)
     b.assembleBatch(mix)
     b.setMode(mode)
@@ -61,6 +62,7 @@ def _run_batch(solver_cls, mix, nsteps, mode=0, window=True, record=False, split
     b.setTuning(solver_cls.TUNE_SPLIT_NARROW, int(split))
     b.setTuning(solver_cls.TUNE_TAIL_GRAPH, int(graph))
     b.setTuning(solver_cls.TUNE_COMBINED_BROAD, int(combined))
+    b.setTuning(solver_cls.TUNE_STRAIN_WARP, int(warp))
     b.setRecording(record)
     pv, pe = b.sceneOffsets()
     x = np.concatenate([s.x for s in mix])
@@ -136,11 +138,19 @@ def test_batch_mixed_and_global_strain_equal_plain(solver_cls):
                                              (0, True, True, True, False), (1, True, True, True, False)):
         got, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, window=window, split=split, graph=graph,
                                combined=comb)
-        for k, (a, b) in enumerate(zip(ref, got)):
-            assert np.array_equal(a["x"], b["x"]), (mode, window, split, k)
-            assert np.array_equal(a["v"], b["v"]), (mode, window, split, k)
-            assert np.array_equal(a["hc"], b["hc"]), (mode, window, split, k)
-            assert np.array_equal(a["hcol"], b["hcol"]), (mode, window, split, k)
+        _compare(ref, got, (mode, window, split, graph, comb))
+    # the one-warp staged sweep instead of the CTA-per-scene one
+    for mode in (0, 1):
+        got, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, warp=True)
+        _compare(ref, got, ("warp sweep", mode))
+
+
+def _compare(ref, got, tag):
+    for k, (a, b) in enumerate(zip(ref, got)):
+        assert np.array_equal(a["x"], b["x"]), (tag, k)
+        assert np.array_equal(a["v"], b["v"]), (tag, k)
+        assert np.array_equal(a["hc"], b["hc"]), (tag, k)
+        assert np.array_equal(a["hcol"], b["hcol"]), (tag, k)
 
 
 def test_batch_per_scene_params(solver_cls):
