@@ -18,7 +18,9 @@ Every array is in the layout the solver's C ABI takes: positions and
 velocities (V,3) float64 point-major, triangles (T,3) int32 with a surface id
 per triangle (contiguous runs), bonds (B,2) int32 with a curve id per bond
 (contiguous runs), rest lengths = initial edge lengths (the reference's
-side_length0 / length0, dcollid.cpp:513-516), fixed flags (V,) uint8.
+side_length0 / length0, dcollid.cpp:513-516), point flags (V,) uint8 (1 fixed,
+2 movable rigid body), and per movable surface its mass, centre of mass and
+centre-of-mass velocity.
 """
 from __future__ import annotations
 
@@ -38,7 +40,7 @@ class Scene:
     name: str
     x: np.ndarray          # (V,3) float64 positions at the start of the step
     v: np.ndarray          # (V,3) float64 velocities
-    fixed: np.ndarray      # (V,) uint8, 1 = fixed obstacle point
+    fixed: np.ndarray      # (V,) uint8: 1 fixed obstacle point, 2 movable rigid body
     tris: np.ndarray       # (T,3) int32
     tri_surf: np.ndarray   # (T,) int32
     tri_rest: np.ndarray   # (T,3) float64
@@ -47,6 +49,8 @@ class Scene:
     bond_rest: np.ndarray  # (B,) float64
     domain: np.ndarray     # (6,) float64: lo xyz, hi xyz
     params: dict
+    # movable rigid bodies: surface id -> dict(mass, com (3,), comv (3,))
+    bodies: dict = dataclasses.field(default_factory=dict)
 
     @property
     def nv(self) -> int:
@@ -70,7 +74,8 @@ class Scene:
     def copy(self) -> "Scene":
         return dataclasses.replace(
             self, **{f.name: (getattr(self, f.name).copy() if isinstance(getattr(self, f.name), np.ndarray)
-                              else dict(getattr(self, f.name)) if isinstance(getattr(self, f.name), dict)
+                              else {k: (dict(v) if isinstance(v, dict) else v) for k, v in getattr(self, f.name).items()}
+              if isinstance(getattr(self, f.name), dict)
                               else getattr(self, f.name))
                      for f in dataclasses.fields(self)})
 
@@ -139,6 +144,39 @@ def box_mesh(lo, hi):
     return pts, np.array(tris, dtype=np.int32)
 
 
+def cuboid_mesh(center, edges, spacing):
+    """Closed box surface, each face a grid of squares about `spacing` wide,
+    split along one diagonal; outward-facing triangles."""
+    c = np.asarray(center, dtype=np.float64)
+    e = np.asarray(edges, dtype=np.float64)
+    n = [max(1, int(round(e[d] / spacing))) for d in range(3)]
+    key = {}
+    pts = []
+
+    def pid(i, j, k):
+        t = (i, j, k)
+        if t not in key:
+            key[t] = len(pts)
+            pts.append(c - 0.5 * e + e * np.array([i / n[0], j / n[1], k / n[2]]))
+        return key[t]
+
+    tris = []
+    for d in range(3):
+        u, w = (d + 1) % 3, (d + 2) % 3
+        for side in (0, n[d]):
+            for a in range(n[u]):
+                for b in range(n[w]):
+                    q = []
+                    for da, db in ((0, 0), (1, 0), (1, 1), (0, 1)):
+                        idx = [0, 0, 0]
+                        idx[d], idx[u], idx[w] = side, a + da, b + db
+                        q.append(pid(*idx))
+                    if side == 0:
+                        q = q[::-1]
+                    tris += [(q[0], q[1], q[2]), (q[0], q[2], q[3])]
+    return np.array(pts), np.array(tris, dtype=np.int32)
+
+
 def _edge_rest(x, tris):
     p0, p1, p2 = x[tris[:, 0]], x[tris[:, 1]], x[tris[:, 2]]
     return np.stack([np.linalg.norm(p0 - p1, axis=1),
@@ -146,15 +184,21 @@ def _edge_rest(x, tris):
                      np.linalg.norm(p2 - p0, axis=1)], axis=1)
 
 
-def assemble(name, parts, params, bonds=None, bond_curve=None, domain_scale=10.0):
-    """parts: list of (points, tris, vel (V,3), fixed_flag). Each part with
-    triangles becomes one surface, in order."""
+def assemble(name, parts, params, bonds=None, bond_curve=None, domain_scale=10.0, masses=None, domain=None):
+    """parts: list of (points, tris, vel (V,3), flag) with flag False/0 free,
+    True/1 fixed, 2 a movable rigid body (mass from `masses[part]`, default
+    1). Each part with triangles becomes one surface, in order."""
     xs, vs, fx, ts, ss = [], [], [], [], []
+    bodies = {}
     off = 0
     for sid, (p, t, v, fixed) in enumerate(parts):
         xs.append(p)
         vs.append(v)
-        fx.append(np.full(len(p), 1 if fixed else 0, dtype=np.uint8))
+        fx.append(np.full(len(p), int(fixed), dtype=np.uint8))
+        if int(fixed) == 2:
+            bodies[sid] = dict(mass=float((masses or {}).get(sid, 1.0)),
+                               com=np.asarray(p, dtype=np.float64).mean(axis=0),
+                               comv=np.asarray(v, dtype=np.float64).mean(axis=0))
         if t is not None and len(t):
             ts.append(t + off)
             ss.append(np.full(len(t), sid, dtype=np.int32))
@@ -172,13 +216,14 @@ def assemble(name, parts, params, bonds=None, bond_curve=None, domain_scale=10.0
     tri_rest = _edge_rest(x, tris) if len(tris) else np.zeros((0, 3))
     bond_rest = (np.linalg.norm(x[bonds[:, 0]] - x[bonds[:, 1]], axis=1)
                  if len(bonds) else np.zeros(0))
-    lo, hi = x.min(axis=0), x.max(axis=0)
-    c, half = 0.5 * (lo + hi), 0.5 * (hi - lo) + 1e-3
-    domain = np.concatenate([c - domain_scale * half, c + domain_scale * half])
+    if domain is None:
+        lo, hi = x.min(axis=0), x.max(axis=0)
+        c, half = 0.5 * (lo + hi), 0.5 * (hi - lo) + 1e-3
+        domain = np.concatenate([c - domain_scale * half, c + domain_scale * half])
     p = dict(DEFAULTS)
     p.update(params)
     return Scene(name, x, v, fixed, tris, tri_surf, tri_rest.astype(np.float64), bonds,
-                 bond_curve, bond_rest.astype(np.float64), domain.astype(np.float64), p)
+                 bond_curve, bond_rest.astype(np.float64), np.asarray(domain, dtype=np.float64), p, bodies)
 
 
 # ------------------------------------------------------------------ workloads
@@ -297,6 +342,77 @@ def large(n=1025, sub=5, radius=0.3, speed=10.0, dt=1e-3, h=2e-4, seed=0):
     return assemble(f"large_{n}", [(cp, ct, cv, False), (sp, st, np.zeros_like(sp), True),
                                    (bp, bt, np.zeros_like(bp), True)],
                     dict(dt=dt, thickness=h, lam=DEFAULTS["lam"]))
+
+
+# ------------------------------------------------------ the reference's decks
+# in-ball_ball, in-ball_plane, in-box_boundary, in-string_box, in-string_slide
+# and in-string_string (cdinit.cpp reads them): spheres (centre, radii,
+# velocity), cuboids (centre, half edges, velocity) and strings (end points,
+# velocity; cdinit.cpp:145-170 splits a string into bonds of about a quarter
+# grid cell) on a 50^3 grid over the deck's domain. MOVABLE_BODY_BOUNDARY
+# surfaces become movable rigid bodies of mass 1; FIRST_PHYSICS_WAVE_TYPE
+# ones are free cloth. FronTier's surface builders are not available, so
+# spheres are icospheres and cuboids are closed grids of about one cell.
+# `advance` moves every part along its velocity by that many seconds first,
+# so that a short run reaches contact.
+
+_DECKS = {
+    "ball_ball": dict(domain=(0, 0, 0, 0.5, 0.5, 0.5), parts=[
+        ("sphere", (0.3, 0.3, 0.3), 0.05, (-0.2, -0.2, -0.2), 0),
+        ("sphere", (0.2, 0.2, 0.2), 0.05, (0.2, 0.2, 0.2), 0)]),
+    "ball_plane": dict(domain=(0, 0, 0.25, 0.5, 0.5, 0.75), parts=[
+        ("sphere", (0.25, 0.25, 0.4), 0.05, (0.0, 0.0, 0.2), 2),
+        ("cuboid", (0.25, 0.25, 0.47), (0.15, 0.15, 0.01), (0.0, 0.0, -0.2), 0)]),
+    "box_boundary": dict(domain=(0, 0, 0, 1.0, 0.5, 0.5), parts=[
+        ("cuboid", (0.25, 0.25, 0.21), (0.1, 0.1, 0.2), (0.4, 0.0, -0.4), 2)]),
+    "string_box": dict(domain=(0, 0, 0, 0.5, 0.5, 0.5), parts=[
+        ("cuboid", (0.25, 0.25, 0.3), (0.15, 0.15, 0.03), (0.0, 0.0, -0.2), 0),
+        ("string", (0.25, 0.01, 0.25), (0.25, 0.49, 0.25), (0.0, 0.0, 0.0), 0)]),
+    "string_slide": dict(domain=(0, 0, 0, 0.5, 0.5, 0.5), parts=[
+        ("cuboid", (0.25, 0.25, 0.13), (0.2, 0.2, 0.02), (0.0, 0.0, 0.0), 2),
+        ("string", (0.25, 0.1, 0.3), (0.25, 0.25, 0.155), (0.0, 0.1, -0.1), 0)]),
+    "string_string": dict(domain=(0, 0, 0, 0.5, 0.5, 0.5), parts=[
+        ("string", (0.25, 0.01, 0.24), (0.25, 0.49, 0.24), (0.0, 0.0, 0.2), 0),
+        ("string", (0.01, 0.25, 0.25), (0.49, 0.25, 0.25), (0.0, 0.0, -0.2), 0)]),
+}
+
+
+def deck(name: str, advance: float = 0.0, dt: float = 1e-3, h: float = 1e-3, sub: int = 3, mu: float = 0.0,
+         cells: int = 50) -> Scene:
+    """One of the reference's decks as a mesh scene (see above)."""
+    spec = _DECKS[name]
+    dom = np.asarray(spec["domain"], dtype=np.float64)
+    cell = float(dom[3] - dom[0]) / cells
+    parts, strings = [], []
+    for kind, a, b, vel, flag in spec["parts"]:
+        vel = np.asarray(vel, dtype=np.float64)
+        if kind == "sphere":
+            p, t = icosphere(sub, b, center=a)
+        elif kind == "cuboid":
+            p, t = cuboid_mesh(a, 2.0 * np.asarray(b), cell)
+        else:
+            e0, e1 = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+            nb = max(1, int(np.linalg.norm(e1 - e0) / (0.25 * cell)))
+            p = e0 + np.linspace(0.0, 1.0, nb + 1)[:, None] * (e1 - e0)
+            t = None
+        p = np.asarray(p, dtype=np.float64) + advance * vel
+        v = np.tile(vel, (len(p), 1))
+        if t is None:
+            strings.append(len(parts))
+        parts.append((p, t, v, flag))
+    # strings after every surface, as assembleFromInterface lists them
+    order = [i for i in range(len(parts)) if i not in strings] + strings
+    parts = [parts[i] for i in order]
+    bonds, curve, off = [], [], 0
+    for ci, (p, t, v, flag) in enumerate(parts):
+        if t is None:
+            n = len(p) - 1
+            bonds.append(np.stack([np.arange(n), np.arange(1, n + 1)], axis=1) + off)
+            curve.append(np.full(n, ci, dtype=np.int32))
+        off += len(p)
+    b = np.concatenate(bonds) if bonds else None
+    c = np.concatenate(curve) if curve else None
+    return assemble(f"deck_{name}", parts, dict(dt=dt, thickness=h, lam=mu), bonds=b, bond_curve=c, domain=dom)
 
 
 def workload(name: str, seed: int = 0):

@@ -18,8 +18,14 @@
  * CCO_ITER_CAP after a configurable cap, and fatal errors return a status
  * instead of exiting (clean_up(ERROR)).
  *
- * Out of scope, as for the GPU library: movable rigid bodies (every
- * is_movableRG branch), the 2D solver, debug printing.
+ * Movable rigid bodies follow the reference's is_movableRG branches: each
+ * surface whose first point is movable is one impact zone from the start of
+ * a step (createImpZoneForRG, dcollid3d.cpp:54-68), impulses between rigid
+ * points spread over that zone (SpreadImpactZoneImpulse, dcollid.cpp:
+ * 1101-1115), the zone moves rigidly after every pass
+ * (updateImpactZoneVelocityForRG, dcollid.cpp:267-288), and its centre of
+ * mass is advanced at the end (updateFinalForRG, dcollid.cpp:626-675). Out
+ * of scope, as for the GPU library: the 2D solver, debug printing.
  */
 #include "cc_oracle.h"
 
@@ -71,8 +77,18 @@ struct cco_solver {
     int* enp;     /* points per element */
     int* esurf;   /* surface id (tris), -1 for bonds */
     double* erest;/* ne*3 rest lengths (side_length0 / length0) */
-    unsigned char* fixed;
+    unsigned char* fixed; /* bit 0 is_fixed, bit 1 is_movableRG */
     unsigned char* in_elem;
+
+    /* surfaces in element order, each with its HYPER_SURF body data */
+    int nsurf;
+    int *surf_id, *surf_t0, *surf_t1;
+    int* vsurf;           /* surface of each point (pt->hs), -1 for none */
+    double *surf_mass, *surf_com, *surf_comv;
+    double* mrg_com;      /* CollisionSolver::mrg_com, collid.h:174 */
+    unsigned char* mrg_set;
+    double* imp_rg;       /* collsnImpulse_RG: the solver never clears it */
+    int* num_rg;          /* collsn_num_RG */
 
     /* per-point state (STATE, collid.h:20-39) */
     double *coords, *x_old, *vel, *avg, *imp, *fric;
@@ -129,10 +145,14 @@ static inline double smax(double a, double b) { return (a < b) ? b : a; }
 #define CO(p) (s->coords + 3 * (p))
 #define AV(p) (s->avg + 3 * (p))
 
-static inline int is_static(const cco_solver* s, int p) { return s->fixed[p] != 0; }
+static inline int is_static(const cco_solver* s, int p) { return (s->fixed[p] & 1) != 0; }
+static inline int is_movable(const cco_solver* s, int p) { return (s->fixed[p] & 2) != 0; }
+static inline int is_rigid(const cco_solver* s, int p) { return s->fixed[p] != 0; }
+/* isRigidBody(hse), dcollid.cpp:1097-1099: a point of the element is fixed
+ * or movable */
 static int elem_rigid(const cco_solver* s, int e) {
     for (int i = 0; i < s->enp[e]; ++i)
-        if (is_static(s, s->ev[3 * e + i])) return 1;
+        if (is_rigid(s, s->ev[3 * e + i])) return 1;
     return 0;
 }
 
@@ -188,13 +208,29 @@ static void merge_point(cco_solver* s, int x, int y) {
     }
 }
 
-static void create_imp_zone(cco_solver* s, const int* pts, int num) {
+/* createImpZone(pts, num, first): with first = NO, pairs with a movable
+ * point are left apart */
+static void create_imp_zone(cco_solver* s, const int* pts, int num, int first) {
     for (int i = 0; i < num; ++i)
-        for (int j = 0; j < i; ++j) merge_point(s, pts[i], pts[j]);
+        for (int j = 0; j < i; ++j) {
+            if (!first && (is_movable(s, pts[i]) || is_movable(s, pts[j]))) continue;
+            merge_point(s, pts[i], pts[j]);
+        }
 }
 
+/* SpreadImpactZoneImpulse, dcollid.cpp:1101-1115: every member of p's zone */
+static void spread_impact_zone_impulse(cco_solver* s, int p, double impulse, const double* nor) {
+    for (int q = find_set(s, p); q >= 0; q = s->uf_next[q]) {
+        for (int i = 0; i < 3; ++i) s->imp_rg[3 * q + i] += impulse * nor[i];
+        s->num_rg[q] += 1;
+    }
+}
+
+/* total_mass(p->hs) */
+static double body_mass(const cco_solver* s, int p) { return s->vsurf[p] >= 0 ? s->surf_mass[s->vsurf[p]] : 0.0; }
+
 /* -------------------------------------------------------------- impulses */
-/* PointToTriImpulse, dcollid3d.cpp:925-1107 (non-movable branches). */
+/* PointToTriImpulse, dcollid3d.cpp:925-1107. */
 static void point_to_tri_impulse(cco_solver* s, const int* pts, const double* nor, double* w, double dist) {
     double v_rel[3] = {0.0, 0.0, 0.0}, vn, vt;
     double impulse = 0.0, m_impulse, sum_w = 0.0;
@@ -215,6 +251,17 @@ static void point_to_tri_impulse(cco_solver* s, const int* pts, const double* no
             impulse = vn;
             rigid_impulse[0] = vn;
             rigid_impulse[1] = vn;
+        } else if (is_movable(s, pts[0]) && is_movable(s, pts[1]) && is_movable(s, pts[2]) &&
+                   is_movable(s, pts[3])) {
+            double m1 = body_mass(s, pts[0]), m2 = body_mass(s, pts[3]);
+            rigid_impulse[0] = vn * m2 / (m1 + m2);
+            rigid_impulse[1] = vn * m1 / (m1 + m2);
+        } else if (is_movable(s, pts[0]) && is_movable(s, pts[1]) && is_movable(s, pts[2])) {
+            rigid_impulse[0] = 0.5 * vn;
+            impulse = 0.5 * vn;
+        } else if (is_movable(s, pts[3])) {
+            impulse = 0.5 * vn;
+            rigid_impulse[1] = 0.5 * vn;
         } else {
             impulse = vn * 0.5;
         }
@@ -227,7 +274,7 @@ static void point_to_tri_impulse(cco_solver* s, const int* pts, const double* no
             for (int i = 0; i < 3; ++i) w[i] = inv * w[i];
         }
     }
-    int all_rigid = is_static(s, pts[0]) && is_static(s, pts[1]) && is_static(s, pts[2]) && is_static(s, pts[3]);
+    int all_rigid = is_rigid(s, pts[0]) && is_rigid(s, pts[1]) && is_rigid(s, pts[2]) && is_rigid(s, pts[3]);
     if (vn * dt < 0.1 * dist) {
         if (all_rigid) {
             rigid_impulse[0] *= 1.0 + cr;
@@ -243,11 +290,16 @@ static void point_to_tri_impulse(cco_solver* s, const int* pts, const double* no
         m_impulse = impulse;
     else
         m_impulse = 2.0 * impulse / (1.0 + dot3(w, w));
-    if (all_rigid) return;
+    if (all_rigid) {
+        if (is_movable(s, pts[0])) spread_impact_zone_impulse(s, pts[0], rigid_impulse[0], nor);
+        if (is_movable(s, pts[3])) spread_impact_zone_impulse(s, pts[3], -1.0 * rigid_impulse[1], nor);
+        return;
+    }
     for (int i = 0; i < 3; ++i) {
         int p = pts[i];
         if (is_static(s, p)) continue;
         double t_impulse = m_impulse;
+        if (is_movable(s, p)) t_impulse = rigid_impulse[0];
         for (int j = 0; j < 3; ++j) {
             s->imp[3 * p + j] += w[i] * t_impulse * nor[j];
             if (fabs(vt) > ROUND_EPS)
@@ -258,6 +310,7 @@ static void point_to_tri_impulse(cco_solver* s, const int* pts, const double* no
     if (!is_static(s, pts[3])) {
         int p = pts[3];
         double t_impulse = m_impulse;
+        if (is_movable(s, p)) t_impulse = rigid_impulse[1];
         for (int j = 0; j < 3; ++j) {
             s->imp[3 * p + j] -= t_impulse * nor[j];
             if (fabs(vt) > ROUND_EPS)
@@ -270,7 +323,7 @@ static void point_to_tri_impulse(cco_solver* s, const int* pts, const double* no
             if (!isfinite(s->imp[3 * pts[j] + i])) s->status = CCO_NAN;
 }
 
-/* EdgeToEdgeImpulse, dcollid3d.cpp:1109-1300 (non-movable branches). */
+/* EdgeToEdgeImpulse, dcollid3d.cpp:1109-1300. */
 static void edge_to_edge_impulse(cco_solver* s, const int* pts, const double* nor, double a, double b, double dist) {
     double v_rel[3], vn, vt;
     double impulse = 0.0, m_impulse;
@@ -292,6 +345,17 @@ static void edge_to_edge_impulse(cco_solver* s, const int* pts, const double* no
             impulse = vn;
             rigid_impulse[0] = vn;
             rigid_impulse[1] = vn;
+        } else if (is_movable(s, pts[0]) && is_movable(s, pts[1]) && is_movable(s, pts[2]) &&
+                   is_movable(s, pts[3])) {
+            double m1 = body_mass(s, pts[0]), m2 = body_mass(s, pts[2]);
+            rigid_impulse[0] = vn * m2 / (m1 + m2);
+            rigid_impulse[1] = vn * m1 / (m1 + m2);
+        } else if (is_movable(s, pts[0]) && is_movable(s, pts[1])) {
+            rigid_impulse[0] = 0.5 * vn;
+            impulse = 0.5 * vn;
+        } else if (is_movable(s, pts[2]) && is_movable(s, pts[3])) {
+            impulse = 0.5 * vn;
+            rigid_impulse[1] = 0.5 * vn;
         } else {
             impulse = vn * 0.5;
         }
@@ -300,7 +364,7 @@ static void edge_to_edge_impulse(cco_solver* s, const int* pts, const double* no
         if (is_static(s, pts[2])) wb[0] = 0.0;
         if (is_static(s, pts[3])) wb[1] = 0.0;
     }
-    int all_rigid = is_static(s, pts[0]) && is_static(s, pts[1]) && is_static(s, pts[2]) && is_static(s, pts[3]);
+    int all_rigid = is_rigid(s, pts[0]) && is_rigid(s, pts[1]) && is_rigid(s, pts[2]) && is_rigid(s, pts[3]);
     if (vn * dt < 0.1 * dist) {
         if (all_rigid) {
             rigid_impulse[0] *= 1.0 + cr;
@@ -316,13 +380,18 @@ static void edge_to_edge_impulse(cco_solver* s, const int* pts, const double* no
         m_impulse = impulse;
     else
         m_impulse = 2.0 * impulse / (wa[0] * wa[0] + wa[1] * wa[1] + wb[0] * wb[0] + wb[1] * wb[1]);
-    if (all_rigid) return;
+    if (all_rigid) {
+        if (is_movable(s, pts[0])) spread_impact_zone_impulse(s, pts[0], rigid_impulse[0], nor);
+        if (is_movable(s, pts[2])) spread_impact_zone_impulse(s, pts[2], -1.0 * rigid_impulse[1], nor);
+        return;
+    }
     const double wgt[4] = {wa[0], wa[1], wb[0], wb[1]};
     for (int j = 0; j < 3; ++j) {
         for (int q = 0; q < 4; ++q) {
             int p = pts[q];
             if (is_static(s, p)) continue;
             double t_impulse = m_impulse;
+            if (is_movable(s, p)) t_impulse = rigid_impulse[q < 2 ? 0 : 1];
             if (q < 2)
                 s->imp[3 * p + j] += wgt[q] * t_impulse * nor[j];
             else
@@ -608,7 +677,7 @@ static int moving_tri_to_tri(cco_solver* s, int ta, int tb, double h) {
             if (pts[3] == pts[0] || pts[3] == pts[1] || pts[3] == pts[2]) continue;
             s->cur_sub = sub;
             if (moving_test(s, pts, h, 0)) status = 1;
-            if (status && zone) create_imp_zone(s, pts, 4);
+            if (status && zone) create_imp_zone(s, pts, 4, 0);
         }
     for (int i = 0; i < 3; ++i) {
         pts[0] = A[i];
@@ -619,7 +688,7 @@ static int moving_tri_to_tri(cco_solver* s, int ta, int tb, double h) {
             if (pts[0] == pts[2] || pts[0] == pts[3] || pts[1] == pts[2] || pts[1] == pts[3]) continue;
             s->cur_sub = sub;
             if (moving_test(s, pts, h, 1)) status = 1;
-            if (status && zone) create_imp_zone(s, pts, 4);
+            if (status && zone) create_imp_zone(s, pts, 4, 0);
         }
     }
     return status;
@@ -637,11 +706,11 @@ static int moving_tri_to_bond(cco_solver* s, int t, int bd, double h) {
     pts[3] = Bd[0];
     s->cur_sub = 0;
     if (moving_test(s, pts, h, 0)) status = 1;
-    if (status && zone) create_imp_zone(s, pts, 4);
+    if (status && zone) create_imp_zone(s, pts, 4, 0);
     pts[3] = Bd[1];
     s->cur_sub = 1;
     if (moving_test(s, pts, h, 0)) status = 1;
-    if (status && zone) create_imp_zone(s, pts, 4);
+    if (status && zone) create_imp_zone(s, pts, 4, 0);
     pts[2] = Bd[0];
     pts[3] = Bd[1];
     for (int i = 0; i < 3; ++i) {
@@ -649,7 +718,7 @@ static int moving_tri_to_bond(cco_solver* s, int t, int bd, double h) {
         pts[1] = T[(i + 1) % 3];
         s->cur_sub = 2 + i;
         if (moving_test(s, pts, h, 1)) status = 1;
-        if (status && zone) create_imp_zone(s, pts, 4);
+        if (status && zone) create_imp_zone(s, pts, 4, 0);
     }
     return status;
 }
@@ -663,7 +732,7 @@ static int moving_bond_to_bond(cco_solver* s, int b1, int b2, double h) {
             if (pts[i] == pts[j]) return 0;
     s->cur_sub = 0;
     if (moving_test(s, pts, h, 1)) status = 1;
-    if (status && s->det_imp_zone) create_imp_zone(s, pts, 4);
+    if (status && s->det_imp_zone) create_imp_zone(s, pts, 4, 0);
     return status;
 }
 
@@ -927,24 +996,6 @@ static int begin_pass(cco_solver* s, int kind) {
     return 0;
 }
 
-/* updateAverageVelocity, dcollid.cpp:677-751 (per point once; static points
- * skipped). */
-static int update_average_velocity(cco_solver* s) {
-    for (int p = 0; p < s->nv; ++p) {
-        if (!s->in_elem[p] || is_static(s, p)) continue;
-        if (s->num[p] > 0) {
-            s->has_collsn[p] = 1;
-            for (int k = 0; k < 3; ++k) {
-                s->avg[3 * p + k] += (s->imp[3 * p + k] + s->fric[3 * p + k]) / s->num[p];
-                if (!isfinite(s->avg[3 * p + k])) return CCO_NAN;
-                s->imp[3 * p + k] = s->fric[3 * p + k] = 0.0;
-            }
-            s->num[p] = 0;
-        }
-    }
-    return 0;
-}
-
 /* updateImpactListVelocity, dcollid3d.cpp:70-200: rigid motion of one zone,
  * walking the member list from its root. */
 static int update_impact_list_velocity(cco_solver* s, int head) {
@@ -1025,6 +1076,49 @@ static int update_impact_list_velocity(cco_solver* s, int head) {
     return 0;
 }
 
+/* updateImpactZoneVelocityForRG, dcollid.cpp:267-288: every zone of more
+ * than one point reached from a movable point moves rigidly. */
+static int update_impact_zone_velocity_for_rg(cco_solver* s) {
+    memset(s->sorted, 0, (size_t)s->nv);
+    for (int e = 0; e < s->ne; ++e)
+        for (int i = 0; i < s->enp[e]; ++i) {
+            int p = s->ev[3 * e + i];
+            if (s->sorted[p] || s->uf_w[find_set(s, p)] == 1) continue;
+            if (!is_movable(s, p)) {
+                s->sorted[p] = 1;
+                continue;
+            }
+            int rc = update_impact_list_velocity(s, find_set(s, p));
+            if (rc) return rc;
+        }
+    return 0;
+}
+
+/* updateAverageVelocity, dcollid.cpp:677-751 (per point once; static points
+ * skipped): the pass's impulses, then the spread rigid-body impulses, then
+ * the rigid motion of the movable bodies. */
+static int update_average_velocity(cco_solver* s) {
+    for (int p = 0; p < s->nv; ++p) {
+        if (!s->in_elem[p] || is_static(s, p)) continue;
+        if (s->num[p] > 0) {
+            s->has_collsn[p] = 1;
+            for (int k = 0; k < 3; ++k) {
+                s->avg[3 * p + k] += (s->imp[3 * p + k] + s->fric[3 * p + k]) / s->num[p];
+                if (!isfinite(s->avg[3 * p + k])) return CCO_NAN;
+                s->imp[3 * p + k] = s->fric[3 * p + k] = 0.0;
+            }
+            s->num[p] = 0;
+        }
+        if (s->num_rg[p] > 0) {
+            s->has_collsn[p] = 1;
+            for (int k = 0; k < 3; ++k) s->avg[3 * p + k] += s->imp_rg[3 * p + k] / s->num_rg[p];
+            s->num_rg[p] = 0;
+        }
+    }
+    if (s->dt > 0.0) return update_impact_zone_velocity_for_rg(s);
+    return 0;
+}
+
 /* updateImpactZoneVelocity, dcollid.cpp:290-310: every zone with more than
  * one point, visited from its first member in element order. */
 static int update_impact_zone_velocity(cco_solver* s) {
@@ -1044,7 +1138,7 @@ static int update_impact_zone_velocity(cco_solver* s) {
 static void detect_domain_boundary(cco_solver* s) {
     double dt = s->dt, mu = s->lambda;
     for (int p = 0; p < s->nv; ++p) {
-        if (!s->in_elem[p]) continue;
+        if (!s->in_elem[p] || is_movable(s, p)) continue;
         double cand[3], dv = 0;
         for (int j = 0; j < 3; ++j) {
             cand[j] = XO(p)[j] + dt * AV(p)[j];
@@ -1135,6 +1229,13 @@ cco_solver* cco_create(int nv, int nt, const int* tris, const int* tri_surf, con
     s->uf_next = malloc(sizeof(int) * V);
     s->uf_tail = malloc(sizeof(int) * V);
     s->uf_w = malloc(sizeof(int) * V);
+    s->vsurf = malloc(sizeof(int) * V);
+    s->imp_rg = calloc(3 * V, sizeof(double));
+    s->num_rg = calloc(V, sizeof(int));
+    if (!s->vsurf || !s->imp_rg || !s->num_rg) {
+        cco_destroy(s);
+        return NULL;
+    }
     if (!s->ev || !s->enp || !s->esurf || !s->erest || !s->fixed || !s->in_elem || !s->coords ||
         !s->x_old || !s->vel || !s->avg || !s->imp || !s->fric || !s->num || !s->has_collsn ||
         !s->sorted || !s->uf_root || !s->uf_next || !s->uf_tail || !s->uf_w) {
@@ -1166,7 +1267,36 @@ cco_solver* cco_create(int nv, int nt, const int* tris, const int* tri_surf, con
         s->enp[e] = 2;
         s->esurf[e] = -1;
     }
-    if (fixed) for (int i = 0; i < nv; ++i) s->fixed[i] = fixed[i] ? 1 : 0;
+    if (fixed) for (int i = 0; i < nv; ++i) s->fixed[i] = fixed[i] & 3;
+    /* surfaces: runs of equal tri_surf; a point's surface is that of the
+     * first triangle holding it */
+    for (int i = 0; i < nv; ++i) s->vsurf[i] = -1;
+    for (int t = 0; t < nt; ++t)
+        if (t == 0 || s->esurf[t] != s->esurf[t - 1]) s->nsurf++;
+    size_t S = (size_t)(s->nsurf > 0 ? s->nsurf : 1);
+    s->surf_id = malloc(sizeof(int) * S);
+    s->surf_t0 = malloc(sizeof(int) * S);
+    s->surf_t1 = malloc(sizeof(int) * S);
+    s->surf_mass = calloc(S, sizeof(double));
+    s->surf_com = calloc(3 * S, sizeof(double));
+    s->surf_comv = calloc(3 * S, sizeof(double));
+    s->mrg_com = calloc(3 * S, sizeof(double));
+    s->mrg_set = calloc(S, 1);
+    if (!s->surf_id || !s->surf_t0 || !s->surf_t1 || !s->surf_mass || !s->surf_com || !s->surf_comv ||
+        !s->mrg_com || !s->mrg_set) {
+        cco_destroy(s);
+        return NULL;
+    }
+    for (int t = 0, k = -1; t < nt; ++t) {
+        if (t == 0 || s->esurf[t] != s->esurf[t - 1]) {
+            ++k;
+            s->surf_id[k] = s->esurf[t];
+            s->surf_t0[k] = t;
+        }
+        s->surf_t1[k] = t + 1;
+        for (int j = 0; j < 3; ++j)
+            if (s->vsurf[s->ev[3 * t + j]] < 0) s->vsurf[s->ev[3 * t + j]] = k;
+    }
     if (s->ne > 0 && (tree_alloc(&s->tree[0], s->ne) || tree_alloc(&s->tree[1], s->ne))) {
         cco_destroy(s);
         return NULL;
@@ -1182,12 +1312,80 @@ void cco_destroy(cco_solver* s) {
     free(s->coords); free(s->x_old); free(s->vel); free(s->avg); free(s->imp); free(s->fric);
     free(s->num); free(s->has_collsn); free(s->sorted);
     free(s->uf_root); free(s->uf_next); free(s->uf_tail); free(s->uf_w);
+    free(s->vsurf); free(s->imp_rg); free(s->num_rg);
+    free(s->surf_id); free(s->surf_t0); free(s->surf_t1); free(s->surf_mass); free(s->surf_com);
+    free(s->surf_comv); free(s->mrg_com); free(s->mrg_set);
     if (s->ne > 0) { tree_free(&s->tree[0]); tree_free(&s->tree[1]); }
     free(s->pass_kind); free(s->pairs); free(s->contacts); free(s->snaps);
     free(s);
 }
 
 void cco_set_recording(cco_solver* s, int flags) { s->record = flags; }
+
+static int surf_of_id(const cco_solver* s, int id) {
+    for (int k = 0; k < s->nsurf; ++k)
+        if (s->surf_id[k] == id) return k;
+    return -1;
+}
+
+/* The HYPER_SURF data of a surface: total_mass, center_of_mass,
+ * center_of_mass_velo. The first call also seeds the solver's remembered
+ * centre of mass (mrg_com), which the reference would otherwise read before
+ * writing when a body's first point collides in the first step. */
+int cco_set_body(cco_solver* s, int surf, double mass, const double* com, const double* comv) {
+    int k = surf_of_id(s, surf);
+    if (k < 0) return CCO_BAD_INPUT;
+    s->surf_mass[k] = mass;
+    for (int i = 0; i < 3; ++i) {
+        s->surf_com[3 * k + i] = com[i];
+        s->surf_comv[3 * k + i] = comv[i];
+    }
+    if (!s->mrg_set[k]) {
+        for (int i = 0; i < 3; ++i) s->mrg_com[3 * k + i] = com[i];
+        s->mrg_set[k] = 1;
+    }
+    return 0;
+}
+
+int cco_get_body(const cco_solver* s, int surf, double* com, double* comv) {
+    int k = surf_of_id(s, surf);
+    if (k < 0) return CCO_BAD_INPUT;
+    for (int i = 0; i < 3; ++i) {
+        com[i] = s->surf_com[3 * k + i];
+        comv[i] = s->surf_comv[3 * k + i];
+    }
+    return 0;
+}
+
+/* updateFinalForRG, dcollid.cpp:626-675: per movable body, the first point
+ * (in element order) with has_collsn gives the body's velocity and moves its
+ * centre of mass from the remembered one. */
+static void update_final_for_rg(cco_solver* s) {
+    unsigned char* done = calloc((size_t)(s->nsurf > 0 ? s->nsurf : 1), 2);
+    if (!done) { s->status = CCO_NOMEM; return; }
+    unsigned char* visited = done + (s->nsurf > 0 ? s->nsurf : 1);  /* 0 absent, 1 false, 2 true */
+    for (int e = 0; e < s->ne; ++e)
+        for (int i = 0; i < s->enp[e]; ++i) {
+            int p = s->ev[3 * e + i];
+            if (!is_movable(s, p)) continue;
+            int k = s->vsurf[p];
+            if (k < 0) continue;
+            if (s->has_collsn[p] && !done[k]) {
+                done[k] = 1;
+                for (int j = 0; j < 3; ++j) {
+                    s->surf_comv[3 * k + j] = AV(p)[j];
+                    s->surf_com[3 * k + j] = AV(p)[j] * s->dt + s->mrg_com[3 * k + j];
+                }
+                visited[k] = 1;
+            }
+            if (visited[k] != 2) {
+                for (int j = 0; j < 3; ++j) s->mrg_com[3 * k + j] = s->surf_com[3 * k + j];
+                s->mrg_set[k] = 1;
+                visited[k] = 2;
+            }
+        }
+    free(done);
+}
 void cco_set_zone_cap(cco_solver* s, int cap) { s->zone_cap = cap; }
 
 /* resolveCollision, dcollid.cpp:317-362, preceded by the host loop's state
@@ -1215,6 +1413,11 @@ int cco_step(cco_solver* s, const double* x_old, const double* x_cand, double* v
         /* makeSet */
         s->uf_root[p] = p; s->uf_next[p] = -1; s->uf_tail[p] = p; s->uf_w[p] = 1;
         s->sorted[p] = 0;
+    }
+    /* createImpZoneForRG, dcollid3d.cpp:54-68 */
+    for (int k = 0; k < s->nsurf; ++k) {
+        if (!is_movable(s, s->ev[3 * s->surf_t0[k]])) continue;
+        for (int t = s->surf_t0[k]; t < s->surf_t1[k]; ++t) create_imp_zone(s, s->ev + 3 * t, 3, 1);
     }
     int rc = 0, hc = 0;
     if (s->ne == 0) goto out; /* the reference dereferences an empty tree here */
@@ -1288,6 +1491,8 @@ int cco_step(cco_solver* s, const double* x_old, const double* x_cand, double* v
     for (int p = 0; p < nv; ++p)
         if (s->in_elem[p] && s->has_collsn[p])
             for (int j = 0; j < 3; ++j) s->vel[3 * p + j] = AV(p)[j];
+    update_final_for_rg(s);
+    if ((rc = s->status)) goto out;
 
 out:
     s->det_imp_zone = 0;

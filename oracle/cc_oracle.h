@@ -29,9 +29,14 @@ typedef struct {
 
 enum { CCO_OK = 0, CCO_NAN = -2, CCO_ITER_CAP = -3, CCO_BAD_INPUT = -4, CCO_NOMEM = -5 };
 
+/* fixed: per point, bit 0 is_fixed (static rigid), bit 1 is_movableRG. */
 cco_solver* cco_create(int nv, int nt, const int* tris, const int* tri_surf,
                        const double* tri_rest, int nb, const int* bonds,
                        const double* bond_rest, const unsigned char* fixed);
+/* Body data of the surface with tri_surf id `surf` (total_mass,
+ * center_of_mass, center_of_mass_velo); read back after a step. */
+int cco_set_body(cco_solver* s, int surf, double mass, const double* com, const double* comv);
+int cco_get_body(const cco_solver* s, int surf, double* com, double* comv);
 void cco_destroy(cco_solver* s);
 /* record: bit0 pairs, bit1 contacts, bit2 pass-entry avgVel snapshots */
 void cco_set_recording(cco_solver* s, int flags);

@@ -75,6 +75,10 @@ def load():
     lib.cco_leaf_rank.restype = C.c_int
     lib.cco_leaf_rank.argtypes = [C.c_void_p, C.c_int, _ip]
     lib.cco_counters.argtypes = [C.c_void_p, _lp]
+    lib.cco_set_body.restype = C.c_int
+    lib.cco_set_body.argtypes = [C.c_void_p, C.c_int, C.c_double, _dp, _dp]
+    lib.cco_get_body.restype = C.c_int
+    lib.cco_get_body.argtypes = [C.c_void_p, C.c_int, _dp, _dp]
     _LIB = lib
     return lib
 
@@ -106,6 +110,21 @@ class OracleSolver:
         if not self.h:
             raise ValueError("oracle rejected the mesh")
         self.lib.cco_set_recording(self.h, int(record))
+        for sid, b in sorted(scene.bodies.items()):
+            self.set_body(sid, b["mass"], b["com"], b["comv"])
+
+    def set_body(self, surf: int, mass: float, com, comv):
+        com = np.ascontiguousarray(com, dtype=np.float64)
+        comv = np.ascontiguousarray(comv, dtype=np.float64)
+        if self.lib.cco_set_body(self.h, int(surf), float(mass), _ptr(com, _dp), _ptr(comv, _dp)):
+            raise ValueError(f"no surface {surf}")
+
+    def body(self, surf: int):
+        """(centre of mass, centre-of-mass velocity) of a movable body."""
+        com, comv = np.zeros(3), np.zeros(3)
+        if self.lib.cco_get_body(self.h, int(surf), _ptr(com, _dp), _ptr(comv, _dp)):
+            raise ValueError(f"no surface {surf}")
+        return com, comv
 
     def close(self):
         if getattr(self, "h", None):

@@ -198,7 +198,8 @@ void* ref_create(int nv, int nt, const int* tris, const int* tri_surf, const dou
         w->pts[i]._right_state = &w->st[i];
         w->pts[i].global_index = i;
         w->pts[i].hs = &w->hs_dummy;
-        w->st[i].is_fixed = fixed ? (fixed[i] != 0) : false;
+        w->st[i].is_fixed = fixed ? (fixed[i] & 1) != 0 : false;
+        w->st[i].is_movableRG = fixed ? (fixed[i] & 2) != 0 : false;
     }
     w->tris.assign(nt, TRI());
     int nsurf = 0;
@@ -217,8 +218,12 @@ void* ref_create(int nv, int nt, const int* tris, const int* tri_surf, const dou
             ++s;
             w->surfs[s].first = &tr;
             w->surfs[s].bdry = 0;
+            w->surfs[s].hs.body_index = tri_surf[t];
         }
         tr.surf = &w->surfs[s];
+        /* a point belongs to (pt->hs) the surface of its first triangle */
+        for (int k = 0; k < 3; ++k)
+            if (tr.__pts[k]->hs == &w->hs_dummy) tr.__pts[k]->hs = &w->surfs[s].hs;
         bool last = (t == nt - 1) || tri_surf[t + 1] != tri_surf[t];
         tr.next = last ? &w->sentinels[s] : &w->tris[t + 1];
         if (last) w->surfs[s].tail_sentinel = &w->sentinels[s];
@@ -260,6 +265,38 @@ void ref_destroy(void* h) {
     RefWorld* w = (RefWorld*)h;
     delete w->solver;
     delete w;
+}
+
+/* HYPER_SURF data of the surface whose tri_surf id is `surf`. The first call
+ * also seeds CollisionSolver::mrg_com (collid.h:174), which updateFinalForRG
+ * would otherwise read before writing (dcollid.cpp:650) when a body's first
+ * point collides in the first step. */
+int ref_set_body(void* h, int surf, double mass, const double* com, const double* comv) {
+    RefWorld* w = (RefWorld*)h;
+    for (auto& sf : w->surfs)
+        if (sf.hs.body_index == surf) {
+            sf.hs.mass = mass;
+            for (int k = 0; k < 3; ++k) {
+                sf.hs.com[k] = com[k];
+                sf.hs.comv[k] = comv[k];
+            }
+            if (!w->solver->mrg_com.count(surf)) w->solver->mrg_com[surf] = std::vector<double>(com, com + 3);
+            return 0;
+        }
+    return -4;
+}
+
+int ref_get_body(void* h, int surf, double* com, double* comv) {
+    RefWorld* w = (RefWorld*)h;
+    for (auto& sf : w->surfs)
+        if (sf.hs.body_index == surf) {
+            for (int k = 0; k < 3; ++k) {
+                com[k] = sf.hs.com[k];
+                comv[k] = sf.hs.comv[k];
+            }
+            return 0;
+        }
+    return -4;
 }
 
 void ref_set_recording(void* h, int record, int snap_vel) {

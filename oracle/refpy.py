@@ -45,6 +45,10 @@ def load():
     lib.ref_num_vel_snaps.restype = C.c_int
     lib.ref_num_vel_snaps.argtypes = [C.c_void_p]
     lib.ref_vel_snaps.argtypes = [C.c_void_p, _dp]
+    lib.ref_set_body.restype = C.c_int
+    lib.ref_set_body.argtypes = [C.c_void_p, C.c_int, C.c_double, _dp, _dp]
+    lib.ref_get_body.restype = C.c_int
+    lib.ref_get_body.argtypes = [C.c_void_p, C.c_int, _dp, _dp]
     return lib
 
 
@@ -66,6 +70,18 @@ class RefSolver:
         self.h = self.lib.ref_create(s.nv, s.nt, _ptr(t, _ip), _ptr(ts, _ip), _ptr(tr, _dp),
                                      s.nb, _ptr(b, _ip), _ptr(bc, _ip), _ptr(br, _dp), _ptr(fx, _up))
         self.lib.ref_set_recording(self.h, int(record), int(snap_vel))
+        for sid, b in sorted(scene.bodies.items()):
+            com = np.ascontiguousarray(b["com"], dtype=np.float64)
+            comv = np.ascontiguousarray(b["comv"], dtype=np.float64)
+            if self.lib.ref_set_body(self.h, int(sid), float(b["mass"]), _ptr(com, _dp), _ptr(comv, _dp)):
+                raise ValueError(f"no surface {sid}")
+
+    def body(self, surf: int):
+        """(centre of mass, centre-of-mass velocity) of a movable body."""
+        com, comv = np.zeros(3), np.zeros(3)
+        if self.lib.ref_get_body(self.h, int(surf), _ptr(com, _dp), _ptr(comv, _dp)):
+            raise ValueError(f"no surface {surf}")
+        return com, comv
 
     def close(self):
         if self.h:

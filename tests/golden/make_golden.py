@@ -4,8 +4,10 @@ Runs the reference's own CollisionSolver3d (AABB.cpp, dcollid.cpp,
 dcollid3d.cpp compiled unmodified against the stub headers by
 oracle/Makefile.ref) through the reference host loop on small seeded scenes,
 and stores per step:
-  inputs   x_old, x_cand, vel, has_collsn
-  outputs  x, vel, has_collsn, has_collision, impact-zone labels
+  inputs   x_old, x_cand, vel, has_collsn (left out for the cases in
+           cases.CHAINED, whose inputs are the previous step's outputs)
+  outputs  x, vel, has_collsn, has_collision, impact-zone labels, and the
+           centre of mass and its velocity of every movable body
   trace    pass kinds; every narrow-phase call that hit (pass, kind, a, b,
            status, collsn_num increments); the count and SHA-256 of the full
            visit record (every call, in order, with orientation)
@@ -30,7 +32,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 from collision_gb300 import scenes  # noqa: E402
-from tests.golden.cases import CASES  # noqa: E402
+from tests.golden.cases import CASES, CHAINED  # noqa: E402
 
 
 def pair_hash(pairs: np.ndarray) -> str:
@@ -54,7 +56,8 @@ def run_case(name, make, nsteps):
     v = sc.v.copy()
     hc = np.zeros(sc.nv, np.uint8)
     rec = {k: [] for k in ("x_old", "x_cand", "vel_in", "hc_in", "x", "vel", "hc", "has_collision",
-                           "zones", "npairs", "pair_sha")}
+                           "zones", "npairs", "pair_sha", "body_com", "body_comv")}
+    body_ids = sorted(sc.bodies)
     hits, kinds = [], []
     for step in range(nsteps):
         xc = scenes.candidate(sc, x, v)
@@ -72,14 +75,24 @@ def run_case(name, make, nsteps):
         hits.append(np.concatenate([np.full((len(h), 1), step, np.int32), h], axis=1))
         k = ref.passes()
         kinds.append(np.stack([np.full(len(k), step, np.int32), k], axis=1))
+        bodies = [ref.body(b) for b in body_ids]
+        rec["body_com"].append(np.array([b[0] for b in bodies]).reshape(-1, 3))
+        rec["body_comv"].append(np.array([b[1] for b in bodies]).reshape(-1, 3))
         x, v, hc = out["x"], out["v"], out["has_collsn"]
     ref.close()
+    if name in CHAINED:
+        for k in ("x_old", "x_cand", "vel_in", "hc_in"):
+            del rec[k]
     arrs = {k: np.array(val) for k, val in rec.items()}
     arrs["hits"] = np.concatenate(hits) if hits else np.zeros((0, 12), np.int32)
     arrs["pass_kinds"] = np.concatenate(kinds)
     for f in ("tris", "tri_surf", "tri_rest", "bonds", "bond_curve", "bond_rest", "fixed", "domain"):
         arrs["scene_" + f] = getattr(sc, f)
     arrs["scene_params"] = sc.param_vec()
+    arrs["scene_body_surf"] = np.array(body_ids, dtype=np.int32)
+    arrs["scene_body_mass"] = np.array([sc.bodies[b]["mass"] for b in body_ids], dtype=np.float64)
+    arrs["scene_body_com"] = np.array([sc.bodies[b]["com"] for b in body_ids], dtype=np.float64).reshape(-1, 3)
+    arrs["scene_body_comv"] = np.array([sc.bodies[b]["comv"] for b in body_ids], dtype=np.float64).reshape(-1, 3)
     arrs["scene_x"] = sc.x
     arrs["scene_v"] = sc.v
     return arrs

@@ -15,19 +15,13 @@ import pytest
 
 from collision_gb300 import scenes
 from oracle.ccopy import OracleSolver, REC_PAIRS, zone_labels
+from tests.gpu_util import golden_inputs, scene_from_golden
 
 GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
 
 
-def scene_from_golden(g):
-    return scenes.Scene("golden", g["scene_x"], g["scene_v"], g["scene_fixed"], g["scene_tris"],
-                        g["scene_tri_surf"], g["scene_tri_rest"], g["scene_bonds"], g["scene_bond_curve"],
-                        g["scene_bond_rest"], g["scene_domain"],
-                        dict(zip(scenes.PARAM_NAMES, g["scene_params"].tolist())))
-
-
 def test_golden_present():
-    assert len(GOLDEN) >= 5
+    assert len(GOLDEN) >= 11
 
 
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
@@ -37,7 +31,7 @@ def test_oracle_matches_reference_golden(path):
     o = OracleSolver(sc, record=REC_PAIRS)
     nsteps = len(g["x"])
     for step in range(nsteps):
-        out = o.step(g["x_old"][step], g["x_cand"][step], g["vel_in"][step], g["hc_in"][step])
+        out = o.step(*golden_inputs(g, sc, step))
         assert out["rc"] == 0
         assert np.array_equal(out["x"], g["x"][step]), f"positions differ at step {step}"
         assert np.array_equal(out["v"], g["vel"][step]), f"velocities differ at step {step}"
@@ -52,6 +46,10 @@ def test_oracle_matches_reference_golden(path):
             str(g["pair_sha"][step])
         hits = g["hits"][g["hits"][:, 0] == step][:, 1:]
         assert np.array_equal(p[p[:, 4] != 0], hits)
+        for i, sid in enumerate(sorted(sc.bodies)):
+            com, comv = o.body(sid)
+            assert np.array_equal(com, g["body_com"][step][i]), f"body {sid} centre of mass, step {step}"
+            assert np.array_equal(comv, g["body_comv"][step][i]), f"body {sid} velocity, step {step}"
     o.close()
 
 
