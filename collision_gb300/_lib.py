@@ -85,6 +85,10 @@ def load(path: str = LIB_PATH):
     lib.cc_set_vtk_dump.argtypes = [vp, C.c_char_p]
     lib.cc_set_zone_cap.restype = C.c_int
     lib.cc_set_zone_cap.argtypes = [vp, C.c_int]
+    lib.cc_set_body.restype = C.c_int
+    lib.cc_set_body.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    lib.cc_get_body.restype = C.c_int
+    lib.cc_get_body.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.cc_get_scene_status.restype = C.c_int
     lib.cc_get_scene_status.argtypes = [vp, ip]
     lib.cc_set_scene_enabled.restype = C.c_int

@@ -131,6 +131,11 @@ struct NarrowArgs {
     int* pair_hit;  // per candidate pair: bit s set when sub-test s hit
     int* pairq;     // candidate pairs with a queued sub-test (capacity: the pair buffer's)
     int static_only;  // proximity pass over swept-box pairs: only those with kPairStatic
+    // movable rigid bodies: the body of each point (-1 none), each body's
+    // mass, and the contribution slot of body 0 (the point count)
+    const int* vbody;
+    const double* body_mass;
+    int body_slot0;
 };
 void narrow_pass(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s, int block = 128);
 // The same pass in stages (mixed precision only, no recording): FP32
@@ -147,35 +152,64 @@ void point_boxes(const double4_32a* xo, const double4_32a* av, const int* vscene
                  cudaStream_t s);
 
 // ------------------------------------------------------------- post-pass
+// Movable rigid bodies, all scenes' in one list. members / member_body: the
+// points of every body in the order of its impact-zone member list (the
+// reference's createImpZoneForRG unions) with their body; zone_off: each
+// body's range there; visit / visit_off: each body's points in element
+// order (updateFinalForRG); acc: the running collsnImpulse_RG per body; num:
+// this pass's collsn_num_RG; out: k_final_rg's result per body.
+struct BodyBufs {
+    int n = 0;
+    int nmembers = 0;
+    const int* members = nullptr;
+    const int* member_body = nullptr;
+    const int* zone_off = nullptr;
+    const int* visit = nullptr;
+    const int* visit_off = nullptr;
+    double4_32a* acc = nullptr;
+    int* num = nullptr;
+    double4_32a* out = nullptr;
+    const uint8_t* fixed = nullptr;
+};
 struct ApplyBufs {
-    int* cnt;      // nv
-    int* off;      // nv
-    int* cur;      // nv
+    int* cnt;      // nv + bodies
+    int* off;      // nv + bodies
+    int* cur;      // nv + bodies
     int* idx;      // contrib_cap
     void* scan_temp;
 };
 // Per-point sums of the pass's contributions in visiting order, then
 // avgVel += (impulse + friction) / n and has_collsn (updateAverageVelocity).
 // dump (may be null): per point, the pass's summed impulse and the number
-// of contributions (zero for points without any).
+// of contributions (zero for points without any). With bodies, contribution
+// slots nv.. are the bodies' spread impulses, applied to their members after
+// each point's own (the buffers in b hold nv + bodies slots).
 void apply_contribs(const Contrib* contrib, const PassCounters* ctr, int contrib_cap, int nv, double4_32a* av,
-                    uint8_t* has_collsn, ApplyBufs& b, cudaStream_t s, double4_32a* dump = nullptr);
+                    uint8_t* has_collsn, ApplyBufs& b, cudaStream_t s, double4_32a* dump = nullptr,
+                    const BodyBufs* bodies = nullptr);
 
 // updateImpactZoneVelocity (dcollid.cpp:290-310): rigid motion of every
 // zone, one thread per zone over members[zone_off[z] .. zone_off[z+1]) in
 // the order of the reference's member list, with its scene's parameters.
+// With run set, the zones are movable bodies and move only in scenes that
+// are in a pass (updateImpactZoneVelocityForRG).
 void zone_solve(const int* members, const int* zone_off, int nzones, const uint8_t* fixed, const double4_32a* xo,
-                double4_32a* av, const int* vscene, const SceneDev* scenes, PassCounters* ctr, cudaStream_t s);
+                double4_32a* av, const int* vscene, const SceneDev* scenes, PassCounters* ctr, cudaStream_t s,
+                const SceneRun* run = nullptr);
+// updateFinalForRG's device part: per body, the first point in element
+// order with has_collsn and its average velocity (into b.out).
+void final_rigid(const BodyBufs& b, const uint8_t* has_collsn, const double4_32a* av, cudaStream_t s);
 
 // Step set-up: pack inputs, average velocity (computeAverageVelocity), each
 // point with its scene's dt.
 void step_init(const double* x_old, const double* x_cand, int nv, const uint8_t* in_elem, const int* vscene,
                const SceneDev* scenes, double4_32a* xo, double4_32a* av, PassCounters* ctr, cudaStream_t s);
 // Domain clamp + final position (detectDomainBoundaryCollision,
-// updateFinalPosition) with each point's scene's parameters and domain box.
+// updateFinalPosition) with each point's scene's parameters and domain box;
+// movable points are not clamped.
 void finalize_positions(const uint8_t* in_elem, const double4_32a* xo, double4_32a* av, uint8_t* has_collsn,
                         const double* x_cand, double* x_out, int nv, const int* vscene, const SceneDev* scenes,
-                        cudaStream_t s);
+                        const uint8_t* fixed, cudaStream_t s);
 // reduceSuperelast: up to 10 Gauss-Seidel passes over each scene's strain
 // edges, one CTA per scene.
 struct StrainEdge {

@@ -18,6 +18,7 @@ template <bool MOVING>
 __global__ void __launch_bounds__(128) k_narrow(NarrowArgs a, int max_pairs) {
     NarrowCtx c;
     c.xo = a.xo; c.av = a.av; c.fixed = a.fixed; c.ev = a.ev; c.esurf = a.esurf; c.erigid = a.erigid;
+    c.vbody = a.vbody; c.body_mass = a.body_mass; c.body_slot0 = a.body_slot0;
     c.rank = a.rank;
     c.contrib = a.contrib; c.contrib_cap = a.contrib_cap; c.ctr = a.ctr; c.urec = a.urec;
     c.urec_cap = a.urec_cap;
@@ -286,6 +287,7 @@ __global__ void __launch_bounds__(128) k_subtests(NarrowArgs a) {
     if (n > a.sub_cap) n = a.sub_cap;
     NarrowCtx c;
     c.xo = a.xo; c.av = a.av; c.fixed = a.fixed; c.ev = a.ev; c.esurf = a.esurf; c.erigid = a.erigid;
+    c.vbody = a.vbody; c.body_mass = a.body_mass; c.body_slot0 = a.body_slot0;
     c.rank = a.rank;
     c.contrib = a.contrib; c.contrib_cap = a.contrib_cap; c.ctr = a.ctr; c.urec = nullptr; c.urec_cap = 0;
     c.rec = nullptr; c.rec_cap = 0;

@@ -15,10 +15,13 @@ namespace ccg {
 struct NarrowCtx {
     const double4_32a* xo;       // x_old per point
     const double4_32a* av;       // average velocity per point
-    const uint8_t* fixed;    // is_fixed per point
+    const uint8_t* fixed;    // per point: bit 0 is_fixed, bit 1 is_movableRG
     const int* ev;           // 3 point ids per element (bonds: third is -1)
     const int* esurf;        // surface id per element (-1 for bonds)
-    const uint8_t* erigid;   // element has a fixed point (isRigidBody(hse))
+    const uint8_t* erigid;   // element has a fixed or movable point (isRigidBody(hse))
+    const int* vbody;        // movable body of each point, -1 for none
+    const double* body_mass; // total_mass of each body
+    int body_slot0;          // contribution slot of body 0 (after every point's)
     const int* rank;         // leaf rank of each element in its scene's reference tree
     int pass;                // the scene's pass index
     int zone;                // impact-zone mode (s_detImpZone) of the scene
@@ -53,7 +56,9 @@ struct CallState {
     int ncontacts;
 };
 
-__device__ __forceinline__ bool is_static(const NarrowCtx& c, int p) { return c.fixed[p] != 0; }
+__device__ __forceinline__ bool is_static(const NarrowCtx& c, int p) { return (c.fixed[p] & 1) != 0; }
+__device__ __forceinline__ bool is_movable(const NarrowCtx& c, int p) { return (c.fixed[p] & 2) != 0; }
+__device__ __forceinline__ bool is_rigid(const NarrowCtx& c, int p) { return c.fixed[p] != 0; }
 
 __device__ __forceinline__ void emit(const NarrowCtx& c, CallState& st, int vertex, const double* imp,
                                      const double* fric, int has_fric) {
@@ -69,6 +74,24 @@ __device__ __forceinline__ void emit(const NarrowCtx& c, CallState& st, int vert
     o.vertex = vertex;
     o.flags = has_fric;
     for (int j = 0; j < 3; ++j) { o.imp[j] = imp[j]; o.fric[j] = fric[j]; }
+}
+
+// SpreadImpactZoneImpulse (dcollid.cpp:1101-1115) adds impulse*nor to the
+// collsnImpulse_RG of every member of p's zone - a movable body's zone is the
+// body - and counts one. Every member gets the same additions in the same
+// order, so the sum is kept once per body, in a contribution slot of its own.
+__device__ __forceinline__ void emit_body(const NarrowCtx& c, CallState& st, int p, double impulse,
+                                          const double* nor) {
+    int slot = aggregated_add(&c.ctr->ncontrib, 1);
+    if (slot >= c.contrib_cap) {
+        atomicOr(&c.ctr->err, kErrContribOverflow);
+        return;
+    }
+    Contrib& o = c.contrib[slot];
+    o.key = st.keybase | (unsigned long long)st.sub;
+    o.vertex = c.body_slot0 + c.vbody[p];
+    o.flags = 0;
+    for (int j = 0; j < 3; ++j) { o.imp[j] = impulse * nor[j]; o.fric[j] = 0.0; }
 }
 
 // ---------------------------------------------------------------- unions
@@ -88,16 +111,18 @@ __device__ __forceinline__ void create_imp_zone(const NarrowCtx& c, const CallSt
 }
 
 // -------------------------------------------------------------- impulses
-// PointToTriImpulse, dcollid3d.cpp:925-1107 (fixed and free points).
+// PointToTriImpulse, dcollid3d.cpp:925-1107.
 static __device__ void point_to_tri_impulse(const NarrowCtx& c, CallState& st, const int* pts, const double* nor,
                                      double* w, double dist) {
     double v_rel[3] = {0.0, 0.0, 0.0}, vn, vt;
     double impulse = 0.0, m_impulse, sum_w = 0.0;
-    const double k = c.p.k, m = c.p.m, dt = c.p.dt, lambda = c.p.lambda, h = c.p.thickness;
+    double rigid_impulse[2] = {0.0, 0.0};
+    const double k = c.p.k, m = c.p.m, dt = c.p.dt, lambda = c.p.lambda, h = c.p.thickness, cr = c.p.cr;
     double av[4][3];
     for (int q = 0; q < 4; ++q) load3(c.av, pts[q], av[q]);
     bool st0 = is_static(c, pts[0]), st1 = is_static(c, pts[1]), st2 = is_static(c, pts[2]),
          st3 = is_static(c, pts[3]);
+    bool mv[4] = {is_movable(c, pts[0]), is_movable(c, pts[1]), is_movable(c, pts[2]), is_movable(c, pts[3])};
     dist = h - dist;
     for (int i = 0; i < 3; ++i) {
         v_rel[i] += av[3][i];
@@ -110,10 +135,23 @@ static __device__ void point_to_tri_impulse(const NarrowCtx& c, CallState& st, c
         vt = 0.0;
     bool tri_static[3] = {st0, st1, st2};
     if (vn < 0) {
-        if (st3 || (st0 && st1 && st2))
+        if (st3 || (st0 && st1 && st2)) {
             impulse = vn;
-        else
+            rigid_impulse[0] = vn;
+            rigid_impulse[1] = vn;
+        } else if (mv[0] && mv[1] && mv[2] && mv[3]) {
+            double m1 = c.body_mass[c.vbody[pts[0]]], m2 = c.body_mass[c.vbody[pts[3]]];
+            rigid_impulse[0] = vn * m2 / (m1 + m2);
+            rigid_impulse[1] = vn * m1 / (m1 + m2);
+        } else if (mv[0] && mv[1] && mv[2]) {
+            rigid_impulse[0] = 0.5 * vn;
+            impulse = 0.5 * vn;
+        } else if (mv[3]) {
+            impulse = 0.5 * vn;
+            rigid_impulse[1] = 0.5 * vn;
+        } else {
             impulse = vn * 0.5;
+        }
         for (int i = 0; i < 3; ++i) {
             if (tri_static[i]) w[i] = 0.0;
             sum_w += w[i];
@@ -123,23 +161,32 @@ static __device__ void point_to_tri_impulse(const NarrowCtx& c, CallState& st, c
             for (int i = 0; i < 3; ++i) w[i] = inv * w[i];
         }
     }
-    bool all_rigid = st0 && st1 && st2 && st3;
+    bool all_rigid = is_rigid(c, pts[0]) && is_rigid(c, pts[1]) && is_rigid(c, pts[2]) && is_rigid(c, pts[3]);
     if (vn * dt < 0.1 * dist) {
-        if (!all_rigid) {
+        if (all_rigid) {
+            rigid_impulse[0] *= 1.0 + cr;
+            rigid_impulse[1] *= 1.0 + cr;
+        } else {
             double tmp = -smin(dt * k * dist / m, (0.1 * dist / dt - vn));
             impulse += tmp;
+            rigid_impulse[0] += tmp;
+            rigid_impulse[1] += tmp;
         }
     }
     if (fabs(sum_w) < kMachEps)
         m_impulse = impulse;
     else
         m_impulse = 2.0 * impulse / (1.0 + dot3(w, w));
-    if (all_rigid) return;
+    if (all_rigid) {
+        if (mv[0]) emit_body(c, st, pts[0], rigid_impulse[0], nor);
+        if (mv[3]) emit_body(c, st, pts[3], -1.0 * rigid_impulse[1], nor);
+        return;
+    }
     int has_fric = fabs(vt) > kRoundEps;
     double imp[3], fric[3];
     for (int i = 0; i < 3; ++i) {
         if (tri_static[i]) continue;
-        double t_impulse = m_impulse;
+        double t_impulse = mv[i] ? rigid_impulse[0] : m_impulse;
         for (int j = 0; j < 3; ++j) {
             imp[j] = w[i] * t_impulse * nor[j];
             fric[j] = has_fric ? smax(-fabs(lambda * w[i] * t_impulse / vt), -1.0) * (v_rel[j] - vn * nor[j]) : 0.0;
@@ -147,7 +194,7 @@ static __device__ void point_to_tri_impulse(const NarrowCtx& c, CallState& st, c
         emit(c, st, pts[i], imp, fric, has_fric);
     }
     if (!st3) {
-        double t_impulse = m_impulse;
+        double t_impulse = mv[3] ? rigid_impulse[1] : m_impulse;
         for (int j = 0; j < 3; ++j) {
             imp[j] = -(t_impulse * nor[j]);
             fric[j] = has_fric ? smax(-fabs(lambda * t_impulse / vt), -1.0) * (v_rel[j] - vn * nor[j]) : 0.0;
@@ -156,16 +203,18 @@ static __device__ void point_to_tri_impulse(const NarrowCtx& c, CallState& st, c
     }
 }
 
-// EdgeToEdgeImpulse, dcollid3d.cpp:1109-1300 (fixed and free points).
+// EdgeToEdgeImpulse, dcollid3d.cpp:1109-1300.
 static __device__ void edge_to_edge_impulse(const NarrowCtx& c, CallState& st, const int* pts, const double* nor,
                                      double a, double b, double dist) {
     double v_rel[3], vn, vt;
     double impulse = 0.0, m_impulse;
-    const double k = c.p.k, m = c.p.m, dt = c.p.dt, lambda = c.p.lambda, h = c.p.thickness;
+    double rigid_impulse[2] = {0.0, 0.0};
+    const double k = c.p.k, m = c.p.m, dt = c.p.dt, lambda = c.p.lambda, h = c.p.thickness, cr = c.p.cr;
     double wa[2] = {1.0 - a, a}, wb[2] = {1.0 - b, b};
     double av[4][3];
     for (int q = 0; q < 4; ++q) load3(c.av, pts[q], av[q]);
     bool sq[4] = {is_static(c, pts[0]), is_static(c, pts[1]), is_static(c, pts[2]), is_static(c, pts[3])};
+    bool mv[4] = {is_movable(c, pts[0]), is_movable(c, pts[1]), is_movable(c, pts[2]), is_movable(c, pts[3])};
     dist = h - dist;
     for (int j = 0; j < 3; ++j) {
         v_rel[j] = (1.0 - b) * av[2][j] + b * av[3][j];
@@ -177,33 +226,55 @@ static __device__ void edge_to_edge_impulse(const NarrowCtx& c, CallState& st, c
     else
         vt = 0.0;
     if (vn < 0.0) {
-        if ((sq[0] && sq[1]) || (sq[2] && sq[3]))
+        if ((sq[0] && sq[1]) || (sq[2] && sq[3])) {
             impulse = vn;
-        else
+            rigid_impulse[0] = vn;
+            rigid_impulse[1] = vn;
+        } else if (mv[0] && mv[1] && mv[2] && mv[3]) {
+            double m1 = c.body_mass[c.vbody[pts[0]]], m2 = c.body_mass[c.vbody[pts[2]]];
+            rigid_impulse[0] = vn * m2 / (m1 + m2);
+            rigid_impulse[1] = vn * m1 / (m1 + m2);
+        } else if (mv[0] && mv[1]) {
+            rigid_impulse[0] = 0.5 * vn;
+            impulse = 0.5 * vn;
+        } else if (mv[2] && mv[3]) {
+            impulse = 0.5 * vn;
+            rigid_impulse[1] = 0.5 * vn;
+        } else {
             impulse = vn * 0.5;
+        }
         if (sq[0]) wa[0] = 0.0;
         if (sq[1]) wa[1] = 0.0;
         if (sq[2]) wb[0] = 0.0;
         if (sq[3]) wb[1] = 0.0;
     }
-    bool all_rigid = sq[0] && sq[1] && sq[2] && sq[3];
+    bool all_rigid = is_rigid(c, pts[0]) && is_rigid(c, pts[1]) && is_rigid(c, pts[2]) && is_rigid(c, pts[3]);
     if (vn * dt < 0.1 * dist) {
-        if (!all_rigid) {
+        if (all_rigid) {
+            rigid_impulse[0] *= 1.0 + cr;
+            rigid_impulse[1] *= 1.0 + cr;
+        } else {
             double tmp = -smin(dt * k * dist / m, (0.1 * dist / dt - vn));
             impulse += tmp;
+            rigid_impulse[0] += tmp;
+            rigid_impulse[1] += tmp;
         }
     }
     if (wa[0] + wa[1] < kMachEps || wb[0] + wb[1] < kMachEps)
         m_impulse = impulse;
     else
         m_impulse = 2.0 * impulse / (wa[0] * wa[0] + wa[1] * wa[1] + wb[0] * wb[0] + wb[1] * wb[1]);
-    if (all_rigid) return;
+    if (all_rigid) {
+        if (mv[0]) emit_body(c, st, pts[0], rigid_impulse[0], nor);
+        if (mv[2]) emit_body(c, st, pts[2], -1.0 * rigid_impulse[1], nor);
+        return;
+    }
     int has_fric = fabs(vt) > kRoundEps;
     const double wgt[4] = {wa[0], wa[1], wb[0], wb[1]};
     double imp[3], fric[3];
     for (int q = 0; q < 4; ++q) {
         if (sq[q]) continue;
-        double t_impulse = m_impulse;
+        double t_impulse = mv[q] ? rigid_impulse[q < 2 ? 0 : 1] : m_impulse;
         for (int j = 0; j < 3; ++j) {
             double d = wgt[q] * t_impulse * nor[j];
             imp[j] = (q < 2) ? d : -d;

@@ -51,13 +51,16 @@ __global__ void k_contrib_scatter(const Contrib* __restrict__ c, const PassCount
 
 // updateAverageVelocity, dcollid.cpp:677-751, for one point: its
 // contributions are put in visiting order and summed one by one from zero,
-// as the reference accumulates collsnImpulse and friction.
+// as the reference accumulates collsnImpulse and friction. Slots nv.. are
+// the movable bodies: their spread impulses are added one by one onto the
+// body's running collsnImpulse_RG, which the reference never clears, and
+// their count is the pass's collsn_num_RG.
 __global__ void k_apply(const Contrib* __restrict__ c, PassCounters* ctr, const int* __restrict__ cnt,
                         const int* __restrict__ off, int* idx, int nv, double4_32a* av, uint8_t* has_collsn,
-                        double4_32a* dump) {
+                        double4_32a* dump, int nbodies, double4_32a* body_acc, int* body_num) {
     if (ctr->err & kErrRetry) return;
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= nv) return;
+    if (p >= nv + nbodies) return;
     int n = cnt[p];
     if (n == 0) return;
     int* seg = idx + off[p];
@@ -71,6 +74,18 @@ __global__ void k_apply(const Contrib* __restrict__ c, PassCounters* ctr, const 
             --j;
         }
         seg[j + 1] = x;
+    }
+    if (p >= nv) {
+        const int b = p - nv;
+        double4_32a a = body_acc[b];
+        double acc[3] = {a.x, a.y, a.z};
+        for (int i = 0; i < n; ++i) {
+            const Contrib& q = c[seg[i]];
+            for (int k = 0; k < 3; ++k) acc[k] += q.imp[k];
+        }
+        body_acc[b] = make_double4_32a(acc[0], acc[1], acc[2], 0.0);
+        body_num[b] = n;
+        return;
     }
     double imp[3] = {0.0, 0.0, 0.0}, fric[3] = {0.0, 0.0, 0.0};
     for (int i = 0; i < n; ++i) {
@@ -92,6 +107,28 @@ __global__ void k_apply(const Contrib* __restrict__ c, PassCounters* ctr, const 
     if (dump) dump[p] = make_double4_32a(imp[0], imp[1], imp[2], (double)n);  // collsnImpulse, collsn_num
 }
 
+// The spread part of updateAverageVelocity (dcollid.cpp:726-733), after
+// each point's own impulses: avgVel += collsnImpulse_RG / collsn_num_RG for
+// every member of a body that received spread impulses this pass.
+__global__ void k_apply_rg(const int* __restrict__ members, const int* __restrict__ member_body, int nmembers,
+                           const PassCounters* ctr, const double4_32a* __restrict__ body_acc,
+                           const int* __restrict__ body_num, const uint8_t* __restrict__ fixed, double4_32a* av,
+                           uint8_t* has_collsn) {
+    if (ctr->err & kErrRetry) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nmembers) return;
+    const int b = member_body[i], n = body_num[b];
+    const int p = members[i];
+    if (n == 0 || (fixed[p] & 1)) return;
+    const double4_32a a = body_acc[b];
+    double4_32a v = av[p];
+    v.x += a.x / n;
+    v.y += a.y / n;
+    v.z += a.z / n;
+    av[p] = v;
+    has_collsn[p] = 1;
+}
+
 __device__ __forceinline__ double det3(const double (*a)[3]) {
     return a[0][0] * (a[1][1] * a[2][2] - a[2][1] * a[1][2]) - a[0][1] * (a[1][0] * a[2][2] - a[2][0] * a[1][2]) +
            a[0][2] * (a[1][0] * a[2][1] - a[2][0] * a[1][1]);
@@ -101,14 +138,19 @@ __device__ __forceinline__ double det3(const double (*a)[3]) {
 // its members in the order of the reference's member list (which fixes the
 // rounding of every sum); sin and cos correctly rounded, as the reference's
 // libm gives them.
+// With `run` set, the zones are movable bodies (updateImpactZoneVelocityForRG,
+// dcollid.cpp:267-288, called from updateAverageVelocity when dt > 0): only
+// those of scenes in a pass, and of more than one point, move.
 __global__ void k_zone_solve(const int* __restrict__ members, const int* __restrict__ zone_off, int nzones,
                              const uint8_t* __restrict__ fixed, const double4_32a* __restrict__ xo, double4_32a* av,
                              const int* __restrict__ vscene, const SceneDev* __restrict__ scenes,
-                             PassCounters* ctr) {
+                             PassCounters* ctr, const SceneRun* __restrict__ run) {
     int z = blockIdx.x * blockDim.x + threadIdx.x;
     if (z >= nzones) return;
     const int i = zone_off[z], end = zone_off[z + 1];
-    const Params prm = scenes[vscene[members[i]]].p;
+    const int zs = vscene[members[i]];
+    const Params prm = scenes[zs].p;
+    if (run && (run[zs].mode == kSceneIdle || !(prm.dt > 0.0) || end - i < 2 || (ctr->err & kErrRetry))) return;
     const double m = prm.m, dt = prm.dt;
     double x_cm[3] = {0.0, 0.0, 0.0}, v_cm[3] = {0.0, 0.0, 0.0};
     double L[3] = {0.0, 0.0, 0.0}, I[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}}, tmp[3][3];
@@ -158,7 +200,7 @@ __global__ void k_zone_solve(const int* __restrict__ members, const int* __restr
     bool bad = false;
     for (int q = i; q < end; ++q) {
         int p = members[q];
-        if (fixed[p]) continue;
+        if (fixed[p] & 1) continue;
         double xs[3], dx[3], xF[3], xR[3], wxR[3], tmpV[3], x_new[3], nv_[3];
         load3(xo, p, xs);
         for (int d = 0; d < 3; ++d) dx[d] = xs[d] - x_cm[d];
@@ -190,7 +232,8 @@ __global__ void k_zone_solve(const int* __restrict__ members, const int* __restr
 // once per point gives the same result.
 __global__ void k_finalize(const uint8_t* __restrict__ in_elem, const double4_32a* __restrict__ xo, double4_32a* av,
                            uint8_t* has_collsn, const double* __restrict__ x_cand, double* x_out, int nv,
-                           const int* __restrict__ vscene, const SceneDev* __restrict__ scenes) {
+                           const int* __restrict__ vscene, const SceneDev* __restrict__ scenes,
+                           const uint8_t* __restrict__ fixed) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nv) return;
     if (!in_elem[p]) {
@@ -208,6 +251,10 @@ __global__ void k_finalize(const uint8_t* __restrict__ in_elem, const double4_32
     load3(xo, p, xs);
     load3(av, p, v);
     double dt = prm.dt, mu = prm.lambda, dv = 0;
+    if (fixed[p] & 2) {  // movable points skip the clamp (dcollid.cpp:123)
+        for (int j = 0; j < 3; ++j) x_out[3 * p + j] = xs[j] + v[j] * dt;
+        return;
+    }
     for (int j = 0; j < 3; ++j) {
         double cand = xs[j] + dt * v[j];
         if (cand <= L[j]) {
@@ -905,6 +952,26 @@ __global__ void k_math_selftest(int fn, const double* a, const double* b, double
     out[i] = r;
 }
 
+// updateFinalForRG, dcollid.cpp:626-675: the first point of each body, in
+// element order, that has has_collsn (its index, -1 for none) and its final
+// average velocity.
+__global__ void k_final_rg(const int* __restrict__ visit, const int* __restrict__ visit_off, int nbodies,
+                           const uint8_t* __restrict__ has_collsn, const double4_32a* __restrict__ av,
+                           double4_32a* out) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbodies) return;
+    double4_32a r = make_double4_32a(0.0, 0.0, 0.0, -1.0);
+    for (int i = visit_off[b]; i < visit_off[b + 1]; ++i) {
+        const int p = visit[i];
+        if (has_collsn[p]) {
+            const double4_32a a = av[p];
+            r = make_double4_32a(a.x, a.y, a.z, (double)p);
+            break;
+        }
+    }
+    out[b] = r;
+}
+
 }  // namespace
 
 size_t strain_warp_smem(int max_slots, int ecap, int lcap, int wcap) {
@@ -925,33 +992,46 @@ void step_init(const double* x_old, const double* x_cand, int nv, const uint8_t*
 }
 
 void apply_contribs(const Contrib* contrib, const PassCounters* ctr, int contrib_cap, int nv, double4_32a* av,
-                    uint8_t* has_collsn, ApplyBufs& b, cudaStream_t s, double4_32a* dump) {
+                    uint8_t* has_collsn, ApplyBufs& b, cudaStream_t s, double4_32a* dump, const BodyBufs* bodies) {
     if (dump && nv > 0) cudaMemsetAsync(dump, 0, sizeof(double4_32a) * (size_t)nv, s);
     if (nv <= 0) return;
-    cudaMemsetAsync(b.cnt, 0, sizeof(int) * (size_t)nv, s);
-    cudaMemsetAsync(b.cur, 0, sizeof(int) * (size_t)nv, s);
+    const int nb = bodies ? bodies->n : 0, nslot = nv + nb;
+    cudaMemsetAsync(b.cnt, 0, sizeof(int) * (size_t)nslot, s);
+    cudaMemsetAsync(b.cur, 0, sizeof(int) * (size_t)nslot, s);
+    if (nb > 0) cudaMemsetAsync(bodies->num, 0, sizeof(int) * (size_t)nb, s);
     int blocks = nblk(contrib_cap, 256);
     if (blocks > 152 * 8) blocks = 152 * 8;
     count_launch(), k_contrib_count<<<blocks, 256, 0, s>>>(contrib, ctr, contrib_cap, b.cnt);
-    exclusive_scan(b.cnt, b.off, nv, nullptr, b.scan_temp, s);
+    exclusive_scan(b.cnt, b.off, nslot, nullptr, b.scan_temp, s);
     count_launch(), k_contrib_scatter<<<blocks, 256, 0, s>>>(contrib, ctr, contrib_cap, b.off, b.cur, b.idx);
-    count_launch(), k_apply<<<nblk(nv, 128), 128, 0, s>>>(contrib, const_cast<PassCounters*>(ctr), b.cnt, b.off,
-                                                          b.idx, nv, av, has_collsn, dump);
+    count_launch(), k_apply<<<nblk(nslot, 128), 128, 0, s>>>(contrib, const_cast<PassCounters*>(ctr), b.cnt, b.off,
+                                                             b.idx, nv, av, has_collsn, dump, nb,
+                                                             nb ? bodies->acc : nullptr, nb ? bodies->num : nullptr);
+    if (nb > 0)
+        count_launch(), k_apply_rg<<<nblk(bodies->nmembers, 128), 128, 0, s>>>(
+            bodies->members, bodies->member_body, bodies->nmembers, ctr, bodies->acc, bodies->num, bodies->fixed, av,
+            has_collsn);
 }
 
 void zone_solve(const int* members, const int* zone_off, int nzones, const uint8_t* fixed, const double4_32a* xo,
-                double4_32a* av, const int* vscene, const SceneDev* scenes, PassCounters* ctr, cudaStream_t s) {
+                double4_32a* av, const int* vscene, const SceneDev* scenes, PassCounters* ctr, cudaStream_t s,
+                const SceneRun* run) {
     if (nzones > 0)
         count_launch(), k_zone_solve<<<nblk(nzones, 128), 128, 0, s>>>(members, zone_off, nzones, fixed, xo, av,
-                                                                       vscene, scenes, ctr);
+                                                                       vscene, scenes, ctr, run);
+}
+
+void final_rigid(const BodyBufs& b, const uint8_t* has_collsn, const double4_32a* av, cudaStream_t s) {
+    if (b.n > 0)
+        count_launch(), k_final_rg<<<nblk(b.n, 128), 128, 0, s>>>(b.visit, b.visit_off, b.n, has_collsn, av, b.out);
 }
 
 void finalize_positions(const uint8_t* in_elem, const double4_32a* xo, double4_32a* av, uint8_t* has_collsn,
                         const double* x_cand, double* x_out, int nv, const int* vscene, const SceneDev* scenes,
-                        cudaStream_t s) {
+                        const uint8_t* fixed, cudaStream_t s) {
     if (nv > 0)
         count_launch(), k_finalize<<<nblk(nv, 256), 256, 0, s>>>(in_elem, xo, av, has_collsn, x_cand, x_out, nv,
-                                                                 vscene, scenes);
+                                                                 vscene, scenes, fixed);
 }
 
 size_t strain_step_bytes(int nedges) {

@@ -298,6 +298,43 @@ struct cc_solver {
     Contrib* d_contrib = nullptr;
     int contrib_cap = 0;
     ApplyBufs apply{};
+
+    // movable rigid bodies: one per surface of movable points
+    // (createImpZoneForRG, dcollid3d.cpp:54-68), all scenes in one list
+    struct BodyHost {
+        int scene, surf;
+        double mass = 1.0;
+        double com[3] = {0.0, 0.0, 0.0}, comv[3] = {0.0, 0.0, 0.0};  // HYPER_SURF
+        double mrg_com[3] = {0.0, 0.0, 0.0};                           // CollisionSolver::mrg_com
+        bool mrg_set = false;
+    };
+    std::vector<BodyHost> bodies;
+    std::vector<int> body_unions;  // createImpZoneForRG triangles, 3 points each, in order
+    std::vector<int> h_body_visit, h_body_visit_off;
+    std::vector<double4_32a> h_body_out;
+    std::vector<uint8_t> h_fixed;
+    int* d_vbody = nullptr;
+    double* d_body_mass = nullptr;
+    int* d_body_members = nullptr;
+    int* d_body_member_body = nullptr;
+    int* d_body_zone_off = nullptr;
+    int* d_body_visit = nullptr;
+    int* d_body_visit_off = nullptr;
+    double4_32a* d_body_acc = nullptr;
+    int* d_body_num = nullptr;
+    double4_32a* d_body_out = nullptr;
+    BodyBufs body_bufs;
+    int find_body(int scene, int surf) const {
+        for (size_t b = 0; b < bodies.size(); ++b)
+            if (bodies[b].scene == scene && bodies[b].surf == surf) return (int)b;
+        return -1;
+    }
+    void upload_body_mass() {
+        if (bodies.empty()) return;
+        std::vector<double> m(bodies.size());
+        for (size_t b = 0; b < bodies.size(); ++b) m[b] = bodies[b].mass;
+        cudaMemcpy(d_body_mass, m.data(), sizeof(double) * m.size(), cudaMemcpyHostToDevice);
+    }
     PassCounters* d_ctr = nullptr;
     PassCounters* h_ctr = nullptr;
     unsigned long long* h_bbox = nullptr;  // pinned, 6 per scene
@@ -410,6 +447,12 @@ struct cc_solver {
         dfree(d_rank[0]); dfree(d_rank[1]);
         dfree(d_rec); dfree(d_pbox_lo); dfree(d_pbox_hi); dfree(d_p32); dfree(d_v32);
         dfree(d_act_e); dfree(d_act_p); dfree(d_sel); dfree(d_dump); dfree(d_av_pre);
+        dfree(d_vbody); dfree(d_body_mass); dfree(d_body_members); dfree(d_body_member_body);
+        dfree(d_body_zone_off); dfree(d_body_visit); dfree(d_body_visit_off); dfree(d_body_acc);
+        dfree(d_body_num); dfree(d_body_out);
+        bodies.clear();
+        body_unions.clear();
+        body_bufs = BodyBufs{};
         if (h_sel) cudaFreeHost(h_sel);
         h_sel = nullptr;
         sel_prev.clear();
@@ -482,7 +525,8 @@ struct cc_solver {
     }
 
     // makeSet for every point (dcollid.cpp:1015-1022), undoing the last
-    // step's unions.
+    // step's unions, then createImpZoneForRG: each movable surface's
+    // triangles in order, createImpZone(pts, 3, YES) (dcollid3d.cpp:54-68).
     void reset_zones() {
         for (int p : uf_touched) {
             uf_root[p] = uf_tail[p] = p;
@@ -490,6 +534,12 @@ struct cc_solver {
             uf_w[p] = 1;
         }
         uf_touched.clear();
+        for (size_t i = 0; i < body_unions.size(); i += 3) {
+            const int* t = &body_unions[i];
+            for (int a = 0; a < 3; ++a) uf_touched.push_back(t[a]);
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < a; ++b) merge_point(t[a], t[b]);
+        }
     }
     // findSet (dcollid.cpp:1024-1031) with path compression.
     int find_set(int p) {
@@ -590,7 +640,7 @@ struct cc_solver {
             long long l0 = g_kernel_launches;
             if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
                 return cuda_check("tail capture");
-            finalize_positions(d_in_elem, d_xo, d_av, d_hc, x_cand, x_out, nv, d_vscene, d_scenes, stream);
+            finalize_positions(d_in_elem, d_xo, d_av, d_hc, x_cand, x_out, nv, d_vscene, d_scenes, d_fixed, stream);
             tail_after_finalize(vel, hc);
             cudaError_t e = cudaStreamEndCapture(stream, &g);
             long long n = g_kernel_launches - l0;
@@ -750,7 +800,9 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
         sd.enabled = 1;
         for (int i = 0; i < snv; ++i) {
             vscene[v0 + i] = si;
-            fixed[v0 + i] = (m->fixed && m->fixed[i]) ? 1 : 0;
+            const uint8_t f = m->fixed ? m->fixed[i] : 0;
+            if (f > 2) return fail(CC_BAD_INPUT, "point flag must be 0 (free), 1 (fixed) or 2 (movable)");
+            fixed[v0 + i] = f;
         }
         for (int t = 0; t < nt; ++t) {
             int* E = &ev[3 * (size_t)(e0 + t)];
@@ -802,6 +854,68 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     }
     nedges = (int)all_edges.size();
 
+    // Movable rigid bodies: a surface (run of equal tri_surface) whose first
+    // point is movable (dcollid3d.cpp:62). Its points must all be movable and
+    // belong to no other element, and every movable point to such a surface,
+    // so that each body stays one impact zone for the whole step.
+    std::vector<int> vbody((size_t)nv, -1);
+    bodies.clear();
+    body_unions.clear();
+    for (int si = 0; si < n; ++si) {
+        const SceneHost& sh = scenes[si];
+        const int nt = meshes[si].n_tris;
+        for (int t0 = 0; t0 < nt;) {
+            int t1 = t0 + 1;
+            while (t1 < nt && esurf[sh.e0 + t1] == esurf[sh.e0 + t0]) ++t1;
+            if (fixed[ev[3 * (size_t)(sh.e0 + t0)]] & 2) {
+                const int b = (int)bodies.size();
+                if (find_body(si, esurf[sh.e0 + t0]) >= 0)
+                    return fail(CC_BAD_INPUT, "two movable surfaces of one scene share a surface id");
+                BodyHost bh;
+                bh.scene = si;
+                bh.surf = esurf[sh.e0 + t0];
+                bodies.push_back(bh);
+                for (int t = t0; t < t1; ++t)
+                    for (int k = 0; k < 3; ++k) {
+                        const int p = ev[3 * (size_t)(sh.e0 + t) + k];
+                        if (!(fixed[p] & 2)) return fail(CC_BAD_INPUT, "a movable surface holds a point that is not movable");
+                        if (vbody[p] >= 0 && vbody[p] != b) return fail(CC_BAD_INPUT, "a point in two movable surfaces");
+                        vbody[p] = b;
+                        body_unions.push_back(p);
+                    }
+            }
+            t0 = t1;
+        }
+    }
+    h_body_visit.clear();
+    h_body_visit_off.assign(bodies.size() + 1, 0);
+    for (int e = 0; e < ne; ++e)
+        for (int k = 0; k < 3; ++k) {
+            const int p = ev[3 * (size_t)e + k];
+            if (p < 0 || !(fixed[p] & 2)) continue;
+            if (vbody[p] < 0) return fail(CC_BAD_INPUT, "a movable point outside a movable surface");
+            const int ts = escene[e], te = e - scenes[ts].e0;
+            if (te >= meshes[ts].n_tris || esurf[e] != bodies[vbody[p]].surf)
+                return fail(CC_BAD_INPUT, "a movable point shared with an element outside its body");
+        }
+    {
+        // each body's points in element order (updateFinalForRG's visit)
+        std::vector<std::vector<int>> visit(bodies.size());
+        std::vector<uint8_t> seen((size_t)nv, 0);
+        for (size_t i = 0; i < body_unions.size(); ++i) {
+            const int p = body_unions[i];
+            if (!seen[p]) {
+                seen[p] = 1;
+                visit[vbody[p]].push_back(p);
+            }
+        }
+        for (size_t b = 0; b < bodies.size(); ++b) {
+            h_body_visit_off[b + 1] = h_body_visit_off[b] + (int)visit[b].size();
+            h_body_visit.insert(h_body_visit.end(), visit[b].begin(), visit[b].end());
+        }
+    }
+    const int nbodies = (int)bodies.size();
+
     bool ok = true;
     ok &= dalloc(&d_scenes, (size_t)n) == cudaSuccess;
     ok &= dalloc(&d_run, (size_t)n) == cudaSuccess;
@@ -845,10 +959,23 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     ok &= dalloc(&bvh.node, (size_t)ne) == cudaSuccess;
     ok &= dalloc(&bvh.bbox_enc, 6 * (size_t)n) == cudaSuccess;
     ok &= cudaMalloc(&bvh.sort_temp, radix_sort_temp_bytes(ne > 0 ? ne : 1)) == cudaSuccess;
-    ok &= dalloc(&apply.cnt, (size_t)nv) == cudaSuccess;
-    ok &= dalloc(&apply.off, (size_t)nv) == cudaSuccess;
-    ok &= dalloc(&apply.cur, (size_t)nv) == cudaSuccess;
-    ok &= cudaMalloc(&apply.scan_temp, scan_temp_bytes(nv > 0 ? nv : 1)) == cudaSuccess;
+    ok &= dalloc(&apply.cnt, (size_t)nv + nbodies) == cudaSuccess;
+    ok &= dalloc(&apply.off, (size_t)nv + nbodies) == cudaSuccess;
+    ok &= dalloc(&apply.cur, (size_t)nv + nbodies) == cudaSuccess;
+    ok &= cudaMalloc(&apply.scan_temp, scan_temp_bytes(nv + nbodies > 0 ? nv + nbodies : 1)) == cudaSuccess;
+    if (nbodies > 0) {
+        const size_t nm = (size_t)h_body_visit.size();
+        ok &= dalloc(&d_vbody, (size_t)nv) == cudaSuccess;
+        ok &= dalloc(&d_body_mass, (size_t)nbodies) == cudaSuccess;
+        ok &= dalloc(&d_body_members, nm) == cudaSuccess;
+        ok &= dalloc(&d_body_member_body, nm) == cudaSuccess;
+        ok &= dalloc(&d_body_zone_off, (size_t)nbodies + 1) == cudaSuccess;
+        ok &= dalloc(&d_body_visit, nm) == cudaSuccess;
+        ok &= dalloc(&d_body_visit_off, (size_t)nbodies + 1) == cudaSuccess;
+        ok &= dalloc(&d_body_acc, (size_t)nbodies) == cudaSuccess;
+        ok &= dalloc(&d_body_num, (size_t)nbodies) == cudaSuccess;
+        ok &= dalloc(&d_body_out, (size_t)nbodies) == cudaSuccess;
+    }
     ok &= dalloc(&d_rank[0], (size_t)ne) == cudaSuccess;
     ok &= dalloc(&d_rank[1], (size_t)ne) == cudaSuccess;
     ok &= dalloc(&d_pbox_lo, (size_t)nv) == cudaSuccess;
@@ -898,6 +1025,41 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     uf_w.assign((size_t)nv, 1);
     for (int p = 0; p < nv; ++p) uf_root[p] = uf_tail[p] = p;
     uf_touched.clear();
+    h_fixed = fixed;
+    if (nbodies > 0) {
+        // each body's zone member list, as the unions leave it
+        reset_zones();
+        std::vector<int> members, member_body, zone_off(1, 0);
+        for (int b = 0; b < nbodies; ++b) {
+            const int r = find_set(h_body_visit[h_body_visit_off[b]]);
+            for (int q = r; q >= 0; q = uf_next[q]) {
+                members.push_back(q);
+                member_body.push_back(b);
+            }
+            zone_off.push_back((int)members.size());
+        }
+        cudaMemcpy(d_vbody, vbody.data(), sizeof(int) * (size_t)nv, cudaMemcpyHostToDevice);
+        cudaMemcpy(d_body_members, members.data(), sizeof(int) * members.size(), cudaMemcpyHostToDevice);
+        cudaMemcpy(d_body_member_body, member_body.data(), sizeof(int) * member_body.size(), cudaMemcpyHostToDevice);
+        cudaMemcpy(d_body_zone_off, zone_off.data(), sizeof(int) * zone_off.size(), cudaMemcpyHostToDevice);
+        cudaMemcpy(d_body_visit, h_body_visit.data(), sizeof(int) * h_body_visit.size(), cudaMemcpyHostToDevice);
+        cudaMemcpy(d_body_visit_off, h_body_visit_off.data(), sizeof(int) * h_body_visit_off.size(),
+                   cudaMemcpyHostToDevice);
+        cudaMemset(d_body_acc, 0, sizeof(double4_32a) * (size_t)nbodies);
+        upload_body_mass();
+        body_bufs.n = nbodies;
+        body_bufs.nmembers = (int)members.size();
+        body_bufs.members = d_body_members;
+        body_bufs.member_body = d_body_member_body;
+        body_bufs.zone_off = d_body_zone_off;
+        body_bufs.visit = d_body_visit;
+        body_bufs.visit_off = d_body_visit_off;
+        body_bufs.acc = d_body_acc;
+        body_bufs.num = d_body_num;
+        body_bufs.out = d_body_out;
+        body_bufs.fixed = d_fixed;
+        h_body_out.assign((size_t)nbodies, double4_32a{});
+    }
     if (grow_unions(1024)) return CC_NO_MEMORY;
     if (grow_subs(2 * ne + 4096)) return CC_NO_MEMORY;
     h_strain_passes.assign(3 * (size_t)n, 0);
@@ -1006,6 +1168,7 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
         prof(kStTraverse, false);
         NarrowArgs a;
         a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
+        a.vbody = d_vbody; a.body_mass = d_body_mass; a.body_slot0 = nv;
         a.rank = d_rank[moving]; a.escene = d_escene; a.scenes = d_scenes; a.run = d_run;
         a.pairs = d_pairs; a.contrib = d_contrib; a.contrib_cap = contrib_cap; a.ctr = d_ctr;
         a.urec = d_urec; a.urec_cap = urec_cap;
@@ -1030,7 +1193,11 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
             narrow_pass(a, moving, pair_cap, stream, tune.narrow_block);
         prof(moving ? kStNarrowCcd : kStNarrowProx, false);
         prof(kStApply, true);
-        apply_contribs(d_contrib, d_ctr, contrib_cap, nv, d_av, d_hc, apply, stream, dump ? d_dump : nullptr);
+        apply_contribs(d_contrib, d_ctr, contrib_cap, nv, d_av, d_hc, apply, stream, dump ? d_dump : nullptr,
+                       bodies.empty() ? nullptr : &body_bufs);
+        if (!bodies.empty())  // updateImpactZoneVelocityForRG (dcollid.cpp:744-745)
+            zone_solve(d_body_members, d_body_zone_off, (int)bodies.size(), d_fixed, d_xo, d_av, d_vscene, d_scenes,
+                       d_ctr, stream, d_run);
         prof(kStApply, false);
         cudaMemcpyAsync(h_ctr, d_ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, stream);
         cudaMemcpyAsync(h_run, d_run, sizeof(SceneRun) * (size_t)nscenes, cudaMemcpyDeviceToHost, stream);
@@ -1066,7 +1233,9 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
         break;
     }
     if (h_ctr->err) return fail(CC_PAIR_OVERFLOW, "buffers kept overflowing");
-    if (combined && h_ctr->ncontrib == 0) {  // velocities unchanged: the swept pairs hold for the next pass
+    if (combined && h_ctr->ncontrib == 0 && bodies.empty()) {
+        // velocities unchanged (no impulse, no rigid-body motion): the swept
+        // pairs hold for the next pass
         reuse_pairs = true;
         reuse_npairs = h_ctr->npairs;
         reuse_set = cur_set;
@@ -1123,7 +1292,8 @@ cc_status cc_solver::zone_pass_unions() {
             const int* pts = h_urec[i].p;
             for (int a = 0; a < 4; ++a) uf_touched.push_back(pts[a]);
             for (int a = 0; a < 4; ++a)  // createImpZone(pts, 4), dcollid.cpp:473-484
-                for (int b = 0; b < a; ++b) merge_point(pts[a], pts[b]);
+                for (int b = 0; b < a; ++b)
+                    if (!((h_fixed[pts[a]] | h_fixed[pts[b]]) & 2)) merge_point(pts[a], pts[b]);
         }
     }
     h_members.clear();
@@ -1267,7 +1437,7 @@ cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, dou
         prof(kStStrain, false);
     } else {
         prof(kStFinalize, true);
-        finalize_positions(d_in_elem, d_xo, d_av, d_hc, x_cand, x_out, nv, d_vscene, d_scenes, stream);
+        finalize_positions(d_in_elem, d_xo, d_av, d_hc, x_cand, x_out, nv, d_vscene, d_scenes, d_fixed, stream);
         prof(kStFinalize, false);
         prof(kStStrain, true);
         tail_after_finalize(vel, hc);
@@ -1275,7 +1445,37 @@ cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, dou
     }
     cudaMemcpyAsync(h_strain_passes.data(), d_strain_passes, sizeof(int) * h_strain_passes.size(),
                     cudaMemcpyDeviceToHost, stream);
+    if (!bodies.empty()) {
+        final_rigid(body_bufs, d_hc, d_av, stream);
+        cudaMemcpyAsync(h_body_out.data(), d_body_out, sizeof(double4_32a) * bodies.size(), cudaMemcpyDeviceToHost,
+                        stream);
+    }
     if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("finalize");
+    // updateFinalForRG (dcollid.cpp:626-675): a body with a collided point
+    // takes that point's velocity, and its centre of mass moves from the
+    // remembered one (if that point is the body's first) or the current one
+    for (size_t b = 0; b < bodies.size(); ++b) {
+        BodyHost& B = bodies[b];
+        if (!scenes[B.scene].enabled) continue;
+        if (!B.mrg_set) {
+            std::copy(B.com, B.com + 3, B.mrg_com);
+            B.mrg_set = true;
+        }
+        const double4_32a o = h_body_out[b];
+        const int p = (int)o.w;
+        if (p >= 0) {
+            const double dt = h_scenes[B.scene].p.dt;
+            const double* base = (p == h_body_visit[h_body_visit_off[b]]) ? B.mrg_com : B.com;
+            const double v[3] = {o.x, o.y, o.z};
+            double com[3];
+            for (int j = 0; j < 3; ++j) com[j] = v[j] * dt + base[j];
+            for (int j = 0; j < 3; ++j) {
+                B.comv[j] = v[j];
+                B.com[j] = com[j];
+            }
+        }
+        std::copy(B.com, B.com + 3, B.mrg_com);
+    }
     for (int s = 0; s < nscenes; ++s) {
         // algorithmic bytes of the sweep: per pass, each edge's 48-byte
         // record and one 32-byte read and write of each point it touches
@@ -1325,6 +1525,7 @@ cc_status cc_solver::check_ccd(const double* x_old, const double* x_new, long lo
         bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, d_ev);
         NarrowArgs a{};
         a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
+        a.vbody = d_vbody; a.body_mass = d_body_mass; a.body_slot0 = nv;
         a.rank = nullptr; a.escene = d_escene; a.scenes = d_scenes; a.run = d_run;
         a.pairs = d_pairs; a.contrib = d_contrib; a.contrib_cap = contrib_cap; a.ctr = d_ctr;
         a.urec = nullptr; a.urec_cap = 0;
@@ -1386,6 +1587,7 @@ cc_status cc_solver::autotune(double* best_ms) {
             bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, d_ev, t.traverse_block);
             NarrowArgs a{};
             a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
+        a.vbody = d_vbody; a.body_mass = d_body_mass; a.body_slot0 = nv;
             a.rank = rank; a.escene = d_escene; a.scenes = d_scenes; a.run = d_run;
             a.pairs = d_pairs; a.contrib = d_contrib; a.contrib_cap = contrib_cap; a.ctr = d_ctr;
             a.urec = d_urec; a.urec_cap = urec_cap;
@@ -1684,6 +1886,36 @@ cc_status cc_set_vtk_dump(cc_solver* s, const char* dir) {
     if (!s->d_dump) ok &= dalloc(&s->d_dump, (size_t)s->nv) == cudaSuccess;
     if (!s->d_av_pre) ok &= dalloc(&s->d_av_pre, (size_t)s->nv) == cudaSuccess;
     if (!ok) return s->fail(CC_NO_MEMORY, "dump buffers");
+    return CC_OK;
+}
+
+cc_status cc_set_body(cc_solver* s, int scene, int surface, double mass, const double* com, const double* comv) {
+    if (!s || !com || !comv) return CC_BAD_INPUT;
+    const int b = s->find_body(scene, surface);
+    if (b < 0) return s->fail(CC_BAD_INPUT, "no movable surface with that id in the scene");
+    auto& B = s->bodies[(size_t)b];
+    B.mass = mass;
+    for (int j = 0; j < 3; ++j) {
+        B.com[j] = com[j];
+        B.comv[j] = comv[j];
+    }
+    if (!B.mrg_set) {
+        std::copy(com, com + 3, B.mrg_com);
+        B.mrg_set = true;
+    }
+    s->upload_body_mass();
+    return s->cuda_check("set body");
+}
+
+cc_status cc_get_body(cc_solver* s, int scene, int surface, double* com, double* comv) {
+    if (!s || !com || !comv) return CC_BAD_INPUT;
+    const int b = s->find_body(scene, surface);
+    if (b < 0) return s->fail(CC_BAD_INPUT, "no movable surface with that id in the scene");
+    const auto& B = s->bodies[(size_t)b];
+    for (int j = 0; j < 3; ++j) {
+        com[j] = B.com[j];
+        comv[j] = B.comv[j];
+    }
     return CC_OK;
 }
 

@@ -113,6 +113,8 @@ class CollisionSolver3d:
                               scene.bond_rest, scene.fixed)
         self.setParams(scene.params)
         self.setDomainBoundary(scene.domain[:3], scene.domain[3:])
+        for sid, b in sorted(scene.bodies.items()):
+            self.setBody(sid, b["mass"], b["com"], b["comv"])
 
     # ------------------------------------------------------------ batches
     def assembleBatch(self, meshes):
@@ -155,6 +157,8 @@ class CollisionSolver3d:
             if sc is not None:
                 self.setSceneParams(i, sc.params)
                 self.setSceneDomainBoundary(i, sc.domain[:3], sc.domain[3:])
+                for sid, b in sorted(sc.bodies.items()):
+                    self.setBody(sid, b["mass"], b["com"], b["comv"], scene=i)
 
     def numScenes(self) -> int:
         return int(self._lib.cc_num_scenes(self._h))
@@ -202,6 +206,24 @@ class CollisionSolver3d:
         """Write a .vtp of every detection pass into `directory` (None: off)."""
         d = None if directory is None else str(directory).encode()
         self._check(self._lib.cc_set_vtk_dump(self._h, d))
+
+    def setBody(self, surface: int, mass: float, com, comv, scene: int = 0):
+        """Mass, centre of mass and centre-of-mass velocity (the HYPER_SURF
+        data) of the movable rigid body formed by surface `surface`."""
+        com = np.ascontiguousarray(com, dtype=np.float64)
+        comv = np.ascontiguousarray(comv, dtype=np.float64)
+        dp = C.POINTER(C.c_double)
+        self._check(self._lib.cc_set_body(self._h, int(scene), int(surface), float(mass), com.ctypes.data_as(dp),
+                                          comv.ctypes.data_as(dp)))
+
+    def body(self, surface: int, scene: int = 0):
+        """(centre of mass, centre-of-mass velocity) of a movable body after
+        the last step (updateFinalForRG)."""
+        com, comv = np.zeros(3), np.zeros(3)
+        dp = C.POINTER(C.c_double)
+        self._check(self._lib.cc_get_body(self._h, int(scene), int(surface), com.ctypes.data_as(dp),
+                                          comv.ctypes.data_as(dp)))
+        return com, comv
 
     def setZoneCap(self, cap: int):
         """Impact-zone passes per scene and step before the loop is stopped."""

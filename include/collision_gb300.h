@@ -62,7 +62,9 @@ typedef struct {
  *   bonds         n_bonds*2 point ids
  *   bond_rest_len n_bonds rest lengths (BOND::length0, dcollid.cpp:515-516)
  *   fixed         n_points flags: 1 = point of a fixed rigid obstacle
- *                 (STATE::is_fixed, cdinit.cpp:199-202)
+ *                 (STATE::is_fixed, cdinit.cpp:199-202), 2 = point of a
+ *                 movable rigid body (STATE::is_movableRG, cdinit.cpp:204;
+ *                 see cc_set_body), 0 = free
  */
 typedef struct {
     int32_t n_points;
@@ -158,6 +160,25 @@ cc_status cc_resolve_batch_device(cc_solver* s, const double* x_old, const doubl
  * reference. Replaces the solver's per-step device state (zone roots and
  * recorded visits are kept). */
 cc_status cc_check_ccd(cc_solver* s, const double* x_old, const double* x_new, long long* hits, int* scene_hits);
+
+/* Movable rigid bodies. A point whose flag (cc_mesh.fixed) is 2 is movable
+ * (is_movableRG). Every triangle surface (a run of equal tri_surface ids)
+ * whose first point is movable is one rigid body: createImpZoneForRG
+ * (dcollid3d.cpp:54-68) makes it one impact zone at the start of each step,
+ * impulses between rigid points spread over it (SpreadImpactZoneImpulse,
+ * dcollid.cpp:1101-1115), it moves rigidly after every pass
+ * (updateImpactZoneVelocityForRG, dcollid.cpp:267-288) and its centre of
+ * mass is advanced at the end of the step (updateFinalForRG,
+ * dcollid.cpp:626-675). Its points must all be movable and belong to no
+ * other element, and every movable point must lie in such a surface
+ * (CC_BAD_INPUT otherwise). cc_set_body gives a body's HYPER_SURF data -
+ * total_mass (default 1), center_of_mass and center_of_mass_velo (default
+ * 0) - and the first call also seeds the remembered centre of mass that
+ * updateFinalForRG reads (dcollid.cpp:650). cc_get_body reads the centre of
+ * mass and its velocity after a step. `surface` is the body's tri_surface
+ * id in scene `scene`. */
+cc_status cc_set_body(cc_solver* s, int scene, int surface, double mass, const double* com, const double* comv);
+cc_status cc_get_body(cc_solver* s, int scene, int surface, double* com, double* comv);
 
 /* Impact-zone passes per scene and step before the loop is stopped
  * (default 10000). The reference's loop (dcollid.cpp:346-352) has no bound

@@ -67,6 +67,16 @@ def _rigid_bodies():
                            masses={0: 2.0, 1: 1.0})
 
 
+def _sphere12_movable():
+    # sphere12_fast with the sphere a movable body of mass 0.5: impact-zone
+    # passes (steps 5-7) with a body among the zones
+    sc = _sphere12_fast()
+    pts = np.unique(sc.tris[sc.tri_surf == 1])
+    sc.fixed[pts] = 2
+    sc.bodies = {1: dict(mass=0.5, com=sc.x[pts].mean(axis=0), comv=np.zeros(3))}
+    return sc
+
+
 def _deck_ball_plane():
     # a movable sphere rising into a free plate
     return _shift_part(scenes.deck("ball_plane", advance=0.021, sub=2, cells=20), 0, 162, (0.0013, 0.0007, 0.0))
@@ -97,6 +107,7 @@ CASES = {
     "folded17": (_folded17, 10),
     "pinned_domain": (_pinned_domain, 8),
     "rigid_bodies": (_rigid_bodies, 8),
+    "sphere12_movable": (_sphere12_movable, 8),
     "deck_ball_plane": (_deck_ball_plane, 8),
     "deck_string_slide": (_deck_string_slide, 10),
     "deck_ball_ball": (_deck_ball_ball, 8),
@@ -106,5 +117,5 @@ CASES = {
 # Cases whose fixtures keep only the outputs of each step: the inputs of step
 # k+1 are the outputs of step k (candidate positions x + dt*v, as the host
 # loop forms them), and step 0 starts from the scene.
-CHAINED = {"rigid_bodies", "deck_ball_plane", "deck_string_slide", "deck_ball_ball", "deck_string_box",
+CHAINED = {"rigid_bodies", "sphere12_movable", "deck_ball_plane", "deck_string_slide", "deck_ball_ball", "deck_string_box",
            "deck_string_string"}

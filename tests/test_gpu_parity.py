@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 
 from collision_gb300 import scenes
-from tests.gpu_util import record_sha, rel_err, scene_from_golden, zone_labels
+from tests.gpu_util import golden_inputs, record_sha, rel_err, scene_from_golden, zone_labels
 
 pytestmark = pytest.mark.gpu
 
@@ -40,7 +40,7 @@ def test_gpu_matches_reference_golden(solver_cls, path):
     s.assembleFromScene(sc)
     s.setRecording(True)
     for step in range(len(g["x"])):
-        x, v, hc = s.resolveCollision(g["x_old"][step], g["x_cand"][step], g["vel_in"][step], g["hc_in"][step])
+        x, v, hc = s.resolveCollision(*golden_inputs(g, sc, step))
         kinds = g["pass_kinds"][g["pass_kinds"][:, 0] == step][:, 1]
         assert np.array_equal(s.passKinds(), kinds), f"pass sequence differs at step {step}"
         rec = ordered_visits(s.visits())
@@ -51,6 +51,10 @@ def test_gpu_matches_reference_golden(solver_cls, path):
         assert np.array_equal(zone_labels(s.zoneRoots()), g["zones"][step])
         assert rel_err(x, g["x"][step]) <= RTOL, f"positions step {step}: {rel_err(x, g['x'][step])}"
         assert rel_err(v, g["vel"][step]) <= RTOL, f"velocities step {step}: {rel_err(v, g['vel'][step])}"
+        for i, sid in enumerate(sorted(sc.bodies)):
+            com, comv = s.body(sid)
+            assert rel_err(com, g["body_com"][step][i]) <= RTOL, f"body {sid} centre of mass, step {step}"
+            assert rel_err(comv, g["body_comv"][step][i]) <= RTOL, f"body {sid} velocity, step {step}"
     s.close()
 
 
@@ -77,6 +81,9 @@ def _oracle_run(sc, nsteps, solver_cls, record=True):
         worst[0] = max(worst[0], rel_err(xg, r["x"]))
         worst[1] = max(worst[1], rel_err(vg, r["v"]))
         assert worst[0] <= RTOL and worst[1] <= RTOL, (step, worst)
+        for sid in sorted(sc.bodies):
+            for a, b in zip(s.body(sid), o.body(sid)):
+                assert rel_err(a, b) <= RTOL, (step, sid, a, b)
         x, v, hc = r["x"], r["v"], r["has_collsn"]
     s.close()
     return worst

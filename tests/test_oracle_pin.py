@@ -21,7 +21,7 @@ GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.n
 
 
 def test_golden_present():
-    assert len(GOLDEN) >= 11
+    assert len(GOLDEN) >= 12
 
 
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
