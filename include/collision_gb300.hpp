@@ -57,6 +57,14 @@ public:
     // collid.h:203
     void setDomainBoundary(const double* L, const double* U) { check(cc_set_domain_boundary(s_, L, U), "domain"); }
 
+    // A movable rigid body's HYPER_SURF data (total_mass, center_of_mass,
+    // center_of_mass_velo) in, and after a step the centre of mass and its
+    // velocity updateFinalForRG (dcollid.cpp:626-675) wrote.
+    void setBody(int surface, double mass, const double* com, const double* comv) {
+        check(cc_set_body(s_, 0, surface, mass, com, comv), "body");
+    }
+    void body(int surface, double* com, double* comv) { check(cc_get_body(s_, 0, surface, com, comv), "body"); }
+
     // Replaces assembleFromInterface (collid.h:242): triangles of every
     // non-boundary surface, then the bonds of every string curve, in the
     // reference's hseList order (dcollid3d.cpp:25-43).
@@ -155,6 +163,12 @@ public:
         check(cc_set_scene_domain_boundary(s_, scene, L, U), "scene domain");
     }
     void setZoneCap(int cap) { check(cc_set_zone_cap(s_, cap), "zone cap"); }
+    void setBody(int scene, int surface, double mass, const double* com, const double* comv) {
+        check(cc_set_body(s_, scene, surface, mass, com, comv), "body");
+    }
+    void body(int scene, int surface, double* com, double* comv) {
+        check(cc_get_body(s_, scene, surface, com, comv), "body");
+    }
     void setSceneEnabled(int scene, bool on) { check(cc_set_scene_enabled(s_, scene, on ? 1 : 0), "enable"); }
 
     // resolveCollision on every scene (host arrays over all points). Returns
