@@ -242,6 +242,11 @@ def run_gpu(args):
     def max_over_ranks(ms):
         return mor(ms, device=dev)
 
+    def apply_tuning(s):
+        for kv in args.tune:
+            k, v = kv.split("=")
+            s.setTuning(getattr(CollisionSolver3d, "TUNE_" + k.strip().upper()), int(v))
+
     # ------------------------------------------- batched, device-resident
     def drop_capped(s, enabled):
         for q in np.nonzero(s.sceneStatus())[0]:
@@ -251,6 +256,7 @@ def run_gpu(args):
     def batched_run(mode, check):
         s = CollisionSolver3d(dev)
         s.assembleBatch(scs)
+        apply_tuning(s)
         s.setMode(mode)
         s.setZoneCap(args.zone_cap)
         s.setStream(stream.cuda_stream)
@@ -300,6 +306,7 @@ def run_gpu(args):
         for sc in scs:
             s = CollisionSolver3d(dev)
             s.assembleFromScene(sc)
+            apply_tuning(s)
             s.setMode(0)
             s.setZoneCap(args.zone_cap)
             s.setStream(stream.cuda_stream)
@@ -352,6 +359,7 @@ def run_gpu(args):
     def e2e_run():
         s2 = CollisionSolver3d(dev)
         s2.assembleBatch(scs)
+        apply_tuning(s2)
         s2.setMode(1)
         s2.setZoneCap(args.zone_cap)
         s2.setStream(stream.cuda_stream)
@@ -404,6 +412,7 @@ def run_gpu(args):
         must be equal bit for bit."""
         s = CollisionSolver3d(dev)
         s.assembleFromScene(scs[0])
+        apply_tuning(s)
         s.setZoneCap(args.zone_cap)
         s.setStream(stream.cuda_stream)
         s.setMode(1)
@@ -571,6 +580,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--tune", action="append", default=[], metavar="KNOB=VALUE",
+                    help="set a tuning knob on every solver, e.g. STRAIN_BLOCK=128 (names: CollisionSolver3d.TUNE_*)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -231,6 +231,7 @@ struct StrainPlan {
     bool warp;             // one warp per scene with staged levels (k_strain_warp)
     int ecap, lcap, wcap;  // most edges, copy-ins, write-backs of one level (scenes that fit)
     size_t warp_smem;      // its dynamic shared memory
+    const int* order;      // device: scene of each sweep CTA, most levels first
 };
 // Dynamic shared memory of the one-warp sweep for these sizes.
 size_t strain_warp_smem(int max_slots, int ecap, int lcap, int wcap);
@@ -246,7 +247,7 @@ size_t strain_step_bytes(int nedges);
 void strain_limit(const StrainEdge* edges, int nedges, const int4* hdr, const int2* load_list, const int2* wb_list,
                   const int2* chunks, int nchunks, const SceneDev* scenes, int nscenes, const StrainPlan& plan,
                   const double4_32a* xo, double4_32a* av, void* step_buf, int* flags, int* passes_out,
-                  cudaStream_t s);
+                  const int* vscene, cudaStream_t s);
 // Correctly rounded cos/sin/acos/pow (fn 0..3) on device arrays, for self-tests.
 void math_selftest(int fn, const double* a, const double* b, double* out, int n, cudaStream_t s);
 // updateFinalVelocity.

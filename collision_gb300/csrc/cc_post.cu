@@ -364,11 +364,9 @@ struct __align__(16) StrainEdgeHot {
 
 // Per-step set-up of the strain sweep: the start-of-step length of every
 // edge (x_old does not change during the sweep) and both sets of bounds.
-__global__ void k_strain_setup(const StrainEdge* __restrict__ edges, int m, const double4_32a* __restrict__ xo,
-                               StrainEdgeStep* out, StrainEdgeHot* hot) {
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= m) return;
-    StrainEdge ed = edges[e];
+// An edge's full record for the step, from its endpoints' x_old: the
+// exact test's inputs and the FP32 view of the window sweep.
+__device__ __forceinline__ StrainEdgeStep strain_step(const StrainEdge& ed, const double4_32a* __restrict__ xo) {
     double x0[3], x1[3];
     load3(xo, ed.p0, x0);
     load3(xo, ed.p1, x1);
@@ -399,7 +397,20 @@ __global__ void k_strain_setup(const StrainEdge* __restrict__ edges, int m, cons
     r.under_hi = __double2float_rd(hno);
     r.under_lo = __double2float_ru(lno);
     r.pad2[0] = r.pad2[1] = 0.f;
-    out[e] = r;
+    return r;
+}
+
+// Per step: every edge's 48-byte hot record; the full record only for the
+// edges of scenes swept by k_strain (too many slots for shared memory) - the
+// shared-memory sweeps rebuild it for their rare exact tests.
+__global__ void k_strain_setup(const StrainEdge* __restrict__ edges, int m, const double4_32a* __restrict__ xo,
+                               StrainEdgeStep* out, StrainEdgeHot* hot, const int* __restrict__ vscene,
+                               const SceneDev* __restrict__ scenes, int slot_cap) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= m) return;
+    const StrainEdge ed = edges[e];
+    const StrainEdgeStep r = strain_step(ed, xo);
+    if (slot_cap < 0 || scenes[vscene[ed.p0]].strain_slots > slot_cap) out[e] = r;
     StrainEdgeHot hh;
     hh.s0 = r.s0;
     hh.s1 = r.s1;
@@ -491,8 +502,9 @@ __device__ __forceinline__ void sweep_done(int pass, int s, int n_avg, int n_exa
 __global__ void __launch_bounds__(256) k_strain(const StrainEdgeStep* __restrict__ edges,
                                                 const int4* __restrict__ hdr_all,
                                                 const SceneDev* __restrict__ scenes, int slot_cap,
-                                                double4_32a* av, int pass, int* flags, int* passes_out_all) {
-    const int sc = blockIdx.x;
+                                                double4_32a* av, int pass, int* flags, int* passes_out_all,
+                                                const int* __restrict__ order) {
+    const int sc = order[blockIdx.x];
     const SceneDev& sd = scenes[sc];
     if ((slot_cap >= 0 && sd.strain_slots <= slot_cap) || !sd.enabled) return;  // k_strain_window's, or left out
     if (!sweep_gate(pass, sc, flags, passes_out_all)) return;
@@ -593,7 +605,8 @@ __device__ __forceinline__ int strain_decide32(const StrainEdgeHot& ed, float4 f
 }
 
 __device__ __forceinline__ void strain_window_edge(const StrainEdgeHot& h, int e,
-                                                   const StrainEdgeStep* __restrict__ edges, WinSlot* s_win,
+                                                   const StrainEdge* __restrict__ edges,
+                                                   const double4_32a* __restrict__ xo, WinSlot* s_win,
                                                    float dt32, double dt, int* n_avg, int* n_exact, bool* has) {
     WinSlot& w0 = s_win[h.s0];
     WinSlot& w1 = s_win[h.s1];
@@ -602,7 +615,7 @@ __device__ __forceinline__ void strain_window_edge(const StrainEdgeHot& h, int e
     double2 a0 = w0.a, a1 = w0.b, b0 = w1.a, b1 = w1.b;
     double v0[3] = {a0.x, a0.y, a1.x}, v1[3] = {b0.x, b0.y, b1.x};
     if (q < 0) {
-        StrainEdgeStep full = edges[e];
+        const StrainEdgeStep full = strain_step(edges[e], xo);
         if (!strain_flag_vals(full, v0, v1, dt, n_exact)) return;
     }
     ++*n_avg;
@@ -647,7 +660,8 @@ __device__ __forceinline__ void win_fetch(WinRing& r, int j, int lk, int nlevels
 }
 
 struct WinArgs {
-    const StrainEdgeStep* edges;
+    const StrainEdge* edges;
+    const double4_32a* xo;
     const StrainEdgeHot* hot;
     const int4* hdr;
     int nlevels;
@@ -656,6 +670,7 @@ struct WinArgs {
     double4_32a* av;
     double dt;
     float dt32;
+    int multi_ld;  // some level has more copy-ins than the block has threads
 };
 
 // One level of the window sweep; J = level mod kWindowAhead.
@@ -702,10 +717,12 @@ __device__ __forceinline__ void win_level(const WinArgs& A, WinRing& r, WinSlot*
     if (cl >= 0 && cslot >= 0) {
         WinSlot& w = s_win[cslot];
         w.f = make_float4((float)w.a.x, (float)w.a.y, (float)w.b.x, 0.f);
-        int4 hc = A.hdr[2 * cl];
-        for (int i = hc.z + tid + (int)blockDim.x; i < hc.w; i += blockDim.x) {
-            WinSlot& w2 = s_win[A.load_list[i].y];
-            w2.f = make_float4((float)w2.a.x, (float)w2.a.y, (float)w2.b.x, 0.f);
+        if (A.multi_ld) {  // the copy-ins past the first per thread (a dependent load: only when needed)
+            int4 hc = A.hdr[2 * cl];
+            for (int i = hc.z + tid + (int)blockDim.x; i < hc.w; i += blockDim.x) {
+                WinSlot& w2 = s_win[A.load_list[i].y];
+                w2.f = make_float4((float)w2.a.x, (float)w2.a.y, (float)w2.b.x, 0.f);
+            }
         }
     }
     __syncthreads();
@@ -721,22 +738,24 @@ __device__ __forceinline__ void win_level(const WinArgs& A, WinRing& r, WinSlot*
     }
     int e = h0.x + tid;
     if (e < h0.y) {
-        strain_window_edge(cur, e, A.edges, s_win, A.dt32, A.dt, n_avg, n_exact, has);
+        strain_window_edge(cur, e, A.edges, A.xo, s_win, A.dt32, A.dt, n_avg, n_exact, has);
         for (e += blockDim.x; e < h0.y; e += blockDim.x)
-            strain_window_edge(A.hot[e], e, A.edges, s_win, A.dt32, A.dt, n_avg, n_exact, has);
+            strain_window_edge(A.hot[e], e, A.edges, A.xo, s_win, A.dt32, A.dt, n_avg, n_exact, has);
     }
 }
 
-__global__ void __launch_bounds__(256) k_strain_window(const StrainEdgeStep* __restrict__ edges,
+__global__ void __launch_bounds__(256) k_strain_window(const StrainEdge* __restrict__ edges,
+                                                       const double4_32a* __restrict__ xo,
                                                        const StrainEdgeHot* __restrict__ hot,
                                                        const int4* __restrict__ hdr_all,
                                                        const SceneDev* __restrict__ scenes, int slot_cap,
                                                        const int2* __restrict__ load_list,
                                                        const int2* __restrict__ wb_list,
                                                        double4_32a* av, int pass, int* flags,
-                                                       int* passes_out_all) {
+                                                       int* passes_out_all, int multi_ld,
+                                                       const int* __restrict__ order) {
     extern __shared__ WinSlot s_win[];
-    const int sc = blockIdx.x;
+    const int sc = order[blockIdx.x];
     const SceneDev& sd = scenes[sc];
     if (sd.strain_slots > slot_cap || !sd.enabled) return;  // k_strain's, or left out
     if (!sweep_gate(pass, sc, flags, passes_out_all)) return;
@@ -745,7 +764,7 @@ __global__ void __launch_bounds__(256) k_strain_window(const StrainEdgeStep* __r
     const int2 wb_final = make_int2(sd.wb_final0, sd.wb_final1);
     const double dt = sd.p.dt;
     const int tid = threadIdx.x;
-    WinArgs A{edges, hot, hdr, nlevels, load_list, wb_list, av, dt, __double2float_ru(dt)};
+    WinArgs A{edges, xo, hot, hdr, nlevels, load_list, wb_list, av, dt, __double2float_ru(dt), multi_ld};
     int n_avg = 0, n_exact = 0;
     bool has = false;
     WinRing r;
@@ -793,16 +812,17 @@ struct WarpSlot {
     double2 a, b;  // x y | z -
 };
 
-__global__ void __launch_bounds__(32) k_strain_warp(const StrainEdgeStep* __restrict__ edges,
+__global__ void __launch_bounds__(32) k_strain_warp(const StrainEdge* __restrict__ edges,
+                                                    const double4_32a* __restrict__ xo,
                                                     const StrainEdgeHot* __restrict__ hot,
                                                     const int4* __restrict__ hdr_all,
                                                     const SceneDev* __restrict__ scenes, int slot_cap,
                                                     const int2* __restrict__ load_list,
                                                     const int2* __restrict__ wb_list, double4_32a* av, int pass,
                                                     int* flags, int* passes_out_all, int max_slots, int ecap,
-                                                    int lcap, int wcap) {
+                                                    int lcap, int wcap, const int* __restrict__ order) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int sc = blockIdx.x;
+    const int sc = order[blockIdx.x];
     const SceneDev& sd = scenes[sc];
     if (sd.strain_slots > slot_cap || !sd.enabled) return;  // k_strain's, or left out
     if (!sweep_gate(pass, sc, flags, passes_out_all)) return;
@@ -876,7 +896,7 @@ __global__ void __launch_bounds__(32) k_strain_warp(const StrainEdgeStep* __rest
                                     make_float4((float)b0.x, (float)b0.y, (float)b1.x, 0.f), dt32);
             if (q == 0) continue;
             double v0[3] = {a0.x, a0.y, a1.x}, v1[3] = {b0.x, b0.y, b1.x};
-            if (q < 0 && !strain_flag_vals(edges[h0.x + i], v0, v1, dt, &n_exact)) continue;
+            if (q < 0 && !strain_flag_vals(strain_step(edges[h0.x + i], xo), v0, v1, dt, &n_exact)) continue;
             ++n_avg;
             double t[3];
             for (int k = 0; k < 3; ++k) {
@@ -899,33 +919,39 @@ __global__ void __launch_bounds__(32) k_strain_warp(const StrainEdgeStep* __rest
     sweep_done(pass, sc, n_avg, n_exact, flags, passes_out_all);
 }
 
-// Would any edge of the chunk average on the current velocities? (One
-// block per chunk of at most 256 edges of one scene.) If none of a scene's
+// Would any edge of the chunk average on the current velocities? (A block
+// per chunk of at most 256 edges of one scene, the grid striding over the
+// chunks; chunks of finished scenes, or of scenes where an averaging edge is
+// already found, are skipped.) If none of a scene's
 // edges would, its sweep changes nothing: before the first edge that
 // averages every edge sees the start-of-pass velocities.
-__global__ void __launch_bounds__(256) k_strain_check(const StrainEdgeStep* __restrict__ edges,
+__global__ void __launch_bounds__(256) k_strain_check(const StrainEdge* __restrict__ edges,
+                                                      const double4_32a* __restrict__ xo,
                                                       const StrainEdgeHot* __restrict__ hot,
-                                                      const int2* __restrict__ chunks,
+                                                      const int2* __restrict__ chunks, int nchunks,
                                                       const SceneDev* __restrict__ scenes,
                                                       const double4_32a* __restrict__ av, int* flags) {
-    const int2 ch = chunks[blockIdx.x];  // (scene, first edge)
-    const SceneDev& sd = scenes[ch.x];
-    if (!sd.enabled || flags[2 * ch.x + 1]) return;
-    const int end = sd.strain_e0 + sd.strain_ne;
-    const int e = ch.y + threadIdx.x;
-    if (e >= end) return;
-    const StrainEdgeHot h = hot[e];
-    const int2 pp = *reinterpret_cast<const int2*>(&edges[e]);  // p0, p1
-    const double4_32a a0 = av[pp.x], a1 = av[pp.y];
-    const float dt32 = __double2float_ru(sd.p.dt);
-    int q = strain_decide32(h, make_float4((float)a0.x, (float)a0.y, (float)a0.z, 0.f),
-                            make_float4((float)a1.x, (float)a1.y, (float)a1.z, 0.f), dt32);
-    if (q < 0) {
-        double v0[3] = {a0.x, a0.y, a0.z}, v1[3] = {a1.x, a1.y, a1.z};
-        int n_exact = 0;
-        q = strain_flag_vals(edges[e], v0, v1, sd.p.dt, &n_exact) ? 1 : 0;
+    for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const int2 ch = chunks[c];  // (scene, first edge)
+        const SceneDev& sd = scenes[ch.x];
+        // done scenes, and scenes where an edge that averages is already found
+        if (!sd.enabled || flags[2 * ch.x + 1] || *(volatile int*)&flags[2 * ch.x]) continue;
+        const int end = sd.strain_e0 + sd.strain_ne;
+        const int e = ch.y + threadIdx.x;
+        if (e >= end) continue;
+        const StrainEdgeHot h = hot[e];
+        const int2 pp = *reinterpret_cast<const int2*>(&edges[e]);  // p0, p1
+        const double4_32a a0 = av[pp.x], a1 = av[pp.y];
+        const float dt32 = __double2float_ru(sd.p.dt);
+        int q = strain_decide32(h, make_float4((float)a0.x, (float)a0.y, (float)a0.z, 0.f),
+                                make_float4((float)a1.x, (float)a1.y, (float)a1.z, 0.f), dt32);
+        if (q < 0) {
+            double v0[3] = {a0.x, a0.y, a0.z}, v1[3] = {a1.x, a1.y, a1.z};
+            int n_exact = 0;
+            q = strain_flag_vals(strain_step(edges[e], xo), v0, v1, sd.p.dt, &n_exact) ? 1 : 0;
+        }
+        if (q > 0 && !flags[2 * ch.x]) atomicOr(&flags[2 * ch.x], 1);
     }
-    if (q > 0 && !flags[2 * ch.x]) atomicOr(&flags[2 * ch.x], 1);
 }
 
 __global__ void k_final_velocity(const uint8_t* __restrict__ in_elem, const uint8_t* __restrict__ has_collsn,
@@ -1049,27 +1075,33 @@ void strain_configure() {
 void strain_limit(const StrainEdge* edges, int nedges, const int4* hdr, const int2* load_list, const int2* wb_list,
                   const int2* chunks, int nchunks, const SceneDev* scenes, int nscenes, const StrainPlan& plan,
                   const double4_32a* xo, double4_32a* av, void* step_buf, int* flags, int* passes_out,
-                  cudaStream_t s) {
+                  const int* vscene, cudaStream_t s) {
     if (nscenes <= 0) return;
     StrainEdgeStep* se = (StrainEdgeStep*)step_buf;
     StrainEdgeHot* hot = (StrainEdgeHot*)(se + (nedges > 0 ? nedges : 1));
     cudaMemsetAsync(flags, 0, sizeof(int) * 2 * (size_t)nscenes, s);
     cudaMemsetAsync(passes_out, 0, sizeof(int) * 3 * (size_t)nscenes, s);
-    if (nedges > 0) count_launch(), k_strain_setup<<<nblk(nedges, 256), 256, 0, s>>>(edges, nedges, xo, se, hot);
     // scenes with at most `cap` slots are swept in shared memory (cap -1: none)
     int cap = plan.window ? strain_window_slot_cap() : -1;
+    if (nedges > 0)
+        count_launch(), k_strain_setup<<<nblk(nedges, 256), 256, 0, s>>>(edges, nedges, xo, se, hot, vscene, scenes,
+                                                                         cap);
     size_t smem = (size_t)plan.max_window_slots * sizeof(WinSlot);
     for (int pass = 0; pass < kStrainMaxIter; ++pass) {
-        if (nchunks > 0) count_launch(), k_strain_check<<<nchunks, 256, 0, s>>>(se, hot, chunks, scenes, av, flags);
+        if (nchunks > 0)
+            count_launch(), k_strain_check<<<nchunks < 152 * 8 ? nchunks : 152 * 8, 256, 0, s>>>(
+                edges, xo, hot, chunks, nchunks, scenes, av, flags);
         if (plan.window && plan.warp)
             count_launch(), k_strain_warp<<<nscenes, 32, plan.warp_smem, s>>>(
-                se, hot, hdr, scenes, cap, load_list, wb_list, av, pass, flags, passes_out, plan.max_window_slots,
-                plan.ecap, plan.lcap, plan.wcap);
+                edges, xo, hot, hdr, scenes, cap, load_list, wb_list, av, pass, flags, passes_out, plan.max_window_slots,
+                plan.ecap, plan.lcap, plan.wcap, plan.order);
         else if (plan.window)
-            count_launch(), k_strain_window<<<nscenes, plan.block, smem, s>>>(se, hot, hdr, scenes, cap, load_list,
-                                                                              wb_list, av, pass, flags, passes_out);
+            count_launch(), k_strain_window<<<nscenes, plan.block, smem, s>>>(
+                edges, xo, hot, hdr, scenes, cap, load_list, wb_list, av, pass, flags, passes_out, plan.lcap > plan.block,
+                plan.order);
         if (!plan.window || plan.any_global)
-            count_launch(), k_strain<<<nscenes, 256, 0, s>>>(se, hdr, scenes, cap, av, pass, flags, passes_out);
+            count_launch(), k_strain<<<nscenes, 256, 0, s>>>(se, hdr, scenes, cap, av, pass, flags, passes_out,
+                                                             plan.order);
     }
 }
 

@@ -252,6 +252,7 @@ struct cc_solver {
     int* d_strain_passes = nullptr;  // 3 per scene
     int* d_strain_flags = nullptr;   // 2 per scene
     int2* d_strain_chunks = nullptr; // (scene, first edge) per run of <= 256 edges
+    int* d_strain_order = nullptr;   // scenes by strain levels, most first (one sweep CTA each)
     int n_strain_chunks = 0;
     std::vector<int> h_strain_passes;
 
@@ -422,7 +423,7 @@ struct cc_solver {
         clear_tail_graphs();
         dfree(d_ev); dfree(d_esurf); dfree(d_erigid); dfree(d_fixed); dfree(d_in_elem); dfree(d_edges);
         dfree(d_strain_hdr); dfree(d_strain_load); dfree(d_strain_wb); dfree(d_strain_passes);
-        dfree(d_strain_flags); dfree(d_strain_chunks);
+        dfree(d_strain_flags); dfree(d_strain_chunks); dfree(d_strain_order);
         n_strain_chunks = 0;
         if (d_strain_step) cudaFree(d_strain_step);
         d_strain_step = nullptr;
@@ -604,7 +605,7 @@ struct cc_solver {
     void tail_after_finalize(double* vel, uint8_t* hc) {
         strain_limit(d_edges, nedges, d_strain_hdr, d_strain_load, d_strain_wb, d_strain_chunks, n_strain_chunks,
                      d_scenes, nscenes, strain_plan(), d_xo, d_av, d_strain_step, d_strain_flags, d_strain_passes,
-                     stream);
+                     d_vscene, stream);
         final_velocity(d_in_elem, d_hc, d_av, d_vscene, d_scenes, vel, nv, stream);
         if (hc != d_hc) cudaMemcpyAsync(hc, d_hc, (size_t)nv, cudaMemcpyDeviceToDevice, stream);
     }
@@ -712,7 +713,7 @@ struct cc_solver {
     }
 
     StrainPlan strain_plan() const {
-        StrainPlan pl{strain_window, 0, false, tune.strain_block, false, 0, 0, 0, 0};
+        StrainPlan pl{strain_window, 0, false, tune.strain_block, false, 0, 0, 0, 0, d_strain_order};
         int cap = strain_window_slot_cap();
         for (int s = 0; s < nscenes; ++s) {
             const SceneDev& sd = h_scenes[s];
@@ -935,6 +936,7 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     ok &= dalloc(&d_strain_passes, 3 * (size_t)n) == cudaSuccess;
     ok &= dalloc(&d_strain_flags, 2 * (size_t)n) == cudaSuccess;
     ok &= dalloc(&d_strain_chunks, chunks.size()) == cudaSuccess;
+    ok &= dalloc(&d_strain_order, (size_t)n) == cudaSuccess;
     n_strain_chunks = (int)chunks.size();
     ok &= cudaMalloc(&d_strain_step, strain_step_bytes(nedges)) == cudaSuccess;
     ok &= dalloc(&d_xo, (size_t)nv) == cudaSuccess;
@@ -1008,6 +1010,15 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
         cudaMemcpyAsync(d_strain_hdr, hdr.data(), sizeof(int4) * hdr.size(), cudaMemcpyHostToDevice, stream);
     if (!chunks.empty())
         cudaMemcpyAsync(d_strain_chunks, chunks.data(), sizeof(int2) * chunks.size(), cudaMemcpyHostToDevice, stream);
+    {
+        // the sweep of a scene is a chain of its levels: the longest chains
+        // start first, so none waits for a second wave of CTAs
+        std::vector<int> order((size_t)n);
+        for (int i = 0; i < n; ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int a, int b) { return h_scenes[a].strain_levels > h_scenes[b].strain_levels; });
+        cudaMemcpy(d_strain_order, order.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice);
+    }
     if (!load.empty()) {
         cudaMemcpyAsync(d_strain_load, load.data(), sizeof(int2) * load.size(), cudaMemcpyHostToDevice, stream);
         cudaMemcpyAsync(d_strain_wb, wb.data(), sizeof(int2) * wb.size(), cudaMemcpyHostToDevice, stream);
