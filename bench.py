@@ -513,8 +513,16 @@ def run_gpu(args):
     ms, calls = prof.get("strain", (0.0, 0))
     if calls:
         per = tot["strain_bytes"] / calls
-        kern["strain"] = {"kernel": "k_strain_window (strain sweep, one CTA per scene)", "bytes_per_launch": per,
+        kern["strain"] = {"kernel": "strain stage: k_strain_setup, k_strain_check and k_strain_window sweeps "
+                          "(one CTA per scene), one launch = one step's tail graph", "bytes_per_launch": per,
                           "ms_per_launch": ms / calls, "achieved": per / (ms / calls / 1e3) / 1e9}
+    ms, calls = prof.get("traverse", (0.0, 0))
+    if calls and tot.get("broad_leaves"):
+        # one read of the hierarchy's FP32 boxes per traversal, (2n-1)*24 B
+        # for n leaves, and the 8-byte pairs written
+        per = (48.0 * tot["broad_leaves"] + 8.0 * tot["broad_pairs"]) / calls
+        kern["traverse"] = {"kernel": "k_traverse (LBVH broad phase, with its leaf records)", "bytes_per_launch": per,
+                            "ms_per_launch": ms / calls, "achieved": per / (ms / calls / 1e3) / 1e9}
     roof = None
     if kern:
         top = max(kern, key=lambda k: prof[k][0])

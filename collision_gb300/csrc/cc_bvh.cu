@@ -279,6 +279,10 @@ __device__ __forceinline__ unsigned long long ord_double(unsigned long long u) {
     if (u == 0x8000000000000000ull) u = 0;
     return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
 }
+// The double ord_double encodes (-0.0 comes back as +0.0).
+__device__ __forceinline__ double unord_double(unsigned long long o) {
+    return __longlong_as_double((long long)((o & 0x8000000000000000ull) ? (o & 0x7fffffffffffffffull) : ~o));
+}
 struct BoxOrd {
     unsigned long long lo[3], hi[3];
 };
@@ -318,28 +322,175 @@ __device__ __forceinline__ void emit_pair(int a, int b, int2* pairs, int cap, Pa
 // idle in this pass report nothing. With ev given, pairs of elements that
 // share a point are dropped: every narrow-phase test of such a pair returns
 // false before any arithmetic (dcollid3d.cpp:493-497, 541-546, 578-582).
+// The leaf records of one pass (see LeafRec).
+__global__ void k_leaf_records(const Box6* __restrict__ box, const unsigned int* __restrict__ order, int n,
+                               const int* __restrict__ ev, LeafRec* out, int ne_all, PassCounters* ctr) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int e = (int)order[j];
+    if (e < 0 || e >= ne_all) {
+        atomicOr(&ctr->err, kErrIndexElem);
+        LeafRec r = {};
+        r.e = -1;  // tested by nobody: the traversal skips it
+        out[j] = r;
+        return;
+    }
+    const BoxOrd o = box_ord(box[e]);
+    LeafRec r;
+    for (int d = 0; d < 3; ++d) {
+        r.lo[d] = o.lo[d];
+        r.hi[d] = o.hi[d];
+    }
+    r.p[0] = ev[3 * e];
+    r.p[1] = ev[3 * e + 1];
+    r.p[2] = ev[3 * e + 2];
+    r.e = e;
+    out[j] = r;
+}
+
+// The same pairs from a warp-cooperative traversal. The 32 lanes of a warp
+// hold 32 consecutive sorted leaves - neighbours in Morton order, so their
+// paths through the tree mostly coincide - and walk the tree as one packet:
+// one node record per step, read once for the warp, a stack per warp in
+// shared memory, and a child pushed when the ballot of the lanes whose query
+// box overlaps it (and that have leaves after theirs below it) is not
+// empty. Leaves reached are tested exactly by the lanes that overlap them.
+// Lanes of different scenes (different subtree roots) walk in turn.
+constexpr int kPacketWarps = 8;
+__global__ void __launch_bounds__(kPacketWarps * 32) k_traverse_packet(
+    const unsigned int* __restrict__ order, int n, const BvhNode32* __restrict__ node,
+    const int* __restrict__ elem_scene, const SceneRun* __restrict__ run, const int* __restrict__ ev, int2* pairs,
+    int cap, PassCounters* ctr, const Box6* __restrict__ box_static, const LeafRec* __restrict__ leaves) {
+    __shared__ int s_stack[kPacketWarps][kTraversalStack];
+    int* stk = s_stack[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool want = i < n - 1;
+    int ei = -1, root = -1, pi0 = -1, pi1 = -1, pi2 = -1;
+    Box32 q32;
+    BoxOrd qo, qs;
+    if (want) {
+        const LeafRec r = leaves[i];
+        ei = r.e;
+        if (ei < 0) want = false;
+        Box6 q;
+        for (int d = 0; d < 3; ++d) {
+            qo.lo[d] = r.lo[d];
+            qo.hi[d] = r.hi[d];
+            q.lo[d] = unord_double(r.lo[d]);
+            q.hi[d] = unord_double(r.hi[d]);
+        }
+        q32 = box32_out(q);
+        if (ev) pi0 = r.p[0], pi1 = r.p[1], pi2 = r.p[2];
+        root = 0;
+        if (want && run) {
+            const SceneRun sr = run[elem_scene[ei]];
+            if (sr.mode == kSceneIdle || sr.root < 0) want = false;
+            root = sr.root;
+        }
+        if (want && root >= n - 1) {
+            atomicOr(&ctr->err, kErrIndexNode);
+            want = false;
+        }
+        if (want && box_static) qs = box_ord(box_static[ei]);
+    }
+    unsigned todo = __ballot_sync(0xffffffffu, want);
+    while (todo) {
+        // this round: the lanes that share the first remaining lane's root
+        const int r0 = __shfl_sync(0xffffffffu, root, __ffs(todo) - 1);
+        const bool mine = want && root == r0;
+        const unsigned in_round = __ballot_sync(0xffffffffu, mine);
+        todo &= ~in_round;
+        int sp = 1;
+        if (lane == 0) stk[0] = r0;
+        __syncwarp();
+        while (sp > 0) {
+            const int nd_id = stk[--sp];  // checked when pushed: in [0, n-1)
+            const float4* r4 = reinterpret_cast<const float4*>(&node[nd_id]);
+            Box32 cb[2];
+            unpack(__ldg(r4), __ldg(r4 + 1), __ldg(r4 + 2), cb[0], cb[1]);
+            const int4 meta = __ldg(reinterpret_cast<const int4*>(r4 + 3));
+            const int cs[2] = {meta.x, meta.y}, last[2] = {meta.z, meta.w};
+            __syncwarp();  // every lane has read the top before it is overwritten
+            for (int k = 0; k < 2; ++k) {
+                const bool hit = mine && last[k] > i && overlap32(q32, cb[k]);
+                if (!__any_sync(0xffffffffu, hit)) continue;
+                const int c = cs[k];
+                if (c < 0) {
+                    if (!hit) continue;
+                    if (~c >= n) {
+                        atomicOr(&ctr->err, kErrIndexLeaf);
+                        continue;
+                    }
+                    const ulonglong2* lr = reinterpret_cast<const ulonglong2*>(&leaves[~c]);
+                    const ulonglong2 u0 = __ldg(lr), u1 = __ldg(lr + 1), u2 = __ldg(lr + 2);
+                    const int4 pe = __ldg(reinterpret_cast<const int4*>(lr + 3));
+                    if (!(qo.lo[0] <= u1.y && qo.hi[0] >= u0.x && qo.lo[1] <= u2.x && qo.hi[1] >= u0.y &&
+                          qo.lo[2] <= u2.y && qo.hi[2] >= u1.x))
+                        continue;
+                    if (ev && (pe.x == pi0 || pe.x == pi1 || pe.x == pi2 || pe.y == pi0 || pe.y == pi1 ||
+                               pe.y == pi2 || (pe.z >= 0 && (pe.z == pi0 || pe.z == pi1 || pe.z == pi2))))
+                        continue;
+                    const int ej = pe.w;
+                    if (ej < 0) continue;  // flagged by k_leaf_records
+                    emit_pair(ei, (box_static && overlap_ord(qs, &box_static[ej])) ? (ej | kPairStatic) : ej, pairs,
+                              cap, ctr);
+                } else if (c >= n - 1) {
+                    if (lane == 0) atomicOr(&ctr->err, kErrIndexNode);
+                } else if (sp < kTraversalStack) {
+                    if (lane == 0) stk[sp] = c;
+                    ++sp;
+                } else {
+                    if (lane == 0) atomicOr(&ctr->err, kErrStack);
+                }
+            }
+            __syncwarp();  // pushes are visible before the next pop
+        }
+    }
+}
+
 __global__ void k_traverse(const Box6* __restrict__ box, const unsigned int* __restrict__ order, int n,
                            const BvhNode32* __restrict__ node, const int* __restrict__ elem_scene,
                            const SceneRun* __restrict__ run, const int* __restrict__ ev, int2* pairs, int cap,
-                           PassCounters* ctr, const Box6* __restrict__ box_static) {
+                           PassCounters* ctr, const Box6* __restrict__ box_static,
+                           const LeafRec* __restrict__ leaves) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
-    int ei = (int)order[i];
+    int ei, pi0 = -1, pi1 = -1, pi2 = -1;
+    Box6 q;
+    BoxOrd qo;
+    if (leaves) {  // the query's own record: a coalesced load
+        const LeafRec r = leaves[i];
+        ei = r.e;
+        if (ei < 0) return;  // flagged by k_leaf_records
+        for (int d = 0; d < 3; ++d) {
+            qo.lo[d] = r.lo[d];
+            qo.hi[d] = r.hi[d];
+            q.lo[d] = unord_double(r.lo[d]);
+            q.hi[d] = unord_double(r.hi[d]);
+        }
+        if (ev) pi0 = r.p[0], pi1 = r.p[1], pi2 = r.p[2];  // -1 for a bond: matches no point
+    } else {
+        ei = (int)order[i];
+        if (ev) {
+            pi0 = ev[3 * ei];
+            pi1 = ev[3 * ei + 1];
+            pi2 = ev[3 * ei + 2];
+        }
+        q = box[ei];
+        qo = box_ord(q);
+    }
     int root = 0;
     if (run) {
         SceneRun r = run[elem_scene[ei]];
         if (r.mode == kSceneIdle || r.root < 0) return;
         root = r.root;
+        if (root >= n - 1) {
+            atomicOr(&ctr->err, kErrIndexNode);
+            return;
+        }
     }
-    int pi0 = -1, pi1 = -1, pi2 = -1;
-    if (ev) {
-        pi0 = ev[3 * ei];
-        pi1 = ev[3 * ei + 1];
-        pi2 = ev[3 * ei + 2];  // -1 for a bond: matches no point
-    }
-    const Box6 q = box[ei];
     const Box32 q32 = box32_out(q);
-    const BoxOrd qo = box_ord(q);
     BoxOrd qs;
     if (box_static) qs = box_ord(box_static[ei]);
     int stk[kTraversalStack];
@@ -357,17 +508,36 @@ __global__ void k_traverse(const Box6* __restrict__ box, const unsigned int* __r
             if (last[k] <= i || !overlap32(q32, cb[k])) continue;
             int c = cs[k];
             if (c < 0) {
-                int ej = (int)order[~c];
-                if (!overlap_ord(qo, &box[ej])) continue;  // the exact test
+                int ej, a, b, c3;
+                if (~c >= n) {
+                    atomicOr(&ctr->err, kErrIndexLeaf);
+                    continue;
+                }
+                if (leaves) {
+                    const ulonglong2* lr = reinterpret_cast<const ulonglong2*>(&leaves[~c]);
+                    const ulonglong2 u0 = __ldg(lr), u1 = __ldg(lr + 1), u2 = __ldg(lr + 2);
+                    const int4 pe = __ldg(reinterpret_cast<const int4*>(lr + 3));
+                    // the exact test on the encoded boxes
+                    if (!(qo.lo[0] <= u1.y && qo.hi[0] >= u0.x && qo.lo[1] <= u2.x && qo.hi[1] >= u0.y &&
+                          qo.lo[2] <= u2.y && qo.hi[2] >= u1.x))
+                        continue;
+                    ej = pe.w;
+                    if (ej < 0) continue;  // flagged by k_leaf_records
+                    a = pe.x, b = pe.y, c3 = pe.z;
+                } else {
+                    ej = (int)order[~c];
+                    if (!overlap_ord(qo, &box[ej])) continue;  // the exact test
+                    if (ev) a = ev[3 * ej], b = ev[3 * ej + 1], c3 = ev[3 * ej + 2];
+                }
                 bool shared = false;
-                if (ev) {
-                    int a = ev[3 * ej], b = ev[3 * ej + 1], c3 = ev[3 * ej + 2];
+                if (ev)
                     shared = a == pi0 || a == pi1 || a == pi2 || b == pi0 || b == pi1 || b == pi2 ||
                              (c3 >= 0 && (c3 == pi0 || c3 == pi1 || c3 == pi2));
-                }
                 if (!shared)
                     emit_pair(ei, (box_static && overlap_ord(qs, &box_static[ej])) ? (ej | kPairStatic) : ej, pairs,
                               cap, ctr);
+            } else if (c >= n - 1) {
+                atomicOr(&ctr->err, kErrIndexNode);
             } else if (sp < kTraversalStack) {
                 stk[sp++] = c;
             } else {
@@ -459,11 +629,18 @@ void bvh_refit(const Box6* box, BvhBufs& b, cudaStream_t s) {
 }
 
 void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCounters* ctr, cudaStream_t s,
-               const int* skip_shared_ev, int block, const Box6* box_static) {
+               const int* skip_shared_ev, int block, const Box6* box_static, bool packet) {
     int n = b.n;
     if (n <= 1) return;
-    count_launch(), k_traverse<<<nblk(n - 1, block), block, 0, s>>>(box, b.order, n, b.node, b.elem_scene, b.run,
-                                                                    skip_shared_ev, pairs, cap, ctr, box_static);
+    if (b.leaf)
+        count_launch(), k_leaf_records<<<nblk(n, 256), 256, 0, s>>>(box, b.order, n, b.ev, b.leaf, b.ne_all, ctr);
+    if (b.leaf && packet)
+        count_launch(), k_traverse_packet<<<nblk(n - 1, kPacketWarps * 32), kPacketWarps * 32, 0, s>>>(
+            b.order, n, b.node, b.elem_scene, b.run, skip_shared_ev, pairs, cap, ctr, box_static, b.leaf);
+    else
+        count_launch(), k_traverse<<<nblk(n - 1, block), block, 0, s>>>(box, b.order, n, b.node, b.elem_scene, b.run,
+                                                                        skip_shared_ev, pairs, cap, ctr, box_static,
+                                                                        b.leaf);
 }
 
 void brute_pairs(const Box6* box, int ne, const int* elem_scene, int2* pairs, int cap, PassCounters* ctr,

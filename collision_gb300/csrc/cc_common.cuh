@@ -56,6 +56,11 @@ enum ErrBits {
     kErrMergeOverflow = 32,
     kErrUnionOverflow = 64,
     kErrSubOverflow = 128,
+    // an index outside its array met in the broad phase (node, leaf,
+    // element): the access is skipped and the call fails
+    kErrIndexNode = 256,
+    kErrIndexLeaf = 512,
+    kErrIndexElem = 1024,
 };
 // Errors after which a pass's results are discarded (and the pass retried
 // with larger buffers, or the call fails): the impulses are not applied.

@@ -15,7 +15,8 @@ inline void count_launch(int n = 1) { g_kernel_launches += n; }
 
 // Launch shapes that do not change results (set through cc_set_tuning).
 struct LaunchTuning {
-    int traverse_block = 128;
+    bool packet_traverse = false;  // warp-cooperative traversal (k_traverse_packet)
+    int traverse_block = 128;     // threads per block of the per-thread traversal
     int narrow_block = 128;
     int strain_block = 256;
 };
@@ -48,6 +49,16 @@ struct __align__(16) BvhNode32 {
     int4 meta;  // child 0, child 1, last leaf under child 0, under child 1
 };
 
+// A sorted leaf as the traversal's exact test reads it: the element's FP64
+// box in the order-preserving integer encoding (lo xyz, hi xyz), its points
+// (third -1 for a bond) and its id - one 64-byte record per leaf visit, with
+// Morton neighbours next to each other.
+struct __align__(64) LeafRec {
+    unsigned long long lo[3], hi[3];
+    int p[3];
+    int e;
+};
+
 struct BvhBufs {
     int n;                        // leaves of this pass's hierarchy
     const int* act;               // their element ids (null: elements 0..n-1)
@@ -64,6 +75,11 @@ struct BvhBufs {
     BvhNode32* node;              // n-1 internal nodes
     unsigned long long* bbox_enc; // 6 encoded doubles per scene (scene boxes)
     void* sort_temp;
+    // optional: one record per sorted leaf for the traversal's leaf test,
+    // filled by bvh_pairs from the boxes and the element points ev
+    struct LeafRec* leaf;
+    const int* ev;
+    int ne_all;  // elements of all scenes (bound of the ids in order)
 };
 
 // Leaf boxes of every element (static: x_old; moving: x_old and
@@ -92,7 +108,8 @@ void bvh_refit(const Box6* box, BvhBufs& b, cudaStream_t s);
 // With box_static, every pair is found on `box` (swept boxes) and carries
 // kPairStatic when the elements' static boxes overlap as well.
 void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCounters* ctr, cudaStream_t s,
-               const int* skip_shared_ev = nullptr, int block = 128, const Box6* box_static = nullptr);
+               const int* skip_shared_ev = nullptr, int block = 128, const Box6* box_static = nullptr,
+               bool packet = false);
 // The same pair set by testing every pair (for cross-checks on small meshes).
 void brute_pairs(const Box6* box, int ne, const int* elem_scene, int2* pairs, int cap, PassCounters* ctr,
                  cudaStream_t s);

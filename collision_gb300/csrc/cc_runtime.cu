@@ -39,7 +39,15 @@ const char* kStageNames[kNumStages] = {"init", "leaf_boxes", "bvh_build", "trave
 
 constexpr int kMaxSceneElems = (1 << 22) - 1;  // leaf ranks fill 22 bits of a contribution key
 constexpr long long kMaxTotal = 1ll << 28;     // points and elements over all scenes
-constexpr int kNumCounters = 16;
+constexpr int kNumCounters = 18;
+constexpr int kErrIndex = kErrIndexNode | kErrIndexLeaf | kErrIndexElem;
+std::string index_error(int e) {
+    std::string m = "broad phase met an index out of range:";
+    if (e & kErrIndexNode) m += " node";
+    if (e & kErrIndexLeaf) m += " leaf";
+    if (e & kErrIndexElem) m += " element";
+    return m;
+}
 
 template <class T>
 cudaError_t dalloc(T** p, size_t n) {
@@ -437,7 +445,7 @@ struct cc_solver {
         urec_cap = members_cap = zones_cap = 0;
         dfree(d_xold_in); dfree(d_xcand_in); dfree(d_vel); dfree(d_xout); dfree(d_hc);
         dfree(d_box); dfree(d_box_st); dfree(bvh.keys); dfree(bvh.order); dfree(bvh.range_hi);
-        dfree(bvh.range_lo); dfree(bvh.parent); dfree(bvh.flags); dfree(bvh.node); dfree(bvh.bbox_enc);
+        dfree(bvh.range_lo); dfree(bvh.parent); dfree(bvh.flags); dfree(bvh.node); dfree(bvh.bbox_enc); dfree(bvh.leaf);
         if (bvh.sort_temp) cudaFree(bvh.sort_temp);
         bvh = BvhBufs{};
         dfree(d_pairs); dfree(d_contrib); dfree(d_pair_hit); dfree(d_pairq); dfree(d_sub_pt); dfree(d_sub_ee);
@@ -959,6 +967,7 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     ok &= dalloc(&bvh.parent, (size_t)2 * ne) == cudaSuccess;
     ok &= dalloc(&bvh.flags, (size_t)ne) == cudaSuccess;
     ok &= dalloc(&bvh.node, (size_t)ne) == cudaSuccess;
+    ok &= dalloc(&bvh.leaf, (size_t)ne) == cudaSuccess;
     ok &= dalloc(&bvh.bbox_enc, 6 * (size_t)n) == cudaSuccess;
     ok &= cudaMalloc(&bvh.sort_temp, radix_sort_temp_bytes(ne > 0 ? ne : 1)) == cudaSuccess;
     ok &= dalloc(&apply.cnt, (size_t)nv + nbodies) == cudaSuccess;
@@ -990,6 +999,8 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     ok &= cudaMallocHost(&h_sel, sizeof(int) * (3 * (size_t)n + 2)) == cudaSuccess;
     if (!ok) return fail(CC_NO_MEMORY, "device allocation failed");
     bvh.elem_scene = d_escene;
+    bvh.ev = d_ev;
+    bvh.ne_all = ne;
     bvh.scenes = d_scenes;
     bvh.run = d_run;
     cc_status st = grow_pairs(8 * ne + 4096);
@@ -1172,11 +1183,13 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
     for (int attempt = 0; attempt < 8; ++attempt) {
         count_launch(), k_reset_pass<<<(nscenes + 255) / 256, 256, 0, stream>>>(d_ctr, d_run, nscenes,
                                                                                 reuse ? reuse_npairs : -1);
-        prof(kStTraverse, true);
-        if (!reuse)
+        if (!reuse) {
+            prof(kStTraverse, true);
             bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, record ? nullptr : d_ev, tune.traverse_block,
-                      combined ? d_box_st : nullptr);
-        prof(kStTraverse, false);
+                      combined ? d_box_st : nullptr, tune.packet_traverse);
+            prof(kStTraverse, false);
+            if (attempt == 0) counters[16] += bvh.n;
+        }
         NarrowArgs a;
         a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
         a.vbody = d_vbody; a.body_mass = d_body_mass; a.body_slot0 = nv;
@@ -1215,6 +1228,7 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
         if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("detection pass");
         int e = h_ctr->err;
         if (e & kErrNan) return fail(CC_NAN_DETECTED, "non-finite velocity or normal (the reference exits here)");
+        if (e & kErrIndex) return fail(CC_CUDA_ERROR, index_error(e));
         if (e & kErrStack) return fail(CC_STACK_OVERFLOW, "BVH traversal stack overflow");
         if (e & kErrPairOverflow) {
             st = grow_pairs(2 * h_ctr->npairs + 1024);
@@ -1262,6 +1276,7 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
     counters[12] += h_ctr->nsub;
     if (moving) counters[13] += h_ctr->nvisits;
     counters[15] += h_ctr->ncr;
+    if (!reuse) counters[17] += h_ctr->npairs;
     if (record && h_ctr->nrec > 0) {
         size_t base = visits.size();
         visits.resize(base + (size_t)h_ctr->nrec);
@@ -1533,7 +1548,8 @@ cc_status cc_solver::check_ccd(const double* x_old, const double* x_new, long lo
     bvh_build(d_box, bvh, stream);
     for (int attempt = 0; attempt < 8; ++attempt) {
         count_launch(), k_reset_pass<<<(nscenes + 255) / 256, 256, 0, stream>>>(d_ctr, d_run, nscenes);
-        bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, d_ev);
+        bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, d_ev, tune.traverse_block, nullptr,
+                  tune.packet_traverse);
         NarrowArgs a{};
         a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
         a.vbody = d_vbody; a.body_mass = d_body_mass; a.body_slot0 = nv;
@@ -1555,6 +1571,7 @@ cc_status cc_solver::check_ccd(const double* x_old, const double* x_new, long lo
     }
     int e = h_ctr->err;
     if (e & kErrNan) return fail(CC_NAN_DETECTED, "non-finite velocity or normal in the CCD check");
+    if (e & kErrIndex) return fail(CC_CUDA_ERROR, index_error(e));
     if (e & kErrStack) return fail(CC_STACK_OVERFLOW, "BVH traversal stack overflow");
     if (e) return fail(CC_PAIR_OVERFLOW, "buffers kept overflowing");
     if (hits) *hits = h_ctr->nhit_pairs;
@@ -1595,7 +1612,8 @@ cc_status cc_solver::autotune(double* best_ms) {
         for (int attempt = 0; attempt < 8; ++attempt) {
             count_launch(), k_reset_pass<<<(nscenes + 255) / 256, 256, 0, stream>>>(d_ctr, d_run, nscenes);
             cudaEventRecord(e0, stream);
-            bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, d_ev, t.traverse_block);
+            bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, d_ev, t.traverse_block, nullptr,
+                      t.packet_traverse);
             NarrowArgs a{};
             a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
         a.vbody = d_vbody; a.body_mass = d_body_mass; a.body_slot0 = nv;
@@ -1636,6 +1654,7 @@ cc_status cc_solver::autotune(double* best_ms) {
                 if (st) return st;
                 continue;
             }
+            if (e & kErrIndex) return fail(CC_CUDA_ERROR, "autotune: " + index_error(e));
             if (e & (kErrStack | kErrNan)) return fail(CC_STACK_OVERFLOW, "autotune pass failed");
             cudaEventElapsedTime(ms, e0, e1);
             return CC_OK;
@@ -1658,7 +1677,7 @@ cc_status cc_solver::autotune(double* best_ms) {
     cc_status st = time_it(best_t, best_split, &best);  // the current setting, which also sizes the buffers
     const int tb[] = {64, 128, 256, 512};
     const int nb[] = {64, 128, 256};
-    for (int a : tb) {
+    for (int a : tb) {  // the traversal with a stack per thread (the warp packets are slower on cloth)
         LaunchTuning t = best_t;
         t.traverse_block = a;
         float m;
@@ -1854,6 +1873,9 @@ cc_status cc_set_tuning(cc_solver* s, int knob, int value) {
         case CC_TUNE_STRAIN_WARP:
             s->strain_warp = value != 0;
             return CC_OK;
+        case CC_TUNE_PACKET_TRAVERSE:
+            s->tune.packet_traverse = value != 0;
+            return CC_OK;
         case CC_TUNE_STRAIN_BLOCK:
             if (value < 32 || value > 256 || value % 32) return CC_BAD_INPUT;
             s->tune.strain_block = value;
@@ -1878,6 +1900,7 @@ int cc_get_tuning(cc_solver* s, int knob) {
         case CC_TUNE_TAIL_GRAPH: return s->tail_graphs_on ? 1 : 0;
         case CC_TUNE_COMBINED_BROAD: return s->combined_broad ? 1 : 0;
         case CC_TUNE_STRAIN_WARP: return s->strain_warp ? 1 : 0;
+        case CC_TUNE_PACKET_TRAVERSE: return s->tune.packet_traverse ? 1 : 0;
         default: return -1;
     }
 }
@@ -2036,7 +2059,8 @@ int cc_debug_candidate_pairs(cc_solver* s, int moving, int brute_force, int* out
         if (brute_force)
             brute_pairs(s->d_box, s->ne, s->d_escene, s->d_pairs, s->pair_cap, s->d_ctr, s->stream);
         else
-            bvh_pairs(s->d_box, s->bvh, s->d_pairs, s->pair_cap, s->d_ctr, s->stream);
+            bvh_pairs(s->d_box, s->bvh, s->d_pairs, s->pair_cap, s->d_ctr, s->stream, nullptr, s->tune.traverse_block,
+                      nullptr, s->tune.packet_traverse);
         cudaMemcpyAsync(s->h_ctr, s->d_ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, s->stream);
         if (cudaStreamSynchronize(s->stream) != cudaSuccess) return -1;
         if (s->h_ctr->err & kErrPairOverflow) {

@@ -184,7 +184,7 @@ class CollisionSolver3d:
         self._check(self._lib.cc_set_scene_domain_boundary(self._h, int(scene), lo.ctypes.data, hi.ctypes.data))
 
     TUNE_SPLIT_NARROW, TUNE_TRAVERSE_BLOCK, TUNE_NARROW_BLOCK, TUNE_STRAIN_BLOCK, TUNE_TAIL_GRAPH = 0, 1, 2, 3, 4
-    TUNE_COMBINED_BROAD, TUNE_STRAIN_WARP = 5, 6
+    TUNE_COMBINED_BROAD, TUNE_STRAIN_WARP, TUNE_PACKET_TRAVERSE = 5, 6, 7
 
     def setTuning(self, knob: int, value: int):
         """Launch shapes and the two-stage narrow phase; none changes results."""
@@ -198,7 +198,8 @@ class CollisionSolver3d:
         returns the chosen settings and the best timed pass in ms."""
         ms = C.c_double(0.0)
         self._check(self._lib.cc_autotune(self._h, C.byref(ms)))
-        return {"traverse_block": self.getTuning(self.TUNE_TRAVERSE_BLOCK),
+        return {"packet_traverse": self.getTuning(self.TUNE_PACKET_TRAVERSE),
+                "traverse_block": self.getTuning(self.TUNE_TRAVERSE_BLOCK),
                 "split_narrow": self.getTuning(self.TUNE_SPLIT_NARROW),
                 "narrow_block": self.getTuning(self.TUNE_NARROW_BLOCK), "pass_ms": ms.value}
 
@@ -338,7 +339,8 @@ class CollisionSolver3d:
     # ------------------------------------------------------- inspection
     COUNTER_NAMES = ("passes", "ccd_passes", "zone_passes", "candidate_pairs", "visits", "hit_pairs",
                      "contacts", "strain_passes", "tree_builds", "kernel_launches", "strain_averaged",
-                     "strain_exact", "fp64_subtests", "moving_visits", "strain_bytes", "cr_roots")
+                     "strain_exact", "fp64_subtests", "moving_visits", "strain_bytes", "cr_roots", "broad_leaves",
+                     "broad_pairs")
 
     def counters(self) -> dict:
         n_all = len(self.COUNTER_NAMES)

@@ -217,6 +217,11 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
  *                           0 (default): on a CTA of CC_TUNE_STRAIN_BLOCK
  *                           threads. Same results; the CTA sweep is faster
  *                           for sheets whose levels hold more than ~32 edges
+ *   CC_TUNE_PACKET_TRAVERSE 1: each warp walks the hierarchy as one packet of
+ *                           32 Morton-consecutive queries with a shared-memory
+ *                           stack; 0 (default): a stack per thread. Same
+ *                           pairs; the packets are slower on the cloth
+ *                           workloads, whose neighbouring queries diverge
  * cc_get_tuning returns the current value, or -1 for an unknown knob. */
 enum {
     CC_TUNE_SPLIT_NARROW = 0,
@@ -225,7 +230,8 @@ enum {
     CC_TUNE_STRAIN_BLOCK = 3,
     CC_TUNE_TAIL_GRAPH = 4,
     CC_TUNE_COMBINED_BROAD = 5,
-    CC_TUNE_STRAIN_WARP = 6
+    CC_TUNE_STRAIN_WARP = 6,
+    CC_TUNE_PACKET_TRAVERSE = 7
 };
 cc_status cc_set_tuning(cc_solver* s, int knob, int value);
 int cc_get_tuning(cc_solver* s, int knob);
@@ -272,7 +278,9 @@ cc_status cc_set_strain_window(cc_solver* s, int on);
  * strain edges averaged, strain tests taken the exact way, sub-tests
  * evaluated in FP64, narrow-phase visits of CCD and impact-zone passes,
  * algorithmic bytes of the strain sweeps, coplanarity cubics whose roots
- * were formed again with correctly rounded functions. Candidate pairs and
+ * were formed again with correctly rounded functions, leaves traversed by
+ * the broad phase (summed over its traversals), candidate pairs those
+ * traversals wrote. Candidate pairs and
  * visits leave out pairs of elements that share a point (their tests
  * return false at once) unless recording is on. Returns how many were
  * written. */

@@ -54,7 +54,7 @@ def _split(a, off, i):
 
 
 def _run_batch(solver_cls, mix, nsteps, mode=0, window=True, record=False, split=True, graph=True, combined=True,
-               warp=False):
+               warp=False, packet=False):
     b = solver_cls(0)
     b.assembleBatch(mix)
     b.setMode(mode)
@@ -63,6 +63,7 @@ def _run_batch(solver_cls, mix, nsteps, mode=0, window=True, record=False, split
     b.setTuning(solver_cls.TUNE_TAIL_GRAPH, int(graph))
     b.setTuning(solver_cls.TUNE_COMBINED_BROAD, int(combined))
     b.setTuning(solver_cls.TUNE_STRAIN_WARP, int(warp))
+    b.setTuning(solver_cls.TUNE_PACKET_TRAVERSE, int(packet))
     b.setRecording(record)
     pv, pe = b.sceneOffsets()
     x = np.concatenate([s.x for s in mix])
@@ -139,10 +140,13 @@ def test_batch_mixed_and_global_strain_equal_plain(solver_cls):
         got, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, window=window, split=split, graph=graph,
                                combined=comb)
         _compare(ref, got, (mode, window, split, graph, comb))
-    # the one-warp staged sweep instead of the CTA-per-scene one
+    # the one-warp staged sweep instead of the CTA-per-scene one, and the
+    # warp-packet traversal instead of the one with a stack per thread
     for mode in (0, 1):
         got, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, warp=True)
         _compare(ref, got, ("warp sweep", mode))
+        got, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, packet=True)
+        _compare(ref, got, ("packet traversal", mode))
 
 
 def _compare(ref, got, tag):

@@ -111,12 +111,14 @@ def test_lbvh_pairs_equal_all_pairs(solver_cls):
     s = solver_cls(0)
     s.assembleFromScene(sc)
     s.resolveCollision(sc.x, scenes.candidate(sc, sc.x, sc.v), sc.v, np.zeros(sc.nv, np.uint8))
-    for moving in (False, True):
-        a = s.candidatePairs(moving, brute_force=False)
-        b = s.candidatePairs(moving, brute_force=True)
-        ka = np.sort(np.minimum(a[:, 0], a[:, 1]).astype(np.int64) * sc.ne + np.maximum(a[:, 0], a[:, 1]))
-        kb = np.sort(np.minimum(b[:, 0], b[:, 1]).astype(np.int64) * sc.ne + np.maximum(b[:, 0], b[:, 1]))
-        assert len(ka) > 0 and np.array_equal(ka, kb)
+    for packet in (1, 0):  # the warp-packet traversal and the one with a stack per thread
+        s.setTuning(s.TUNE_PACKET_TRAVERSE, packet)
+        for moving in (False, True):
+            a = s.candidatePairs(moving, brute_force=False)
+            b = s.candidatePairs(moving, brute_force=True)
+            ka = np.sort(np.minimum(a[:, 0], a[:, 1]).astype(np.int64) * sc.ne + np.maximum(a[:, 0], a[:, 1]))
+            kb = np.sort(np.minimum(b[:, 0], b[:, 1]).astype(np.int64) * sc.ne + np.maximum(b[:, 0], b[:, 1]))
+            assert len(ka) > 0 and np.array_equal(ka, kb), packet
     s.close()
 
 
