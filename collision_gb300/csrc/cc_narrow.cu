@@ -385,6 +385,10 @@ void narrow_pass(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s,
 
 void narrow_pass_split(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s, int block, bool zone) {
     if (max_pairs <= 0) return;
+    if (!a.pbox_lo || !a.p32 || (moving && !a.v32)) {  // the filters need the FP32 point data (mode 1)
+        narrow_pass(a, moving, max_pairs, s, block);
+        return;
+    }
     const int cap_blocks = 152 * 16 * 128 / block;
     int blocks = (max_pairs + block - 1) / block;
     if (blocks > cap_blocks) blocks = cap_blocks;

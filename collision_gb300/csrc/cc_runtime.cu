@@ -1672,7 +1672,7 @@ cc_status cc_solver::autotune(double* best_ms) {
         return CC_OK;
     };
     LaunchTuning best_t = tune;
-    bool best_split = split_narrow;
+    bool best_split = split_narrow && mode == 1;  // the staged pass needs the FP32 point data of mode 1
     float best = 1e30f;
     cc_status st = time_it(best_t, best_split, &best);  // the current setting, which also sizes the buffers
     const int tb[] = {64, 128, 256, 512};
@@ -1699,7 +1699,7 @@ cc_status cc_solver::autotune(double* best_ms) {
     cudaEventDestroy(e1);
     if (st) return st;
     tune = best_t;
-    split_narrow = best_split;
+    if (mode == 1) split_narrow = best_split;
     if (best_ms) *best_ms = best;
     return cuda_check("autotune");
 }

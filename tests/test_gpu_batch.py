@@ -280,14 +280,16 @@ def test_zone_cap_stops_one_scene_only(solver_cls):
     s.close()
 
 
-def test_autotune_keeps_results(solver_cls):
+@pytest.mark.parametrize("mode", [1, 0])
+def test_autotune_keeps_results(solver_cls, mode):
     """The autotuner changes launch shapes and buffer sizes only: a solver
-    tuned after its second step produces the same bits as one that is not."""
+    tuned after its second step produces the same bits as one that is not
+    (in both arithmetic modes)."""
     mix = _mix()
-    ref, pv, _ = _run_batch(solver_cls, mix, 6, mode=1)
+    ref, pv, _ = _run_batch(solver_cls, mix, 6, mode=mode)
     b = solver_cls(0)
     b.assembleBatch(mix)
-    b.setMode(1)
+    b.setMode(mode)
     x = np.concatenate([s.x for s in mix])
     v = np.concatenate([s.v for s in mix])
     hc = np.zeros(len(x), np.uint8)
