@@ -249,6 +249,9 @@ struct StrainPlan {
     int ecap, lcap, wcap;  // most edges, copy-ins, write-backs of one level (scenes that fit)
     size_t warp_smem;      // its dynamic shared memory
     const int* order;      // device: scene of each sweep CTA, most levels first
+    // window sweep: first thread of the copy-in and the write-back roles (a
+    // level's edges on threads [0, cbase)); 0, 0: every thread takes all three
+    int cbase, wbase;
 };
 // Dynamic shared memory of the one-warp sweep for these sizes.
 size_t strain_warp_smem(int max_slots, int ecap, int lcap, int wcap);

@@ -646,7 +646,9 @@ struct WinRing {
     int lslot[kWindowAhead];  // slot this thread copied in, per recent level (-1: none)
 };
 
-__device__ __forceinline__ void win_fetch(WinRing& r, int j, int lk, int nlevels, int tid,
+// tid: this thread's edge of the level; tc, tw: its copy-in and write-back
+// (negative: none first-hand)
+__device__ __forceinline__ void win_fetch(WinRing& r, int j, int lk, int nlevels, int tid, int tc, int tw,
                                           const int4* __restrict__ hdr, const StrainEdgeHot* __restrict__ hot,
                                           const int2* __restrict__ load_list, const int2* __restrict__ wb_list) {
     if (lk < nlevels) {
@@ -654,8 +656,8 @@ __device__ __forceinline__ void win_fetch(WinRing& r, int j, int lk, int nlevels
         r.h0[j] = a;
         r.h1[j] = b;
         if (a.x + tid < a.y) r.hot[j] = hot[a.x + tid];
-        if (a.z + tid < a.w) r.ld[j] = load_list[a.z + tid];
-        if (b.x + tid < b.y) r.wb[j] = wb_list[b.x + tid];
+        if (tc >= 0 && a.z + tc < a.w) r.ld[j] = load_list[a.z + tc];
+        if (tw >= 0 && b.x + tw < b.y) r.wb[j] = wb_list[b.x + tw];
     }
 }
 
@@ -671,6 +673,9 @@ struct WinArgs {
     double dt;
     float dt32;
     int multi_ld;  // some level has more copy-ins than the block has threads
+    // first thread of the copy-in and write-back roles; both 0 when every
+    // thread takes all three roles (edge, copy-in, write-back number tid)
+    int cbase, wbase;
 };
 
 // One level of the window sweep; J = level mod kWindowAhead.
@@ -681,14 +686,15 @@ __device__ __forceinline__ void win_level(const WinArgs& A, WinRing& r, WinSlot*
     const int4 h0 = r.h0[R], h1 = r.h1[R];
     const StrainEdgeHot cur = r.hot[R];
     const int2 ld = r.ld[R], wb = r.wb[R];
-    win_fetch(r, R, l + kRing, A.nlevels, tid, A.hdr, A.hot, A.load_list, A.wb_list);
+    const int tc = tid - A.cbase, tw = tid - A.wbase;
+    win_fetch(r, R, l + kRing, A.nlevels, tid, tc, tw, A.hdr, A.hot, A.load_list, A.wb_list);
     // copy in the points whose slot opens now
     int my_slot = -1;
-    if (h0.z + tid < h0.w) {
+    if (tc >= 0 && h0.z + tc < h0.w) {
         my_slot = ld.y;
         cp_async16(&s_win[ld.y].a, &A.av[ld.x]);
         cp_async16(&s_win[ld.y].b, reinterpret_cast<const double2*>(&A.av[ld.x]) + 1);
-        for (int i = h0.z + tid + (int)blockDim.x; i < h0.w; i += blockDim.x) {
+        for (int i = h0.z + tc + (int)blockDim.x; i < h0.w; i += blockDim.x) {
             int2 ps = A.load_list[i];
             cp_async16(&s_win[ps.y].a, &A.av[ps.x]);
             cp_async16(&s_win[ps.y].b, reinterpret_cast<const double2*>(&A.av[ps.x]) + 1);
@@ -719,7 +725,7 @@ __device__ __forceinline__ void win_level(const WinArgs& A, WinRing& r, WinSlot*
         w.f = make_float4((float)w.a.x, (float)w.a.y, (float)w.b.x, 0.f);
         if (A.multi_ld) {  // the copy-ins past the first per thread (a dependent load: only when needed)
             int4 hc = A.hdr[2 * cl];
-            for (int i = hc.z + tid + (int)blockDim.x; i < hc.w; i += blockDim.x) {
+            for (int i = hc.z + tc + (int)blockDim.x; i < hc.w; i += blockDim.x) {
                 WinSlot& w2 = s_win[A.load_list[i].y];
                 w2.f = make_float4((float)w2.a.x, (float)w2.a.y, (float)w2.b.x, 0.f);
             }
@@ -727,10 +733,10 @@ __device__ __forceinline__ void win_level(const WinArgs& A, WinRing& r, WinSlot*
     }
     __syncthreads();
     // write back the points last used at the previous level
-    if (h1.x + tid < h1.y) {
+    if (tw >= 0 && h1.x + tw < h1.y) {
         double2 a = s_win[wb.y].a, b = s_win[wb.y].b;
         A.av[wb.x] = make_double4_32a(a.x, a.y, b.x, 0.0);
-        for (int i = h1.x + tid + (int)blockDim.x; i < h1.y; i += blockDim.x) {
+        for (int i = h1.x + tw + (int)blockDim.x; i < h1.y; i += blockDim.x) {
             int2 ps = A.wb_list[i];
             double2 a2 = s_win[ps.y].a, b2 = s_win[ps.y].b;
             A.av[ps.x] = make_double4_32a(a2.x, a2.y, b2.x, 0.0);
@@ -753,7 +759,7 @@ __global__ void __launch_bounds__(256) k_strain_window(const StrainEdge* __restr
                                                        const int2* __restrict__ wb_list,
                                                        double4_32a* av, int pass, int* flags,
                                                        int* passes_out_all, int multi_ld,
-                                                       const int* __restrict__ order) {
+                                                       const int* __restrict__ order, int cbase, int wbase) {
     extern __shared__ WinSlot s_win[];
     const int sc = order[blockIdx.x];
     const SceneDev& sd = scenes[sc];
@@ -764,14 +770,14 @@ __global__ void __launch_bounds__(256) k_strain_window(const StrainEdge* __restr
     const int2 wb_final = make_int2(sd.wb_final0, sd.wb_final1);
     const double dt = sd.p.dt;
     const int tid = threadIdx.x;
-    WinArgs A{edges, xo, hot, hdr, nlevels, load_list, wb_list, av, dt, __double2float_ru(dt), multi_ld};
+    WinArgs A{edges, xo, hot, hdr, nlevels, load_list, wb_list, av, dt, __double2float_ru(dt), multi_ld, cbase, wbase};
     int n_avg = 0, n_exact = 0;
     bool has = false;
     WinRing r;
 #pragma unroll
     for (int j = 0; j < kWindowAhead; ++j) r.lslot[j] = -1;
 #pragma unroll
-    for (int j = 0; j < kRing; ++j) win_fetch(r, j, j, nlevels, tid, hdr, hot, load_list, wb_list);
+    for (int j = 0; j < kRing; ++j) win_fetch(r, j, j, nlevels, tid, tid - cbase, tid - wbase, hdr, hot, load_list, wb_list);
     for (int lb = 0; lb < nlevels; lb += kWindowAhead) {
         win_level<0>(A, r, s_win, lb + 0, tid, &n_avg, &n_exact, &has);
         if (lb + 1 < nlevels) win_level<1>(A, r, s_win, lb + 1, tid, &n_avg, &n_exact, &has);
@@ -1098,7 +1104,7 @@ void strain_limit(const StrainEdge* edges, int nedges, const int4* hdr, const in
         else if (plan.window)
             count_launch(), k_strain_window<<<nscenes, plan.block, smem, s>>>(
                 edges, xo, hot, hdr, scenes, cap, load_list, wb_list, av, pass, flags, passes_out, plan.lcap > plan.block,
-                plan.order);
+                plan.order, plan.cbase, plan.wbase);
         if (!plan.window || plan.any_global)
             count_launch(), k_strain<<<nscenes, 256, 0, s>>>(se, hdr, scenes, cap, av, pass, flags, passes_out,
                                                              plan.order);

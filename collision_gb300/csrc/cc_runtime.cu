@@ -389,6 +389,7 @@ struct cc_solver {
     bool strain_window = true;
     bool split_narrow = true;  // two-stage narrow phase for mixed passes
     bool strain_warp = false;  // one-warp strain sweep with staged levels
+    bool strain_roles = true;  // window sweep: edges, copy-ins and write-backs on separate threads
     LaunchTuning tune;
     int host_threads = 0;  // tree emulation threads (0: hardware concurrency)
 
@@ -621,7 +622,7 @@ struct cc_solver {
     // strain settings, then replayed.
     struct TailGraph {
         const void* key[4];
-        int block, window, warp;
+        int block, window, warp, roles;
         cudaGraphExec_t exec;
         long long launches;
     };
@@ -636,7 +637,7 @@ struct cc_solver {
         TailGraph* hit = nullptr;
         for (auto& g : tail_graphs)
             if (std::equal(key, key + 4, g.key) && g.block == tune.strain_block && g.window == (int)strain_window &&
-                g.warp == (int)strain_warp) {
+                g.warp == (int)strain_warp && g.roles == (int)strain_roles) {
                 hit = &g;
                 break;
             }
@@ -660,6 +661,7 @@ struct cc_solver {
             tg.block = tune.strain_block;
             tg.window = (int)strain_window;
             tg.warp = (int)strain_warp;
+            tg.roles = (int)strain_roles;
             tg.launches = n;
             e = cudaGraphInstantiate(&tg.exec, g, 0);
             cudaGraphDestroy(g);
@@ -735,6 +737,16 @@ struct cc_solver {
             }
         }
         pl.warp_smem = strain_warp_smem(pl.max_window_slots, pl.ecap, pl.lcap, pl.wcap);
+        // separate threads for a level's edges, copy-ins and write-backs,
+        // each role from a warp boundary, where they fit in the block
+        pl.cbase = pl.wbase = 0;
+        if (strain_roles) {
+            const int cb = (pl.ecap + 31) / 32 * 32, wb = cb + (pl.lcap + 31) / 32 * 32;
+            if (pl.ecap > 0 && wb + pl.wcap <= pl.block) {
+                pl.cbase = cb;
+                pl.wbase = wb;
+            }
+        }
         pl.warp = strain_window && strain_warp && pl.warp_smem <= 200 * 1024;
         return pl;
     }
@@ -1876,6 +1888,9 @@ cc_status cc_set_tuning(cc_solver* s, int knob, int value) {
         case CC_TUNE_PACKET_TRAVERSE:
             s->tune.packet_traverse = value != 0;
             return CC_OK;
+        case CC_TUNE_STRAIN_ROLES:
+            s->strain_roles = value != 0;
+            return CC_OK;
         case CC_TUNE_STRAIN_BLOCK:
             if (value < 32 || value > 256 || value % 32) return CC_BAD_INPUT;
             s->tune.strain_block = value;
@@ -1901,6 +1916,7 @@ int cc_get_tuning(cc_solver* s, int knob) {
         case CC_TUNE_COMBINED_BROAD: return s->combined_broad ? 1 : 0;
         case CC_TUNE_STRAIN_WARP: return s->strain_warp ? 1 : 0;
         case CC_TUNE_PACKET_TRAVERSE: return s->tune.packet_traverse ? 1 : 0;
+        case CC_TUNE_STRAIN_ROLES: return s->strain_roles ? 1 : 0;
         default: return -1;
     }
 }

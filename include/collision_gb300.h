@@ -222,6 +222,10 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
  *                           stack; 0 (default): a stack per thread. Same
  *                           pairs; the packets are slower on the cloth
  *                           workloads, whose neighbouring queries diverge
+ *   CC_TUNE_STRAIN_ROLES    1 (default): in the shared-memory strain sweep a
+ *                           level's edges, copy-ins and write-backs run on
+ *                           separate threads (when they fit in the block);
+ *                           0: every thread takes one of each
  * cc_get_tuning returns the current value, or -1 for an unknown knob. */
 enum {
     CC_TUNE_SPLIT_NARROW = 0,
@@ -231,7 +235,8 @@ enum {
     CC_TUNE_TAIL_GRAPH = 4,
     CC_TUNE_COMBINED_BROAD = 5,
     CC_TUNE_STRAIN_WARP = 6,
-    CC_TUNE_PACKET_TRAVERSE = 7
+    CC_TUNE_PACKET_TRAVERSE = 7,
+    CC_TUNE_STRAIN_ROLES = 8
 };
 cc_status cc_set_tuning(cc_solver* s, int knob, int value);
 int cc_get_tuning(cc_solver* s, int knob);
