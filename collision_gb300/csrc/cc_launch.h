@@ -226,7 +226,7 @@ void step_init(const double* x_old, const double* x_cand, int nv, const uint8_t*
 // movable points are not clamped.
 void finalize_positions(const uint8_t* in_elem, const double4_32a* xo, double4_32a* av, uint8_t* has_collsn,
                         const double* x_cand, double* x_out, int nv, const int* vscene, const SceneDev* scenes,
-                        const uint8_t* fixed, cudaStream_t s);
+                        const uint8_t* fixed, const uint8_t* mask, cudaStream_t s);
 // reduceSuperelast: up to 10 Gauss-Seidel passes over each scene's strain
 // edges, one CTA per scene.
 struct StrainEdge {
@@ -264,14 +264,18 @@ void strain_configure();
 size_t strain_step_bytes(int nedges);
 // chunks: (scene, first edge) of every run of at most 256 edges of one
 // scene; flags: 2 ints per scene.
+// Per step, before any strain_limit: each edge's records from x_old.
+void strain_setup(const StrainEdge* edges, int nedges, const SceneDev* scenes, const StrainPlan& plan,
+                  const double4_32a* xo, void* step_buf, const int* vscene, cudaStream_t s);
+// The strain loop of the scenes in mask (per scene, nonzero: in; null: all).
 void strain_limit(const StrainEdge* edges, int nedges, const int4* hdr, const int2* load_list, const int2* wb_list,
                   const int2* chunks, int nchunks, const SceneDev* scenes, int nscenes, const StrainPlan& plan,
                   const double4_32a* xo, double4_32a* av, void* step_buf, int* flags, int* passes_out,
-                  const int* vscene, cudaStream_t s);
+                  const uint8_t* mask, cudaStream_t s);
 // Correctly rounded cos/sin/acos/pow (fn 0..3) on device arrays, for self-tests.
 void math_selftest(int fn, const double* a, const double* b, double* out, int n, cudaStream_t s);
 // updateFinalVelocity.
 void final_velocity(const uint8_t* in_elem, const uint8_t* has_collsn, const double4_32a* av, const int* vscene,
-                    const SceneDev* scenes, double* vel, int nv, cudaStream_t s);
+                    const SceneDev* scenes, double* vel, int nv, const uint8_t* mask, cudaStream_t s);
 
 }  // namespace ccg

@@ -233,9 +233,10 @@ __global__ void k_zone_solve(const int* __restrict__ members, const int* __restr
 __global__ void k_finalize(const uint8_t* __restrict__ in_elem, const double4_32a* __restrict__ xo, double4_32a* av,
                            uint8_t* has_collsn, const double* __restrict__ x_cand, double* x_out, int nv,
                            const int* __restrict__ vscene, const SceneDev* __restrict__ scenes,
-                           const uint8_t* __restrict__ fixed) {
+                           const uint8_t* __restrict__ fixed, const uint8_t* __restrict__ mask) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nv) return;
+    if (mask && !mask[vscene[p]]) return;  // another scene set's end of step
     if (!in_elem[p]) {
         for (int j = 0; j < 3; ++j) x_out[3 * p + j] = x_cand[3 * p + j];
         return;
@@ -960,11 +961,27 @@ __global__ void __launch_bounds__(256) k_strain_check(const StrainEdge* __restri
     }
 }
 
+// Start of a strain loop for the scenes in mask (all: mask null): their
+// flags and counters cleared; the others marked finished, so that every
+// kernel of this loop leaves them and their counters alone.
+__global__ void k_strain_init(const uint8_t* __restrict__ mask, int nscenes, int* flags, int* passes_out) {
+    int sc = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sc >= nscenes) return;
+    if (mask && !mask[sc]) {
+        flags[2 * sc + 1] = 1;
+        return;
+    }
+    flags[2 * sc] = flags[2 * sc + 1] = 0;
+    passes_out[3 * sc] = passes_out[3 * sc + 1] = passes_out[3 * sc + 2] = 0;
+}
+
 __global__ void k_final_velocity(const uint8_t* __restrict__ in_elem, const uint8_t* __restrict__ has_collsn,
                                  const double4_32a* __restrict__ av, const int* __restrict__ vscene,
-                                 const SceneDev* __restrict__ scenes, double* vel, int nv) {
+                                 const SceneDev* __restrict__ scenes, double* vel, int nv,
+                                 const uint8_t* __restrict__ mask) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nv || !in_elem[p] || !has_collsn[p] || !scenes[vscene[p]].enabled) return;
+    if (mask && !mask[vscene[p]]) return;
     double4_32a a = av[p];
     vel[3 * p] = a.x;
     vel[3 * p + 1] = a.y;
@@ -1060,10 +1077,10 @@ void final_rigid(const BodyBufs& b, const uint8_t* has_collsn, const double4_32a
 
 void finalize_positions(const uint8_t* in_elem, const double4_32a* xo, double4_32a* av, uint8_t* has_collsn,
                         const double* x_cand, double* x_out, int nv, const int* vscene, const SceneDev* scenes,
-                        const uint8_t* fixed, cudaStream_t s) {
+                        const uint8_t* fixed, const uint8_t* mask, cudaStream_t s) {
     if (nv > 0)
         count_launch(), k_finalize<<<nblk(nv, 256), 256, 0, s>>>(in_elem, xo, av, has_collsn, x_cand, x_out, nv,
-                                                                 vscene, scenes, fixed);
+                                                                 vscene, scenes, fixed, mask);
 }
 
 size_t strain_step_bytes(int nedges) {
@@ -1078,20 +1095,25 @@ void strain_configure() {
     cudaFuncSetAttribute(k_strain_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStrainWarpBytes);
 }
 
+void strain_setup(const StrainEdge* edges, int nedges, const SceneDev* scenes, const StrainPlan& plan,
+                  const double4_32a* xo, void* step_buf, const int* vscene, cudaStream_t s) {
+    if (nedges <= 0) return;
+    StrainEdgeStep* se = (StrainEdgeStep*)step_buf;
+    StrainEdgeHot* hot = (StrainEdgeHot*)(se + nedges);
+    const int cap = plan.window ? strain_window_slot_cap() : -1;
+    count_launch(), k_strain_setup<<<nblk(nedges, 256), 256, 0, s>>>(edges, nedges, xo, se, hot, vscene, scenes, cap);
+}
+
 void strain_limit(const StrainEdge* edges, int nedges, const int4* hdr, const int2* load_list, const int2* wb_list,
                   const int2* chunks, int nchunks, const SceneDev* scenes, int nscenes, const StrainPlan& plan,
                   const double4_32a* xo, double4_32a* av, void* step_buf, int* flags, int* passes_out,
-                  const int* vscene, cudaStream_t s) {
+                  const uint8_t* mask, cudaStream_t s) {
     if (nscenes <= 0) return;
     StrainEdgeStep* se = (StrainEdgeStep*)step_buf;
     StrainEdgeHot* hot = (StrainEdgeHot*)(se + (nedges > 0 ? nedges : 1));
-    cudaMemsetAsync(flags, 0, sizeof(int) * 2 * (size_t)nscenes, s);
-    cudaMemsetAsync(passes_out, 0, sizeof(int) * 3 * (size_t)nscenes, s);
+    count_launch(), k_strain_init<<<nblk(nscenes, 128), 128, 0, s>>>(mask, nscenes, flags, passes_out);
     // scenes with at most `cap` slots are swept in shared memory (cap -1: none)
     int cap = plan.window ? strain_window_slot_cap() : -1;
-    if (nedges > 0)
-        count_launch(), k_strain_setup<<<nblk(nedges, 256), 256, 0, s>>>(edges, nedges, xo, se, hot, vscene, scenes,
-                                                                         cap);
     size_t smem = (size_t)plan.max_window_slots * sizeof(WinSlot);
     for (int pass = 0; pass < kStrainMaxIter; ++pass) {
         if (nchunks > 0)
@@ -1112,10 +1134,10 @@ void strain_limit(const StrainEdge* edges, int nedges, const int4* hdr, const in
 }
 
 void final_velocity(const uint8_t* in_elem, const uint8_t* has_collsn, const double4_32a* av, const int* vscene,
-                    const SceneDev* scenes, double* vel, int nv, cudaStream_t s) {
+                    const SceneDev* scenes, double* vel, int nv, const uint8_t* mask, cudaStream_t s) {
     if (nv > 0)
         count_launch(), k_final_velocity<<<nblk(nv, 256), 256, 0, s>>>(in_elem, has_collsn, av, vscene, scenes, vel,
-                                                                       nv);
+                                                                       nv, mask);
 }
 
 }  // namespace ccg

@@ -399,7 +399,8 @@ struct cc_solver {
     std::vector<std::pair<int, int>> ev_marks;  // (stage, event index of its start; end = start+1)
     double stage_ms[kNumStages] = {0};
     long long stage_calls[kNumStages] = {0};
-    void prof(int stage, bool begin) {
+    void prof(int stage, bool begin) { prof_on(stage, begin, stream); }
+    void prof_on(int stage, bool begin, cudaStream_t on) {
         if (!profiling) return;
         size_t need = ev_marks.size() * 2 + 2;
         while (ev_pool.size() < need) {
@@ -409,9 +410,9 @@ struct cc_solver {
         }
         if (begin) {
             ev_marks.push_back({stage, (int)(ev_marks.size() * 2)});
-            cudaEventRecord(ev_pool[ev_marks.back().second], stream);
+            cudaEventRecord(ev_pool[ev_marks.back().second], on);
         } else {
-            cudaEventRecord(ev_pool[ev_marks.back().second + 1], stream);
+            cudaEventRecord(ev_pool[ev_marks.back().second + 1], on);
         }
     }
     void prof_collect() {
@@ -436,7 +437,9 @@ struct cc_solver {
         n_strain_chunks = 0;
         if (d_strain_step) cudaFree(d_strain_step);
         d_strain_step = nullptr;
-        dfree(d_scenes); dfree(d_run); dfree(d_vscene); dfree(d_escene);
+        dfree(d_scenes); dfree(d_run); dfree(d_vscene); dfree(d_escene); dfree(d_tail_mask);
+        if (h_tail_masks) cudaFreeHost(h_tail_masks);
+        h_tail_masks = nullptr;
         if (h_run) cudaFreeHost(h_run);
         h_run = nullptr;
         if (h_bbox) cudaFreeHost(h_bbox);
@@ -481,6 +484,11 @@ struct cc_solver {
         h_ctr = nullptr;
         for (auto e : ev_pool) cudaEventDestroy(e);
         ev_pool.clear();
+        if (ev_pass) cudaEventDestroy(ev_pass);
+        if (ev_tail) cudaEventDestroy(ev_tail);
+        ev_pass = ev_tail = nullptr;
+        if (tail_stream) cudaStreamDestroy(tail_stream);
+        tail_stream = nullptr;
         if (stream && own_stream) cudaStreamDestroy(stream);
         stream = nullptr;
     }
@@ -609,14 +617,55 @@ struct cc_solver {
         return CC_OK;
     }
 
-    // The end of a step: strain limiting and final velocities (after
-    // finalize_positions).
-    void tail_after_finalize(double* vel, uint8_t* hc) {
+    // The end of a step of the scenes in d_tail_mask: final positions,
+    // strain limiting and final velocities, on the tail stream.
+    void tail(const double* x_cand, double* x_out, double* vel) {
+        finalize_positions(d_in_elem, d_xo, d_av, d_hc, x_cand, x_out, nv, d_vscene, d_scenes, d_fixed, d_tail_mask,
+                           tail_stream);
         strain_limit(d_edges, nedges, d_strain_hdr, d_strain_load, d_strain_wb, d_strain_chunks, n_strain_chunks,
                      d_scenes, nscenes, strain_plan(), d_xo, d_av, d_strain_step, d_strain_flags, d_strain_passes,
-                     d_vscene, stream);
-        final_velocity(d_in_elem, d_hc, d_av, d_vscene, d_scenes, vel, nv, stream);
-        if (hc != d_hc) cudaMemcpyAsync(hc, d_hc, (size_t)nv, cudaMemcpyDeviceToDevice, stream);
+                     d_tail_mask, tail_stream);
+        final_velocity(d_in_elem, d_hc, d_av, d_vscene, d_scenes, vel, nv, d_tail_mask, tail_stream);
+    }
+    // Tail streams: the ends of steps of the scenes that have finished their
+    // detection passes run there while the other scenes' passes go on (a
+    // scene's end of step reads and writes only its own points).
+    cudaStream_t tail_stream = nullptr;
+    cudaEvent_t ev_pass = nullptr, ev_tail = nullptr;
+    uint8_t* d_tail_mask = nullptr;
+    uint8_t* h_tail_masks = nullptr;  // pinned, (nscenes + 1) masks: one per tail of a step
+    int tails_this_step = 0;
+    std::vector<uint8_t> tail_done;
+    bool overlap_tails = false;
+    // Ends the step of every finished scene without one yet (all: every
+    // scene), after the main stream's work so far.
+    cc_status launch_tail(const double* x_cand, double* x_out, double* vel, bool all) {
+        std::vector<int> ids;
+        for (int s = 0; s < nscenes; ++s)
+            if (!tail_done[s] && (all || scenes[s].state == kHsDone)) ids.push_back(s);
+        if (ids.empty()) return CC_OK;
+        // besides the last, one early end of step, once at least half the
+        // scenes have finished (each one runs the whole tail's launches)
+        if (!all && (tails_this_step > 0 || 2 * (int)ids.size() < nscenes)) return CC_OK;
+        uint8_t* m = h_tail_masks + (size_t)(tails_this_step % (nscenes + 1)) * (size_t)nscenes;
+        tails_this_step++;
+        std::memset(m, 0, (size_t)nscenes);
+        for (int s : ids) {
+            m[s] = 1;
+            tail_done[s] = 1;
+        }
+        cudaEventRecord(ev_pass, stream);
+        cudaStreamWaitEvent(tail_stream, ev_pass, 0);
+        cudaMemcpyAsync(d_tail_mask, m, (size_t)nscenes, cudaMemcpyHostToDevice, tail_stream);
+        prof_on(kStStrain, true, tail_stream);
+        if (tail_graphs_on) {
+            cc_status st = run_tail_graph(x_cand, x_out, vel);
+            if (st) return st;
+        } else {
+            tail(x_cand, x_out, vel);
+        }
+        prof_on(kStStrain, false, tail_stream);
+        return CC_OK;
     }
     // The whole end of a step captured once per set of caller pointers and
     // strain settings, then replayed.
@@ -632,8 +681,8 @@ struct cc_solver {
         for (auto& g : tail_graphs) cudaGraphExecDestroy(g.exec);
         tail_graphs.clear();
     }
-    cc_status run_tail_graph(const double* x_cand, double* x_out, double* vel, uint8_t* hc) {
-        const void* key[4] = {x_cand, x_out, vel, hc};
+    cc_status run_tail_graph(const double* x_cand, double* x_out, double* vel) {
+        const void* key[4] = {x_cand, x_out, vel, nullptr};
         TailGraph* hit = nullptr;
         for (auto& g : tail_graphs)
             if (std::equal(key, key + 4, g.key) && g.block == tune.strain_block && g.window == (int)strain_window &&
@@ -648,11 +697,10 @@ struct cc_solver {
             }
             cudaGraph_t g = nullptr;
             long long l0 = g_kernel_launches;
-            if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+            if (cudaStreamBeginCapture(tail_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
                 return cuda_check("tail capture");
-            finalize_positions(d_in_elem, d_xo, d_av, d_hc, x_cand, x_out, nv, d_vscene, d_scenes, d_fixed, stream);
-            tail_after_finalize(vel, hc);
-            cudaError_t e = cudaStreamEndCapture(stream, &g);
+            tail(x_cand, x_out, vel);
+            cudaError_t e = cudaStreamEndCapture(tail_stream, &g);
             long long n = g_kernel_launches - l0;
             g_kernel_launches = l0;
             if (e != cudaSuccess || !g) return fail(CC_CUDA_ERROR, std::string("tail capture: ") + cudaGetErrorString(e));
@@ -669,7 +717,7 @@ struct cc_solver {
             tail_graphs.push_back(tg);
             hit = &tail_graphs.back();
         }
-        if (cudaGraphLaunch(hit->exec, stream) != cudaSuccess) return cuda_check("tail graph launch");
+        if (cudaGraphLaunch(hit->exec, tail_stream) != cudaSuccess) return cuda_check("tail graph launch");
         count_launch((int)hit->launches);
         return CC_OK;
     }
@@ -940,6 +988,8 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     bool ok = true;
     ok &= dalloc(&d_scenes, (size_t)n) == cudaSuccess;
     ok &= dalloc(&d_run, (size_t)n) == cudaSuccess;
+    ok &= dalloc(&d_tail_mask, (size_t)n) == cudaSuccess;
+    ok &= cudaMallocHost(&h_tail_masks, (size_t)n * (size_t)(n + 1)) == cudaSuccess;
     ok &= cudaMallocHost(&h_run, sizeof(SceneRun) * (size_t)n) == cudaSuccess;
     ok &= cudaMallocHost(&h_bbox, 6 * sizeof(unsigned long long) * (size_t)n) == cudaSuccess;
     ok &= dalloc(&d_vscene, (size_t)nv) == cudaSuccess;
@@ -1404,6 +1454,10 @@ cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, dou
     ev_marks.clear();
     prof(kStInit, true);
     step_init(x_old, x_cand, nv, d_in_elem, d_vscene, d_scenes, d_xo, d_av, d_ctr, stream);
+    // the strain records depend on x_old only
+    strain_setup(d_edges, nedges, d_scenes, strain_plan(), d_xo, d_strain_step, d_vscene, stream);
+    tail_done.assign((size_t)nscenes, 0);
+    tails_this_step = 0;
     reset_zones();
     bvh_this_step = false;
     reuse_pairs = false;
@@ -1465,22 +1519,22 @@ cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, dou
                     break;
             }
         }
+        if (overlap_tails) {
+            // once half the scenes have finished, they end their step now,
+            // beside the passes of the others (finalize, strain limiting,
+            // final velocities: one graph, whose strain loop ends on the
+            // device)
+            cc_status st = launch_tail(x_cand, x_out, vel, false);
+            if (st) return st;
+        }
     }
-    if (tail_graphs_on) {
-        // finalize, strain limiting and final velocities as one graph
-        // (the strain loop ends on the device); profiled as "strain"
-        prof(kStStrain, true);
-        cc_status st = run_tail_graph(x_cand, x_out, vel, hc);
+    {
+        cc_status st = launch_tail(x_cand, x_out, vel, true);
         if (st) return st;
-        prof(kStStrain, false);
-    } else {
-        prof(kStFinalize, true);
-        finalize_positions(d_in_elem, d_xo, d_av, d_hc, x_cand, x_out, nv, d_vscene, d_scenes, d_fixed, stream);
-        prof(kStFinalize, false);
-        prof(kStStrain, true);
-        tail_after_finalize(vel, hc);
-        prof(kStStrain, false);
     }
+    cudaEventRecord(ev_tail, tail_stream);
+    cudaStreamWaitEvent(stream, ev_tail, 0);
+    if (hc != d_hc) cudaMemcpyAsync(hc, d_hc, (size_t)nv, cudaMemcpyDeviceToDevice, stream);
     cudaMemcpyAsync(h_strain_passes.data(), d_strain_passes, sizeof(int) * h_strain_passes.size(),
                     cudaMemcpyDeviceToHost, stream);
     if (!bodies.empty()) {
@@ -1768,6 +1822,9 @@ cc_status cc_create(int device, cc_solver** out) {
     s->device = device;
     cudaSetDevice(device);
     if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->tail_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->ev_pass, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->ev_tail, cudaEventDisableTiming) != cudaSuccess ||
         dalloc(&s->d_ctr, 1) != cudaSuccess || cudaMallocHost(&s->h_ctr, sizeof(PassCounters)) != cudaSuccess) {
         delete s;
         return CC_CUDA_ERROR;
@@ -1891,6 +1948,9 @@ cc_status cc_set_tuning(cc_solver* s, int knob, int value) {
         case CC_TUNE_STRAIN_ROLES:
             s->strain_roles = value != 0;
             return CC_OK;
+        case CC_TUNE_TAIL_OVERLAP:
+            s->overlap_tails = value != 0;
+            return CC_OK;
         case CC_TUNE_STRAIN_BLOCK:
             if (value < 32 || value > 256 || value % 32) return CC_BAD_INPUT;
             s->tune.strain_block = value;
@@ -1917,6 +1977,7 @@ int cc_get_tuning(cc_solver* s, int knob) {
         case CC_TUNE_STRAIN_WARP: return s->strain_warp ? 1 : 0;
         case CC_TUNE_PACKET_TRAVERSE: return s->tune.packet_traverse ? 1 : 0;
         case CC_TUNE_STRAIN_ROLES: return s->strain_roles ? 1 : 0;
+        case CC_TUNE_TAIL_OVERLAP: return s->overlap_tails ? 1 : 0;
         default: return -1;
     }
 }

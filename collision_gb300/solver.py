@@ -184,7 +184,7 @@ class CollisionSolver3d:
         self._check(self._lib.cc_set_scene_domain_boundary(self._h, int(scene), lo.ctypes.data, hi.ctypes.data))
 
     TUNE_SPLIT_NARROW, TUNE_TRAVERSE_BLOCK, TUNE_NARROW_BLOCK, TUNE_STRAIN_BLOCK, TUNE_TAIL_GRAPH = 0, 1, 2, 3, 4
-    TUNE_COMBINED_BROAD, TUNE_STRAIN_WARP, TUNE_PACKET_TRAVERSE, TUNE_STRAIN_ROLES = 5, 6, 7, 8
+    TUNE_COMBINED_BROAD, TUNE_STRAIN_WARP, TUNE_PACKET_TRAVERSE, TUNE_STRAIN_ROLES, TUNE_TAIL_OVERLAP = 5, 6, 7, 8, 9
 
     def setTuning(self, knob: int, value: int):
         """Launch shapes and the two-stage narrow phase; none changes results."""

@@ -222,6 +222,14 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
  *                           stack; 0 (default): a stack per thread. Same
  *                           pairs; the packets are slower on the cloth
  *                           workloads, whose neighbouring queries diverge
+ *   CC_TUNE_TAIL_OVERLAP    1: once half the scenes have finished their
+ *                           detection passes, those end their step (final
+ *                           positions, strain limiting, final velocities) on
+ *                           a second stream while the other scenes' passes
+ *                           go on; 0 (default): every scene's end of step
+ *                           after the last pass. Same results; no faster on
+ *                           the cloth batches, whose strain sweep then
+ *                           competes with the passes for the SMs
  *   CC_TUNE_STRAIN_ROLES    1 (default): in the shared-memory strain sweep a
  *                           level's edges, copy-ins and write-backs run on
  *                           separate threads (when they fit in the block);
@@ -236,7 +244,8 @@ enum {
     CC_TUNE_COMBINED_BROAD = 5,
     CC_TUNE_STRAIN_WARP = 6,
     CC_TUNE_PACKET_TRAVERSE = 7,
-    CC_TUNE_STRAIN_ROLES = 8
+    CC_TUNE_STRAIN_ROLES = 8,
+    CC_TUNE_TAIL_OVERLAP = 9
 };
 cc_status cc_set_tuning(cc_solver* s, int knob, int value);
 int cc_get_tuning(cc_solver* s, int knob);

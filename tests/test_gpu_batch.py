@@ -54,7 +54,7 @@ def _split(a, off, i):
 
 
 def _run_batch(solver_cls, mix, nsteps, mode=0, window=True, record=False, split=True, graph=True, combined=True,
-               warp=False, packet=False, roles=True):
+               warp=False, packet=False, roles=True, overlap=False):
     b = solver_cls(0)
     b.assembleBatch(mix)
     b.setMode(mode)
@@ -65,6 +65,7 @@ def _run_batch(solver_cls, mix, nsteps, mode=0, window=True, record=False, split
     b.setTuning(solver_cls.TUNE_STRAIN_WARP, int(warp))
     b.setTuning(solver_cls.TUNE_PACKET_TRAVERSE, int(packet))
     b.setTuning(solver_cls.TUNE_STRAIN_ROLES, int(roles))
+    b.setTuning(solver_cls.TUNE_TAIL_OVERLAP, int(overlap))
     b.setRecording(record)
     pv, pe = b.sceneOffsets()
     x = np.concatenate([s.x for s in mix])
@@ -150,6 +151,10 @@ def test_batch_mixed_and_global_strain_equal_plain(solver_cls):
         _compare(ref, got, ("packet traversal", mode))
         got, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, roles=False)
         _compare(ref, got, ("strain sweep without separate roles", mode))
+        got, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, overlap=True)
+        _compare(ref, got, ("ends of steps beside the other scenes' passes", mode))
+        got, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, overlap=True, graph=False)
+        _compare(ref, got, ("overlapped ends of steps launched kernel by kernel", mode))
 
 
 def _compare(ref, got, tag):
