@@ -164,8 +164,12 @@ __device__ __forceinline__ int delta(const unsigned long long* keys, int n, int 
 
 // Karras, "Maximizing parallelism in the construction of BVHs, octrees and
 // k-d trees" (HPG 2012), with index tie-breaking for equal keys.
+// With rope given, the node that splits sorted leaves gamma and gamma+1
+// (every boundary has exactly one) records its right child as the rope of
+// that boundary, or kRopeEnd where the two leaves' scenes differ (the scene
+// id sits above the 30 Morton bits of the keys).
 __global__ void k_karras(const unsigned long long* __restrict__ keys, int n, BvhNode32* node, int* range_hi,
-                         int* range_lo, int* parent) {
+                         int* range_lo, int* parent, int* rope) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
     int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
@@ -194,6 +198,17 @@ __global__ void k_karras(const unsigned long long* __restrict__ keys, int n, Bvh
     if (left >= 0) parent[left] = i; else parent[n - 1 + ~left] = i;
     if (right >= 0) parent[right] = i; else parent[n - 1 + ~right] = i;
     if (i == 0) parent[0] = -1;
+    if (rope) rope[gamma] = ((keys[gamma] ^ keys[gamma + 1]) >> 30) ? kRopeEnd : right;
+}
+
+// Each internal node's first child and rope: a node covering sorted leaves
+// [lo, hi] is followed in depth-first order by the rope of boundary hi.
+__global__ void k_ropes(const BvhNode32* __restrict__ node, const int* __restrict__ rope, int n, RopeNode* rn) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const int4 meta = node[i].meta;
+    const int hi = meta.w;
+    *reinterpret_cast<int2*>(&rn[i].left) = make_int2(meta.x, hi < n - 1 ? rope[hi] : kRopeEnd);
 }
 
 struct Box32 {
@@ -230,11 +245,16 @@ __device__ __forceinline__ Box32 node_union_cg(const BvhNode32* nd) {
 
 // Bottom-up refit: the second child to arrive at a node writes the node's
 // two child boxes (leaf boxes rounded outward to FP32, internal children as
-// the union of their own records).
+// the union of their own records), and with rn given the node's own box.
+// With sub given, only those leaves and the nodes above them up to their
+// scenes' roots (a node with one child in an idle scene sees one arrival).
 __global__ void k_refit(const Box6* __restrict__ box, const unsigned int* __restrict__ order, int n,
-                        const int* __restrict__ parent, int* flags, BvhNode32* node) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+                        const int* __restrict__ sub, int nsub, const int* __restrict__ parent, int* flags,
+                        BvhNode32* node, RopeNode* rn) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= (sub ? nsub : n)) return;
+    const int i = sub ? sub[k] : k;
+    if (i < 0 || i >= n) return;  // sub lists sorted leaves of scenes of this hierarchy
     int nd = parent[n - 1 + i];
     while (nd >= 0) {
         __threadfence();
@@ -247,6 +267,12 @@ __global__ void k_refit(const Box6* __restrict__ box, const unsigned int* __rest
         q[0] = make_float4(a.lo[0], a.lo[1], a.lo[2], a.hi[0]);
         q[1] = make_float4(a.hi[1], a.hi[2], b.lo[0], b.lo[1]);
         q[2] = make_float4(b.lo[2], b.hi[0], b.hi[1], b.hi[2]);
+        if (rn) {
+            float* o = rn[nd].lo;
+            *reinterpret_cast<float4*>(o) = make_float4(fminf(a.lo[0], b.lo[0]), fminf(a.lo[1], b.lo[1]),
+                                                        fminf(a.lo[2], b.lo[2]), fmaxf(a.hi[0], b.hi[0]));
+            *reinterpret_cast<float2*>(o + 4) = make_float2(fmaxf(a.hi[1], b.hi[1]), fmaxf(a.hi[2], b.hi[2]));
+        }
         nd = parent[nd];
     }
 }
@@ -324,9 +350,15 @@ __device__ __forceinline__ void emit_pair(int a, int b, int2* pairs, int cap, Pa
 // false before any arithmetic (dcollid3d.cpp:493-497, 541-546, 578-582).
 // The leaf records of one pass (see LeafRec).
 __global__ void k_leaf_records(const Box6* __restrict__ box, const unsigned int* __restrict__ order, int n,
-                               const int* __restrict__ ev, LeafRec* out, int ne_all, PassCounters* ctr) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
+                               const int* __restrict__ sub, int nsub, const int* __restrict__ ev, LeafRec* out,
+                               int ne_all, PassCounters* ctr) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= (sub ? nsub : n)) return;
+    const int j = sub ? sub[k] : k;
+    if (j < 0 || j >= n) {
+        atomicOr(&ctr->err, kErrIndexLeaf);
+        return;
+    }
     const int e = (int)order[j];
     if (e < 0 || e >= ne_all) {
         atomicOr(&ctr->err, kErrIndexElem);
@@ -453,9 +485,15 @@ __global__ void k_traverse(const Box6* __restrict__ box, const unsigned int* __r
                            const BvhNode32* __restrict__ node, const int* __restrict__ elem_scene,
                            const SceneRun* __restrict__ run, const int* __restrict__ ev, int2* pairs, int cap,
                            PassCounters* ctr, const Box6* __restrict__ box_static,
-                           const LeafRec* __restrict__ leaves) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n - 1) return;
+                           const LeafRec* __restrict__ leaves, const int* __restrict__ sub, int nsub) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (sub ? nsub : n - 1)) return;
+    const int i = sub ? sub[t] : t;
+    if (i >= n - 1) return;  // the last leaf has no leaf after it
+    if (i < 0) {
+        atomicOr(&ctr->err, kErrIndexLeaf);
+        return;
+    }
     int ei, pi0 = -1, pi1 = -1, pi2 = -1;
     Box6 q;
     BoxOrd qo;
@@ -547,6 +585,86 @@ __global__ void k_traverse(const Box6* __restrict__ box, const unsigned int* __r
     }
 }
 
+// The same pairs without a stack. Thread i starts at the rope of its own
+// leaf - the subtree right after leaf i in depth-first order - so the nodes
+// above leaf i are never visited and only leaves after i are reached; an
+// overlapping node is entered at its first child, any other node (or leaf)
+// is left along its rope, and the walk ends at its scene's end (kRopeEnd).
+// Every step moves forward in depth-first order, so a walk takes fewer than
+// 2n steps; a longer one, or an index outside its array, sets an error bit
+// and ends the thread.
+__global__ void k_traverse_rope(int n, const RopeNode* __restrict__ rn, const int* __restrict__ rope,
+                                const int* __restrict__ elem_scene, const SceneRun* __restrict__ run,
+                                const int* __restrict__ ev, int2* pairs, int cap, PassCounters* ctr,
+                                const Box6* __restrict__ box_static, const LeafRec* __restrict__ leaves,
+                                const int* __restrict__ sub, int nsub) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (sub ? nsub : n - 1)) return;
+    const int i = sub ? sub[t] : t;
+    if (i >= n - 1) return;  // the last leaf has no leaf after it
+    if (i < 0) {
+        atomicOr(&ctr->err, kErrIndexLeaf);
+        return;
+    }
+    const LeafRec r = leaves[i];
+    const int ei = r.e;
+    if (ei < 0) return;  // flagged by k_leaf_records
+    if (run) {
+        const SceneRun sr = run[elem_scene[ei]];
+        if (sr.mode == kSceneIdle || sr.root < 0) return;
+    }
+    BoxOrd qo;
+    Box6 q;
+    for (int d = 0; d < 3; ++d) {
+        qo.lo[d] = r.lo[d];
+        qo.hi[d] = r.hi[d];
+        q.lo[d] = unord_double(r.lo[d]);
+        q.hi[d] = unord_double(r.hi[d]);
+    }
+    const int pi0 = ev ? r.p[0] : -1, pi1 = ev ? r.p[1] : -1, pi2 = ev ? r.p[2] : -1;
+    const Box32 q32 = box32_out(q);
+    BoxOrd qs;
+    if (box_static) qs = box_ord(box_static[ei]);
+    int x = __ldg(&rope[i]);
+    for (int steps = 0; x != kRopeEnd; ++steps) {
+        if (steps >= 2 * n) {
+            atomicOr(&ctr->err, kErrIndexNode);
+            return;
+        }
+        if (x >= 0) {
+            if (x >= n - 1) {
+                atomicOr(&ctr->err, kErrIndexNode);
+                return;
+            }
+            const float4* p4 = reinterpret_cast<const float4*>(&rn[x]);
+            const float4 a = __ldg(p4), b = __ldg(p4 + 1);  // lo xyz hi.x | hi.y hi.z left rope
+            const bool hit = q32.lo[0] <= a.w && q32.hi[0] >= a.x && q32.lo[1] <= b.x && q32.hi[1] >= a.y &&
+                             q32.lo[2] <= b.y && q32.hi[2] >= a.z;
+            x = __float_as_int(hit ? b.z : b.w);
+            continue;
+        }
+        const int k = ~x;
+        if (k >= n) {
+            atomicOr(&ctr->err, kErrIndexLeaf);
+            return;
+        }
+        x = k < n - 1 ? __ldg(&rope[k]) : kRopeEnd;
+        const ulonglong2* lr = reinterpret_cast<const ulonglong2*>(&leaves[k]);
+        const ulonglong2 u0 = __ldg(lr), u1 = __ldg(lr + 1), u2 = __ldg(lr + 2);
+        // the exact test on the encoded boxes
+        if (!(qo.lo[0] <= u1.y && qo.hi[0] >= u0.x && qo.lo[1] <= u2.x && qo.hi[1] >= u0.y && qo.lo[2] <= u2.y &&
+              qo.hi[2] >= u1.x))
+            continue;
+        const int4 pe = __ldg(reinterpret_cast<const int4*>(lr + 3));
+        const int ej = pe.w;
+        if (ej < 0) continue;  // flagged by k_leaf_records
+        if (ev && (pe.x == pi0 || pe.x == pi1 || pe.x == pi2 || pe.y == pi0 || pe.y == pi1 || pe.y == pi2 ||
+                   (pe.z >= 0 && (pe.z == pi0 || pe.z == pi1 || pe.z == pi2))))
+            continue;
+        emit_pair(ei, (box_static && overlap_ord(qs, &box_static[ej])) ? (ej | kPairStatic) : ej, pairs, cap, ctr);
+    }
+}
+
 __global__ void k_brute_pairs(const Box6* __restrict__ box, int n, const int* __restrict__ elem_scene, int2* pairs,
                               int cap, PassCounters* ctr) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -610,9 +728,13 @@ void bvh_build(const Box6* box, BvhBufs& b, cudaStream_t s) {
     int bits = 30;
     while (bits < 62 && (b.nscenes - 1) >> (bits - 30)) ++bits;
     radix_sort_pairs(b.keys, b.order, n, bits, b.sort_temp, s);
-    count_launch(), k_karras<<<nblk(n - 1, 256), 256, 0, s>>>(b.keys, n, b.node, b.range_hi, b.range_lo, b.parent);
+    const bool ropes = b.rnode && b.rope;
+    count_launch(), k_karras<<<nblk(n - 1, 256), 256, 0, s>>>(b.keys, n, b.node, b.range_hi, b.range_lo, b.parent,
+                                                              ropes ? b.rope : nullptr);
+    if (ropes) count_launch(), k_ropes<<<nblk(n - 1, 256), 256, 0, s>>>(b.node, b.rope, n, b.rnode);
     cudaMemsetAsync(b.flags, 0, sizeof(int) * (size_t)(n - 1), s);
-    count_launch(), k_refit<<<nblk(n, 256), 256, 0, s>>>(box, b.order, n, b.parent, b.flags, b.node);
+    count_launch(), k_refit<<<nblk(n, 256), 256, 0, s>>>(box, b.order, n, nullptr, 0, b.parent, b.flags, b.node,
+                                                         ropes ? b.rnode : nullptr);
     if (b.run)
         count_launch(), k_scene_roots<<<nblk(b.nscenes, 128), 128, 0, s>>>(b.scenes, b.run, b.nscenes, n, b.parent,
                                                                           b.range_lo, b.range_hi);
@@ -622,25 +744,35 @@ void bvh_refit(const Box6* box, BvhBufs& b, cudaStream_t s) {
     int n = b.n;
     if (n <= 1) return;
     cudaMemsetAsync(b.flags, 0, sizeof(int) * (size_t)(n - 1), s);
-    count_launch(), k_refit<<<nblk(n, 256), 256, 0, s>>>(box, b.order, n, b.parent, b.flags, b.node);
+    const int nleaf = b.sub ? b.nsub : n;
+    if (nleaf > 0)
+        count_launch(), k_refit<<<nblk(nleaf, 256), 256, 0, s>>>(box, b.order, n, b.sub, b.nsub, b.parent, b.flags,
+                                                                 b.node, b.rnode && b.rope ? b.rnode : nullptr);
     if (b.run)
         count_launch(), k_scene_roots<<<nblk(b.nscenes, 128), 128, 0, s>>>(b.scenes, b.run, b.nscenes, n, b.parent,
                                                                           b.range_lo, b.range_hi);
 }
 
 void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCounters* ctr, cudaStream_t s,
-               const int* skip_shared_ev, int block, const Box6* box_static, bool packet) {
+               const int* skip_shared_ev, int block, const Box6* box_static, bool packet, bool rope) {
     int n = b.n;
     if (n <= 1) return;
+    const int nleaf = b.sub ? b.nsub : n, nq = b.sub ? b.nsub : n - 1;
+    if (nq <= 0) return;
     if (b.leaf)
-        count_launch(), k_leaf_records<<<nblk(n, 256), 256, 0, s>>>(box, b.order, n, b.ev, b.leaf, b.ne_all, ctr);
-    if (b.leaf && packet)
+        count_launch(), k_leaf_records<<<nblk(nleaf, 256), 256, 0, s>>>(box, b.order, n, b.sub, b.nsub, b.ev,
+                                                                        b.leaf, b.ne_all, ctr);
+    if (b.leaf && rope && b.rnode && b.rope)
+        count_launch(), k_traverse_rope<<<nblk(nq, block), block, 0, s>>>(
+            n, b.rnode, b.rope, b.elem_scene, b.run, skip_shared_ev, pairs, cap, ctr, box_static, b.leaf, b.sub,
+            b.nsub);
+    else if (b.leaf && packet && !b.sub)
         count_launch(), k_traverse_packet<<<nblk(n - 1, kPacketWarps * 32), kPacketWarps * 32, 0, s>>>(
             b.order, n, b.node, b.elem_scene, b.run, skip_shared_ev, pairs, cap, ctr, box_static, b.leaf);
     else
-        count_launch(), k_traverse<<<nblk(n - 1, block), block, 0, s>>>(box, b.order, n, b.node, b.elem_scene, b.run,
-                                                                        skip_shared_ev, pairs, cap, ctr, box_static,
-                                                                        b.leaf);
+        count_launch(), k_traverse<<<nblk(nq, block), block, 0, s>>>(box, b.order, n, b.node, b.elem_scene, b.run,
+                                                                     skip_shared_ev, pairs, cap, ctr, box_static,
+                                                                     b.leaf, b.sub, b.nsub);
 }
 
 void brute_pairs(const Box6* box, int ne, const int* elem_scene, int2* pairs, int cap, PassCounters* ctr,

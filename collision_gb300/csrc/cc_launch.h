@@ -16,6 +16,7 @@ inline void count_launch(int n = 1) { g_kernel_launches += n; }
 // Launch shapes that do not change results (set through cc_set_tuning).
 struct LaunchTuning {
     bool packet_traverse = false;  // warp-cooperative traversal (k_traverse_packet)
+    bool rope_traverse = true;     // stackless traversal along ropes (k_traverse_rope)
     int traverse_block = 128;     // threads per block of the per-thread traversal
     int narrow_block = 128;
     int strain_block = 256;
@@ -49,6 +50,17 @@ struct __align__(16) BvhNode32 {
     int4 meta;  // child 0, child 1, last leaf under child 0, under child 1
 };
 
+// An internal LBVH node as the stackless traversal reads it: its own box in
+// FP32 (rounded outward), its first child (>= 0 internal, < 0 ~leaf) and its
+// rope - the subtree that follows it in depth-first order within its scene
+// (kRopeEnd: none).
+struct __align__(32) RopeNode {
+    float lo[3], hi[3];
+    int left;
+    int rope;
+};
+constexpr int kRopeEnd = 0x7fffffff;
+
 // A sorted leaf as the traversal's exact test reads it: the element's FP64
 // box in the order-preserving integer encoding (lo xyz, hi xyz), its points
 // (third -1 for a bond) and its id - one 64-byte record per leaf visit, with
@@ -80,6 +92,17 @@ struct BvhBufs {
     struct LeafRec* leaf;
     const int* ev;
     int ne_all;  // elements of all scenes (bound of the ids in order)
+    // optional: the stackless traversal's nodes and the rope of every leaf
+    // boundary (rope[k]: the subtree after sorted leaf k in depth-first
+    // order, the right child of the node that splits leaves k and k+1),
+    // filled by bvh_build and bvh_refit
+    RopeNode* rnode;  // n-1
+    int* rope;        // n-1
+    // optional: for a hierarchy over all elements (act null), the sorted
+    // leaves of the scenes in this pass; the refit, the leaf records and the
+    // traversal then cover only those (walks never leave their scene)
+    const int* sub;
+    int nsub;
 };
 
 // Leaf boxes of every element (static: x_old; moving: x_old and
@@ -106,10 +129,12 @@ void bvh_refit(const Box6* box, BvhBufs& b, cudaStream_t s);
 // once; scenes idle in this pass are skipped. With skip_shared_ev (the
 // elements' point ids), pairs of elements sharing a point are left out.
 // With box_static, every pair is found on `box` (swept boxes) and carries
-// kPairStatic when the elements' static boxes overlap as well.
+// kPairStatic when the elements' static boxes overlap as well. Traversal:
+// a stack per thread (default), a warp-cooperative packet, or (rope, with
+// the leaf records and rope nodes present) stackless along the ropes.
 void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCounters* ctr, cudaStream_t s,
                const int* skip_shared_ev = nullptr, int block = 128, const Box6* box_static = nullptr,
-               bool packet = false);
+               bool packet = false, bool rope = false);
 // The same pair set by testing every pair (for cross-checks on small meshes).
 void brute_pairs(const Box6* box, int ne, const int* elem_scene, int2* pairs, int cap, PassCounters* ctr,
                  cudaStream_t s);

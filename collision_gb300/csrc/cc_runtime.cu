@@ -366,6 +366,22 @@ struct cc_solver {
     // step over the same scenes refit it instead of building anew
     bool bvh_this_step = false;
     std::vector<int> bvh_set, cur_set;
+    // the LBVH in bvh was built this step over all elements; with
+    // subset_refit, later passes over some of the scenes refit it over those
+    // scenes' leaves instead of building their own
+    bool full_this_step = false;
+    bool subset_refit = true;
+    // The hierarchy over all elements, restricted to the scenes of this pass:
+    // scene s's sorted leaves there are its element range [e0, e0 + ne), so
+    // the pass's element list doubles as its list of leaves.
+    BvhBufs full_view() const {
+        BvhBufs f = bvh;
+        f.n = ne;
+        f.act = nullptr;
+        f.sub = bvh.act;
+        f.nsub = bvh.n;
+        return f;
+    }
 
     // VTK dumps of every pass (empty: off)
     std::string vtk_dir;
@@ -450,6 +466,7 @@ struct cc_solver {
         dfree(d_xold_in); dfree(d_xcand_in); dfree(d_vel); dfree(d_xout); dfree(d_hc);
         dfree(d_box); dfree(d_box_st); dfree(bvh.keys); dfree(bvh.order); dfree(bvh.range_hi);
         dfree(bvh.range_lo); dfree(bvh.parent); dfree(bvh.flags); dfree(bvh.node); dfree(bvh.bbox_enc); dfree(bvh.leaf);
+        dfree(bvh.rnode); dfree(bvh.rope);
         if (bvh.sort_temp) cudaFree(bvh.sort_temp);
         bvh = BvhBufs{};
         dfree(d_pairs); dfree(d_contrib); dfree(d_pair_hit); dfree(d_pairq); dfree(d_sub_pt); dfree(d_sub_ee);
@@ -1030,6 +1047,8 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     ok &= dalloc(&bvh.flags, (size_t)ne) == cudaSuccess;
     ok &= dalloc(&bvh.node, (size_t)ne) == cudaSuccess;
     ok &= dalloc(&bvh.leaf, (size_t)ne) == cudaSuccess;
+    ok &= dalloc(&bvh.rnode, (size_t)ne) == cudaSuccess;
+    ok &= dalloc(&bvh.rope, (size_t)ne) == cudaSuccess;
     ok &= dalloc(&bvh.bbox_enc, 6 * (size_t)n) == cudaSuccess;
     ok &= cudaMalloc(&bvh.sort_temp, radix_sort_temp_bytes(ne > 0 ? ne : 1)) == cudaSuccess;
     ok &= dalloc(&apply.cnt, (size_t)nv + nbodies) == cudaSuccess;
@@ -1204,12 +1223,17 @@ cc_status cc_solver::update_trees(int which, const Box6* boxes) {
 // every scene's hit count in h_run.
 cc_status cc_solver::detect_pass(int moving, bool any_zone) {
     select_active();
-    cudaMemcpyAsync(d_run, h_run, sizeof(SceneRun) * (size_t)nscenes, cudaMemcpyHostToDevice, stream);
     // proximity pass: pairs on swept boxes with the static-overlap flag;
     // first CCD pass after a proximity pass without impulses: those pairs
     const bool combined = combined_broad && !moving;
     const bool reuse = moving && reuse_pairs && cur_set == reuse_set;
     reuse_pairs = false;
+    // some of the scenes, after this step's hierarchy over all elements: it
+    // is refit over their leaves, where each scene starts at its e0
+    const bool on_full = subset_refit && !reuse && full_this_step && bvh.act != nullptr;
+    if (on_full)
+        for (int s : cur_set) h_run[s].leaf0 = scenes[s].e0;
+    cudaMemcpyAsync(d_run, h_run, sizeof(SceneRun) * (size_t)nscenes, cudaMemcpyHostToDevice, stream);
     cc_status st = CC_OK;
     prof(kStBoxes, true);
     if (combined) {
@@ -1228,12 +1252,16 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
     prof(kStBvh, true);
     if (reuse) {
         // the hierarchy and the pairs of the proximity pass stand
+    } else if (on_full) {
+        BvhBufs fv = full_view();
+        bvh_refit(d_box, fv, stream);
     } else if (bvh_this_step && cur_set == bvh_set) {
         bvh_refit(d_box, bvh, stream);
     } else {
         bvh_build(d_box, bvh, stream);
         bvh_this_step = true;
         bvh_set = cur_set;
+        full_this_step = bvh.act == nullptr;
     }
     if (mode == 1)
         point_boxes(d_xo, d_av, d_vscene, d_scenes, bvh.act ? d_act_p : nullptr, n_act_p, moving, d_pbox_lo,
@@ -1247,8 +1275,9 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
                                                                                 reuse ? reuse_npairs : -1);
         if (!reuse) {
             prof(kStTraverse, true);
-            bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, record ? nullptr : d_ev, tune.traverse_block,
-                      combined ? d_box_st : nullptr, tune.packet_traverse);
+            bvh_pairs(d_box, on_full ? full_view() : bvh, d_pairs, pair_cap, d_ctr, stream, record ? nullptr : d_ev,
+                      tune.traverse_block,
+                      combined ? d_box_st : nullptr, tune.packet_traverse, tune.rope_traverse);
             prof(kStTraverse, false);
             if (attempt == 0) counters[16] += bvh.n;
         }
@@ -1460,6 +1489,7 @@ cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, dou
     tails_this_step = 0;
     reset_zones();
     bvh_this_step = false;
+    full_this_step = false;
     reuse_pairs = false;
     prof(kStInit, false);
     for (bool first = true;; first = false) {
@@ -1610,12 +1640,13 @@ cc_status cc_solver::check_ccd(const double* x_old, const double* x_new, long lo
     cudaMemcpyAsync(d_run, h_run, sizeof(SceneRun) * (size_t)nscenes, cudaMemcpyHostToDevice, stream);
     leaf_boxes(d_ev, bvh.act, bvh.n, d_escene, d_scenes, nscenes, d_xo, d_av, 1, d_box, bvh.bbox_enc, stream);
     bvh_this_step = false;  // the pass hierarchy and pairs are replaced
+    full_this_step = false;
     reuse_pairs = false;
     bvh_build(d_box, bvh, stream);
     for (int attempt = 0; attempt < 8; ++attempt) {
         count_launch(), k_reset_pass<<<(nscenes + 255) / 256, 256, 0, stream>>>(d_ctr, d_run, nscenes);
         bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, d_ev, tune.traverse_block, nullptr,
-                  tune.packet_traverse);
+                  tune.packet_traverse, tune.rope_traverse);
         NarrowArgs a{};
         a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
         a.vbody = d_vbody; a.body_mass = d_body_mass; a.body_slot0 = nv;
@@ -1664,6 +1695,7 @@ cc_status cc_solver::autotune(double* best_ms) {
     cudaMemcpyAsync(d_run, h_run, sizeof(SceneRun) * (size_t)nscenes, cudaMemcpyHostToDevice, stream);
     leaf_boxes(d_ev, bvh.act, bvh.n, d_escene, d_scenes, nscenes, d_xo, d_av, 1, d_box, bvh.bbox_enc, stream);
     bvh_this_step = false;
+    full_this_step = false;
     reuse_pairs = false;
     bvh_build(d_box, bvh, stream);
     if (mode == 1)
@@ -1679,7 +1711,7 @@ cc_status cc_solver::autotune(double* best_ms) {
             count_launch(), k_reset_pass<<<(nscenes + 255) / 256, 256, 0, stream>>>(d_ctr, d_run, nscenes);
             cudaEventRecord(e0, stream);
             bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, d_ev, t.traverse_block, nullptr,
-                      t.packet_traverse);
+                      t.packet_traverse, t.rope_traverse);
             NarrowArgs a{};
             a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
         a.vbody = d_vbody; a.body_mass = d_body_mass; a.body_slot0 = nv;
@@ -1743,12 +1775,17 @@ cc_status cc_solver::autotune(double* best_ms) {
     cc_status st = time_it(best_t, best_split, &best);  // the current setting, which also sizes the buffers
     const int tb[] = {64, 128, 256, 512};
     const int nb[] = {64, 128, 256};
-    for (int a : tb) {  // the traversal with a stack per thread (the warp packets are slower on cloth)
-        LaunchTuning t = best_t;
-        t.traverse_block = a;
-        float m;
-        if (!st) st = time_it(t, best_split, &m);
-        if (!st && m < best) { best = m; best_t = t; }
+    // the stackless traversal and the one with a stack per thread (the warp
+    // packets are slower on cloth)
+    for (int rope = 1; rope >= 0; --rope) {
+        for (int a : tb) {
+            LaunchTuning t = best_t;
+            t.rope_traverse = rope != 0;
+            t.traverse_block = a;
+            float m;
+            if (!st) st = time_it(t, best_split, &m);
+            if (!st && m < best) { best = m; best_t = t; }
+        }
     }
     for (int split = (mode == 1 ? 0 : 1); split <= (mode == 1 ? 1 : 0) && !st; ++split) {
         for (int b : nb) {
@@ -1951,6 +1988,12 @@ cc_status cc_set_tuning(cc_solver* s, int knob, int value) {
         case CC_TUNE_TAIL_OVERLAP:
             s->overlap_tails = value != 0;
             return CC_OK;
+        case CC_TUNE_ROPE_TRAVERSE:
+            s->tune.rope_traverse = value != 0;
+            return CC_OK;
+        case CC_TUNE_SUBSET_REFIT:
+            s->subset_refit = value != 0;
+            return CC_OK;
         case CC_TUNE_STRAIN_BLOCK:
             if (value < 32 || value > 256 || value % 32) return CC_BAD_INPUT;
             s->tune.strain_block = value;
@@ -1978,6 +2021,8 @@ int cc_get_tuning(cc_solver* s, int knob) {
         case CC_TUNE_PACKET_TRAVERSE: return s->tune.packet_traverse ? 1 : 0;
         case CC_TUNE_STRAIN_ROLES: return s->strain_roles ? 1 : 0;
         case CC_TUNE_TAIL_OVERLAP: return s->overlap_tails ? 1 : 0;
+        case CC_TUNE_ROPE_TRAVERSE: return s->tune.rope_traverse ? 1 : 0;
+        case CC_TUNE_SUBSET_REFIT: return s->subset_refit ? 1 : 0;
         default: return -1;
     }
 }
@@ -2128,6 +2173,7 @@ int cc_debug_candidate_pairs(cc_solver* s, int moving, int brute_force, int* out
     leaf_boxes(s->d_ev, s->bvh.act, s->bvh.n, s->d_escene, s->d_scenes, s->nscenes, s->d_xo, s->d_av, moving,
                s->d_box, s->bvh.bbox_enc, s->stream);
     s->bvh_this_step = false;
+    s->full_this_step = false;
     s->reuse_pairs = false;
     if (!brute_force) bvh_build(s->d_box, s->bvh, s->stream);
     for (int attempt = 0; attempt < 8; ++attempt) {
@@ -2137,7 +2183,7 @@ int cc_debug_candidate_pairs(cc_solver* s, int moving, int brute_force, int* out
             brute_pairs(s->d_box, s->ne, s->d_escene, s->d_pairs, s->pair_cap, s->d_ctr, s->stream);
         else
             bvh_pairs(s->d_box, s->bvh, s->d_pairs, s->pair_cap, s->d_ctr, s->stream, nullptr, s->tune.traverse_block,
-                      nullptr, s->tune.packet_traverse);
+                      nullptr, s->tune.packet_traverse, s->tune.rope_traverse);
         cudaMemcpyAsync(s->h_ctr, s->d_ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, s->stream);
         if (cudaStreamSynchronize(s->stream) != cudaSuccess) return -1;
         if (s->h_ctr->err & kErrPairOverflow) {

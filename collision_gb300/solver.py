@@ -185,6 +185,7 @@ class CollisionSolver3d:
 
     TUNE_SPLIT_NARROW, TUNE_TRAVERSE_BLOCK, TUNE_NARROW_BLOCK, TUNE_STRAIN_BLOCK, TUNE_TAIL_GRAPH = 0, 1, 2, 3, 4
     TUNE_COMBINED_BROAD, TUNE_STRAIN_WARP, TUNE_PACKET_TRAVERSE, TUNE_STRAIN_ROLES, TUNE_TAIL_OVERLAP = 5, 6, 7, 8, 9
+    TUNE_ROPE_TRAVERSE, TUNE_SUBSET_REFIT = 10, 11
 
     def setTuning(self, knob: int, value: int):
         """Launch shapes and the two-stage narrow phase; none changes results."""
@@ -199,6 +200,7 @@ class CollisionSolver3d:
         ms = C.c_double(0.0)
         self._check(self._lib.cc_autotune(self._h, C.byref(ms)))
         return {"packet_traverse": self.getTuning(self.TUNE_PACKET_TRAVERSE),
+                "rope_traverse": self.getTuning(self.TUNE_ROPE_TRAVERSE),
                 "traverse_block": self.getTuning(self.TUNE_TRAVERSE_BLOCK),
                 "split_narrow": self.getTuning(self.TUNE_SPLIT_NARROW),
                 "narrow_block": self.getTuning(self.TUNE_NARROW_BLOCK), "pass_ms": ms.value}

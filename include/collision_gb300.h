@@ -230,6 +230,16 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
  *                           after the last pass. Same results; no faster on
  *                           the cloth batches, whose strain sweep then
  *                           competes with the passes for the SMs
+ *   CC_TUNE_ROPE_TRAVERSE   1 (default): each query walks the hierarchy
+ *                           without a stack, from the subtree after its own
+ *                           leaf along ropes (the next subtree in depth-first
+ *                           order); 0: a stack per thread from the scene's
+ *                           root. Same pairs
+ *   CC_TUNE_SUBSET_REFIT    1 (default): a detection pass over some of the
+ *                           scenes, after the step's first pass built the
+ *                           hierarchy over all of them, refits that hierarchy
+ *                           over its scenes' leaves; 0: it sorts and builds a
+ *                           hierarchy of its own. Same pairs
  *   CC_TUNE_STRAIN_ROLES    1 (default): in the shared-memory strain sweep a
  *                           level's edges, copy-ins and write-backs run on
  *                           separate threads (when they fit in the block);
@@ -245,7 +255,9 @@ enum {
     CC_TUNE_STRAIN_WARP = 6,
     CC_TUNE_PACKET_TRAVERSE = 7,
     CC_TUNE_STRAIN_ROLES = 8,
-    CC_TUNE_TAIL_OVERLAP = 9
+    CC_TUNE_TAIL_OVERLAP = 9,
+    CC_TUNE_ROPE_TRAVERSE = 10,
+    CC_TUNE_SUBSET_REFIT = 11
 };
 cc_status cc_set_tuning(cc_solver* s, int knob, int value);
 int cc_get_tuning(cc_solver* s, int knob);

@@ -54,7 +54,7 @@ def _split(a, off, i):
 
 
 def _run_batch(solver_cls, mix, nsteps, mode=0, window=True, record=False, split=True, graph=True, combined=True,
-               warp=False, packet=False, roles=True, overlap=False):
+               warp=False, packet=False, roles=True, overlap=False, rope=True, subset_refit=True):
     b = solver_cls(0)
     b.assembleBatch(mix)
     b.setMode(mode)
@@ -64,6 +64,8 @@ def _run_batch(solver_cls, mix, nsteps, mode=0, window=True, record=False, split
     b.setTuning(solver_cls.TUNE_COMBINED_BROAD, int(combined))
     b.setTuning(solver_cls.TUNE_STRAIN_WARP, int(warp))
     b.setTuning(solver_cls.TUNE_PACKET_TRAVERSE, int(packet))
+    b.setTuning(solver_cls.TUNE_ROPE_TRAVERSE, int(rope))
+    b.setTuning(solver_cls.TUNE_SUBSET_REFIT, int(subset_refit))
     b.setTuning(solver_cls.TUNE_STRAIN_ROLES, int(roles))
     b.setTuning(solver_cls.TUNE_TAIL_OVERLAP, int(overlap))
     b.setRecording(record)
@@ -143,12 +145,21 @@ def test_batch_mixed_and_global_strain_equal_plain(solver_cls):
                                combined=comb)
         _compare(ref, got, (mode, window, split, graph, comb))
     # the one-warp staged sweep instead of the CTA-per-scene one, and the
-    # warp-packet traversal instead of the one with a stack per thread
+    # warp-packet traversal or the one with a stack per thread instead of the
+    # stackless one
     for mode in (0, 1):
         got, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, warp=True)
         _compare(ref, got, ("warp sweep", mode))
-        got, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, packet=True)
+        got, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, packet=True, rope=False)
         _compare(ref, got, ("packet traversal", mode))
+        got, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, rope=False)
+        _compare(ref, got, ("traversal with a stack per thread", mode))
+        got, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, rope=False, combined=False)
+        _compare(ref, got, ("stack per thread, separate proximity and CCD broad phases", mode))
+        got, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, subset_refit=False)
+        _compare(ref, got, ("a hierarchy of their own for passes over some scenes", mode))
+        got, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, subset_refit=True, rope=False)
+        _compare(ref, got, ("stack per thread over some scenes' leaves", mode))
         got, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, roles=False)
         _compare(ref, got, ("strain sweep without separate roles", mode))
         got, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, overlap=True)

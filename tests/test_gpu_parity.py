@@ -58,13 +58,14 @@ def test_gpu_matches_reference_golden(solver_cls, path):
     s.close()
 
 
-def _oracle_run(sc, nsteps, solver_cls, record=True):
+def _oracle_run(sc, nsteps, solver_cls, record=True, rope=True):
     from collision_gb300.solver import ordered_visits
     from oracle.ccopy import OracleSolver, REC_PAIRS
     o = OracleSolver(sc, record=REC_PAIRS if record else 0)
     s = solver_cls(0)
     s.assembleFromScene(sc)
     s.setRecording(record)
+    s.setTuning(s.TUNE_ROPE_TRAVERSE, int(rope))
     x, v, hc = sc.x.copy(), sc.v.copy(), np.zeros(sc.nv, np.uint8)
     worst = [0.0, 0.0]
     for step in range(nsteps):
@@ -106,19 +107,29 @@ def test_gpu_vs_oracle_folded_self_collision(solver_cls):
     _oracle_run(sc, 6, solver_cls)
 
 
+def test_gpu_vs_oracle_stack_traversal(solver_cls):
+    # the traversal with a stack per thread instead of the stackless one:
+    # the same visit record, pass sequence and state
+    sc = scenes.folded_cloth(n=33, dt=5e-4, h=2e-3, seed=1, vscale=20.0)
+    _oracle_run(sc, 6, solver_cls, rope=False)
+
+
 def test_lbvh_pairs_equal_all_pairs(solver_cls):
     sc = scenes.folded_cloth(n=33, dt=5e-4, h=2e-3, seed=1, vscale=20.0)
     s = solver_cls(0)
     s.assembleFromScene(sc)
     s.resolveCollision(sc.x, scenes.candidate(sc, sc.x, sc.v), sc.v, np.zeros(sc.nv, np.uint8))
-    for packet in (1, 0):  # the warp-packet traversal and the one with a stack per thread
+    # the warp-packet traversal, the stackless one along ropes, and the one
+    # with a stack per thread
+    for packet, rope in ((1, 0), (0, 1), (0, 0)):
         s.setTuning(s.TUNE_PACKET_TRAVERSE, packet)
+        s.setTuning(s.TUNE_ROPE_TRAVERSE, rope)
         for moving in (False, True):
             a = s.candidatePairs(moving, brute_force=False)
             b = s.candidatePairs(moving, brute_force=True)
             ka = np.sort(np.minimum(a[:, 0], a[:, 1]).astype(np.int64) * sc.ne + np.maximum(a[:, 0], a[:, 1]))
             kb = np.sort(np.minimum(b[:, 0], b[:, 1]).astype(np.int64) * sc.ne + np.maximum(b[:, 0], b[:, 1]))
-            assert len(ka) > 0 and np.array_equal(ka, kb), packet
+            assert len(ka) > 0 and np.array_equal(ka, kb), (packet, rope)
     s.close()
 
 
