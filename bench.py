@@ -57,9 +57,11 @@ METRIC = "cloth collision steps/s: mixed-prec batched vs FP64 plain, 0 missed CC
 UNIT = "scene-steps/s"
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 NARROW_BYTES_PER_VISIT = 8 + 8 + 24 + 6 * 64  # pair, two leaf ranks, two elements' ids, x_old+avgVel of 6 points
-# k_traverse's DRAM traffic per query leaf, measured with ncu on the batched
-# workload cut to 96 scenes (221 MB per launch of 1,298,248 leaves)
-TRAVERSE_DRAM_BYTES_PER_LEAF = 170.4
+# The traversal's DRAM traffic per query leaf, measured with ncu on the
+# batched workload cut to 96 scenes (launches of 1,298,248 query leaves):
+# k_traverse_rope 184 MB per launch, k_traverse (a stack per thread) 221 MB
+TRAVERSE_DRAM_BYTES_PER_LEAF = {True: 141.6, False: 170.4}
+TRAVERSE_LANES_ACTIVE = {True: 6.3, False: 7.4}
 
 
 def make_workload(name, seed, nscenes=0, large_n=1025):
@@ -298,10 +300,11 @@ def run_gpu(args):
         torch.cuda.synchronize()
         step_ms = [a.elapsed_time(b) for a, b in evs]
         prof = s.profile()
+        rope = bool(s.getTuning(CollisionSolver3d.TUNE_ROPE_TRAVERSE))
         s.close()
         return dict(total_ms=max_over_ranks(float(sum(step_ms))), step_ms=step_ms, counters=counters,
                     missed=missed, snap=snap, prof=prof, clocks=clk.summary(), scene_steps=scene_steps,
-                    capped=int((~enabled).sum()), tuned=tuned)
+                    capped=int((~enabled).sum()), tuned=tuned, rope=rope)
 
     # ------------------------------ plain FP64, one scene at a time
     def plain_sequential():
@@ -524,24 +527,32 @@ def run_gpu(args):
         # one read of the hierarchy's FP32 boxes per traversal, (2n-1)*24 B
         # for n leaves, and the 8-byte pairs written
         per = (48.0 * tot["broad_leaves"] + 8.0 * tot["broad_pairs"]) / calls
-        kern["traverse"] = {"kernel": "k_traverse (LBVH broad phase, with its leaf records)", "bytes_per_launch": per,
+        kern["traverse"] = {"kernel": ("k_traverse_rope (LBVH broad phase, stackless along ropes)" if mixed["rope"]
+                                       else "k_traverse (LBVH broad phase, a stack per thread)"),
+                            "bytes_per_launch": per,
                             "ms_per_launch": ms / calls, "achieved": per / (ms / calls / 1e3) / 1e9}
     roof = None
     if kern:
-        # the largest single kernel of the timed steps in the launch list
-        # (profiles/launch_list_batched_256_mixed.md) is the traversal; the
-        # strain stage is several kernels
+        # the two largest kernels of the timed steps in the launch list
+        # (profiles/launch_list_batched_256_mixed.md) are the strain sweep
+        # (23% of the step) and the traversal (22%); the traversal is timed
+        # per launch here, the strain stage only as a whole (several kernels
+        # in one graph), so the traversal is the roofline entry and the
+        # strain stage is listed under "kernels"
         top = "traverse" if "traverse" in kern else max(kern, key=lambda k: prof[k][0])
         kt = kern[top]
         traffic = None
         if top == "traverse":
             # DRAM bytes read + written per query leaf from one ncu capture
-            # (profiles/k_traverse_batched_96.md), scaled to this run's launches
-            traffic = TRAVERSE_DRAM_BYTES_PER_LEAF * tot["broad_leaves"] / max(prof["traverse"][1], 1)
+            # (profiles/k_traverse_rope_batched_96.md, k_traverse_batched_96.md),
+            # scaled to this run's launches
+            traffic = (TRAVERSE_DRAM_BYTES_PER_LEAF[mixed["rope"]] * tot["broad_leaves"] /
+                       max(prof["traverse"][1], 1))
         roof = {"bound": "hbm", "kernel": kt["kernel"], "achieved": kt["achieved"], "peak": hbm, "unit": "GB/s",
                 "frac": kt["achieved"] / hbm, "peak_source": peak_src, "traffic": traffic,
-                "note": "latency and divergence bound (7.7 of 32 lanes active per instruction, dependent node "
-                        "loads), not bandwidth bound", "kernels": kern}
+                "note": f"latency and divergence bound ({TRAVERSE_LANES_ACTIVE[mixed['rope']]} of 32 lanes active "
+                        "per instruction, dependent node loads), not bandwidth bound; k_strain_window has a "
+                        "similar share of the step (kernels.strain)", "kernels": kern}
     cpu = None
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
