@@ -533,9 +533,9 @@ def run_gpu(args):
                             "ms_per_launch": ms / calls, "achieved": per / (ms / calls / 1e3) / 1e9}
     roof = None
     if kern:
-        # the two largest kernels of the timed steps in the launch list
-        # (profiles/launch_list_batched_256_mixed.md) are the strain sweep
-        # (23% of the step) and the traversal (22%); the traversal is timed
+        # the two largest kernels of the timed steps in the ncu launch list of
+        # the contact phase are the strain sweep (23% of the step) and the
+        # traversal (22%); the traversal is timed
         # per launch here, the strain stage only as a whole (several kernels
         # in one graph), so the traversal is the roofline entry and the
         # strain stage is listed under "kernels"
@@ -543,9 +543,8 @@ def run_gpu(args):
         kt = kern[top]
         traffic = None
         if top == "traverse":
-            # DRAM bytes read + written per query leaf from one ncu capture
-            # (profiles/k_traverse_rope_batched_96.md, k_traverse_batched_96.md),
-            # scaled to this run's launches
+            # DRAM bytes read + written per query leaf from one ncu capture of
+            # each traversal kernel on 96 scenes, scaled to this run's launches
             traffic = (TRAVERSE_DRAM_BYTES_PER_LEAF[mixed["rope"]] * tot["broad_leaves"] /
                        max(prof["traverse"][1], 1))
         roof = {"bound": "hbm", "kernel": kt["kernel"], "achieved": kt["achieved"], "peak": hbm, "unit": "GB/s",
