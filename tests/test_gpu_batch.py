@@ -112,6 +112,46 @@ def test_batch_equals_single_scenes(solver_cls):
         s.close()
 
 
+def _first_elements(k, seed):
+    # a cloth-on-sphere scene cut to its first k triangles (the other points
+    # stay, referenced by no element)
+    sc = scenes.cloth_on_sphere(n=2, sub=0, side=0.1, speed=2.0, seed=seed)
+    sc.tris, sc.tri_surf, sc.tri_rest = sc.tris[:k], sc.tri_surf[:k], sc.tri_rest[:k]
+    return sc
+
+
+def test_batch_with_one_and_two_element_scenes(solver_cls):
+    # scenes of one and two elements between larger ones and an empty one:
+    # ropes that end at every scene boundary, and passes over some scenes
+    # that refit the hierarchy around them
+    mix = [_first_elements(1, 1), scenes.cloth_on_obstacle(10, "sphere", 0.2, 1.5, seed=1), _first_elements(2, 2),
+           _points_only(), scenes.folded_cloth(n=17, seed=1), _first_elements(1, 3), _first_elements(2, 4)]
+    singles = []
+    for i, sc in enumerate(mix):
+        s = solver_cls(0)
+        s.assembleFromScene(sc)
+        s.setMode(1)
+        singles.append(s)
+    ref = None
+    for rope, subset_refit in ((True, True), (False, True), (True, False), (False, False)):
+        steps, pv, pe = _run_batch(solver_cls, mix, 6, mode=1, rope=rope, subset_refit=subset_refit)
+        if ref is None:
+            ref = steps
+            for i, s in enumerate(singles):
+                for k, st in enumerate(steps):
+                    xs, vs, hs = s.resolveCollision(_split(st["x_in"], pv, i), _split(st["xc"], pv, i),
+                                                    _split(st["v_in"], pv, i), _split(st["hc_in"], pv, i))
+                    tag = f"scene {i} ({mix[i].name}, {mix[i].ne} elements) step {k}"
+                    assert np.array_equal(xs, _split(st["x"], pv, i)), tag
+                    assert np.array_equal(vs, _split(st["v"], pv, i)), tag
+                    assert np.array_equal(hs, _split(st["hc"], pv, i)), tag
+                    assert np.array_equal(s.passKinds(), st["kinds"][i]), tag
+        else:
+            _compare(ref, steps, ("rope", rope, "subset refit", subset_refit))
+    for s in singles:
+        s.close()
+
+
 def test_batch_matches_oracle(solver_cls):
     from oracle.ccopy import OracleSolver
     mix = _mix()
