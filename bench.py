@@ -139,6 +139,19 @@ class Clocks:
 ORACLE_ITER_CAP = -3
 
 
+def one_core_rate(scs, max_steps, budget_s, zone_cap):
+    """The CPU restatement on one host core - the reference's own
+    single-threaded form - over a sample of the scenes by size: the median
+    scene of every sixteenth of them in size order (one scene when there are
+    fewer than 16). Same trajectory and bounds as oracle_rate."""
+    order = sorted(range(len(scs)), key=lambda i: scs[i].ne)
+    one = [scs[i] for i in order[len(order) // 32::16]]
+    rate, n, t, steps = oracle_rate(one, max_steps, budget_s, 1, zone_cap)
+    return {"value": rate, "unit": UNIT, "cores": 1,
+            "sample": f"{len(one)} of {len(scs)} scenes (the median of every sixteenth by size), first {steps} "
+                      f"steps ({n} scene-steps, {t:.1f} s)"}
+
+
 def oracle_rate(scs, max_steps, budget_s, threads, zone_cap, skip_steps=0):
     """Scene-steps/s of the CPU restatement over the trajectory, all scenes
     stepped together (one scene per thread, `threads` at once); the first
@@ -552,6 +565,14 @@ def run_gpu(args):
                 "note": f"latency and divergence bound ({TRAVERSE_LANES_ACTIVE[mixed['rope']]} of 32 lanes active "
                         "per instruction, dependent node loads), not bandwidth bound; k_strain_window has a "
                         "similar share of the step (kernels.strain)", "kernels": kern}
+    if roof is not None and tot.get("path_bytes"):
+        # the whole step's algorithmic bytes (the path_bytes counter: state in
+        # and out, per pass the points, connectivity, hierarchy, pairs and
+        # contact records, per strain pass the points and edges) over the
+        # timed steps' device time
+        achieved = tot["path_bytes"] / (mixed["total_ms"] / 1e3) / 1e9
+        roof["path"] = {"bytes_per_scene_step": tot["path_bytes"] / max(mixed["scene_steps"], 1),
+                        "achieved": achieved, "frac": achieved / hbm, "unit": "GB/s"}
     cpu = None
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -559,6 +580,7 @@ def run_gpu(args):
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{args.workload}: {nsc} scenes, first {steps} steps of the trajectory "
                          f"({n} scene-steps, {t:.1f} s), one scene per thread"}
+        cpu["one_core"] = one_core_rate(scs, steps, args.cpu_budget, args.zone_cap)
     launches = sum(c["kernel_launches"] + 2 for c in mixed["counters"])
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
             "ms_per_step": mixed["total_ms"] / K, "higher_is_better": True, "scaling": "weak",

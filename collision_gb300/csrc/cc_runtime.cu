@@ -39,7 +39,7 @@ const char* kStageNames[kNumStages] = {"init", "leaf_boxes", "bvh_build", "trave
 
 constexpr int kMaxSceneElems = (1 << 22) - 1;  // leaf ranks fill 22 bits of a contribution key
 constexpr long long kMaxTotal = 1ll << 28;     // points and elements over all scenes
-constexpr int kNumCounters = 18;
+constexpr int kNumCounters = 19;
 constexpr int kErrIndex = kErrIndexNode | kErrIndexLeaf | kErrIndexElem;
 std::string index_error(int e) {
     std::string m = "broad phase met an index out of range:";
@@ -113,7 +113,7 @@ void parallel_for(int n, int threads, F f) {
 enum HostState { kHsDone = 0, kHsProx, kHsCcd, kHsZone };
 
 struct SceneHost {
-    int v0 = 0, nv = 0, e0 = 0, ne = 0;
+    int v0 = 0, nv = 0, e0 = 0, ne = 0, nt = 0;  // nt: triangles (the first nt elements)
     RefTreeOrder tree[2];
     double volume = 0.0;  // shared by both trees (dcollid.cpp:381, 422)
     int strain_edges = 0, strain_points = 0;
@@ -875,7 +875,7 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
         const cc_mesh* m = &meshes[si];
         const int snv = m->n_points, nt = m->n_tris, nb = m->n_bonds, sne = nt + nb;
         SceneHost& sh = scenes[si];
-        sh.v0 = v0; sh.nv = snv; sh.e0 = e0; sh.ne = sne;
+        sh.v0 = v0; sh.nv = snv; sh.e0 = e0; sh.ne = sne; sh.nt = nt;
         SceneDev& sd = h_scenes[si];
         sd.p = Params{prm.dt, prm.thickness, prm.eps, prm.k, prm.m, prm.lambda, prm.cr};
         for (int d = 0; d < 3; ++d) {
@@ -1361,6 +1361,9 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
         if (st) return st;
     }
     counters[3] += h_ctr->npairs;
+    // path bytes per pass: pairs written and read, per-point impulse,
+    // friction and count records written and read for each contact
+    counters[18] += 16ll * h_ctr->npairs + 4ll * 2 * 52 * h_ctr->ncontacts;
     counters[4] += h_ctr->nvisits;
     counters[5] += h_ctr->nhit_pairs;
     counters[6] += h_ctr->ncontacts;
@@ -1464,6 +1467,8 @@ cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, dou
     for (auto& sh : scenes) {
         sh.pass_kinds.clear();
         sh.state = (sh.ne > 0 && sh.enabled) ? kHsProx : kHsDone;
+        // path bytes per scene-step: x_old, x_cand, v read; x, v written
+        if (sh.enabled) counters[18] += 120ll * sh.nv;
         sh.niter = sh.cd_count = sh.zone_it = sh.hcol = sh.npass = 0;
         sh.status = CC_OK;
     }
@@ -1521,6 +1526,11 @@ cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, dou
             counters[0]++;
             if (m == kSceneCcd) counters[1]++;
             if (m == kSceneZone) counters[2]++;
+            // path bytes per scene-pass: x_old and avgVel read, connectivity,
+            // the FP32 hierarchy written by the refit and read once by the
+            // traversal, avgVel updated; a zone pass reads the state again
+            counters[18] += 72ll * sh.nv + 12ll * sh.nt + 8ll * (sh.ne - sh.nt) + 48ll * (2ll * sh.ne - 1) +
+                            (m == kSceneZone ? 48ll * sh.nv : 0ll);
         }
         if (!any) break;
         // proximity is every scene's first pass, so a pass is all static or all moving
@@ -1603,6 +1613,10 @@ cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, dou
         // record and one 32-byte read and write of each point it touches
         counters[14] += (long long)h_strain_passes[3 * s] *
                         (48ll * scenes[s].strain_edges + 64ll * scenes[s].strain_points);
+        // path bytes per strain pass: points read and written, each
+        // element edge (three per triangle, one per bond) read
+        counters[18] += (long long)h_strain_passes[3 * s] *
+                        (48ll * scenes[s].nv + 24ll * (3ll * scenes[s].nt + (scenes[s].ne - scenes[s].nt)));
         counters[7] += h_strain_passes[3 * s];
         counters[10] += h_strain_passes[3 * s + 1];
         counters[11] += h_strain_passes[3 * s + 2];

@@ -342,7 +342,7 @@ class CollisionSolver3d:
     COUNTER_NAMES = ("passes", "ccd_passes", "zone_passes", "candidate_pairs", "visits", "hit_pairs",
                      "contacts", "strain_passes", "tree_builds", "kernel_launches", "strain_averaged",
                      "strain_exact", "fp64_subtests", "moving_visits", "strain_bytes", "cr_roots", "broad_leaves",
-                     "broad_pairs")
+                     "broad_pairs", "path_bytes")
 
     def counters(self) -> dict:
         n_all = len(self.COUNTER_NAMES)

@@ -79,3 +79,14 @@ def test_cpp_headers_compile_and_link(tmp_path):
     r = subprocess.run(["g++", "-std=c++17", "-I", inc, str(src), "-o", str(out), "-L", libdir,
                         "-lcollision_gb300", f"-Wl,-rpath,{libdir}"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_one_core_baseline_samples_by_size():
+    # the bench's one-core CPU baseline: the median scene of every sixteenth
+    # of the scenes in size order, stepped on one thread by the oracle
+    import bench
+    from collision_gb300 import scenes
+    scs = [scenes.cloth_on_sphere(n=3 + (i * 7) % 6, sub=0, side=0.2, seed=i) for i in range(32)]
+    r = bench.one_core_rate(scs, 1, 0.01, 1000)
+    assert r["cores"] == 1 and r["value"] > 0
+    assert r["sample"].startswith("2 of 32 scenes"), r["sample"]
