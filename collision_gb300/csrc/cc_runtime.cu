@@ -650,7 +650,7 @@ struct cc_solver {
     cudaStream_t tail_stream = nullptr;
     cudaEvent_t ev_pass = nullptr, ev_tail = nullptr;
     uint8_t* d_tail_mask = nullptr;
-    uint8_t* h_tail_masks = nullptr;  // pinned, (nscenes + 1) masks: one per tail of a step
+    uint8_t* h_tail_masks = nullptr;  // pinned, two masks: a step runs at most two tails
     int tails_this_step = 0;
     std::vector<uint8_t> tail_done;
     bool overlap_tails = false;
@@ -664,7 +664,9 @@ struct cc_solver {
         // besides the last, one early end of step, once at least half the
         // scenes have finished (each one runs the whole tail's launches)
         if (!all && (tails_this_step > 0 || 2 * (int)ids.size() < nscenes)) return CC_OK;
-        uint8_t* m = h_tail_masks + (size_t)(tails_this_step % (nscenes + 1)) * (size_t)nscenes;
+        // at most one early tail, then the last: each has its own mask, whose
+        // copy may still be in flight when the next is written
+        uint8_t* m = h_tail_masks + (size_t)(tails_this_step % 2) * (size_t)nscenes;
         tails_this_step++;
         std::memset(m, 0, (size_t)nscenes);
         for (int s : ids) {
@@ -1006,7 +1008,7 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     ok &= dalloc(&d_scenes, (size_t)n) == cudaSuccess;
     ok &= dalloc(&d_run, (size_t)n) == cudaSuccess;
     ok &= dalloc(&d_tail_mask, (size_t)n) == cudaSuccess;
-    ok &= cudaMallocHost(&h_tail_masks, (size_t)n * (size_t)(n + 1)) == cudaSuccess;
+    ok &= cudaMallocHost(&h_tail_masks, 2 * (size_t)n) == cudaSuccess;
     ok &= cudaMallocHost(&h_run, sizeof(SceneRun) * (size_t)n) == cudaSuccess;
     ok &= cudaMallocHost(&h_bbox, 6 * sizeof(unsigned long long) * (size_t)n) == cudaSuccess;
     ok &= dalloc(&d_vscene, (size_t)nv) == cudaSuccess;
