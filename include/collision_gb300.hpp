@@ -97,6 +97,24 @@ public:
     // collid.h:205
     bool hasCollision() const { return has_collision_; }
 
+    // Arithmetic of the narrow phase (0 plain FP64, 1 mixed precision with
+    // the same results), launch tuning and the last step's counters; none of
+    // these changes results (cc_set_mode, cc_autotune, cc_set_tuning,
+    // cc_get_counters).
+    void setMode(int mode) { check(cc_set_mode(s_, mode), "mode"); }
+    double autotune() {
+        double ms = 0.0;
+        check(cc_autotune(s_, &ms), "autotune");
+        return ms;
+    }
+    void setTuning(int knob, int value) { check(cc_set_tuning(s_, knob, value), "tuning"); }
+    int tuning(int knob) { return cc_get_tuning(s_, knob); }
+    std::vector<long long> counters() {
+        std::vector<long long> c(64);
+        c.resize((size_t)cc_get_counters(s_, c.data(), (int)c.size()));
+        return c;
+    }
+
     cc_solver* handle() { return s_; }
 
 private:
@@ -182,6 +200,24 @@ public:
     }
     bool hasCollision(int scene) const { return has_collision_[(size_t)scene] != 0; }
     int status(int scene) const { return status_[(size_t)scene]; }
+
+    // Arithmetic of the narrow phase (0 plain FP64, 1 mixed precision with
+    // the same results), launch tuning and the last step's counters; none of
+    // these changes results (cc_set_mode, cc_autotune, cc_set_tuning,
+    // cc_get_counters).
+    void setMode(int mode) { check(cc_set_mode(s_, mode), "mode"); }
+    double autotune() {
+        double ms = 0.0;
+        check(cc_autotune(s_, &ms), "autotune");
+        return ms;
+    }
+    void setTuning(int knob, int value) { check(cc_set_tuning(s_, knob, value), "tuning"); }
+    int tuning(int knob) { return cc_get_tuning(s_, knob); }
+    std::vector<long long> counters() {
+        std::vector<long long> c(64);
+        c.resize((size_t)cc_get_counters(s_, c.data(), (int)c.size()));
+        return c;
+    }
 
     cc_solver* handle() { return s_; }
 

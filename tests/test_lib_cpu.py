@@ -69,7 +69,11 @@ def test_cpp_headers_compile_and_link(tmp_path):
         '    collision_gb300::CollisionSolver3d s(0);\n'
         '    collision_gb300::SceneBatch b(0);\n'
         '    b.assemble({});\n'
-        '    return s.hasCollision() + b.numScenes();\n'
+        '    s.setMode(1); b.setMode(1);\n'
+        '    s.setTuning(CC_TUNE_ROPE_TRAVERSE, 1); b.setTuning(CC_TUNE_SUBSET_REFIT, 1);\n'
+        '    double ms = s.autotune() + b.autotune();\n'
+        '    return s.hasCollision() + b.numScenes() + s.tuning(CC_TUNE_ROPE_TRAVERSE) + (int)ms +\n'
+        '           (int)s.counters().size() + (int)b.counters().size();\n'
         '  }\n'
         '  return 0;\n'
         '}\n')
