@@ -4,6 +4,7 @@
 // 290-310, 486-624, 677-751; dcollid3d.cpp:70-200).
 #include "cc_launch.h"
 #include "cc_narrow.cuh"
+#include "cc_strain_plan.h"
 
 namespace ccg {
 
@@ -573,6 +574,7 @@ __global__ void __launch_bounds__(256) k_strain(const StrainEdgeStep* __restrict
 // the outward-rounded bounds does the FP64 decision (bounds, then the exact
 // test) run. The averaging itself is FP64, as in the reference.
 constexpr int kWindowAhead = 8;
+static_assert(kWindowAhead == kStrainAhead, "copy-ins are scheduled for the sweep's look-ahead");
 constexpr size_t kStrainWindowBytes = 200 * 1024;  // dynamic shared memory of one sweep CTA at most
 constexpr size_t kStrainWarpBytes = 200 * 1024;
 
