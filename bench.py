@@ -3,26 +3,34 @@
 Default workload (`batched`): 256 independent cloth-on-obstacle scenes -
 sheet resolution 16..128 vertices per side, a fixed sphere (642 points,
 r ~ U(0.1, 0.3)) or box (12 triangles) by coin flip, v = (0,0,-U(0.5,3))
-+-1 %, dt = h = 1e-3 - all seeded, synthetic. One step = one
-resolveCollision() of every scene on its current state, as the reference's
-host loop does (x_cand = x_old + dt*vel, then resolve); the trajectory runs
-on across warm-up and timed steps. Metric: collision-resolved scene-steps
-per second.
++-1 %, dt = h = 1e-3 - all seeded, synthetic. Each cloth starts above its
+obstacle by the distance it falls in U(1, 4) steps, so every scene is in
+contact from its first steps on and the warm-up and timed steps are contact
+steps (--placement freefall puts the cloths 0.05 above a sphere and 0.10
+above a box instead, which most take 20-200 steps of free fall to cross).
+One step = one resolveCollision() of every scene on its current state, as the
+reference's host loop does (x_cand = x_old + dt*vel, then resolve); the
+trajectory runs on across warm-up and timed steps. Metric: collision-resolved
+scene-steps per second.
 
   value       mixed precision, batched: all scenes in one solver, inputs in
               HBM, each step through cc_resolve_batch_device
   plain_fp64  the plain FP64 GPU path one scene at a time (one solver per
-              scene, cc_resolve_device on each) over the same steps of the
-              same trajectory; its final state must equal the batch's bit
-              for bit
+              scene, cc_resolve_device on each) over the first
+              --plain-steps timed steps of the same trajectory; its state
+              must equal the batch's bit for bit
+  batched_plain_fp64  the whole batch in plain FP64 over the same steps
   e2e         the batched mixed path through cc_resolve_batch with pinned
               host buffers, copies inside the timed region
   missed_ccd  element pairs that still collide after a step, by the exact
               FP64 CCD re-check (cc_check_ccd) after every timed step,
               outside the timed region
-  zone cap    the reference's impact-zone loop does not end on some of these
-              scenes (an 80x80 cloth on a box at step 56 is the first); such a
-              scene stops after --zone-cap zone passes, is counted in
+  parity_vs_cpu  the CPU baseline's scenes stepped by the oracle (the C
+              restatement, bit-exact to the reference) over the same steps
+              from the same initial state, against the GPU batch's state for
+              those scenes after the same number of steps
+  zone cap    the reference's impact-zone loop does not end on some scenes;
+              such a scene stops after --zone-cap zone passes, is counted in
               capped_scenes and is left out of the following steps (in every
               arm alike)
   autotune    after the warm-up steps, cc_autotune picks the traversal and
@@ -34,8 +42,9 @@ per second.
 cloth_on_sphere, strings, large) as a batch of one. --impl reference times
 the CPU implementation of the same path (the C restatement of the reference
 in oracle/, which is bit-exact to it; the reference's own sources are not on
-the GPU host) on all host cores, one scene per thread. Under torchrun every
-rank runs an independent replica (different seed).
+the GPU host) on all host cores, one scene per thread, on the CPU sample of
+the workload (batched: every fourth scene by size, 64 of 256). Under
+torchrun every rank runs an independent replica (different seed).
 """
 from __future__ import annotations
 
@@ -64,15 +73,28 @@ TRAVERSE_DRAM_BYTES_PER_LEAF = {True: 141.6, False: 170.4}
 TRAVERSE_LANES_ACTIVE = {True: 6.3, False: 7.4}
 
 
-def make_workload(name, seed, nscenes=0, large_n=1025):
+def make_workload(name, seed, nscenes=0, large_n=1025, placement="contact"):
     from collision_gb300 import scenes
     if name == "large":
         return [scenes.large(n=large_n, seed=seed)]
-    scs = scenes.workload(name, seed=seed)
+    if name == "batched":
+        scs = scenes.batched(seed=seed, approach_steps=(1.0, 4.0) if placement == "contact" else None)
+    else:
+        scs = scenes.workload(name, seed=seed)
     return scs[:nscenes] if nscenes > 0 else scs
 
 
-def describe(name, scs):
+def cpu_sample(scs):
+    """Indices of the scenes the CPU legs step: every fourth scene in size
+    order (the second of each group of four) for batches of 16 or more,
+    else all."""
+    if len(scs) < 16:
+        return list(range(len(scs)))
+    order = sorted(range(len(scs)), key=lambda i: scs[i].ne)
+    return sorted(order[1::4])
+
+
+def describe(name, scs, placement=None):
     nv = sum(s.nv for s in scs)
     nt = sum(s.nt for s in scs)
     nb = sum(s.nb for s in scs)
@@ -81,6 +103,9 @@ def describe(name, scs):
     if name == "batched":
         d["sheet_sides"] = [16, 128]
         d["obstacles"] = {"sphere": sum("sphere" in s.name for s in scs), "box": sum("box" in s.name for s in scs)}
+        if placement:
+            d["placement"] = ("each cloth above its obstacle by its fall in U(1, 4) steps: contact from the first "
+                              "steps" if placement == "contact" else "0.05 above a sphere, 0.10 above a box")
     return d
 
 
@@ -146,7 +171,7 @@ def one_core_rate(scs, max_steps, budget_s, zone_cap):
     fewer than 16). Same trajectory and bounds as oracle_rate."""
     order = sorted(range(len(scs)), key=lambda i: scs[i].ne)
     one = [scs[i] for i in order[len(order) // 32::16]]
-    rate, n, t, steps = oracle_rate(one, max_steps, budget_s, 1, zone_cap)
+    rate, n, t, steps, _ = oracle_rate(one, max_steps, budget_s, 1, zone_cap)
     return {"value": rate, "unit": UNIT, "cores": 1,
             "sample": f"{len(one)} of {len(scs)} scenes (the median of every sixteenth by size), first {steps} "
                       f"steps ({n} scene-steps, {t:.1f} s)"}
@@ -154,11 +179,12 @@ def one_core_rate(scs, max_steps, budget_s, zone_cap):
 
 def oracle_rate(scs, max_steps, budget_s, threads, zone_cap, skip_steps=0):
     """Scene-steps/s of the CPU restatement over the trajectory, all scenes
-    stepped together (one scene per thread, `threads` at once); the first
-    `skip_steps` steps are run untimed. Stops after max_steps timed steps or
-    once budget_s of timed steps has passed. A scene whose impact-zone loop
-    reaches zone_cap is left out from then on, as in the GPU arms. Returns
-    (rate, scene-steps, seconds, steps)."""
+    stepped together (one scene per thread, `threads` at once, largest
+    first); the first `skip_steps` steps are run untimed. Stops after
+    max_steps timed steps or once budget_s of timed steps has passed. A scene
+    whose impact-zone loop reaches zone_cap is left out from then on, as in
+    the GPU arms. Returns (rate, scene-steps, seconds, steps, final states:
+    (x, v, has_collsn, live) per scene)."""
     from collision_gb300 import scenes
     from oracle.ccopy import OracleSolver
     solvers = [OracleSolver(sc, record=0) for sc in scs]
@@ -166,6 +192,7 @@ def oracle_rate(scs, max_steps, budget_s, threads, zone_cap, skip_steps=0):
         o.set_zone_cap(zone_cap)
     state = [(sc.x.copy(), sc.v.copy(), np.zeros(sc.nv, np.uint8)) for sc in scs]
     live = [True] * len(scs)
+    by_size = sorted(range(len(scs)), key=lambda i: -scs[i].ne)
 
     def one(i):
         if not live[i]:
@@ -183,30 +210,36 @@ def oracle_rate(scs, max_steps, budget_s, threads, zone_cap, skip_steps=0):
     done, t_total, steps = 0, 0.0, 0
     with ThreadPoolExecutor(max_workers=threads) as ex:
         for _ in range(skip_steps):
-            list(ex.map(one, range(len(scs))))
+            list(ex.map(one, by_size))
         while steps < max_steps and t_total < budget_s:
             t0 = time.perf_counter()
-            n = sum(ex.map(one, range(len(scs))))
+            n = sum(ex.map(one, by_size))
             t_total += time.perf_counter() - t0
             done += n
             steps += 1
-    return done / t_total, done, t_total, steps
+    for o in solvers:
+        o.close()
+    final = [(x, v, hc, lv) for (x, v, hc), lv in zip(state, live)]
+    return done / t_total, done, t_total, steps, final
 
 
 def run_reference(args):
     ws, rk, _ = dist_env()
     if rk != 0:
         return
-    scs = make_workload(args.workload, args.seed, args.scenes, args.large_n)
+    scs = make_workload(args.workload, args.seed, args.scenes, args.large_n, args.placement)
+    idx = cpu_sample(scs)
+    sub = [scs[i] for i in idx]
     threads = os.cpu_count() or 1
-    rate, n, t, steps = oracle_rate(scs, args.steps, args.ref_budget, threads, args.zone_cap,
-                                    skip_steps=args.warmup)
-    sample = (f"{args.workload}: {len(scs)} scenes, steps {args.warmup}..{args.warmup + steps - 1} of the "
-              f"trajectory ({n} scene-steps, {t:.1f} s), one scene per thread")
+    rate, n, t, steps, _ = oracle_rate(sub, args.steps, args.ref_budget, threads, args.zone_cap,
+                                       skip_steps=args.warmup)
+    sample = (f"{args.workload}: {len(sub)} of {len(scs)} scenes"
+              f"{' (every fourth by size)' if len(sub) < len(scs) else ''}, steps {args.warmup}.."
+              f"{args.warmup + steps - 1} of the trajectory ({n} scene-steps, {t:.1f} s), one scene per thread")
     line = {"metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": ws, "steps": steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t / max(steps, 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": dict(describe(args.workload, scs), parallelism="replicas"),
+            "config": dict(describe(args.workload, scs, args.placement), parallelism="replicas"),
             "impl": "reference",
             "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -226,7 +259,7 @@ def run_gpu(args):
     from collision_gb300.solver import CollisionSolver3d
     from collision_gb300.replicas import max_over_ranks as mor, rank_seed
     seed = rank_seed(args.seed, rk)
-    scs = make_workload(args.workload, seed, args.scenes, args.large_n)
+    scs = make_workload(args.workload, seed, args.scenes, args.large_n, args.placement)
     nsc = len(scs)
     stream = torch.cuda.Stream(device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -280,12 +313,21 @@ def run_gpu(args):
         s.setStream(stream.cuda_stream)
         st = device_state()
         enabled = np.ones(nsc, dtype=bool)
+        cpu_snap = None
+
+        def snap_for_cpu(done):
+            # the state of the CPU leg's scenes after as many steps as it ran
+            nonlocal cpu_snap
+            if cpu is not None and done == cpu["steps"]:
+                cpu_snap = (st["x"].cpu().numpy(), st["v"].cpu().numpy(), st["hc"].cpu().numpy(), enabled.copy())
+
         with torch.cuda.stream(stream):
-            for _ in range(W):
+            for w in range(W):
                 candidate(st)
                 s.resolveCollisionBatchDevice(st["x"], st["xc"], st["v"], st["hc"], st["xo"])
                 drop_capped(s, enabled)
                 st["x"], st["xo"] = st["xo"], st["x"]
+                snap_for_cpu(w + 1)
         sync_all()
         tuned = s.autotune() if not args.no_autotune else None
         sync_all()
@@ -309,6 +351,8 @@ def run_gpu(args):
                 st["x"], st["xo"] = st["xo"], st["x"]
                 if k + 1 == n_plain:
                     snap = (st["x"].cpu().numpy(), st["v"].cpu().numpy())
+                if check:
+                    snap_for_cpu(W + k + 1)
             stream.synchronize()
         torch.cuda.synchronize()
         step_ms = [a.elapsed_time(b) for a, b in evs]
@@ -317,7 +361,7 @@ def run_gpu(args):
         s.close()
         return dict(total_ms=max_over_ranks(float(sum(step_ms))), step_ms=step_ms, counters=counters,
                     missed=missed, snap=snap, prof=prof, clocks=clk.summary(), scene_steps=scene_steps,
-                    capped=int((~enabled).sum()), tuned=tuned, rope=rope)
+                    capped=int((~enabled).sum()), tuned=tuned, rope=rope, cpu_snap=cpu_snap)
 
     # ------------------------------ plain FP64, one scene at a time
     def plain_sequential():
@@ -477,6 +521,23 @@ def run_gpu(args):
         return dict(mixed_ms=max_over_ranks(ms[1]), plain_ms=max_over_ranks(ms[0]), same=same, tuned=tuned,
                     counters=counters, prof=prof, clocks=clk.summary())
 
+    # ------------------------------------- CPU baseline (rank 0, first)
+    # The oracle steps the CPU sample of the scenes from the initial state
+    # over the first W + K steps (or its time budget); the GPU batch's state
+    # of those scenes after as many steps is compared with its result.
+    cpu = None
+    if rk == 0 and not args.no_cpu_baseline and nsc > 1:
+        threads = os.cpu_count() or 1
+        idx = cpu_sample(scs)
+        sub = [scs[i] for i in idx]
+        rate, n, t, steps, final = oracle_rate(sub, W + K, args.cpu_budget, threads, args.zone_cap)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "steps": steps, "idx": idx,
+               "final": final,
+               "sample": f"{args.workload}: {len(sub)} of {nsc} scenes"
+                         f"{' (every fourth by size)' if len(sub) < nsc else ''}, first {steps} steps of the "
+                         f"trajectory ({n} scene-steps, {t:.1f} s), one scene per thread"}
+        cpu["one_core"] = one_core_rate(scs, steps, args.cpu_budget, args.zone_cap)
+
     arms = set(args.arms.split(","))
     if nsc == 1 and "plain" in arms:
         pair = single_scene_pair()
@@ -487,7 +548,7 @@ def run_gpu(args):
             line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
                     "ms_per_step": pair["mixed_ms"] / K, "higher_is_better": True, "scaling": "weak",
                     "vs_baseline": None, "dtype": "f64 (f32 filters)", "data": "synthetic",
-                    "config": dict(describe(args.workload, scs), l2="flushed before every timed step",
+                    "config": dict(describe(args.workload, scs, args.placement), l2="flushed before every timed step",
                                    path="one scene: mixed precision and plain FP64 on the same inputs"),
                     "plain_fp64": {"value": plain_value, "ms_per_step": pair["plain_ms"] / K,
                                    "state_equal_every_step": pair["same"]},
@@ -573,19 +634,41 @@ def run_gpu(args):
         achieved = tot["path_bytes"] / (mixed["total_ms"] / 1e3) / 1e9
         roof["path"] = {"bytes_per_scene_step": tot["path_bytes"] / max(mixed["scene_steps"], 1),
                         "achieved": achieved, "frac": achieved / hbm, "unit": "GB/s"}
-    cpu = None
-    if not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        rate, n, t, steps = oracle_rate(scs, W + K, args.cpu_budget, threads, args.zone_cap)
-        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{args.workload}: {nsc} scenes, first {steps} steps of the trajectory "
-                         f"({n} scene-steps, {t:.1f} s), one scene per thread"}
-        cpu["one_core"] = one_core_rate(scs, steps, args.cpu_budget, args.zone_cap)
+    parity = None
+    if cpu is not None:
+        # the oracle's state of each sampled scene against the GPU batch's
+        if mixed["cpu_snap"] is None:
+            parity = {"equal": None, "note": "no GPU state after the CPU leg's steps (run with the CCD check)"}
+        else:
+            gx, gv, ghc, gen = mixed["cpu_snap"]
+            ndiff, nlive, max_abs, max_rel, capped_mismatch = 0, 0, 0.0, 0.0, 0
+            for j, i in enumerate(cpu["idx"]):
+                ox, ov, ohc, olive = cpu["final"][j]
+                if not olive or not gen[i]:
+                    capped_mismatch += int(olive != bool(gen[i]))
+                    continue
+                nlive += 1
+                a, b = int(offs[i]), int(offs[i + 1])
+                eq = (np.array_equal(gx[a:b], ox) and np.array_equal(gv[a:b], ov) and
+                      np.array_equal(ghc[a:b], ohc))
+                if not eq:
+                    ndiff += 1
+                    for g_, o_ in ((gx[a:b], ox), (gv[a:b], ov)):
+                        d = np.abs(g_ - o_)
+                        max_abs = max(max_abs, float(d.max()))
+                        max_rel = max(max_rel, float((d / np.maximum(np.abs(o_), 1e-6)).max()))
+            parity = {"equal": ndiff == 0 and capped_mismatch == 0, "scenes": nlive, "scenes_differing": ndiff,
+                      "capped_mismatch": capped_mismatch, "steps": cpu["steps"], "max_abs": max_abs,
+                      "max_rel": max_rel,
+                      "what": "positions, velocities and has_collsn of the CPU sample's scenes after the CPU "
+                              "leg's steps, GPU batch (mixed precision) vs the oracle, bit for bit"}
+        for k in ("idx", "final", "steps"):
+            cpu.pop(k)
     launches = sum(c["kernel_launches"] + 2 for c in mixed["counters"])
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
             "ms_per_step": mixed["total_ms"] / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64 (f32 filters)", "data": "synthetic",
-            "config": dict(describe(args.workload, scs),
+            "config": dict(describe(args.workload, scs, args.placement),
                            path="mixed precision, batched: FP32 sub-test filters in front of unchanged FP64 "
                                 "tests, all scenes per launch",
                            l2="flushed before every timed step",
@@ -600,7 +683,7 @@ def run_gpu(args):
             "missed_ccd": None if args.no_check else int(mixed["missed"]),
             "capped_scenes": mixed["capped"], "zone_cap": args.zone_cap,
             "autotune": mixed["tuned"],
-            "roofline": roof, "cpu_baseline": cpu, "clocks": mixed["clocks"],
+            "roofline": roof, "cpu_baseline": cpu, "parity_vs_cpu": parity, "clocks": mixed["clocks"],
             "e2e": None if e2e_value is None else
                    {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),
@@ -620,12 +703,15 @@ def main():
     ap.add_argument("--workload", default="batched",
                     choices=["batched", "folded_cloth", "cloth_on_sphere", "strings", "large"])
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--plain-steps", type=int, default=0,
+    ap.add_argument("--plain-steps", type=int, default=5,
                     help="timed steps of the one-scene-at-a-time run (0: all K)")
     ap.add_argument("--zone-cap", type=int, default=1000)
     ap.add_argument("--arms", default="mixed,batch_plain,plain,e2e",
                     help="arms to run besides the headline batched mixed one (for profiling runs)")
     ap.add_argument("--scenes", type=int, default=0, help="first N scenes of the batched workload (0: all)")
+    ap.add_argument("--placement", default="contact", choices=["contact", "freefall"],
+                    help="batched workload: cloths within four steps of their obstacles (contact) or 0.05/0.10 "
+                         "above them (freefall)")
     ap.add_argument("--large-n", type=int, default=1025, help="cloth vertices per side of the large workload")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--ref-budget", type=float, default=120.0)

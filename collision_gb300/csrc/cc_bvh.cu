@@ -351,7 +351,7 @@ __device__ __forceinline__ void emit_pair(int a, int b, int2* pairs, int cap, Pa
 // The leaf records of one pass (see LeafRec).
 __global__ void k_leaf_records(const Box6* __restrict__ box, const unsigned int* __restrict__ order, int n,
                                const int* __restrict__ sub, int nsub, const int* __restrict__ ev, LeafRec* out,
-                               int ne_all, PassCounters* ctr) {
+                               int ne_all, PassCounters* ctr, const int* __restrict__ rope, LeafBox32* out32) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= (sub ? nsub : n)) return;
     const int j = sub ? sub[k] : k;
@@ -365,9 +365,22 @@ __global__ void k_leaf_records(const Box6* __restrict__ box, const unsigned int*
         LeafRec r = {};
         r.e = -1;  // tested by nobody: the traversal skips it
         out[j] = r;
+        if (out32) {
+            LeafBox32 q = {};
+            q.rope = j < n - 1 ? rope[j] : kRopeEnd;
+            q.e = -1;
+            out32[j] = q;
+        }
         return;
     }
-    const BoxOrd o = box_ord(box[e]);
+    const Box6 bx = box[e];
+    if (out32) {
+        const Box32 f = box32_out(bx);
+        float4* q = reinterpret_cast<float4*>(&out32[j]);
+        q[0] = make_float4(f.lo[0], f.lo[1], f.lo[2], f.hi[0]);
+        q[1] = make_float4(f.hi[1], f.hi[2], __int_as_float(j < n - 1 ? rope[j] : kRopeEnd), __int_as_float(e));
+    }
+    const BoxOrd o = box_ord(bx);
     LeafRec r;
     for (int d = 0; d < 3; ++d) {
         r.lo[d] = o.lo[d];
@@ -481,6 +494,7 @@ __global__ void __launch_bounds__(kPacketWarps * 32) k_traverse_packet(
     }
 }
 
+template <int DEPTH>
 __global__ void k_traverse(const Box6* __restrict__ box, const unsigned int* __restrict__ order, int n,
                            const BvhNode32* __restrict__ node, const int* __restrict__ elem_scene,
                            const SceneRun* __restrict__ run, const int* __restrict__ ev, int2* pairs, int cap,
@@ -531,7 +545,7 @@ __global__ void k_traverse(const Box6* __restrict__ box, const unsigned int* __r
     const Box32 q32 = box32_out(q);
     BoxOrd qs;
     if (box_static) qs = box_ord(box_static[ei]);
-    int stk[kTraversalStack];
+    int stk[DEPTH];
     int sp = 0;
     stk[sp++] = root;
     while (sp > 0) {
@@ -576,7 +590,7 @@ __global__ void k_traverse(const Box6* __restrict__ box, const unsigned int* __r
                               cap, ctr);
             } else if (c >= n - 1) {
                 atomicOr(&ctr->err, kErrIndexNode);
-            } else if (sp < kTraversalStack) {
+            } else if (sp < DEPTH) {
                 stk[sp++] = c;
             } else {
                 atomicOr(&ctr->err, kErrStack);
@@ -661,6 +675,116 @@ __global__ void k_traverse_rope(int n, const RopeNode* __restrict__ rn, const in
         if (ev && (pe.x == pi0 || pe.x == pi1 || pe.x == pi2 || pe.y == pi0 || pe.y == pi1 || pe.y == pi2 ||
                    (pe.z >= 0 && (pe.z == pi0 || pe.z == pi1 || pe.z == pi2))))
             continue;
+        emit_pair(ei, (box_static && overlap_ord(qs, &box_static[ej])) ? (ej | kPairStatic) : ej, pairs, cap, ctr);
+    }
+}
+
+// The stackless walk with dynamic query fetch. The walks of neighbouring
+// queries differ in length, and with one thread per query a warp runs until
+// its longest walk ends while its other lanes idle. Here warps stay resident
+// and a lane whose walk has ended takes the next query from a global counter:
+// once at least `refill` lanes of a warp are idle, they fetch that many
+// consecutive queries with one atomic. A leaf is tested first on its 32-byte
+// FP32 record (outward-rounded box, rope, element), and only a leaf that
+// passes loads its 64-byte exact record. Same pairs as k_traverse_rope.
+__global__ void __launch_bounds__(128) k_traverse_rope_dyn(
+    int n, const RopeNode* __restrict__ rn, const int* __restrict__ elem_scene, const SceneRun* __restrict__ run,
+    const int* __restrict__ ev, int2* pairs, int cap, PassCounters* ctr, const Box6* __restrict__ box_static,
+    const LeafRec* __restrict__ leaves, const LeafBox32* __restrict__ leaf32, const int* __restrict__ sub, int nsub,
+    int* qnext, int refill) {
+    const int nq = sub ? nsub : n - 1;
+    const unsigned lane_lt = (1u << (threadIdx.x & 31)) - 1u;
+    int x = kRopeEnd, ei = -1, steps = 0;
+    int pi0 = -1, pi1 = -1, pi2 = -1;
+    BoxOrd qo, qs;
+    Box32 q32;
+    bool more = true;  // queries left to fetch (warp-uniform)
+    for (;;) {
+        const unsigned idle = __ballot_sync(0xffffffffu, x == kRopeEnd);
+        if (more && (__popc(idle) >= refill || idle == 0xffffffffu)) {
+            int base = 0;
+            const int want = __popc(idle);
+            if ((threadIdx.x & 31) == __ffs(idle) - 1) base = atomicAdd(qnext, want);
+            base = __shfl_sync(0xffffffffu, base, __ffs(idle) - 1);
+            if (base + want >= nq) more = false;
+            const int t = base + __popc(idle & lane_lt);
+            if (x == kRopeEnd && t < nq) {
+                // a new query: its own leaf record, then the rope after it
+                const int i = sub ? sub[t] : t;
+                if (i < 0) {
+                    atomicOr(&ctr->err, kErrIndexLeaf);
+                } else if (i < n - 1) {
+                    const LeafRec r = leaves[i];
+                    ei = r.e;
+                    bool on = ei >= 0;  // negative: flagged by k_leaf_records
+                    if (on && run) {
+                        const SceneRun sr = run[elem_scene[ei]];
+                        on = sr.mode != kSceneIdle && sr.root >= 0;
+                    }
+                    if (on) {
+                        Box6 q;
+                        for (int d = 0; d < 3; ++d) {
+                            qo.lo[d] = r.lo[d];
+                            qo.hi[d] = r.hi[d];
+                            q.lo[d] = unord_double(r.lo[d]);
+                            q.hi[d] = unord_double(r.hi[d]);
+                        }
+                        q32 = box32_out(q);
+                        if (ev) pi0 = r.p[0], pi1 = r.p[1], pi2 = r.p[2];
+                        if (box_static) qs = box_ord(box_static[ei]);
+                        x = __float_as_int(__ldg(reinterpret_cast<const float*>(&leaf32[i]) + 6));
+                        steps = 0;
+                    }
+                }
+            }
+        }
+        if (!more && __all_sync(0xffffffffu, x == kRopeEnd)) break;
+        if (x == kRopeEnd) continue;
+        if (++steps > 2 * n) {
+            atomicOr(&ctr->err, kErrIndexNode);
+            x = kRopeEnd;
+            continue;
+        }
+        if (x >= 0) {
+            if (x >= n - 1) {
+                atomicOr(&ctr->err, kErrIndexNode);
+                x = kRopeEnd;
+                continue;
+            }
+            const float4* p4 = reinterpret_cast<const float4*>(&rn[x]);
+            const float4 a = __ldg(p4), b = __ldg(p4 + 1);  // lo xyz hi.x | hi.y hi.z left rope
+            const bool hit = q32.lo[0] <= a.w && q32.hi[0] >= a.x && q32.lo[1] <= b.x && q32.hi[1] >= a.y &&
+                             q32.lo[2] <= b.y && q32.hi[2] >= a.z;
+            x = __float_as_int(hit ? b.z : b.w);
+            continue;
+        }
+        const int k = ~x;
+        if (k >= n) {
+            atomicOr(&ctr->err, kErrIndexLeaf);
+            x = kRopeEnd;
+            continue;
+        }
+        const float4* l4 = reinterpret_cast<const float4*>(&leaf32[k]);
+        const float4 a = __ldg(l4), b = __ldg(l4 + 1);  // lo xyz hi.x | hi.y hi.z rope e
+        x = __float_as_int(b.z);
+        // the FP32 boxes hold the exact ones: a miss here is a miss
+        if (!(q32.lo[0] <= a.w && q32.hi[0] >= a.x && q32.lo[1] <= b.x && q32.hi[1] >= a.y && q32.lo[2] <= b.y &&
+              q32.hi[2] >= a.z))
+            continue;
+        const int ej = __float_as_int(b.w);
+        if (ej < 0) continue;  // flagged by k_leaf_records
+        const ulonglong2* lr = reinterpret_cast<const ulonglong2*>(&leaves[k]);
+        const ulonglong2 u0 = __ldg(lr), u1 = __ldg(lr + 1), u2 = __ldg(lr + 2);
+        // the exact test on the encoded boxes
+        if (!(qo.lo[0] <= u1.y && qo.hi[0] >= u0.x && qo.lo[1] <= u2.x && qo.hi[1] >= u0.y && qo.lo[2] <= u2.y &&
+              qo.hi[2] >= u1.x))
+            continue;
+        if (ev) {
+            const int4 pe = __ldg(reinterpret_cast<const int4*>(lr + 3));
+            if (pe.x == pi0 || pe.x == pi1 || pe.x == pi2 || pe.y == pi0 || pe.y == pi1 || pe.y == pi2 ||
+                (pe.z >= 0 && (pe.z == pi0 || pe.z == pi1 || pe.z == pi2)))
+                continue;
+        }
         emit_pair(ei, (box_static && overlap_ord(qs, &box_static[ej])) ? (ej | kPairStatic) : ej, pairs, cap, ctr);
     }
 }
@@ -753,26 +877,68 @@ void bvh_refit(const Box6* box, BvhBufs& b, cudaStream_t s) {
                                                                           b.range_lo, b.range_hi);
 }
 
+template <int DEPTH>
+void launch_stack_traverse(const Box6* box, const BvhBufs& b, int nq, int block, int2* pairs, int cap,
+                           PassCounters* ctr, cudaStream_t s, const int* skip_shared_ev, const Box6* box_static) {
+    count_launch(), k_traverse<DEPTH><<<nblk(nq, block), block, 0, s>>>(box, b.order, b.n, b.node, b.elem_scene, b.run,
+                                                                      skip_shared_ev, pairs, cap, ctr, box_static,
+                                                                      b.leaf, b.sub, b.nsub);
+}
+
+// Resident blocks of the dynamic-fetch traversal per SM, looked up once.
+int dyn_blocks_per_sm() {
+    static int cached = 0;
+    if (!cached) {
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_traverse_rope_dyn, 128, 0) != cudaSuccess || nb < 1)
+            nb = 8;
+        cached = nb;
+    }
+    return cached;
+}
+
 void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCounters* ctr, cudaStream_t s,
-               const int* skip_shared_ev, int block, const Box6* box_static, bool packet, bool rope) {
+               const int* skip_shared_ev, int block, const Box6* box_static, bool packet, bool rope, int refill,
+               int stack_depth) {
     int n = b.n;
     if (n <= 1) return;
     const int nleaf = b.sub ? b.nsub : n, nq = b.sub ? b.nsub : n - 1;
     if (nq <= 0) return;
+    const bool dyn = b.leaf && rope && b.rnode && b.rope && b.leaf32 && b.qnext && refill > 0;
     if (b.leaf)
         count_launch(), k_leaf_records<<<nblk(nleaf, 256), 256, 0, s>>>(box, b.order, n, b.sub, b.nsub, b.ev,
-                                                                        b.leaf, b.ne_all, ctr);
-    if (b.leaf && rope && b.rnode && b.rope)
+                                                                        b.leaf, b.ne_all, ctr, b.rope,
+                                                                        dyn ? b.leaf32 : nullptr);
+    if (dyn) {
+        static int num_sms = 0;
+        if (!num_sms) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            if (cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) num_sms = 152;
+        }
+        int blocks = num_sms * dyn_blocks_per_sm();
+        const int need = nblk(nq, 128);
+        if (blocks > need) blocks = need;
+        cudaMemsetAsync(b.qnext, 0, sizeof(int), s);
+        count_launch(), k_traverse_rope_dyn<<<blocks, 128, 0, s>>>(n, b.rnode, b.elem_scene, b.run, skip_shared_ev,
+                                                                   pairs, cap, ctr, box_static, b.leaf, b.leaf32,
+                                                                   b.sub, b.nsub, b.qnext, refill > 32 ? 32 : refill);
+    } else if (b.leaf && rope && b.rnode && b.rope) {
         count_launch(), k_traverse_rope<<<nblk(nq, block), block, 0, s>>>(
             n, b.rnode, b.rope, b.elem_scene, b.run, skip_shared_ev, pairs, cap, ctr, box_static, b.leaf, b.sub,
             b.nsub);
-    else if (b.leaf && packet && !b.sub)
+    } else if (b.leaf && packet && !b.sub) {
         count_launch(), k_traverse_packet<<<nblk(n - 1, kPacketWarps * 32), kPacketWarps * 32, 0, s>>>(
             b.order, n, b.node, b.elem_scene, b.run, skip_shared_ev, pairs, cap, ctr, box_static, b.leaf);
-    else
-        count_launch(), k_traverse<<<nblk(nq, block), block, 0, s>>>(box, b.order, n, b.node, b.elem_scene, b.run,
-                                                                     skip_shared_ev, pairs, cap, ctr, box_static,
-                                                                     b.leaf, b.sub, b.nsub);
+    } else if (stack_depth <= 24) {
+        launch_stack_traverse<24>(box, b, nq, block, pairs, cap, ctr, s, skip_shared_ev, box_static);
+    } else if (stack_depth <= 32) {
+        launch_stack_traverse<32>(box, b, nq, block, pairs, cap, ctr, s, skip_shared_ev, box_static);
+    } else if (stack_depth <= 48) {
+        launch_stack_traverse<48>(box, b, nq, block, pairs, cap, ctr, s, skip_shared_ev, box_static);
+    } else {
+        launch_stack_traverse<64>(box, b, nq, block, pairs, cap, ctr, s, skip_shared_ev, box_static);
+    }
 }
 
 void brute_pairs(const Box6* box, int ne, const int* elem_scene, int2* pairs, int cap, PassCounters* ctr,

@@ -158,7 +158,17 @@ struct PassCounters {
     int nsub_pt;      // point-triangle sub-tests queued by a split pass
     int nsub_ee;      // edge-edge sub-tests queued by a split pass
     int npairq;       // pairs with a queued sub-test (split passes)
-    int pad[3];
+    int nzones;       // impact zones listed for the zone solve (impact-zone passes)
+    int nmembers;     // their members
+    int nseg;         // union-record segments, one per zone the pass's unions touch
+};
+
+// One point's entry in the reference's union-find with member lists
+// (UF{next_pt, root, tail, num_pts}, collid.h:22-27; makeSet, findSet,
+// mergePoint, dcollid.cpp:1015-1059): parent, next member, last member and
+// member count (the last two meaningful at a root).
+struct __align__(16) UfNode {
+    int root, next, tail, w;
 };
 
 #ifdef __CUDACC__

@@ -17,6 +17,8 @@ inline void count_launch(int n = 1) { g_kernel_launches += n; }
 struct LaunchTuning {
     bool packet_traverse = false;  // warp-cooperative traversal (k_traverse_packet)
     bool rope_traverse = true;     // stackless traversal along ropes (k_traverse_rope)
+    int traverse_refill = 8;       // stackless: lanes that refill together (0: one thread per query)
+    int stack_depth = kTraversalStack;  // stack traversal: entries per thread
     int traverse_block = 128;     // threads per block of the per-thread traversal
     int narrow_block = 128;
     int strain_block = 256;
@@ -29,6 +31,10 @@ size_t radix_sort_temp_bytes(int n);
 // keys/vals are sorted in place (the temp buffer holds the ping-pong copy).
 void radix_sort_pairs(unsigned long long* keys, unsigned int* vals, int n, int bits, void* temp,
                       cudaStream_t s);
+// The same for the first min(*dn, cap) pairs, the count in device memory
+// (temp sized for cap; the arrays hold cap pairs).
+void radix_sort_pairs_dev(unsigned long long* keys, unsigned int* vals, const int* dn, int cap, int bits, void* temp,
+                          cudaStream_t s);
 // Exclusive scan of n ints (out may alias in); total written to *total.
 size_t scan_temp_bytes(int n);
 void exclusive_scan(const int* in, int* out, int n, int* total, void* temp, cudaStream_t s);
@@ -71,6 +77,15 @@ struct __align__(64) LeafRec {
     int e;
 };
 
+// A sorted leaf as the stackless traversal tests it first: the element's box
+// rounded outward to FP32, the rope after the leaf and the element id - 32
+// bytes, so a leaf whose box misses the query costs half a LeafRec load.
+struct __align__(32) LeafBox32 {
+    float lo[3], hi[3];
+    int rope;
+    int e;
+};
+
 struct BvhBufs {
     int n;                        // leaves of this pass's hierarchy
     const int* act;               // their element ids (null: elements 0..n-1)
@@ -98,6 +113,10 @@ struct BvhBufs {
     // filled by bvh_build and bvh_refit
     RopeNode* rnode;  // n-1
     int* rope;        // n-1
+    // optional: the FP32 leaf boxes of the stackless traversal with dynamic
+    // query fetch, written with the leaf records; qnext: its query counter
+    LeafBox32* leaf32;
+    int* qnext;
     // optional: for a hierarchy over all elements (act null), the sorted
     // leaves of the scenes in this pass; the refit, the leaf records and the
     // traversal then cover only those (walks never leave their scene)
@@ -132,9 +151,14 @@ void bvh_refit(const Box6* box, BvhBufs& b, cudaStream_t s);
 // kPairStatic when the elements' static boxes overlap as well. Traversal:
 // a stack per thread (default), a warp-cooperative packet, or (rope, with
 // the leaf records and rope nodes present) stackless along the ropes.
+// refill (rope only, with leaf32 and qnext present): persistent warps whose
+// lanes take new queries from a counter once `refill` of them have finished
+// their walks (0: one thread per query). stack_depth: entries of the
+// per-thread stack of the stack traversal (24, 32, 48 or 64); a walk that
+// needs more sets kErrStack.
 void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCounters* ctr, cudaStream_t s,
                const int* skip_shared_ev = nullptr, int block = 128, const Box6* box_static = nullptr,
-               bool packet = false, bool rope = false);
+               bool packet = false, bool rope = false, int refill = 0, int stack_depth = kTraversalStack);
 // The same pair set by testing every pair (for cross-checks on small meshes).
 void brute_pairs(const Box6* box, int ne, const int* elem_scene, int2* pairs, int cap, PassCounters* ctr,
                  cudaStream_t s);
@@ -238,6 +262,38 @@ void apply_contribs(const Contrib* contrib, const PassCounters* ctr, int contrib
 void zone_solve(const int* members, const int* zone_off, int nzones, const uint8_t* fixed, const double4_32a* xo,
                 double4_32a* av, const int* vscene, const SceneDev* scenes, PassCounters* ctr, cudaStream_t s,
                 const SceneRun* run = nullptr);
+// The same with zone z's members at members[zone_rng[z].x .. .y) and the
+// zone count in device memory (*dnz, at most zone_cap).
+void zone_solve_dev(const int* members, const int2* zone_rng, const int* dnz, int zone_cap, const uint8_t* fixed,
+                    const double4_32a* xo, double4_32a* av, const int* vscene, const SceneDev* scenes,
+                    PassCounters* ctr, cudaStream_t s);
+
+// Impact zones of a pass on the GPU (cc_zones.cu): buffers of the union
+// replay and of the zone lists.
+struct ZoneBufs {
+    int cap = 0;                         // union records the buffers below hold
+    const UnionRec* rec = nullptr;       // the pass's createImpZone records (count: PassCounters::nunion)
+    unsigned long long* keys = nullptr;  // cap sort keys
+    unsigned int* vals = nullptr;        // cap record indices
+    int* seg = nullptr;                  // cap segment starts
+    void* sort_temp = nullptr;           // zone_sort_temp_bytes(cap)
+    int* cc = nullptr;                   // per point: parent in the lock-free union-find
+    UfNode* uf = nullptr;                // per point: the reference's union-find
+    int zone_cap = 0;                    // zones the zone arrays hold
+    int2* zone_rng = nullptr;            // per zone: its run of members
+    int* zone_root = nullptr;            // per zone: its root
+    int* members = nullptr;              // per point (at most one zone each)
+};
+size_t zone_sort_temp_bytes(int cap);
+// After a pass's impulses: join the pass's createImpZone records in the
+// reference's order (scenes in impact-zone mode only), list every zone of a
+// scene in that mode and move it rigidly (updateImpactZoneVelocity,
+// dcollid.cpp:290-310). act_pts / n_pts: the points of the pass's scenes
+// (null: all n_pts points; dn_pts, if given, holds the count on the device).
+void zone_pass(const ZoneBufs& z, const PassCounters* ctr, const uint8_t* fixed, const int* act_pts, int n_pts,
+               const int* dn_pts, const int* vscene, const SceneRun* run, const SceneDev* scenes, double4_32a* av,
+               const double4_32a* xo, cudaStream_t s);
+
 // updateFinalForRG's device part: per body, the first point in element
 // order with has_collsn and its average velocity (into b.out).
 void final_rigid(const BodyBufs& b, const uint8_t* has_collsn, const double4_32a* av, cudaStream_t s);

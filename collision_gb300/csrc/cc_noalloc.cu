@@ -19,7 +19,8 @@
 // code only sees a stand-in for the array's name: its device address comes
 // from cudaGetSymbolAddress, taken once per device, with that device current,
 // on the first call there (that first call should come before any stream
-// capture begins).
+// capture begins). A call makes its device current while it runs and gives
+// the calling thread its previous current device back before it returns.
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -56,16 +57,36 @@ cudaError_t scratch_address(int device, void** out) {
     return cudaSuccess;
 }
 
-__global__ void k_clear_counters(PassCounters* c) {
-    c->npairs = 0; c->ncontrib = 0; c->nhit_pairs = 0; c->nrec = 0;
-    c->nvisits = 0; c->ncontacts = 0; c->err = 0; c->nsub = 0; c->ncr = 0; c->nunion = 0;
-    c->nsub_pt = 0; c->nsub_ee = 0; c->npairq = 0;
+// Flags boxes that no hierarchy can order: a coordinate that is NaN or
+// infinite, or a lower corner above the upper one.
+__global__ void k_check_boxes(const Box6* __restrict__ box, int n, PassCounters* c) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Box6 b = box[i];
+    bool bad = false;
+    for (int k = 0; k < 3; ++k)
+        bad |= !isfinite(b.lo[k]) || !isfinite(b.hi[k]) || !(b.lo[k] <= b.hi[k]);
+    if (bad) atomicOr(&c->err, kErrNan);
 }
 
 cc_status static_fail(cc_status st, const char* msg) {
     std::snprintf(g_static_err, sizeof(g_static_err), "%s", msg);
     return st;
 }
+
+// Makes `device` current for the lifetime of the guard and gives the calling
+// thread its previous current device back on every return path.
+struct DeviceGuard {
+    int prev = -1;
+    bool ok = false;
+    explicit DeviceGuard(int device) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        ok = cudaSetDevice(device) == cudaSuccess;
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
 
 }  // namespace
 
@@ -87,7 +108,16 @@ cc_status cc_candidate_pairs_static(int device, const double* boxes, int n, int*
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev || device >= kMaxDevices)
         return static_fail(CC_CUDA_ERROR, "no such device");
-    if (cudaSetDevice(device) != cudaSuccess) return static_fail(CC_CUDA_ERROR, "cudaSetDevice failed");
+    DeviceGuard guard(device);
+    if (!guard.ok) return static_fail(CC_CUDA_ERROR, "cudaSetDevice failed");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (s) {
+        // a stream of another device would accept the copies below but not
+        // the launches
+        int sdev = -1;
+        if (cudaStreamGetDevice(s, &sdev) != cudaSuccess || sdev != device)
+            return static_fail(CC_BAD_INPUT, "the stream does not belong to the given device");
+    }
     if (n <= 1) return CC_OK;
     void* base = nullptr;
     if (scratch_address(device, &base) != cudaSuccess)
@@ -117,17 +147,32 @@ cc_status cc_candidate_pairs_static(int device, const double* boxes, int n, int*
     b.sort_temp = take(radix_sort_temp_bytes(n));
     if (used > kScratchBytes) return static_fail(CC_NO_MEMORY, "static scratch layout exceeds its size");
 
-    cudaStream_t s = (cudaStream_t)stream;
     const Box6* box = (const Box6*)boxes;
-    count_launch(), k_clear_counters<<<1, 1, 0, s>>>(ctr);
+    PassCounters h{};
+    // every counter starts at zero: the scratch area keeps the last call's
+    if (cudaMemsetAsync(ctr, 0, sizeof(PassCounters), s) != cudaSuccess)
+        return static_fail(CC_CUDA_ERROR, cudaGetErrorString(cudaGetLastError()));
+    // boxes a hierarchy cannot order are rejected before any is built
+    count_launch(), k_check_boxes<<<(n + 255) / 256, 256, 0, s>>>(box, n, ctr);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return static_fail(CC_CUDA_ERROR, cudaGetErrorString(e));
+    if (h.err & kErrNan) return static_fail(CC_BAD_INPUT, "a box is NaN or infinite, or has lo > hi");
+
     boxes_bbox(box, n, b.bbox_enc, s);
     bvh_build(box, b, s);  // clears the refit arrival flags itself
     bvh_pairs(box, b, (int2*)pairs, cap, ctr, s);
-    PassCounters h{};
-    if (cudaMemcpyAsync(&h, ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
-        return static_fail(CC_CUDA_ERROR, cudaGetErrorString(cudaGetLastError()));
+    // a failed launch leaves the counters of an earlier call in place
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return static_fail(CC_CUDA_ERROR, cudaGetErrorString(e));
     *npairs = h.npairs;
+    if (h.err & (kErrIndexNode | kErrIndexLeaf | kErrIndexElem)) {
+        *npairs = 0;
+        return static_fail(CC_CUDA_ERROR, "broad phase met an index out of range; the pairs are incomplete");
+    }
     if (h.err & kErrStack) return static_fail(CC_STACK_OVERFLOW, "BVH traversal stack overflow");
     if (h.npairs > cap) return static_fail(CC_PAIR_OVERFLOW, "more pairs than cap; *npairs holds the count");
     return CC_OK;

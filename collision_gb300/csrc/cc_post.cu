@@ -142,13 +142,11 @@ __device__ __forceinline__ double det3(const double (*a)[3]) {
 // With `run` set, the zones are movable bodies (updateImpactZoneVelocityForRG,
 // dcollid.cpp:267-288, called from updateAverageVelocity when dt > 0): only
 // those of scenes in a pass, and of more than one point, move.
-__global__ void k_zone_solve(const int* __restrict__ members, const int* __restrict__ zone_off, int nzones,
-                             const uint8_t* __restrict__ fixed, const double4_32a* __restrict__ xo, double4_32a* av,
-                             const int* __restrict__ vscene, const SceneDev* __restrict__ scenes,
-                             PassCounters* ctr, const SceneRun* __restrict__ run) {
-    int z = blockIdx.x * blockDim.x + threadIdx.x;
-    if (z >= nzones) return;
-    const int i = zone_off[z], end = zone_off[z + 1];
+__device__ void zone_motion(const int* __restrict__ members, int i, int end,
+                                         const uint8_t* __restrict__ fixed, const double4_32a* __restrict__ xo,
+                                         double4_32a* av, const int* __restrict__ vscene,
+                                         const SceneDev* __restrict__ scenes, PassCounters* ctr,
+                                         const SceneRun* __restrict__ run) {
     const int zs = vscene[members[i]];
     const Params prm = scenes[zs].p;
     if (run && (run[zs].mode == kSceneIdle || !(prm.dt > 0.0) || end - i < 2 || (ctr->err & kErrRetry))) return;
@@ -225,6 +223,23 @@ __global__ void k_zone_solve(const int* __restrict__ members, const int* __restr
         av[p] = make_double4_32a(nv_[0], nv_[1], nv_[2], 0.0);
     }
     if (bad) atomicOr(&ctr->err, kErrNan);
+}
+
+// Zone z's members are members[zone_off[z] .. zone_off[z+1]), or with
+// zone_rng members[zone_rng[z].x .. zone_rng[z].y); dnz (may be null): the
+// zone count in device memory, at most nzones.
+__global__ void k_zone_solve(const int* __restrict__ members, const int* __restrict__ zone_off,
+                             const int2* __restrict__ zone_rng, int nzones, const int* __restrict__ dnz,
+                             const uint8_t* __restrict__ fixed, const double4_32a* __restrict__ xo, double4_32a* av,
+                             const int* __restrict__ vscene, const SceneDev* __restrict__ scenes,
+                             PassCounters* ctr, const SceneRun* __restrict__ run) {
+    if (dnz) {
+        if (ctr->err & kErrRetry) return;
+        if (*dnz < nzones) nzones = *dnz;
+    }
+    for (int z = blockIdx.x * blockDim.x + threadIdx.x; z < nzones; z += gridDim.x * blockDim.x)
+        zone_motion(members, zone_rng ? zone_rng[z].x : zone_off[z], zone_rng ? zone_rng[z].y : zone_off[z + 1],
+                    fixed, xo, av, vscene, scenes, ctr, run);
 }
 
 // detectDomainBoundaryCollision (dcollid.cpp:116-158) then
@@ -1068,8 +1083,18 @@ void zone_solve(const int* members, const int* zone_off, int nzones, const uint8
                 double4_32a* av, const int* vscene, const SceneDev* scenes, PassCounters* ctr, cudaStream_t s,
                 const SceneRun* run) {
     if (nzones > 0)
-        count_launch(), k_zone_solve<<<nblk(nzones, 128), 128, 0, s>>>(members, zone_off, nzones, fixed, xo, av,
-                                                                       vscene, scenes, ctr, run);
+        count_launch(), k_zone_solve<<<nblk(nzones, 128), 128, 0, s>>>(members, zone_off, nullptr, nzones, nullptr,
+                                                                       fixed, xo, av, vscene, scenes, ctr, run);
+}
+
+void zone_solve_dev(const int* members, const int2* zone_rng, const int* dnz, int zone_cap, const uint8_t* fixed,
+                    const double4_32a* xo, double4_32a* av, const int* vscene, const SceneDev* scenes,
+                    PassCounters* ctr, cudaStream_t s) {
+    int blocks = nblk(zone_cap, 64);
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    if (blocks > 0)
+        count_launch(), k_zone_solve<<<blocks, 64, 0, s>>>(members, nullptr, zone_rng, zone_cap, dnz, fixed, xo, av,
+                                                           vscene, scenes, ctr, nullptr);
 }
 
 void final_rigid(const BodyBufs& b, const uint8_t* has_collsn, const double4_32a* av, cudaStream_t s) {

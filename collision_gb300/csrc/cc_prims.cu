@@ -102,7 +102,16 @@ constexpr int kSortItems = 8;
 constexpr int kSortTile = kSortThreads * kSortItems;
 constexpr int kRadix = 256;
 
-__global__ void k_radix_hist(const unsigned long long* keys, int n, int shift, int* hist, int nblocks) {
+// dn (may be null): the number of pairs to sort is min(*dn, n).
+__device__ __forceinline__ int sort_count(const int* dn, int n) {
+    if (!dn) return n;
+    const int m = *dn;
+    return m < n ? (m > 0 ? m : 0) : n;
+}
+
+__global__ void k_radix_hist(const unsigned long long* keys, int n, int shift, int* hist, int nblocks,
+                             const int* dn) {
+    n = sort_count(dn, n);
     __shared__ int h[kRadix];
     h[threadIdx.x] = 0;
     __syncthreads();
@@ -117,7 +126,8 @@ __global__ void k_radix_hist(const unsigned long long* keys, int n, int shift, i
 }
 
 __global__ void k_radix_scatter(const unsigned long long* keys, const unsigned int* vals, unsigned long long* okeys,
-                                unsigned int* ovals, int n, int shift, const int* off, int nblocks) {
+                                unsigned int* ovals, int n, int shift, const int* off, int nblocks, const int* dn) {
+    n = sort_count(dn, n);
     __shared__ int run[kRadix];
     __shared__ int wcnt[kSortThreads / 32][kRadix];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -176,6 +186,11 @@ size_t radix_sort_temp_bytes(int n) {
 }
 
 void radix_sort_pairs(unsigned long long* keys, unsigned int* vals, int n, int bits, void* temp, cudaStream_t s) {
+    radix_sort_pairs_dev(keys, vals, nullptr, n, bits, temp, s);
+}
+
+void radix_sort_pairs_dev(unsigned long long* keys, unsigned int* vals, const int* dn, int n, int bits, void* temp,
+                          cudaStream_t s) {
     if (n <= 1 || bits <= 0) return;
     int nb = ceil_div(n, kSortTile);
     size_t hist_n = (size_t)kRadix * nb;
@@ -197,9 +212,9 @@ void radix_sort_pairs(unsigned long long* keys, unsigned int* vals, int n, int b
     int passes = (bits + 7) / 8;
     for (int ps = 0; ps < passes; ++ps) {
         int shift = ps * 8;
-        count_launch(), k_radix_hist<<<nb, kSortThreads, 0, s>>>(ka, n, shift, hist, nb);
+        count_launch(), k_radix_hist<<<nb, kSortThreads, 0, s>>>(ka, n, shift, hist, nb, dn);
         exclusive_scan(hist, off, (int)hist_n, nullptr, stemp, s);
-        count_launch(), k_radix_scatter<<<nb, kSortThreads, 0, s>>>(ka, va, kb, vb, n, shift, off, nb);
+        count_launch(), k_radix_scatter<<<nb, kSortThreads, 0, s>>>(ka, va, kb, vb, n, shift, off, nb, dn);
         unsigned long long* tk = ka; ka = kb; kb = tk;
         unsigned int* tv = va; va = vb; vb = tv;
     }

@@ -67,6 +67,7 @@ __global__ void k_reset_counters(PassCounters* c) {
     int keep = c->err & kErrNan;
     c->npairs = 0; c->ncontrib = 0; c->nhit_pairs = 0; c->nrec = 0;
     c->nvisits = 0; c->ncontacts = 0; c->nsub = 0; c->ncr = 0; c->nunion = 0; c->nsub_pt = 0; c->nsub_ee = 0; c->npairq = 0;
+    c->nzones = 0; c->nmembers = 0; c->nseg = 0;
     c->err = keep;
 }
 
@@ -79,7 +80,8 @@ __global__ void k_reset_pass(PassCounters* c, SceneRun* run, int nscenes, int np
         int keep = c->err & kErrNan;
         c->npairs = npairs_keep >= 0 ? npairs_keep : 0; c->ncontrib = 0; c->nhit_pairs = 0; c->nrec = 0;
         c->nvisits = 0; c->ncontacts = 0; c->nsub = 0; c->ncr = 0; c->nunion = 0; c->nsub_pt = 0; c->nsub_ee = 0; c->npairq = 0;
-    c->err = keep;
+        c->nzones = 0; c->nmembers = 0; c->nseg = 0;
+        c->err = keep;
     }
     if (i < nscenes) run[i].hits = 0;
 }
@@ -169,17 +171,18 @@ struct cc_solver {
     double4_32a* d_xo = nullptr;
     double4_32a* d_av = nullptr;
     // impact zones: the reference's union-find with member lists
-    // (dcollid.cpp:1015-1059), kept on the host and rebuilt from the
-    // recorded createImpZone calls of each impact-zone pass in visiting order
+    // (dcollid.cpp:1015-1059) on the device (cc_zones.cu), joined by each
+    // impact-zone pass's createImpZone records in visiting order. The host
+    // arrays compute the state every step starts from (makeSet and the
+    // movable bodies' unions) at assembly, and read the zones back on request.
     std::vector<int> uf_root, uf_next, uf_tail, uf_w, uf_touched;
     std::vector<int> h_vscene;
     UnionRec* d_urec = nullptr;
     int urec_cap = 0;
-    std::vector<UnionRec> h_urec;
-    std::vector<int> h_members, h_zone_off;
-    int* d_members = nullptr;
-    int* d_zone_off = nullptr;
-    int members_cap = 0, zones_cap = 0;
+    ZoneBufs zb;
+    UfNode* d_uf0 = nullptr;  // the union-find every step starts from
+    int* d_cc0 = nullptr;
+    bool uf_on_device = false;  // the host arrays are stale: the device holds the last step's zones
     // staging for host-buffer calls
     double* d_xold_in = nullptr;
     double* d_xcand_in = nullptr;
@@ -362,12 +365,17 @@ struct cc_solver {
         if (h_bbox) cudaFreeHost(h_bbox);
         h_bbox = nullptr;
         dfree(d_xo); dfree(d_av);
-        dfree(d_urec); dfree(d_members); dfree(d_zone_off);
-        urec_cap = members_cap = zones_cap = 0;
+        dfree(d_urec);
+        urec_cap = 0;
+        dfree(zb.keys); dfree(zb.vals); dfree(zb.seg); dfree(zb.cc); dfree(zb.uf); dfree(zb.zone_rng);
+        dfree(zb.zone_root); dfree(zb.members); dfree(d_uf0); dfree(d_cc0);
+        if (zb.sort_temp) cudaFree(zb.sort_temp);
+        zb = ZoneBufs{};
+        uf_on_device = false;
         dfree(d_xold_in); dfree(d_xcand_in); dfree(d_vel); dfree(d_xout); dfree(d_hc);
         dfree(d_box); dfree(d_box_st); dfree(bvh.keys); dfree(bvh.order); dfree(bvh.range_hi);
         dfree(bvh.range_lo); dfree(bvh.parent); dfree(bvh.flags); dfree(bvh.node); dfree(bvh.bbox_enc); dfree(bvh.leaf);
-        dfree(bvh.rnode); dfree(bvh.rope);
+        dfree(bvh.rnode); dfree(bvh.rope); dfree(bvh.leaf32); dfree(bvh.qnext);
         if (bvh.sort_temp) cudaFree(bvh.sort_temp);
         bvh = BvhBufs{};
         dfree(d_pairs); dfree(d_contrib); dfree(d_pair_hit); dfree(d_pairq); dfree(d_sub_pt); dfree(d_sub_ee);
@@ -455,8 +463,43 @@ struct cc_solver {
     }
     cc_status grow_unions(int cap) {
         dfree(d_urec);
-        if (dalloc(&d_urec, (size_t)cap) != cudaSuccess) return fail(CC_NO_MEMORY, "union record buffer");
+        dfree(zb.keys);
+        dfree(zb.vals);
+        dfree(zb.seg);
+        if (zb.sort_temp) cudaFree(zb.sort_temp);
+        zb.sort_temp = nullptr;
+        if (dalloc(&d_urec, (size_t)cap) != cudaSuccess || dalloc(&zb.keys, (size_t)cap) != cudaSuccess ||
+            dalloc(&zb.vals, (size_t)cap) != cudaSuccess || dalloc(&zb.seg, (size_t)cap) != cudaSuccess ||
+            cudaMalloc(&zb.sort_temp, zone_sort_temp_bytes(cap)) != cudaSuccess)
+            return fail(CC_NO_MEMORY, "union record buffer");
         urec_cap = cap;
+        zb.cap = cap;
+        zb.rec = d_urec;
+        return CC_OK;
+    }
+    // The device union-find as every step starts it.
+    void start_zones() {
+        if (nv == 0) return;
+        cudaMemcpyAsync(zb.uf, d_uf0, sizeof(UfNode) * (size_t)nv, cudaMemcpyDeviceToDevice, stream);
+        cudaMemcpyAsync(zb.cc, d_cc0, sizeof(int) * (size_t)nv, cudaMemcpyDeviceToDevice, stream);
+        uf_on_device = true;
+    }
+    // The zone root of every point after the last step.
+    cc_status zone_roots(int* out) {
+        if (!uf_on_device) {
+            for (int i = 0; i < nv; ++i) out[i] = find_set(i);
+            return CC_OK;
+        }
+        std::vector<UfNode> u((size_t)nv);
+        if (nv && cudaMemcpyAsync(u.data(), zb.uf, sizeof(UfNode) * (size_t)nv, cudaMemcpyDeviceToHost, stream) !=
+                      cudaSuccess)
+            return cuda_check("zone roots");
+        if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("zone roots");
+        for (int i = 0; i < nv; ++i) {
+            int r = i;
+            for (int k = 0; u[r].root != r && k <= nv; ++k) r = u[r].root;
+            out[i] = r;
+        }
         return CC_OK;
     }
 
@@ -500,7 +543,6 @@ struct cc_solver {
         uf_next[uf_tail[py]] = px;
         uf_tail[py] = uf_tail[px];
     }
-    cc_status zone_pass_unions();
 
     // One .vtp per scene of the pass just applied (cc_vtk.cpp).
     cc_status write_vtk_pass() {
@@ -952,6 +994,8 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     ok &= dalloc(&bvh.leaf, (size_t)ne) == cudaSuccess;
     ok &= dalloc(&bvh.rnode, (size_t)ne) == cudaSuccess;
     ok &= dalloc(&bvh.rope, (size_t)ne) == cudaSuccess;
+    ok &= dalloc(&bvh.leaf32, (size_t)ne) == cudaSuccess;
+    ok &= dalloc(&bvh.qnext, 1) == cudaSuccess;
     ok &= dalloc(&bvh.bbox_enc, 6 * (size_t)n) == cudaSuccess;
     ok &= cudaMalloc(&bvh.sort_temp, radix_sort_temp_bytes(ne > 0 ? ne : 1)) == cudaSuccess;
     ok &= dalloc(&apply.cnt, (size_t)nv + nbodies) == cudaSuccess;
@@ -1066,6 +1110,28 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
         body_bufs.fixed = d_fixed;
         h_body_out.assign((size_t)nbodies, double4_32a{});
     }
+    {
+        // the union-find every step starts from: makeSet, then the movable
+        // bodies' unions (reset_zones above, when there are bodies)
+        const int nz = nv / 2 + 1;
+        bool zok = dalloc(&zb.cc, (size_t)nv) == cudaSuccess && dalloc(&zb.uf, (size_t)nv) == cudaSuccess &&
+                   dalloc(&d_cc0, (size_t)nv) == cudaSuccess && dalloc(&d_uf0, (size_t)nv) == cudaSuccess &&
+                   dalloc(&zb.zone_rng, (size_t)nz) == cudaSuccess && dalloc(&zb.zone_root, (size_t)nz) == cudaSuccess &&
+                   dalloc(&zb.members, (size_t)nv) == cudaSuccess;
+        if (!zok) return fail(CC_NO_MEMORY, "zone buffers");
+        zb.zone_cap = nz;
+        std::vector<UfNode> u0((size_t)nv);
+        std::vector<int> c0((size_t)nv);
+        for (int p = 0; p < nv; ++p) {
+            u0[p] = UfNode{uf_root[p], uf_next[p], uf_tail[p], uf_w[p]};
+            c0[p] = find_set(p);
+        }
+        if (nv) {
+            cudaMemcpy(d_uf0, u0.data(), sizeof(UfNode) * (size_t)nv, cudaMemcpyHostToDevice);
+            cudaMemcpy(d_cc0, c0.data(), sizeof(int) * (size_t)nv, cudaMemcpyHostToDevice);
+        }
+        uf_on_device = false;
+    }
     if (grow_unions(1024)) return CC_NO_MEMORY;
     if (grow_subs(2 * ne + 4096)) return CC_NO_MEMORY;
     h_strain_passes.assign(3 * (size_t)n, 0);
@@ -1179,8 +1245,8 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
         if (!reuse) {
             prof(kStTraverse, true);
             bvh_pairs(d_box, on_full ? full_view() : bvh, d_pairs, pair_cap, d_ctr, stream, record ? nullptr : d_ev,
-                      tune.traverse_block,
-                      combined ? d_box_st : nullptr, tune.packet_traverse, tune.rope_traverse);
+                      tune.traverse_block, combined ? d_box_st : nullptr, tune.packet_traverse, tune.rope_traverse,
+                      tune.traverse_refill, tune.stack_depth);
             prof(kStTraverse, false);
             if (attempt == 0) counters[16] += bvh.n;
         }
@@ -1223,6 +1289,10 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
         int e = h_ctr->err;
         if (e & kErrNan) return fail(CC_NAN_DETECTED, "non-finite velocity or normal (the reference exits here)");
         if (e & kErrIndex) return fail(CC_CUDA_ERROR, index_error(e));
+        if ((e & kErrStack) && tune.stack_depth < kTraversalStack) {
+            tune.stack_depth = kTraversalStack;  // a tuned shallower stack was too shallow here
+            continue;
+        }
         if (e & kErrStack) return fail(CC_STACK_OVERFLOW, "BVH traversal stack overflow");
         if (e & kErrPairOverflow) {
             st = grow_pairs(2 * h_ctr->npairs + 1024);
@@ -1282,72 +1352,13 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
     }
     if (any_zone) {
         prof(kStZone, true);
-        st = zone_pass_unions();
-        if (st) return st;
+        zone_pass(zb, d_ctr, d_fixed, bvh.act ? d_act_p : nullptr, n_act_p, nullptr, d_vscene, d_run, d_scenes, d_av,
+                  d_xo, stream);
         prof(kStZone, false);
         cudaMemcpyAsync(h_ctr, d_ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, stream);
     }
     if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("pass tail");
     if (h_ctr->err & kErrNan) return fail(CC_NAN_DETECTED, "non-finite zone velocity (the reference exits here)");
-    return CC_OK;
-}
-
-// The unions of an impact-zone pass and the zones' rigid motion
-// (computeImpactZone, dcollid.cpp:236-262). The pass's createImpZone calls
-// are replayed in the reference's visiting order of each scene - the order
-// decides which point heads each member list and how the lists are
-// concatenated - and every zone of more than one point in a scene in
-// impact-zone mode is solved over its list (updateImpactZoneVelocity,
-// dcollid.cpp:290-310).
-cc_status cc_solver::zone_pass_unions() {
-    int n = h_ctr->nunion;
-    if (n > 0) {
-        h_urec.resize((size_t)n);
-        cudaMemcpyAsync(h_urec.data(), d_urec, sizeof(UnionRec) * (size_t)n, cudaMemcpyDeviceToHost, stream);
-        if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("union records");
-        std::vector<int> ord((size_t)n);
-        for (int i = 0; i < n; ++i) ord[i] = i;
-        std::sort(ord.begin(), ord.end(), [&](int a, int b) {
-            int sa = h_vscene[h_urec[a].p[0]], sb = h_vscene[h_urec[b].p[0]];
-            return sa != sb ? sa < sb : h_urec[a].key < h_urec[b].key;
-        });
-        for (int i : ord) {
-            const int* pts = h_urec[i].p;
-            for (int a = 0; a < 4; ++a) uf_touched.push_back(pts[a]);
-            for (int a = 0; a < 4; ++a)  // createImpZone(pts, 4), dcollid.cpp:473-484
-                for (int b = 0; b < a; ++b)
-                    if (!((h_fixed[pts[a]] | h_fixed[pts[b]]) & 2)) merge_point(pts[a], pts[b]);
-        }
-    }
-    h_members.clear();
-    h_zone_off.clear();
-    for (int p : uf_touched) {
-        if (uf_root[p] != p || uf_w[p] < 2 || uf_w[p] < 0) continue;
-        if (h_run[h_vscene[p]].mode != kSceneZone) continue;
-        uf_w[p] = -uf_w[p];  // listed (restored below)
-        h_zone_off.push_back((int)h_members.size());
-        for (int q = p; q >= 0; q = uf_next[q]) h_members.push_back(q);
-    }
-    int nz = (int)h_zone_off.size();
-    for (int z = 0; z < nz; ++z) {
-        int r = h_members[h_zone_off[z]];
-        uf_w[r] = -uf_w[r];
-    }
-    h_zone_off.push_back((int)h_members.size());
-    if (nz == 0) return CC_OK;
-    if ((int)h_members.size() > members_cap) {
-        dfree(d_members);
-        members_cap = 2 * (int)h_members.size();
-        if (dalloc(&d_members, (size_t)members_cap) != cudaSuccess) return fail(CC_NO_MEMORY, "zone members");
-    }
-    if (nz + 1 > zones_cap) {
-        dfree(d_zone_off);
-        zones_cap = 2 * (nz + 1);
-        if (dalloc(&d_zone_off, (size_t)zones_cap) != cudaSuccess) return fail(CC_NO_MEMORY, "zone offsets");
-    }
-    cudaMemcpyAsync(d_members, h_members.data(), sizeof(int) * h_members.size(), cudaMemcpyHostToDevice, stream);
-    cudaMemcpyAsync(d_zone_off, h_zone_off.data(), sizeof(int) * h_zone_off.size(), cudaMemcpyHostToDevice, stream);
-    zone_solve(d_members, d_zone_off, nz, d_fixed, d_xo, d_av, d_vscene, d_scenes, d_ctr, stream);
     return CC_OK;
 }
 
@@ -1379,7 +1390,7 @@ cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, dou
     if (ne == 0) {
         // the reference dereferences an empty tree here; nothing collides
         if (nv) cudaMemcpyAsync(x_out, x_cand, sizeof(double) * 3 * (size_t)nv, cudaMemcpyDeviceToDevice, stream);
-        reset_zones();
+        start_zones();
         cudaStreamSynchronize(stream);
         return cuda_check("empty mesh");
     }
@@ -1395,7 +1406,7 @@ cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, dou
     strain_setup(d_edges, nedges, d_scenes, strain_plan(), d_xo, d_strain_step, d_vscene, stream);
     tail_done.assign((size_t)nscenes, 0);
     tails_this_step = 0;
-    reset_zones();
+    start_zones();
     bvh_this_step = false;
     full_this_step = false;
     reuse_pairs = false;
@@ -1563,7 +1574,7 @@ cc_status cc_solver::check_ccd(const double* x_old, const double* x_new, long lo
     for (int attempt = 0; attempt < 8; ++attempt) {
         count_launch(), k_reset_pass<<<(nscenes + 255) / 256, 256, 0, stream>>>(d_ctr, d_run, nscenes);
         bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, d_ev, tune.traverse_block, nullptr,
-                  tune.packet_traverse, tune.rope_traverse);
+                  tune.packet_traverse, tune.rope_traverse, tune.traverse_refill, kTraversalStack);
         NarrowArgs a{};
         a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
         a.vbody = d_vbody; a.body_mass = d_body_mass; a.body_slot0 = nv;
@@ -1628,7 +1639,7 @@ cc_status cc_solver::autotune(double* best_ms) {
             count_launch(), k_reset_pass<<<(nscenes + 255) / 256, 256, 0, stream>>>(d_ctr, d_run, nscenes);
             cudaEventRecord(e0, stream);
             bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, d_ev, t.traverse_block, nullptr,
-                      t.packet_traverse, t.rope_traverse);
+                      t.packet_traverse, t.rope_traverse, t.traverse_refill, t.stack_depth);
             NarrowArgs a{};
             a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
         a.vbody = d_vbody; a.body_mass = d_body_mass; a.body_slot0 = nv;
@@ -1670,6 +1681,10 @@ cc_status cc_solver::autotune(double* best_ms) {
                 continue;
             }
             if (e & kErrIndex) return fail(CC_CUDA_ERROR, "autotune: " + index_error(e));
+            if ((e & kErrStack) && t.stack_depth < kTraversalStack && !t.rope_traverse) {
+                *ms = 1e30f;  // too shallow a stack for this state: not a candidate
+                return CC_OK;
+            }
             if (e & (kErrStack | kErrNan)) return fail(CC_STACK_OVERFLOW, "autotune pass failed");
             cudaEventElapsedTime(ms, e0, e1);
             return CC_OK;
@@ -1692,18 +1707,46 @@ cc_status cc_solver::autotune(double* best_ms) {
     cc_status st = time_it(best_t, best_split, &best);  // the current setting, which also sizes the buffers
     const int tb[] = {64, 128, 256, 512};
     const int nb[] = {64, 128, 256};
-    // the stackless traversal and the one with a stack per thread (the warp
-    // packets are slower on cloth)
-    for (int rope = 1; rope >= 0; --rope) {
-        for (int a : tb) {
+    const int refills[] = {4, 8, 16, 32};
+    const int depths[] = {24, 32, 48, 64};
+    // the stackless traversal with dynamic query fetch (lanes refilling
+    // together), and with one thread per query over the block sizes
+    for (int r : refills) {
+        LaunchTuning t = best_t;
+        t.rope_traverse = true;
+        t.traverse_refill = r;
+        float m;
+        if (!st) st = time_it(t, best_split, &m);
+        if (!st && m < best) { best = m; best_t = t; }
+    }
+    for (int a : tb) {
+        LaunchTuning t = best_t;
+        t.rope_traverse = true;
+        t.traverse_refill = 0;
+        t.traverse_block = a;
+        float m;
+        if (!st) st = time_it(t, best_split, &m);
+        if (!st && m < best) { best = m; best_t = t; }
+    }
+    // the traversal with a stack per thread: block size, then stack depth
+    // (the warp packets are slower on cloth)
+    for (int a : tb) {
+        LaunchTuning t = best_t;
+        t.rope_traverse = false;
+        t.traverse_block = a;
+        t.stack_depth = kTraversalStack;
+        float m;
+        if (!st) st = time_it(t, best_split, &m);
+        if (!st && m < best) { best = m; best_t = t; }
+    }
+    if (!best_t.rope_traverse)
+        for (int d : depths) {
             LaunchTuning t = best_t;
-            t.rope_traverse = rope != 0;
-            t.traverse_block = a;
+            t.stack_depth = d;
             float m;
             if (!st) st = time_it(t, best_split, &m);
             if (!st && m < best) { best = m; best_t = t; }
         }
-    }
     for (int split = (mode == 1 ? 0 : 1); split <= (mode == 1 ? 1 : 0) && !st; ++split) {
         for (int b : nb) {
             LaunchTuning t = best_t;
@@ -1911,6 +1954,19 @@ cc_status cc_set_tuning(cc_solver* s, int knob, int value) {
         case CC_TUNE_SUBSET_REFIT:
             s->subset_refit = value != 0;
             return CC_OK;
+        case CC_TUNE_TRAVERSE_REFILL:
+            if (value < 0 || value > 32) return CC_BAD_INPUT;
+            s->tune.traverse_refill = value;
+            return CC_OK;
+        case CC_TUNE_STACK_DEPTH:
+            if (value != 24 && value != 32 && value != 48 && value != 64) return CC_BAD_INPUT;
+            s->tune.stack_depth = value;
+            return CC_OK;
+        case CC_TUNE_PAIR_CAPACITY:
+            if (value < 4096) return CC_BAD_INPUT;
+            cudaSetDevice(s->device);
+            cudaStreamSynchronize(s->stream);
+            return s->grow_pairs(value);
         case CC_TUNE_STRAIN_BLOCK:
             if (value < 32 || value > 256 || value % 32) return CC_BAD_INPUT;
             s->tune.strain_block = value;
@@ -1940,6 +1996,9 @@ int cc_get_tuning(cc_solver* s, int knob) {
         case CC_TUNE_TAIL_OVERLAP: return s->overlap_tails ? 1 : 0;
         case CC_TUNE_ROPE_TRAVERSE: return s->tune.rope_traverse ? 1 : 0;
         case CC_TUNE_SUBSET_REFIT: return s->subset_refit ? 1 : 0;
+        case CC_TUNE_TRAVERSE_REFILL: return s->tune.traverse_refill;
+        case CC_TUNE_STACK_DEPTH: return s->tune.stack_depth;
+        case CC_TUNE_PAIR_CAPACITY: return s->pair_cap;
         default: return -1;
     }
 }
@@ -2065,8 +2124,8 @@ int cc_get_pass_kinds(cc_solver* s, int* out, int cap) {
 
 cc_status cc_get_zone_roots(cc_solver* s, int* out) {
     if (!s || !out) return CC_BAD_INPUT;
-    for (int i = 0; i < s->nv; ++i) out[i] = s->find_set(i);
-    return CC_OK;
+    cudaSetDevice(s->device);
+    return s->zone_roots(out);
 }
 
 cc_status cc_get_leaf_ranks(cc_solver* s, int which, int* out) {
@@ -2100,7 +2159,8 @@ int cc_debug_candidate_pairs(cc_solver* s, int moving, int brute_force, int* out
             brute_pairs(s->d_box, s->ne, s->d_escene, s->d_pairs, s->pair_cap, s->d_ctr, s->stream);
         else
             bvh_pairs(s->d_box, s->bvh, s->d_pairs, s->pair_cap, s->d_ctr, s->stream, nullptr, s->tune.traverse_block,
-                      nullptr, s->tune.packet_traverse, s->tune.rope_traverse);
+                      nullptr, s->tune.packet_traverse, s->tune.rope_traverse, s->tune.traverse_refill,
+                      kTraversalStack);
         cudaMemcpyAsync(s->h_ctr, s->d_ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, s->stream);
         if (cudaStreamSynchronize(s->stream) != cudaSuccess) return -1;
         if (s->h_ctr->err & kErrPairOverflow) {

@@ -1,0 +1,238 @@
+// Impact zones on the GPU: the reference's union-find with member lists
+// (makeSet / findSet / mergePoint / createImpZone, dcollid.cpp:473-484,
+// 1015-1059) and the rigid motion of every zone (computeImpactZone,
+// dcollid.cpp:236-262).
+//
+// The member list of a zone fixes the order in which updateImpactListVelocity
+// (dcollid3d.cpp:70-200) sums its centre of mass, momentum and inertia, and
+// that order comes from the exact sequence of weighted unions with list
+// concatenation: the lighter set's list is appended to the heavier one's.
+// A concurrent union-find gives the same partition but another order, so the
+// unions of a pass are replayed in the reference's visiting order - but only
+// where order matters: the unions of different final zones touch disjoint
+// points, so every final zone replays its own unions, one thread per zone,
+// all zones at once.
+//
+//   1. A lock-free union-find over the same points (cc: parent links, the
+//      smaller index as root) joins the pass's pairs: its roots label the
+//      final zone of every createImpZone record.
+//   2. The records are sorted by (label, visiting-order key) - two stable
+//      radix sorts, key first - and cut into one segment per label.
+//   3. One thread per segment replays its records' unions in key order on
+//      the exact union-find (UfNode), with path compression.
+//   4. Every root of two or more points in a scene in impact-zone mode is a
+//      zone: its members are written out by walking its list, and the zone
+//      moves rigidly (k_zone_solve).
+// Both union-finds start every step from the state makeSet and the movable
+// bodies' unions (createImpZoneForRG, dcollid3d.cpp:54-68) leave.
+#include "cc_launch.h"
+
+namespace ccg {
+
+namespace {
+
+inline int nblk(int n, int t) { return (n + t - 1) / t; }
+
+__device__ __forceinline__ int count_of(const int* c, int cap) {
+    const int n = *c;
+    return n < cap ? n : cap;
+}
+
+// A pair of a createImpZone(pts, 4) call that mergePoint joins: every pair
+// (a, b), b < a, without a movable point (dcollid.cpp:478-480).
+__device__ __forceinline__ bool joins(const uint8_t* fixed, int pa, int pb) {
+    return !((fixed[pa] | fixed[pb]) & 2);
+}
+
+__device__ __forceinline__ int cc_find(int* cc, int p) {
+    // path halving: every link written points to an ancestor, so concurrent
+    // finds and unions stay correct
+    int q = cc[p];
+    while (q != p) {
+        const int g = cc[q];
+        if (g != q) cc[p] = g;
+        p = q;
+        q = g;
+    }
+    return p;
+}
+
+__device__ __forceinline__ void cc_union(int* cc, int a, int b) {
+    for (;;) {
+        a = cc_find(cc, a);
+        b = cc_find(cc, b);
+        if (a == b) return;
+        if (a < b) {
+            const int t = a;
+            a = b;
+            b = t;
+        }
+        // the larger root is linked under the smaller one, if still a root
+        if (atomicCAS(&cc[a], a, b) == a) return;
+    }
+}
+
+__global__ void k_cc_union(const UnionRec* __restrict__ rec, const PassCounters* ctr, int cap,
+                           const uint8_t* __restrict__ fixed, int* cc) {
+    if (ctr->err & kErrRetry) return;
+    const int n = count_of(&ctr->nunion, cap);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const UnionRec r = rec[i];
+        for (int a = 1; a < 4; ++a)
+            for (int b = 0; b < a; ++b)
+                if (joins(fixed, r.p[a], r.p[b])) cc_union(cc, r.p[a], r.p[b]);
+    }
+}
+
+// Sort keys, first pass: the visiting-order key of every record.
+__global__ void k_union_keys(const UnionRec* __restrict__ rec, const PassCounters* ctr, int cap,
+                             unsigned long long* keys, unsigned int* vals) {
+    if (ctr->err & kErrRetry) return;
+    const int n = count_of(&ctr->nunion, cap);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        keys[i] = rec[i].key;
+        vals[i] = (unsigned int)i;
+    }
+}
+
+constexpr unsigned long long kNoLabel = (1ull << 31) - 1;
+
+// Second pass: the final zone of each record (in key order), or kNoLabel for
+// a record that joins nothing.
+__global__ void k_union_labels(const UnionRec* __restrict__ rec, const PassCounters* ctr, int cap,
+                               const uint8_t* __restrict__ fixed, int* cc, const unsigned int* __restrict__ vals,
+                               unsigned long long* keys) {
+    if (ctr->err & kErrRetry) return;
+    const int n = count_of(&ctr->nunion, cap);
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const UnionRec r = rec[vals[j]];
+        unsigned long long lab = kNoLabel;
+        for (int a = 1; a < 4 && lab == kNoLabel; ++a)
+            for (int b = 0; b < a; ++b)
+                if (joins(fixed, r.p[a], r.p[b])) {
+                    lab = (unsigned long long)cc_find(cc, r.p[a]);
+                    break;
+                }
+        keys[j] = lab;
+    }
+}
+
+// The first record of every label's run.
+__global__ void k_union_segments(const unsigned long long* __restrict__ keys, PassCounters* ctr, int cap, int* seg) {
+    if (ctr->err & kErrRetry) return;
+    const int n = count_of(&ctr->nunion, cap);
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const unsigned long long k = keys[j];
+        if (k != kNoLabel && (j == 0 || keys[j - 1] != k)) seg[atomicAdd(&ctr->nseg, 1)] = j;
+    }
+}
+
+// findSet (dcollid.cpp:1024-1031) with path compression.
+__device__ __forceinline__ int uf_find(UfNode* uf, int p) {
+    int r = p;
+    while (uf[r].root != r) r = uf[r].root;
+    while (uf[p].root != r) {
+        const int nx = uf[p].root;
+        uf[p].root = r;
+        p = nx;
+    }
+    return r;
+}
+
+// mergePoint (dcollid.cpp:1033-1059): the lighter set joins the heavier one
+// (the second on equal weights) and its member list is appended.
+__device__ __forceinline__ void uf_merge(UfNode* uf, int x, int y) {
+    int px = uf_find(uf, x), py = uf_find(uf, y);
+    if (px == py) return;
+    if (uf[px].w > uf[py].w) {
+        const int t = px;
+        px = py;
+        py = t;
+    }
+    uf[py].w += uf[px].w;
+    uf[px].root = py;
+    uf[uf[py].tail].next = px;
+    uf[py].tail = uf[px].tail;
+}
+
+// One thread per final zone touched by the pass: its records' unions in
+// visiting order, as createImpZone makes them.
+__global__ void k_union_replay(const UnionRec* __restrict__ rec, const PassCounters* ctr, int cap,
+                               const unsigned long long* __restrict__ keys, const unsigned int* __restrict__ vals,
+                               const int* __restrict__ seg, const uint8_t* __restrict__ fixed, UfNode* uf) {
+    if (ctr->err & kErrRetry) return;
+    const int n = count_of(&ctr->nunion, cap);
+    const int nseg = ctr->nseg;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nseg; s += gridDim.x * blockDim.x) {
+        const int j0 = seg[s];
+        const unsigned long long lab = keys[j0];
+        for (int j = j0; j < n && keys[j] == lab; ++j) {
+            const UnionRec r = rec[vals[j]];
+            for (int a = 1; a < 4; ++a)
+                for (int b = 0; b < a; ++b)
+                    if (joins(fixed, r.p[a], r.p[b])) uf_merge(uf, r.p[a], r.p[b]);
+        }
+    }
+}
+
+// Every zone of a scene in impact-zone mode: a root of two or more points.
+// Each gets a contiguous run of the member array (zones in any order: each
+// one's rigid motion depends on its own members only).
+__global__ void k_zone_enum(const int* __restrict__ act_pts, int n, const int* __restrict__ dn,
+                            const int* __restrict__ vscene, const SceneRun* __restrict__ run,
+                            const UfNode* __restrict__ uf, PassCounters* ctr, int2* zone_rng, int* zone_root) {
+    if (ctr->err & kErrRetry) return;
+    if (dn) n = *dn;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int p = act_pts ? act_pts[k] : k;
+        const UfNode u = uf[p];
+        if (u.root != p || u.w < 2 || run[vscene[p]].mode != kSceneZone) continue;
+        const int z = atomicAdd(&ctr->nzones, 1);
+        const int m = atomicAdd(&ctr->nmembers, u.w);
+        zone_rng[z] = make_int2(m, m + u.w);
+        zone_root[z] = p;
+    }
+}
+
+// The member list of every zone, from its root along the next links.
+__global__ void k_zone_members(const PassCounters* ctr, const int2* __restrict__ zone_rng,
+                               const int* __restrict__ zone_root, const UfNode* __restrict__ uf, int* members) {
+    if (ctr->err & kErrRetry) return;
+    const int nz = ctr->nzones;
+    for (int z = blockIdx.x * blockDim.x + threadIdx.x; z < nz; z += gridDim.x * blockDim.x) {
+        const int2 r = zone_rng[z];
+        int p = zone_root[z];
+        for (int i = r.x; i < r.y && p >= 0; ++i) {
+            members[i] = p;
+            p = uf[p].next;
+        }
+    }
+}
+
+}  // namespace
+
+size_t zone_sort_temp_bytes(int cap) { return radix_sort_temp_bytes(cap); }
+
+void zone_pass(const ZoneBufs& z, const PassCounters* ctr_c, const uint8_t* fixed, const int* act_pts, int n_pts,
+               const int* dn_pts, const int* vscene, const SceneRun* run, const SceneDev* scenes, double4_32a* av,
+               const double4_32a* xo, cudaStream_t s) {
+    PassCounters* ctr = const_cast<PassCounters*>(ctr_c);
+    const int cap = z.cap;
+    const int blocks = nblk(cap, 256) < 152 * 8 ? nblk(cap, 256) : 152 * 8;
+    count_launch(), k_cc_union<<<blocks, 256, 0, s>>>(z.rec, ctr, cap, fixed, z.cc);
+    count_launch(), k_union_keys<<<blocks, 256, 0, s>>>(z.rec, ctr, cap, z.keys, z.vals);
+    radix_sort_pairs_dev(z.keys, z.vals, &ctr->nunion, cap, 48, z.sort_temp, s);
+    count_launch(), k_union_labels<<<blocks, 256, 0, s>>>(z.rec, ctr, cap, fixed, z.cc, z.vals, z.keys);
+    radix_sort_pairs_dev(z.keys, z.vals, &ctr->nunion, cap, 31, z.sort_temp, s);
+    count_launch(), k_union_segments<<<blocks, 256, 0, s>>>(z.keys, ctr, cap, z.seg);
+    count_launch(), k_union_replay<<<blocks, 128, 0, s>>>(z.rec, ctr, cap, z.keys, z.vals, z.seg, fixed, z.uf);
+    const int pb = dn_pts ? 152 * 8 : (nblk(n_pts, 256) < 152 * 8 ? nblk(n_pts, 256) : 152 * 8);
+    if (pb > 0)
+        count_launch(), k_zone_enum<<<pb, 256, 0, s>>>(act_pts, n_pts, dn_pts, vscene, run, z.uf, ctr, z.zone_rng,
+                                                       z.zone_root);
+    const int zb = nblk(z.zone_cap, 128) < 152 * 8 ? nblk(z.zone_cap, 128) : 152 * 8;
+    count_launch(), k_zone_members<<<zb, 128, 0, s>>>(ctr, z.zone_rng, z.zone_root, z.uf, z.members);
+    zone_solve_dev(z.members, z.zone_rng, &ctr->nzones, z.zone_cap, fixed, xo, av, vscene, scenes, ctr, s);
+}
+
+}  // namespace ccg

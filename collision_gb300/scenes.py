@@ -306,9 +306,15 @@ def strings(nstr=64, nseg=512, seglen=2e-3, dt=1e-3, h=1e-3, seed=0, speed=2.0,
                     bonds=b, bond_curve=c)
 
 
-def cloth_on_obstacle(n, obstacle, radius, speed, dt=1e-3, h=1e-3, seed=0, noise_rel=0.01):
+def cloth_on_obstacle(n, obstacle, radius, speed, dt=1e-3, h=1e-3, seed=0, noise_rel=0.01, gap=None):
+    """A cloth above a sphere (top at z = radius) or a 0.4x0.4x0.1 box (top at
+    z = 0.05), `gap` above the obstacle's top (default: 0.05 over a sphere,
+    0.10 over a box)."""
     rng = np.random.default_rng(seed)
-    cp, ct = grid_cloth(n, 1.0, radius + 0.05 if obstacle == "sphere" else 0.15)
+    top = radius if obstacle == "sphere" else 0.05
+    if gap is None:
+        gap = 0.05 if obstacle == "sphere" else 0.10
+    cp, ct = grid_cloth(n, 1.0, top + gap)
     cv = np.tile(np.array([0.0, 0.0, -speed]), (len(cp), 1))
     cv *= 1.0 + rng.uniform(-noise_rel, noise_rel, size=cv.shape)
     if obstacle == "sphere":
@@ -320,15 +326,25 @@ def cloth_on_obstacle(n, obstacle, radius, speed, dt=1e-3, h=1e-3, seed=0, noise
                     dict(dt=dt, thickness=h, lam=DEFAULTS["lam"]))
 
 
-def batched(nscenes=256, nmin=16, nmax=128, seed=0, dt=1e-3, h=1e-3):
+def batched(nscenes=256, nmin=16, nmax=128, seed=0, dt=1e-3, h=1e-3, approach_steps=(1.0, 4.0)):
+    """The batched workload. Each cloth starts above its obstacle by the
+    distance it falls in U(approach_steps) steps (drawn from a stream of its
+    own, so sizes, obstacles and speeds do not depend on it): every scene is
+    in contact from its first few steps on. approach_steps=None places the
+    cloths 0.05 above a sphere and 0.10 above a box instead, which the
+    slower cloths take up to 200 steps of free fall to cross."""
     rng = np.random.default_rng(seed)
+    gap_rng = np.random.default_rng([seed, 0x9a9])
     out = []
     for s in range(nscenes):
         n = int(rng.integers(nmin, nmax + 1))
         obst = "sphere" if rng.random() < 0.5 else "box"
         r = float(rng.uniform(0.1, 0.3))
         speed = float(rng.uniform(0.5, 3.0))
-        out.append(cloth_on_obstacle(n, obst, r, speed, dt=dt, h=h, seed=seed * 100003 + s))
+        gap = None
+        if approach_steps is not None:
+            gap = speed * dt * float(gap_rng.uniform(*approach_steps))
+        out.append(cloth_on_obstacle(n, obst, r, speed, dt=dt, h=h, seed=seed * 100003 + s, gap=gap))
     return out
 
 

@@ -244,6 +244,19 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
  *                           level's edges, copy-ins and write-backs run on
  *                           separate threads (when they fit in the block);
  *                           0: every thread takes one of each
+ *   CC_TUNE_TRAVERSE_REFILL 1..32 (default 8): the stackless traversal runs
+ *                           on resident warps whose lanes take new queries
+ *                           from a counter once this many of them have
+ *                           finished their walks, testing each leaf on a
+ *                           32-byte FP32 record before its exact one; 0: one
+ *                           thread per query. Same pairs
+ *   CC_TUNE_STACK_DEPTH     entries of the per-thread stack of the stack
+ *                           traversal: 24, 32, 48 or 64 (default); a pass
+ *                           whose walk needs more is run again with 64
+ *   CC_TUNE_PAIR_CAPACITY   candidate pairs the pair buffer holds (>= 4096;
+ *                           default 8 per element + 4096, grown on overflow
+ *                           and by cc_autotune to a timed pass's need plus a
+ *                           quarter)
  * cc_get_tuning returns the current value, or -1 for an unknown knob. */
 enum {
     CC_TUNE_SPLIT_NARROW = 0,
@@ -257,16 +270,21 @@ enum {
     CC_TUNE_STRAIN_ROLES = 8,
     CC_TUNE_TAIL_OVERLAP = 9,
     CC_TUNE_ROPE_TRAVERSE = 10,
-    CC_TUNE_SUBSET_REFIT = 11
+    CC_TUNE_SUBSET_REFIT = 11,
+    CC_TUNE_TRAVERSE_REFILL = 12,
+    CC_TUNE_STACK_DEPTH = 13,
+    CC_TUNE_PAIR_CAPACITY = 14
 };
 cc_status cc_set_tuning(cc_solver* s, int knob, int value);
 int cc_get_tuning(cc_solver* s, int knob);
 /* Autotuner: on the state of the last resolve call, times one moving pass
  * of every scene (traversal and narrow phase, no impulses applied) for
- * candidate CC_TUNE_TRAVERSE_BLOCK, CC_TUNE_SPLIT_NARROW and
- * CC_TUNE_NARROW_BLOCK settings, keeps the fastest, and grows the pair and
- * sub-test buffers to that pass's needs plus a quarter. The solver's state
- * is unchanged. *best_ms (may be NULL) receives the best time. */
+ * candidate settings - CC_TUNE_TRAVERSE_REFILL, the stackless traversal's
+ * CC_TUNE_TRAVERSE_BLOCK, the stack traversal's block and
+ * CC_TUNE_STACK_DEPTH, CC_TUNE_SPLIT_NARROW and CC_TUNE_NARROW_BLOCK -
+ * keeps the fastest, and grows the pair and sub-test buffers to at least
+ * that pass's needs plus a quarter (CC_TUNE_PAIR_CAPACITY). The solver's
+ * state is unchanged. *best_ms (may be NULL) receives the best time. */
 cc_status cc_autotune(cc_solver* s, double* best_ms);
 
 /* Debugging dumps, as the reference writes under its "CollisionImpulse"
@@ -368,14 +386,18 @@ int cc_selftest_math(int device, int fn, const double* a, const double* b, doubl
  * fragmentation. Nothing is allocated: the caller owns the inputs and outputs,
  * and every intermediate array lives in an 8 MiB scratch area compiled into
  * the library (held on every GPU that loads it until exit). Limit: n <= 65536.
- *   boxes   device, n x 6 doubles (lo x,y,z, hi x,y,z), 16-byte aligned
+ *   boxes   device, n x 6 doubles (lo x,y,z, hi x,y,z), 16-byte aligned;
+ *           every coordinate finite and lo <= hi (else CC_BAD_INPUT)
  *   pairs   device, cap x 2 ints (element indices), 8-byte aligned
  *   npairs  host: the number of overlapping pairs (may exceed cap, then only
  *           cap are written and CC_PAIR_OVERFLOW is returned)
- *   stream  cudaStream_t or NULL; the call waits for its work to finish.
+ *   stream  cudaStream_t of `device` (else CC_BAD_INPUT) or NULL; the call
+ *           waits for its work to finish.
  * The first call on a device looks up the scratch area's address there; make
  * it before any stream capture starts. Calls share the scratch area: calls
- * that overlap on the GPU race. Errors: cc_static_last_error.
+ * that overlap on the GPU race. The calling thread's current device is the
+ * same after the call as before. A hierarchy index found out of range
+ * returns CC_CUDA_ERROR with *npairs = 0. Errors: cc_static_last_error.
  */
 cc_status cc_candidate_pairs_static(int device, const double* boxes, int n, int* pairs, int cap, int* npairs,
                                     void* stream);

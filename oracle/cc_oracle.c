@@ -37,6 +37,26 @@
 #ifndef M_PI
 #define M_PI 3.14159265358979323846
 #endif
+/* The reference's libm calls (isCoplanar, updateImpactListVelocity). Built
+ * with CCO_CRMATH, the correctly rounded versions of cc_oracle_crmath.cpp
+ * take their place: the reference's algorithm with correctly rounded
+ * transcendental functions, which tells a difference that comes from
+ * glibc's rare misroundings apart from any other. */
+#ifdef CCO_CRMATH
+double cco_cr_acos(double x);
+double cco_cr_cos(double x);
+double cco_cr_sin(double x);
+double cco_cr_pow(double x, double y);
+#define LM_ACOS cco_cr_acos
+#define LM_COS cco_cr_cos
+#define LM_SIN cco_cr_sin
+#define LM_POW cco_cr_pow
+#else
+#define LM_ACOS acos
+#define LM_COS cos
+#define LM_SIN sin
+#define LM_POW pow
+#endif
 #define MACH_EPS DBL_EPSILON
 #define ROUND_EPS 1e-10     /* collid.h:17 */
 #define BOX_PAD 1e-6        /* AABB.cpp:10-11, 15-16, 65-71 */
@@ -536,13 +556,13 @@ static int is_coplanar(cco_solver* s, const int* pts, double dt, double* roots) 
         double R2 = R * R;
         if (R2 < Q3) {
             double Qsqrt = sqrt(Q);
-            double theta = acos(R / sqrt(Q3));
-            roots[0] = -2 * Qsqrt * cos(theta / 3) - a / 3;
-            roots[1] = -2 * Qsqrt * cos((theta + 2 * M_PI) / 3) - a / 3;
-            roots[2] = -2 * Qsqrt * cos((theta - 2 * M_PI) / 3) - a / 3;
+            double theta = LM_ACOS(R / sqrt(Q3));
+            roots[0] = -2 * Qsqrt * LM_COS(theta / 3) - a / 3;
+            roots[1] = -2 * Qsqrt * LM_COS((theta + 2 * M_PI) / 3) - a / 3;
+            roots[2] = -2 * Qsqrt * LM_COS((theta - 2 * M_PI) / 3) - a / 3;
         } else {
             double sgn = (R > 0) ? 1.0 : -1.0;
-            double A = -sgn * pow(fabs(R) + sqrt(R2 - Q3), 1.0 / 3.0);
+            double A = -sgn * LM_POW(fabs(R) + sqrt(R2 - Q3), 1.0 / 3.0);
             double B = (fabs(A) < ROUND_EPS) ? 0.0 : Q / A;
             roots[0] = (A + B) - a / 3.0;
             if (fabs(A - B) < ROUND_EPS) roots[1] = roots[2] = -0.5 * (A + B) - a / 3.0;
@@ -1063,12 +1083,12 @@ static int update_impact_list_velocity(cco_solver* s, int head) {
             double sc = dot3(dx, w) / dot3(w, w);
             for (int i = 0; i < 3; ++i) xF[i] = sc * w[i];
             for (int i = 0; i < 3; ++i) xR[i] = dx[i] - xF[i];
-            double sw = sin(dt * mag_w) / mag_w;
+            double sw = LM_SIN(dt * mag_w) / mag_w;
             for (int i = 0; i < 3; ++i) tmpV[i] = sw * w[i];
             cross3(tmpV, xR, wxR);
         }
         for (int i = 0; i < 3; ++i) {
-            x_new[i] = x_cm[i] + dt * v_cm[i] + xF[i] + cos(dt * mag_w) * xR[i] + wxR[i];
+            x_new[i] = x_cm[i] + dt * v_cm[i] + xF[i] + LM_COS(dt * mag_w) * xR[i] + wxR[i];
             AV(p)[i] = (x_new[i] - XO(p)[i]) / dt;
             if (isnan(AV(p)[i])) return CCO_NAN;
         }

@@ -35,26 +35,47 @@ class ContactRec(C.Structure):
                 ("subtest", C.c_int), ("v", C.c_int * 4)]
 
 
+CR_SRC = os.path.join(HERE, "cc_oracle_crmath.cpp")
+CR_HDR = os.path.join(os.path.dirname(HERE), "collision_gb300", "csrc", "cc_crmath.cuh")
+CR_LIB_PATH = os.path.join(BUILD_DIR, "libcc_oracle_cr.so")
+
+
+def _fresh(lib: str, deps) -> bool:
+    return os.path.exists(lib) and os.path.getmtime(lib) >= max(os.path.getmtime(d) for d in deps)
+
+
 def build(force: bool = False) -> str:
-    """Compile the oracle with the host C compiler (seconds)."""
-    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= max(
-            os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "cc_oracle.h"))):
-        return LIB_PATH
+    """Compile the oracle with the host C compiler (seconds), and its
+    CCO_CRMATH build, whose acos/cos/sin/pow are correctly rounded."""
+    hdr = os.path.join(HERE, "cc_oracle.h")
     os.makedirs(BUILD_DIR, exist_ok=True)
-    tmp = LIB_PATH + f".tmp{os.getpid()}"
-    subprocess.check_call(["gcc", *CFLAGS, "-o", tmp, SRC, "-lm"])
-    os.replace(tmp, LIB_PATH)
+    if force or not _fresh(LIB_PATH, [SRC, hdr]):
+        tmp = LIB_PATH + f".tmp{os.getpid()}"
+        subprocess.check_call(["gcc", *CFLAGS, "-o", tmp, SRC, "-lm"])
+        os.replace(tmp, LIB_PATH)
+    if force or not _fresh(CR_LIB_PATH, [SRC, hdr, CR_SRC, CR_HDR]):
+        tmp = CR_LIB_PATH + f".tmp{os.getpid()}"
+        obj_c, obj_cpp = tmp + ".c.o", tmp + ".cpp.o"
+        flags = [f for f in CFLAGS if f != "-shared"]
+        subprocess.check_call(["gcc", *flags, "-DCCO_CRMATH", "-c", SRC, "-o", obj_c])
+        subprocess.check_call(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-c", CR_SRC, "-o", obj_cpp])
+        subprocess.check_call(["g++", "-shared", "-Wl,-Bsymbolic", "-o", tmp, obj_c, obj_cpp, "-lm"])
+        os.remove(obj_c)
+        os.remove(obj_cpp)
+        os.replace(tmp, CR_LIB_PATH)
     return LIB_PATH
 
 
-_LIB = None
+_LIBS = {}
 
 
-def load():
-    global _LIB
-    if _LIB is not None:
-        return _LIB
-    lib = C.CDLL(build())
+def load(crmath: bool = False):
+    """The oracle library; crmath: its build with correctly rounded
+    acos/cos/sin/pow."""
+    if crmath in _LIBS:
+        return _LIBS[crmath]
+    build()
+    lib = C.CDLL(CR_LIB_PATH if crmath else LIB_PATH)
     lib.cco_create.restype = C.c_void_p
     lib.cco_create.argtypes = [C.c_int, C.c_int, _ip, _ip, _dp, C.c_int, _ip, _dp, _up]
     lib.cco_destroy.argtypes = [C.c_void_p]
@@ -79,7 +100,7 @@ def load():
     lib.cco_set_body.argtypes = [C.c_void_p, C.c_int, C.c_double, _dp, _dp]
     lib.cco_get_body.restype = C.c_int
     lib.cco_get_body.argtypes = [C.c_void_p, C.c_int, _dp, _dp]
-    _LIB = lib
+    _LIBS[crmath] = lib
     return lib
 
 
@@ -94,8 +115,8 @@ class OracleSolver:
     """One CPU oracle solver: persistent trees and point state, like one
     reference CollisionSolver3d driven by the reference's host loop."""
 
-    def __init__(self, scene, record: int = REC_PAIRS | REC_CONTACTS):
-        self.lib = load()
+    def __init__(self, scene, record: int = REC_PAIRS | REC_CONTACTS, crmath: bool = False):
+        self.lib = load(crmath)
         s = scene
         self.scene = s
         self._keep = [np.ascontiguousarray(s.tris, dtype=np.int32),

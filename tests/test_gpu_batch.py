@@ -296,12 +296,12 @@ def test_ccd_recheck_after_resolved_steps(solver_cls):
 
 
 def test_zone_cap_stops_one_scene_only(solver_cls):
-    """Scene 186 of the 256-scene workload (an 80x80 cloth on a box) reaches
-    an impact-zone loop that the reference never leaves (the oracle runs
-    into its cap there too). In a batch, that scene stops at the cap and the
+    """Scene 186 of the 256-scene workload placed for free fall (an 80x80
+    cloth 0.10 above a box) reaches an impact-zone loop that the reference
+    never leaves (the oracle runs into its cap there too). In a batch, that scene stops at the cap and the
     others finish exactly as they do alone; disabled afterwards, its points
     pass through."""
-    stuck = scenes.batched(nscenes=256, seed=0)[186]
+    stuck = scenes.batched(nscenes=256, seed=0, approach_steps=None)[186]
     other = scenes.cloth_on_obstacle(20, "sphere", 0.2, 2.0, seed=3)
     mix = [stuck, other]
     b = solver_cls(0)

@@ -4,7 +4,10 @@ The golden fixtures were produced by the reference's own solver sources
 (tests/golden/make_golden.py). For every step the oracle is fed the same
 inputs and must return identical positions, velocities, collision flags,
 impact-zone partition, pass sequence, narrow-phase visit record (order,
-orientation and status of every call, by SHA-256) and hit list.
+orientation and status of every call, by SHA-256) and hit list. The
+oracle's build with correctly rounded acos/cos/sin/pow (CCO_CRMATH), which
+the GPU parity runs use to tell glibc's misroundings apart, must give the
+same on every golden step: none of them depends on such a misrounding.
 """
 import glob
 import hashlib
@@ -24,11 +27,12 @@ def test_golden_present():
     assert len(GOLDEN) >= 12
 
 
+@pytest.mark.parametrize("crmath", [False, True], ids=["libm", "crmath"])
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
-def test_oracle_matches_reference_golden(path):
+def test_oracle_matches_reference_golden(path, crmath):
     g = np.load(path)
     sc = scene_from_golden(g)
-    o = OracleSolver(sc, record=REC_PAIRS)
+    o = OracleSolver(sc, record=REC_PAIRS, crmath=crmath)
     nsteps = len(g["x"])
     for step in range(nsteps):
         out = o.step(*golden_inputs(g, sc, step))
