@@ -22,7 +22,10 @@ __device__ __forceinline__ double dec_double(unsigned long long e) {
     return __longlong_as_double((long long)u);
 }
 
-__global__ void k_bbox_init(unsigned long long* bb, int n6) {
+// dn (may be null): the boxes keep their last values when *dn is 0 (a pass
+// that computes no new leaf boxes).
+__global__ void k_bbox_init(unsigned long long* bb, int n6, const int* dn = nullptr) {
+    if (dn && *dn == 0) return;
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n6) bb[t] = (t % 6 < 3) ? ~0ull : 0ull;
 }
@@ -53,11 +56,10 @@ __device__ __forceinline__ void scene_bbox_accumulate(unsigned long long* bb, in
 }
 
 template <int MOVING>
-__global__ void k_leaf_boxes(const int* __restrict__ ev, const int* __restrict__ act, int n,
-                             const int* __restrict__ elem_scene, const SceneDev* __restrict__ scenes,
-                             const double4_32a* __restrict__ xo, const double4_32a* __restrict__ av,
-                             Box6* __restrict__ box, unsigned long long* bb) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void leaf_box(const int* __restrict__ ev, const int* __restrict__ act, int n, int k,
+                                         const int* __restrict__ elem_scene, const SceneDev* __restrict__ scenes,
+                                         const double4_32a* __restrict__ xo, const double4_32a* __restrict__ av,
+                                         Box6* __restrict__ box, unsigned long long* bb) {
     bool valid = k < n;
     int e = valid ? (act ? act[k] : k) : 0;
     int scene = valid ? elem_scene[e] : -1;
@@ -97,6 +99,18 @@ __global__ void k_leaf_boxes(const int* __restrict__ ev, const int* __restrict__
     }
     scene_bbox_accumulate(bb, scene, valid, lo, hi);
 }
+
+// dn (may be null): the element count in device memory; the grid strides.
+template <int MOVING>
+__global__ void k_leaf_boxes(const int* __restrict__ ev, const int* __restrict__ act, int n,
+                             const int* __restrict__ dn, const int* __restrict__ elem_scene,
+                             const SceneDev* __restrict__ scenes, const double4_32a* __restrict__ xo,
+                             const double4_32a* __restrict__ av, Box6* __restrict__ box, unsigned long long* bb) {
+    if (dn) n = *dn;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x)
+        leaf_box<MOVING>(ev, act, n, base + threadIdx.x, elem_scene, scenes, xo, av, box, bb);
+}
+
 
 // Union of n given boxes into bb (encoded as for k_leaf_boxes).
 __global__ void k_boxes_bbox(const Box6* __restrict__ box, int n, unsigned long long* bb) {
@@ -248,12 +262,9 @@ __device__ __forceinline__ Box32 node_union_cg(const BvhNode32* nd) {
 // the union of their own records), and with rn given the node's own box.
 // With sub given, only those leaves and the nodes above them up to their
 // scenes' roots (a node with one child in an idle scene sees one arrival).
-__global__ void k_refit(const Box6* __restrict__ box, const unsigned int* __restrict__ order, int n,
-                        const int* __restrict__ sub, int nsub, const int* __restrict__ parent, int* flags,
-                        BvhNode32* node, RopeNode* rn) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= (sub ? nsub : n)) return;
-    const int i = sub ? sub[k] : k;
+__device__ __forceinline__ void refit_from(const Box6* __restrict__ box, const unsigned int* __restrict__ order,
+                                           int n, int i, const int* __restrict__ parent, int* flags, BvhNode32* node,
+                                           RopeNode* rn) {
     if (i < 0 || i >= n) return;  // sub lists sorted leaves of scenes of this hierarchy
     int nd = parent[n - 1 + i];
     while (nd >= 0) {
@@ -275,6 +286,15 @@ __global__ void k_refit(const Box6* __restrict__ box, const unsigned int* __rest
         }
         nd = parent[nd];
     }
+}
+
+// dnsub (may be null): the count of sub in device memory; the grid strides.
+__global__ void k_refit(const Box6* __restrict__ box, const unsigned int* __restrict__ order, int n,
+                        const int* __restrict__ sub, int nsub, const int* __restrict__ dnsub,
+                        const int* __restrict__ parent, int* flags, BvhNode32* node, RopeNode* rn) {
+    const int m = sub ? (dnsub ? *dnsub : nsub) : n;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x)
+        refit_from(box, order, n, sub ? sub[k] : k, parent, flags, node, rn);
 }
 
 // The LBVH node whose leaves are exactly scene s's (keys carry the scene id
@@ -349,12 +369,9 @@ __device__ __forceinline__ void emit_pair(int a, int b, int2* pairs, int cap, Pa
 // share a point are dropped: every narrow-phase test of such a pair returns
 // false before any arithmetic (dcollid3d.cpp:493-497, 541-546, 578-582).
 // The leaf records of one pass (see LeafRec).
-__global__ void k_leaf_records(const Box6* __restrict__ box, const unsigned int* __restrict__ order, int n,
-                               const int* __restrict__ sub, int nsub, const int* __restrict__ ev, LeafRec* out,
-                               int ne_all, PassCounters* ctr, const int* __restrict__ rope, LeafBox32* out32) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= (sub ? nsub : n)) return;
-    const int j = sub ? sub[k] : k;
+__device__ __forceinline__ void leaf_record(const Box6* __restrict__ box, const unsigned int* __restrict__ order,
+                                            int n, int j, const int* __restrict__ ev, LeafRec* out, int ne_all,
+                                            PassCounters* ctr, const int* __restrict__ rope, LeafBox32* out32) {
     if (j < 0 || j >= n) {
         atomicOr(&ctr->err, kErrIndexLeaf);
         return;
@@ -391,6 +408,16 @@ __global__ void k_leaf_records(const Box6* __restrict__ box, const unsigned int*
     r.p[2] = ev[3 * e + 2];
     r.e = e;
     out[j] = r;
+}
+
+// dnsub (may be null): the count of sub in device memory; the grid strides.
+__global__ void k_leaf_records(const Box6* __restrict__ box, const unsigned int* __restrict__ order, int n,
+                               const int* __restrict__ sub, int nsub, const int* __restrict__ dnsub,
+                               const int* __restrict__ ev, LeafRec* out, int ne_all, PassCounters* ctr,
+                               const int* __restrict__ rope, LeafBox32* out32) {
+    const int m = sub ? (dnsub ? *dnsub : nsub) : n;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x)
+        leaf_record(box, order, n, sub ? sub[k] : k, ev, out, ne_all, ctr, rope, out32);
 }
 
 // The same pairs from a warp-cooperative traversal. The 32 lanes of a warp
@@ -495,14 +522,12 @@ __global__ void __launch_bounds__(kPacketWarps * 32) k_traverse_packet(
 }
 
 template <int DEPTH>
-__global__ void k_traverse(const Box6* __restrict__ box, const unsigned int* __restrict__ order, int n,
-                           const BvhNode32* __restrict__ node, const int* __restrict__ elem_scene,
-                           const SceneRun* __restrict__ run, const int* __restrict__ ev, int2* pairs, int cap,
-                           PassCounters* ctr, const Box6* __restrict__ box_static,
-                           const LeafRec* __restrict__ leaves, const int* __restrict__ sub, int nsub) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (sub ? nsub : n - 1)) return;
-    const int i = sub ? sub[t] : t;
+__device__ __forceinline__ void traverse_stack(const Box6* __restrict__ box, const unsigned int* __restrict__ order,
+                                               int n, const BvhNode32* __restrict__ node,
+                                               const int* __restrict__ elem_scene, const SceneRun* __restrict__ run,
+                                               const int* __restrict__ ev, int2* pairs, int cap, PassCounters* ctr,
+                                               const Box6* __restrict__ box_static,
+                                               const LeafRec* __restrict__ leaves, int i) {
     if (i >= n - 1) return;  // the last leaf has no leaf after it
     if (i < 0) {
         atomicOr(&ctr->err, kErrIndexLeaf);
@@ -599,6 +624,21 @@ __global__ void k_traverse(const Box6* __restrict__ box, const unsigned int* __r
     }
 }
 
+// One thread per query leaf (sub, or all leaves but the last); dnsub (may be
+// null): the count of sub in device memory, the grid striding over it.
+template <int DEPTH>
+__global__ void k_traverse(const Box6* __restrict__ box, const unsigned int* __restrict__ order, int n,
+                           const BvhNode32* __restrict__ node, const int* __restrict__ elem_scene,
+                           const SceneRun* __restrict__ run, const int* __restrict__ ev, int2* pairs, int cap,
+                           PassCounters* ctr, const Box6* __restrict__ box_static,
+                           const LeafRec* __restrict__ leaves, const int* __restrict__ sub, int nsub,
+                           const int* __restrict__ dnsub) {
+    const int m = sub ? (dnsub ? *dnsub : nsub) : n - 1;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < m; t += gridDim.x * blockDim.x)
+        traverse_stack<DEPTH>(box, order, n, node, elem_scene, run, ev, pairs, cap, ctr, box_static, leaves,
+                              sub ? sub[t] : t);
+}
+
 // The same pairs without a stack. Thread i starts at the rope of its own
 // leaf - the subtree right after leaf i in depth-first order - so the nodes
 // above leaf i are never visited and only leaves after i are reached; an
@@ -607,14 +647,11 @@ __global__ void k_traverse(const Box6* __restrict__ box, const unsigned int* __r
 // Every step moves forward in depth-first order, so a walk takes fewer than
 // 2n steps; a longer one, or an index outside its array, sets an error bit
 // and ends the thread.
-__global__ void k_traverse_rope(int n, const RopeNode* __restrict__ rn, const int* __restrict__ rope,
-                                const int* __restrict__ elem_scene, const SceneRun* __restrict__ run,
-                                const int* __restrict__ ev, int2* pairs, int cap, PassCounters* ctr,
-                                const Box6* __restrict__ box_static, const LeafRec* __restrict__ leaves,
-                                const int* __restrict__ sub, int nsub) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (sub ? nsub : n - 1)) return;
-    const int i = sub ? sub[t] : t;
+__device__ __forceinline__ void traverse_rope(int n, const RopeNode* __restrict__ rn, const int* __restrict__ rope,
+                                              const int* __restrict__ elem_scene, const SceneRun* __restrict__ run,
+                                              const int* __restrict__ ev, int2* pairs, int cap, PassCounters* ctr,
+                                              const Box6* __restrict__ box_static,
+                                              const LeafRec* __restrict__ leaves, int i) {
     if (i >= n - 1) return;  // the last leaf has no leaf after it
     if (i < 0) {
         atomicOr(&ctr->err, kErrIndexLeaf);
@@ -679,6 +716,18 @@ __global__ void k_traverse_rope(int n, const RopeNode* __restrict__ rn, const in
     }
 }
 
+// One thread per query leaf (sub, or all leaves but the last); dnsub (may be
+// null): the count of sub in device memory, the grid striding over it.
+__global__ void k_traverse_rope(int n, const RopeNode* __restrict__ rn, const int* __restrict__ rope,
+                                const int* __restrict__ elem_scene, const SceneRun* __restrict__ run,
+                                const int* __restrict__ ev, int2* pairs, int cap, PassCounters* ctr,
+                                const Box6* __restrict__ box_static, const LeafRec* __restrict__ leaves,
+                                const int* __restrict__ sub, int nsub, const int* __restrict__ dnsub) {
+    const int m = sub ? (dnsub ? *dnsub : nsub) : n - 1;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < m; t += gridDim.x * blockDim.x)
+        traverse_rope(n, rn, rope, elem_scene, run, ev, pairs, cap, ctr, box_static, leaves, sub ? sub[t] : t);
+}
+
 // The stackless walk with dynamic query fetch. The walks of neighbouring
 // queries differ in length, and with one thread per query a warp runs until
 // its longest walk ends while its other lanes idle. Here warps stay resident
@@ -691,8 +740,8 @@ __global__ void __launch_bounds__(128) k_traverse_rope_dyn(
     int n, const RopeNode* __restrict__ rn, const int* __restrict__ elem_scene, const SceneRun* __restrict__ run,
     const int* __restrict__ ev, int2* pairs, int cap, PassCounters* ctr, const Box6* __restrict__ box_static,
     const LeafRec* __restrict__ leaves, const LeafBox32* __restrict__ leaf32, const int* __restrict__ sub, int nsub,
-    int* qnext, int refill) {
-    const int nq = sub ? nsub : n - 1;
+    const int* __restrict__ dnsub, int* qnext, int refill) {
+    const int nq = sub ? (dnsub ? *dnsub : nsub) : n - 1;
     const unsigned lane_lt = (1u << (threadIdx.x & 31)) - 1u;
     int x = kRopeEnd, ei = -1, steps = 0;
     int pi0 = -1, pi1 = -1, pi2 = -1;
@@ -803,17 +852,23 @@ inline int nblk(int n, int t) { return (n + t - 1) / t; }
 
 }  // namespace
 
+// Grid of a kernel over at most n items whose count is in device memory:
+// strided, a few waves at most.
+inline int dev_grid(int n, int t) {
+    const int b = nblk(n, t);
+    return b < 152 * 8 ? b : 152 * 8;
+}
+
 void leaf_boxes(const int* ev, const int* act, int n, const int* elem_scene, const SceneDev* scenes, int nscenes,
                 const double4_32a* xo, const double4_32a* av, int moving, Box6* box, unsigned long long* bbox_enc,
-                cudaStream_t s) {
-    count_launch(), k_bbox_init<<<nblk(6 * nscenes, 256), 256, 0, s>>>(bbox_enc, 6 * nscenes);
+                cudaStream_t s, const int* dn) {
+    count_launch(), k_bbox_init<<<nblk(6 * nscenes, 256), 256, 0, s>>>(bbox_enc, 6 * nscenes, dn);
     if (n <= 0) return;
+    const int g = dn ? dev_grid(n, 256) : nblk(n, 256);
     if (moving)
-        count_launch(), k_leaf_boxes<1><<<nblk(n, 256), 256, 0, s>>>(ev, act, n, elem_scene, scenes, xo, av, box,
-                                                                     bbox_enc);
+        count_launch(), k_leaf_boxes<1><<<g, 256, 0, s>>>(ev, act, n, dn, elem_scene, scenes, xo, av, box, bbox_enc);
     else
-        count_launch(), k_leaf_boxes<0><<<nblk(n, 256), 256, 0, s>>>(ev, act, n, elem_scene, scenes, xo, av, box,
-                                                                     bbox_enc);
+        count_launch(), k_leaf_boxes<0><<<g, 256, 0, s>>>(ev, act, n, dn, elem_scene, scenes, xo, av, box, bbox_enc);
 }
 
 // Element / point k of the selection: scene j with off[j] <= k < off[j+1].
@@ -857,8 +912,8 @@ void bvh_build(const Box6* box, BvhBufs& b, cudaStream_t s) {
                                                               ropes ? b.rope : nullptr);
     if (ropes) count_launch(), k_ropes<<<nblk(n - 1, 256), 256, 0, s>>>(b.node, b.rope, n, b.rnode);
     cudaMemsetAsync(b.flags, 0, sizeof(int) * (size_t)(n - 1), s);
-    count_launch(), k_refit<<<nblk(n, 256), 256, 0, s>>>(box, b.order, n, nullptr, 0, b.parent, b.flags, b.node,
-                                                         ropes ? b.rnode : nullptr);
+    count_launch(), k_refit<<<nblk(n, 256), 256, 0, s>>>(box, b.order, n, nullptr, 0, nullptr, b.parent, b.flags,
+                                                         b.node, ropes ? b.rnode : nullptr);
     if (b.run)
         count_launch(), k_scene_roots<<<nblk(b.nscenes, 128), 128, 0, s>>>(b.scenes, b.run, b.nscenes, n, b.parent,
                                                                           b.range_lo, b.range_hi);
@@ -870,8 +925,9 @@ void bvh_refit(const Box6* box, BvhBufs& b, cudaStream_t s) {
     cudaMemsetAsync(b.flags, 0, sizeof(int) * (size_t)(n - 1), s);
     const int nleaf = b.sub ? b.nsub : n;
     if (nleaf > 0)
-        count_launch(), k_refit<<<nblk(nleaf, 256), 256, 0, s>>>(box, b.order, n, b.sub, b.nsub, b.parent, b.flags,
-                                                                 b.node, b.rnode && b.rope ? b.rnode : nullptr);
+        count_launch(), k_refit<<<b.sub && b.dnsub ? dev_grid(nleaf, 256) : nblk(nleaf, 256), 256, 0, s>>>(
+            box, b.order, n, b.sub, b.nsub, b.sub ? b.dnsub : nullptr, b.parent, b.flags, b.node,
+            b.rnode && b.rope ? b.rnode : nullptr);
     if (b.run)
         count_launch(), k_scene_roots<<<nblk(b.nscenes, 128), 128, 0, s>>>(b.scenes, b.run, b.nscenes, n, b.parent,
                                                                           b.range_lo, b.range_hi);
@@ -880,9 +936,10 @@ void bvh_refit(const Box6* box, BvhBufs& b, cudaStream_t s) {
 template <int DEPTH>
 void launch_stack_traverse(const Box6* box, const BvhBufs& b, int nq, int block, int2* pairs, int cap,
                            PassCounters* ctr, cudaStream_t s, const int* skip_shared_ev, const Box6* box_static) {
-    count_launch(), k_traverse<DEPTH><<<nblk(nq, block), block, 0, s>>>(box, b.order, b.n, b.node, b.elem_scene, b.run,
-                                                                      skip_shared_ev, pairs, cap, ctr, box_static,
-                                                                      b.leaf, b.sub, b.nsub);
+    const int g = b.sub && b.dnsub ? dev_grid(nq, block) : nblk(nq, block);
+    count_launch(), k_traverse<DEPTH><<<g, block, 0, s>>>(box, b.order, b.n, b.node, b.elem_scene, b.run,
+                                                        skip_shared_ev, pairs, cap, ctr, box_static, b.leaf, b.sub,
+                                                        b.nsub, b.sub ? b.dnsub : nullptr);
 }
 
 // Resident blocks of the dynamic-fetch traversal per SM, looked up once.
@@ -905,10 +962,10 @@ void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCoun
     const int nleaf = b.sub ? b.nsub : n, nq = b.sub ? b.nsub : n - 1;
     if (nq <= 0) return;
     const bool dyn = b.leaf && rope && b.rnode && b.rope && b.leaf32 && b.qnext && refill > 0;
+    const int* dnsub = b.sub ? b.dnsub : nullptr;
     if (b.leaf)
-        count_launch(), k_leaf_records<<<nblk(nleaf, 256), 256, 0, s>>>(box, b.order, n, b.sub, b.nsub, b.ev,
-                                                                        b.leaf, b.ne_all, ctr, b.rope,
-                                                                        dyn ? b.leaf32 : nullptr);
+        count_launch(), k_leaf_records<<<dnsub ? dev_grid(nleaf, 256) : nblk(nleaf, 256), 256, 0, s>>>(
+            box, b.order, n, b.sub, b.nsub, dnsub, b.ev, b.leaf, b.ne_all, ctr, b.rope, dyn ? b.leaf32 : nullptr);
     if (dyn) {
         static int num_sms = 0;
         if (!num_sms) {
@@ -922,11 +979,12 @@ void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCoun
         cudaMemsetAsync(b.qnext, 0, sizeof(int), s);
         count_launch(), k_traverse_rope_dyn<<<blocks, 128, 0, s>>>(n, b.rnode, b.elem_scene, b.run, skip_shared_ev,
                                                                    pairs, cap, ctr, box_static, b.leaf, b.leaf32,
-                                                                   b.sub, b.nsub, b.qnext, refill > 32 ? 32 : refill);
+                                                                   b.sub, b.nsub, dnsub, b.qnext,
+                                                                   refill > 32 ? 32 : refill);
     } else if (b.leaf && rope && b.rnode && b.rope) {
-        count_launch(), k_traverse_rope<<<nblk(nq, block), block, 0, s>>>(
+        count_launch(), k_traverse_rope<<<dnsub ? dev_grid(nq, block) : nblk(nq, block), block, 0, s>>>(
             n, b.rnode, b.rope, b.elem_scene, b.run, skip_shared_ev, pairs, cap, ctr, box_static, b.leaf, b.sub,
-            b.nsub);
+            b.nsub, dnsub);
     } else if (b.leaf && packet && !b.sub) {
         count_launch(), k_traverse_packet<<<nblk(n - 1, kPacketWarps * 32), kPacketWarps * 32, 0, s>>>(
             b.order, n, b.node, b.elem_scene, b.run, skip_shared_ev, pairs, cap, ctr, box_static, b.leaf);

@@ -61,11 +61,14 @@ enum ErrBits {
     kErrIndexNode = 256,
     kErrIndexLeaf = 512,
     kErrIndexElem = 1024,
+    // the pass stopped for the host (a tree to rebuild, buffers to grow):
+    // nothing of it is applied, and it runs again afterwards
+    kErrHost = 2048,
 };
 // Errors after which a pass's results are discarded (and the pass retried
 // with larger buffers, or the call fails): the impulses are not applied.
-constexpr int kErrRetry =
-    kErrPairOverflow | kErrStack | kErrContribOverflow | kErrRecordOverflow | kErrUnionOverflow | kErrSubOverflow;
+constexpr int kErrRetry = kErrPairOverflow | kErrStack | kErrContribOverflow | kErrRecordOverflow |
+                          kErrUnionOverflow | kErrSubOverflow | kErrHost;
 
 // Candidate pairs found on swept boxes carry this bit in .y when the two
 // elements' static boxes overlap too (the proximity pass's pairs).
@@ -130,6 +133,7 @@ struct SceneDev {
     int wb_final0, wb_final1;  // write-backs after its last level
     int enabled;          // 0: left out of resolve calls (candidates pass through)
     int strain_e0, strain_ne;  // its strain edges
+    int nt;               // triangles (its first nt elements)
 };
 
 // Per-pass state of a scene (written by the host before a pass, except
@@ -142,6 +146,42 @@ struct SceneRun {
     int root;   // the scene's subtree root in the LBVH (-1: fewer than 2 elements)
     int leaf0;  // first sorted leaf of the scene in this pass's LBVH (-1: not in it)
     int pad[3];
+};
+
+// Where a scene is in the pass sequence of resolveCollision
+// (dcollid.cpp:323-356) during one call.
+enum SeqState { kSeqDone = 0, kSeqProx, kSeqCcd, kSeqZone };
+
+// The pass sequence of one scene on the device (the device-resident
+// detection loop): state, CCD iteration, CCD and impact-zone passes run this
+// step, hasCollision, status (kOk or kIterCap), the scene's first sorted
+// leaf in the step's hierarchy, and the tree the host must rebuild
+// (0 none, 1 the proximity tree, 2 the collision tree).
+struct SceneCtl {
+    int state, niter, nccd, nzone;
+    int hcol, status, leafbase, rebuild;
+};
+
+// The device-resident detection loop's own state.
+enum LoopHost { kHostRebuild = 1, kHostRetry = 2, kHostFatal = 4 };
+enum LoopAcc {
+    kAccPasses, kAccCcd, kAccZone, kAccPairs, kAccVisits, kAccHits, kAccContacts, kAccSub, kAccMovingVisits,
+    kAccCr, kAccLeaves, kAccBroadPairs, kAccPathBytes, kAccZonePasses, kAccIters, kAccProxPairs, kNumAcc
+};
+struct LoopCtl {
+    int host;       // LoopHost bits: the loop stopped for the host
+    int err;        // the stopping pass's error bits
+    int pending;    // the current pass's modes are set: run it again as it is
+    int nact;       // scenes in the current pass
+    int nact_e;     // their elements
+    int nact_p;     // their points
+    int nbroad;     // elements the broad phase boxes and walks (0: pairs reused, or stopped)
+    int npts;       // points the pass's point kernels cover (0: stopped)
+    int any_zone;   // a scene of the pass is in impact-zone mode
+    int reuse;      // >= 0: the next pass takes this many pairs of the proximity pass
+    int reuse_n;    // pairs the current pass took (-1: none)
+    int zone_cap;   // impact-zone passes per scene and step
+    unsigned long long acc[kNumAcc];  // counters over the step's passes (LoopAcc)
 };
 
 struct PassCounters {

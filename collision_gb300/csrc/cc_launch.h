@@ -122,6 +122,9 @@ struct BvhBufs {
     // traversal then cover only those (walks never leave their scene)
     const int* sub;
     int nsub;
+    // optional: the count of sub in device memory (nsub is then its
+    // capacity), for passes whose scenes are chosen on the device
+    const int* dnsub;
 };
 
 // Leaf boxes of every element (static: x_old; moving: x_old and
@@ -129,9 +132,11 @@ struct BvhBufs {
 // each scene's union in bbox_enc[6*scene ..].
 // Only the n elements listed in act (null: elements 0..n-1) are boxed; box
 // is indexed by element id.
+// dn (may be null): the element count in device memory, n its capacity; a
+// count of 0 leaves the boxes and bbox_enc as they are.
 void leaf_boxes(const int* ev, const int* act, int n, const int* elem_scene, const SceneDev* scenes, int nscenes,
                 const double4_32a* xo, const double4_32a* av, int moving, Box6* box, unsigned long long* bbox_enc,
-                cudaStream_t s);
+                cudaStream_t s, const int* dn = nullptr);
 // The elements and points of the given scenes, in scene order:
 // elem_off / pt_off are the exclusive prefix sums of their counts.
 void expand_scenes(const int* scene_ids, const int* elem_off, const int* pt_off, int nsel, int n_elems, int n_pts,
@@ -215,7 +220,7 @@ void narrow_pass_split(const NarrowArgs& a, int moving, int max_pairs, cudaStrea
 // (moving passes) avgVel rounded to FP32.
 void point_boxes(const double4_32a* xo, const double4_32a* av, const int* vscene, const SceneDev* scenes,
                  const int* act_pts, int n, int moving, float4* lo, float4* hi, float4* p32, float4* v32,
-                 cudaStream_t s);
+                 cudaStream_t s, const int* dn = nullptr);
 
 // ------------------------------------------------------------- post-pass
 // Movable rigid bodies, all scenes' in one list. members / member_body: the
@@ -293,6 +298,24 @@ size_t zone_sort_temp_bytes(int cap);
 void zone_pass(const ZoneBufs& z, const PassCounters* ctr, const uint8_t* fixed, const int* act_pts, int n_pts,
                const int* dn_pts, const int* vscene, const SceneRun* run, const SceneDev* scenes, double4_32a* av,
                const double4_32a* xo, cudaStream_t s);
+
+// ------------------------------------------------ device detection loop
+// (cc_loop.cu) One pass of the loop: k_loop_plan picks each scene's mode and
+// lists the pass's scenes (sel) with their element and point offsets
+// (eoff, poff: nscenes + 1 each); loop_expand writes the pass's elements,
+// their sorted leaves in the step's hierarchy and points; tree_check flags
+// scenes whose tree `which` must be rebuilt on the host; loop_reset opens
+// the pass; pass_end closes it and, in the graph, decides whether the loop
+// goes on.
+void loop_plan(SceneCtl* ctl, SceneRun* run, const SceneDev* scenes, int nscenes, LoopCtl* L, int* sel, int* eoff,
+               int* poff, cudaGraphConditionalHandle h_zone, cudaStream_t s);
+void loop_expand(const int* sel, const int* eoff, const int* poff, const SceneDev* scenes, const SceneCtl* ctl,
+                 const LoopCtl* L, int cap, int* act_e, int* act_l, int* act_p, cudaStream_t s);
+void tree_check(const SceneRun* run, int nscenes, const unsigned long long* bbox_enc, const double* vol,
+                const int* built, int which, int* rebuild, LoopCtl* L, cudaStream_t s);
+void loop_reset(PassCounters* c, SceneRun* run, int nscenes, LoopCtl* L, cudaStream_t s);
+void pass_end(const PassCounters* c, SceneCtl* ctl, const SceneRun* run, int nscenes, LoopCtl* L, int combined,
+              bool in_graph, cudaGraphConditionalHandle h_loop, cudaStream_t s);
 
 // updateFinalForRG's device part: per body, the first point in element
 // order with has_collsn and its average velocity (into b.out).

@@ -332,12 +332,9 @@ __global__ void __launch_bounds__(128) k_subtests(NarrowArgs a) {
 // FP32 box of every point over the pass's time window, rounded outward:
 // [x_old] for proximity, [x_old, x_old + dt*avgVel] for CCD.
 template <bool MOVING>
-__global__ void k_point_boxes(const double4_32a* __restrict__ xo, const double4_32a* __restrict__ av,
-                              const int* __restrict__ vscene, const SceneDev* __restrict__ scenes,
-                              const int* __restrict__ act, int n, float4* lo, float4* hi, float4* p32, float4* v32) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    int p = act ? act[k] : k;
+__device__ __forceinline__ void point_box(const double4_32a* __restrict__ xo, const double4_32a* __restrict__ av,
+                                          const int* __restrict__ vscene, const SceneDev* __restrict__ scenes, int p,
+                                          float4* lo, float4* hi, float4* p32, float4* v32) {
     double dt = MOVING ? scenes[vscene[p]].p.dt : 0.0;
     double4_32a x = xo[p];
     double a[3] = {x.x, x.y, x.z}, b[3] = {x.x, x.y, x.z};
@@ -358,18 +355,31 @@ __global__ void k_point_boxes(const double4_32a* __restrict__ xo, const double4_
     }
 }
 
+// dn (may be null): the point count in device memory; the grid strides.
+template <bool MOVING>
+__global__ void k_point_boxes(const double4_32a* __restrict__ xo, const double4_32a* __restrict__ av,
+                              const int* __restrict__ vscene, const SceneDev* __restrict__ scenes,
+                              const int* __restrict__ act, int n, const int* __restrict__ dn, float4* lo, float4* hi,
+                              float4* p32, float4* v32) {
+    if (dn) n = *dn;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        point_box<MOVING>(xo, av, vscene, scenes, act ? act[k] : k, lo, hi, p32, v32);
+}
+
 }  // namespace
 
 void point_boxes(const double4_32a* xo, const double4_32a* av, const int* vscene, const SceneDev* scenes,
                  const int* act_pts, int n, int moving, float4* lo, float4* hi, float4* p32, float4* v32,
-                 cudaStream_t s) {
+                 cudaStream_t s, const int* dn) {
     if (n <= 0) return;
+    int g = (n + 255) / 256;
+    if (dn && g > 152 * 8) g = 152 * 8;
     if (moving)
-        count_launch(), k_point_boxes<true><<<(n + 255) / 256, 256, 0, s>>>(xo, av, vscene, scenes, act_pts, n, lo,
-                                                                            hi, p32, v32);
+        count_launch(), k_point_boxes<true><<<g, 256, 0, s>>>(xo, av, vscene, scenes, act_pts, n, dn, lo, hi, p32,
+                                                              v32);
     else
-        count_launch(), k_point_boxes<false><<<(n + 255) / 256, 256, 0, s>>>(xo, av, vscene, scenes, act_pts, n, lo,
-                                                                             hi, p32, v32);
+        count_launch(), k_point_boxes<false><<<g, 256, 0, s>>>(xo, av, vscene, scenes, act_pts, n, dn, lo, hi, p32,
+                                                               v32);
 }
 
 void narrow_pass(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s, int) {

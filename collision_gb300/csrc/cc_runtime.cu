@@ -34,13 +34,13 @@ namespace {
 
 // Stages timed by cc_set_profiling / cc_get_profile.
 enum Stage { kStInit, kStBoxes, kStBvh, kStTraverse, kStNarrowProx, kStNarrowCcd, kStApply, kStZone,
-             kStFinalize, kStStrain, kNumStages };
+             kStFinalize, kStStrain, kStLoop, kNumStages };
 const char* kStageNames[kNumStages] = {"init", "leaf_boxes", "bvh_build", "traverse", "narrow_prox",
-                                       "narrow_ccd", "apply", "zone", "finalize", "strain"};
+                                       "narrow_ccd", "apply", "zone", "finalize", "strain", "detect_loop"};
 
 constexpr int kMaxSceneElems = (1 << 22) - 1;  // leaf ranks fill 22 bits of a contribution key
 constexpr long long kMaxTotal = 1ll << 28;     // points and elements over all scenes
-constexpr int kNumCounters = 19;
+constexpr int kNumCounters = 22;
 constexpr int kErrIndex = kErrIndexNode | kErrIndexLeaf | kErrIndexElem;
 std::string index_error(int e) {
     std::string m = "broad phase met an index out of range:";
@@ -287,6 +287,53 @@ struct cc_solver {
         return f;
     }
 
+    // The device-resident detection loop (cc_loop.cu): every scene's pass
+    // sequence and the loop's state on the device, the passes after the
+    // proximity pass in one graph with a WHILE node
+    bool device_loop = true;
+    SceneCtl* d_ctl = nullptr;
+    SceneCtl* h_ctl = nullptr;  // pinned, nscenes
+    LoopCtl* d_loop = nullptr;
+    LoopCtl* h_loop = nullptr;  // pinned
+    int* d_lsel = nullptr;      // 3 * (nscenes + 1): the pass's scenes, element and point offsets
+    int* d_act_l = nullptr;     // the pass's sorted leaves
+    int* d_rebuild = nullptr;   // per scene: tree to rebuild on the host (0 none, 1 proximity, 2 collision)
+    int* h_rebuild = nullptr;   // pinned
+    double* d_tree_vol = nullptr;  // per scene: the volume both trees share
+    int* d_tree_built = nullptr;   // 2 * nscenes: tree built (proximity, then collision)
+    cudaStream_t cap_stream = nullptr, cap_stream2 = nullptr;  // graph capture only
+    cudaGraphExec_t loop_exec = nullptr;
+    bool loop_dirty = true;  // buffers or settings the graph holds have changed
+    int loop_key_n = -1;     // leaves of the hierarchy the graph was built for
+    long long loop_body_launches = 0, loop_zone_launches = 0;
+    void clear_loop_graph() {
+        if (loop_exec) cudaGraphExecDestroy(loop_exec);
+        loop_exec = nullptr;
+        loop_dirty = true;
+    }
+    bool use_device_loop() const { return device_loop && !record && vtk_dir.empty() && !overlap_tails; }
+    NarrowArgs narrow_args(int moving, bool combined) const {
+        NarrowArgs a{};
+        a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
+        a.vbody = d_vbody; a.body_mass = d_body_mass; a.body_slot0 = nv;
+        a.rank = d_rank[moving]; a.escene = d_escene; a.scenes = d_scenes; a.run = d_run;
+        a.pairs = d_pairs; a.contrib = d_contrib; a.contrib_cap = contrib_cap; a.ctr = d_ctr;
+        a.urec = d_urec; a.urec_cap = urec_cap;
+        a.rec = nullptr; a.rec_cap = 0;
+        a.pbox_lo = mode == 1 ? d_pbox_lo : nullptr;
+        a.pbox_hi = mode == 1 ? d_pbox_hi : nullptr;
+        a.p32 = d_p32; a.v32 = d_v32;
+        a.check = 0;
+        a.sub_pt = d_sub_pt; a.sub_ee = d_sub_ee; a.sub_cap = sub_cap;
+        a.pair_hit = d_pair_hit; a.pairq = d_pairq;
+        a.static_only = combined ? 1 : 0;
+        return a;
+    }
+    void prox_pass_async();
+    cc_status build_loop_graph(int n_hier);
+    cc_status device_passes(std::string& capped);
+    cc_status rebuild_flagged();
+
     // VTK dumps of every pass (empty: off)
     std::string vtk_dir;
     std::vector<int> vtk_count, h_ev;
@@ -386,6 +433,16 @@ struct cc_solver {
         dfree(d_rank[0]); dfree(d_rank[1]);
         dfree(d_rec); dfree(d_pbox_lo); dfree(d_pbox_hi); dfree(d_p32); dfree(d_v32);
         dfree(d_act_e); dfree(d_act_p); dfree(d_sel); dfree(d_dump); dfree(d_av_pre);
+        clear_loop_graph();
+        loop_key_n = -1;
+        dfree(d_ctl); dfree(d_loop); dfree(d_lsel); dfree(d_act_l); dfree(d_rebuild); dfree(d_tree_vol);
+        dfree(d_tree_built);
+        if (h_ctl) cudaFreeHost(h_ctl);
+        if (h_loop) cudaFreeHost(h_loop);
+        if (h_rebuild) cudaFreeHost(h_rebuild);
+        h_ctl = nullptr;
+        h_loop = nullptr;
+        h_rebuild = nullptr;
         dfree(d_vbody); dfree(d_body_mass); dfree(d_body_members); dfree(d_body_member_body);
         dfree(d_body_zone_off); dfree(d_body_visit); dfree(d_body_visit_off); dfree(d_body_acc);
         dfree(d_body_num); dfree(d_body_out);
@@ -415,6 +472,9 @@ struct cc_solver {
         ev_pass = ev_tail = nullptr;
         if (tail_stream) cudaStreamDestroy(tail_stream);
         tail_stream = nullptr;
+        if (cap_stream) cudaStreamDestroy(cap_stream);
+        if (cap_stream2) cudaStreamDestroy(cap_stream2);
+        cap_stream = cap_stream2 = nullptr;
         if (stream && own_stream) cudaStreamDestroy(stream);
         stream = nullptr;
     }
@@ -430,6 +490,7 @@ struct cc_solver {
     }
 
     cc_status grow_pairs(int cap) {
+        loop_dirty = true;
         dfree(d_pairs);
         dfree(d_pair_hit);
         dfree(d_pairq);
@@ -445,6 +506,7 @@ struct cc_solver {
         return CC_OK;
     }
     cc_status grow_contrib(int cap) {
+        loop_dirty = true;
         dfree(d_contrib);
         dfree(apply.idx);
         if (dalloc(&d_contrib, (size_t)cap) != cudaSuccess || dalloc(&apply.idx, (size_t)cap) != cudaSuccess)
@@ -454,6 +516,7 @@ struct cc_solver {
     }
 
     cc_status grow_subs(int cap) {
+        loop_dirty = true;
         dfree(d_sub_pt);
         dfree(d_sub_ee);
         if (dalloc(&d_sub_pt, (size_t)cap) != cudaSuccess || dalloc(&d_sub_ee, (size_t)cap) != cudaSuccess)
@@ -462,6 +525,7 @@ struct cc_solver {
         return CC_OK;
     }
     cc_status grow_unions(int cap) {
+        loop_dirty = true;
         dfree(d_urec);
         dfree(zb.keys);
         dfree(zb.vals);
@@ -787,6 +851,8 @@ struct cc_solver {
     cc_status check_ccd(const double* x_old, const double* x_new, long long* hits, int* scene_hits);
     cc_status autotune(double* best_ms);
     cc_status update_trees(int which, const Box6* boxes);
+    void sync_tree_state(const std::vector<int>& ids, int which);
+    std::vector<double> h_tree_vol_stage;
 };
 
 cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
@@ -827,7 +893,7 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
             sd.lo[d] = lo[d];
             sd.hi[d] = hi[d];
         }
-        sd.v0 = v0; sd.nv = snv; sd.e0 = e0; sd.ne = sne;
+        sd.v0 = v0; sd.nv = snv; sd.e0 = e0; sd.ne = sne; sd.nt = nt;
         sd.enabled = 1;
         for (int i = 0; i < snv; ++i) {
             vscene[v0 + i] = si;
@@ -1025,6 +1091,16 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     ok &= dalloc(&d_act_p, (size_t)nv) == cudaSuccess;
     ok &= dalloc(&d_sel, 3 * (size_t)n + 2) == cudaSuccess;
     ok &= cudaMallocHost(&h_sel, sizeof(int) * (3 * (size_t)n + 2)) == cudaSuccess;
+    ok &= dalloc(&d_ctl, (size_t)n) == cudaSuccess;
+    ok &= dalloc(&d_loop, 1) == cudaSuccess;
+    ok &= dalloc(&d_lsel, 3 * ((size_t)n + 1)) == cudaSuccess;
+    ok &= dalloc(&d_act_l, (size_t)ne) == cudaSuccess;
+    ok &= dalloc(&d_rebuild, (size_t)n) == cudaSuccess;
+    ok &= dalloc(&d_tree_vol, (size_t)n) == cudaSuccess;
+    ok &= dalloc(&d_tree_built, 2 * (size_t)n) == cudaSuccess;
+    ok &= cudaMallocHost(&h_ctl, sizeof(SceneCtl) * (size_t)n) == cudaSuccess;
+    ok &= cudaMallocHost(&h_loop, sizeof(LoopCtl)) == cudaSuccess;
+    ok &= cudaMallocHost(&h_rebuild, sizeof(int) * (size_t)n) == cudaSuccess;
     if (!ok) return fail(CC_NO_MEMORY, "device allocation failed");
     bvh.elem_scene = d_escene;
     bvh.ev = d_ev;
@@ -1064,8 +1140,15 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     }
     cudaMemsetAsync(d_av, 0, sizeof(double4_32a) * (size_t)(nv > 0 ? nv : 1), stream);
     cudaMemsetAsync(d_run, 0, sizeof(SceneRun) * (size_t)n, stream);
+    cudaMemsetAsync(d_rank[0], 0, sizeof(int) * (size_t)(ne > 0 ? ne : 1), stream);
+    cudaMemsetAsync(d_rank[1], 0, sizeof(int) * (size_t)(ne > 0 ? ne : 1), stream);
+    cudaMemsetAsync(d_lsel, 0, sizeof(int) * 3 * ((size_t)n + 1), stream);
+    cudaMemsetAsync(d_rebuild, 0, sizeof(int) * (size_t)n, stream);
+    cudaMemsetAsync(d_tree_vol, 0, sizeof(double) * (size_t)n, stream);
+    cudaMemsetAsync(d_tree_built, 0, sizeof(int) * 2 * (size_t)n, stream);
     h_boxes.resize((size_t)ne);
     h_rank.resize((size_t)ne);
+    h_tree_vol_stage.assign((size_t)n, 0.0);
     h_vscene.swap(vscene);
     h_ev = ev;
     vtk_count.assign((size_t)n, 0);
@@ -1181,6 +1264,337 @@ cc_status cc_solver::update_trees(int which, const Box6* boxes) {
         cudaMemcpyAsync(d_rank[which] + scenes[s].e0, h_rank.data() + scenes[s].e0, sizeof(int) * (size_t)scenes[s].ne,
                         cudaMemcpyHostToDevice, stream);
     counters[8] += (long long)todo.size();
+    sync_tree_state(todo, which);
+    return CC_OK;
+}
+
+// The device copy of the trees' shared volume and built flags, for the
+// scenes whose tree `which` was just built (the device loop's rebuild test
+// reads them).
+void cc_solver::sync_tree_state(const std::vector<int>& ids, int which) {
+    for (int s : ids) {
+        h_tree_vol_stage[s] = scenes[s].volume;
+        cudaMemcpyAsync(d_tree_vol + s, &h_tree_vol_stage[s], sizeof(double), cudaMemcpyHostToDevice, stream);
+        cudaMemsetAsync(d_tree_built + (size_t)which * nscenes + s, 0x01, 1, stream);
+    }
+    // the staging values must not change before the copies have run
+    cudaStreamSynchronize(stream);
+}
+
+// The trees the device loop flagged (d_rebuild, read into h_rebuild): the
+// reference's insertion order emulated on host threads for those scenes,
+// from the boxes of the pass that flagged them, and the new ranks, volumes
+// and built flags uploaded.
+cc_status cc_solver::rebuild_flagged() {
+    std::vector<int> todo[2];
+    for (int s = 0; s < nscenes; ++s)
+        if (h_rebuild[s] == 1 || h_rebuild[s] == 2) todo[h_rebuild[s] - 1].push_back(s);
+    for (int which = 0; which < 2; ++which) {
+        std::vector<int>& ids = todo[which];
+        if (ids.empty()) continue;
+        const Box6* boxes = (which == 0 && combined_broad) ? d_box_st : d_box;
+        for (int s : ids)
+            cudaMemcpyAsync(h_boxes.data() + scenes[s].e0, boxes + scenes[s].e0, sizeof(Box6) * (size_t)scenes[s].ne,
+                            cudaMemcpyDeviceToHost, stream);
+        if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("leaf boxes to host");
+        std::sort(ids.begin(), ids.end(), [&](int a, int b) { return scenes[a].ne > scenes[b].ne; });
+        int threads = host_threads > 0 ? host_threads : (int)std::thread::hardware_concurrency();
+        if (threads <= 0) threads = 1;
+        parallel_for((int)ids.size(), threads, [&](int i) {
+            SceneHost& sh = scenes[ids[i]];
+            sh.volume = sh.tree[which].build(h_boxes.data() + sh.e0, sh.ne);
+            sh.tree[which].ranks(h_rank.data() + sh.e0);
+        });
+        for (int s : ids)
+            cudaMemcpyAsync(d_rank[which] + scenes[s].e0, h_rank.data() + scenes[s].e0,
+                            sizeof(int) * (size_t)scenes[s].ne, cudaMemcpyHostToDevice, stream);
+        counters[8] += (long long)ids.size();
+        sync_tree_state(ids, which);
+    }
+    cudaMemsetAsync(d_rebuild, 0, sizeof(int) * (size_t)nscenes, stream);
+    return cuda_check("tree rebuild");
+}
+
+// The proximity pass of a step in the device-loop form: the same work as
+// detect_pass(0), launched without waiting for any of it. Whether the
+// proximity tree must be built or rebuilt is tested on the device
+// (tree_check); if so, nothing of the pass is applied and the host finds out
+// after the loop.
+void cc_solver::prox_pass_async() {
+    cudaMemcpyAsync(d_run, h_run, sizeof(SceneRun) * (size_t)nscenes, cudaMemcpyHostToDevice, stream);
+    const bool combined = combined_broad;
+    prof(kStBoxes, true);
+    leaf_boxes(d_ev, bvh.act, bvh.n, d_escene, d_scenes, nscenes, d_xo, d_av, 0, combined ? d_box_st : d_box,
+               bvh.bbox_enc, stream);
+    tree_check(d_run, nscenes, bvh.bbox_enc, d_tree_vol, d_tree_built, 0, d_rebuild, d_loop, stream);
+    if (combined)
+        leaf_boxes(d_ev, bvh.act, bvh.n, d_escene, d_scenes, nscenes, d_xo, d_av, 1, d_box, bvh.bbox_enc, stream);
+    prof(kStBoxes, false);
+    prof(kStBvh, true);
+    bvh_build(d_box, bvh, stream);
+    bvh_this_step = true;
+    bvh_set = cur_set;
+    full_this_step = bvh.act == nullptr;
+    if (mode == 1)
+        point_boxes(d_xo, d_av, d_vscene, d_scenes, bvh.act ? d_act_p : nullptr, n_act_p, 0, d_pbox_lo, d_pbox_hi,
+                    d_p32, d_v32, stream);
+    prof(kStBvh, false);
+    loop_reset(d_ctr, d_run, nscenes, d_loop, stream);
+    prof(kStTraverse, true);
+    bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, d_ev, tune.traverse_block, combined ? d_box_st : nullptr,
+              tune.packet_traverse, tune.rope_traverse, tune.traverse_refill, tune.stack_depth);
+    prof(kStTraverse, false);
+    prof(kStNarrowProx, true);
+    const NarrowArgs a = narrow_args(0, combined);
+    if (mode == 1 && split_narrow)
+        narrow_pass_split(a, 0, pair_cap, stream, tune.narrow_block, false);
+    else
+        narrow_pass(a, 0, pair_cap, stream, tune.narrow_block);
+    prof(kStNarrowProx, false);
+    prof(kStApply, true);
+    apply_contribs(d_contrib, d_ctr, contrib_cap, nv, d_av, d_hc, apply, stream, nullptr,
+                   bodies.empty() ? nullptr : &body_bufs);
+    if (!bodies.empty())  // updateImpactZoneVelocityForRG (dcollid.cpp:744-745)
+        zone_solve(d_body_members, d_body_zone_off, (int)bodies.size(), d_fixed, d_xo, d_av, d_vscene, d_scenes, d_ctr,
+                   stream, d_run);
+    prof(kStApply, false);
+    pass_end(d_ctr, d_ctl, d_run, nscenes, d_loop, (combined && bodies.empty()) ? 1 : 0, false, 0, stream);
+}
+
+// The graph of the passes after the proximity pass: a WHILE node whose body
+// is one detection pass over the scenes that still have one (planned on the
+// device), with the impact-zone stage behind an IF node, and the loop's
+// condition set by the pass's last kernel. Built for the hierarchy of
+// n_hier leaves that the step's proximity pass builds, and again whenever a
+// buffer or a setting it holds changes.
+cc_status cc_solver::build_loop_graph(int n_hier) {
+    clear_loop_graph();
+    if (!cap_stream && (cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking) != cudaSuccess ||
+                        cudaStreamCreateWithFlags(&cap_stream2, cudaStreamNonBlocking) != cudaSuccess))
+        return cuda_check("capture streams");
+    cudaGraph_t g = nullptr;
+    if (cudaGraphCreate(&g, 0) != cudaSuccess) return cuda_check("loop graph");
+    cudaGraphConditionalHandle h_loop_c, h_zone;
+    cudaGraphNodeParams wp = {};
+    cudaGraphNode_t wnode;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h_loop_c, g, 1, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess) {
+        wp.type = cudaGraphNodeTypeConditional;
+        wp.conditional.handle = h_loop_c;
+        wp.conditional.type = cudaGraphCondTypeWhile;
+        wp.conditional.size = 1;
+        e = cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &wp);
+    }
+    cudaGraph_t body = e == cudaSuccess ? wp.conditional.phGraph_out[0] : nullptr;
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h_zone, body, 0, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess)
+        e = cudaStreamBeginCaptureToGraph(cap_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return fail(CC_CUDA_ERROR, std::string("loop graph: ") + cudaGetErrorString(e));
+    }
+    const long long l0 = g_kernel_launches;
+    cudaStream_t cs = cap_stream;
+    int* sel = d_lsel;
+    int* eoff = d_lsel + (nscenes + 1);
+    int* poff = d_lsel + 2 * (nscenes + 1);
+    BvhBufs lb = bvh;  // the step's hierarchy, over the pass's scenes' leaves
+    lb.n = n_hier;
+    lb.act = nullptr;
+    lb.sub = d_act_l;
+    lb.nsub = ne;
+    lb.dnsub = &d_loop->nbroad;
+    loop_plan(d_ctl, d_run, d_scenes, nscenes, d_loop, sel, eoff, poff, h_zone, cs);
+    loop_expand(sel, eoff, poff, d_scenes, d_ctl, d_loop, ne + nv, d_act_e, d_act_l, d_act_p, cs);
+    leaf_boxes(d_ev, d_act_e, ne, d_escene, d_scenes, nscenes, d_xo, d_av, 1, d_box, bvh.bbox_enc, cs,
+               &d_loop->nbroad);
+    tree_check(d_run, nscenes, bvh.bbox_enc, d_tree_vol, d_tree_built + nscenes, 1, d_rebuild, d_loop, cs);
+    loop_reset(d_ctr, d_run, nscenes, d_loop, cs);
+    bvh_refit(d_box, lb, cs);
+    if (mode == 1)
+        point_boxes(d_xo, d_av, d_vscene, d_scenes, d_act_p, nv, 1, d_pbox_lo, d_pbox_hi, d_p32, d_v32, cs,
+                    &d_loop->npts);
+    bvh_pairs(d_box, lb, d_pairs, pair_cap, d_ctr, cs, d_ev, tune.traverse_block, nullptr, false, tune.rope_traverse,
+              tune.traverse_refill, tune.stack_depth);
+    const NarrowArgs a = narrow_args(1, false);
+    if (mode == 1 && split_narrow)
+        narrow_pass_split(a, 1, pair_cap, cs, tune.narrow_block, true);
+    else
+        narrow_pass(a, 1, pair_cap, cs, tune.narrow_block);
+    apply_contribs(d_contrib, d_ctr, contrib_cap, nv, d_av, d_hc, apply, cs, nullptr,
+                   bodies.empty() ? nullptr : &body_bufs);
+    if (!bodies.empty())
+        zone_solve(d_body_members, d_body_zone_off, (int)bodies.size(), d_fixed, d_xo, d_av, d_vscene, d_scenes, d_ctr,
+                   cs, d_run);
+    const long long l1 = g_kernel_launches;
+    // the impact-zone stage, only in passes with a scene in that mode
+    cudaStreamCaptureStatus cst;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    cudaGraphNodeParams ip = {};
+    cudaGraphNode_t inode;
+    e = cudaStreamGetCaptureInfo(cs, &cst, nullptr, &cg, &deps, nullptr, &ndeps);
+    if (e == cudaSuccess) {
+        ip.type = cudaGraphNodeTypeConditional;
+        ip.conditional.handle = h_zone;
+        ip.conditional.type = cudaGraphCondTypeIf;
+        ip.conditional.size = 1;
+        e = cudaGraphAddNode(&inode, cg, deps, nullptr, ndeps, &ip);
+    }
+    if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(cs, &inode, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e == cudaSuccess)
+        e = cudaStreamBeginCaptureToGraph(cap_stream2, ip.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        zone_pass(zb, d_ctr, d_fixed, d_act_p, nv, &d_loop->npts, d_vscene, d_run, d_scenes, d_av, d_xo, cap_stream2);
+        cudaGraph_t zg = nullptr;
+        e = cudaStreamEndCapture(cap_stream2, &zg);
+    }
+    const long long l2 = g_kernel_launches;
+    pass_end(d_ctr, d_ctl, d_run, nscenes, d_loop, 0, true, h_loop_c, cs);
+    cudaGraph_t bg = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(cs, &bg);
+    loop_body_launches = (l1 - l0) + (g_kernel_launches - l2);
+    loop_zone_launches = l2 - l1;
+    g_kernel_launches = l0;
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&loop_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        loop_exec = nullptr;
+        cudaGetLastError();
+        return fail(CC_CUDA_ERROR, std::string("loop graph: ") + cudaGetErrorString(e));
+    }
+    loop_dirty = false;
+    loop_key_n = n_hier;
+    return CC_OK;
+}
+
+// All detection passes of a step in the device-loop form: the proximity
+// pass, then the loop graph, then one synchronisation. When the device asks
+// for the host (a tree to rebuild, a buffer to grow), the host does that and
+// the stopped pass runs again (the proximity pass and the loop, or the loop
+// alone). Fills each scene's pass kinds, hasCollision and status.
+cc_status cc_solver::device_passes(std::string& capped) {
+    int nact = 0;
+    for (int s = 0; s < nscenes; ++s) {
+        SceneHost& sh = scenes[s];
+        const bool on = sh.ne > 0 && sh.enabled;
+        h_ctl[s] = SceneCtl{on ? kSeqProx : kSeqDone, 0, 0, 0, 0, 0, -1, 0};
+        h_run[s] = SceneRun{on ? kSceneProx : kSceneIdle, 0, 0, -1, -1, {0, 0, 0}};
+        if (!on) continue;
+        ++nact;
+        counters[0]++;
+        counters[18] += 72ll * sh.nv + 12ll * sh.nt + 8ll * (sh.ne - sh.nt) + 48ll * (2ll * sh.ne - 1);
+    }
+    if (nact == 0) return CC_OK;
+    select_active();
+    for (int s = 0; s < nscenes; ++s) h_ctl[s].leafbase = h_run[s].leaf0;
+    const int n_hier = bvh.n;
+    std::memset(h_loop, 0, sizeof(LoopCtl));
+    h_loop->nact = nact;
+    h_loop->nact_e = bvh.n;
+    h_loop->nact_p = n_act_p;
+    h_loop->nbroad = bvh.n;
+    h_loop->npts = n_act_p;
+    h_loop->reuse = -1;
+    h_loop->reuse_n = -1;
+    h_loop->zone_cap = zone_cap;
+    const LoopCtl loop_init = *h_loop;
+    cudaMemcpyAsync(d_ctl, h_ctl, sizeof(SceneCtl) * (size_t)nscenes, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(d_loop, h_loop, sizeof(LoopCtl), cudaMemcpyHostToDevice, stream);
+    bool need_prox = true;
+    long long graph_runs = 0;
+    for (int round = 0;; ++round) {
+        if (round >= 64) return fail(CC_PAIR_OVERFLOW, "the detection loop kept stopping for the host");
+        if (need_prox) prox_pass_async();
+        if (loop_dirty || !loop_exec || loop_key_n != n_hier) {
+            cc_status st = build_loop_graph(n_hier);
+            if (st) return st;
+        }
+        prof(kStLoop, true);
+        if (cudaGraphLaunch(loop_exec, stream) != cudaSuccess) return cuda_check("loop graph launch");
+        prof(kStLoop, false);
+        ++graph_runs;
+        cudaMemcpyAsync(h_loop, d_loop, sizeof(LoopCtl), cudaMemcpyDeviceToHost, stream);
+        cudaMemcpyAsync(h_ctl, d_ctl, sizeof(SceneCtl) * (size_t)nscenes, cudaMemcpyDeviceToHost, stream);
+        cudaMemcpyAsync(h_rebuild, d_rebuild, sizeof(int) * (size_t)nscenes, cudaMemcpyDeviceToHost, stream);
+        cudaMemcpyAsync(h_ctr, d_ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, stream);
+        if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("detection loop");
+        const int host = h_loop->host;
+        if (!host) break;
+        // the proximity pass stopped if no pass has completed yet
+        const bool in_prox = h_loop->acc[kAccIters] == 0;
+        const int err = h_loop->err;
+        if (host & kHostFatal) {
+            if (err & kErrNan) return fail(CC_NAN_DETECTED, "non-finite velocity or normal (the reference exits here)");
+            return fail(CC_CUDA_ERROR, index_error(err));
+        }
+        if (host & kHostRebuild) {
+            cc_status st = rebuild_flagged();
+            if (st) return st;
+        }
+        if (host & kHostRetry) {
+            cc_status st = CC_OK;
+            if (err & kErrStack) {
+                if (tune.stack_depth >= kTraversalStack)
+                    return fail(CC_STACK_OVERFLOW, "BVH traversal stack overflow");
+                tune.stack_depth = kTraversalStack;  // a tuned shallower stack was too shallow here
+                loop_dirty = true;
+            }
+            if (!st && (err & kErrPairOverflow)) st = grow_pairs(2 * h_ctr->npairs + 1024);
+            if (!st && (err & kErrContribOverflow)) st = grow_contrib(2 * h_ctr->ncontrib + 1024);
+            if (!st && (err & kErrSubOverflow)) st = grow_subs(2 * std::max(h_ctr->nsub_pt, h_ctr->nsub_ee) + 1024);
+            if (!st && (err & kErrUnionOverflow)) st = grow_unions(2 * h_ctr->nunion + 1024);
+            if (st) return st;
+        }
+        // the stopped pass runs again: the proximity pass from the start (no
+        // pass has counted anything yet), a later pass with its modes as they
+        // are (pending)
+        if (in_prox) {
+            cudaMemcpy(d_loop, &loop_init, sizeof(LoopCtl), cudaMemcpyHostToDevice);
+        } else {
+            cudaMemsetAsync(&d_loop->host, 0, sizeof(int), stream);
+            cudaMemsetAsync(&d_loop->err, 0, sizeof(int), stream);
+        }
+        need_prox = in_prox;
+    }
+    // the passes' counters (the proximity pass's scene-pass counts are above)
+    const unsigned long long* a = h_loop->acc;
+    counters[0] += (long long)a[kAccPasses];
+    counters[1] += (long long)a[kAccCcd];
+    counters[2] += (long long)a[kAccZone];
+    counters[3] += (long long)a[kAccPairs];
+    counters[4] += (long long)a[kAccVisits];
+    counters[5] += (long long)a[kAccHits];
+    counters[6] += (long long)a[kAccContacts];
+    counters[12] += (long long)a[kAccSub];
+    counters[13] += (long long)a[kAccMovingVisits];
+    counters[15] += (long long)a[kAccCr];
+    counters[16] += (long long)a[kAccLeaves];
+    counters[17] += (long long)a[kAccBroadPairs];
+    counters[18] += (long long)a[kAccPathBytes];
+    counters[19] += n_hier;
+    counters[20] += (long long)a[kAccProxPairs];
+    const long long loop_iters = (long long)a[kAccIters] - 1;
+    counters[21] += loop_iters;
+    count_launch((int)(loop_body_launches * (loop_iters + graph_runs) + loop_zone_launches * (long long)a[kAccZonePasses]));
+    for (int s = 0; s < nscenes; ++s) {
+        SceneHost& sh = scenes[s];
+        const SceneCtl& c = h_ctl[s];
+        if (!(sh.ne > 0 && sh.enabled)) continue;
+        sh.pass_kinds.push_back(kPassProx);
+        for (int i = 0; i < c.nccd; ++i) sh.pass_kinds.push_back(kPassCcd);
+        for (int i = 0; i < c.nzone; ++i) sh.pass_kinds.push_back(kPassZone);
+        sh.npass = (int)sh.pass_kinds.size();
+        sh.hcol = c.hcol;
+        sh.state = kHsDone;
+        if (c.status == kIterCap) {
+            sh.status = CC_ITER_CAP;
+            capped += (capped.empty() ? "" : " ") + std::to_string(s);
+        }
+    }
     return CC_OK;
 }
 
@@ -1248,7 +1662,10 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
                       tune.traverse_block, combined ? d_box_st : nullptr, tune.packet_traverse, tune.rope_traverse,
                       tune.traverse_refill, tune.stack_depth);
             prof(kStTraverse, false);
-            if (attempt == 0) counters[16] += bvh.n;
+            if (attempt == 0) {
+                counters[16] += bvh.n;
+                counters[19] += bvh.n;
+            }
         }
         NarrowArgs a;
         a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
@@ -1343,7 +1760,10 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
     counters[12] += h_ctr->nsub;
     if (moving) counters[13] += h_ctr->nvisits;
     counters[15] += h_ctr->ncr;
-    if (!reuse) counters[17] += h_ctr->npairs;
+    if (!reuse) {
+        counters[17] += h_ctr->npairs;
+        counters[20] += h_ctr->npairs;
+    }
     if (record && h_ctr->nrec > 0) {
         size_t base = visits.size();
         visits.resize(base + (size_t)h_ctr->nrec);
@@ -1411,7 +1831,11 @@ cc_status cc_solver::resolve_impl(const double* x_old, const double* x_cand, dou
     full_this_step = false;
     reuse_pairs = false;
     prof(kStInit, false);
-    for (bool first = true;; first = false) {
+    if (use_device_loop()) {
+        cc_status st = device_passes(capped);
+        if (st) return st;
+    }
+    for (bool first = true; !use_device_loop(); first = false) {
         bool any = false, any_zone = false;
         for (int s = 0; s < nscenes; ++s) {
             SceneHost& sh = scenes[s];
@@ -1926,6 +2350,7 @@ cc_status cc_autotune(cc_solver* s, double* best_ms) {
 
 cc_status cc_set_tuning(cc_solver* s, int knob, int value) {
     if (!s) return CC_BAD_INPUT;
+    s->loop_dirty = true;
     switch (knob) {
         case CC_TUNE_SPLIT_NARROW:
             s->split_narrow = value != 0;
@@ -1953,6 +2378,9 @@ cc_status cc_set_tuning(cc_solver* s, int knob, int value) {
             return CC_OK;
         case CC_TUNE_SUBSET_REFIT:
             s->subset_refit = value != 0;
+            return CC_OK;
+        case CC_TUNE_DEVICE_LOOP:
+            s->device_loop = value != 0;
             return CC_OK;
         case CC_TUNE_TRAVERSE_REFILL:
             if (value < 0 || value > 32) return CC_BAD_INPUT;
@@ -1997,6 +2425,7 @@ int cc_get_tuning(cc_solver* s, int knob) {
         case CC_TUNE_ROPE_TRAVERSE: return s->tune.rope_traverse ? 1 : 0;
         case CC_TUNE_SUBSET_REFIT: return s->subset_refit ? 1 : 0;
         case CC_TUNE_TRAVERSE_REFILL: return s->tune.traverse_refill;
+        case CC_TUNE_DEVICE_LOOP: return s->device_loop ? 1 : 0;
         case CC_TUNE_STACK_DEPTH: return s->tune.stack_depth;
         case CC_TUNE_PAIR_CAPACITY: return s->pair_cap;
         default: return -1;
@@ -2203,6 +2632,7 @@ cc_status cc_set_strain_window(cc_solver* s, int on) {
 cc_status cc_set_mode(cc_solver* s, int mode) {
     if (!s || mode < 0 || mode > 1) return CC_BAD_INPUT;
     s->mode = mode;
+    s->loop_dirty = true;
     return CC_OK;
 }
 

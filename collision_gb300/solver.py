@@ -185,7 +185,8 @@ class CollisionSolver3d:
 
     TUNE_SPLIT_NARROW, TUNE_TRAVERSE_BLOCK, TUNE_NARROW_BLOCK, TUNE_STRAIN_BLOCK, TUNE_TAIL_GRAPH = 0, 1, 2, 3, 4
     TUNE_COMBINED_BROAD, TUNE_STRAIN_WARP, TUNE_PACKET_TRAVERSE, TUNE_STRAIN_ROLES, TUNE_TAIL_OVERLAP = 5, 6, 7, 8, 9
-    TUNE_ROPE_TRAVERSE, TUNE_SUBSET_REFIT = 10, 11
+    TUNE_ROPE_TRAVERSE, TUNE_SUBSET_REFIT, TUNE_TRAVERSE_REFILL, TUNE_STACK_DEPTH, TUNE_PAIR_CAPACITY = 10, 11, 12, 13, 14
+    TUNE_DEVICE_LOOP = 15
 
     def setTuning(self, knob: int, value: int):
         """Launch shapes and the two-stage narrow phase; none changes results."""
@@ -201,6 +202,9 @@ class CollisionSolver3d:
         self._check(self._lib.cc_autotune(self._h, C.byref(ms)))
         return {"packet_traverse": self.getTuning(self.TUNE_PACKET_TRAVERSE),
                 "rope_traverse": self.getTuning(self.TUNE_ROPE_TRAVERSE),
+                "traverse_refill": self.getTuning(self.TUNE_TRAVERSE_REFILL),
+                "stack_depth": self.getTuning(self.TUNE_STACK_DEPTH),
+                "pair_capacity": self.getTuning(self.TUNE_PAIR_CAPACITY),
                 "traverse_block": self.getTuning(self.TUNE_TRAVERSE_BLOCK),
                 "split_narrow": self.getTuning(self.TUNE_SPLIT_NARROW),
                 "narrow_block": self.getTuning(self.TUNE_NARROW_BLOCK), "pass_ms": ms.value}
@@ -342,7 +346,7 @@ class CollisionSolver3d:
     COUNTER_NAMES = ("passes", "ccd_passes", "zone_passes", "candidate_pairs", "visits", "hit_pairs",
                      "contacts", "strain_passes", "tree_builds", "kernel_launches", "strain_averaged",
                      "strain_exact", "fp64_subtests", "moving_visits", "strain_bytes", "cr_roots", "broad_leaves",
-                     "broad_pairs", "path_bytes")
+                     "broad_pairs", "path_bytes", "timed_traverse_leaves", "timed_traverse_pairs", "loop_passes")
 
     def counters(self) -> dict:
         n_all = len(self.COUNTER_NAMES)

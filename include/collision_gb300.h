@@ -257,6 +257,14 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
  *                           default 8 per element + 4096, grown on overflow
  *                           and by cc_autotune to a timed pass's need plus a
  *                           quarter)
+ *   CC_TUNE_DEVICE_LOOP     1 (default): after the proximity pass, every
+ *                           detection pass of a step runs in one CUDA graph
+ *                           (a WHILE node over one pass, the impact-zone
+ *                           stage behind an IF node) with each scene's pass
+ *                           sequence on the device; the host steps in only to
+ *                           rebuild a reference tree or grow a buffer. Not
+ *                           with recording or VTK dumps, which take the host
+ *                           loop. 0: the host runs every pass. Same results
  * cc_get_tuning returns the current value, or -1 for an unknown knob. */
 enum {
     CC_TUNE_SPLIT_NARROW = 0,
@@ -273,7 +281,8 @@ enum {
     CC_TUNE_SUBSET_REFIT = 11,
     CC_TUNE_TRAVERSE_REFILL = 12,
     CC_TUNE_STACK_DEPTH = 13,
-    CC_TUNE_PAIR_CAPACITY = 14
+    CC_TUNE_PAIR_CAPACITY = 14,
+    CC_TUNE_DEVICE_LOOP = 15
 };
 cc_status cc_set_tuning(cc_solver* s, int knob, int value);
 int cc_get_tuning(cc_solver* s, int knob);
@@ -324,7 +333,11 @@ cc_status cc_set_strain_window(cc_solver* s, int on);
  * algorithmic bytes of the strain sweeps, coplanarity cubics whose roots
  * were formed again with correctly rounded functions, leaves traversed by
  * the broad phase (summed over its traversals), candidate pairs those
- * traversals wrote, and the step's algorithmic bytes: per scene-step 120 per
+ * traversals wrote, the step's algorithmic bytes (below), the leaves and
+ * pairs of the traversals launched from the host (those the "traverse" stage
+ * of cc_get_profile times: every traversal in the host loop, the proximity
+ * pass's with CC_TUNE_DEVICE_LOOP), and the passes the device loop ran.
+ * Algorithmic bytes: per scene-step 120 per
  * point (x_old, x_cand, v read; x, v written); per scene-pass 72 per point,
  * 12 per triangle, 8 per bond and 48 per hierarchy node (2E-1 nodes of
  * 24-byte FP32 boxes, written by the refit and read by the traversal), plus

@@ -54,10 +54,15 @@ def _split(a, off, i):
 
 
 def _run_batch(solver_cls, mix, nsteps, mode=0, window=True, record=False, split=True, graph=True, combined=True,
-               warp=False, packet=False, roles=True, overlap=False, rope=True, subset_refit=True):
+               warp=False, packet=False, roles=True, overlap=False, rope=True, subset_refit=True, device_loop=True,
+               refill=8, zone_cap=None):
     b = solver_cls(0)
     b.assembleBatch(mix)
     b.setMode(mode)
+    b.setTuning(solver_cls.TUNE_DEVICE_LOOP, int(device_loop))
+    b.setTuning(solver_cls.TUNE_TRAVERSE_REFILL, int(refill))
+    if zone_cap is not None:
+        b.setZoneCap(zone_cap)
     b.setStrainWindow(window)
     b.setTuning(solver_cls.TUNE_SPLIT_NARROW, int(split))
     b.setTuning(solver_cls.TUNE_TAIL_GRAPH, int(graph))
@@ -80,7 +85,8 @@ def _run_batch(solver_cls, mix, nsteps, mode=0, window=True, record=False, split
         xo, vo, ho, hcol = b.resolveCollisionBatch(x, xc, v, hc)
         info = dict(x_in=x, xc=xc, v_in=v, hc_in=hc, x=xo, v=vo, hc=ho, hcol=hcol,
                     kinds=[b.scenePassKinds(i) for i in range(len(mix))],
-                    zones=b.zoneRoots(), visits=b.visits() if record else None)
+                    zones=b.zoneRoots(), visits=b.visits() if record else None, counters=b.counters(),
+                    status=b.sceneStatus())
         steps.append(info)
         x, v, hc = xo, vo, ho
     b.close()
@@ -405,3 +411,45 @@ def test_vtk_dumps(solver_cls, tmp_path):
         x, v, hc = x1, v1, hc1
     s.setVtkDump(None)
     s.close()
+
+
+def _contact_sample(k=6, seed=0):
+    # scenes of the batched workload (each cloth within four steps of its
+    # obstacle), the k median sizes of evenly spaced size groups, cut to at
+    # most 40 vertices per side so the test stays short
+    out = []
+    for sc in scenes.batched(nscenes=48, seed=seed)[::8][:k]:
+        n = int(round(np.sqrt(sc.nv - (642 if "sphere" in sc.name else 8))))
+        m = min(n, 40)
+        obst = "sphere" if "sphere" in sc.name else "box"
+        r = 0.25 if obst == "sphere" else 0.2
+        speed = -float(sc.v[0, 2])
+        out.append(scenes.cloth_on_obstacle(m, obst, r, speed, seed=seed + len(out), gap=2.5e-3 * speed))
+    return out
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["plain", "mixed"])
+def test_device_loop_equals_host_loop(solver_cls, mode):
+    """Every detection pass after the proximity pass in one CUDA graph, with
+    each scene's pass sequence and the impact-zone union-find on the device,
+    gives every scene the same bits, pass sequence, zones and counters as the
+    host-driven loop - on the mix above and on contact-heavy cloth scenes
+    with impact-zone passes, a capped zone loop included."""
+    for mix, cap in ((_mix(), None), (_contact_sample(), 3)):
+        a, pv, _ = _run_batch(solver_cls, mix, 10, mode=mode, device_loop=True, zone_cap=cap)
+        b, _, _ = _run_batch(solver_cls, mix, 10, mode=mode, device_loop=False, zone_cap=cap)
+        zone_steps = capped = 0
+        for k, (u, w) in enumerate(zip(a, b)):
+            capped += int((u["status"] != 0).sum())
+            for key in ("x", "v", "hc", "hcol", "status"):
+                assert np.array_equal(u[key], w[key]), (k, key)
+            for i in range(len(mix)):
+                assert np.array_equal(u["kinds"][i], w["kinds"][i]), (k, i)
+                zone_steps += int((np.asarray(u["kinds"][i]) == 2).any())
+            assert np.array_equal(zone_labels(u["zones"]), zone_labels(w["zones"])), k
+            for c in ("passes", "ccd_passes", "zone_passes", "candidate_pairs", "visits", "hit_pairs", "contacts",
+                      "path_bytes"):
+                assert u["counters"][c] == w["counters"][c], (k, c)
+            assert u["counters"]["loop_passes"] > 0 and w["counters"]["loop_passes"] == 0, k
+        if cap is not None:
+            assert zone_steps > 0 and capped > 0

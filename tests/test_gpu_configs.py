@@ -10,9 +10,13 @@ reference compiled from its sources gives the same, tests/test_oracle_pin.py),
 and the narrow-phase visit record by SHA-256 on the single-scene runs; the
 mixed-precision path equal to the plain one bit for bit. The only allowed
 exception is a step on which the oracle built with correctly rounded
-acos/cos/sin/pow gives exactly the GPU's result (glibc misrounded an argument
-the result depended on); such steps are counted and their deviation from the
-oracle is bounded below.
+acos/cos/sin/pow gives exactly the GPU's result, bit for bit, visit record
+included: glibc misrounded an argument the result depended on (its acos, cos
+and pow are not correctly rounded on roughly 0.1% of arguments). Such steps
+are counted and their deviation from the oracle is printed; it is not
+bounded, because a misrounded coplanarity root can flip a contact decision
+and the zone loop then takes another path (on the 129x129 folded cloth one
+such step moved positions by 1e-4).
 """
 import numpy as np
 import pytest
@@ -21,10 +25,6 @@ from collision_gb300 import scenes
 from tests.lockstep import fast_forward, run_batch, run_scene
 
 pytestmark = pytest.mark.gpu
-
-# A step explained by glibc's rounding may move outputs of an ill-conditioned
-# contact; the fuzz of near-parallel edges showed 1.2e-7 in positions.
-GLIBC_RESIDUAL_ABS = 1e-6
 
 
 @pytest.fixture(scope="module")
@@ -40,7 +40,6 @@ def _check(t, label, min_contact=1, min_zone=0):
     assert t.exact + t.glibc == t.steps
     assert t.contact_steps >= min_contact, f"{label}: no contact steps in the window"
     assert t.zone_steps >= min_zone, f"{label}: no impact-zone steps in the window"
-    assert t.max_abs_x <= GLIBC_RESIDUAL_ABS and t.max_abs_v <= GLIBC_RESIDUAL_ABS / 1e-3, t
 
 
 def test_cloth_on_sphere_33_all_200_steps(solver_cls):
