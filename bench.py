@@ -191,6 +191,7 @@ def oracle_rate(scs, max_steps, budget_s, threads, zone_cap, skip_steps=0):
     for o in solvers:
         o.set_zone_cap(zone_cap)
     state = [(sc.x.copy(), sc.v.copy(), np.zeros(sc.nv, np.uint8)) for sc in scs]
+    prev = [None] * len(scs)
     live = [True] * len(scs)
     by_size = sorted(range(len(scs)), key=lambda i: -scs[i].ne)
 
@@ -204,6 +205,7 @@ def oracle_rate(scs, max_steps, budget_s, threads, zone_cap, skip_steps=0):
             return 1
         if r["rc"] != 0:
             raise RuntimeError(f"oracle step failed on scene {i}: {r['rc']}")
+        prev[i] = x
         state[i] = (r["x"], r["v"], r["has_collsn"])
         return 1
 
@@ -217,9 +219,13 @@ def oracle_rate(scs, max_steps, budget_s, threads, zone_cap, skip_steps=0):
             t_total += time.perf_counter() - t0
             done += n
             steps += 1
+    # the exact CCD re-check of each scene's last step, on the oracle's own
+    # results (untimed)
+    missed = [solvers[i].check_ccd(prev[i], state[i][0]) if live[i] and prev[i] is not None else 0
+              for i in range(len(scs))]
     for o in solvers:
         o.close()
-    final = [(x, v, hc, lv) for (x, v, hc), lv in zip(state, live)]
+    final = [(x, v, hc, lv, m) for (x, v, hc), lv, m in zip(state, live, missed)]
     return done / t_total, done, t_total, steps, final
 
 
@@ -333,7 +339,7 @@ def run_gpu(args):
         sync_all()
         scene_steps = 0
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-        counters, missed, snap = [], 0, None
+        counters, missed, snap, cpu_missed = [], 0, None, None
         s.setProfiling(True)
         with Clocks(dev) as clk, torch.cuda.stream(stream):
             for k in range(K):
@@ -346,8 +352,10 @@ def run_gpu(args):
                 counters.append(s.counters())
                 drop_capped(s, enabled)
                 if check:
-                    hits, _ = s.checkCCD(st["x"], st["xo"])
+                    hits, per = s.checkCCD(st["x"], st["xo"])
                     missed += hits
+                    if cpu is not None and W + k + 1 == cpu["steps"]:
+                        cpu_missed = per.copy()
                 st["x"], st["xo"] = st["xo"], st["x"]
                 if k + 1 == n_plain:
                     snap = (st["x"].cpu().numpy(), st["v"].cpu().numpy())
@@ -361,7 +369,7 @@ def run_gpu(args):
         s.close()
         return dict(total_ms=max_over_ranks(float(sum(step_ms))), step_ms=step_ms, counters=counters,
                     missed=missed, snap=snap, prof=prof, clocks=clk.summary(), scene_steps=scene_steps,
-                    capped=int((~enabled).sum()), tuned=tuned, rope=rope, cpu_snap=cpu_snap)
+                    capped=int((~enabled).sum()), tuned=tuned, rope=rope, cpu_snap=cpu_snap, cpu_missed=cpu_missed)
 
     # ------------------------------ plain FP64, one scene at a time
     def plain_sequential():
@@ -642,8 +650,10 @@ def run_gpu(args):
         else:
             gx, gv, ghc, gen = mixed["cpu_snap"]
             ndiff, nlive, max_abs, max_rel, capped_mismatch = 0, 0, 0.0, 0.0, 0
+            ref_missed = sum(f[4] for f in cpu["final"])
+            gpu_missed = None if mixed["cpu_missed"] is None else int(sum(mixed["cpu_missed"][i] for i in cpu["idx"]))
             for j, i in enumerate(cpu["idx"]):
-                ox, ov, ohc, olive = cpu["final"][j]
+                ox, ov, ohc, olive, _ = cpu["final"][j]
                 if not olive or not gen[i]:
                     capped_mismatch += int(olive != bool(gen[i]))
                     continue
@@ -660,6 +670,9 @@ def run_gpu(args):
             parity = {"equal": ndiff == 0 and capped_mismatch == 0, "scenes": nlive, "scenes_differing": ndiff,
                       "capped_mismatch": capped_mismatch, "steps": cpu["steps"], "max_abs": max_abs,
                       "max_rel": max_rel,
+                      "missed_ccd_last_step": {"oracle": ref_missed, "gpu": gpu_missed,
+                                               "what": "pairs the exact CCD re-check finds after the last of those "
+                                                       "steps on these scenes, on the oracle's and the GPU's states"},
                       "what": "positions, velocities and has_collsn of the CPU sample's scenes after the CPU "
                               "leg's steps, GPU batch (mixed precision) vs the oracle, bit for bit"}
         for k in ("idx", "final", "steps"):

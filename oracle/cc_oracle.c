@@ -140,6 +140,7 @@ struct cco_solver {
     /* current narrow-phase call being recorded */
     int cur_a, cur_b, cur_kind, cur_sub;
     long long ctr[7];
+    int check; /* cco_check_ccd: hit decisions only, no impulses */
 };
 
 /* ------------------------------------------------------------ vector ops */
@@ -468,6 +469,7 @@ static int point_to_tri(cco_solver* s, const int* pts, double h) {
     if (dist > h) return 0;
     for (int i = 0; i < 3; ++i)
         if (w[i] > 1 + s->eps || w[i] < -s->eps) return 0;
+    if (s->check) return 1;
     rec_contact(s, pts);
     point_to_tri_impulse(s, pts, nor, w, dist);
     return 1;
@@ -514,6 +516,7 @@ static int edge_to_edge(cco_solver* s, const int* pts, double h) {
         return 0;
     }
     for (int i = 0; i < 3; ++i) nor[i] /= nor_mag;
+    if (s->check) return 1;
     rec_contact(s, pts);
     edge_to_edge_impulse(s, pts, nor, a, b, dist);
     return 1;
@@ -1527,6 +1530,82 @@ out:
     }
     if (has_collision) *has_collision = hc;
     return rc;
+}
+
+/* The exact CCD re-check of a finished step (the metric's zero-interpenetration
+ * test, not part of the reference): every element pair whose swept boxes over
+ * [x_old, x_new] overlap goes through the reference's CCD predicate
+ * (isCollision's Moving* tests with h = eps, dcollid.cpp:753-836,
+ * dcollid3d.cpp:203-482) with avgVel = (x_new - x_old)/dt, without impulses
+ * or impact zones; pairs of one rigid surface are skipped as the reference
+ * skips them. Candidate pairs come from a sort and sweep of the boxes on x.
+ * Returns the number of pairs that still collide, or a negative status. The
+ * solver's step state is left as it was, except its current positions. */
+static const box_t* g_sweep_boxes;
+static int sweep_cmp(const void* a, const void* b) {
+    const double la = g_sweep_boxes[*(const int*)a].lo[0], lb = g_sweep_boxes[*(const int*)b].lo[0];
+    if (la < lb) return -1;
+    if (la > lb) return 1;
+    return *(const int*)a - *(const int*)b;
+}
+
+long long cco_check_ccd(cco_solver* s, const double* x_old, const double* x_new, const double* params) {
+    const int nv = s->nv, ne = s->ne;
+    const double dt = params[0];
+    double* keep = malloc(sizeof(double) * 6 * (size_t)(nv > 0 ? nv : 1));
+    box_t* box = malloc(sizeof(box_t) * (size_t)(ne > 0 ? ne : 1));
+    int* order = malloc(sizeof(int) * (size_t)(ne > 0 ? ne : 1));
+    if (!keep || !box || !order) {
+        free(keep); free(box); free(order);
+        return CCO_NOMEM;
+    }
+    memcpy(keep, s->x_old, sizeof(double) * 3 * (size_t)nv);
+    memcpy(keep + 3 * (size_t)nv, s->avg, sizeof(double) * 3 * (size_t)nv);
+    const double sdt = s->dt, seps = s->eps;
+    const int zone = s->det_imp_zone, rec = s->record, st0 = s->status;
+    s->dt = dt;
+    s->eps = params[2];
+    s->det_imp_zone = 0;
+    s->record = 0;
+    s->check = 1;
+    s->status = 0;
+    for (int p = 0; p < nv; ++p)
+        for (int j = 0; j < 3; ++j) {
+            s->x_old[3 * p + j] = x_old[3 * p + j];
+            s->avg[3 * p + j] = (x_new[3 * p + j] - x_old[3 * p + j]) / dt;
+            s->coords[3 * p + j] = x_old[3 * p + j];
+        }
+    for (int e = 0; e < ne; ++e) {
+        leaf_box(s, e, TREE_MOVING, &box[e]);
+        order[e] = e;
+    }
+    g_sweep_boxes = box;
+    qsort(order, (size_t)ne, sizeof(int), sweep_cmp);
+    long long hits = 0;
+    for (int i = 0; i < ne && s->status == 0; ++i) {
+        const box_t* a = &box[order[i]];
+        for (int j = i + 1; j < ne && box[order[j]].lo[0] <= a->hi[0]; ++j) {
+            if (!box_overlap(a, &box[order[j]])) continue;
+            int ea = order[i], eb = order[j];
+            if (ea < eb) {
+                int t = ea;
+                ea = eb;
+                eb = t;
+            }
+            hits += pair_test(s, ea, eb, 1);
+        }
+    }
+    const int bad = s->status;
+    memcpy(s->x_old, keep, sizeof(double) * 3 * (size_t)nv);
+    memcpy(s->avg, keep + 3 * (size_t)nv, sizeof(double) * 3 * (size_t)nv);
+    s->dt = sdt;
+    s->eps = seps;
+    s->det_imp_zone = zone;
+    s->record = rec;
+    s->check = 0;
+    s->status = st0;
+    free(keep); free(box); free(order);
+    return bad ? bad : hits;
 }
 
 int cco_num_passes(const cco_solver* s) { return s->npass; }

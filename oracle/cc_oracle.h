@@ -63,6 +63,10 @@ int cco_leaf_rank(const cco_solver* s, int which, int* rank_out);
 /* Counters of the last step: passes, proximity pairs, ccd pairs, contacts,
  * zone iterations, strain passes, tree rebuilds. */
 void cco_counters(const cco_solver* s, long long* out7);
+/* Exact CCD re-check of a finished step: element pairs that still collide
+ * over [x_old, x_new] by the reference's CCD predicate (h = eps, avgVel =
+ * (x_new - x_old)/dt, no impulses); negative on error. params as cco_step. */
+long long cco_check_ccd(cco_solver* s, const double* x_old, const double* x_new, const double* params);
 
 #ifdef __cplusplus
 }

@@ -96,6 +96,8 @@ def load(crmath: bool = False):
     lib.cco_leaf_rank.restype = C.c_int
     lib.cco_leaf_rank.argtypes = [C.c_void_p, C.c_int, _ip]
     lib.cco_counters.argtypes = [C.c_void_p, _lp]
+    lib.cco_check_ccd.restype = C.c_longlong
+    lib.cco_check_ccd.argtypes = [C.c_void_p, _dp, _dp, _dp]
     lib.cco_set_body.restype = C.c_int
     lib.cco_set_body.argtypes = [C.c_void_p, C.c_int, C.c_double, _dp, _dp]
     lib.cco_get_body.restype = C.c_int
@@ -178,6 +180,17 @@ class OracleSolver:
                                _ptr(x_out, _dp), _ptr(avg, _dp), C.byref(hcol), _ptr(zr, _ip))
         return dict(rc=rc, x=x_out, v=vel, has_collsn=hc, avgvel=avg,
                     has_collision=hcol.value, zone_root=zr)
+
+    def check_ccd(self, x_old, x_new, params=None):
+        """Element pairs that still collide over [x_old, x_new] by the
+        reference's CCD predicate (the exact re-check of a finished step)."""
+        x_old = np.ascontiguousarray(x_old, dtype=np.float64)
+        x_new = np.ascontiguousarray(x_new, dtype=np.float64)
+        params = self.scene.param_vec() if params is None else np.ascontiguousarray(params, dtype=np.float64)
+        n = self.lib.cco_check_ccd(self.h, _ptr(x_old, _dp), _ptr(x_new, _dp), _ptr(params, _dp))
+        if n < 0:
+            raise RuntimeError(f"oracle CCD check failed: {n}")
+        return int(n)
 
     def passes(self):
         n = self.lib.cco_num_passes(self.h)

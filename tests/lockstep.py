@@ -43,6 +43,7 @@ class Tally:
     max_rel_v: float = 0.0
     cr_roots: int = 0         # GPU cubics re-rooted with the correctly rounded functions
     capped: int = 0           # scene-steps stopped at the zone cap (both sides)
+    missed: int = 0           # pairs the exact CCD re-check finds after exact steps (GPU = oracle)
 
     def note(self, kinds):
         k = np.asarray(kinds)
@@ -168,7 +169,10 @@ def run_batch(solver_cls, scs, nsteps, mode=1, zone_cap=200, threads=16, label="
     """Scenes resolved together in one batch (the batched path; mixed
     precision by default, no recording) against both oracle builds of every
     scene. A scene that reaches the zone cap on both sides is left out from
-    then on."""
+    then on. After every step the exact CCD re-check runs on the GPU
+    (cc_check_ccd) and on the oracle's CPU restatement of it, and on every
+    scene whose step was exact the two must find the same pairs."""
+    import torch
     b = solver_cls(0)
     b.assembleBatch(scs)
     b.setMode(mode)
@@ -194,6 +198,9 @@ def run_batch(solver_cls, scs, nsteps, mode=1, zone_cap=200, threads=16, label="
             xo, vo, ho, hcol = b.resolveCollisionBatch(x, xc, v, hc)
             status = b.sceneStatus()
             roots = b.zoneRoots()
+            kinds = [b.scenePassKinds(i) for i in range(len(scs))]
+            _, missed = b.checkCCD(torch.tensor(x, device="cuda:0"), torch.tensor(xo, device="cuda:0"))
+            x_in = x
             x, v, hc = xo.copy(), vo.copy(), ho.copy()
             for i, fo, fc in jobs:
                 a, e = int(pv[i]), int(pv[i + 1])
@@ -206,9 +213,14 @@ def run_batch(solver_cls, scs, nsteps, mode=1, zone_cap=200, threads=16, label="
                     t.capped += 1
                     continue
                 assert r["rc"] == 0 and q["rc"] == 0 and status[i] == 0, (where, r["rc"], q["rc"], status[i])
-                g = dict(x=xo[a:e], v=vo[a:e], hc=ho[a:e], hcol=bool(hcol[i]), kinds=b.scenePassKinds(i),
+                g = dict(x=xo[a:e], v=vo[a:e], hc=ho[a:e], hcol=bool(hcol[i]), kinds=kinds[i],
                          zones=zone_labels(roots[a:e]), sha=None)
+                exact_before = t.exact
                 _judge(t, g, refs[i].view(refs[i].o, r), refs[i].view(refs[i].c, q), where)
+                if t.exact > exact_before:
+                    om = refs[i].o.check_ccd(x_in[a:e], r["x"])
+                    assert om == missed[i], f"{where}: CCD re-check, GPU {missed[i]} vs oracle {om}"
+                    t.missed += om
                 t.note(g["kinds"])
                 t.steps += 1
                 x[a:e], v[a:e], hc[a:e] = r["x"], r["v"], r["has_collsn"]
