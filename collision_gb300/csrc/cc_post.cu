@@ -139,6 +139,55 @@ __device__ __forceinline__ double det3(const double (*a)[3]) {
 // its members in the order of the reference's member list (which fixes the
 // rounding of every sum); sin and cos correctly rounded, as the reference's
 // libm gives them.
+// The last loop of updateImpactListVelocity (dcollid3d.cpp:160-199) for one
+// member p of a zone: its new average velocity from the zone's rigid motion
+// (centre x_cm moving at v_cm, angular velocity w of magnitude mag_w, and
+// sw = sin(dt mag_w) / mag_w, cw = cos(dt mag_w), which the reference forms
+// again for every member with the same result). Static points keep theirs.
+// True when a velocity is NaN.
+__device__ __forceinline__ bool zone_member_motion(int p, const uint8_t* __restrict__ fixed,
+                                                   const double4_32a* __restrict__ xo, double4_32a* av,
+                                                   const double* x_cm, const double* v_cm, const double* w,
+                                                   double mag_w, double sw, double cw, double dt) {
+    if (fixed[p] & 1) return false;
+    double xs[3], dx[3], xF[3], xR[3], wxR[3], tmpV[3], x_new[3], nv_[3];
+    load3(xo, p, xs);
+    for (int d = 0; d < 3; ++d) dx[d] = xs[d] - x_cm[d];
+    if (mag_w < kRoundEps) {
+        for (int d = 0; d < 3; ++d) { xF[d] = dx[d]; wxR[d] = 0.0; }
+        for (int d = 0; d < 3; ++d) xR[d] = dx[d] - xF[d];
+    } else {
+        double sc = dot3(dx, w) / dot3(w, w);
+        for (int d = 0; d < 3; ++d) xF[d] = sc * w[d];
+        for (int d = 0; d < 3; ++d) xR[d] = dx[d] - xF[d];
+        for (int d = 0; d < 3; ++d) tmpV[d] = sw * w[d];
+        cross3(tmpV, xR, wxR);
+    }
+    bool bad = false;
+    for (int d = 0; d < 3; ++d) {
+        x_new[d] = x_cm[d] + dt * v_cm[d] + xF[d] + cw * xR[d] + wxR[d];
+        nv_[d] = (x_new[d] - xs[d]) / dt;
+        if (isnan(nv_[d])) bad = true;
+    }
+    av[p] = make_double4_32a(nv_[0], nv_[1], nv_[2], 0.0);
+    return bad;
+}
+
+// Angular velocity of a zone from its angular momentum L and inertia I
+// (Cramer's rule, dcollid3d.cpp:143-153).
+__device__ __forceinline__ void zone_omega(const double (*I)[3], const double* L, double* w) {
+    double tmp[3][3];
+    for (int r = 0; r < 3; ++r) {
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) tmp[a][b] = I[a][b];
+        for (int s = 0; s < 3; ++s) tmp[s][r] = L[s];
+        if (det3(I) < kRoundEps)
+            w[r] = 0.0;
+        else
+            w[r] = det3(tmp) / det3(I);
+    }
+}
+
 // With `run` set, the zones are movable bodies (updateImpactZoneVelocityForRG,
 // dcollid.cpp:267-288, called from updateAverageVelocity when dt > 0): only
 // those of scenes in a pass, and of more than one point, move.
@@ -186,44 +235,19 @@ __device__ void zone_motion(const int* __restrict__ members, int i, int end,
             }
     }
     double w[3];
-    for (int r = 0; r < 3; ++r) {
-        for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) tmp[a][b] = I[a][b];
-        for (int s = 0; s < 3; ++s) tmp[s][r] = L[s];
-        if (det3(I) < kRoundEps)
-            w[r] = 0.0;
-        else
-            w[r] = det3(tmp) / det3(I);
-    }
+    zone_omega(I, L, w);
     double mag_w = mag3(w);
+    const double sw = mag_w < kRoundEps ? 0.0 : cr::sin(dt * mag_w) / mag_w;
+    const double cw = cr::cos(dt * mag_w);
     bool bad = false;
-    for (int q = i; q < end; ++q) {
-        int p = members[q];
-        if (fixed[p] & 1) continue;
-        double xs[3], dx[3], xF[3], xR[3], wxR[3], tmpV[3], x_new[3], nv_[3];
-        load3(xo, p, xs);
-        for (int d = 0; d < 3; ++d) dx[d] = xs[d] - x_cm[d];
-        if (mag_w < kRoundEps) {
-            for (int d = 0; d < 3; ++d) { xF[d] = dx[d]; wxR[d] = 0.0; }
-            for (int d = 0; d < 3; ++d) xR[d] = dx[d] - xF[d];
-        } else {
-            double sc = dot3(dx, w) / dot3(w, w);
-            for (int d = 0; d < 3; ++d) xF[d] = sc * w[d];
-            for (int d = 0; d < 3; ++d) xR[d] = dx[d] - xF[d];
-            double sw = cr::sin(dt * mag_w) / mag_w;
-            for (int d = 0; d < 3; ++d) tmpV[d] = sw * w[d];
-            cross3(tmpV, xR, wxR);
-        }
-        double cw = cr::cos(dt * mag_w);
-        for (int d = 0; d < 3; ++d) {
-            x_new[d] = x_cm[d] + dt * v_cm[d] + xF[d] + cw * xR[d] + wxR[d];
-            nv_[d] = (x_new[d] - xs[d]) / dt;
-            if (isnan(nv_[d])) bad = true;
-        }
-        av[p] = make_double4_32a(nv_[0], nv_[1], nv_[2], 0.0);
-    }
+    for (int q = i; q < end; ++q) bad |= zone_member_motion(members[q], fixed, xo, av, x_cm, v_cm, w, mag_w, sw, cw, dt);
     if (bad) atomicOr(&ctr->err, kErrNan);
 }
+
+// Zones of at least this many members are solved one warp per zone
+// (k_zone_solve_warp) where the zone list is built on the device.
+constexpr int kZoneWarpMin = 16;
+constexpr int kZoneWarpBlock = 128;
 
 // Zone z's members are members[zone_off[z] .. zone_off[z+1]), or with
 // zone_rng members[zone_rng[z].x .. zone_rng[z].y); dnz (may be null): the
@@ -237,9 +261,107 @@ __global__ void k_zone_solve(const int* __restrict__ members, const int* __restr
         if (ctr->err & kErrRetry) return;
         if (*dnz < nzones) nzones = *dnz;
     }
-    for (int z = blockIdx.x * blockDim.x + threadIdx.x; z < nzones; z += gridDim.x * blockDim.x)
-        zone_motion(members, zone_rng ? zone_rng[z].x : zone_off[z], zone_rng ? zone_rng[z].y : zone_off[z + 1],
-                    fixed, xo, av, vscene, scenes, ctr, run);
+    for (int z = blockIdx.x * blockDim.x + threadIdx.x; z < nzones; z += gridDim.x * blockDim.x) {
+        const int i = zone_rng ? zone_rng[z].x : zone_off[z], end = zone_rng ? zone_rng[z].y : zone_off[z + 1];
+        if (dnz && end - i >= kZoneWarpMin) continue;  // k_zone_solve_warp's
+        zone_motion(members, i, end, fixed, xo, av, vscene, scenes, ctr, run);
+    }
+}
+
+// Zones of at least kZoneWarpMin members: one warp per zone. The sums of
+// updateImpactListVelocity (centre of mass and velocity, angular momentum,
+// inertia) must be formed member by member in list order to round as the
+// reference's do, and GB300's FP64 pipe makes such a chain slow on one
+// thread: here the lanes load 32 members at a time and form every per-member
+// term in parallel (offsets, m * (dx x dv), m * (|dx|^2 delta - dx dx)),
+// and lane 0 only adds the staged terms in order - the same additions on
+// the same operands as the one-thread form. The final per-member motion is
+// spread over the lanes.
+__global__ void __launch_bounds__(kZoneWarpBlock) k_zone_solve_warp(
+    const int* __restrict__ members, const int2* __restrict__ zone_rng, int nzones, const int* __restrict__ dnz,
+    const uint8_t* __restrict__ fixed, const double4_32a* __restrict__ xo, double4_32a* av,
+    const int* __restrict__ vscene, const SceneDev* __restrict__ scenes, PassCounters* ctr) {
+    __shared__ double stage[kZoneWarpBlock / 32][32][12];
+    if (ctr->err & kErrRetry) return;
+    if (*dnz < nzones) nzones = *dnz;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    double(*st)[12] = stage[wib];
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    bool bad = false;
+    for (int z = gw; z < nzones; z += nw) {
+        const int i = zone_rng[z].x, end = zone_rng[z].y;
+        if (end - i < kZoneWarpMin) continue;
+        const Params prm = scenes[vscene[members[i]]].p;
+        const double m = prm.m, dt = prm.dt;
+        const int num_pts = end - i;
+        double x_cm[3] = {0.0, 0.0, 0.0}, v_cm[3] = {0.0, 0.0, 0.0};
+        double L[3] = {0.0, 0.0, 0.0}, I[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+        for (int c = i; c < end; c += 32) {
+            const int q = c + lane;
+            if (q < end) {
+                const int p = members[q];
+                double xs[3], vs[3];
+                load3(xo, p, xs);
+                load3(av, p, vs);
+                for (int d = 0; d < 3; ++d) st[lane][d] = xs[d], st[lane][3 + d] = vs[d];
+            }
+            __syncwarp();
+            if (lane == 0) {
+                const int k1 = end - c < 32 ? end - c : 32;
+                for (int k = 0; k < k1; ++k)
+                    for (int d = 0; d < 3; ++d) { x_cm[d] += st[k][d]; v_cm[d] += st[k][3 + d]; }
+            }
+            __syncwarp();
+        }
+        for (int d = 0; d < 3; ++d) {
+            x_cm[d] = __shfl_sync(0xffffffffu, x_cm[d] / num_pts, 0);
+            v_cm[d] = __shfl_sync(0xffffffffu, v_cm[d] / num_pts, 0);
+        }
+        for (int c = i; c < end; c += 32) {
+            const int q = c + lane;
+            if (q < end) {
+                const int p = members[q];
+                double xs[3], vs[3], dx[3], dv[3], Li[3];
+                load3(xo, p, xs);
+                load3(av, p, vs);
+                for (int d = 0; d < 3; ++d) { dx[d] = xs[d] - x_cm[d]; dv[d] = vs[d] - v_cm[d]; }
+                cross3(dx, dv, Li);
+                for (int d = 0; d < 3; ++d) st[lane][d] = m * Li[d];
+                const double mag_dx = mag3(dx);
+                for (int r = 0; r < 3; ++r)
+                    for (int s = 0; s < 3; ++s) {
+                        double t = -dx[r] * dx[s];
+                        if (r == s) t += mag_dx * mag_dx;
+                        st[lane][3 + 3 * r + s] = t * m;
+                    }
+            }
+            __syncwarp();
+            if (lane == 0) {
+                const int k1 = end - c < 32 ? end - c : 32;
+                for (int k = 0; k < k1; ++k) {
+                    for (int d = 0; d < 3; ++d) L[d] = st[k][d] + L[d];
+                    for (int r = 0; r < 3; ++r)
+                        for (int s = 0; s < 3; ++s) I[r][s] += st[k][3 + 3 * r + s];
+                }
+            }
+            __syncwarp();
+        }
+        double w[3] = {0.0, 0.0, 0.0}, mag_w = 0.0, sw = 0.0, cw = 0.0;
+        if (lane == 0) {
+            zone_omega(I, L, w);
+            mag_w = mag3(w);
+            sw = mag_w < kRoundEps ? 0.0 : cr::sin(dt * mag_w) / mag_w;
+            cw = cr::cos(dt * mag_w);
+        }
+        for (int d = 0; d < 3; ++d) w[d] = __shfl_sync(0xffffffffu, w[d], 0);
+        mag_w = __shfl_sync(0xffffffffu, mag_w, 0);
+        sw = __shfl_sync(0xffffffffu, sw, 0);
+        cw = __shfl_sync(0xffffffffu, cw, 0);
+        for (int q = i + lane; q < end; q += 32)
+            bad |= zone_member_motion(members[q], fixed, xo, av, x_cm, v_cm, w, mag_w, sw, cw, dt);
+        __syncwarp();
+    }
+    if (bad) atomicOr(&ctr->err, kErrNan);
 }
 
 // detectDomainBoundaryCollision (dcollid.cpp:116-158) then
@@ -1095,6 +1217,11 @@ void zone_solve_dev(const int* members, const int2* zone_rng, const int* dnz, in
     if (blocks > 0)
         count_launch(), k_zone_solve<<<blocks, 64, 0, s>>>(members, nullptr, zone_rng, zone_cap, dnz, fixed, xo, av,
                                                            vscene, scenes, ctr, nullptr);
+    int wblocks = nblk(zone_cap, kZoneWarpBlock / 32);
+    if (wblocks > 152 * 4) wblocks = 152 * 4;
+    if (wblocks > 0)
+        count_launch(), k_zone_solve_warp<<<wblocks, kZoneWarpBlock, 0, s>>>(members, zone_rng, zone_cap, dnz, fixed,
+                                                                            xo, av, vscene, scenes, ctr);
 }
 
 void final_rigid(const BodyBufs& b, const uint8_t* has_collsn, const double4_32a* av, cudaStream_t s) {

@@ -100,6 +100,12 @@ def _deck_string_string():
     return scenes.deck("string_string", advance=0.022, cells=20)
 
 
+def _deck_box_boundary():
+    # a movable box heading for the domain's floor (the clamp leaves movable
+    # points alone, dcollid.cpp:123)
+    return scenes.deck("box_boundary", advance=0.02, cells=20)
+
+
 CASES = {
     "sphere9": (_sphere9, 10),
     "sphere12_fast": (_sphere12_fast, 8),
@@ -113,9 +119,10 @@ CASES = {
     "deck_ball_ball": (_deck_ball_ball, 8),
     "deck_string_box": (_deck_string_box, 8),
     "deck_string_string": (_deck_string_string, 8),
+    "deck_box_boundary": (_deck_box_boundary, 8),
 }
 # Cases whose fixtures keep only the outputs of each step: the inputs of step
 # k+1 are the outputs of step k (candidate positions x + dt*v, as the host
 # loop forms them), and step 0 starts from the scene.
 CHAINED = {"rigid_bodies", "sphere12_movable", "deck_ball_plane", "deck_string_slide", "deck_ball_ball", "deck_string_box",
-           "deck_string_string"}
+           "deck_string_string", "deck_box_boundary"}

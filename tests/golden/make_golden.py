@@ -12,7 +12,8 @@ and stores per step:
            status, collsn_num increments); the count and SHA-256 of the full
            visit record (every call, in order, with orientation)
 
-Needs the reference sources (REF, default /root/reference) and g++. The
+Needs the reference sources (--ref or CC_REFERENCE; default: a directory
+named reference beside the repository) and g++. The
 fixtures it writes are self-contained: tests read only the .npz files.
 
     python tests/golden/make_golden.py [--ref /path/to/reference]
@@ -100,7 +101,7 @@ def run_case(name, make, nsteps):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=os.environ.get("CC_REFERENCE", "/root/reference"))
+    ap.add_argument("--ref", default=os.environ.get("CC_REFERENCE", os.path.join(os.path.dirname(ROOT), "reference")))
     ap.add_argument("--only", default=None)
     args = ap.parse_args()
     subprocess.check_call(["make", "-s", "-f", os.path.join(ROOT, "oracle", "Makefile.ref"),
