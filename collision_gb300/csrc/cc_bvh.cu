@@ -838,6 +838,104 @@ __global__ void __launch_bounds__(128) k_traverse_rope_dyn(
     }
 }
 
+// The queries of a pruned pass. Its scenes ran the previous pass too (a
+// scene runs its passes one after the other until it is done), and an
+// element pair none of whose points that pass touched - no impulse, no
+// impact-zone or rigid-body motion, no hitting sub-test - has the inputs it
+// had when it was last tested: in the pass after the last change of one of
+// its points, or in the step's first CCD pass, which tests every pair.
+// There it did not hit (a hit stamps the sub-test's points), so it does not
+// hit now, and the pass needs only the pairs with an element holding a
+// point stamped by the previous pass ("dirty"). Flags every element of the
+// pass and lists the dirty ones' sorted leaves.
+__global__ void k_dirty_queries(const int* __restrict__ act_e, const int* __restrict__ act_l,
+                                const int* __restrict__ ev, const unsigned* __restrict__ stamp, LoopCtl* L,
+                                uint8_t* edirty, int* query) {
+    if (!L->prune) return;
+    const int n = L->nact_e;
+    const unsigned prev = L->serial - 1u;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int e = act_e[k];
+        const int p2 = ev[3 * e + 2];
+        const bool d = stamp[ev[3 * e]] == prev || stamp[ev[3 * e + 1]] == prev || (p2 >= 0 && stamp[p2] == prev);
+        edirty[e] = d ? 1 : 0;
+        if (d) query[aggregated_add(&L->nquery, 1)] = act_l[k];
+    }
+}
+
+// The pruned traversal: each dirty element walks its whole scene along the
+// ropes from the scene's root and writes every overlapping leaf that is not
+// itself, shares no point with it, and is clean or dirty with a larger
+// element id (a pair of two dirty elements is written by the smaller one).
+__global__ void k_traverse_rope_full(int n, const RopeNode* __restrict__ rn, const int* __restrict__ rope,
+                                     const int* __restrict__ elem_scene, const SceneRun* __restrict__ run,
+                                     const int* __restrict__ ev, int2* pairs, int cap, PassCounters* ctr,
+                                     const LeafRec* __restrict__ leaves, const int* __restrict__ query,
+                                     const LoopCtl* __restrict__ L, const uint8_t* __restrict__ edirty) {
+    const int m = L->prune ? L->nquery : 0;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < m; t += gridDim.x * blockDim.x) {
+        const int i = query[t];
+        if (i < 0 || i >= n) {
+            atomicOr(&ctr->err, kErrIndexLeaf);
+            continue;
+        }
+        const LeafRec r = leaves[i];
+        const int ei = r.e;
+        if (ei < 0) continue;  // flagged by k_leaf_records
+        const SceneRun sr = run[elem_scene[ei]];
+        if (sr.mode == kSceneIdle || sr.root < 0) continue;
+        BoxOrd qo;
+        Box6 q;
+        for (int d = 0; d < 3; ++d) {
+            qo.lo[d] = r.lo[d];
+            qo.hi[d] = r.hi[d];
+            q.lo[d] = unord_double(r.lo[d]);
+            q.hi[d] = unord_double(r.hi[d]);
+        }
+        const int pi0 = r.p[0], pi1 = r.p[1], pi2 = r.p[2];
+        const Box32 q32 = box32_out(q);
+        int x = sr.root;
+        for (int steps = 0; x != kRopeEnd; ++steps) {
+            if (steps >= 2 * n) {
+                atomicOr(&ctr->err, kErrIndexNode);
+                break;
+            }
+            if (x >= 0) {
+                if (x >= n - 1) {
+                    atomicOr(&ctr->err, kErrIndexNode);
+                    break;
+                }
+                const float4* p4 = reinterpret_cast<const float4*>(&rn[x]);
+                const float4 a = __ldg(p4), b = __ldg(p4 + 1);  // lo xyz hi.x | hi.y hi.z left rope
+                const bool hit = q32.lo[0] <= a.w && q32.hi[0] >= a.x && q32.lo[1] <= b.x && q32.hi[1] >= a.y &&
+                                 q32.lo[2] <= b.y && q32.hi[2] >= a.z;
+                x = __float_as_int(hit ? b.z : b.w);
+                continue;
+            }
+            const int k = ~x;
+            if (k >= n) {
+                atomicOr(&ctr->err, kErrIndexLeaf);
+                break;
+            }
+            x = k < n - 1 ? __ldg(&rope[k]) : kRopeEnd;
+            if (k == i) continue;
+            const ulonglong2* lr = reinterpret_cast<const ulonglong2*>(&leaves[k]);
+            const ulonglong2 u0 = __ldg(lr), u1 = __ldg(lr + 1), u2 = __ldg(lr + 2);
+            if (!(qo.lo[0] <= u1.y && qo.hi[0] >= u0.x && qo.lo[1] <= u2.x && qo.hi[1] >= u0.y &&
+                  qo.lo[2] <= u2.y && qo.hi[2] >= u1.x))
+                continue;
+            const int4 pe = __ldg(reinterpret_cast<const int4*>(lr + 3));
+            const int ej = pe.w;
+            if (ej < 0) continue;
+            if (ev && (pe.x == pi0 || pe.x == pi1 || pe.x == pi2 || pe.y == pi0 || pe.y == pi1 || pe.y == pi2 ||
+                       (pe.z >= 0 && (pe.z == pi0 || pe.z == pi1 || pe.z == pi2))))
+                continue;
+            if (edirty[ej] && ej < ei) continue;  // written by ej's query
+            emit_pair(ei, ej, pairs, cap, ctr);
+        }
+    }
+}
+
 __global__ void k_brute_pairs(const Box6* __restrict__ box, int n, const int* __restrict__ elem_scene, int2* pairs,
                               int cap, PassCounters* ctr) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -936,10 +1034,11 @@ void bvh_refit(const Box6* box, BvhBufs& b, cudaStream_t s) {
 template <int DEPTH>
 void launch_stack_traverse(const Box6* box, const BvhBufs& b, int nq, int block, int2* pairs, int cap,
                            PassCounters* ctr, cudaStream_t s, const int* skip_shared_ev, const Box6* box_static) {
-    const int g = b.sub && b.dnsub ? dev_grid(nq, block) : nblk(nq, block);
+    const int* dq = b.sub ? (b.dnq ? b.dnq : b.dnsub) : nullptr;
+    const int g = dq ? dev_grid(nq, block) : nblk(nq, block);
     count_launch(), k_traverse<DEPTH><<<g, block, 0, s>>>(box, b.order, b.n, b.node, b.elem_scene, b.run,
                                                         skip_shared_ev, pairs, cap, ctr, box_static, b.leaf, b.sub,
-                                                        b.nsub, b.sub ? b.dnsub : nullptr);
+                                                        b.nsub, dq);
 }
 
 // Resident blocks of the dynamic-fetch traversal per SM, looked up once.
@@ -963,6 +1062,7 @@ void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCoun
     if (nq <= 0) return;
     const bool dyn = b.leaf && rope && b.rnode && b.rope && b.leaf32 && b.qnext && refill > 0;
     const int* dnsub = b.sub ? b.dnsub : nullptr;
+    const int* dq = b.sub ? (b.dnq ? b.dnq : b.dnsub) : nullptr;  // queries of the traversal
     if (b.leaf)
         count_launch(), k_leaf_records<<<dnsub ? dev_grid(nleaf, 256) : nblk(nleaf, 256), 256, 0, s>>>(
             box, b.order, n, b.sub, b.nsub, dnsub, b.ev, b.leaf, b.ne_all, ctr, b.rope, dyn ? b.leaf32 : nullptr);
@@ -979,12 +1079,12 @@ void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCoun
         cudaMemsetAsync(b.qnext, 0, sizeof(int), s);
         count_launch(), k_traverse_rope_dyn<<<blocks, 128, 0, s>>>(n, b.rnode, b.elem_scene, b.run, skip_shared_ev,
                                                                    pairs, cap, ctr, box_static, b.leaf, b.leaf32,
-                                                                   b.sub, b.nsub, dnsub, b.qnext,
+                                                                   b.sub, b.nsub, dq, b.qnext,
                                                                    refill > 32 ? 32 : refill);
     } else if (b.leaf && rope && b.rnode && b.rope) {
-        count_launch(), k_traverse_rope<<<dnsub ? dev_grid(nq, block) : nblk(nq, block), block, 0, s>>>(
+        count_launch(), k_traverse_rope<<<dq ? dev_grid(nq, block) : nblk(nq, block), block, 0, s>>>(
             n, b.rnode, b.rope, b.elem_scene, b.run, skip_shared_ev, pairs, cap, ctr, box_static, b.leaf, b.sub,
-            b.nsub, dnsub);
+            b.nsub, dq);
     } else if (b.leaf && packet && !b.sub) {
         count_launch(), k_traverse_packet<<<nblk(n - 1, kPacketWarps * 32), kPacketWarps * 32, 0, s>>>(
             b.order, n, b.node, b.elem_scene, b.run, skip_shared_ev, pairs, cap, ctr, box_static, b.leaf);
@@ -997,6 +1097,15 @@ void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCoun
     } else {
         launch_stack_traverse<64>(box, b, nq, block, pairs, cap, ctr, s, skip_shared_ev, box_static);
     }
+}
+
+void pruned_pairs(const BvhBufs& b, const int* act_e, const int* act_l, const unsigned* stamp, LoopCtl* L,
+                  uint8_t* edirty, int* query, int ne_cap, int2* pairs, int cap, PassCounters* ctr, const int* ev,
+                  cudaStream_t s) {
+    if (ne_cap <= 1 || b.n <= 1) return;
+    count_launch(), k_dirty_queries<<<dev_grid(ne_cap, 256), 256, 0, s>>>(act_e, act_l, ev, stamp, L, edirty, query);
+    count_launch(), k_traverse_rope_full<<<dev_grid(ne_cap, 128), 128, 0, s>>>(
+        b.n, b.rnode, b.rope, b.elem_scene, b.run, ev, pairs, cap, ctr, b.leaf, query, L, edirty);
 }
 
 void brute_pairs(const Box6* box, int ne, const int* elem_scene, int2* pairs, int cap, PassCounters* ctr,

@@ -181,6 +181,10 @@ struct LoopCtl {
     int reuse;      // >= 0: the next pass takes this many pairs of the proximity pass
     int reuse_n;    // pairs the current pass took (-1: none)
     int zone_cap;   // impact-zone passes per scene and step
+    unsigned serial;  // the current pass's serial (pass stamps), increasing across steps
+    int prune;      // the pass queries only elements with a point the previous pass touched
+    int nq_full;    // queries of the pass's full traversal (0 when it prunes or reuses)
+    int nquery;     // queries of the pruned traversal
     unsigned long long acc[kNumAcc];  // counters over the step's passes (LoopAcc)
 };
 

@@ -125,6 +125,9 @@ struct BvhBufs {
     // optional: the count of sub in device memory (nsub is then its
     // capacity), for passes whose scenes are chosen on the device
     const int* dnsub;
+    // optional: the traversal's query count in device memory, when it
+    // differs from the leaf count dnsub (the queries are sub's first ones)
+    const int* dnq;
 };
 
 // Leaf boxes of every element (static: x_old; moving: x_old and
@@ -168,6 +171,20 @@ void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCoun
 void brute_pairs(const Box6* box, int ne, const int* elem_scene, int2* pairs, int cap, PassCounters* ctr,
                  cudaStream_t s);
 
+// Pass stamps (the device loop's pruning of later passes): the kernels that
+// change a point's average velocity in a pass, and the narrow phase for the
+// points of every sub-test that hits, write the pass's serial into the
+// point's stamp. Null: no stamps.
+struct PassStamp {
+    unsigned* stamp = nullptr;         // per point
+    const unsigned* serial = nullptr;  // the current pass's serial, in device memory
+};
+__device__ __forceinline__ void stamp_point(const PassStamp& ps, int p) {
+#ifdef __CUDACC__
+    if (ps.stamp) ps.stamp[p] = *ps.serial;
+#endif
+}
+
 // ------------------------------------------------------------ narrow phase
 struct NarrowArgs {
     const double4_32a* xo;
@@ -202,6 +219,7 @@ struct NarrowArgs {
     int* pair_hit;  // per candidate pair: bit s set when sub-test s hit
     int* pairq;     // candidate pairs with a queued sub-test (capacity: the pair buffer's)
     int static_only;  // proximity pass over swept-box pairs: only those with kPairStatic
+    PassStamp ps;     // stamps of the points of every sub-test that hits
     // movable rigid bodies: the body of each point (-1 none), each body's
     // mass, and the contribution slot of body 0 (the point count)
     const int* vbody;
@@ -248,6 +266,7 @@ struct ApplyBufs {
     int* cur;      // nv + bodies
     int* idx;      // contrib_cap
     void* scan_temp;
+    PassStamp ps;  // stamps of the points whose velocity the pass changes
 };
 // Per-point sums of the pass's contributions in visiting order, then
 // avgVel += (impulse + friction) / n and has_collsn (updateAverageVelocity).
@@ -266,12 +285,12 @@ void apply_contribs(const Contrib* contrib, const PassCounters* ctr, int contrib
 // are in a pass (updateImpactZoneVelocityForRG).
 void zone_solve(const int* members, const int* zone_off, int nzones, const uint8_t* fixed, const double4_32a* xo,
                 double4_32a* av, const int* vscene, const SceneDev* scenes, PassCounters* ctr, cudaStream_t s,
-                const SceneRun* run = nullptr);
+                const SceneRun* run = nullptr, PassStamp ps = PassStamp{});
 // The same with zone z's members at members[zone_rng[z].x .. .y) and the
 // zone count in device memory (*dnz, at most zone_cap).
 void zone_solve_dev(const int* members, const int2* zone_rng, const int* dnz, int zone_cap, const uint8_t* fixed,
                     const double4_32a* xo, double4_32a* av, const int* vscene, const SceneDev* scenes,
-                    PassCounters* ctr, cudaStream_t s);
+                    PassCounters* ctr, cudaStream_t s, PassStamp ps = PassStamp{});
 
 // Impact zones of a pass on the GPU (cc_zones.cu): buffers of the union
 // replay and of the zone lists.
@@ -297,7 +316,7 @@ size_t zone_sort_temp_bytes(int cap);
 // (null: all n_pts points; dn_pts, if given, holds the count on the device).
 void zone_pass(const ZoneBufs& z, const PassCounters* ctr, const uint8_t* fixed, const int* act_pts, int n_pts,
                const int* dn_pts, const int* vscene, const SceneRun* run, const SceneDev* scenes, double4_32a* av,
-               const double4_32a* xo, cudaStream_t s);
+               const double4_32a* xo, cudaStream_t s, PassStamp ps = PassStamp{});
 
 // ------------------------------------------------ device detection loop
 // (cc_loop.cu) One pass of the loop: k_loop_plan picks each scene's mode and
@@ -316,6 +335,14 @@ void tree_check(const SceneRun* run, int nscenes, const unsigned long long* bbox
 void loop_reset(PassCounters* c, SceneRun* run, int nscenes, LoopCtl* L, cudaStream_t s);
 void pass_end(const PassCounters* c, SceneCtl* ctl, const SceneRun* run, int nscenes, LoopCtl* L, int combined,
               bool in_graph, cudaGraphConditionalHandle h_loop, cudaStream_t s);
+// The pruned broad phase of the device loop's later passes (L->prune): the
+// pass's elements with a point whose stamp is the previous pass's serial
+// walk their whole scene, from its root, and every overlapping pair with
+// such an element is written once. act_e / act_l: the pass's elements and
+// their sorted leaves (L->nact_e of them); edirty, query: ne_cap each.
+void pruned_pairs(const BvhBufs& b, const int* act_e, const int* act_l, const unsigned* stamp, LoopCtl* L,
+                  uint8_t* edirty, int* query, int ne_cap, int2* pairs, int cap, PassCounters* ctr, const int* ev,
+                  cudaStream_t s);
 
 // updateFinalForRG's device part: per body, the first point in element
 // order with has_collsn and its average velocity (into b.out).

@@ -66,6 +66,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_loop_plan(SceneCtl* ctl, Scene
         if (threadIdx.x == 0) {
             L->nact = L->nact_e = L->nact_p = 0;
             L->nbroad = L->npts = 0;
+            L->nq_full = L->nquery = 0;
             L->any_zone = 0;
             cudaGraphSetConditional(h_zone, 0u);
         }
@@ -150,8 +151,14 @@ __global__ void __launch_bounds__(kPlanThreads) k_loop_plan(SceneCtl* ctl, Scene
         if (fresh) {
             L->reuse_n = L->reuse;  // the proximity pass's pairs, for the first CCD pass only
             L->reuse = -1;
+            L->serial++;
+            // from the second CCD pass on, only pairs with a point the
+            // previous pass touched can hit (see k_dirty_queries)
+            L->prune = L->acc[kAccIters] >= 2 ? 1 : 0;
         }
         L->nbroad = L->reuse_n >= 0 ? 0 : carry.x;
+        L->nq_full = L->prune ? 0 : L->nbroad;
+        L->nquery = 0;
         L->npts = carry.y;
         L->pending = 0;
         cudaGraphSetConditional(h_zone, any_zone ? 1u : 0u);
@@ -227,6 +234,8 @@ __global__ void k_loop_reset(PassCounters* c, SceneRun* run, int nscenes, LoopCt
         if (stop) {
             L->nbroad = 0;
             L->npts = 0;
+            L->nq_full = 0;
+            L->prune = 0;
         }
     }
     if (i < nscenes) run[i].hits = 0;

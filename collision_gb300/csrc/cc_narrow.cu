@@ -84,6 +84,10 @@ __global__ void __launch_bounds__(128) k_narrow(NarrowArgs a, int max_pairs) {
         if (status) {
             t_hits++;
             atomicAdd(&a.run[sc].hits, 1);
+            for (int q = 0; q < 3; ++q) {
+                if (A[q] >= 0) stamp_point(a.ps, A[q]);
+                if (B[q] >= 0) stamp_point(a.ps, B[q]);
+            }
         }
         if (c.rec) {
             int slot = atomicAdd(&c.ctr->nrec, 1);
@@ -310,6 +314,8 @@ __global__ void __launch_bounds__(128) k_subtests(NarrowArgs a) {
         t_sub++;
         t_cr += st.ncr;
         t_contacts += st.ncontacts;
+        if (hit)
+            for (int q = 0; q < 4; ++q) stamp_point(a.ps, r.p[q]);
         if (hit && atomicOr(&a.pair_hit[r.pair], 1 << r.sub) == 0) {
             t_hits++;
             atomicAdd(&a.run[r.scene].hits, 1);

@@ -58,7 +58,7 @@ __global__ void k_contrib_scatter(const Contrib* __restrict__ c, const PassCount
 // their count is the pass's collsn_num_RG.
 __global__ void k_apply(const Contrib* __restrict__ c, PassCounters* ctr, const int* __restrict__ cnt,
                         const int* __restrict__ off, int* idx, int nv, double4_32a* av, uint8_t* has_collsn,
-                        double4_32a* dump, int nbodies, double4_32a* body_acc, int* body_num) {
+                        double4_32a* dump, int nbodies, double4_32a* body_acc, int* body_num, PassStamp ps) {
     if (ctr->err & kErrRetry) return;
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nv + nbodies) return;
@@ -105,6 +105,7 @@ __global__ void k_apply(const Contrib* __restrict__ c, PassCounters* ctr, const 
     if (bad) atomicOr(&ctr->err, kErrNan);
     av[p] = make_double4_32a(v[0], v[1], v[2], 0.0);
     has_collsn[p] = 1;
+    stamp_point(ps, p);
     if (dump) dump[p] = make_double4_32a(imp[0], imp[1], imp[2], (double)n);  // collsnImpulse, collsn_num
 }
 
@@ -114,7 +115,7 @@ __global__ void k_apply(const Contrib* __restrict__ c, PassCounters* ctr, const 
 __global__ void k_apply_rg(const int* __restrict__ members, const int* __restrict__ member_body, int nmembers,
                            const PassCounters* ctr, const double4_32a* __restrict__ body_acc,
                            const int* __restrict__ body_num, const uint8_t* __restrict__ fixed, double4_32a* av,
-                           uint8_t* has_collsn) {
+                           uint8_t* has_collsn, PassStamp ps) {
     if (ctr->err & kErrRetry) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nmembers) return;
@@ -128,6 +129,7 @@ __global__ void k_apply_rg(const int* __restrict__ members, const int* __restric
     v.z += a.z / n;
     av[p] = v;
     has_collsn[p] = 1;
+    stamp_point(ps, p);
 }
 
 __device__ __forceinline__ double det3(const double (*a)[3]) {
@@ -148,8 +150,10 @@ __device__ __forceinline__ double det3(const double (*a)[3]) {
 __device__ __forceinline__ bool zone_member_motion(int p, const uint8_t* __restrict__ fixed,
                                                    const double4_32a* __restrict__ xo, double4_32a* av,
                                                    const double* x_cm, const double* v_cm, const double* w,
-                                                   double mag_w, double sw, double cw, double dt) {
+                                                   double mag_w, double sw, double cw, double dt,
+                                                   const PassStamp& ps) {
     if (fixed[p] & 1) return false;
+    stamp_point(ps, p);
     double xs[3], dx[3], xF[3], xR[3], wxR[3], tmpV[3], x_new[3], nv_[3];
     load3(xo, p, xs);
     for (int d = 0; d < 3; ++d) dx[d] = xs[d] - x_cm[d];
@@ -191,11 +195,10 @@ __device__ __forceinline__ void zone_omega(const double (*I)[3], const double* L
 // With `run` set, the zones are movable bodies (updateImpactZoneVelocityForRG,
 // dcollid.cpp:267-288, called from updateAverageVelocity when dt > 0): only
 // those of scenes in a pass, and of more than one point, move.
-__device__ void zone_motion(const int* __restrict__ members, int i, int end,
-                                         const uint8_t* __restrict__ fixed, const double4_32a* __restrict__ xo,
-                                         double4_32a* av, const int* __restrict__ vscene,
-                                         const SceneDev* __restrict__ scenes, PassCounters* ctr,
-                                         const SceneRun* __restrict__ run) {
+__device__ void zone_motion(const int* __restrict__ members, int i, int end, const uint8_t* __restrict__ fixed,
+                            const double4_32a* __restrict__ xo, double4_32a* av, const int* __restrict__ vscene,
+                            const SceneDev* __restrict__ scenes, PassCounters* ctr,
+                            const SceneRun* __restrict__ run, const PassStamp& ps) {
     const int zs = vscene[members[i]];
     const Params prm = scenes[zs].p;
     if (run && (run[zs].mode == kSceneIdle || !(prm.dt > 0.0) || end - i < 2 || (ctr->err & kErrRetry))) return;
@@ -240,7 +243,8 @@ __device__ void zone_motion(const int* __restrict__ members, int i, int end,
     const double sw = mag_w < kRoundEps ? 0.0 : cr::sin(dt * mag_w) / mag_w;
     const double cw = cr::cos(dt * mag_w);
     bool bad = false;
-    for (int q = i; q < end; ++q) bad |= zone_member_motion(members[q], fixed, xo, av, x_cm, v_cm, w, mag_w, sw, cw, dt);
+    for (int q = i; q < end; ++q)
+        bad |= zone_member_motion(members[q], fixed, xo, av, x_cm, v_cm, w, mag_w, sw, cw, dt, ps);
     if (bad) atomicOr(&ctr->err, kErrNan);
 }
 
@@ -256,7 +260,7 @@ __global__ void k_zone_solve(const int* __restrict__ members, const int* __restr
                              const int2* __restrict__ zone_rng, int nzones, const int* __restrict__ dnz,
                              const uint8_t* __restrict__ fixed, const double4_32a* __restrict__ xo, double4_32a* av,
                              const int* __restrict__ vscene, const SceneDev* __restrict__ scenes,
-                             PassCounters* ctr, const SceneRun* __restrict__ run) {
+                             PassCounters* ctr, const SceneRun* __restrict__ run, PassStamp ps) {
     if (dnz) {
         if (ctr->err & kErrRetry) return;
         if (*dnz < nzones) nzones = *dnz;
@@ -264,7 +268,7 @@ __global__ void k_zone_solve(const int* __restrict__ members, const int* __restr
     for (int z = blockIdx.x * blockDim.x + threadIdx.x; z < nzones; z += gridDim.x * blockDim.x) {
         const int i = zone_rng ? zone_rng[z].x : zone_off[z], end = zone_rng ? zone_rng[z].y : zone_off[z + 1];
         if (dnz && end - i >= kZoneWarpMin) continue;  // k_zone_solve_warp's
-        zone_motion(members, i, end, fixed, xo, av, vscene, scenes, ctr, run);
+        zone_motion(members, i, end, fixed, xo, av, vscene, scenes, ctr, run, ps);
     }
 }
 
@@ -280,7 +284,7 @@ __global__ void k_zone_solve(const int* __restrict__ members, const int* __restr
 __global__ void __launch_bounds__(kZoneWarpBlock) k_zone_solve_warp(
     const int* __restrict__ members, const int2* __restrict__ zone_rng, int nzones, const int* __restrict__ dnz,
     const uint8_t* __restrict__ fixed, const double4_32a* __restrict__ xo, double4_32a* av,
-    const int* __restrict__ vscene, const SceneDev* __restrict__ scenes, PassCounters* ctr) {
+    const int* __restrict__ vscene, const SceneDev* __restrict__ scenes, PassCounters* ctr, PassStamp ps) {
     __shared__ double stage[kZoneWarpBlock / 32][32][12];
     if (ctr->err & kErrRetry) return;
     if (*dnz < nzones) nzones = *dnz;
@@ -358,7 +362,7 @@ __global__ void __launch_bounds__(kZoneWarpBlock) k_zone_solve_warp(
         sw = __shfl_sync(0xffffffffu, sw, 0);
         cw = __shfl_sync(0xffffffffu, cw, 0);
         for (int q = i + lane; q < end; q += 32)
-            bad |= zone_member_motion(members[q], fixed, xo, av, x_cm, v_cm, w, mag_w, sw, cw, dt);
+            bad |= zone_member_motion(members[q], fixed, xo, av, x_cm, v_cm, w, mag_w, sw, cw, dt, ps);
         __syncwarp();
     }
     if (bad) atomicOr(&ctr->err, kErrNan);
@@ -1194,34 +1198,35 @@ void apply_contribs(const Contrib* contrib, const PassCounters* ctr, int contrib
     count_launch(), k_contrib_scatter<<<blocks, 256, 0, s>>>(contrib, ctr, contrib_cap, b.off, b.cur, b.idx);
     count_launch(), k_apply<<<nblk(nslot, 128), 128, 0, s>>>(contrib, const_cast<PassCounters*>(ctr), b.cnt, b.off,
                                                              b.idx, nv, av, has_collsn, dump, nb,
-                                                             nb ? bodies->acc : nullptr, nb ? bodies->num : nullptr);
+                                                             nb ? bodies->acc : nullptr, nb ? bodies->num : nullptr,
+                                                             b.ps);
     if (nb > 0)
         count_launch(), k_apply_rg<<<nblk(bodies->nmembers, 128), 128, 0, s>>>(
             bodies->members, bodies->member_body, bodies->nmembers, ctr, bodies->acc, bodies->num, bodies->fixed, av,
-            has_collsn);
+            has_collsn, b.ps);
 }
 
 void zone_solve(const int* members, const int* zone_off, int nzones, const uint8_t* fixed, const double4_32a* xo,
                 double4_32a* av, const int* vscene, const SceneDev* scenes, PassCounters* ctr, cudaStream_t s,
-                const SceneRun* run) {
+                const SceneRun* run, PassStamp ps) {
     if (nzones > 0)
         count_launch(), k_zone_solve<<<nblk(nzones, 128), 128, 0, s>>>(members, zone_off, nullptr, nzones, nullptr,
-                                                                       fixed, xo, av, vscene, scenes, ctr, run);
+                                                                       fixed, xo, av, vscene, scenes, ctr, run, ps);
 }
 
 void zone_solve_dev(const int* members, const int2* zone_rng, const int* dnz, int zone_cap, const uint8_t* fixed,
                     const double4_32a* xo, double4_32a* av, const int* vscene, const SceneDev* scenes,
-                    PassCounters* ctr, cudaStream_t s) {
+                    PassCounters* ctr, cudaStream_t s, PassStamp ps) {
     int blocks = nblk(zone_cap, 64);
     if (blocks > 152 * 8) blocks = 152 * 8;
     if (blocks > 0)
         count_launch(), k_zone_solve<<<blocks, 64, 0, s>>>(members, nullptr, zone_rng, zone_cap, dnz, fixed, xo, av,
-                                                           vscene, scenes, ctr, nullptr);
+                                                           vscene, scenes, ctr, nullptr, ps);
     int wblocks = nblk(zone_cap, kZoneWarpBlock / 32);
     if (wblocks > 152 * 4) wblocks = 152 * 4;
     if (wblocks > 0)
         count_launch(), k_zone_solve_warp<<<wblocks, kZoneWarpBlock, 0, s>>>(members, zone_rng, zone_cap, dnz, fixed,
-                                                                            xo, av, vscene, scenes, ctr);
+                                                                            xo, av, vscene, scenes, ctr, ps);
 }
 
 void final_rigid(const BodyBufs& b, const uint8_t* has_collsn, const double4_32a* av, cudaStream_t s) {

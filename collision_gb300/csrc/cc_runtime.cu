@@ -299,6 +299,11 @@ struct cc_solver {
     int* d_act_l = nullptr;     // the pass's sorted leaves
     int* d_rebuild = nullptr;   // per scene: tree to rebuild on the host (0 none, 1 proximity, 2 collision)
     int* h_rebuild = nullptr;   // pinned
+    unsigned* d_pstamp = nullptr;  // per point: serial of the last pass that touched it
+    uint8_t* d_edirty = nullptr;   // per element: a point touched by the previous pass
+    int* d_query = nullptr;        // the pruned traversal's queries
+    unsigned serial_base = 1;      // the next step's proximity pass serial
+    PassStamp loop_stamp() const { return PassStamp{d_pstamp, &d_loop->serial}; }
     double* d_tree_vol = nullptr;  // per scene: the volume both trees share
     int* d_tree_built = nullptr;   // 2 * nscenes: tree built (proximity, then collision)
     cudaStream_t cap_stream = nullptr, cap_stream2 = nullptr;  // graph capture only
@@ -435,6 +440,7 @@ struct cc_solver {
         dfree(d_act_e); dfree(d_act_p); dfree(d_sel); dfree(d_dump); dfree(d_av_pre);
         clear_loop_graph();
         loop_key_n = -1;
+        dfree(d_pstamp); dfree(d_edirty); dfree(d_query);
         dfree(d_ctl); dfree(d_loop); dfree(d_lsel); dfree(d_act_l); dfree(d_rebuild); dfree(d_tree_vol);
         dfree(d_tree_built);
         if (h_ctl) cudaFreeHost(h_ctl);
@@ -1091,6 +1097,9 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     ok &= dalloc(&d_act_p, (size_t)nv) == cudaSuccess;
     ok &= dalloc(&d_sel, 3 * (size_t)n + 2) == cudaSuccess;
     ok &= cudaMallocHost(&h_sel, sizeof(int) * (3 * (size_t)n + 2)) == cudaSuccess;
+    ok &= dalloc(&d_pstamp, (size_t)nv) == cudaSuccess;
+    ok &= dalloc(&d_edirty, (size_t)ne) == cudaSuccess;
+    ok &= dalloc(&d_query, (size_t)ne) == cudaSuccess;
     ok &= dalloc(&d_ctl, (size_t)n) == cudaSuccess;
     ok &= dalloc(&d_loop, 1) == cudaSuccess;
     ok &= dalloc(&d_lsel, 3 * ((size_t)n + 1)) == cudaSuccess;
@@ -1143,6 +1152,8 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     cudaMemsetAsync(d_rank[0], 0, sizeof(int) * (size_t)(ne > 0 ? ne : 1), stream);
     cudaMemsetAsync(d_rank[1], 0, sizeof(int) * (size_t)(ne > 0 ? ne : 1), stream);
     cudaMemsetAsync(d_lsel, 0, sizeof(int) * 3 * ((size_t)n + 1), stream);
+    cudaMemsetAsync(d_pstamp, 0xff, sizeof(unsigned) * (size_t)(nv > 0 ? nv : 1), stream);
+    cudaMemsetAsync(d_edirty, 0, (size_t)(ne > 0 ? ne : 1), stream);
     cudaMemsetAsync(d_rebuild, 0, sizeof(int) * (size_t)n, stream);
     cudaMemsetAsync(d_tree_vol, 0, sizeof(double) * (size_t)n, stream);
     cudaMemsetAsync(d_tree_built, 0, sizeof(int) * 2 * (size_t)n, stream);
@@ -1345,18 +1356,21 @@ void cc_solver::prox_pass_async() {
               tune.packet_traverse, tune.rope_traverse, tune.traverse_refill, tune.stack_depth);
     prof(kStTraverse, false);
     prof(kStNarrowProx, true);
-    const NarrowArgs a = narrow_args(0, combined);
+    NarrowArgs a = narrow_args(0, combined);
+    a.ps = loop_stamp();
     if (mode == 1 && split_narrow)
         narrow_pass_split(a, 0, pair_cap, stream, tune.narrow_block, false);
     else
         narrow_pass(a, 0, pair_cap, stream, tune.narrow_block);
     prof(kStNarrowProx, false);
     prof(kStApply, true);
-    apply_contribs(d_contrib, d_ctr, contrib_cap, nv, d_av, d_hc, apply, stream, nullptr,
+    ApplyBufs ab = apply;
+    ab.ps = loop_stamp();
+    apply_contribs(d_contrib, d_ctr, contrib_cap, nv, d_av, d_hc, ab, stream, nullptr,
                    bodies.empty() ? nullptr : &body_bufs);
     if (!bodies.empty())  // updateImpactZoneVelocityForRG (dcollid.cpp:744-745)
         zone_solve(d_body_members, d_body_zone_off, (int)bodies.size(), d_fixed, d_xo, d_av, d_vscene, d_scenes, d_ctr,
-                   stream, d_run);
+                   stream, d_run, loop_stamp());
     prof(kStApply, false);
     pass_end(d_ctr, d_ctl, d_run, nscenes, d_loop, (combined && bodies.empty()) ? 1 : 0, false, 0, stream);
 }
@@ -1414,18 +1428,24 @@ cc_status cc_solver::build_loop_graph(int n_hier) {
     if (mode == 1)
         point_boxes(d_xo, d_av, d_vscene, d_scenes, d_act_p, nv, 1, d_pbox_lo, d_pbox_hi, d_p32, d_v32, cs,
                     &d_loop->npts);
+    // the full traversal (first CCD pass) or the pruned one (later passes)
+    lb.dnq = &d_loop->nq_full;
     bvh_pairs(d_box, lb, d_pairs, pair_cap, d_ctr, cs, d_ev, tune.traverse_block, nullptr, false, tune.rope_traverse,
               tune.traverse_refill, tune.stack_depth);
-    const NarrowArgs a = narrow_args(1, false);
+    pruned_pairs(lb, d_act_e, d_act_l, d_pstamp, d_loop, d_edirty, d_query, ne, d_pairs, pair_cap, d_ctr, d_ev, cs);
+    NarrowArgs a = narrow_args(1, false);
+    a.ps = loop_stamp();
     if (mode == 1 && split_narrow)
         narrow_pass_split(a, 1, pair_cap, cs, tune.narrow_block, true);
     else
         narrow_pass(a, 1, pair_cap, cs, tune.narrow_block);
-    apply_contribs(d_contrib, d_ctr, contrib_cap, nv, d_av, d_hc, apply, cs, nullptr,
+    ApplyBufs ab = apply;
+    ab.ps = loop_stamp();
+    apply_contribs(d_contrib, d_ctr, contrib_cap, nv, d_av, d_hc, ab, cs, nullptr,
                    bodies.empty() ? nullptr : &body_bufs);
     if (!bodies.empty())
         zone_solve(d_body_members, d_body_zone_off, (int)bodies.size(), d_fixed, d_xo, d_av, d_vscene, d_scenes, d_ctr,
-                   cs, d_run);
+                   cs, d_run, loop_stamp());
     const long long l1 = g_kernel_launches;
     // the impact-zone stage, only in passes with a scene in that mode
     cudaStreamCaptureStatus cst;
@@ -1447,7 +1467,8 @@ cc_status cc_solver::build_loop_graph(int n_hier) {
         e = cudaStreamBeginCaptureToGraph(cap_stream2, ip.conditional.phGraph_out[0], nullptr, nullptr, 0,
                                           cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        zone_pass(zb, d_ctr, d_fixed, d_act_p, nv, &d_loop->npts, d_vscene, d_run, d_scenes, d_av, d_xo, cap_stream2);
+        zone_pass(zb, d_ctr, d_fixed, d_act_p, nv, &d_loop->npts, d_vscene, d_run, d_scenes, d_av, d_xo, cap_stream2,
+                  loop_stamp());
         cudaGraph_t zg = nullptr;
         e = cudaStreamEndCapture(cap_stream2, &zg);
     }
@@ -1501,6 +1522,8 @@ cc_status cc_solver::device_passes(std::string& capped) {
     h_loop->reuse = -1;
     h_loop->reuse_n = -1;
     h_loop->zone_cap = zone_cap;
+    h_loop->serial = serial_base;
+    h_loop->nq_full = bvh.n;
     const LoopCtl loop_init = *h_loop;
     cudaMemcpyAsync(d_ctl, h_ctl, sizeof(SceneCtl) * (size_t)nscenes, cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d_loop, h_loop, sizeof(LoopCtl), cudaMemcpyHostToDevice, stream);
@@ -1560,6 +1583,7 @@ cc_status cc_solver::device_passes(std::string& capped) {
         }
         need_prox = in_prox;
     }
+    serial_base = h_loop->serial + 1u;
     // the passes' counters (the proximity pass's scene-pass counts are above)
     const unsigned long long* a = h_loop->acc;
     counters[0] += (long long)a[kAccPasses];

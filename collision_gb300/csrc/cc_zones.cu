@@ -215,7 +215,7 @@ size_t zone_sort_temp_bytes(int cap) { return radix_sort_temp_bytes(cap); }
 
 void zone_pass(const ZoneBufs& z, const PassCounters* ctr_c, const uint8_t* fixed, const int* act_pts, int n_pts,
                const int* dn_pts, const int* vscene, const SceneRun* run, const SceneDev* scenes, double4_32a* av,
-               const double4_32a* xo, cudaStream_t s) {
+               const double4_32a* xo, cudaStream_t s, PassStamp ps) {
     PassCounters* ctr = const_cast<PassCounters*>(ctr_c);
     const int cap = z.cap;
     const int blocks = nblk(cap, 256) < 152 * 8 ? nblk(cap, 256) : 152 * 8;
@@ -232,7 +232,7 @@ void zone_pass(const ZoneBufs& z, const PassCounters* ctr_c, const uint8_t* fixe
                                                        z.zone_root);
     const int zb = nblk(z.zone_cap, 128) < 152 * 8 ? nblk(z.zone_cap, 128) : 152 * 8;
     count_launch(), k_zone_members<<<zb, 128, 0, s>>>(ctr, z.zone_rng, z.zone_root, z.uf, z.members);
-    zone_solve_dev(z.members, z.zone_rng, &ctr->nzones, z.zone_cap, fixed, xo, av, vscene, scenes, ctr, s);
+    zone_solve_dev(z.members, z.zone_rng, &ctr->nzones, z.zone_cap, fixed, xo, av, vscene, scenes, ctr, s, ps);
 }
 
 }  // namespace ccg
