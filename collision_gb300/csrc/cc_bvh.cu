@@ -846,20 +846,26 @@ __global__ void __launch_bounds__(128) k_traverse_rope_dyn(
 // its points, or in the step's first CCD pass, which tests every pair.
 // There it did not hit (a hit stamps the sub-test's points), so it does not
 // hit now, and the pass needs only the pairs with an element holding a
-// point stamped by the previous pass ("dirty"). Flags every element of the
-// pass and lists the dirty ones' sorted leaves.
-__global__ void k_dirty_queries(const int* __restrict__ act_e, const int* __restrict__ act_l,
-                                const int* __restrict__ ev, const unsigned* __restrict__ stamp, LoopCtl* L,
-                                uint8_t* edirty, int* query) {
+// point stamped by the previous pass ("dirty"). Flags the element of every
+// sorted leaf of the pass (act_l: the pass's leaves; order: the element of
+// each sorted leaf) and lists the dirty ones' leaves.
+__global__ void k_dirty_queries(const int* __restrict__ act_l, const unsigned int* __restrict__ order, int n_hier,
+                                int ne_all, const int* __restrict__ ev, const unsigned* __restrict__ stamp, LoopCtl* L,
+                                uint8_t* edirty, int* query, PassCounters* ctr) {
     if (!L->prune) return;
     const int n = L->nact_e;
     const unsigned prev = L->serial - 1u;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const int e = act_e[k];
+        const int j = act_l[k];
+        const int e = (j >= 0 && j < n_hier) ? (int)order[j] : -1;
+        if (e < 0 || e >= ne_all) {
+            atomicOr(&ctr->err, kErrIndexLeaf);
+            continue;
+        }
         const int p2 = ev[3 * e + 2];
         const bool d = stamp[ev[3 * e]] == prev || stamp[ev[3 * e + 1]] == prev || (p2 >= 0 && stamp[p2] == prev);
         edirty[e] = d ? 1 : 0;
-        if (d) query[aggregated_add(&L->nquery, 1)] = act_l[k];
+        if (d) query[aggregated_add(&L->nquery, 1)] = j;
     }
 }
 
@@ -1103,7 +1109,8 @@ void pruned_pairs(const BvhBufs& b, const int* act_e, const int* act_l, const un
                   uint8_t* edirty, int* query, int ne_cap, int2* pairs, int cap, PassCounters* ctr, const int* ev,
                   cudaStream_t s) {
     if (ne_cap <= 1 || b.n <= 1) return;
-    count_launch(), k_dirty_queries<<<dev_grid(ne_cap, 256), 256, 0, s>>>(act_e, act_l, ev, stamp, L, edirty, query);
+    count_launch(), k_dirty_queries<<<dev_grid(ne_cap, 256), 256, 0, s>>>(act_l, b.order, b.n, b.ne_all, ev, stamp, L,
+                                                                          edirty, query, ctr);
     count_launch(), k_traverse_rope_full<<<dev_grid(ne_cap, 128), 128, 0, s>>>(
         b.n, b.rnode, b.rope, b.elem_scene, b.run, ev, pairs, cap, ctr, b.leaf, query, L, edirty);
 }

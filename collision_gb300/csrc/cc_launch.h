@@ -338,8 +338,8 @@ void pass_end(const PassCounters* c, SceneCtl* ctl, const SceneRun* run, int nsc
 // The pruned broad phase of the device loop's later passes (L->prune): the
 // pass's elements with a point whose stamp is the previous pass's serial
 // walk their whole scene, from its root, and every overlapping pair with
-// such an element is written once. act_e / act_l: the pass's elements and
-// their sorted leaves (L->nact_e of them); edirty, query: ne_cap each.
+// such an element is written once. act_l: the pass's sorted leaves
+// (L->nact_e of them; act_e is unused); edirty, query: ne_cap each.
 void pruned_pairs(const BvhBufs& b, const int* act_e, const int* act_l, const unsigned* stamp, LoopCtl* L,
                   uint8_t* edirty, int* query, int ne_cap, int2* pairs, int cap, PassCounters* ctr, const int* ev,
                   cudaStream_t s);

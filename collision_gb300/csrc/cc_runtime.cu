@@ -12,6 +12,7 @@
 // own hit count. A single mesh is the one-scene case of the same code.
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -40,7 +41,7 @@ const char* kStageNames[kNumStages] = {"init", "leaf_boxes", "bvh_build", "trave
 
 constexpr int kMaxSceneElems = (1 << 22) - 1;  // leaf ranks fill 22 bits of a contribution key
 constexpr long long kMaxTotal = 1ll << 28;     // points and elements over all scenes
-constexpr int kNumCounters = 22;
+constexpr int kNumCounters = 23;
 constexpr int kErrIndex = kErrIndexNode | kErrIndexLeaf | kErrIndexElem;
 std::string index_error(int e) {
     std::string m = "broad phase met an index out of range:";
@@ -1266,11 +1267,13 @@ cc_status cc_solver::update_trees(int which, const Box6* boxes) {
     std::sort(todo.begin(), todo.end(), [&](int a, int b) { return scenes[a].ne > scenes[b].ne; });
     int threads = host_threads > 0 ? host_threads : (int)std::thread::hardware_concurrency();
     if (threads <= 0) threads = 1;
+    const auto t0 = std::chrono::steady_clock::now();
     parallel_for((int)todo.size(), threads, [&](int i) {
         SceneHost& sh = scenes[todo[i]];
         sh.volume = sh.tree[which].build(h_boxes.data() + sh.e0, sh.ne);
         sh.tree[which].ranks(h_rank.data() + sh.e0);
     });
+    counters[22] += std::chrono::duration_cast<std::chrono::microseconds>(std::chrono::steady_clock::now() - t0).count();
     for (int s : todo)
         cudaMemcpyAsync(d_rank[which] + scenes[s].e0, h_rank.data() + scenes[s].e0, sizeof(int) * (size_t)scenes[s].ne,
                         cudaMemcpyHostToDevice, stream);
@@ -1311,11 +1314,14 @@ cc_status cc_solver::rebuild_flagged() {
         std::sort(ids.begin(), ids.end(), [&](int a, int b) { return scenes[a].ne > scenes[b].ne; });
         int threads = host_threads > 0 ? host_threads : (int)std::thread::hardware_concurrency();
         if (threads <= 0) threads = 1;
+        const auto t0 = std::chrono::steady_clock::now();
         parallel_for((int)ids.size(), threads, [&](int i) {
             SceneHost& sh = scenes[ids[i]];
             sh.volume = sh.tree[which].build(h_boxes.data() + sh.e0, sh.ne);
             sh.tree[which].ranks(h_rank.data() + sh.e0);
         });
+        counters[22] +=
+            std::chrono::duration_cast<std::chrono::microseconds>(std::chrono::steady_clock::now() - t0).count();
         for (int s : ids)
             cudaMemcpyAsync(d_rank[which] + scenes[s].e0, h_rank.data() + scenes[s].e0,
                             sizeof(int) * (size_t)scenes[s].ne, cudaMemcpyHostToDevice, stream);

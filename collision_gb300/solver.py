@@ -346,7 +346,8 @@ class CollisionSolver3d:
     COUNTER_NAMES = ("passes", "ccd_passes", "zone_passes", "candidate_pairs", "visits", "hit_pairs",
                      "contacts", "strain_passes", "tree_builds", "kernel_launches", "strain_averaged",
                      "strain_exact", "fp64_subtests", "moving_visits", "strain_bytes", "cr_roots", "broad_leaves",
-                     "broad_pairs", "path_bytes", "timed_traverse_leaves", "timed_traverse_pairs", "loop_passes")
+                     "broad_pairs", "path_bytes", "timed_traverse_leaves", "timed_traverse_pairs", "loop_passes",
+                     "tree_build_us")
 
     def counters(self) -> dict:
         n_all = len(self.COUNTER_NAMES)
