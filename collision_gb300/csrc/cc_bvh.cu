@@ -854,7 +854,11 @@ __global__ void k_dirty_queries(const int* __restrict__ act_l, const unsigned in
                                 uint8_t* edirty, int* query, PassCounters* ctr) {
     if (!L->prune) return;
     const int n = L->nact_e;
-    const unsigned prev = L->serial - 1u;
+    // stamped by the previous pass - or by this pass's own earlier attempt,
+    // when it stopped for a larger buffer after its narrow phase had stamped
+    // hits and now runs again: those points were dirty before it, or are
+    // touched by it now (a superset is safe)
+    const unsigned prev = L->serial - 1u, cur = L->serial;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const int j = act_l[k];
         const int e = (j >= 0 && j < n_hier) ? (int)order[j] : -1;
@@ -863,7 +867,8 @@ __global__ void k_dirty_queries(const int* __restrict__ act_l, const unsigned in
             continue;
         }
         const int p2 = ev[3 * e + 2];
-        const bool d = stamp[ev[3 * e]] == prev || stamp[ev[3 * e + 1]] == prev || (p2 >= 0 && stamp[p2] == prev);
+        const unsigned s0 = stamp[ev[3 * e]], s1 = stamp[ev[3 * e + 1]], s2 = p2 >= 0 ? stamp[p2] : 0u;
+        const bool d = s0 == prev || s0 == cur || s1 == prev || s1 == cur || (p2 >= 0 && (s2 == prev || s2 == cur));
         edirty[e] = d ? 1 : 0;
         if (d) query[aggregated_add(&L->nquery, 1)] = j;
     }

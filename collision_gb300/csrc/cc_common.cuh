@@ -183,6 +183,7 @@ struct LoopCtl {
     int zone_cap;   // impact-zone passes per scene and step
     unsigned serial;  // the current pass's serial (pass stamps), increasing across steps
     int prune;      // the pass queries only elements with a point the previous pass touched
+    int prune_on;   // later passes may prune (CC_TUNE_PRUNE)
     int nq_full;    // queries of the pass's full traversal (0 when it prunes or reuses)
     int nquery;     // queries of the pruned traversal
     unsigned long long acc[kNumAcc];  // counters over the step's passes (LoopAcc)

@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_loop_plan(SceneCtl* ctl, Scene
             L->serial++;
             // from the second CCD pass on, only pairs with a point the
             // previous pass touched can hit (see k_dirty_queries)
-            L->prune = L->acc[kAccIters] >= 2 ? 1 : 0;
+            L->prune = (L->prune_on && L->acc[kAccIters] >= 2) ? 1 : 0;
         }
         L->nbroad = L->reuse_n >= 0 ? 0 : carry.x;
         L->nq_full = L->prune ? 0 : L->nbroad;

@@ -292,6 +292,7 @@ struct cc_solver {
     // sequence and the loop's state on the device, the passes after the
     // proximity pass in one graph with a WHILE node
     bool device_loop = true;
+    bool prune = true;  // the device loop's later passes test only touched pairs
     SceneCtl* d_ctl = nullptr;
     SceneCtl* h_ctl = nullptr;  // pinned, nscenes
     LoopCtl* d_loop = nullptr;
@@ -1529,6 +1530,7 @@ cc_status cc_solver::device_passes(std::string& capped) {
     h_loop->reuse_n = -1;
     h_loop->zone_cap = zone_cap;
     h_loop->serial = serial_base;
+    h_loop->prune_on = prune ? 1 : 0;
     h_loop->nq_full = bvh.n;
     const LoopCtl loop_init = *h_loop;
     cudaMemcpyAsync(d_ctl, h_ctl, sizeof(SceneCtl) * (size_t)nscenes, cudaMemcpyHostToDevice, stream);
@@ -2412,6 +2414,9 @@ cc_status cc_set_tuning(cc_solver* s, int knob, int value) {
         case CC_TUNE_DEVICE_LOOP:
             s->device_loop = value != 0;
             return CC_OK;
+        case CC_TUNE_PRUNE:
+            s->prune = value != 0;
+            return CC_OK;
         case CC_TUNE_TRAVERSE_REFILL:
             if (value < 0 || value > 32) return CC_BAD_INPUT;
             s->tune.traverse_refill = value;
@@ -2456,6 +2461,7 @@ int cc_get_tuning(cc_solver* s, int knob) {
         case CC_TUNE_SUBSET_REFIT: return s->subset_refit ? 1 : 0;
         case CC_TUNE_TRAVERSE_REFILL: return s->tune.traverse_refill;
         case CC_TUNE_DEVICE_LOOP: return s->device_loop ? 1 : 0;
+        case CC_TUNE_PRUNE: return s->prune ? 1 : 0;
         case CC_TUNE_STACK_DEPTH: return s->tune.stack_depth;
         case CC_TUNE_PAIR_CAPACITY: return s->pair_cap;
         default: return -1;

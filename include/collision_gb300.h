@@ -265,6 +265,10 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
  *                           rebuild a reference tree or grow a buffer. Not
  *                           with recording or VTK dumps, which take the host
  *                           loop. 0: the host runs every pass. Same results
+ *   CC_TUNE_PRUNE           1 (default): in the device loop, passes after the
+ *                           first CCD pass test only the element pairs with a
+ *                           point the previous pass touched (the only pairs
+ *                           that can hit); 0: every pair. Same results
  * cc_get_tuning returns the current value, or -1 for an unknown knob. */
 enum {
     CC_TUNE_SPLIT_NARROW = 0,
@@ -282,7 +286,8 @@ enum {
     CC_TUNE_TRAVERSE_REFILL = 12,
     CC_TUNE_STACK_DEPTH = 13,
     CC_TUNE_PAIR_CAPACITY = 14,
-    CC_TUNE_DEVICE_LOOP = 15
+    CC_TUNE_DEVICE_LOOP = 15,
+    CC_TUNE_PRUNE = 16
 };
 cc_status cc_set_tuning(cc_solver* s, int knob, int value);
 int cc_get_tuning(cc_solver* s, int knob);
