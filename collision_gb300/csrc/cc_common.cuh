@@ -162,6 +162,25 @@ struct SceneCtl {
     int hcol, status, leafbase, rebuild;
 };
 
+struct PassCounters {
+    int npairs;       // candidate pairs written by the traversal
+    int ncontrib;     // contributions written by the narrow phase
+    int nhit_pairs;   // narrow-phase calls that returned true
+    int nrec;         // visit records written
+    int err;          // ErrBits
+    int nvisits;      // narrow-phase calls (pairs not skipped as same-rigid-surface)
+    int ncontacts;    // sub-tests that applied an impulse
+    int nsub;         // sub-tests evaluated in FP64 (not rejected by a filter)
+    int ncr;          // coplanarity cubics whose roots were formed again correctly rounded
+    int nunion;       // union records written (impact-zone passes)
+    int nsub_pt;      // point-triangle sub-tests queued by a split pass
+    int nsub_ee;      // edge-edge sub-tests queued by a split pass
+    int npairq;       // pairs with a queued sub-test (split passes)
+    int nzones;       // impact zones listed for the zone solve (impact-zone passes)
+    int nmembers;     // their members
+    int nseg;         // union-record segments, one per zone the pass's unions touch
+};
+
 // The device-resident detection loop's own state.
 enum LoopHost { kHostRebuild = 1, kHostRetry = 2, kHostFatal = 4 };
 enum LoopAcc {
@@ -187,26 +206,9 @@ struct LoopCtl {
     int nq_full;    // queries of the pass's full traversal (0 when it prunes or reuses)
     int nquery;     // queries of the pruned traversal
     unsigned long long acc[kNumAcc];  // counters over the step's passes (LoopAcc)
+    PassCounters stopped;  // the counters of the pass that stopped the loop (the sizes to grow to)
 };
 
-struct PassCounters {
-    int npairs;       // candidate pairs written by the traversal
-    int ncontrib;     // contributions written by the narrow phase
-    int nhit_pairs;   // narrow-phase calls that returned true
-    int nrec;         // visit records written
-    int err;          // ErrBits
-    int nvisits;      // narrow-phase calls (pairs not skipped as same-rigid-surface)
-    int ncontacts;    // sub-tests that applied an impulse
-    int nsub;         // sub-tests evaluated in FP64 (not rejected by a filter)
-    int ncr;          // coplanarity cubics whose roots were formed again correctly rounded
-    int nunion;       // union records written (impact-zone passes)
-    int nsub_pt;      // point-triangle sub-tests queued by a split pass
-    int nsub_ee;      // edge-edge sub-tests queued by a split pass
-    int npairq;       // pairs with a queued sub-test (split passes)
-    int nzones;       // impact zones listed for the zone solve (impact-zone passes)
-    int nmembers;     // their members
-    int nseg;         // union-record segments, one per zone the pass's unions touch
-};
 
 // One point's entry in the reference's union-find with member lists
 // (UF{next_pt, root, tail, num_pts}, collid.h:22-27; makeSet, findSet,

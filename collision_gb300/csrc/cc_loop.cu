@@ -263,9 +263,11 @@ __global__ void __launch_bounds__(kPlanThreads) k_pass_end(const PassCounters* _
         } else if (e & (kErrNan | kErrIndexNode | kErrIndexLeaf | kErrIndexElem)) {
             L->host |= kHostFatal;
             L->err = e;
+            L->stopped = *c;
         } else if (e & kErrRetry) {
             L->host |= kHostRetry;
             L->err = e;
+            L->stopped = *c;  // later iterations of the stopped loop reset *c
         } else {
             stop = 0;
             unsigned long long* a = L->acc;

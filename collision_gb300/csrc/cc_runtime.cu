@@ -309,14 +309,33 @@ struct cc_solver {
     double* d_tree_vol = nullptr;  // per scene: the volume both trees share
     int* d_tree_built = nullptr;   // 2 * nscenes: tree built (proximity, then collision)
     cudaStream_t cap_stream = nullptr, cap_stream2 = nullptr;  // graph capture only
-    cudaGraphExec_t loop_exec = nullptr;
-    bool loop_dirty = true;  // buffers or settings the graph holds have changed
-    int loop_key_n = -1;     // leaves of the hierarchy the graph was built for
-    long long loop_body_launches = 0, loop_zone_launches = 0;
+    // One graph per arithmetic mode, each valid while the buffers and
+    // settings it holds stand (gen) and for the hierarchy size it was built
+    // for, so that alternating modes does not rebuild it.
+    struct LoopGraph {
+        cudaGraphExec_t exec = nullptr;
+        unsigned gen = 0;
+        int key_n = -1;
+        long long body_launches = 0, zone_launches = 0;
+    };
+    LoopGraph loop_graphs[2];
+    unsigned loop_gen = 1;   // bumped whenever a buffer or setting a graph holds changes
+    bool loop_dirty = false; // set by the code that changes one; folded into loop_gen
     void clear_loop_graph() {
-        if (loop_exec) cudaGraphExecDestroy(loop_exec);
-        loop_exec = nullptr;
-        loop_dirty = true;
+        for (auto& lg : loop_graphs) {
+            if (lg.exec) cudaGraphExecDestroy(lg.exec);
+            lg = LoopGraph{};
+        }
+        ++loop_gen;
+        loop_dirty = false;
+    }
+    LoopGraph* current_loop_graph(int n_hier) {
+        if (loop_dirty) {
+            ++loop_gen;
+            loop_dirty = false;
+        }
+        LoopGraph& lg = loop_graphs[mode];
+        return (lg.exec && lg.gen == loop_gen && lg.key_n == n_hier) ? &lg : nullptr;
     }
     bool use_device_loop() const { return device_loop && !record && vtk_dir.empty() && !overlap_tails; }
     NarrowArgs narrow_args(int moving, bool combined) const {
@@ -441,7 +460,6 @@ struct cc_solver {
         dfree(d_rec); dfree(d_pbox_lo); dfree(d_pbox_hi); dfree(d_p32); dfree(d_v32);
         dfree(d_act_e); dfree(d_act_p); dfree(d_sel); dfree(d_dump); dfree(d_av_pre);
         clear_loop_graph();
-        loop_key_n = -1;
         dfree(d_pstamp); dfree(d_edirty); dfree(d_query);
         dfree(d_ctl); dfree(d_loop); dfree(d_lsel); dfree(d_act_l); dfree(d_rebuild); dfree(d_tree_vol);
         dfree(d_tree_built);
@@ -1389,7 +1407,9 @@ void cc_solver::prox_pass_async() {
 // n_hier leaves that the step's proximity pass builds, and again whenever a
 // buffer or a setting it holds changes.
 cc_status cc_solver::build_loop_graph(int n_hier) {
-    clear_loop_graph();
+    LoopGraph& lg = loop_graphs[mode];
+    if (lg.exec) cudaGraphExecDestroy(lg.exec);
+    lg = LoopGraph{};
     if (!cap_stream && (cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking) != cudaSuccess ||
                         cudaStreamCreateWithFlags(&cap_stream2, cudaStreamNonBlocking) != cudaSuccess))
         return cuda_check("capture streams");
@@ -1483,19 +1503,19 @@ cc_status cc_solver::build_loop_graph(int n_hier) {
     pass_end(d_ctr, d_ctl, d_run, nscenes, d_loop, 0, true, h_loop_c, cs);
     cudaGraph_t bg = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(cs, &bg);
-    loop_body_launches = (l1 - l0) + (g_kernel_launches - l2);
-    loop_zone_launches = l2 - l1;
+    lg.body_launches = (l1 - l0) + (g_kernel_launches - l2);
+    lg.zone_launches = l2 - l1;
     g_kernel_launches = l0;
     if (e == cudaSuccess) e = e2;
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&loop_exec, g, 0);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&lg.exec, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) {
-        loop_exec = nullptr;
+        lg.exec = nullptr;
         cudaGetLastError();
         return fail(CC_CUDA_ERROR, std::string("loop graph: ") + cudaGetErrorString(e));
     }
-    loop_dirty = false;
-    loop_key_n = n_hier;
+    lg.gen = loop_gen;
+    lg.key_n = n_hier;
     return CC_OK;
 }
 
@@ -1537,21 +1557,24 @@ cc_status cc_solver::device_passes(std::string& capped) {
     cudaMemcpyAsync(d_loop, h_loop, sizeof(LoopCtl), cudaMemcpyHostToDevice, stream);
     bool need_prox = true;
     long long graph_runs = 0;
+    LoopGraph* lgraph = nullptr;
     for (int round = 0;; ++round) {
         if (round >= 64) return fail(CC_PAIR_OVERFLOW, "the detection loop kept stopping for the host");
         if (need_prox) prox_pass_async();
-        if (loop_dirty || !loop_exec || loop_key_n != n_hier) {
+        LoopGraph* lgp = current_loop_graph(n_hier);
+        if (!lgp) {
             cc_status st = build_loop_graph(n_hier);
             if (st) return st;
+            lgp = &loop_graphs[mode];
         }
+        lgraph = lgp;
         prof(kStLoop, true);
-        if (cudaGraphLaunch(loop_exec, stream) != cudaSuccess) return cuda_check("loop graph launch");
+        if (cudaGraphLaunch(lgp->exec, stream) != cudaSuccess) return cuda_check("loop graph launch");
         prof(kStLoop, false);
         ++graph_runs;
         cudaMemcpyAsync(h_loop, d_loop, sizeof(LoopCtl), cudaMemcpyDeviceToHost, stream);
         cudaMemcpyAsync(h_ctl, d_ctl, sizeof(SceneCtl) * (size_t)nscenes, cudaMemcpyDeviceToHost, stream);
         cudaMemcpyAsync(h_rebuild, d_rebuild, sizeof(int) * (size_t)nscenes, cudaMemcpyDeviceToHost, stream);
-        cudaMemcpyAsync(h_ctr, d_ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, stream);
         if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("detection loop");
         const int host = h_loop->host;
         if (!host) break;
@@ -1574,10 +1597,11 @@ cc_status cc_solver::device_passes(std::string& capped) {
                 tune.stack_depth = kTraversalStack;  // a tuned shallower stack was too shallow here
                 loop_dirty = true;
             }
-            if (!st && (err & kErrPairOverflow)) st = grow_pairs(2 * h_ctr->npairs + 1024);
-            if (!st && (err & kErrContribOverflow)) st = grow_contrib(2 * h_ctr->ncontrib + 1024);
-            if (!st && (err & kErrSubOverflow)) st = grow_subs(2 * std::max(h_ctr->nsub_pt, h_ctr->nsub_ee) + 1024);
-            if (!st && (err & kErrUnionOverflow)) st = grow_unions(2 * h_ctr->nunion + 1024);
+            const PassCounters& c = h_loop->stopped;  // the stopped pass's counts
+            if (!st && (err & kErrPairOverflow)) st = grow_pairs(2 * c.npairs + 1024);
+            if (!st && (err & kErrContribOverflow)) st = grow_contrib(2 * c.ncontrib + 1024);
+            if (!st && (err & kErrSubOverflow)) st = grow_subs(2 * std::max(c.nsub_pt, c.nsub_ee) + 1024);
+            if (!st && (err & kErrUnionOverflow)) st = grow_unions(2 * c.nunion + 1024);
             if (st) return st;
         }
         // the stopped pass runs again: the proximity pass from the start (no
@@ -1611,7 +1635,8 @@ cc_status cc_solver::device_passes(std::string& capped) {
     counters[20] += (long long)a[kAccProxPairs];
     const long long loop_iters = (long long)a[kAccIters] - 1;
     counters[21] += loop_iters;
-    count_launch((int)(loop_body_launches * (loop_iters + graph_runs) + loop_zone_launches * (long long)a[kAccZonePasses]));
+    count_launch((int)(lgraph->body_launches * (loop_iters + graph_runs) +
+                       lgraph->zone_launches * (long long)a[kAccZonePasses]));
     for (int s = 0; s < nscenes; ++s) {
         SceneHost& sh = scenes[s];
         const SceneCtl& c = h_ctl[s];
@@ -2667,8 +2692,7 @@ cc_status cc_set_strain_window(cc_solver* s, int on) {
 
 cc_status cc_set_mode(cc_solver* s, int mode) {
     if (!s || mode < 0 || mode > 1) return CC_BAD_INPUT;
-    s->mode = mode;
-    s->loop_dirty = true;
+    s->mode = mode;  // each mode keeps its own loop graph
     return CC_OK;
 }
 
