@@ -112,6 +112,8 @@ def load(path: str = LIB_PATH):
     lib.cc_get_zone_roots.argtypes = [vp, ip]
     lib.cc_get_leaf_ranks.restype = C.c_int
     lib.cc_get_leaf_ranks.argtypes = [vp, C.c_int, ip]
+    lib.cc_get_tree_volume.restype = C.c_int
+    lib.cc_get_tree_volume.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
     lib.cc_debug_candidate_pairs.restype = C.c_int
     lib.cc_debug_candidate_pairs.argtypes = [vp, C.c_int, C.c_int, ip, C.c_int]
     lib.cc_set_stream.restype = C.c_int

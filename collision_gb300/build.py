@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libcollision_gb300.so")
 SOURCES = ["cc_prims.cu", "cc_bvh.cu", "cc_narrow.cu", "cc_post.cu", "cc_zones.cu", "cc_loop.cu", "cc_runtime.cu", "cc_noalloc.cu",
-           "cc_tree_order.cpp", "cc_strain_plan.cpp", "cc_vtk.cpp"]
+           "cc_tree_order.cpp", "cc_tree_gpu.cu", "cc_strain_plan.cpp", "cc_vtk.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off"]
 

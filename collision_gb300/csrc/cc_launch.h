@@ -409,4 +409,13 @@ void math_selftest(int fn, const double* a, const double* b, double* out, int n,
 void final_velocity(const uint8_t* in_elem, const uint8_t* has_collsn, const double4_32a* av, const int* vscene,
                     const SceneDev* scenes, double* vel, int nv, const uint8_t* mask, cudaStream_t s);
 
+// The reference trees' leaf order on the GPU (cc_tree_gpu.cu). jobs: 3 ints
+// per tree (scene, first element, elements); boxes and rank indexed by
+// element. Writes each leaf's inorder rank within its tree, each tree's root
+// node and root volume. scratch holds tree_scratch_bytes(ne_total), where
+// ne_total bounds every tree's first element + elements.
+size_t tree_scratch_bytes(long long ne_total);
+void tree_order_gpu(const Box6* boxes, const int* jobs, int njobs, int max_ne, void* scratch, long long ne_total,
+                    int* rank, int* root_out, double* vol_out, cudaStream_t s);
+
 }  // namespace ccg

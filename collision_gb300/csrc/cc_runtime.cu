@@ -118,7 +118,8 @@ enum HostState { kHsDone = 0, kHsProx, kHsCcd, kHsZone };
 
 struct SceneHost {
     int v0 = 0, nv = 0, e0 = 0, ne = 0, nt = 0;  // nt: triangles (the first nt elements)
-    RefTreeOrder tree[2];
+    RefTreeOrder tree[2];  // host emulation (CC_TUNE_HOST_TREE) only
+    bool built[2] = {false, false};
     double volume = 0.0;  // shared by both trees (dcollid.cpp:381, 422)
     int strain_edges = 0, strain_points = 0;
     int strain_caps[3] = {0, 0, 0};
@@ -308,6 +309,15 @@ struct cc_solver {
     PassStamp loop_stamp() const { return PassStamp{d_pstamp, &d_loop->serial}; }
     double* d_tree_vol = nullptr;  // per scene: the volume both trees share
     int* d_tree_built = nullptr;   // 2 * nscenes: tree built (proximity, then collision)
+    // reference tree order built on the GPU (cc_tree_gpu.cu)
+    bool host_tree = false;          // CC_TUNE_HOST_TREE: emulate the insertions on host threads instead
+    void* d_tree_scratch = nullptr;  // nodes, parent links and leaf counts of the trees being built
+    int* d_tree_jobs = nullptr;      // 3 per tree: scene, first element, elements
+    int* h_tree_jobs = nullptr;      // pinned
+    int* d_tree_root = nullptr;
+    double* d_tree_vol_out = nullptr;
+    double* h_tree_vol_out = nullptr;  // pinned
+    cc_status build_trees(int which, std::vector<int>& ids, const Box6* boxes);
     cudaStream_t cap_stream = nullptr, cap_stream2 = nullptr;  // graph capture only
     // One graph per arithmetic mode, each valid while the buffers and
     // settings it holds stand (gen) and for the hierarchy size it was built
@@ -463,6 +473,13 @@ struct cc_solver {
         dfree(d_pstamp); dfree(d_edirty); dfree(d_query);
         dfree(d_ctl); dfree(d_loop); dfree(d_lsel); dfree(d_act_l); dfree(d_rebuild); dfree(d_tree_vol);
         dfree(d_tree_built);
+        if (d_tree_scratch) cudaFree(d_tree_scratch);
+        d_tree_scratch = nullptr;
+        dfree(d_tree_jobs); dfree(d_tree_root); dfree(d_tree_vol_out);
+        if (h_tree_jobs) cudaFreeHost(h_tree_jobs);
+        if (h_tree_vol_out) cudaFreeHost(h_tree_vol_out);
+        h_tree_jobs = nullptr;
+        h_tree_vol_out = nullptr;
         if (h_ctl) cudaFreeHost(h_ctl);
         if (h_loop) cudaFreeHost(h_loop);
         if (h_rebuild) cudaFreeHost(h_rebuild);
@@ -1127,6 +1144,11 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     ok &= dalloc(&d_rebuild, (size_t)n) == cudaSuccess;
     ok &= dalloc(&d_tree_vol, (size_t)n) == cudaSuccess;
     ok &= dalloc(&d_tree_built, 2 * (size_t)n) == cudaSuccess;
+    ok &= dalloc(&d_tree_jobs, 3 * (size_t)n) == cudaSuccess;
+    ok &= dalloc(&d_tree_root, (size_t)n) == cudaSuccess;
+    ok &= dalloc(&d_tree_vol_out, (size_t)n) == cudaSuccess;
+    ok &= cudaMallocHost(&h_tree_jobs, sizeof(int) * 3 * (size_t)n) == cudaSuccess;
+    ok &= cudaMallocHost(&h_tree_vol_out, sizeof(double) * (size_t)n) == cudaSuccess;
     ok &= cudaMallocHost(&h_ctl, sizeof(SceneCtl) * (size_t)n) == cudaSuccess;
     ok &= cudaMallocHost(&h_loop, sizeof(LoopCtl)) == cudaSuccess;
     ok &= cudaMallocHost(&h_rebuild, sizeof(int) * (size_t)n) == cudaSuccess;
@@ -1275,29 +1297,63 @@ cc_status cc_solver::update_trees(int which, const Box6* boxes) {
             rhi[d] = dec_host(h_bbox[6 * s + 3 + d]);
         }
         double v = box_volume(rlo, rhi);
-        if (!sh.tree[which].built() || (v - sh.volume) > 0.2 * sh.volume) todo.push_back(s);
+        if (!sh.built[which] || (v - sh.volume) > 0.2 * sh.volume) todo.push_back(s);
     }
     if (todo.empty()) return CC_OK;
-    for (int s : todo)
-        cudaMemcpyAsync(h_boxes.data() + scenes[s].e0, boxes + scenes[s].e0, sizeof(Box6) * (size_t)scenes[s].ne,
-                        cudaMemcpyDeviceToHost, stream);
-    if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("leaf boxes to host");
-    // largest scenes first: they bound the time of the parallel build
-    std::sort(todo.begin(), todo.end(), [&](int a, int b) { return scenes[a].ne > scenes[b].ne; });
-    int threads = host_threads > 0 ? host_threads : (int)std::thread::hardware_concurrency();
-    if (threads <= 0) threads = 1;
+    return build_trees(which, todo, boxes);
+}
+
+// Build tree `which` of the scenes in `ids` from their leaf boxes (device):
+// the ranks go to d_rank[which], the root volumes to the scenes' shared
+// volume. By default on the GPU (cc_tree_gpu.cu: the reference's insertions
+// pipelined in one CTA per tree); with CC_TUNE_HOST_TREE on host threads,
+// one tree per thread (cc_tree_order.cpp). Both give the same ranks and
+// volumes.
+cc_status cc_solver::build_trees(int which, std::vector<int>& ids, const Box6* boxes) {
     const auto t0 = std::chrono::steady_clock::now();
-    parallel_for((int)todo.size(), threads, [&](int i) {
-        SceneHost& sh = scenes[todo[i]];
-        sh.volume = sh.tree[which].build(h_boxes.data() + sh.e0, sh.ne);
-        sh.tree[which].ranks(h_rank.data() + sh.e0);
-    });
+    if (host_tree) {
+        for (int s : ids)
+            cudaMemcpyAsync(h_boxes.data() + scenes[s].e0, boxes + scenes[s].e0, sizeof(Box6) * (size_t)scenes[s].ne,
+                            cudaMemcpyDeviceToHost, stream);
+        if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("leaf boxes to host");
+        // largest scenes first: they bound the time of the parallel build
+        std::sort(ids.begin(), ids.end(), [&](int a, int b) { return scenes[a].ne > scenes[b].ne; });
+        int threads = host_threads > 0 ? host_threads : (int)std::thread::hardware_concurrency();
+        if (threads <= 0) threads = 1;
+        parallel_for((int)ids.size(), threads, [&](int i) {
+            SceneHost& sh = scenes[ids[i]];
+            sh.volume = sh.tree[which].build(h_boxes.data() + sh.e0, sh.ne);
+            sh.tree[which].ranks(h_rank.data() + sh.e0);
+        });
+        for (int s : ids)
+            cudaMemcpyAsync(d_rank[which] + scenes[s].e0, h_rank.data() + scenes[s].e0,
+                            sizeof(int) * (size_t)scenes[s].ne, cudaMemcpyHostToDevice, stream);
+    } else {
+        if (!d_tree_scratch &&
+            cudaMalloc(&d_tree_scratch, tree_scratch_bytes(bvh.ne_all)) != cudaSuccess) {
+            d_tree_scratch = nullptr;
+            return fail(CC_NO_MEMORY, "tree build scratch allocation failed");
+        }
+        int max_ne = 0;
+        for (size_t i = 0; i < ids.size(); ++i) {
+            const SceneHost& sh = scenes[ids[i]];
+            h_tree_jobs[3 * i] = ids[i];
+            h_tree_jobs[3 * i + 1] = sh.e0;
+            h_tree_jobs[3 * i + 2] = sh.ne;
+            max_ne = std::max(max_ne, sh.ne);
+        }
+        const int nj = (int)ids.size();
+        cudaMemcpyAsync(d_tree_jobs, h_tree_jobs, sizeof(int) * 3 * (size_t)nj, cudaMemcpyHostToDevice, stream);
+        tree_order_gpu(boxes, d_tree_jobs, nj, max_ne, d_tree_scratch, bvh.ne_all, d_rank[which], d_tree_root,
+                       d_tree_vol_out, stream);
+        cudaMemcpyAsync(h_tree_vol_out, d_tree_vol_out, sizeof(double) * (size_t)nj, cudaMemcpyDeviceToHost, stream);
+        if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("tree build");
+        for (int i = 0; i < nj; ++i) scenes[ids[i]].volume = h_tree_vol_out[i];
+    }
+    for (int s : ids) scenes[s].built[which] = scenes[s].ne > 0;
     counters[22] += std::chrono::duration_cast<std::chrono::microseconds>(std::chrono::steady_clock::now() - t0).count();
-    for (int s : todo)
-        cudaMemcpyAsync(d_rank[which] + scenes[s].e0, h_rank.data() + scenes[s].e0, sizeof(int) * (size_t)scenes[s].ne,
-                        cudaMemcpyHostToDevice, stream);
-    counters[8] += (long long)todo.size();
-    sync_tree_state(todo, which);
+    counters[8] += (long long)ids.size();
+    sync_tree_state(ids, which);
     return CC_OK;
 }
 
@@ -1326,26 +1382,8 @@ cc_status cc_solver::rebuild_flagged() {
         std::vector<int>& ids = todo[which];
         if (ids.empty()) continue;
         const Box6* boxes = (which == 0 && combined_broad) ? d_box_st : d_box;
-        for (int s : ids)
-            cudaMemcpyAsync(h_boxes.data() + scenes[s].e0, boxes + scenes[s].e0, sizeof(Box6) * (size_t)scenes[s].ne,
-                            cudaMemcpyDeviceToHost, stream);
-        if (cudaStreamSynchronize(stream) != cudaSuccess) return cuda_check("leaf boxes to host");
-        std::sort(ids.begin(), ids.end(), [&](int a, int b) { return scenes[a].ne > scenes[b].ne; });
-        int threads = host_threads > 0 ? host_threads : (int)std::thread::hardware_concurrency();
-        if (threads <= 0) threads = 1;
-        const auto t0 = std::chrono::steady_clock::now();
-        parallel_for((int)ids.size(), threads, [&](int i) {
-            SceneHost& sh = scenes[ids[i]];
-            sh.volume = sh.tree[which].build(h_boxes.data() + sh.e0, sh.ne);
-            sh.tree[which].ranks(h_rank.data() + sh.e0);
-        });
-        counters[22] +=
-            std::chrono::duration_cast<std::chrono::microseconds>(std::chrono::steady_clock::now() - t0).count();
-        for (int s : ids)
-            cudaMemcpyAsync(d_rank[which] + scenes[s].e0, h_rank.data() + scenes[s].e0,
-                            sizeof(int) * (size_t)scenes[s].ne, cudaMemcpyHostToDevice, stream);
-        counters[8] += (long long)ids.size();
-        sync_tree_state(ids, which);
+        const cc_status st = build_trees(which, ids, boxes);
+        if (st) return st;
     }
     cudaMemsetAsync(d_rebuild, 0, sizeof(int) * (size_t)nscenes, stream);
     return cuda_check("tree rebuild");
@@ -2442,6 +2480,9 @@ cc_status cc_set_tuning(cc_solver* s, int knob, int value) {
         case CC_TUNE_PRUNE:
             s->prune = value != 0;
             return CC_OK;
+        case CC_TUNE_HOST_TREE:
+            s->host_tree = value != 0;
+            return CC_OK;
         case CC_TUNE_TRAVERSE_REFILL:
             if (value < 0 || value > 32) return CC_BAD_INPUT;
             s->tune.traverse_refill = value;
@@ -2487,6 +2528,7 @@ int cc_get_tuning(cc_solver* s, int knob) {
         case CC_TUNE_TRAVERSE_REFILL: return s->tune.traverse_refill;
         case CC_TUNE_DEVICE_LOOP: return s->device_loop ? 1 : 0;
         case CC_TUNE_PRUNE: return s->prune ? 1 : 0;
+        case CC_TUNE_HOST_TREE: return s->host_tree ? 1 : 0;
         case CC_TUNE_STACK_DEPTH: return s->tune.stack_depth;
         case CC_TUNE_PAIR_CAPACITY: return s->pair_cap;
         default: return -1;
@@ -2621,9 +2663,16 @@ cc_status cc_get_zone_roots(cc_solver* s, int* out) {
 cc_status cc_get_leaf_ranks(cc_solver* s, int which, int* out) {
     if (!s || !out || which < 0 || which > 1) return CC_BAD_INPUT;
     for (const SceneHost& sh : s->scenes)
-        if (sh.ne > 0 && !sh.tree[which].built()) return CC_BAD_INPUT;
-    for (const SceneHost& sh : s->scenes)
-        if (sh.ne > 0) sh.tree[which].ranks(out + sh.e0);
+        if (sh.ne > 0 && !sh.built[which]) return CC_BAD_INPUT;
+    if (s->ne == 0) return CC_OK;
+    cudaSetDevice(s->device);
+    cudaMemcpyAsync(out, s->d_rank[which], sizeof(int) * (size_t)s->ne, cudaMemcpyDeviceToHost, s->stream);
+    if (cudaStreamSynchronize(s->stream) != cudaSuccess) return s->cuda_check("leaf ranks");
+    return CC_OK;
+}
+cc_status cc_get_tree_volume(cc_solver* s, int scene, double* out) {
+    if (!s || !out || scene < 0 || scene >= s->nscenes) return CC_BAD_INPUT;
+    *out = s->scenes[scene].volume;
     return CC_OK;
 }
 

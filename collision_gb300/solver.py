@@ -186,7 +186,7 @@ class CollisionSolver3d:
     TUNE_SPLIT_NARROW, TUNE_TRAVERSE_BLOCK, TUNE_NARROW_BLOCK, TUNE_STRAIN_BLOCK, TUNE_TAIL_GRAPH = 0, 1, 2, 3, 4
     TUNE_COMBINED_BROAD, TUNE_STRAIN_WARP, TUNE_PACKET_TRAVERSE, TUNE_STRAIN_ROLES, TUNE_TAIL_OVERLAP = 5, 6, 7, 8, 9
     TUNE_ROPE_TRAVERSE, TUNE_SUBSET_REFIT, TUNE_TRAVERSE_REFILL, TUNE_STACK_DEPTH, TUNE_PAIR_CAPACITY = 10, 11, 12, 13, 14
-    TUNE_DEVICE_LOOP, TUNE_PRUNE = 15, 16
+    TUNE_DEVICE_LOOP, TUNE_PRUNE, TUNE_HOST_TREE = 15, 16, 17
 
     def setTuning(self, knob: int, value: int):
         """Launch shapes and the two-stage narrow phase; none changes results."""
@@ -382,6 +382,12 @@ class CollisionSolver3d:
         out = np.zeros(self._ne, dtype=np.int32)
         st = self._lib.cc_get_leaf_ranks(self._h, int(which), out.ctypes.data_as(C.POINTER(C.c_int)))
         return out if st == 0 else None
+
+    def treeVolume(self, scene: int = 0) -> float:
+        """Root volume of the scene's last built tree (both trees share it)."""
+        v = C.c_double(0.0)
+        self._check(self._lib.cc_get_tree_volume(self._h, int(scene), C.byref(v)))
+        return v.value
 
     def candidatePairs(self, moving: bool, brute_force: bool = False) -> np.ndarray:
         n = self._lib.cc_debug_candidate_pairs(self._h, int(moving), int(brute_force), None, 0)

@@ -269,6 +269,10 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
  *                           first CCD pass test only the element pairs with a
  *                           point the previous pass touched (the only pairs
  *                           that can hit); 0: every pair. Same results
+ *   CC_TUNE_HOST_TREE       0 (default): the reference trees' leaf order is
+ *                           built on the GPU (the insertions pipelined, one
+ *                           CTA per tree); 1: on host threads, one tree per
+ *                           thread. Same ranks and volumes
  * cc_get_tuning returns the current value, or -1 for an unknown knob. */
 enum {
     CC_TUNE_SPLIT_NARROW = 0,
@@ -287,7 +291,8 @@ enum {
     CC_TUNE_STACK_DEPTH = 13,
     CC_TUNE_PAIR_CAPACITY = 14,
     CC_TUNE_DEVICE_LOOP = 15,
-    CC_TUNE_PRUNE = 16
+    CC_TUNE_PRUNE = 16,
+    CC_TUNE_HOST_TREE = 17
 };
 cc_status cc_set_tuning(cc_solver* s, int knob, int value);
 int cc_get_tuning(cc_solver* s, int knob);
@@ -371,6 +376,9 @@ cc_status cc_get_zone_roots(cc_solver* s, int* out);
 /* Leaf rank of every element in its scene's proximity (which=0) or
  * collision (which=1) tree; CC_BAD_INPUT while one of them is unbuilt. */
 cc_status cc_get_leaf_ranks(cc_solver* s, int which, int* out);
+/* Root volume of the scene's last built tree (AABBTree::getVolume,
+ * AABB.h:114; the rebuild test of dcollid.cpp:381, 422 compares with it). */
+cc_status cc_get_tree_volume(cc_solver* s, int scene, double* out);
 
 /* Candidate pairs of the current state (after cc_resolve: the final x_old
  * and average velocities), by LBVH traversal or by testing all pairs; for

@@ -133,11 +133,14 @@ def test_lbvh_pairs_equal_all_pairs(solver_cls):
     s.close()
 
 
-def test_leaf_ranks_match_oracle(solver_cls):
+@pytest.mark.parametrize("host_tree", [0, 1])
+def test_leaf_ranks_match_oracle(solver_cls, host_tree):
+    # the trees built on the GPU (default) and by the host emulation
     from oracle.ccopy import OracleSolver
     sc = scenes.cloth_on_sphere(n=12, z=0.252, radius=0.25, sub=2, side=0.4, speed=3.0, seed=2)
     o = OracleSolver(sc, record=0)
     s = solver_cls(0)
+    s.setTuning(s.TUNE_HOST_TREE, host_tree)
     s.assembleFromScene(sc)
     x, v, hc = sc.x.copy(), sc.v.copy(), np.zeros(sc.nv, np.uint8)
     for _ in range(3):
