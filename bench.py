@@ -383,10 +383,30 @@ def run_gpu(args):
         step_ms = [a.elapsed_time(b) for a, b in evs]
         prof = s.profile()
         rope = bool(s.getTuning(CollisionSolver3d.TUNE_ROPE_TRAVERSE))
+        kprof = None
+        if mode == 1 and args.kernel_steps > 0:
+            # after the timed steps, untimed: a few more steps with every
+            # pass's stages timed inside the device loop's graph too
+            # (profiling level 2 adds boundary kernels to each pass, so the
+            # timed steps run without them), for the per-kernel roofline
+            # entries
+            s.setProfiling(2)
+            kc = []
+            with torch.cuda.stream(stream):
+                for k in range(args.kernel_steps):
+                    candidate(st)
+                    s.resolveCollisionBatchDevice(st["x"], st["xc"], st["v"], st["hc"], st["xo"])
+                    kc.append(s.counters())
+                    drop_capped(s, enabled)
+                    st["x"], st["xo"] = st["xo"], st["x"]
+                stream.synchronize()
+            kprof = dict(prof=s.profile(), counters={k: sum(c[k] for c in kc) for k in kc[0]},
+                         steps=args.kernel_steps)
         s.close()
         return dict(total_ms=max_over_ranks(float(sum(step_ms))), step_ms=step_ms, counters=counters,
                     missed=missed, snap=snap, prof=prof, clocks=clk.summary(), scene_steps=scene_steps,
-                    capped=int((~enabled).sum()), tuned=tuned, rope=rope, cpu_snap=cpu_snap, cpu_missed=cpu_missed)
+                    capped=int((~enabled).sum()), tuned=tuned, rope=rope, cpu_snap=cpu_snap, cpu_missed=cpu_missed,
+                    kprof=kprof)
 
     # ------------------------------ plain FP64, one scene at a time
     def plain_sequential():
@@ -769,6 +789,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--kernel-steps", type=int, default=2,
+                    help="untimed steps after the timed ones with every pass's stages timed (roofline.kernels)")
     ap.add_argument("--tune", action="append", default=[], metavar="KNOB=VALUE",
                     help="set a tuning knob on every solver, e.g. STRAIN_BLOCK=128 (names: CollisionSolver3d.TUNE_*)")
     args = ap.parse_args()

@@ -230,9 +230,11 @@ void narrow_pass(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s,
 // The same pass in stages (mixed precision only, no recording): FP32
 // filters per pair, then the FP64 sub-tests that pass them, one thread
 // each, then - for scenes in impact-zone mode - the createImpZone calls of
-// every pair that hit.
+// every pair that hit. parts selects the filters (kSplitFilter), the rest
+// (kSplitSubtests) or both, so that the two can be timed apart.
+enum { kSplitFilter = 1, kSplitSubtests = 2, kSplitAll = 3 };
 void narrow_pass_split(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s, int block = 128,
-                       bool zone = false);
+                       bool zone = false, int parts = kSplitAll);
 // Inputs of the mixed-precision filter: outward-rounded FP32 boxes of every
 // point over the pass's time window (with its scene's dt), and x_old and
 // (moving passes) avgVel rounded to FP32.
@@ -333,6 +335,9 @@ void loop_expand(const int* sel, const int* eoff, const int* poff, const SceneDe
 void tree_check(const SceneRun* run, int nscenes, const unsigned long long* bbox_enc, const double* vol,
                 const int* built, int which, int* rebuild, LoopCtl* L, cudaStream_t s);
 void loop_reset(PassCounters* c, SceneRun* run, int nscenes, LoopCtl* L, cudaStream_t s);
+// Stage profiling inside the loop graph: acc[0] the last boundary's time,
+// then (ns, count) per slot 1.. - the time since the previous boundary.
+void stage_mark(unsigned long long* acc, int slot, cudaStream_t s);
 void pass_end(const PassCounters* c, SceneCtl* ctl, const SceneRun* run, int nscenes, LoopCtl* L, int combined,
               bool in_graph, cudaGraphConditionalHandle h_loop, cudaStream_t s);
 // The pruned broad phase of the device loop's later passes (L->prune): the

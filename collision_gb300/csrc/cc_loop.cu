@@ -356,6 +356,23 @@ void loop_reset(PassCounters* c, SceneRun* run, int nscenes, LoopCtl* L, cudaStr
     count_launch(), k_loop_reset<<<nblk(nscenes > 0 ? nscenes : 1, 256), 256, 0, s>>>(c, run, nscenes, L);
 }
 
+// A stage boundary inside the loop graph (stage profiling): the device time
+// since the previous boundary, from the global nanosecond timer, goes to
+// `slot` (0 only records the time).
+__global__ void k_stage_mark(unsigned long long* acc, int slot) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (slot > 0) {
+        acc[2 * slot - 1] += t - acc[0];
+        acc[2 * slot] += 1;
+    }
+    acc[0] = t;
+}
+
+void stage_mark(unsigned long long* acc, int slot, cudaStream_t s) {
+    count_launch(), k_stage_mark<<<1, 1, 0, s>>>(acc, slot);
+}
+
 void pass_end(const PassCounters* c, SceneCtl* ctl, const SceneRun* run, int nscenes, LoopCtl* L, int combined,
               bool in_graph, cudaGraphConditionalHandle h_loop, cudaStream_t s) {
     count_launch(), k_pass_end<<<1, kPlanThreads, 0, s>>>(c, ctl, run, nscenes, L, combined, in_graph ? 1 : 0,

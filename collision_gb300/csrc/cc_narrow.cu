@@ -399,10 +399,11 @@ void narrow_pass(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s,
         count_launch(), k_narrow<false><<<blocks, threads, 0, s>>>(a, max_pairs);
 }
 
-void narrow_pass_split(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s, int block, bool zone) {
+void narrow_pass_split(const NarrowArgs& a, int moving, int max_pairs, cudaStream_t s, int block, bool zone,
+                       int parts) {
     if (max_pairs <= 0) return;
     if (!a.pbox_lo || !a.p32 || (moving && !a.v32)) {  // the filters need the FP32 point data (mode 1)
-        narrow_pass(a, moving, max_pairs, s, block);
+        if (parts & kSplitFilter) narrow_pass(a, moving, max_pairs, s, block);
         return;
     }
     const int cap_blocks = 152 * 16 * 128 / block;
@@ -411,14 +412,18 @@ void narrow_pass_split(const NarrowArgs& a, int moving, int max_pairs, cudaStrea
     int sblocks = (a.sub_cap + 127) / 128;
     if (sblocks > 152 * 16) sblocks = 152 * 16;
     if (moving) {
-        count_launch(), k_narrow_filter<true><<<blocks, block, 0, s>>>(a, max_pairs);
-        count_launch(), k_subtests<true, false><<<sblocks, 128, 0, s>>>(a);
-        count_launch(), k_subtests<true, true><<<sblocks, 128, 0, s>>>(a);
-        if (zone) count_launch(), k_zone_unions<<<blocks, 128, 0, s>>>(a);
+        if (parts & kSplitFilter) count_launch(), k_narrow_filter<true><<<blocks, block, 0, s>>>(a, max_pairs);
+        if (parts & kSplitSubtests) {
+            count_launch(), k_subtests<true, false><<<sblocks, 128, 0, s>>>(a);
+            count_launch(), k_subtests<true, true><<<sblocks, 128, 0, s>>>(a);
+            if (zone) count_launch(), k_zone_unions<<<blocks, 128, 0, s>>>(a);
+        }
     } else {
-        count_launch(), k_narrow_filter<false><<<blocks, block, 0, s>>>(a, max_pairs);
-        count_launch(), k_subtests<false, false><<<sblocks, 128, 0, s>>>(a);
-        count_launch(), k_subtests<false, true><<<sblocks, 128, 0, s>>>(a);
+        if (parts & kSplitFilter) count_launch(), k_narrow_filter<false><<<blocks, block, 0, s>>>(a, max_pairs);
+        if (parts & kSplitSubtests) {
+            count_launch(), k_subtests<false, false><<<sblocks, 128, 0, s>>>(a);
+            count_launch(), k_subtests<false, true><<<sblocks, 128, 0, s>>>(a);
+        }
     }
 }
 

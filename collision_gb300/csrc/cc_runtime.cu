@@ -34,10 +34,19 @@ using namespace ccg;
 namespace {
 
 // Stages timed by cc_set_profiling / cc_get_profile.
+// In mixed-precision CCD passes of the host loop, narrow_ccd is the
+// per-pair FP32 filter stage and ccd_subtests the FP64 sub-tests after it.
+// With profiling level 2 the loop graph's passes are split into the loop_*
+// stages by boundary kernels reading the global timer (events cannot be
+// recorded inside a graph's loop body).
 enum Stage { kStInit, kStBoxes, kStBvh, kStTraverse, kStNarrowProx, kStNarrowCcd, kStApply, kStZone,
-             kStFinalize, kStStrain, kStLoop, kNumStages };
+             kStFinalize, kStStrain, kStLoop, kStSubtests, kStLoopPlan, kStLoopBoxes, kStLoopRefit,
+             kStLoopTraverse, kStLoopFilter, kStLoopSubtests, kStLoopApply, kStLoopZone, kStLoopEnd, kNumStages };
 const char* kStageNames[kNumStages] = {"init", "leaf_boxes", "bvh_build", "traverse", "narrow_prox",
-                                       "narrow_ccd", "apply", "zone", "finalize", "strain", "detect_loop"};
+                                       "narrow_ccd", "apply", "zone", "finalize", "strain", "detect_loop",
+                                       "ccd_subtests", "loop_plan", "loop_boxes", "loop_refit", "loop_traverse",
+                                       "loop_filter", "loop_subtests", "loop_apply", "loop_zone", "loop_end"};
+constexpr int kNumLoopMarks = kNumStages - kStLoopPlan;
 
 constexpr int kMaxSceneElems = (1 << 22) - 1;  // leaf ranks fill 22 bits of a contribution key
 constexpr long long kMaxTotal = 1ll << 28;     // points and elements over all scenes
@@ -398,6 +407,11 @@ struct cc_solver {
 
     // per-stage GPU time, measured with events on the solver's stream
     bool profiling = false;
+    bool loop_marks = false;                   // profiling level 2: stage marks inside the loop graph
+    unsigned long long* d_marks = nullptr;     // 1 + 2 * kNumLoopMarks
+    void mark(int slot, cudaStream_t on) {
+        if (loop_marks && d_marks) stage_mark(d_marks, slot, on);
+    }
     std::vector<cudaEvent_t> ev_pool;
     std::vector<std::pair<int, int>> ev_marks;  // (stage, event index of its start; end = start+1)
     double stage_ms[kNumStages] = {0};
@@ -506,6 +520,7 @@ struct cc_solver {
         if (device >= 0) cudaSetDevice(device);
         release_mesh();
         dfree(d_ctr);
+        dfree(d_marks);
         if (h_ctr) cudaFreeHost(h_ctr);
         h_ctr = nullptr;
         for (auto e : ev_pool) cudaEventDestroy(e);
@@ -1483,27 +1498,38 @@ cc_status cc_solver::build_loop_graph(int n_hier) {
     lb.sub = d_act_l;
     lb.nsub = ne;
     lb.dnsub = &d_loop->nbroad;
+    const int m0 = kStLoopPlan - 1;  // mark slot of stage st: st - m0
+    mark(0, cs);
     loop_plan(d_ctl, d_run, d_scenes, nscenes, d_loop, sel, eoff, poff, h_zone, cs);
     loop_expand(sel, eoff, poff, d_scenes, d_ctl, d_loop, ne + nv, d_act_e, d_act_l, d_act_p, cs);
+    mark(kStLoopPlan - m0, cs);
     leaf_boxes(d_ev, d_act_e, ne, d_escene, d_scenes, nscenes, d_xo, d_av, 1, d_box, bvh.bbox_enc, cs,
                &d_loop->nbroad);
     tree_check(d_run, nscenes, bvh.bbox_enc, d_tree_vol, d_tree_built + nscenes, 1, d_rebuild, d_loop, cs);
     loop_reset(d_ctr, d_run, nscenes, d_loop, cs);
+    mark(kStLoopBoxes - m0, cs);
     bvh_refit(d_box, lb, cs);
     if (mode == 1)
         point_boxes(d_xo, d_av, d_vscene, d_scenes, d_act_p, nv, 1, d_pbox_lo, d_pbox_hi, d_p32, d_v32, cs,
                     &d_loop->npts);
+    mark(kStLoopRefit - m0, cs);
     // the full traversal (first CCD pass) or the pruned one (later passes)
     lb.dnq = &d_loop->nq_full;
     bvh_pairs(d_box, lb, d_pairs, pair_cap, d_ctr, cs, d_ev, tune.traverse_block, nullptr, false, tune.rope_traverse,
               tune.traverse_refill, tune.stack_depth);
     pruned_pairs(lb, d_act_e, d_act_l, d_pstamp, d_loop, d_edirty, d_query, ne, d_pairs, pair_cap, d_ctr, d_ev, cs);
+    mark(kStLoopTraverse - m0, cs);
     NarrowArgs a = narrow_args(1, false);
     a.ps = loop_stamp();
-    if (mode == 1 && split_narrow)
-        narrow_pass_split(a, 1, pair_cap, cs, tune.narrow_block, true);
-    else
+    if (mode == 1 && split_narrow) {
+        narrow_pass_split(a, 1, pair_cap, cs, tune.narrow_block, true, kSplitFilter);
+        mark(kStLoopFilter - m0, cs);
+        narrow_pass_split(a, 1, pair_cap, cs, tune.narrow_block, true, kSplitSubtests);
+        mark(kStLoopSubtests - m0, cs);
+    } else {
         narrow_pass(a, 1, pair_cap, cs, tune.narrow_block);
+        mark(kStLoopSubtests - m0, cs);
+    }
     ApplyBufs ab = apply;
     ab.ps = loop_stamp();
     apply_contribs(d_contrib, d_ctr, contrib_cap, nv, d_av, d_hc, ab, cs, nullptr,
@@ -1511,6 +1537,7 @@ cc_status cc_solver::build_loop_graph(int n_hier) {
     if (!bodies.empty())
         zone_solve(d_body_members, d_body_zone_off, (int)bodies.size(), d_fixed, d_xo, d_av, d_vscene, d_scenes, d_ctr,
                    cs, d_run, loop_stamp());
+    mark(kStLoopApply - m0, cs);
     const long long l1 = g_kernel_launches;
     // the impact-zone stage, only in passes with a scene in that mode
     cudaStreamCaptureStatus cst;
@@ -1534,11 +1561,13 @@ cc_status cc_solver::build_loop_graph(int n_hier) {
     if (e == cudaSuccess) {
         zone_pass(zb, d_ctr, d_fixed, d_act_p, nv, &d_loop->npts, d_vscene, d_run, d_scenes, d_av, d_xo, cap_stream2,
                   loop_stamp());
+        mark(kStLoopZone - m0, cap_stream2);
         cudaGraph_t zg = nullptr;
         e = cudaStreamEndCapture(cap_stream2, &zg);
     }
     const long long l2 = g_kernel_launches;
     pass_end(d_ctr, d_ctl, d_run, nscenes, d_loop, 0, true, h_loop_c, cs);
+    mark(kStLoopEnd - m0, cs);
     cudaGraph_t bg = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(cs, &bg);
     lg.body_launches = (l1 - l0) + (g_kernel_launches - l2);
@@ -1780,14 +1809,24 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
         a.pair_hit = d_pair_hit;
         a.pairq = d_pairq;
         a.static_only = combined ? 1 : 0;
-        prof(moving ? kStNarrowCcd : kStNarrowProx, true);
         // mixed passes without recording run in stages: per-pair FP32
         // filters, the surviving FP64 sub-tests densely, then the zone unions
-        if (mode == 1 && !record && split_narrow)
-            narrow_pass_split(a, moving, pair_cap, stream, tune.narrow_block, any_zone);
-        else
-            narrow_pass(a, moving, pair_cap, stream, tune.narrow_block);
-        prof(moving ? kStNarrowCcd : kStNarrowProx, false);
+        const bool split = mode == 1 && !record && split_narrow;
+        if (split && moving && profiling) {
+            prof(kStNarrowCcd, true);
+            narrow_pass_split(a, moving, pair_cap, stream, tune.narrow_block, any_zone, kSplitFilter);
+            prof(kStNarrowCcd, false);
+            prof(kStSubtests, true);
+            narrow_pass_split(a, moving, pair_cap, stream, tune.narrow_block, any_zone, kSplitSubtests);
+            prof(kStSubtests, false);
+        } else {
+            prof(moving ? kStNarrowCcd : kStNarrowProx, true);
+            if (split)
+                narrow_pass_split(a, moving, pair_cap, stream, tune.narrow_block, any_zone);
+            else
+                narrow_pass(a, moving, pair_cap, stream, tune.narrow_block);
+            prof(moving ? kStNarrowCcd : kStNarrowProx, false);
+        }
         prof(kStApply, true);
         apply_contribs(d_contrib, d_ctr, contrib_cap, nv, d_av, d_hc, apply, stream, dump ? d_dump : nullptr,
                        bodies.empty() ? nullptr : &body_bufs);
@@ -2746,8 +2785,23 @@ cc_status cc_set_mode(cc_solver* s, int mode) {
 }
 
 cc_status cc_set_profiling(cc_solver* s, int on) {
-    if (!s) return CC_BAD_INPUT;
+    if (!s || on < 0 || on > 2) return CC_BAD_INPUT;
     s->profiling = on != 0;
+    const bool marks = on == 2;
+    if (marks != s->loop_marks) s->loop_dirty = true;  // the loop graph holds the marks or not
+    s->loop_marks = marks;
+    if (marks && !s->d_marks) {
+        cudaSetDevice(s->device);
+        if (cudaMalloc(&s->d_marks, sizeof(unsigned long long) * (1 + 2 * kNumLoopMarks)) != cudaSuccess) {
+            s->d_marks = nullptr;
+            s->loop_marks = false;
+            return s->fail(CC_NO_MEMORY, "stage marks");
+        }
+    }
+    if (s->d_marks) {
+        cudaSetDevice(s->device);
+        cudaMemsetAsync(s->d_marks, 0, sizeof(unsigned long long) * (1 + 2 * kNumLoopMarks), s->stream);
+    }
     for (int i = 0; i < kNumStages; ++i) {
         s->stage_ms[i] = 0.0;
         s->stage_calls[i] = 0;
@@ -2757,6 +2811,16 @@ cc_status cc_set_profiling(cc_solver* s, int on) {
 
 int cc_get_profile(cc_solver* s, double* ms, long long* calls, int cap) {
     if (!s) return -1;
+    if (s->loop_marks && s->d_marks) {
+        unsigned long long h[1 + 2 * kNumLoopMarks];
+        cudaSetDevice(s->device);
+        cudaMemcpyAsync(h, s->d_marks, sizeof(h), cudaMemcpyDeviceToHost, s->stream);
+        if (cudaStreamSynchronize(s->stream) == cudaSuccess)
+            for (int k = 0; k < kNumLoopMarks; ++k) {
+                s->stage_ms[kStLoopPlan + k] = (double)h[1 + 2 * k] * 1e-6;
+                s->stage_calls[kStLoopPlan + k] = (long long)h[2 + 2 * k];
+            }
+    }
     for (int i = 0; i < kNumStages && i < cap; ++i) {
         if (ms) ms[i] = s->stage_ms[i];
         if (calls) calls[i] = s->stage_calls[i];

@@ -330,8 +330,10 @@ class CollisionSolver3d:
         """Shared-memory window for the strain sweep (default) or global memory."""
         self._check(self._lib.cc_set_strain_window(self._h, int(bool(on))))
 
-    def setProfiling(self, on: bool):
-        self._check(self._lib.cc_set_profiling(self._h, int(bool(on))))
+    def setProfiling(self, on):
+        """Stage timing: True/1 outside the device loop's graph, 2 also per
+        stage inside it, False/0 off."""
+        self._check(self._lib.cc_set_profiling(self._h, int(on)))
 
     def profile(self) -> dict:
         ms = (C.c_double * 32)()

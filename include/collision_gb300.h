@@ -392,7 +392,10 @@ cc_status cc_set_stream(cc_solver* s, void* stream);
 /* Per-stage GPU time of the following steps, measured with CUDA events on
  * the solver's stream: cc_get_profile writes accumulated milliseconds and
  * call counts per stage (names from cc_profile_stage_name) and returns the
- * number of stages. */
+ * number of stages. on = 1: stages outside the device loop's graph (that
+ * graph counts as one stage, detect_loop); on = 2: also the stages of every
+ * pass inside it (loop_*), from boundary kernels that read the global timer
+ * (a few launches per pass more); 0: off. */
 cc_status cc_set_profiling(cc_solver* s, int on);
 int cc_get_profile(cc_solver* s, double* ms, long long* calls, int cap);
 const char* cc_profile_stage_name(int i);

@@ -462,3 +462,29 @@ def test_device_loop_equals_host_loop(solver_cls, mode):
             assert u["counters"]["loop_passes"] > 0 and w["counters"]["loop_passes"] == 0, k
         if cap is not None:
             assert zone_steps > 0 and capped > 0
+
+
+def test_loop_stage_marks_change_nothing(solver_cls):
+    # profiling level 2 puts boundary kernels between the stages of every
+    # pass of the loop graph; results are unchanged and every pass is split
+    mix = _contact_sample()
+    ref, _, _ = _run_batch(solver_cls, mix, 3, mode=1)
+    b = solver_cls(0)
+    b.assembleBatch(mix)
+    b.setMode(1)
+    b.setProfiling(2)
+    x = np.concatenate([s.x for s in mix])
+    v = np.concatenate([s.v for s in mix])
+    hc = np.zeros(len(x), np.uint8)
+    dt = np.concatenate([np.full(s.nv, s.params["dt"]) for s in mix])[:, None]
+    for r in ref:
+        xo, vo, ho, hcol = b.resolveCollisionBatch(x, x + dt * v, v, hc)
+        assert np.array_equal(xo, r["x"]) and np.array_equal(vo, r["v"]) and np.array_equal(ho, r["hc"])
+        x, v, hc = xo, vo, ho
+    prof = b.profile()
+    loop_passes = sum(r["counters"]["loop_passes"] for r in ref)
+    assert loop_passes > 0
+    assert prof["loop_traverse"][1] == prof["loop_end"][1] >= loop_passes
+    loop_ms = sum(prof[k][0] for k in prof if k.startswith("loop_"))
+    assert 0 < loop_ms <= prof["detect_loop"][0] * 1.05
+    b.close()
