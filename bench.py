@@ -566,10 +566,23 @@ def run_gpu(args):
                 st["x"], st["xo"] = st["xo"], st["x"]
             stream.synchronize()
         prof = s.profile()
+        kprof = None
+        if args.kernel_steps > 0:
+            # untimed, after the timed steps: mixed-precision steps with every
+            # pass's stages timed inside the loop graph too
+            s.setMode(1)
+            s.setProfiling(2)
+            with torch.cuda.stream(stream):
+                for _ in range(args.kernel_steps):
+                    candidate(st)
+                    s.resolveCollisionBatchDevice(st["x"], st["xc"], st["v"], st["hc"], st["xo"])
+                    st["x"], st["xo"] = st["xo"], st["x"]
+                stream.synchronize()
+            kprof = {k: round(v[0] / args.kernel_steps, 3) for k, v in s.profile().items() if v[0]}
         s.close()
         tree_us += sum(c["tree_build_us"] for c in counters)
         return dict(mixed_ms=max_over_ranks(ms[1]), plain_ms=max_over_ranks(ms[0]), same=same, tuned=tuned,
-                    counters=counters, prof=prof, clocks=clk.summary(), tree_s=tree_us / 1e6)
+                    counters=counters, prof=prof, clocks=clk.summary(), tree_s=tree_us / 1e6, kprof=kprof)
 
     # ------------------------------------- CPU baseline (rank 0, first)
     # The oracle steps the CPU sample of the scenes from the initial state
@@ -606,7 +619,8 @@ def run_gpu(args):
                     "approach_steps": args.approach,
                     "tree_build_s": pair["tree_s"], "tree_builds_per_timed_step": tot["tree_builds"] / K,
                     "zone_cap": args.zone_cap, "clocks": pair["clocks"], "counters": tot,
-                    "stages_ms": {k: round(v[0], 3) for k, v in pair["prof"].items()}}
+                    "stages_ms": {k: round(v[0], 3) for k, v in pair["prof"].items()},
+                    "stages_ms_per_mixed_step": pair["kprof"]}
             print(json.dumps(line), flush=True)
         if ws > 1:
             torch.distributed.destroy_process_group()
@@ -758,6 +772,12 @@ def run_gpu(args):
             "gpu_launches": int(launches),
             "step_ms_quantiles": [round(float(q), 3) for q in np.quantile(mixed["step_ms"], [0, .25, .5, .75, 1])],
             "counters": tot, "stages_ms": {k: round(v[0], 3) for k, v in prof.items()}}
+    if mixed["kprof"]:
+        kp = mixed["kprof"]
+        line["stages_ms_per_step_after"] = {
+            "steps": kp["steps"], "what": "untimed steps after the timed ones, every pass's stages timed "
+                                          "(inside the loop graph by global-timer boundary kernels)",
+            "ms": {k: round(v[0] / kp["steps"], 3) for k, v in kp["prof"].items() if v[0]}}
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()

@@ -404,6 +404,7 @@ struct cc_solver {
     bool strain_roles = true;  // window sweep: edges, copy-ins and write-backs on separate threads
     LaunchTuning tune;
     int host_threads = 0;  // tree emulation threads (0: hardware concurrency)
+    const bool pass_log = std::getenv("CC_PASS_LOG") != nullptr;
 
     // per-stage GPU time, measured with events on the solver's stream
     bool profiling = false;
@@ -1887,6 +1888,9 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
     counters[3] += h_ctr->npairs;
     // path bytes per pass: pairs written and read, per-point impulse,
     // friction and count records written and read for each contact
+    if (pass_log)  // CC_PASS_LOG: one line per host-loop pass, for matching profiler launches to passes
+        std::fprintf(stderr, "cc_pass moving=%d pairs=%d visits=%d sub_pt=%d sub_ee=%d contacts=%d\n", moving,
+                     h_ctr->npairs, h_ctr->nvisits, h_ctr->nsub_pt, h_ctr->nsub_ee, h_ctr->ncontacts);
     counters[18] += 16ll * h_ctr->npairs + 4ll * 2 * 52 * h_ctr->ncontacts;
     counters[4] += h_ctr->nvisits;
     counters[5] += h_ctr->nhit_pairs;
