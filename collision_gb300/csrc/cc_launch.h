@@ -35,6 +35,13 @@ void radix_sort_pairs(unsigned long long* keys, unsigned int* vals, int n, int b
 // (temp sized for cap; the arrays hold cap pairs).
 void radix_sort_pairs_dev(unsigned long long* keys, unsigned int* vals, const int* dn, int cap, int bits, void* temp,
                           cudaStream_t s);
+// The same with counts of up to 8192 pairs sorted by one CTA in shared
+// memory (keys below 2^51); eff: a device int the two stages share. On a
+// stream that is being captured, with `nested` (a second stream) given, the
+// general sort sits behind a conditional node and runs only for larger
+// counts. small = false: always the general sort.
+cudaError_t sort_pairs_dev(unsigned long long* keys, unsigned int* vals, const int* dn, int cap, int bits,
+                           void* temp, int* eff, cudaStream_t s, cudaStream_t nested, bool small = true);
 // Exclusive scan of n ints (out may alias in); total written to *total.
 size_t scan_temp_bytes(int n);
 void exclusive_scan(const int* in, int* out, int n, int* total, void* temp, cudaStream_t s);
@@ -309,6 +316,7 @@ struct ZoneBufs {
     int2* zone_rng = nullptr;            // per zone: its run of members
     int* zone_root = nullptr;            // per zone: its root
     int* members = nullptr;              // per point (at most one zone each)
+    bool small_sort = true;              // sorts of up to 8192 records in one CTA
 };
 size_t zone_sort_temp_bytes(int cap);
 // After a pass's impulses: join the pass's createImpZone records in the
@@ -316,9 +324,12 @@ size_t zone_sort_temp_bytes(int cap);
 // scene in that mode and move it rigidly (updateImpactZoneVelocity,
 // dcollid.cpp:290-310). act_pts / n_pts: the points of the pass's scenes
 // (null: all n_pts points; dn_pts, if given, holds the count on the device).
-void zone_pass(const ZoneBufs& z, const PassCounters* ctr, const uint8_t* fixed, const int* act_pts, int n_pts,
-               const int* dn_pts, const int* vscene, const SceneRun* run, const SceneDev* scenes, double4_32a* av,
-               const double4_32a* xo, cudaStream_t s, PassStamp ps = PassStamp{});
+// nested: a second stream for conditional sorts while s is being captured
+// (null otherwise). Returns a launch or capture error.
+cudaError_t zone_pass(const ZoneBufs& z, const PassCounters* ctr, const uint8_t* fixed, const int* act_pts, int n_pts,
+                      const int* dn_pts, const int* vscene, const SceneRun* run, const SceneDev* scenes,
+                      double4_32a* av, const double4_32a* xo, cudaStream_t s, PassStamp ps = PassStamp{},
+                      cudaStream_t nested = nullptr);
 
 // ------------------------------------------------ device detection loop
 // (cc_loop.cu) One pass of the loop: k_loop_plan picks each scene's mode and

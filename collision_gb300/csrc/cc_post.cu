@@ -790,13 +790,21 @@ struct WinRing {
     int lslot[kWindowAhead];  // slot this thread copied in, per recent level (-1: none)
 };
 
+// The level headers come from a shared-memory ring of kHdrRing levels,
+// filled kHdrAhead levels ahead with cp.async, so that the record loads that
+// depend on a header are issued without waiting on a global load.
+constexpr int kHdrRing = 64;
+constexpr int kHdrChunk = 16;                  // levels per refill, issued at levels l = 0 mod kHdrChunk
+constexpr int kHdrAhead = kHdrRing - kHdrChunk;  // a refill at level l brings levels [l + kHdrAhead, l + kHdrRing)
+
 // tid: this thread's edge of the level; tc, tw: its copy-in and write-back
 // (negative: none first-hand)
 __device__ __forceinline__ void win_fetch(WinRing& r, int j, int lk, int nlevels, int tid, int tc, int tw,
-                                          const int4* __restrict__ hdr, const StrainEdgeHot* __restrict__ hot,
+                                          const int4* s_hdr, const StrainEdgeHot* __restrict__ hot,
                                           const int2* __restrict__ load_list, const int2* __restrict__ wb_list) {
     if (lk < nlevels) {
-        int4 a = hdr[2 * lk], b = hdr[2 * lk + 1];
+        const int q = 2 * (lk % kHdrRing);
+        int4 a = s_hdr[q], b = s_hdr[q + 1];
         r.h0[j] = a;
         r.h1[j] = b;
         if (a.x + tid < a.y) r.hot[j] = hot[a.x + tid];
@@ -810,6 +818,7 @@ struct WinArgs {
     const double4_32a* xo;
     const StrainEdgeHot* hot;
     const int4* hdr;
+    int4* s_hdr;  // the header ring
     int nlevels;
     const int2* load_list;
     const int2* wb_list;
@@ -831,7 +840,15 @@ __device__ __forceinline__ void win_level(const WinArgs& A, WinRing& r, WinSlot*
     const StrainEdgeHot cur = r.hot[R];
     const int2 ld = r.ld[R], wb = r.wb[R];
     const int tc = tid - A.cbase, tw = tid - A.wbase;
-    win_fetch(r, R, l + kRing, A.nlevels, tid, tc, tw, A.hdr, A.hot, A.load_list, A.wb_list);
+    win_fetch(r, R, l + kRing, A.nlevels, tid, tc, tw, A.s_hdr, A.hot, A.load_list, A.wb_list);
+    if (J % kHdrChunk == 0 && l % kHdrChunk == 0 && l > 0) {
+        // headers of levels [l + kHdrAhead, l + kHdrRing) into the slots of
+        // levels [l - kHdrChunk, l), whose records were fetched kRing levels
+        // early and a barrier ago; they land in this level's copy group
+        const int m = l + kHdrAhead + (tid >> 1);
+        if (tid < 2 * kHdrChunk && m < A.nlevels)
+            cp_async16(&A.s_hdr[2 * (m % kHdrRing) + (tid & 1)], &A.hdr[2 * m + (tid & 1)]);
+    }
     // copy in the points whose slot opens now
     int my_slot = -1;
     if (tc >= 0 && h0.z + tc < h0.w) {
@@ -914,14 +931,19 @@ __global__ void __launch_bounds__(256) k_strain_window(const StrainEdge* __restr
     const int2 wb_final = make_int2(sd.wb_final0, sd.wb_final1);
     const double dt = sd.p.dt;
     const int tid = threadIdx.x;
-    WinArgs A{edges, xo, hot, hdr, nlevels, load_list, wb_list, av, dt, __double2float_ru(dt), multi_ld, cbase, wbase};
+    __shared__ int4 s_hdr[2 * kHdrRing];
+    for (int i = tid; i < 2 * kHdrRing && i < 2 * nlevels; i += blockDim.x) s_hdr[i] = hdr[i];
+    __syncthreads();
+    WinArgs A{edges, xo, hot, hdr, s_hdr, nlevels, load_list, wb_list, av, dt, __double2float_ru(dt), multi_ld,
+              cbase, wbase};
     int n_avg = 0, n_exact = 0;
     bool has = false;
     WinRing r;
 #pragma unroll
     for (int j = 0; j < kWindowAhead; ++j) r.lslot[j] = -1;
 #pragma unroll
-    for (int j = 0; j < kRing; ++j) win_fetch(r, j, j, nlevels, tid, tid - cbase, tid - wbase, hdr, hot, load_list, wb_list);
+    for (int j = 0; j < kRing; ++j)
+        win_fetch(r, j, j, nlevels, tid, tid - cbase, tid - wbase, s_hdr, hot, load_list, wb_list);
     for (int lb = 0; lb < nlevels; lb += kWindowAhead) {
         win_level<0>(A, r, s_win, lb + 0, tid, &n_avg, &n_exact, &has);
         if (lb + 1 < nlevels) win_level<1>(A, r, s_win, lb + 1, tid, &n_avg, &n_exact, &has);

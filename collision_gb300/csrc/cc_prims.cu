@@ -161,7 +161,119 @@ __global__ void k_radix_scatter(const unsigned long long* keys, const unsigned i
     }
 }
 
+// Small sorts in one CTA: up to kSmallSort pairs, each key extended by its
+// input position (so the keys are distinct and a bitonic network gives the
+// stable order), sorted in shared memory.
+constexpr int kSmallSort = 8192;
+constexpr int kSmallThreads = 1024;
+constexpr int kIdxBits = 13;  // 2^13 = kSmallSort
+constexpr size_t kSmallBytes = (size_t)kSmallSort * (sizeof(unsigned long long) + sizeof(unsigned int));
+
+// Sorts the first m = min(*dn, n) pairs when m <= small_max (<= kSmallSort) and sets *eff
+// to 0; otherwise leaves them and sets *eff = m. In a graph, also sets the
+// conditional handle h (if use_h) to whether the general sort must run.
+__global__ void __launch_bounds__(kSmallThreads) k_sort_small(unsigned long long* keys, unsigned int* vals,
+                                                             const int* dn, int n, int small_max, int* eff,
+                                                             cudaGraphConditionalHandle h, int use_h) {
+    extern __shared__ unsigned long long s_k[];
+    unsigned int* s_v = reinterpret_cast<unsigned int*>(s_k + kSmallSort);
+    const int m = sort_count(dn, n);
+    if (m > small_max) {
+        if (threadIdx.x == 0) {
+            *eff = m;
+            if (use_h) cudaGraphSetConditional(h, 1u);
+        }
+        return;
+    }
+    int P = 1;
+    while (P < m) P <<= 1;
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        if (i < m) {
+            s_k[i] = (keys[i] << kIdxBits) | (unsigned long long)i;
+            s_v[i] = vals[i];
+        } else {
+            s_k[i] = ~0ull;
+        }
+    }
+    __syncthreads();
+    for (int k = 2; k <= P; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < P; i += blockDim.x) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const unsigned long long a = s_k[i], b = s_k[ixj];
+                    if ((a > b) == ((i & k) == 0)) {
+                        s_k[i] = b;
+                        s_k[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const unsigned long long c = s_k[i];
+        keys[i] = c >> kIdxBits;
+        vals[i] = s_v[c & (kSmallSort - 1)];
+    }
+    if (threadIdx.x == 0) {
+        *eff = 0;
+        if (use_h) cudaGraphSetConditional(h, 0u);
+    }
+}
+
 }  // namespace
+
+cudaError_t sort_pairs_dev(unsigned long long* keys, unsigned int* vals, const int* dn, int cap, int bits,
+                           void* temp, int* eff, cudaStream_t s, cudaStream_t nested, bool small) {
+    const int small_max = small ? kSmallSort : -1;
+    if (cap <= 1 || bits <= 0) return cudaSuccess;
+    if (bits > 64 - kIdxBits) {
+        radix_sort_pairs_dev(keys, vals, dn, cap, bits, temp, s);
+        return cudaGetLastError();
+    }
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_sort_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kSmallBytes);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(s, &cst);
+    if (e != cudaSuccess) return e;
+    if (cst != cudaStreamCaptureStatusActive || !nested) {
+        count_launch(), k_sort_small<<<1, kSmallThreads, kSmallBytes, s>>>(keys, vals, dn, cap, small_max, eff, 0, 0);
+        radix_sort_pairs_dev(keys, vals, eff, cap, bits, temp, s);
+        return cudaGetLastError();
+    }
+    // in a graph: the general sort behind an IF node that the small sort sets
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    e = cudaStreamGetCaptureInfo(s, &cst, nullptr, &g, &deps, nullptr, &ndeps);
+    cudaGraphConditionalHandle h;
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return e;
+    count_launch(), k_sort_small<<<1, kSmallThreads, kSmallBytes, s>>>(keys, vals, dn, cap, small_max, eff, h, 1);
+    e = cudaStreamGetCaptureInfo(s, &cst, nullptr, &g, &deps, nullptr, &ndeps);
+    cudaGraphNodeParams ip = {};
+    cudaGraphNode_t node;
+    if (e == cudaSuccess) {
+        ip.type = cudaGraphNodeTypeConditional;
+        ip.conditional.handle = h;
+        ip.conditional.type = cudaGraphCondTypeIf;
+        ip.conditional.size = 1;
+        e = cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &ip);
+    }
+    if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e == cudaSuccess)
+        e = cudaStreamBeginCaptureToGraph(nested, ip.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    radix_sort_pairs_dev(keys, vals, eff, cap, bits, temp, nested);
+    cudaGraph_t body = nullptr;
+    return cudaStreamEndCapture(nested, &body);
+}
 
 size_t scan_temp_bytes(int n) { return scan_levels_bytes(n) + 256; }
 

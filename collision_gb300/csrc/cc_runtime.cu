@@ -41,11 +41,13 @@ namespace {
 // recorded inside a graph's loop body).
 enum Stage { kStInit, kStBoxes, kStBvh, kStTraverse, kStNarrowProx, kStNarrowCcd, kStApply, kStZone,
              kStFinalize, kStStrain, kStLoop, kStSubtests, kStLoopPlan, kStLoopBoxes, kStLoopRefit,
-             kStLoopTraverse, kStLoopFilter, kStLoopSubtests, kStLoopApply, kStLoopZone, kStLoopEnd, kNumStages };
+             kStLoopTraverse, kStLoopPruned, kStLoopFilter, kStLoopSubtests, kStLoopApply, kStLoopZone, kStLoopEnd,
+             kNumStages };
 const char* kStageNames[kNumStages] = {"init", "leaf_boxes", "bvh_build", "traverse", "narrow_prox",
                                        "narrow_ccd", "apply", "zone", "finalize", "strain", "detect_loop",
                                        "ccd_subtests", "loop_plan", "loop_boxes", "loop_refit", "loop_traverse",
-                                       "loop_filter", "loop_subtests", "loop_apply", "loop_zone", "loop_end"};
+                                       "loop_pruned", "loop_filter", "loop_subtests", "loop_apply", "loop_zone",
+                                       "loop_end"};
 constexpr int kNumLoopMarks = kNumStages - kStLoopPlan;
 
 constexpr int kMaxSceneElems = (1 << 22) - 1;  // leaf ranks fill 22 bits of a contribution key
@@ -327,7 +329,7 @@ struct cc_solver {
     double* d_tree_vol_out = nullptr;
     double* h_tree_vol_out = nullptr;  // pinned
     cc_status build_trees(int which, std::vector<int>& ids, const Box6* boxes);
-    cudaStream_t cap_stream = nullptr, cap_stream2 = nullptr;  // graph capture only
+    cudaStream_t cap_stream = nullptr, cap_stream2 = nullptr, cap_stream3 = nullptr;  // graph capture only
     // One graph per arithmetic mode, each valid while the buffers and
     // settings it holds stand (gen) and for the hierarchy size it was built
     // for, so that alternating modes does not rebuild it.
@@ -468,7 +470,9 @@ struct cc_solver {
         dfree(zb.keys); dfree(zb.vals); dfree(zb.seg); dfree(zb.cc); dfree(zb.uf); dfree(zb.zone_rng);
         dfree(zb.zone_root); dfree(zb.members); dfree(d_uf0); dfree(d_cc0);
         if (zb.sort_temp) cudaFree(zb.sort_temp);
+        const bool small_sort = zb.small_sort;  // a setting, not a buffer
         zb = ZoneBufs{};
+        zb.small_sort = small_sort;
         uf_on_device = false;
         dfree(d_xold_in); dfree(d_xcand_in); dfree(d_vel); dfree(d_xout); dfree(d_hc);
         dfree(d_box); dfree(d_box_st); dfree(bvh.keys); dfree(bvh.order); dfree(bvh.range_hi);
@@ -533,7 +537,8 @@ struct cc_solver {
         tail_stream = nullptr;
         if (cap_stream) cudaStreamDestroy(cap_stream);
         if (cap_stream2) cudaStreamDestroy(cap_stream2);
-        cap_stream = cap_stream2 = nullptr;
+        if (cap_stream3) cudaStreamDestroy(cap_stream3);
+        cap_stream = cap_stream2 = cap_stream3 = nullptr;
         if (stream && own_stream) cudaStreamDestroy(stream);
         stream = nullptr;
     }
@@ -1465,7 +1470,8 @@ cc_status cc_solver::build_loop_graph(int n_hier) {
     if (lg.exec) cudaGraphExecDestroy(lg.exec);
     lg = LoopGraph{};
     if (!cap_stream && (cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking) != cudaSuccess ||
-                        cudaStreamCreateWithFlags(&cap_stream2, cudaStreamNonBlocking) != cudaSuccess))
+                        cudaStreamCreateWithFlags(&cap_stream2, cudaStreamNonBlocking) != cudaSuccess ||
+                        cudaStreamCreateWithFlags(&cap_stream3, cudaStreamNonBlocking) != cudaSuccess))
         return cuda_check("capture streams");
     cudaGraph_t g = nullptr;
     if (cudaGraphCreate(&g, 0) != cudaSuccess) return cuda_check("loop graph");
@@ -1518,8 +1524,9 @@ cc_status cc_solver::build_loop_graph(int n_hier) {
     lb.dnq = &d_loop->nq_full;
     bvh_pairs(d_box, lb, d_pairs, pair_cap, d_ctr, cs, d_ev, tune.traverse_block, nullptr, false, tune.rope_traverse,
               tune.traverse_refill, tune.stack_depth);
-    pruned_pairs(lb, d_act_e, d_act_l, d_pstamp, d_loop, d_edirty, d_query, ne, d_pairs, pair_cap, d_ctr, d_ev, cs);
     mark(kStLoopTraverse - m0, cs);
+    pruned_pairs(lb, d_act_e, d_act_l, d_pstamp, d_loop, d_edirty, d_query, ne, d_pairs, pair_cap, d_ctr, d_ev, cs);
+    mark(kStLoopPruned - m0, cs);
     NarrowArgs a = narrow_args(1, false);
     a.ps = loop_stamp();
     if (mode == 1 && split_narrow) {
@@ -1560,11 +1567,12 @@ cc_status cc_solver::build_loop_graph(int n_hier) {
         e = cudaStreamBeginCaptureToGraph(cap_stream2, ip.conditional.phGraph_out[0], nullptr, nullptr, 0,
                                           cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        zone_pass(zb, d_ctr, d_fixed, d_act_p, nv, &d_loop->npts, d_vscene, d_run, d_scenes, d_av, d_xo, cap_stream2,
-                  loop_stamp());
+        const cudaError_t ez = zone_pass(zb, d_ctr, d_fixed, d_act_p, nv, &d_loop->npts, d_vscene, d_run, d_scenes,
+                                         d_av, d_xo, cap_stream2, loop_stamp(), cap_stream3);
         mark(kStLoopZone - m0, cap_stream2);
         cudaGraph_t zg = nullptr;
         e = cudaStreamEndCapture(cap_stream2, &zg);
+        if (e == cudaSuccess) e = ez;
     }
     const long long l2 = g_kernel_launches;
     pass_end(d_ctr, d_ctl, d_run, nscenes, d_loop, 0, true, h_loop_c, cs);
@@ -1910,8 +1918,9 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
     }
     if (any_zone) {
         prof(kStZone, true);
-        zone_pass(zb, d_ctr, d_fixed, bvh.act ? d_act_p : nullptr, n_act_p, nullptr, d_vscene, d_run, d_scenes, d_av,
-                  d_xo, stream);
+        const cudaError_t ez = zone_pass(zb, d_ctr, d_fixed, bvh.act ? d_act_p : nullptr, n_act_p, nullptr, d_vscene,
+                                         d_run, d_scenes, d_av, d_xo, stream);
+        if (ez != cudaSuccess) return fail(CC_CUDA_ERROR, std::string("zone pass: ") + cudaGetErrorString(ez));
         prof(kStZone, false);
         cudaMemcpyAsync(h_ctr, d_ctr, sizeof(PassCounters), cudaMemcpyDeviceToHost, stream);
     }
@@ -2526,6 +2535,10 @@ cc_status cc_set_tuning(cc_solver* s, int knob, int value) {
         case CC_TUNE_HOST_TREE:
             s->host_tree = value != 0;
             return CC_OK;
+        case CC_TUNE_SMALL_SORT:
+            s->zb.small_sort = value != 0;
+            s->loop_dirty = true;
+            return CC_OK;
         case CC_TUNE_TRAVERSE_REFILL:
             if (value < 0 || value > 32) return CC_BAD_INPUT;
             s->tune.traverse_refill = value;
@@ -2572,6 +2585,7 @@ int cc_get_tuning(cc_solver* s, int knob) {
         case CC_TUNE_DEVICE_LOOP: return s->device_loop ? 1 : 0;
         case CC_TUNE_PRUNE: return s->prune ? 1 : 0;
         case CC_TUNE_HOST_TREE: return s->host_tree ? 1 : 0;
+        case CC_TUNE_SMALL_SORT: return s->zb.small_sort ? 1 : 0;
         case CC_TUNE_STACK_DEPTH: return s->tune.stack_depth;
         case CC_TUNE_PAIR_CAPACITY: return s->pair_cap;
         default: return -1;

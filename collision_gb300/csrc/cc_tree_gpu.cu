@@ -16,7 +16,7 @@
 // then reaches every depth at least one step after insertion e-1 and sees
 // exactly the tree the reference's insertion e sees; in one step no two
 // insertions touch the same depth. Boxes are widened on the way down (the
-// union with the new leaf's box), which gives the same doubles as the
+// union with the new leaf's box), which gives the same box as the
 // reference's bottom-up union of the children: min and max are exact.
 //
 // Leaves are nodes 0..n-1 and insertion e (e >= 1) creates node n+e-1, so
@@ -31,26 +31,57 @@ namespace {
 
 constexpr int kTreeThreads = 1024;
 
+// Box coordinates are kept as order-preserving integer keys: key(a) <
+// key(b) exactly when a < b for doubles that are not NaN, except that -0
+// orders below +0. So min and max run on the integer pipe (GB300's FP64
+// rate is a small fraction of its integer rate), and containment is six
+// integer compares. Where the reference's std::min/std::max would keep +0
+// and the key order keeps -0, the difference is only the sign of a zero
+// coordinate, which changes no box extent, volume comparison or decision.
 struct __align__(16) TreeNode {
-    double lo[3], hi[3];
-    double vol;  // AABB::volume of the box (AABB.cpp:51-54), kept with it
+    long long lo[3], hi[3];  // keys
+    double vol;              // AABB::volume of the box (AABB.cpp:51-54), kept with it
     int left, right;
 };
 
-__device__ __forceinline__ double mn(double a, double b) { return (b < a) ? b : a; }
-__device__ __forceinline__ double mx(double a, double b) { return (a < b) ? b : a; }
+__device__ __forceinline__ long long okey(double d) {
+    const long long b = __double_as_longlong(d);
+    return b ^ ((b >> 63) & 0x7fffffffffffffffll);
+}
+__device__ __forceinline__ double odec(long long k) {
+    return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffll));
+}
+__device__ __forceinline__ long long kmin(long long a, long long b) { return b < a ? b : a; }
+__device__ __forceinline__ long long kmax(long long a, long long b) { return a < b ? b : a; }
 
 // (hi - lo) products in the reference's order, never contracted
-__device__ __forceinline__ double volume3(const double* lo, const double* hi) {
-    return __dmul_rn(__dmul_rn(__dsub_rn(hi[0], lo[0]), __dsub_rn(hi[1], lo[1])), __dsub_rn(hi[2], lo[2]));
+__device__ __forceinline__ double volume_k(const long long* lo, const long long* hi) {
+    return __dmul_rn(__dmul_rn(__dsub_rn(odec(hi[0]), odec(lo[0])), __dsub_rn(odec(hi[1]), odec(lo[1]))),
+                     __dsub_rn(odec(hi[2]), odec(lo[2])));
+}
+// the volume of the union of two boxes
+__device__ __forceinline__ double volume_union(const long long* alo, const long long* ahi, const long long* blo,
+                                               const long long* bhi) {
+    long long lo[3], hi[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        lo[d] = kmin(alo[d], blo[d]);
+        hi[d] = kmax(ahi[d], bhi[d]);
+    }
+    return volume_k(lo, hi);
+}
+__device__ __forceinline__ bool contains(const long long* olo, const long long* ohi, const long long* ilo,
+                                         const long long* ihi) {
+    return olo[0] <= ilo[0] && olo[1] <= ilo[1] && olo[2] <= ilo[2] && ihi[0] <= ohi[0] && ihi[1] <= ohi[1] &&
+           ihi[2] <= ohi[2];
 }
 
-__device__ __forceinline__ void load_node(const TreeNode* t, double* lo, double* hi, double& vol) {
-    const double2* p = reinterpret_cast<const double2*>(t);
-    const double2 a = p[0], b = p[1], c = p[2], d = p[3];
+__device__ __forceinline__ void load_node(const TreeNode* t, long long* lo, long long* hi, double& vol) {
+    const longlong2* p = reinterpret_cast<const longlong2*>(t);
+    const longlong2 a = p[0], b = p[1], c = p[2];
     lo[0] = a.x; lo[1] = a.y; lo[2] = b.x;
     hi[0] = b.y; hi[1] = c.x; hi[2] = c.y;
-    vol = d.x;
+    vol = reinterpret_cast<const double*>(t)[6];
 }
 
 __global__ void __launch_bounds__(kTreeThreads) k_tree_build(const Box6* __restrict__ boxes, const int* __restrict__ jobs,
@@ -65,10 +96,11 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_build(const Box6* __restr
         const Box6 b = boxes[e0 + e];
         TreeNode& L = nd[e];
         for (int d = 0; d < 3; ++d) {
-            L.lo[d] = b.lo[d];
-            L.hi[d] = b.hi[d];
+            L.lo[d] = okey(b.lo[d]);
+            L.hi[d] = okey(b.hi[d]);
         }
-        L.vol = volume3(b.lo, b.hi);
+        L.vol = __dmul_rn(__dmul_rn(__dsub_rn(b.hi[0], b.lo[0]), __dsub_rn(b.hi[1], b.lo[1])),
+                          __dsub_rn(b.hi[2], b.lo[2]));
         L.left = L.right = -1;
         parent[e] = -1;
         count[e] = 1;
@@ -85,10 +117,10 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_build(const Box6* __restr
     if (tid == 0) {
         TreeNode& q = nd[n];
         for (int d = 0; d < 3; ++d) {
-            q.lo[d] = mn(nd[1].lo[d], nd[0].lo[d]);
-            q.hi[d] = mx(nd[1].hi[d], nd[0].hi[d]);
+            q.lo[d] = kmin(nd[1].lo[d], nd[0].lo[d]);
+            q.hi[d] = kmax(nd[1].hi[d], nd[0].hi[d]);
         }
-        q.vol = volume3(q.lo, q.hi);
+        q.vol = volume_k(q.lo, q.hi);
         q.left = 1;
         q.right = 0;
         parent[n] = -1;
@@ -98,52 +130,69 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_build(const Box6* __restr
     __syncthreads();
 
     int my_e = -1, p = -1;
-    double nlo[3], nhi[3];
+    long long nlo[3], nhi[3];
     int next = 2;  // the next insertion to start; the same in every thread
     for (;;) {
         const bool start = next < n && my_e < 0 && next % T == tid;
         if (start) {
+            // the root's box is widened here; its volume is formed at the end
             my_e = next;
             p = root;
             double v;
             load_node(&nd[my_e], nlo, nhi, v);
             TreeNode& R = nd[root];
             for (int d = 0; d < 3; ++d) {
-                R.lo[d] = mn(R.lo[d], nlo[d]);
-                R.hi[d] = mx(R.hi[d], nhi[d]);
+                R.lo[d] = kmin(R.lo[d], nlo[d]);
+                R.hi[d] = kmax(R.hi[d], nhi[d]);
             }
-            R.vol = volume3(R.lo, R.hi);
             ++count[root];
         }
         if (my_e >= 0) {
             // one level: p is an internal node on the path, its box already widened
             const int l = nd[p].left, r = nd[p].right;
-            double llo[3], lhi[3], lv, rlo[3], rhi[3], rv;
+            long long llo[3], lhi[3], rlo[3], rhi[3];
+            double lv, rv;
             load_node(&nd[l], llo, lhi, lv);
             load_node(&nd[r], rlo, rhi, rv);
-            // volume growth of each child's box by the new leaf's (AABB::merge, AABB.cpp:38-49)
-            double gl = 1.0, gr = 1.0;
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                gl = __dmul_rn(gl, __dsub_rn(mx(lhi[d], nhi[d]), mn(llo[d], nlo[d])));
-                gr = __dmul_rn(gr, __dsub_rn(mx(rhi[d], nhi[d]), mn(rlo[d], nlo[d])));
+            // the volume growth of each child's box by the new leaf's
+            // (AABB::merge, AABB.cpp:38-49); a box that holds the new leaf's
+            // does not grow (the same doubles), and a growth is never below 0
+            bool go_left, grows;
+            double gc;  // the chosen child's new volume
+            if (contains(rlo, rhi, nlo, nhi)) {
+                go_left = false;  // vdiff2 = 0 <= vdiff1
+                grows = false;
+                gc = rv;
+            } else {
+                const double gr = volume_union(rlo, rhi, nlo, nhi);
+                if (contains(llo, lhi, nlo, nhi)) {
+                    go_left = 0.0 < __dsub_rn(gr, rv);  // vdiff1 = 0
+                    grows = !go_left;
+                    gc = go_left ? lv : gr;
+                } else {
+                    const double gl = volume_union(llo, lhi, nlo, nhi);
+                    go_left = __dsub_rn(gl, lv) < __dsub_rn(gr, rv);
+                    grows = true;
+                    gc = go_left ? gl : gr;
+                }
             }
-            const bool go_left = __dsub_rn(gl, lv) < __dsub_rn(gr, rv);
             const int c = go_left ? l : r;
-            double clo[3], chi[3];
+            long long clo[3], chi[3];
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
                 clo[d] = go_left ? llo[d] : rlo[d];
                 chi[d] = go_left ? lhi[d] : rhi[d];
             }
             if (c >= n) {
-                TreeNode& C = nd[c];
+                if (grows) {
+                    TreeNode& C = nd[c];
 #pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    C.lo[d] = mn(clo[d], nlo[d]);
-                    C.hi[d] = mx(chi[d], nhi[d]);
+                    for (int d = 0; d < 3; ++d) {
+                        C.lo[d] = kmin(clo[d], nlo[d]);
+                        C.hi[d] = kmax(chi[d], nhi[d]);
+                    }
+                    C.vol = gc;
                 }
-                C.vol = go_left ? gl : gr;
                 ++count[c];
                 p = c;
             } else {
@@ -151,10 +200,10 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_build(const Box6* __restr
                 TreeNode& Q = nd[q];
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
-                    Q.lo[d] = mn(nlo[d], clo[d]);
-                    Q.hi[d] = mx(nhi[d], chi[d]);
+                    Q.lo[d] = kmin(nlo[d], clo[d]);
+                    Q.hi[d] = kmax(nhi[d], chi[d]);
                 }
-                Q.vol = volume3(Q.lo, Q.hi);
+                Q.vol = gc;  // the union of the leaf's box and the new one's
                 Q.left = my_e;
                 Q.right = c;
                 parent[q] = p;
@@ -171,7 +220,7 @@ __global__ void __launch_bounds__(kTreeThreads) k_tree_build(const Box6* __restr
     }
     if (tid == 0) {
         root_out[blockIdx.x] = root;
-        vol_out[blockIdx.x] = nd[root].vol;
+        vol_out[blockIdx.x] = volume_k(nd[root].lo, nd[root].hi);
     }
 }
 

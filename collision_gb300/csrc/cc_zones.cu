@@ -211,19 +211,23 @@ __global__ void k_zone_members(const PassCounters* ctr, const int2* __restrict__
 
 }  // namespace
 
-size_t zone_sort_temp_bytes(int cap) { return radix_sort_temp_bytes(cap); }
+// the sort's scratch, then two ints for the sorts' stage counts
+size_t zone_sort_temp_bytes(int cap) { return radix_sort_temp_bytes(cap) + 256; }
 
-void zone_pass(const ZoneBufs& z, const PassCounters* ctr_c, const uint8_t* fixed, const int* act_pts, int n_pts,
-               const int* dn_pts, const int* vscene, const SceneRun* run, const SceneDev* scenes, double4_32a* av,
-               const double4_32a* xo, cudaStream_t s, PassStamp ps) {
+cudaError_t zone_pass(const ZoneBufs& z, const PassCounters* ctr_c, const uint8_t* fixed, const int* act_pts,
+                      int n_pts, const int* dn_pts, const int* vscene, const SceneRun* run, const SceneDev* scenes,
+                      double4_32a* av, const double4_32a* xo, cudaStream_t s, PassStamp ps, cudaStream_t nested) {
     PassCounters* ctr = const_cast<PassCounters*>(ctr_c);
     const int cap = z.cap;
+    int* eff = reinterpret_cast<int*>(static_cast<char*>(z.sort_temp) + radix_sort_temp_bytes(cap));
     const int blocks = nblk(cap, 256) < 152 * 8 ? nblk(cap, 256) : 152 * 8;
     count_launch(), k_cc_union<<<blocks, 256, 0, s>>>(z.rec, ctr, cap, fixed, z.cc);
     count_launch(), k_union_keys<<<blocks, 256, 0, s>>>(z.rec, ctr, cap, z.keys, z.vals);
-    radix_sort_pairs_dev(z.keys, z.vals, &ctr->nunion, cap, 48, z.sort_temp, s);
+    cudaError_t e = sort_pairs_dev(z.keys, z.vals, &ctr->nunion, cap, 48, z.sort_temp, eff, s, nested, z.small_sort);
+    if (e != cudaSuccess) return e;
     count_launch(), k_union_labels<<<blocks, 256, 0, s>>>(z.rec, ctr, cap, fixed, z.cc, z.vals, z.keys);
-    radix_sort_pairs_dev(z.keys, z.vals, &ctr->nunion, cap, 31, z.sort_temp, s);
+    e = sort_pairs_dev(z.keys, z.vals, &ctr->nunion, cap, 31, z.sort_temp, eff + 1, s, nested, z.small_sort);
+    if (e != cudaSuccess) return e;
     count_launch(), k_union_segments<<<blocks, 256, 0, s>>>(z.keys, ctr, cap, z.seg);
     count_launch(), k_union_replay<<<blocks, 128, 0, s>>>(z.rec, ctr, cap, z.keys, z.vals, z.seg, fixed, z.uf);
     const int pb = dn_pts ? 152 * 8 : (nblk(n_pts, 256) < 152 * 8 ? nblk(n_pts, 256) : 152 * 8);
@@ -233,6 +237,7 @@ void zone_pass(const ZoneBufs& z, const PassCounters* ctr_c, const uint8_t* fixe
     const int zb = nblk(z.zone_cap, 128) < 152 * 8 ? nblk(z.zone_cap, 128) : 152 * 8;
     count_launch(), k_zone_members<<<zb, 128, 0, s>>>(ctr, z.zone_rng, z.zone_root, z.uf, z.members);
     zone_solve_dev(z.members, z.zone_rng, &ctr->nzones, z.zone_cap, fixed, xo, av, vscene, scenes, ctr, s, ps);
+    return cudaGetLastError();
 }
 
 }  // namespace ccg

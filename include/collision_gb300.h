@@ -273,6 +273,10 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
  *                           built on the GPU (the insertions pipelined, one
  *                           CTA per tree); 1: on host threads, one tree per
  *                           thread. Same ranks and volumes
+ *   CC_TUNE_SMALL_SORT      1 (default): an impact-zone pass sorts up to
+ *                           8,192 union records in one CTA (in the device
+ *                           loop the general radix sort then does not run);
+ *                           0: always the general sort. Same results
  * cc_get_tuning returns the current value, or -1 for an unknown knob. */
 enum {
     CC_TUNE_SPLIT_NARROW = 0,
@@ -292,7 +296,8 @@ enum {
     CC_TUNE_PAIR_CAPACITY = 14,
     CC_TUNE_DEVICE_LOOP = 15,
     CC_TUNE_PRUNE = 16,
-    CC_TUNE_HOST_TREE = 17
+    CC_TUNE_HOST_TREE = 17,
+    CC_TUNE_SMALL_SORT = 18
 };
 cc_status cc_set_tuning(cc_solver* s, int knob, int value);
 int cc_get_tuning(cc_solver* s, int knob);

@@ -55,10 +55,11 @@ def _split(a, off, i):
 
 def _run_batch(solver_cls, mix, nsteps, mode=0, window=True, record=False, split=True, graph=True, combined=True,
                warp=False, packet=False, roles=True, overlap=False, rope=True, subset_refit=True, device_loop=True,
-               refill=8, zone_cap=None, pair_capacity=None):
+               refill=8, zone_cap=None, pair_capacity=None, small_sort=True):
     b = solver_cls(0)
     b.assembleBatch(mix)
     b.setMode(mode)
+    b.setTuning(solver_cls.TUNE_SMALL_SORT, int(small_sort))
     if pair_capacity is not None:
         b.setTuning(solver_cls.TUNE_PAIR_CAPACITY, pair_capacity)
     b.setTuning(solver_cls.TUNE_DEVICE_LOOP, int(device_loop))
@@ -440,9 +441,13 @@ def test_device_loop_equals_host_loop(solver_cls, mode):
     above and on contact-heavy cloth scenes with impact-zone passes, a capped
     zone loop included."""
     # the last case starts with a pair buffer far too small, so that passes
-    # stop after their narrow phase has run, grow the buffer and run again
-    for mix, cap, pc in ((_mix(), None, None), (_contact_sample(), 3, None), (_contact_sample(), 3, 4096)):
-        a, pv, _ = _run_batch(solver_cls, mix, 10, mode=mode, device_loop=True, zone_cap=cap, pair_capacity=pc)
+    # stop after their narrow phase has run, grow the buffer and run again,
+    # and sorts its union records with the general sort (behind the graph's
+    # conditional node) instead of the one-CTA sort
+    for mix, cap, pc, small in ((_mix(), None, None, True), (_contact_sample(), 3, None, True),
+                                (_contact_sample(), 3, 4096, False)):
+        a, pv, _ = _run_batch(solver_cls, mix, 10, mode=mode, device_loop=True, zone_cap=cap, pair_capacity=pc,
+                              small_sort=small)
         b, _, _ = _run_batch(solver_cls, mix, 10, mode=mode, device_loop=False, zone_cap=cap)
         zone_steps = capped = 0
         for k, (u, w) in enumerate(zip(a, b)):
