@@ -185,7 +185,8 @@ struct PassCounters {
 enum LoopHost { kHostRebuild = 1, kHostRetry = 2, kHostFatal = 4 };
 enum LoopAcc {
     kAccPasses, kAccCcd, kAccZone, kAccPairs, kAccVisits, kAccHits, kAccContacts, kAccSub, kAccMovingVisits,
-    kAccCr, kAccLeaves, kAccBroadPairs, kAccPathBytes, kAccZonePasses, kAccIters, kAccProxPairs, kNumAcc
+    kAccCr, kAccLeaves, kAccBroadPairs, kAccPathBytes, kAccZonePasses, kAccIters, kAccProxPairs, kAccQueries,
+    kAccUnions, kNumAcc
 };
 struct LoopCtl {
     int host;       // LoopHost bits: the loop stopped for the host

@@ -325,11 +325,13 @@ size_t zone_sort_temp_bytes(int cap);
 // dcollid.cpp:290-310). act_pts / n_pts: the points of the pass's scenes
 // (null: all n_pts points; dn_pts, if given, holds the count on the device).
 // nested: a second stream for conditional sorts while s is being captured
-// (null otherwise). Returns a launch or capture error.
+// (null otherwise); marks (may be null): stage boundaries after the sorts,
+// the replay, the zone lists and the solve go to slots mark0..mark0+3
+// (stage_mark). Returns a launch or capture error.
 cudaError_t zone_pass(const ZoneBufs& z, const PassCounters* ctr, const uint8_t* fixed, const int* act_pts, int n_pts,
                       const int* dn_pts, const int* vscene, const SceneRun* run, const SceneDev* scenes,
                       double4_32a* av, const double4_32a* xo, cudaStream_t s, PassStamp ps = PassStamp{},
-                      cudaStream_t nested = nullptr);
+                      cudaStream_t nested = nullptr, unsigned long long* marks = nullptr, int mark0 = 0);
 
 // ------------------------------------------------ device detection loop
 // (cc_loop.cu) One pass of the loop: k_loop_plan picks each scene's mode and

@@ -278,6 +278,8 @@ __global__ void __launch_bounds__(kPlanThreads) k_pass_end(const PassCounters* _
             a[kAccSub] += (unsigned)c->nsub;
             a[kAccCr] += (unsigned)c->ncr;
             a[kAccZonePasses] += L->any_zone ? 1u : 0u;
+            a[kAccQueries] += L->prune ? (unsigned)L->nquery : 0u;
+            a[kAccUnions] += L->any_zone ? (unsigned)c->nunion : 0u;
             a[kAccIters] += 1;
             if (in_graph) a[kAccMovingVisits] += (unsigned)c->nvisits;
             // path bytes per pass: pairs written and read, per-point impulse,

@@ -41,18 +41,19 @@ namespace {
 // recorded inside a graph's loop body).
 enum Stage { kStInit, kStBoxes, kStBvh, kStTraverse, kStNarrowProx, kStNarrowCcd, kStApply, kStZone,
              kStFinalize, kStStrain, kStLoop, kStSubtests, kStLoopPlan, kStLoopBoxes, kStLoopRefit,
-             kStLoopTraverse, kStLoopPruned, kStLoopFilter, kStLoopSubtests, kStLoopApply, kStLoopZone, kStLoopEnd,
-             kNumStages };
+             kStLoopTraverse, kStLoopPruned, kStLoopFilter, kStLoopSubtests, kStLoopApply, kStLoopZoneSort,
+             kStLoopZoneReplay, kStLoopZoneList, kStLoopZoneSolve, kStLoopEnd, kNumStages };
 const char* kStageNames[kNumStages] = {"init", "leaf_boxes", "bvh_build", "traverse", "narrow_prox",
                                        "narrow_ccd", "apply", "zone", "finalize", "strain", "detect_loop",
                                        "ccd_subtests", "loop_plan", "loop_boxes", "loop_refit", "loop_traverse",
-                                       "loop_pruned", "loop_filter", "loop_subtests", "loop_apply", "loop_zone",
+                                       "loop_pruned", "loop_filter", "loop_subtests", "loop_apply",
+                                       "loop_zone_sort", "loop_zone_replay", "loop_zone_list", "loop_zone_solve",
                                        "loop_end"};
 constexpr int kNumLoopMarks = kNumStages - kStLoopPlan;
 
 constexpr int kMaxSceneElems = (1 << 22) - 1;  // leaf ranks fill 22 bits of a contribution key
 constexpr long long kMaxTotal = 1ll << 28;     // points and elements over all scenes
-constexpr int kNumCounters = 23;
+constexpr int kNumCounters = 25;
 constexpr int kErrIndex = kErrIndexNode | kErrIndexLeaf | kErrIndexElem;
 std::string index_error(int e) {
     std::string m = "broad phase met an index out of range:";
@@ -1568,8 +1569,8 @@ cc_status cc_solver::build_loop_graph(int n_hier) {
                                           cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
         const cudaError_t ez = zone_pass(zb, d_ctr, d_fixed, d_act_p, nv, &d_loop->npts, d_vscene, d_run, d_scenes,
-                                         d_av, d_xo, cap_stream2, loop_stamp(), cap_stream3);
-        mark(kStLoopZone - m0, cap_stream2);
+                                         d_av, d_xo, cap_stream2, loop_stamp(), cap_stream3,
+                                         loop_marks ? d_marks : nullptr, kStLoopZoneSort - m0);
         cudaGraph_t zg = nullptr;
         e = cudaStreamEndCapture(cap_stream2, &zg);
         if (e == cudaSuccess) e = ez;
@@ -1709,6 +1710,8 @@ cc_status cc_solver::device_passes(std::string& capped) {
     counters[18] += (long long)a[kAccPathBytes];
     counters[19] += n_hier;
     counters[20] += (long long)a[kAccProxPairs];
+    counters[23] += (long long)a[kAccQueries];
+    counters[24] += (long long)a[kAccUnions];
     const long long loop_iters = (long long)a[kAccIters] - 1;
     counters[21] += loop_iters;
     count_launch((int)(lgraph->body_launches * (loop_iters + graph_runs) +

@@ -216,7 +216,8 @@ size_t zone_sort_temp_bytes(int cap) { return radix_sort_temp_bytes(cap) + 256; 
 
 cudaError_t zone_pass(const ZoneBufs& z, const PassCounters* ctr_c, const uint8_t* fixed, const int* act_pts,
                       int n_pts, const int* dn_pts, const int* vscene, const SceneRun* run, const SceneDev* scenes,
-                      double4_32a* av, const double4_32a* xo, cudaStream_t s, PassStamp ps, cudaStream_t nested) {
+                      double4_32a* av, const double4_32a* xo, cudaStream_t s, PassStamp ps, cudaStream_t nested,
+                      unsigned long long* marks, int mark0) {
     PassCounters* ctr = const_cast<PassCounters*>(ctr_c);
     const int cap = z.cap;
     int* eff = reinterpret_cast<int*>(static_cast<char*>(z.sort_temp) + radix_sort_temp_bytes(cap));
@@ -228,15 +229,19 @@ cudaError_t zone_pass(const ZoneBufs& z, const PassCounters* ctr_c, const uint8_
     count_launch(), k_union_labels<<<blocks, 256, 0, s>>>(z.rec, ctr, cap, fixed, z.cc, z.vals, z.keys);
     e = sort_pairs_dev(z.keys, z.vals, &ctr->nunion, cap, 31, z.sort_temp, eff + 1, s, nested, z.small_sort);
     if (e != cudaSuccess) return e;
+    if (marks) stage_mark(marks, mark0, s);
     count_launch(), k_union_segments<<<blocks, 256, 0, s>>>(z.keys, ctr, cap, z.seg);
     count_launch(), k_union_replay<<<blocks, 128, 0, s>>>(z.rec, ctr, cap, z.keys, z.vals, z.seg, fixed, z.uf);
+    if (marks) stage_mark(marks, mark0 + 1, s);
     const int pb = dn_pts ? 152 * 8 : (nblk(n_pts, 256) < 152 * 8 ? nblk(n_pts, 256) : 152 * 8);
     if (pb > 0)
         count_launch(), k_zone_enum<<<pb, 256, 0, s>>>(act_pts, n_pts, dn_pts, vscene, run, z.uf, ctr, z.zone_rng,
                                                        z.zone_root);
     const int zb = nblk(z.zone_cap, 128) < 152 * 8 ? nblk(z.zone_cap, 128) : 152 * 8;
     count_launch(), k_zone_members<<<zb, 128, 0, s>>>(ctr, z.zone_rng, z.zone_root, z.uf, z.members);
+    if (marks) stage_mark(marks, mark0 + 2, s);
     zone_solve_dev(z.members, z.zone_rng, &ctr->nzones, z.zone_cap, fixed, xo, av, vscene, scenes, ctr, s, ps);
+    if (marks) stage_mark(marks, mark0 + 3, s);
     return cudaGetLastError();
 }
 

@@ -349,7 +349,7 @@ class CollisionSolver3d:
                      "contacts", "strain_passes", "tree_builds", "kernel_launches", "strain_averaged",
                      "strain_exact", "fp64_subtests", "moving_visits", "strain_bytes", "cr_roots", "broad_leaves",
                      "broad_pairs", "path_bytes", "timed_traverse_leaves", "timed_traverse_pairs", "loop_passes",
-                     "tree_build_us")
+                     "tree_build_us", "pruned_queries", "zone_unions")
 
     def counters(self) -> dict:
         n_all = len(self.COUNTER_NAMES)

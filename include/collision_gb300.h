@@ -351,9 +351,11 @@ cc_status cc_set_strain_window(cc_solver* s, int on);
  * traversals wrote, the step's algorithmic bytes (below), the leaves and
  * pairs of the traversals launched from the host (those the "traverse" stage
  * of cc_get_profile times: every traversal in the host loop, the proximity
- * pass's with CC_TUNE_DEVICE_LOOP), the passes the device loop ran, and
- * the host time spent emulating the reference trees' insertion order
- * (microseconds).
+ * pass's with CC_TUNE_DEVICE_LOOP), the passes the device loop ran, the
+ * time spent building the reference trees' leaf order (microseconds, the
+ * build on the GPU or its emulation on host threads, with the copies and
+ * synchronisation around it), the queries of the device loop's pruned
+ * traversals, and the union records of impact-zone passes.
  * Algorithmic bytes: per scene-step 120 per
  * point (x_old, x_cand, v read; x, v written); per scene-pass 72 per point,
  * 12 per triangle, 8 per bond and 48 per hierarchy node (2E-1 nodes of
