@@ -947,6 +947,120 @@ __global__ void k_traverse_rope_full(int n, const RopeNode* __restrict__ rn, con
     }
 }
 
+// The pruned traversal with one warp per dirty element: the walk from the
+// scene's root keeps its pending nodes in a shared-memory stack, and each
+// round the lanes take up to 32 of them at once, test both children of each
+// (the node record holds their FP32 boxes), test the overlapping leaves
+// exactly and push the overlapping internal children. A walk then takes
+// about as many rounds as the tree is deep, instead of one dependent load
+// per visited node. Same pairs as k_traverse_rope_full.
+constexpr int kPrunedWarps = 4;     // warps per block
+constexpr int kWarpStack = 2048;    // pending nodes per warp
+
+__global__ void __launch_bounds__(kPrunedWarps * 32) k_traverse_warp_full(
+    int n, const BvhNode32* __restrict__ node, const int* __restrict__ elem_scene, const SceneRun* __restrict__ run,
+    const int* __restrict__ ev, int2* pairs, int cap, PassCounters* ctr, const LeafRec* __restrict__ leaves,
+    const int* __restrict__ query, const LoopCtl* __restrict__ L, const uint8_t* __restrict__ edirty) {
+    __shared__ int s_stk[kPrunedWarps][kWarpStack];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int* stk = s_stk[w];
+    const int m = L->prune ? L->nquery : 0;
+    for (int t = blockIdx.x * kPrunedWarps + w; t < m; t += gridDim.x * kPrunedWarps) {
+        const int i = query[t];
+        if (i < 0 || i >= n) {
+            if (lane == 0) atomicOr(&ctr->err, kErrIndexLeaf);
+            continue;
+        }
+        const LeafRec r = leaves[i];
+        const int ei = r.e;
+        if (ei < 0) continue;  // flagged by k_leaf_records
+        const SceneRun sr = run[elem_scene[ei]];
+        if (sr.mode == kSceneIdle || sr.root < 0) continue;
+        if (sr.root >= n - 1) {
+            if (lane == 0) atomicOr(&ctr->err, kErrIndexNode);
+            continue;
+        }
+        BoxOrd qo;
+        Box6 q;
+        for (int d = 0; d < 3; ++d) {
+            qo.lo[d] = r.lo[d];
+            qo.hi[d] = r.hi[d];
+            q.lo[d] = unord_double(r.lo[d]);
+            q.hi[d] = unord_double(r.hi[d]);
+        }
+        const int pi0 = r.p[0], pi1 = r.p[1], pi2 = r.p[2];
+        const Box32 q32 = box32_out(q);
+        __syncwarp();
+        if (lane == 0) stk[0] = sr.root;
+        __syncwarp();
+        int sp = 1;  // the same in every lane
+        for (int rounds = 0; sp > 0; ++rounds) {
+            if (rounds >= 2 * n) {  // a valid hierarchy has fewer nodes than that
+                if (lane == 0) atomicOr(&ctr->err, kErrIndexNode);
+                break;
+            }
+            const int take = sp < 32 ? sp : 32;
+            const int x = lane < take ? stk[sp - take + lane] : -1;
+            __syncwarp();
+            sp -= take;
+            int push[2] = {-1, -1};
+            if (x >= 0) {
+                const float4* r4 = reinterpret_cast<const float4*>(&node[x]);
+                Box32 cb[2];
+                unpack(__ldg(r4), __ldg(r4 + 1), __ldg(r4 + 2), cb[0], cb[1]);
+                const int4 meta = __ldg(reinterpret_cast<const int4*>(r4 + 3));
+                const int cs[2] = {meta.x, meta.y};
+                for (int k = 0; k < 2; ++k) {
+                    if (!overlap32(q32, cb[k])) continue;
+                    const int c = cs[k];
+                    if (c >= 0) {
+                        if (c >= n - 1) atomicOr(&ctr->err, kErrIndexNode);
+                        else push[k] = c;
+                        continue;
+                    }
+                    const int kl = ~c;
+                    if (kl >= n) {
+                        atomicOr(&ctr->err, kErrIndexLeaf);
+                        continue;
+                    }
+                    if (kl == i) continue;
+                    const ulonglong2* lr = reinterpret_cast<const ulonglong2*>(&leaves[kl]);
+                    const ulonglong2 u0 = __ldg(lr), u1 = __ldg(lr + 1), u2 = __ldg(lr + 2);
+                    if (!(qo.lo[0] <= u1.y && qo.hi[0] >= u0.x && qo.lo[1] <= u2.x && qo.hi[1] >= u0.y &&
+                          qo.lo[2] <= u2.y && qo.hi[2] >= u1.x))
+                        continue;
+                    const int4 pe = __ldg(reinterpret_cast<const int4*>(lr + 3));
+                    const int ej = pe.w;
+                    if (ej < 0) continue;
+                    if (ev && (pe.x == pi0 || pe.x == pi1 || pe.x == pi2 || pe.y == pi0 || pe.y == pi1 ||
+                               pe.y == pi2 || (pe.z >= 0 && (pe.z == pi0 || pe.z == pi1 || pe.z == pi2))))
+                        continue;
+                    if (edirty[ej] && ej < ei) continue;  // written by ej's query
+                    emit_pair(ei, ej, pairs, cap, ctr);
+                }
+            }
+            // push the overlapping internal children (exclusive prefix over the lanes)
+            const int cnt = (push[0] >= 0) + (push[1] >= 0);
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            if (sp + total > kWarpStack) {  // the same in every lane: the walk stops with an error
+                if (lane == 0) atomicOr(&ctr->err, kErrStack);
+                break;
+            }
+            int at = sp + incl - cnt;
+            if (push[0] >= 0) stk[at++] = push[0];
+            if (push[1] >= 0) stk[at] = push[1];
+            sp += total;
+            __syncwarp();
+        }
+    }
+}
+
 __global__ void k_brute_pairs(const Box6* __restrict__ box, int n, const int* __restrict__ elem_scene, int2* pairs,
                               int cap, PassCounters* ctr) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1112,12 +1226,16 @@ void bvh_pairs(const Box6* box, const BvhBufs& b, int2* pairs, int cap, PassCoun
 
 void pruned_pairs(const BvhBufs& b, const int* act_e, const int* act_l, const unsigned* stamp, LoopCtl* L,
                   uint8_t* edirty, int* query, int ne_cap, int2* pairs, int cap, PassCounters* ctr, const int* ev,
-                  cudaStream_t s) {
+                  cudaStream_t s, bool warp) {
     if (ne_cap <= 1 || b.n <= 1) return;
     count_launch(), k_dirty_queries<<<dev_grid(ne_cap, 256), 256, 0, s>>>(act_l, b.order, b.n, b.ne_all, ev, stamp, L,
                                                                           edirty, query, ctr);
-    count_launch(), k_traverse_rope_full<<<dev_grid(ne_cap, 128), 128, 0, s>>>(
-        b.n, b.rnode, b.rope, b.elem_scene, b.run, ev, pairs, cap, ctr, b.leaf, query, L, edirty);
+    if (warp && b.node)
+        count_launch(), k_traverse_warp_full<<<dev_grid(ne_cap, kPrunedWarps), kPrunedWarps * 32, 0, s>>>(
+            b.n, b.node, b.elem_scene, b.run, ev, pairs, cap, ctr, b.leaf, query, L, edirty);
+    else
+        count_launch(), k_traverse_rope_full<<<dev_grid(ne_cap, 128), 128, 0, s>>>(
+            b.n, b.rnode, b.rope, b.elem_scene, b.run, ev, pairs, cap, ctr, b.leaf, query, L, edirty);
 }
 
 void brute_pairs(const Box6* box, int ne, const int* elem_scene, int2* pairs, int cap, PassCounters* ctr,

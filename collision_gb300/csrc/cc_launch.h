@@ -358,9 +358,11 @@ void pass_end(const PassCounters* c, SceneCtl* ctl, const SceneRun* run, int nsc
 // walk their whole scene, from its root, and every overlapping pair with
 // such an element is written once. act_l: the pass's sorted leaves
 // (L->nact_e of them; act_e is unused); edirty, query: ne_cap each.
+// warp: one warp per dirty element walking with a shared-memory stack
+// (k_traverse_warp_full); otherwise one thread along the ropes.
 void pruned_pairs(const BvhBufs& b, const int* act_e, const int* act_l, const unsigned* stamp, LoopCtl* L,
                   uint8_t* edirty, int* query, int ne_cap, int2* pairs, int cap, PassCounters* ctr, const int* ev,
-                  cudaStream_t s);
+                  cudaStream_t s, bool warp = true);
 
 // updateFinalForRG's device part: per body, the first point in element
 // order with has_collsn and its average velocity (into b.out).

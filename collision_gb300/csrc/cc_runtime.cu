@@ -323,6 +323,7 @@ struct cc_solver {
     int* d_tree_built = nullptr;   // 2 * nscenes: tree built (proximity, then collision)
     // reference tree order built on the GPU (cc_tree_gpu.cu)
     bool host_tree = false;          // CC_TUNE_HOST_TREE: emulate the insertions on host threads instead
+    bool pruned_warp = true;         // CC_TUNE_PRUNED_WARP: one warp per pruned query
     void* d_tree_scratch = nullptr;  // nodes, parent links and leaf counts of the trees being built
     int* d_tree_jobs = nullptr;      // 3 per tree: scene, first element, elements
     int* h_tree_jobs = nullptr;      // pinned
@@ -1526,7 +1527,8 @@ cc_status cc_solver::build_loop_graph(int n_hier) {
     bvh_pairs(d_box, lb, d_pairs, pair_cap, d_ctr, cs, d_ev, tune.traverse_block, nullptr, false, tune.rope_traverse,
               tune.traverse_refill, tune.stack_depth);
     mark(kStLoopTraverse - m0, cs);
-    pruned_pairs(lb, d_act_e, d_act_l, d_pstamp, d_loop, d_edirty, d_query, ne, d_pairs, pair_cap, d_ctr, d_ev, cs);
+    pruned_pairs(lb, d_act_e, d_act_l, d_pstamp, d_loop, d_edirty, d_query, ne, d_pairs, pair_cap, d_ctr, d_ev, cs,
+                 pruned_warp);
     mark(kStLoopPruned - m0, cs);
     NarrowArgs a = narrow_args(1, false);
     a.ps = loop_stamp();
@@ -2542,6 +2544,10 @@ cc_status cc_set_tuning(cc_solver* s, int knob, int value) {
             s->zb.small_sort = value != 0;
             s->loop_dirty = true;
             return CC_OK;
+        case CC_TUNE_PRUNED_WARP:
+            s->pruned_warp = value != 0;
+            s->loop_dirty = true;
+            return CC_OK;
         case CC_TUNE_TRAVERSE_REFILL:
             if (value < 0 || value > 32) return CC_BAD_INPUT;
             s->tune.traverse_refill = value;
@@ -2589,6 +2595,7 @@ int cc_get_tuning(cc_solver* s, int knob) {
         case CC_TUNE_PRUNE: return s->prune ? 1 : 0;
         case CC_TUNE_HOST_TREE: return s->host_tree ? 1 : 0;
         case CC_TUNE_SMALL_SORT: return s->zb.small_sort ? 1 : 0;
+        case CC_TUNE_PRUNED_WARP: return s->pruned_warp ? 1 : 0;
         case CC_TUNE_STACK_DEPTH: return s->tune.stack_depth;
         case CC_TUNE_PAIR_CAPACITY: return s->pair_cap;
         default: return -1;

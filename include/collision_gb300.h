@@ -277,6 +277,10 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
  *                           8,192 union records in one CTA (in the device
  *                           loop the general radix sort then does not run);
  *                           0: always the general sort. Same results
+ *   CC_TUNE_PRUNED_WARP     1 (default): in the device loop's pruned passes
+ *                           each query walks its scene with one warp (a
+ *                           shared-memory stack, up to 32 nodes per round);
+ *                           0: one thread along the ropes. Same results
  * cc_get_tuning returns the current value, or -1 for an unknown knob. */
 enum {
     CC_TUNE_SPLIT_NARROW = 0,
@@ -297,7 +301,8 @@ enum {
     CC_TUNE_DEVICE_LOOP = 15,
     CC_TUNE_PRUNE = 16,
     CC_TUNE_HOST_TREE = 17,
-    CC_TUNE_SMALL_SORT = 18
+    CC_TUNE_SMALL_SORT = 18,
+    CC_TUNE_PRUNED_WARP = 19
 };
 cc_status cc_set_tuning(cc_solver* s, int knob, int value);
 int cc_get_tuning(cc_solver* s, int knob);

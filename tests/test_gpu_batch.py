@@ -55,11 +55,12 @@ def _split(a, off, i):
 
 def _run_batch(solver_cls, mix, nsteps, mode=0, window=True, record=False, split=True, graph=True, combined=True,
                warp=False, packet=False, roles=True, overlap=False, rope=True, subset_refit=True, device_loop=True,
-               refill=8, zone_cap=None, pair_capacity=None, small_sort=True):
+               refill=8, zone_cap=None, pair_capacity=None, small_sort=True, pruned_warp=True):
     b = solver_cls(0)
     b.assembleBatch(mix)
     b.setMode(mode)
     b.setTuning(solver_cls.TUNE_SMALL_SORT, int(small_sort))
+    b.setTuning(solver_cls.TUNE_PRUNED_WARP, int(pruned_warp))
     if pair_capacity is not None:
         b.setTuning(solver_cls.TUNE_PAIR_CAPACITY, pair_capacity)
     b.setTuning(solver_cls.TUNE_DEVICE_LOOP, int(device_loop))
@@ -493,3 +494,19 @@ def test_loop_stage_marks_change_nothing(solver_cls):
     loop_ms = sum(prof[k][0] for k in prof if k.startswith("loop_"))
     assert 0 < loop_ms <= prof["detect_loop"][0] * 1.05
     b.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["plain", "mixed"])
+def test_pruned_walks_agree(solver_cls, mode):
+    # the device loop's pruned passes walk each dirty element's scene with
+    # one warp and a shared-memory stack, or with one thread along the
+    # ropes: the same candidate pairs, so the same counts and results
+    mix = _contact_sample()
+    a, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, zone_cap=3, pruned_warp=True)
+    b, _, _ = _run_batch(solver_cls, mix, 8, mode=mode, zone_cap=3, pruned_warp=False)
+    for k, (u, w) in enumerate(zip(a, b)):
+        for key in ("x", "v", "hc", "hcol", "status"):
+            assert np.array_equal(u[key], w[key]), (k, key)
+        for c in ("passes", "candidate_pairs", "visits", "hit_pairs", "contacts", "pruned_queries"):
+            assert u["counters"][c] == w["counters"][c], (k, c)
+    assert sum(u["counters"]["pruned_queries"] for u in a) > 0
