@@ -187,19 +187,51 @@ CR_HD void sincos_dd(double x, dd* s, dd* c) {
     }
 }
 
+// cos and sin each need one of the two polynomials (which one depends on
+// the quadrant); the value is the one sincos_dd gives.
 CR_HD double cos(double x) {
     if (!(fabs(x) < 1048576.0)) return ::cos(x);  // outside the reduction range: not used here
-    dd s, c;
-    sincos_dd(x, &s, &c);
-    return c.hi;
+    int q;
+    const dd r = reduce_pio2(x, &q);
+    const dd r2 = mul(r, r);
+    switch (q) {
+        case 0: return cos_poly(r2).hi;
+        case 1: return neg(mul(sin_poly(r2), r)).hi;
+        case 2: return neg(cos_poly(r2)).hi;
+        default: return mul(sin_poly(r2), r).hi;
+    }
 }
 
 CR_HD double sin(double x) {
     if (x == 0.0) return x;
     if (!(fabs(x) < 1048576.0)) return ::sin(x);
+    int q;
+    const dd r = reduce_pio2(x, &q);
+    const dd r2 = mul(r, r);
+    switch (q) {
+        case 0: return mul(sin_poly(r2), r).hi;
+        case 1: return cos_poly(r2).hi;
+        case 2: return neg(mul(sin_poly(r2), r)).hi;
+        default: return neg(cos_poly(r2)).hi;
+    }
+}
+
+// sin(x) and cos(x) of one argument: the same values as sin and cos.
+CR_HD void sincos(double x, double* sn, double* cs) {
+    if (!(fabs(x) < 1048576.0)) {
+        *sn = x == 0.0 ? x : ::sin(x);
+        *cs = ::cos(x);
+        return;
+    }
+    if (x == 0.0) {
+        *sn = x;
+        *cs = cos(x);
+        return;
+    }
     dd s, c;
     sincos_dd(x, &s, &c);
-    return s.hi;
+    *sn = s.hi;
+    *cs = c.hi;
 }
 
 // asin(t) for t in [0, 0.5] given as a double-double, as a double-double.

@@ -240,8 +240,10 @@ __device__ void zone_motion(const int* __restrict__ members, int i, int end, con
     double w[3];
     zone_omega(I, L, w);
     double mag_w = mag3(w);
-    const double sw = mag_w < kRoundEps ? 0.0 : cr::sin(dt * mag_w) / mag_w;
-    const double cw = cr::cos(dt * mag_w);
+    double sn, cs;
+    cr::sincos(dt * mag_w, &sn, &cs);
+    const double sw = mag_w < kRoundEps ? 0.0 : sn / mag_w;
+    const double cw = cs;
     bool bad = false;
     for (int q = i; q < end; ++q)
         bad |= zone_member_motion(members[q], fixed, xo, av, x_cm, v_cm, w, mag_w, sw, cw, dt, ps);
@@ -298,8 +300,8 @@ __global__ void __launch_bounds__(kZoneWarpBlock) k_zone_solve_warp(
         const Params prm = scenes[vscene[members[i]]].p;
         const double m = prm.m, dt = prm.dt;
         const int num_pts = end - i;
-        double x_cm[3] = {0.0, 0.0, 0.0}, v_cm[3] = {0.0, 0.0, 0.0};
-        double L[3] = {0.0, 0.0, 0.0}, I[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+        double x_cm[3], v_cm[3], L[3], I[3][3];
+        double acc = 0.0;  // this lane's component of the current sum
         for (int c = i; c < end; c += 32) {
             const int q = c + lane;
             if (q < end) {
@@ -310,17 +312,17 @@ __global__ void __launch_bounds__(kZoneWarpBlock) k_zone_solve_warp(
                 for (int d = 0; d < 3; ++d) st[lane][d] = xs[d], st[lane][3 + d] = vs[d];
             }
             __syncwarp();
-            if (lane == 0) {
+            if (lane < 6) {  // lane d sums component d over the members in list order
                 const int k1 = end - c < 32 ? end - c : 32;
-                for (int k = 0; k < k1; ++k)
-                    for (int d = 0; d < 3; ++d) { x_cm[d] += st[k][d]; v_cm[d] += st[k][3 + d]; }
+                for (int k = 0; k < k1; ++k) acc += st[k][lane];
             }
             __syncwarp();
         }
         for (int d = 0; d < 3; ++d) {
-            x_cm[d] = __shfl_sync(0xffffffffu, x_cm[d] / num_pts, 0);
-            v_cm[d] = __shfl_sync(0xffffffffu, v_cm[d] / num_pts, 0);
+            x_cm[d] = __shfl_sync(0xffffffffu, acc / num_pts, d);
+            v_cm[d] = __shfl_sync(0xffffffffu, acc / num_pts, 3 + d);
         }
+        acc = 0.0;
         for (int c = i; c < end; c += 32) {
             const int q = c + lane;
             if (q < end) {
@@ -340,22 +342,23 @@ __global__ void __launch_bounds__(kZoneWarpBlock) k_zone_solve_warp(
                     }
             }
             __syncwarp();
-            if (lane == 0) {
+            if (lane < 12) {  // lane c sums component c (L, then I row by row) in list order
                 const int k1 = end - c < 32 ? end - c : 32;
-                for (int k = 0; k < k1; ++k) {
-                    for (int d = 0; d < 3; ++d) L[d] = st[k][d] + L[d];
-                    for (int r = 0; r < 3; ++r)
-                        for (int s = 0; s < 3; ++s) I[r][s] += st[k][3 + 3 * r + s];
-                }
+                for (int k = 0; k < k1; ++k) acc = st[k][lane] + acc;
             }
             __syncwarp();
         }
+        for (int d = 0; d < 3; ++d) L[d] = __shfl_sync(0xffffffffu, acc, d);
+        for (int r = 0; r < 3; ++r)
+            for (int q = 0; q < 3; ++q) I[r][q] = __shfl_sync(0xffffffffu, acc, 3 + 3 * r + q);
         double w[3] = {0.0, 0.0, 0.0}, mag_w = 0.0, sw = 0.0, cw = 0.0;
         if (lane == 0) {
             zone_omega(I, L, w);
             mag_w = mag3(w);
-            sw = mag_w < kRoundEps ? 0.0 : cr::sin(dt * mag_w) / mag_w;
-            cw = cr::cos(dt * mag_w);
+            double sn, cs;
+            cr::sincos(dt * mag_w, &sn, &cs);
+            sw = mag_w < kRoundEps ? 0.0 : sn / mag_w;
+            cw = cs;
         }
         for (int d = 0; d < 3; ++d) w[d] = __shfl_sync(0xffffffffu, w[d], 0);
         mag_w = __shfl_sync(0xffffffffu, mag_w, 0);

@@ -139,20 +139,39 @@ __device__ __forceinline__ int uf_find(UfNode* uf, int p) {
     return r;
 }
 
-// mergePoint (dcollid.cpp:1033-1059): the lighter set joins the heavier one
-// (the second on equal weights) and its member list is appended.
-__device__ __forceinline__ void uf_merge(UfNode* uf, int x, int y) {
-    int px = uf_find(uf, x), py = uf_find(uf, y);
-    if (px == py) return;
-    if (uf[px].w > uf[py].w) {
-        const int t = px;
-        px = py;
-        py = t;
-    }
-    uf[py].w += uf[px].w;
-    uf[px].root = py;
-    uf[uf[py].tail].next = px;
-    uf[py].tail = uf[px].tail;
+// One createImpZone(pts, 4) call: mergePoint (dcollid.cpp:1033-1059) on
+// every pair of its points in the reference's order - the lighter set joins
+// the heavier one (the second on equal weights) and its member list is
+// appended. Only roots, weights, tails and next links are
+// observable (membership, list order, the next unions' choices); the root
+// links path compression shortens are not. So each point's root is found
+// once, kept in a register and updated as the call's merges go, instead of
+// two finds per pair.
+__device__ __forceinline__ void replay_record(UfNode* uf, const uint8_t* __restrict__ fixed, const UnionRec& r) {
+    int rt[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) rt[q] = uf_find(uf, r.p[q]);
+#pragma unroll
+    for (int a = 1; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < a; ++b) {
+            if (!joins(fixed, r.p[a], r.p[b])) continue;
+            int px = rt[a], py = rt[b];
+            if (px == py) continue;
+            const int wx = uf[px].w, wy = uf[py].w;
+            if (wx > wy) {  // the heavier set keeps its root (the second on equal weights)
+                const int t = px;
+                px = py;
+                py = t;
+            }
+            uf[py].w = wx + wy;
+            uf[px].root = py;
+            uf[uf[py].tail].next = px;
+            uf[py].tail = uf[px].tail;
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (rt[q] == px) rt[q] = py;
+        }
 }
 
 // One thread per final zone touched by the pass: its records' unions in
@@ -166,12 +185,7 @@ __global__ void k_union_replay(const UnionRec* __restrict__ rec, const PassCount
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nseg; s += gridDim.x * blockDim.x) {
         const int j0 = seg[s];
         const unsigned long long lab = keys[j0];
-        for (int j = j0; j < n && keys[j] == lab; ++j) {
-            const UnionRec r = rec[vals[j]];
-            for (int a = 1; a < 4; ++a)
-                for (int b = 0; b < a; ++b)
-                    if (joins(fixed, r.p[a], r.p[b])) uf_merge(uf, r.p[a], r.p[b]);
-        }
+        for (int j = j0; j < n && keys[j] == lab; ++j) replay_record(uf, fixed, rec[vals[j]]);
     }
 }
 
