@@ -65,12 +65,26 @@ sys.path.insert(0, ROOT)
 METRIC = "cloth collision steps/s: mixed-prec batched vs FP64 plain, 0 missed CCD"
 UNIT = "scene-steps/s"
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
-NARROW_BYTES_PER_VISIT = 8 + 8 + 24 + 6 * 64  # pair, two leaf ranks, two elements' ids, x_old+avgVel of 6 points
-# The traversal's DRAM traffic per query leaf, measured with ncu on the
-# batched workload cut to 96 scenes (launches of 1,298,248 query leaves):
-# k_traverse_rope 184 MB per launch, k_traverse (a stack per thread) 221 MB
-TRAVERSE_DRAM_BYTES_PER_LEAF = {True: 141.6, False: 170.4}
-TRAVERSE_LANES_ACTIVE = {True: 6.3, False: 7.4}
+# The traversal's DRAM traffic (bytes read + written) per query leaf and
+# its threads active per instruction, from one ncu capture of each kernel on
+# the batched workload cut to 96 scenes, each a full traversal of all
+# 1,298,248 elements: k_traverse_rope_dyn 257.1 MB (the first traversal of
+# the run), k_traverse_rope 184 MB and k_traverse (a stack per thread)
+# 221 MB (free-fall steps of the same scenes)
+TRAVERSE_DRAM_BYTES_PER_LEAF = {"dyn": 198.0, "rope": 141.6, "stack": 170.4}
+TRAVERSE_LANES_ACTIVE = {"dyn": 7.8, "rope": 6.3, "stack": 7.4}
+TRAVERSE_KERNEL = {"dyn": "k_traverse_rope_dyn (LBVH broad phase, stackless, persistent warps refilling lanes)",
+                   "rope": "k_traverse_rope (LBVH broad phase, stackless along ropes, one thread per query)",
+                   "stack": "k_traverse (LBVH broad phase, a stack per thread)"}
+# FP64 operations (dadd + dmul + 2 dfma) per queued FP64 sub-test, from one
+# ncu capture of both k_subtests launches of a CCD pass of the same 96
+# scenes: 85.6 MFLOP for 123,752 point-triangle and 44,900 edge-edge
+# sub-tests; GB300's FP64 peak is 1.25 TFLOP/s (nominal: none measured)
+SUBTEST_FP64_FLOPS = 507.6
+FP64_PEAK_TFLOPS = 1.25
+# the CCD filter's algorithmic bytes per visited pair: the pair, two ranks,
+# the two elements' point ids, FP32 x_old and avgVel of six points
+FILTER_BYTES_PER_VISIT = 8 + 8 + 24 + 6 * 32
 
 
 def make_workload(name, seed, nscenes=0, large_n=1025, placement="contact"):
@@ -382,7 +396,8 @@ def run_gpu(args):
         torch.cuda.synchronize()
         step_ms = [a.elapsed_time(b) for a, b in evs]
         prof = s.profile()
-        rope = bool(s.getTuning(CollisionSolver3d.TUNE_ROPE_TRAVERSE))
+        rope = ("dyn" if s.getTuning(CollisionSolver3d.TUNE_TRAVERSE_REFILL) > 0 else "rope") \
+            if s.getTuning(CollisionSolver3d.TUNE_ROPE_TRAVERSE) else "stack"
         kprof = None
         if mode == 1 and args.kernel_steps > 0:
             # after the timed steps, untimed: a few more steps with every
@@ -651,47 +666,54 @@ def run_gpu(args):
     tot = {k: sum(c[k] for c in mixed["counters"]) for k in mixed["counters"][0]}
     prof = mixed["prof"]
     kern = {}
-    ms, calls = prof.get("narrow_ccd", (0.0, 0))
-    if calls:
-        per = NARROW_BYTES_PER_VISIT * tot["moving_visits"] / calls
-        kern["narrow_ccd"] = {"kernel": "k_narrow<true> (CCD narrow phase)", "bytes_per_launch": per,
-                              "ms_per_launch": ms / calls, "achieved": per / (ms / calls / 1e3) / 1e9}
+    ms, calls = prof.get("traverse", (0.0, 0))
+    if calls and tot.get("timed_traverse_leaves"):
+        # the traversals the "traverse" stage times (the proximity pass's,
+        # launched from the host): one read of the hierarchy's FP32 boxes,
+        # (2n-1)*24 B for n leaves, and the 8-byte pairs written
+        per = (48.0 * tot["timed_traverse_leaves"] + 8.0 * tot["timed_traverse_pairs"]) / calls
+        kern["traverse"] = {"kernel": TRAVERSE_KERNEL[mixed["rope"]], "bytes_per_launch": per,
+                            "ms_per_launch": ms / calls, "achieved": per / (ms / calls / 1e3) / 1e9,
+                            "leaves_per_launch": tot["timed_traverse_leaves"] / calls}
     ms, calls = prof.get("strain", (0.0, 0))
     if calls:
         per = tot["strain_bytes"] / calls
         kern["strain"] = {"kernel": "strain stage: k_strain_setup, k_strain_check and k_strain_window sweeps "
                           "(one CTA per scene), one launch = one step's tail graph", "bytes_per_launch": per,
                           "ms_per_launch": ms / calls, "achieved": per / (ms / calls / 1e3) / 1e9}
-    ms, calls = prof.get("traverse", (0.0, 0))
-    if calls and tot.get("broad_leaves"):
-        # one read of the hierarchy's FP32 boxes per traversal, (2n-1)*24 B
-        # for n leaves, and the 8-byte pairs written
-        per = (48.0 * tot["broad_leaves"] + 8.0 * tot["broad_pairs"]) / calls
-        kern["traverse"] = {"kernel": ("k_traverse_rope (LBVH broad phase, stackless along ropes)" if mixed["rope"]
-                                       else "k_traverse (LBVH broad phase, a stack per thread)"),
-                            "bytes_per_launch": per,
-                            "ms_per_launch": ms / calls, "achieved": per / (ms / calls / 1e3) / 1e9}
+    kp = mixed["kprof"]
+    if kp:
+        # the untimed steps after the timed ones, every stage of every pass
+        # timed (inside the loop graph by global-timer boundary kernels)
+        kc, kpr = kp["counters"], kp["prof"]
+        t_sub = (kpr.get("loop_subtests", (0.0, 0))[0] + kpr.get("ccd_subtests", (0.0, 0))[0]) / 1e3
+        if t_sub > 0 and kc.get("fp64_subtests"):
+            flops = SUBTEST_FP64_FLOPS * kc["fp64_subtests"]
+            kern["ccd_subtests"] = {
+                "kernel": "k_subtests (the FP64 sub-tests that pass the FP32 filters)", "bound": "fp64",
+                "flops": flops, "s": t_sub, "achieved_tflops": flops / t_sub / 1e12, "peak_tflops": FP64_PEAK_TFLOPS,
+                "frac": flops / t_sub / 1e12 / FP64_PEAK_TFLOPS, "peak_source": "nominal",
+                "flops_per_subtest": SUBTEST_FP64_FLOPS, "cr_roots": kc.get("cr_roots"),
+                "note": "FP64 pipe 77% busy in the ncu capture: most FP64 issue slots are compares, selects and "
+                        "conversions, run at the FP64 rate"}
+        t_f = kpr.get("loop_filter", (0.0, 0))[0] / 1e3
+        if t_f > 0 and kc.get("moving_visits"):
+            b = FILTER_BYTES_PER_VISIT * kc["moving_visits"]
+            kern["ccd_filter"] = {"kernel": "k_narrow_filter<1> (FP32 per-pair filters of the CCD passes)",
+                                  "bytes": b, "s": t_f, "achieved": b / t_f / 1e9}
     roof = None
-    if kern:
-        # the two largest kernels of the timed steps in the ncu launch list of
-        # the contact phase are the strain sweep (23% of the step) and the
-        # traversal (22%); the traversal is timed
-        # per launch here, the strain stage only as a whole (several kernels
-        # in one graph), so the traversal is the roofline entry and the
-        # strain stage is listed under "kernels"
-        top = "traverse" if "traverse" in kern else max(kern, key=lambda k: prof[k][0])
-        kt = kern[top]
-        traffic = None
-        if top == "traverse":
-            # DRAM bytes read + written per query leaf from one ncu capture of
-            # each traversal kernel on 96 scenes, scaled to this run's launches
-            traffic = (TRAVERSE_DRAM_BYTES_PER_LEAF[mixed["rope"]] * tot["broad_leaves"] /
-                       max(prof["traverse"][1], 1))
+    if "traverse" in kern:
+        # the traversal is the largest kernel the timed region times per
+        # launch with CUDA events (inside the loop graph, only the untimed
+        # profiled steps split the stages; their shares are printed as
+        # stages_ms_per_step_after)
+        kt = kern["traverse"]
+        traffic = TRAVERSE_DRAM_BYTES_PER_LEAF[mixed["rope"]] * kt["leaves_per_launch"]
         roof = {"bound": "hbm", "kernel": kt["kernel"], "achieved": kt["achieved"], "peak": hbm, "unit": "GB/s",
                 "frac": kt["achieved"] / hbm, "peak_source": peak_src, "traffic": traffic,
                 "note": f"latency and divergence bound ({TRAVERSE_LANES_ACTIVE[mixed['rope']]} of 32 lanes active "
-                        "per instruction, dependent node loads), not bandwidth bound; k_strain_window has a "
-                        "similar share of the step (kernels.strain)", "kernels": kern}
+                        "per instruction, dependent node loads), not bandwidth bound; traffic = the ncu capture's "
+                        "DRAM bytes per query leaf x this launch's leaves", "kernels": kern}
     if roof is not None and tot.get("path_bytes"):
         # the whole step's algorithmic bytes (the path_bytes counter: state in
         # and out, per pass the points, connectivity, hierarchy, pairs and
