@@ -68,11 +68,11 @@ PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # The traversal's DRAM traffic (bytes read + written) per query leaf and
 # its threads active per instruction, from one ncu capture of each kernel on
 # the batched workload cut to 96 scenes, each a full traversal of all
-# 1,298,248 elements: k_traverse_rope_dyn 257.1 MB (the first traversal of
-# the run), k_traverse_rope 184 MB and k_traverse (a stack per thread)
-# 221 MB (free-fall steps of the same scenes)
-TRAVERSE_DRAM_BYTES_PER_LEAF = {"dyn": 198.0, "rope": 141.6, "stack": 170.4}
-TRAVERSE_LANES_ACTIVE = {"dyn": 7.8, "rope": 6.3, "stack": 7.4}
+# 1,298,248 elements: k_traverse_rope_dyn 257.1 MB and k_traverse_rope
+# 215.8 MB (the first traversal of the run, the proximity pass of step 1),
+# k_traverse (a stack per thread) 221 MB (a free-fall step)
+TRAVERSE_DRAM_BYTES_PER_LEAF = {"dyn": 198.0, "rope": 166.2, "stack": 170.4}
+TRAVERSE_LANES_ACTIVE = {"dyn": 7.8, "rope": 6.2, "stack": 7.4}
 TRAVERSE_KERNEL = {"dyn": "k_traverse_rope_dyn (LBVH broad phase, stackless, persistent warps refilling lanes)",
                    "rope": "k_traverse_rope (LBVH broad phase, stackless along ropes, one thread per query)",
                    "stack": "k_traverse (LBVH broad phase, a stack per thread)"}
