@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(128) k_zone_unions(NarrowArgs a) {
 
 // Stage 2: one queued sub-test per thread, the FP64 test of k_narrow.
 template <bool MOVING, bool EE>
-__global__ void __launch_bounds__(128) k_subtests(NarrowArgs a) {
+__global__ void __launch_bounds__(128, 4) k_subtests(NarrowArgs a) {
     const SubRec* list = EE ? a.sub_ee : a.sub_pt;
     int n = EE ? a.ctr->nsub_ee : a.ctr->nsub_pt;
     if (n > a.sub_cap) n = a.sub_cap;
