@@ -349,8 +349,17 @@ void tree_check(const SceneRun* run, int nscenes, const unsigned long long* bbox
                 const int* built, int which, int* rebuild, LoopCtl* L, cudaStream_t s);
 void loop_reset(PassCounters* c, SceneRun* run, int nscenes, LoopCtl* L, cudaStream_t s);
 // Stage profiling inside the loop graph: acc[0] the last boundary's time,
-// then (ns, count) per slot 1.. - the time since the previous boundary.
-void stage_mark(unsigned long long* acc, int slot, cudaStream_t s);
+// then (ns, count) for each of kLoopMarkSlots slots 1.. - the time since the
+// previous boundary - then a per-pass log (the row count, then
+// kPassLogRows rows of kPassLogCols: each slot's time, and at the slot
+// given c the pass's candidate pairs, queued sub-tests (point-triangle,
+// edge-edge), union records and pruned queries).
+constexpr int kLoopMarkSlots = 16;
+constexpr int kPassLogRows = 4096;
+constexpr int kPassLogCols = kLoopMarkSlots + 5;
+constexpr size_t kMarkWords = 1 + 2 * kLoopMarkSlots + 1 + (size_t)kPassLogRows * kPassLogCols;
+void stage_mark(unsigned long long* acc, int slot, cudaStream_t s, const PassCounters* c = nullptr,
+                const LoopCtl* L = nullptr);
 void pass_end(const PassCounters* c, SceneCtl* ctl, const SceneRun* run, int nscenes, LoopCtl* L, int combined,
               bool in_graph, cudaGraphConditionalHandle h_loop, cudaStream_t s);
 // The pruned broad phase of the device loop's later passes (L->prune): the

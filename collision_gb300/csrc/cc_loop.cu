@@ -360,19 +360,45 @@ void loop_reset(PassCounters* c, SceneRun* run, int nscenes, LoopCtl* L, cudaStr
 
 // A stage boundary inside the loop graph (stage profiling): the device time
 // since the previous boundary, from the global nanosecond timer, goes to
-// `slot` (0 only records the time).
-__global__ void k_stage_mark(unsigned long long* acc, int slot) {
+// `slot` (0 only records the time and starts a pass's row of the pass log).
+// Layout of acc: [0] the last boundary's time, then (ns, count) per slot,
+// then the pass log's row counter and kPassLogRows rows of kPassLogCols:
+// the pass's time per slot, then (with c given, at the pass's last slot)
+// its candidate pairs, queued point-triangle and edge-edge sub-tests,
+// union records and pruned queries.
+__global__ void k_stage_mark(unsigned long long* acc, int slot, const PassCounters* c, const LoopCtl* L) {
+    constexpr int nslots = kLoopMarkSlots;
     unsigned long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    unsigned long long* rows = acc + 1 + 2 * nslots;
+    unsigned long long* log = rows + 1;
     if (slot > 0) {
-        acc[2 * slot - 1] += t - acc[0];
+        const unsigned long long d = t - acc[0];
+        acc[2 * slot - 1] += d;
         acc[2 * slot] += 1;
+        const unsigned long long r = *rows;
+        if (r > 0) {
+            unsigned long long* row = log + ((r - 1) % kPassLogRows) * kPassLogCols;
+            row[slot - 1] = d;
+            if (c) {
+                row[nslots + 0] = (unsigned)c->npairs;
+                row[nslots + 1] = (unsigned)c->nsub_pt;
+                row[nslots + 2] = (unsigned)c->nsub_ee;
+                row[nslots + 3] = (unsigned)c->nunion;
+                row[nslots + 4] = L ? (unsigned)(L->prune ? L->nquery : -1) : 0u;
+            }
+        }
+    } else {
+        const unsigned long long r = *rows;
+        unsigned long long* row = log + (r % kPassLogRows) * kPassLogCols;
+        for (int k = 0; k < kPassLogCols; ++k) row[k] = 0;
+        *rows = r + 1;
     }
     acc[0] = t;
 }
 
-void stage_mark(unsigned long long* acc, int slot, cudaStream_t s) {
-    count_launch(), k_stage_mark<<<1, 1, 0, s>>>(acc, slot);
+void stage_mark(unsigned long long* acc, int slot, cudaStream_t s, const PassCounters* c, const LoopCtl* L) {
+    count_launch(), k_stage_mark<<<1, 1, 0, s>>>(acc, slot, c, L);
 }
 
 void pass_end(const PassCounters* c, SceneCtl* ctl, const SceneRun* run, int nscenes, LoopCtl* L, int combined,

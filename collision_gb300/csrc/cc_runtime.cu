@@ -50,6 +50,7 @@ const char* kStageNames[kNumStages] = {"init", "leaf_boxes", "bvh_build", "trave
                                        "loop_zone_sort", "loop_zone_replay", "loop_zone_list", "loop_zone_solve",
                                        "loop_end"};
 constexpr int kNumLoopMarks = kNumStages - kStLoopPlan;
+static_assert(kNumLoopMarks <= kLoopMarkSlots, "stage mark slots");
 
 constexpr int kMaxSceneElems = (1 << 22) - 1;  // leaf ranks fill 22 bits of a contribution key
 constexpr long long kMaxTotal = 1ll << 28;     // points and elements over all scenes
@@ -380,6 +381,28 @@ struct cc_solver {
     }
     void prox_pass_async();
     cc_status build_loop_graph(int n_hier);
+    // CC_PASS_LOG with profiling level 2: the loop passes of the last step,
+    // one line each (stage times in microseconds, then the pass's counts)
+    void print_pass_log() {
+        std::vector<unsigned long long> h(kMarkWords);
+        cudaMemcpyAsync(h.data(), d_marks, sizeof(unsigned long long) * kMarkWords, cudaMemcpyDeviceToHost, stream);
+        if (cudaStreamSynchronize(stream) != cudaSuccess) return;
+        const unsigned long long rows = h[1 + 2 * kLoopMarkSlots];
+        const unsigned long long* log = h.data() + 2 + 2 * kLoopMarkSlots;
+        const unsigned long long n = rows < (unsigned long long)kPassLogRows ? rows : kPassLogRows;
+        for (unsigned long long r = 0; r < n; ++r) {
+            const unsigned long long* row = log + r * kPassLogCols;
+            std::string line = "cc_loop_pass " + std::to_string(r);
+            for (int k = 0; k < kNumLoopMarks; ++k)
+                line += " " + std::string(kStageNames[kStLoopPlan + k] + 5) + "=" +
+                        std::to_string(row[k] / 1000.0).substr(0, 7);
+            line += " pairs=" + std::to_string(row[kLoopMarkSlots]) + " sub_pt=" +
+                    std::to_string(row[kLoopMarkSlots + 1]) + " sub_ee=" + std::to_string(row[kLoopMarkSlots + 2]) +
+                    " unions=" + std::to_string(row[kLoopMarkSlots + 3]) + " queries=" +
+                    std::to_string((long long)(int)row[kLoopMarkSlots + 4]);
+            std::fprintf(stderr, "%s\n", line.c_str());
+        }
+    }
     cc_status device_passes(std::string& capped);
     cc_status rebuild_flagged();
 
@@ -413,7 +436,7 @@ struct cc_solver {
     // per-stage GPU time, measured with events on the solver's stream
     bool profiling = false;
     bool loop_marks = false;                   // profiling level 2: stage marks inside the loop graph
-    unsigned long long* d_marks = nullptr;     // 1 + 2 * kNumLoopMarks
+    unsigned long long* d_marks = nullptr;     // kMarkWords (stage_mark)
     void mark(int slot, cudaStream_t on) {
         if (loop_marks && d_marks) stage_mark(d_marks, slot, on);
     }
@@ -1579,7 +1602,7 @@ cc_status cc_solver::build_loop_graph(int n_hier) {
     }
     const long long l2 = g_kernel_launches;
     pass_end(d_ctr, d_ctl, d_run, nscenes, d_loop, 0, true, h_loop_c, cs);
-    mark(kStLoopEnd - m0, cs);
+    if (loop_marks && d_marks) stage_mark(d_marks, kStLoopEnd - m0, cs, d_ctr, d_loop);
     cudaGraph_t bg = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(cs, &bg);
     lg.body_launches = (l1 - l0) + (g_kernel_launches - l2);
@@ -1632,6 +1655,8 @@ cc_status cc_solver::device_passes(std::string& capped) {
     h_loop->prune_on = prune ? 1 : 0;
     h_loop->nq_full = bvh.n;
     const LoopCtl loop_init = *h_loop;
+    if (pass_log && loop_marks && d_marks)  // this step's rows of the pass log from row 0
+        cudaMemsetAsync(d_marks + 1 + 2 * kLoopMarkSlots, 0, sizeof(unsigned long long), stream);
     cudaMemcpyAsync(d_ctl, h_ctl, sizeof(SceneCtl) * (size_t)nscenes, cudaMemcpyHostToDevice, stream);
     cudaMemcpyAsync(d_loop, h_loop, sizeof(LoopCtl), cudaMemcpyHostToDevice, stream);
     bool need_prox = true;
@@ -1716,6 +1741,7 @@ cc_status cc_solver::device_passes(std::string& capped) {
     counters[24] += (long long)a[kAccUnions];
     const long long loop_iters = (long long)a[kAccIters] - 1;
     counters[21] += loop_iters;
+    if (pass_log && loop_marks && d_marks) print_pass_log();
     count_launch((int)(lgraph->body_launches * (loop_iters + graph_runs) +
                        lgraph->zone_launches * (long long)a[kAccZonePasses]));
     for (int s = 0; s < nscenes; ++s) {
@@ -2820,7 +2846,7 @@ cc_status cc_set_profiling(cc_solver* s, int on) {
     s->loop_marks = marks;
     if (marks && !s->d_marks) {
         cudaSetDevice(s->device);
-        if (cudaMalloc(&s->d_marks, sizeof(unsigned long long) * (1 + 2 * kNumLoopMarks)) != cudaSuccess) {
+        if (cudaMalloc(&s->d_marks, sizeof(unsigned long long) * kMarkWords) != cudaSuccess) {
             s->d_marks = nullptr;
             s->loop_marks = false;
             return s->fail(CC_NO_MEMORY, "stage marks");
@@ -2828,7 +2854,7 @@ cc_status cc_set_profiling(cc_solver* s, int on) {
     }
     if (s->d_marks) {
         cudaSetDevice(s->device);
-        cudaMemsetAsync(s->d_marks, 0, sizeof(unsigned long long) * (1 + 2 * kNumLoopMarks), s->stream);
+        cudaMemsetAsync(s->d_marks, 0, sizeof(unsigned long long) * kMarkWords, s->stream);
     }
     for (int i = 0; i < kNumStages; ++i) {
         s->stage_ms[i] = 0.0;
