@@ -227,6 +227,9 @@ struct NarrowArgs {
     int* pairq;     // candidate pairs with a queued sub-test (capacity: the pair buffer's)
     int static_only;  // proximity pass over swept-box pairs: only those with kPairStatic
     PassStamp ps;     // stamps of the points of every sub-test that hits
+    // the split sub-tests form a root again with correctly rounded functions
+    // only where a decision can depend on it (is_coplanar's rb); 0: always
+    int robust_roots = 1;
     // movable rigid bodies: the body of each point (-1 none), each body's
     // mass, and the contribution slot of body 0 (the point count)
     const int* vbody;

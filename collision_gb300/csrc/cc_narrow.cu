@@ -25,6 +25,7 @@ __global__ void __launch_bounds__(128) k_narrow(NarrowArgs a, int max_pairs) {
     c.rec = a.rec; c.rec_cap = a.rec_cap;
     c.pbox_lo = a.pbox_lo; c.pbox_hi = a.pbox_hi; c.p32 = a.p32; c.v32 = a.v32;
     c.check = a.check;
+    c.robust_roots = 0;
     int np = a.ctr->npairs;
     if (np > max_pairs) np = max_pairs;
     // counters summed per thread, added once per warp at the end
@@ -221,6 +222,7 @@ __device__ __forceinline__ void queue_sub(const NarrowArgs& a, const NarrowCtx& 
 template <bool MOVING>
 __global__ void __launch_bounds__(512) k_narrow_filter(NarrowArgs a, int max_pairs) {
     NarrowCtx c;
+    c.robust_roots = 0;
     c.pbox_lo = a.pbox_lo; c.pbox_hi = a.pbox_hi; c.p32 = a.p32; c.v32 = a.v32;
     int np = a.ctr->npairs;
     if (np > max_pairs) np = max_pairs;
@@ -297,6 +299,7 @@ __global__ void __launch_bounds__(128, 4) k_subtests(NarrowArgs a) {
     c.rec = nullptr; c.rec_cap = 0;
     c.pbox_lo = nullptr; c.pbox_hi = nullptr; c.p32 = nullptr; c.v32 = nullptr;
     c.check = 0;
+    c.robust_roots = a.robust_roots;
     c.zone = 0;
     int t_hits = 0, t_cr = 0, t_contacts = 0, t_sub = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {

@@ -42,6 +42,7 @@ struct NarrowCtx {
     float hpad;   // h of the sub-tests, rounded up
     float epad;   // eps (barycentric tolerance), rounded up
     int check;    // decide hits only: no impulses, contacts or zones
+    int robust_roots;  // mixed sub-tests: skip the correctly rounded roots where no decision needs them
     float dt32;   // dt rounded up to FP32
 };
 
@@ -387,10 +388,54 @@ static __device__ bool edge_to_edge(const NarrowCtx& c, CallState& st, const int
 }
 
 // ------------------------------------------------------------------- CCD
+// Whether the static test (h, barycentric tolerance eps) returns false at
+// every time within terr of t: the points' boxes at t, padded as in
+// mixed_may_hit (which bounds where a hit can lie) and widened by how far a
+// point moves in terr plus the positions' rounding, are apart along an axis.
+template <bool EE>
+__device__ __forceinline__ bool root_misses(const double (*xo4)[3], const double (*av4)[3], double t, double terr,
+                                            double h, double eps) {
+    double X[4][3];
+    double vmax = 0.0, xmax = 0.0;
+    for (int q = 0; q < 4; ++q)
+        for (int k = 0; k < 3; ++k) {
+            X[q][k] = xo4[q][k] + t * av4[q][k];
+            vmax = fmax(vmax, fabs(av4[q][k]));
+            xmax = fmax(xmax, fabs(X[q][k]));
+        }
+    constexpr int na = EE ? 2 : 3;
+    double alo[3], ahi[3], blo[3], bhi[3];
+    for (int k = 0; k < 3; ++k) {
+        alo[k] = ahi[k] = X[0][k];
+        for (int q = 1; q < na; ++q) alo[k] = fmin(alo[k], X[q][k]), ahi[k] = fmax(ahi[k], X[q][k]);
+        blo[k] = bhi[k] = X[na][k];
+        for (int q = na + 1; q < 4; ++q) blo[k] = fmin(blo[k], X[q][k]), bhi[k] = fmax(bhi[k], X[q][k]);
+    }
+    double ext = 0.0, extb = 0.0;
+    for (int k = 0; k < 3; ++k) ext += ahi[k] - alo[k], extb += bhi[k] - blo[k];
+    double pad = EE ? h + (ext + extb) * 0x1p-20 : h + ext * (8.0 * eps + 0x1p-10);
+    pad = pad * 1.001 + terr * vmax * 1.001 + xmax * 0x1p-48;
+    for (int k = 0; k < 3; ++k)
+        if (alo[k] - pad > bhi[k] || blo[k] - pad > ahi[k]) return true;
+    return false;
+}
+
 // isCoplanar, dcollid3d.cpp:371-482: roots of the coplanarity cubic in
 // [0, dt], shifted by -MACH_EPS and sorted; roots[3] holds dt.
+//
+// rb (mixed sub-tests): a root the fast functions put well inside the
+// window - farther than twice the margin from its ends, so the correctly
+// rounded root is inside too and on the same side of MACH_EPS - and at
+// which the static test misses whichever root within the margin it is
+// (root_misses), needs no correctly rounded value: its test returns false
+// either way and nothing else depends on its exact value. When every root
+// near the window is such a root, none is formed again; those roots count
+// towards the return value and are then dropped, as their tests would
+// return false. Any other root near the window (or a branch threshold
+// within the margin) makes all of them formed again, as without rb.
+template <bool EE>
 static __device__ bool is_coplanar(const double (*xo4)[3], const double (*av4)[3], double dt, double* roots,
-                                   int* ncr) {
+                                   int* ncr, bool rb = false, double h = 0.0, double eps = 0.0) {
     double v[4][3], x[4][3];
     for (int j = 0; j < 3; ++j) {
         v[0][j] = av4[0][j];
@@ -449,6 +494,20 @@ static __device__ bool is_coplanar(const double (*xo4)[3], const double (*av4)[3
                 near_[i] = f[i] > lo && f[i] < hi;
                 any |= near_[i];
             }
+            if (any && rb) {
+                bool skip = true;
+                for (int i = 0; i < 3 && skip; ++i)
+                    if (near_[i]) {
+                        const double t = f[i] - kMachEps;
+                        skip = t > kMachEps + 2 * margin && t < dt - 2 * margin &&
+                               root_misses<EE>(xo4, av4, t, 2 * margin, h, eps);
+                    }
+                if (skip) {
+                    // every root near the window is inside it and misses
+                    for (int i = 0; i < 3; ++i) roots[i] = -1;
+                    return true;
+                }
+            }
             if (any) {
                 ++*ncr;
                 theta = cr::acos(z);
@@ -469,9 +528,31 @@ static __device__ bool is_coplanar(const double (*xo4)[3], const double (*av4)[3
             double scale = fabs(A) + fabs(B) + fabs(a);
             double margin = 1e-14 * scale + 1e-300;
             double lo = kMachEps - margin, hi = dt + kMachEps + margin;
-            bool near_ = (f0 > lo && f0 < hi) || (f1 > lo && f1 < hi) ||
-                         fabs(fabs(A) - kRoundEps) <= 1e-14 * fabs(A) + 1e-300 ||
-                         fabs(fabs(A - B) - kRoundEps) <= 1e-14 * scale + 1e-300;
+            const bool n0 = f0 > lo && f0 < hi, n1 = f1 > lo && f1 < hi;
+            const bool thr = fabs(fabs(A) - kRoundEps) <= 1e-14 * fabs(A) + 1e-300 ||
+                             fabs(fabs(A - B) - kRoundEps) <= 1e-14 * scale + 1e-300;
+            bool near_ = n0 || n1 || thr;
+            if (near_ && rb && !thr) {
+                // f1 is a root only when |A - B| < ROUND_EPS (no threshold
+                // within the margin, so the same holds correctly rounded)
+                const bool use1 = fabs(A - B) < kRoundEps;
+                bool skip = true;
+                if (n0) {
+                    const double t = f0 - kMachEps;
+                    skip = t > kMachEps + 2 * margin && t < dt - 2 * margin &&
+                           root_misses<EE>(xo4, av4, t, 2 * margin, h, eps);
+                }
+                if (skip && use1 && n1) {
+                    const double t = f1 - kMachEps;
+                    skip = t > kMachEps + 2 * margin && t < dt - 2 * margin &&
+                           root_misses<EE>(xo4, av4, t, 2 * margin, h, eps);
+                }
+                if (skip && (n0 || (use1 && n1))) {
+                    for (int i = 0; i < 3; ++i) roots[i] = -1;
+                    return true;
+                }
+                if (skip) near_ = false;  // f1 near but not a root, f0 far: nothing to form again
+            }
             if (near_) {
                 ++*ncr;
                 A = -sgn * cr::pow(base, 1.0 / 3.0);
@@ -515,7 +596,7 @@ static __device__ bool moving_test(const NarrowCtx& c, CallState& st, const int*
     }
     double dt = c.p.dt;
     double roots[4] = {-1, -1, -1, dt};
-    if (!is_coplanar(xo4, av4, dt, roots, &st.ncr)) return false;
+    if (!is_coplanar<EE>(xo4, av4, dt, roots, &st.ncr, c.robust_roots != 0, c.p.eps, c.p.eps)) return false;
     for (int i = 0; i < 4; ++i) {
         if (roots[i] < 0) continue;
         double X[4][3];

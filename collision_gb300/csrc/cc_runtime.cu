@@ -325,6 +325,7 @@ struct cc_solver {
     // reference tree order built on the GPU (cc_tree_gpu.cu)
     bool host_tree = false;          // CC_TUNE_HOST_TREE: emulate the insertions on host threads instead
     bool pruned_warp = true;         // CC_TUNE_PRUNED_WARP: one warp per pruned query
+    bool robust_roots = true;        // CC_TUNE_ROBUST_ROOTS: correctly rounded roots only where decisive
     void* d_tree_scratch = nullptr;  // nodes, parent links and leaf counts of the trees being built
     int* d_tree_jobs = nullptr;      // 3 per tree: scene, first element, elements
     int* h_tree_jobs = nullptr;      // pinned
@@ -364,6 +365,7 @@ struct cc_solver {
     bool use_device_loop() const { return device_loop && !record && vtk_dir.empty() && !overlap_tails; }
     NarrowArgs narrow_args(int moving, bool combined) const {
         NarrowArgs a{};
+        a.robust_roots = robust_roots ? 1 : 0;
         a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
         a.vbody = d_vbody; a.body_mass = d_body_mass; a.body_slot0 = nv;
         a.rank = d_rank[moving]; a.escene = d_escene; a.scenes = d_scenes; a.run = d_run;
@@ -1832,6 +1834,7 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
             }
         }
         NarrowArgs a;
+        a.robust_roots = robust_roots ? 1 : 0;
         a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
         a.vbody = d_vbody; a.body_mass = d_body_mass; a.body_slot0 = nv;
         a.rank = d_rank[moving]; a.escene = d_escene; a.scenes = d_scenes; a.run = d_run;
@@ -2178,6 +2181,7 @@ cc_status cc_solver::check_ccd(const double* x_old, const double* x_new, long lo
         bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, d_ev, tune.traverse_block, nullptr,
                   tune.packet_traverse, tune.rope_traverse, tune.traverse_refill, kTraversalStack);
         NarrowArgs a{};
+        a.robust_roots = robust_roots ? 1 : 0;
         a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
         a.vbody = d_vbody; a.body_mass = d_body_mass; a.body_slot0 = nv;
         a.rank = nullptr; a.escene = d_escene; a.scenes = d_scenes; a.run = d_run;
@@ -2243,6 +2247,7 @@ cc_status cc_solver::autotune(double* best_ms) {
             bvh_pairs(d_box, bvh, d_pairs, pair_cap, d_ctr, stream, d_ev, t.traverse_block, nullptr,
                       t.packet_traverse, t.rope_traverse, t.traverse_refill, t.stack_depth);
             NarrowArgs a{};
+            a.robust_roots = robust_roots ? 1 : 0;
             a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
         a.vbody = d_vbody; a.body_mass = d_body_mass; a.body_slot0 = nv;
             a.rank = rank; a.escene = d_escene; a.scenes = d_scenes; a.run = d_run;
@@ -2574,6 +2579,10 @@ cc_status cc_set_tuning(cc_solver* s, int knob, int value) {
             s->pruned_warp = value != 0;
             s->loop_dirty = true;
             return CC_OK;
+        case CC_TUNE_ROBUST_ROOTS:
+            s->robust_roots = value != 0;
+            s->loop_dirty = true;
+            return CC_OK;
         case CC_TUNE_TRAVERSE_REFILL:
             if (value < 0 || value > 32) return CC_BAD_INPUT;
             s->tune.traverse_refill = value;
@@ -2622,6 +2631,7 @@ int cc_get_tuning(cc_solver* s, int knob) {
         case CC_TUNE_HOST_TREE: return s->host_tree ? 1 : 0;
         case CC_TUNE_SMALL_SORT: return s->zb.small_sort ? 1 : 0;
         case CC_TUNE_PRUNED_WARP: return s->pruned_warp ? 1 : 0;
+        case CC_TUNE_ROBUST_ROOTS: return s->robust_roots ? 1 : 0;
         case CC_TUNE_STACK_DEPTH: return s->tune.stack_depth;
         case CC_TUNE_PAIR_CAPACITY: return s->pair_cap;
         default: return -1;

@@ -281,6 +281,13 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
  *                           each query walks its scene with one warp (a
  *                           shared-memory stack, up to 32 nodes per round);
  *                           0: one thread along the ropes. Same results
+ *   CC_TUNE_ROBUST_ROOTS    1 (default): the mixed path's FP64 sub-tests
+ *                           form a coplanarity root again with correctly
+ *                           rounded functions only where a decision can
+ *                           depend on it (not for roots well inside the time
+ *                           window at which the test misses with a margin
+ *                           covering the root's error); 0: every root near
+ *                           the window. Same results
  * cc_get_tuning returns the current value, or -1 for an unknown knob. */
 enum {
     CC_TUNE_SPLIT_NARROW = 0,
@@ -302,7 +309,8 @@ enum {
     CC_TUNE_PRUNE = 16,
     CC_TUNE_HOST_TREE = 17,
     CC_TUNE_SMALL_SORT = 18,
-    CC_TUNE_PRUNED_WARP = 19
+    CC_TUNE_PRUNED_WARP = 19,
+    CC_TUNE_ROBUST_ROOTS = 20
 };
 cc_status cc_set_tuning(cc_solver* s, int knob, int value);
 int cc_get_tuning(cc_solver* s, int knob);
