@@ -254,6 +254,7 @@ __device__ void zone_motion(const int* __restrict__ members, int i, int end, con
 // (k_zone_solve_warp) where the zone list is built on the device.
 constexpr int kZoneWarpMin = 16;
 constexpr int kZoneWarpBlock = 128;
+constexpr int kZoneCtaThreads = 256;
 
 // Zone z's members are members[zone_off[z] .. zone_off[z+1]), or with
 // zone_rng members[zone_rng[z].x .. zone_rng[z].y); dnz (may be null): the
@@ -286,7 +287,8 @@ __global__ void k_zone_solve(const int* __restrict__ members, const int* __restr
 __global__ void __launch_bounds__(kZoneWarpBlock) k_zone_solve_warp(
     const int* __restrict__ members, const int2* __restrict__ zone_rng, int nzones, const int* __restrict__ dnz,
     const uint8_t* __restrict__ fixed, const double4_32a* __restrict__ xo, double4_32a* av,
-    const int* __restrict__ vscene, const SceneDev* __restrict__ scenes, PassCounters* ctr, PassStamp ps) {
+    const int* __restrict__ vscene, const SceneDev* __restrict__ scenes, PassCounters* ctr, PassStamp ps,
+    int cta_min) {
     __shared__ double stage[kZoneWarpBlock / 32][32][12];
     if (ctr->err & kErrRetry) return;
     if (*dnz < nzones) nzones = *dnz;
@@ -296,7 +298,7 @@ __global__ void __launch_bounds__(kZoneWarpBlock) k_zone_solve_warp(
     bool bad = false;
     for (int z = gw; z < nzones; z += nw) {
         const int i = zone_rng[z].x, end = zone_rng[z].y;
-        if (end - i < kZoneWarpMin) continue;
+        if (end - i < kZoneWarpMin || end - i >= cta_min) continue;
         const Params prm = scenes[vscene[members[i]]].p;
         const double m = prm.m, dt = prm.dt;
         const int num_pts = end - i;
@@ -367,6 +369,101 @@ __global__ void __launch_bounds__(kZoneWarpBlock) k_zone_solve_warp(
         for (int q = i + lane; q < end; q += 32)
             bad |= zone_member_motion(members[q], fixed, xo, av, x_cm, v_cm, w, mag_w, sw, cw, dt, ps);
         __syncwarp();
+    }
+    if (bad) atomicOr(&ctr->err, kErrNan);
+}
+
+// Zones of at least cta_min members: one CTA per zone. The same sums
+// as k_zone_solve_warp, in the same order - one thread per summed component
+// adding the members in list order - but every member's terms and its
+// final motion are computed by all the CTA's threads (a large zone is
+// otherwise bound by one warp's share of the SM's FP64 pipe).
+__global__ void __launch_bounds__(kZoneCtaThreads) k_zone_solve_cta(
+    const int* __restrict__ members, const int2* __restrict__ zone_rng, int nzones, const int* __restrict__ dnz,
+    const uint8_t* __restrict__ fixed, const double4_32a* __restrict__ xo, double4_32a* av,
+    const int* __restrict__ vscene, const SceneDev* __restrict__ scenes, PassCounters* ctr, PassStamp ps,
+    int cta_min) {
+    __shared__ double st[kZoneCtaThreads][12];
+    __shared__ double s_sum[12];
+    __shared__ double s_rot[6];  // w, mag_w, sw, cw
+    if (ctr->err & kErrRetry) return;
+    if (*dnz < nzones) nzones = *dnz;
+    const int tid = threadIdx.x;
+    bool bad = false;
+    for (int z = blockIdx.x; z < nzones; z += gridDim.x) {
+        const int i = zone_rng[z].x, end = zone_rng[z].y;
+        if (end - i < cta_min) continue;
+        const Params prm = scenes[vscene[members[i]]].p;
+        const double m = prm.m, dt = prm.dt;
+        const int num_pts = end - i;
+        double acc = 0.0;  // this thread's component of the current sum (threads 0..11)
+        for (int c = i; c < end; c += kZoneCtaThreads) {
+            const int q = c + tid;
+            if (q < end) {
+                const int p = members[q];
+                double xs[3], vs[3];
+                load3(xo, p, xs);
+                load3(av, p, vs);
+                for (int d = 0; d < 3; ++d) st[tid][d] = xs[d], st[tid][3 + d] = vs[d];
+            }
+            __syncthreads();
+            if (tid < 6) {
+                const int k1 = end - c < kZoneCtaThreads ? end - c : kZoneCtaThreads;
+                for (int k = 0; k < k1; ++k) acc += st[k][tid];
+            }
+            __syncthreads();
+        }
+        if (tid < 6) s_sum[tid] = acc / num_pts;
+        __syncthreads();
+        double x_cm[3], v_cm[3];
+        for (int d = 0; d < 3; ++d) x_cm[d] = s_sum[d], v_cm[d] = s_sum[3 + d];
+        acc = 0.0;
+        for (int c = i; c < end; c += kZoneCtaThreads) {
+            const int q = c + tid;
+            if (q < end) {
+                const int p = members[q];
+                double xs[3], vs[3], dx[3], dv[3], Li[3];
+                load3(xo, p, xs);
+                load3(av, p, vs);
+                for (int d = 0; d < 3; ++d) { dx[d] = xs[d] - x_cm[d]; dv[d] = vs[d] - v_cm[d]; }
+                cross3(dx, dv, Li);
+                for (int d = 0; d < 3; ++d) st[tid][d] = m * Li[d];
+                const double mag_dx = mag3(dx);
+                for (int r = 0; r < 3; ++r)
+                    for (int s2 = 0; s2 < 3; ++s2) {
+                        double t = -dx[r] * dx[s2];
+                        if (r == s2) t += mag_dx * mag_dx;
+                        st[tid][3 + 3 * r + s2] = t * m;
+                    }
+            }
+            __syncthreads();
+            if (tid < 12) {
+                const int k1 = end - c < kZoneCtaThreads ? end - c : kZoneCtaThreads;
+                for (int k = 0; k < k1; ++k) acc = st[k][tid] + acc;
+            }
+            __syncthreads();
+        }
+        if (tid < 12) s_sum[tid] = acc;
+        __syncthreads();
+        if (tid == 0) {
+            double L[3], I[3][3], w[3];
+            for (int d = 0; d < 3; ++d) L[d] = s_sum[d];
+            for (int r = 0; r < 3; ++r)
+                for (int q = 0; q < 3; ++q) I[r][q] = s_sum[3 + 3 * r + q];
+            zone_omega(I, L, w);
+            const double mag_w = mag3(w);
+            double sn, cs;
+            cr::sincos(dt * mag_w, &sn, &cs);
+            for (int d = 0; d < 3; ++d) s_rot[d] = w[d];
+            s_rot[3] = mag_w;
+            s_rot[4] = mag_w < kRoundEps ? 0.0 : sn / mag_w;
+            s_rot[5] = cs;
+        }
+        __syncthreads();
+        const double w[3] = {s_rot[0], s_rot[1], s_rot[2]};
+        for (int q = i + tid; q < end; q += kZoneCtaThreads)
+            bad |= zone_member_motion(members[q], fixed, xo, av, x_cm, v_cm, w, s_rot[3], s_rot[4], s_rot[5], dt, ps);
+        __syncthreads();  // the next zone reuses the shared arrays
     }
     if (bad) atomicOr(&ctr->err, kErrNan);
 }
@@ -1241,7 +1338,8 @@ void zone_solve(const int* members, const int* zone_off, int nzones, const uint8
 
 void zone_solve_dev(const int* members, const int2* zone_rng, const int* dnz, int zone_cap, const uint8_t* fixed,
                     const double4_32a* xo, double4_32a* av, const int* vscene, const SceneDev* scenes,
-                    PassCounters* ctr, cudaStream_t s, PassStamp ps) {
+                    PassCounters* ctr, cudaStream_t s, PassStamp ps, int cta_min) {
+    if (cta_min < kZoneWarpMin) cta_min = kZoneWarpMin;
     int blocks = nblk(zone_cap, 64);
     if (blocks > 152 * 8) blocks = 152 * 8;
     if (blocks > 0)
@@ -1251,7 +1349,11 @@ void zone_solve_dev(const int* members, const int2* zone_rng, const int* dnz, in
     if (wblocks > 152 * 4) wblocks = 152 * 4;
     if (wblocks > 0)
         count_launch(), k_zone_solve_warp<<<wblocks, kZoneWarpBlock, 0, s>>>(members, zone_rng, zone_cap, dnz, fixed,
-                                                                            xo, av, vscene, scenes, ctr, ps);
+                                                                            xo, av, vscene, scenes, ctr, ps, cta_min);
+    const int cblocks = zone_cap < 152 * 2 ? zone_cap : 152 * 2;
+    if (cblocks > 0)
+        count_launch(), k_zone_solve_cta<<<cblocks, kZoneCtaThreads, 0, s>>>(members, zone_rng, zone_cap, dnz, fixed,
+                                                                            xo, av, vscene, scenes, ctr, ps, cta_min);
 }
 
 void final_rigid(const BodyBufs& b, const uint8_t* has_collsn, const double4_32a* av, cudaStream_t s) {

@@ -288,6 +288,10 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
  *                           window at which the test misses with a margin
  *                           covering the root's error); 0: every root near
  *                           the window. Same results
+ *   CC_TUNE_ZONE_CTA_MIN    members from which an impact zone's rigid
+ *                           motion is computed by a CTA of its own (>= 16,
+ *                           default 256; smaller zones of 16+ members get a
+ *                           warp, the rest a thread). Same results
  * cc_get_tuning returns the current value, or -1 for an unknown knob. */
 enum {
     CC_TUNE_SPLIT_NARROW = 0,
@@ -310,7 +314,8 @@ enum {
     CC_TUNE_HOST_TREE = 17,
     CC_TUNE_SMALL_SORT = 18,
     CC_TUNE_PRUNED_WARP = 19,
-    CC_TUNE_ROBUST_ROOTS = 20
+    CC_TUNE_ROBUST_ROOTS = 20,
+    CC_TUNE_ZONE_CTA_MIN = 21
 };
 cc_status cc_set_tuning(cc_solver* s, int knob, int value);
 int cc_get_tuning(cc_solver* s, int knob);
