@@ -389,9 +389,22 @@ static __device__ bool edge_to_edge(const NarrowCtx& c, CallState& st, const int
 
 // ------------------------------------------------------------------- CCD
 // Whether the static test (h, barycentric tolerance eps) returns false at
-// every time within terr of t: the points' boxes at t, padded as in
-// mixed_may_hit (which bounds where a hit can lie) and widened by how far a
-// point moves in terr plus the positions' rounding, are apart along an axis.
+// every time within terr of t. Positions at any such time, as the test
+// computes them, lie within dp of X = x_old + t * avgVel (the motion in terr
+// plus the positions' rounding). A miss is certain when
+//  - the points' boxes at t, padded as in mixed_may_hit (which bounds where
+//    a hit can lie) and by dp, are apart along an axis; or
+//  - point-triangle (dcollid3d.cpp:778-922): a barycentric coordinate at t
+//    is outside [-eps, 1+eps] by more than twice a bound on the formulas'
+//    rounding error (the same formulas as the test's) plus how far the
+//    coordinates can move when the points move by dp; if the test's
+//    determinant is below its cut instead, it returns false too; or
+//  - edge-edge (dcollid3d.cpp:643-776): the test's distance is between two
+//    points on the segments, so it is at least their true distance, which
+//    is at least the gap between the segments' projections on any unit
+//    vector (here the one between the segments' closest points): a gap
+//    above h by 2 dp plus rounding rules a hit out (and near-parallel
+//    edges return false anyway).
 template <bool EE>
 __device__ __forceinline__ bool root_misses(const double (*xo4)[3], const double (*av4)[3], double t, double terr,
                                             double h, double eps) {
@@ -403,6 +416,8 @@ __device__ __forceinline__ bool root_misses(const double (*xo4)[3], const double
             vmax = fmax(vmax, fabs(av4[q][k]));
             xmax = fmax(xmax, fabs(X[q][k]));
         }
+    if (!(xmax < 1e30) || !(vmax < 1e30)) return false;  // NaN or huge: no claim
+    const double dp = terr * vmax * 1.001 + xmax * 0x1p-48;
     constexpr int na = EE ? 2 : 3;
     double alo[3], ahi[3], blo[3], bhi[3];
     for (int k = 0; k < 3; ++k) {
@@ -414,10 +429,71 @@ __device__ __forceinline__ bool root_misses(const double (*xo4)[3], const double
     double ext = 0.0, extb = 0.0;
     for (int k = 0; k < 3; ++k) ext += ahi[k] - alo[k], extb += bhi[k] - blo[k];
     double pad = EE ? h + (ext + extb) * 0x1p-20 : h + ext * (8.0 * eps + 0x1p-10);
-    pad = pad * 1.001 + terr * vmax * 1.001 + xmax * 0x1p-48;
+    pad = pad * 1.001 + dp;
     for (int k = 0; k < 3; ++k)
         if (alo[k] - pad > bhi[k] || blo[k] - pad > ahi[k]) return true;
-    return false;
+    if (!EE) {
+        double x13[3], x23[3], x43[3];
+        for (int k = 0; k < 3; ++k) {
+            x13[k] = X[0][k] - X[2][k];
+            x23[k] = X[1][k] - X[2][k];
+            x43[k] = X[3][k] - X[2][k];
+        }
+        const double a11 = dot3(x13, x13), a22 = dot3(x23, x23), a12 = dot3(x13, x23), a44 = dot3(x43, x43);
+        const double det = a11 * a22 - a12 * a12;
+        if (!(det > 0.0)) return false;
+        const double w0 = (dot3(x13, x43) * a22 - dot3(x23, x43) * a12) / det;
+        const double w1 = (a11 * dot3(x23, x43) - a12 * dot3(x13, x43)) / det;
+        const double w2 = 1 - w0 - w1;
+        const double W = 1.0 + 1.01 * fmax(fmax(fabs(w0), fabs(w1)), fabs(w2));
+        // the rounding error of w0 or w1 from these formulas (dot products
+        // within 3 units of 2^-53 of their magnitude, then two products, a
+        // difference and the quotient): below 15 units times S^2 (1 + |w|)
+        // over det, bounded here by 2^-48 S^2 W / det; w2 = 1 - w0 - w1
+        // carries at most twice that, and the test's own coordinates, at its
+        // own positions, as much again
+        const double S = a11 + a22 + a44;
+        const double E = 0x1p-48 * S * S * W / det;
+        // and how far a coordinate moves when the four points move by dp: a
+        // coordinate is a ratio of in-plane areas, each changing by at most
+        // dp times the lengths (L bounds every distance among the points;
+        // sqrt(det) is twice the triangle's area), padded twice
+        const double L = sqrt(a11) + sqrt(a22) + sqrt(a44);
+        const double D = 6.0 * dp * L * W / sqrt(det);
+        const double m = eps + 4.04 * E + D;
+        if (!(m < 0.5)) return false;
+        return w0 < -m || w1 < -m || w2 < -m || w0 > 1 + m || w1 > 1 + m || w2 > 1 + m;
+    }
+    // edge-edge: the closest points of the two segments (clamped), then the
+    // gap of the projections on the unit vector between them
+    double d1[3], d2[3], r[3];
+    for (int k = 0; k < 3; ++k) {
+        d1[k] = X[1][k] - X[0][k];
+        d2[k] = X[3][k] - X[2][k];
+        r[k] = X[0][k] - X[2][k];
+    }
+    const double aa = dot3(d1, d1), ee = dot3(d2, d2), ff = dot3(d2, r);
+    if (!(aa > 0.0) || !(ee > 0.0)) return false;
+    const double cc = dot3(d1, r), bb = dot3(d1, d2), den = aa * ee - bb * bb;
+    double s1 = den > 0.0 ? fmin(fmax((bb * ff - cc * ee) / den, 0.0), 1.0) : 0.0;
+    double s2 = (bb * s1 + ff) / ee;
+    if (s2 < 0.0) {
+        s2 = 0.0;
+        s1 = fmin(fmax(-cc / aa, 0.0), 1.0);
+    } else if (s2 > 1.0) {
+        s2 = 1.0;
+        s1 = fmin(fmax((bb - cc) / aa, 0.0), 1.0);
+    }
+    double n[3];
+    for (int k = 0; k < 3; ++k) n[k] = (X[2][k] + s2 * d2[k]) - (X[0][k] + s1 * d1[k]);
+    const double nm = sqrt(dot3(n, n));
+    if (!(nm > h)) return false;
+    for (int k = 0; k < 3; ++k) n[k] /= nm;
+    const double p0 = dot3(X[0], n), p1 = dot3(X[1], n), p2 = dot3(X[2], n), p3 = dot3(X[3], n);
+    const double gap = fmax(fmin(p2, p3) - fmax(p0, p1), fmin(p0, p1) - fmax(p2, p3));
+    // rounding: the projections (3 products and sums of coordinates up to
+    // xmax, n within a few ulp of unit) and the test's own distance
+    return gap - 2.0 * dp - xmax * 0x1p-44 > h * 1.001;
 }
 
 // isCoplanar, dcollid3d.cpp:371-482: roots of the coplanarity cubic in
