@@ -139,18 +139,45 @@ __device__ __forceinline__ int uf_find(UfNode* uf, int p) {
     return r;
 }
 
+// The root of each of a record's four points: the four parent links are
+// loaded together, then their parents' links; a point whose parent is a
+// root (path compression keeps almost every point there) needs nothing
+// more, any other takes the full find with path compression.
+__device__ __forceinline__ void find4(UfNode* uf, const int* p, int* rt) {
+    int a[4], b[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) a[q] = uf[p[q]].root;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) b[q] = uf[a[q]].root;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) rt[q] = b[q] == a[q] ? a[q] : uf_find(uf, p[q]);
+}
+
+// The weight and tail of the root that won the thread's last merge, kept in
+// registers: the next records of a zone mostly join sets to that root, and
+// only this thread writes the nodes of its zone.
+struct RootCache {
+    int id = -1, w = 0, tail = 0;
+};
+
+__device__ __forceinline__ int2 root_wt(const UfNode* uf, const RootCache& c, int r) {
+    if (r == c.id) return make_int2(c.w, c.tail);
+    const int4 u = *reinterpret_cast<const int4*>(&uf[r]);  // root, next, tail, w
+    return make_int2(u.w, u.z);
+}
+
 // One createImpZone(pts, 4) call: mergePoint (dcollid.cpp:1033-1059) on
 // every pair of its points in the reference's order - the lighter set joins
 // the heavier one (the second on equal weights) and its member list is
-// appended. Only roots, weights, tails and next links are
-// observable (membership, list order, the next unions' choices); the root
-// links path compression shortens are not. So each point's root is found
-// once, kept in a register and updated as the call's merges go, instead of
-// two finds per pair.
-__device__ __forceinline__ void replay_record(UfNode* uf, const uint8_t* __restrict__ fixed, const UnionRec& r) {
+// appended. Only roots, weights, tails and next links are observable
+// (membership, list order, the next unions' choices); the root links path
+// compression shortens are not. So each point's root is found once, kept in
+// a register and updated as the call's merges go, instead of two finds per
+// pair.
+__device__ __forceinline__ void replay_record(UfNode* uf, const uint8_t* __restrict__ fixed, const UnionRec& r,
+                                              RootCache& cache) {
     int rt[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) rt[q] = uf_find(uf, r.p[q]);
+    find4(uf, r.p, rt);
 #pragma unroll
     for (int a = 1; a < 4; ++a)
 #pragma unroll
@@ -158,16 +185,23 @@ __device__ __forceinline__ void replay_record(UfNode* uf, const uint8_t* __restr
             if (!joins(fixed, r.p[a], r.p[b])) continue;
             int px = rt[a], py = rt[b];
             if (px == py) continue;
-            const int wx = uf[px].w, wy = uf[py].w;
-            if (wx > wy) {  // the heavier set keeps its root (the second on equal weights)
+            int2 sx = root_wt(uf, cache, px), sy = root_wt(uf, cache, py);
+            if (sx.x > sy.x) {  // the heavier set keeps its root (the second on equal weights)
                 const int t = px;
                 px = py;
                 py = t;
+                const int2 ts = sx;
+                sx = sy;
+                sy = ts;
             }
-            uf[py].w = wx + wy;
+            const int w = sx.x + sy.x;
+            uf[py].w = w;
             uf[px].root = py;
-            uf[uf[py].tail].next = px;
-            uf[py].tail = uf[px].tail;
+            uf[sy.y].next = px;
+            uf[py].tail = sx.y;
+            cache.id = py;
+            cache.w = w;
+            cache.tail = sx.y;
 #pragma unroll
             for (int q = 0; q < 4; ++q)
                 if (rt[q] == px) rt[q] = py;
@@ -185,7 +219,8 @@ __global__ void k_union_replay(const UnionRec* __restrict__ rec, const PassCount
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nseg; s += gridDim.x * blockDim.x) {
         const int j0 = seg[s];
         const unsigned long long lab = keys[j0];
-        for (int j = j0; j < n && keys[j] == lab; ++j) replay_record(uf, fixed, rec[vals[j]]);
+        RootCache cache;
+        for (int j = j0; j < n && keys[j] == lab; ++j) replay_record(uf, fixed, rec[vals[j]], cache);
     }
 }
 
