@@ -139,14 +139,14 @@ __device__ __forceinline__ int uf_find(UfNode* uf, int p) {
     return r;
 }
 
-// The root of each of a record's four points, given their parent links a
-// (loaded earlier, before the previous record's merges: a link only ever
-// points to an ancestor, so a stale one is still an ancestor): the
-// parents' links are loaded together; a point whose parent is still a root
-// (path compression keeps almost every point there) needs nothing more, any
-// other takes the full find with path compression.
-__device__ __forceinline__ void find4(UfNode* uf, const int* p, const int* a, int* rt) {
-    int b[4];
+// The root of each of a record's four points: the four parent links are
+// loaded together, then their parents' links; a point whose parent is a
+// root (path compression keeps almost every point there) needs nothing
+// more, any other takes the full find with path compression.
+__device__ __forceinline__ void find4(UfNode* uf, const int* p, int* rt) {
+    int a[4], b[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) a[q] = uf[p[q]].root;
 #pragma unroll
     for (int q = 0; q < 4; ++q) b[q] = uf[a[q]].root;
 #pragma unroll
@@ -175,9 +175,9 @@ __device__ __forceinline__ int2 root_wt(const UfNode* uf, const RootCache& c, in
 // a register and updated as the call's merges go, instead of two finds per
 // pair.
 __device__ __forceinline__ void replay_record(UfNode* uf, const uint8_t* __restrict__ fixed, const UnionRec& r,
-                                              const int* a, RootCache& cache) {
+                                              RootCache& cache) {
     int rt[4];
-    find4(uf, r.p, a, rt);
+    find4(uf, r.p, rt);
 #pragma unroll
     for (int a = 1; a < 4; ++a)
 #pragma unroll
@@ -220,27 +220,7 @@ __global__ void k_union_replay(const UnionRec* __restrict__ rec, const PassCount
         const int j0 = seg[s];
         const unsigned long long lab = keys[j0];
         RootCache cache;
-        // the next record and its points' parent links are loaded while the
-        // current record's unions are made
-        UnionRec rc = rec[vals[j0]];
-        int a[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) a[q] = uf[rc.p[q]].root;
-        for (int j = j0;; ++j) {
-            const bool more = j + 1 < n && keys[j + 1] == lab;
-            UnionRec rn;
-            int an[4];
-            if (more) {
-                rn = rec[vals[j + 1]];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) an[q] = uf[rn.p[q]].root;
-            }
-            replay_record(uf, fixed, rc, a, cache);
-            if (!more) break;
-            rc = rn;
-#pragma unroll
-            for (int q = 0; q < 4; ++q) a[q] = an[q];
-        }
+        for (int j = j0; j < n && keys[j] == lab; ++j) replay_record(uf, fixed, rec[vals[j]], cache);
     }
 }
 
