@@ -319,6 +319,16 @@ struct ZoneBufs {
     int2* zone_rng = nullptr;            // per zone: its run of members
     int* zone_root = nullptr;            // per zone: its root
     int* members = nullptr;              // per point (at most one zone each)
+    // the previous zone pass's lists (k_zone_members starts from them): a
+    // copy of its member array, and per root its run and the epoch it was
+    // listed in (prev_epoch == *epoch: the pass just before); n_pts_cap
+    // bounds the members and zones of a pass (the points)
+    int* prev_members = nullptr;
+    int* prev_off = nullptr;
+    int* prev_len = nullptr;
+    unsigned* prev_epoch = nullptr;
+    unsigned* epoch = nullptr;
+    int n_pts_cap = 0;
     bool small_sort = true;              // sorts of up to 8192 records in one CTA
     int zone_cta_min = 256;              // zones of this many members are solved by a CTA each
 };

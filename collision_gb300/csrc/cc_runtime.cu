@@ -496,6 +496,7 @@ struct cc_solver {
         urec_cap = 0;
         dfree(zb.keys); dfree(zb.vals); dfree(zb.seg); dfree(zb.cc); dfree(zb.uf); dfree(zb.zone_rng);
         dfree(zb.zone_root); dfree(zb.members); dfree(d_uf0); dfree(d_cc0);
+        dfree(zb.prev_members); dfree(zb.prev_off); dfree(zb.prev_len); dfree(zb.prev_epoch); dfree(zb.epoch);
         if (zb.sort_temp) cudaFree(zb.sort_temp);
         const bool small_sort = zb.small_sort;  // settings, not buffers
         const int zone_cta_min = zb.zone_cta_min;
@@ -639,6 +640,8 @@ struct cc_solver {
         if (nv == 0) return;
         cudaMemcpyAsync(zb.uf, d_uf0, sizeof(UfNode) * (size_t)nv, cudaMemcpyDeviceToDevice, stream);
         cudaMemcpyAsync(zb.cc, d_cc0, sizeof(int) * (size_t)nv, cudaMemcpyDeviceToDevice, stream);
+        // the lists of the last step's zones no longer hold
+        if (zb.prev_epoch) cudaMemsetAsync(zb.prev_epoch, 0xff, sizeof(unsigned) * (size_t)nv, stream);
         uf_on_device = true;
     }
     // The zone root of every point after the last step.
@@ -1303,9 +1306,14 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
         bool zok = dalloc(&zb.cc, (size_t)nv) == cudaSuccess && dalloc(&zb.uf, (size_t)nv) == cudaSuccess &&
                    dalloc(&d_cc0, (size_t)nv) == cudaSuccess && dalloc(&d_uf0, (size_t)nv) == cudaSuccess &&
                    dalloc(&zb.zone_rng, (size_t)nz) == cudaSuccess && dalloc(&zb.zone_root, (size_t)nz) == cudaSuccess &&
-                   dalloc(&zb.members, (size_t)nv) == cudaSuccess;
+                   dalloc(&zb.members, (size_t)nv) == cudaSuccess &&
+                   dalloc(&zb.prev_members, (size_t)nv) == cudaSuccess &&
+                   dalloc(&zb.prev_off, (size_t)nv) == cudaSuccess && dalloc(&zb.prev_len, (size_t)nv) == cudaSuccess &&
+                   dalloc(&zb.prev_epoch, (size_t)nv) == cudaSuccess && dalloc(&zb.epoch, 1) == cudaSuccess;
         if (!zok) return fail(CC_NO_MEMORY, "zone buffers");
         zb.zone_cap = nz;
+        zb.n_pts_cap = nv;
+        cudaMemsetAsync(zb.epoch, 0, sizeof(unsigned), stream);
         std::vector<UfNode> u0((size_t)nv);
         std::vector<int> c0((size_t)nv);
         for (int p = 0; p < nv; ++p) {

@@ -243,19 +243,64 @@ __global__ void k_zone_enum(const int* __restrict__ act_pts, int n, const int* _
     }
 }
 
-// The member list of every zone, from its root along the next links.
+// The member list of every zone, from its root along the next links, one
+// warp per zone. A root's list only ever grows at its end while the root
+// stays a root (mergePoint appends the lighter set's list to the heavier
+// one's), so a zone listed by the previous zone pass (prev_epoch == epoch)
+// starts as a copy of that list, which the warp's lanes make together, and
+// only the members appended since are walked.
 __global__ void k_zone_members(const PassCounters* ctr, const int2* __restrict__ zone_rng,
-                               const int* __restrict__ zone_root, const UfNode* __restrict__ uf, int* members) {
+                               const int* __restrict__ zone_root, const UfNode* __restrict__ uf, int* members,
+                               const int* __restrict__ prev_members, const int* __restrict__ prev_off,
+                               const int* __restrict__ prev_len, const unsigned* __restrict__ prev_epoch,
+                               const unsigned* __restrict__ epoch) {
     if (ctr->err & kErrRetry) return;
     const int nz = ctr->nzones;
-    for (int z = blockIdx.x * blockDim.x + threadIdx.x; z < nz; z += gridDim.x * blockDim.x) {
+    const unsigned e = *epoch;
+    const int lane = threadIdx.x & 31;
+    for (int z = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; z < nz; z += (gridDim.x * blockDim.x) >> 5) {
         const int2 r = zone_rng[z];
-        int p = zone_root[z];
-        for (int i = r.x; i < r.y && p >= 0; ++i) {
-            members[i] = p;
-            p = uf[p].next;
+        const int root = zone_root[z];
+        int copied = 0;
+        if (prev_epoch[root] == e) {
+            const int off = prev_off[root];
+            const int len = prev_len[root];
+            copied = len < r.y - r.x ? len : r.y - r.x;
+            for (int k = lane; k < copied; k += 32) members[r.x + k] = prev_members[off + k];
+        }
+        __syncwarp();
+        if (lane == 0) {
+            int p = copied > 0 ? uf[members[r.x + copied - 1]].next : root;
+            for (int i = r.x + copied; i < r.y && p >= 0; ++i) {
+                members[i] = p;
+                p = uf[p].next;
+            }
         }
     }
+}
+
+// This pass's lists as the next zone pass's previous ones.
+__global__ void k_zone_save(const PassCounters* ctr, const int2* __restrict__ zone_rng,
+                            const int* __restrict__ zone_root, const int* __restrict__ members, int* prev_members,
+                            int* prev_off, int* prev_len, unsigned* prev_epoch, const unsigned* __restrict__ epoch) {
+    if (ctr->err & kErrRetry) return;
+    const int nz = ctr->nzones, nm = ctr->nmembers;
+    const unsigned e = *epoch + 1u;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nm || i < nz; i += gridDim.x * blockDim.x) {
+        if (i < nm) prev_members[i] = members[i];
+        if (i < nz) {
+            const int root = zone_root[i];
+            const int2 r = zone_rng[i];
+            prev_off[root] = r.x;
+            prev_len[root] = r.y - r.x;
+            prev_epoch[root] = e;
+        }
+    }
+}
+
+__global__ void k_zone_epoch(const PassCounters* ctr, unsigned* epoch) {
+    if (ctr->err & kErrRetry) return;
+    *epoch += 1u;
 }
 
 }  // namespace
@@ -286,8 +331,13 @@ cudaError_t zone_pass(const ZoneBufs& z, const PassCounters* ctr_c, const uint8_
     if (pb > 0)
         count_launch(), k_zone_enum<<<pb, 256, 0, s>>>(act_pts, n_pts, dn_pts, vscene, run, z.uf, ctr, z.zone_rng,
                                                        z.zone_root);
-    const int zb = nblk(z.zone_cap, 128) < 152 * 8 ? nblk(z.zone_cap, 128) : 152 * 8;
-    count_launch(), k_zone_members<<<zb, 128, 0, s>>>(ctr, z.zone_rng, z.zone_root, z.uf, z.members);
+    const int zw = nblk(z.zone_cap, 4) < 152 * 8 ? nblk(z.zone_cap, 4) : 152 * 8;
+    count_launch(), k_zone_members<<<zw, 128, 0, s>>>(ctr, z.zone_rng, z.zone_root, z.uf, z.members, z.prev_members,
+                                                      z.prev_off, z.prev_len, z.prev_epoch, z.epoch);
+    const int zs = nblk(z.n_pts_cap, 256) < 152 * 8 ? nblk(z.n_pts_cap, 256) : 152 * 8;
+    count_launch(), k_zone_save<<<zs, 256, 0, s>>>(ctr, z.zone_rng, z.zone_root, z.members, z.prev_members,
+                                                   z.prev_off, z.prev_len, z.prev_epoch, z.epoch);
+    count_launch(), k_zone_epoch<<<1, 1, 0, s>>>(ctr, z.epoch);
     if (marks) stage_mark(marks, mark0 + 2, s);
     zone_solve_dev(z.members, z.zone_rng, &ctr->nzones, z.zone_cap, fixed, xo, av, vscene, scenes, ctr, s, ps,
                    z.zone_cta_min);
