@@ -499,10 +499,11 @@ struct cc_solver {
         dfree(zb.prev_members); dfree(zb.prev_off); dfree(zb.prev_len); dfree(zb.prev_epoch); dfree(zb.epoch);
         if (zb.sort_temp) cudaFree(zb.sort_temp);
         const bool small_sort = zb.small_sort;  // settings, not buffers
-        const int zone_cta_min = zb.zone_cta_min;
+        const int zone_cta_min = zb.zone_cta_min, replay_cta_min = zb.replay_cta_min;
         zb = ZoneBufs{};
         zb.small_sort = small_sort;
         zb.zone_cta_min = zone_cta_min;
+        zb.replay_cta_min = replay_cta_min;
         uf_on_device = false;
         dfree(d_xold_in); dfree(d_xcand_in); dfree(d_vel); dfree(d_xout); dfree(d_hc);
         dfree(d_box); dfree(d_box_st); dfree(bvh.keys); dfree(bvh.order); dfree(bvh.range_hi);
@@ -2598,6 +2599,11 @@ cc_status cc_set_tuning(cc_solver* s, int knob, int value) {
             s->zb.zone_cta_min = value;
             s->loop_dirty = true;
             return CC_OK;
+        case CC_TUNE_REPLAY_CTA_MIN:
+            if (value < 0) return CC_BAD_INPUT;
+            s->zb.replay_cta_min = value;
+            s->loop_dirty = true;
+            return CC_OK;
         case CC_TUNE_TRAVERSE_REFILL:
             if (value < 0 || value > 32) return CC_BAD_INPUT;
             s->tune.traverse_refill = value;
@@ -2648,6 +2654,7 @@ int cc_get_tuning(cc_solver* s, int knob) {
         case CC_TUNE_PRUNED_WARP: return s->pruned_warp ? 1 : 0;
         case CC_TUNE_ROBUST_ROOTS: return s->robust_roots ? 1 : 0;
         case CC_TUNE_ZONE_CTA_MIN: return s->zb.zone_cta_min;
+        case CC_TUNE_REPLAY_CTA_MIN: return s->zb.replay_cta_min;
         case CC_TUNE_STACK_DEPTH: return s->tune.stack_depth;
         case CC_TUNE_PAIR_CAPACITY: return s->pair_cap;
         default: return -1;

@@ -210,17 +210,185 @@ __device__ __forceinline__ void replay_record(UfNode* uf, const uint8_t* __restr
 
 // One thread per final zone touched by the pass: its records' unions in
 // visiting order, as createImpZone makes them.
+// Final zones with at least big records are replayed by k_union_replay_cta.
+__device__ __forceinline__ bool big_segment(const unsigned long long* keys, int j0, int n, int big) {
+    return j0 + big - 1 < n && keys[j0 + big - 1] == keys[j0];  // keys sorted by label
+}
+
 __global__ void k_union_replay(const UnionRec* __restrict__ rec, const PassCounters* ctr, int cap,
                                const unsigned long long* __restrict__ keys, const unsigned int* __restrict__ vals,
-                               const int* __restrict__ seg, const uint8_t* __restrict__ fixed, UfNode* uf) {
+                               const int* __restrict__ seg, const uint8_t* __restrict__ fixed, UfNode* uf, int big) {
     if (ctr->err & kErrRetry) return;
     const int n = count_of(&ctr->nunion, cap);
     const int nseg = ctr->nseg;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nseg; s += gridDim.x * blockDim.x) {
         const int j0 = seg[s];
+        if (big_segment(keys, j0, n, big)) continue;
         const unsigned long long lab = keys[j0];
         RootCache cache;
         for (int j = j0; j < n && keys[j] == lab; ++j) replay_record(uf, fixed, rec[vals[j]], cache);
+    }
+}
+
+// A large final zone replayed in shared memory: the union-find nodes its
+// records touch (their points, then any ancestor or tail the replay reaches)
+// are copied into a hash table in shared memory, one thread replays the
+// records there - the same unions in the same order, each access a shared
+// memory one instead of an L2 round trip - and the nodes are written back.
+// Only this CTA touches the zone's nodes. If the table fills up, the zone is
+// replayed from global memory instead (nothing was written back yet).
+constexpr int kTabBits = 13;
+constexpr int kTabSize = 1 << kTabBits;
+constexpr int kTabMax = kTabSize * 3 / 4;
+constexpr int kReplayThreads = 256;
+constexpr size_t kTabBytes = (size_t)kTabSize * (sizeof(int) + sizeof(UfNode));
+
+struct SmemUf {
+    int* key;      // point id per slot, -1 empty
+    UfNode* node;  // the point's node
+    int* count;
+    const UfNode* uf;
+    // the slot of point p, inserting it (single thread) if absent; -1: full
+    __device__ __forceinline__ int slot(int p) {
+        unsigned h = ((unsigned)p * 2654435761u) >> (32 - kTabBits);
+        for (int probe = 0; probe < kTabSize; ++probe) {
+            const int k = key[h];
+            if (k == p) return (int)h;
+            if (k < 0) {
+                if (*count >= kTabMax) return -1;
+                key[h] = p;
+                node[h] = uf[p];
+                ++*count;
+                return (int)h;
+            }
+            h = (h + 1) & (kTabSize - 1);
+        }
+        return -1;
+    }
+    // findSet with path compression; -1: full (or a root chain longer than
+    // the table, which a valid union-find does not have)
+    __device__ __forceinline__ int find(int p) {
+        int r = p, sr = slot(r);
+        if (sr < 0) return -1;
+        for (int k = 0; node[sr].root != r; ++k) {
+            if (k >= kTabSize) return -1;
+            r = node[sr].root;
+            sr = slot(r);
+            if (sr < 0) return -1;
+        }
+        int x = p, sx = slot(x);  // every node on the path is in the table now
+        for (int k = 0; sx >= 0 && node[sx].root != r && k < kTabSize; ++k) {
+            const int nx = node[sx].root;
+            node[sx].root = r;
+            x = nx;
+            sx = slot(x);
+        }
+        return r;
+    }
+};
+
+__global__ void __launch_bounds__(kReplayThreads) k_union_replay_cta(
+    const UnionRec* __restrict__ rec, const PassCounters* ctr, int cap, const unsigned long long* __restrict__ keys,
+    const unsigned int* __restrict__ vals, const int* __restrict__ seg, const uint8_t* __restrict__ fixed,
+    UfNode* uf, int big) {
+    extern __shared__ int s_key[];
+    UfNode* s_node = reinterpret_cast<UfNode*>(s_key + kTabSize);
+    __shared__ int s_count, s_end, s_bad;
+    if (ctr->err & kErrRetry) return;
+    const int n = count_of(&ctr->nunion, cap);
+    const int nseg = ctr->nseg;
+    const int tid = threadIdx.x;
+    for (int si = blockIdx.x; si < nseg; si += gridDim.x) {
+        const int j0 = seg[si];
+        if (!big_segment(keys, j0, n, big)) continue;
+        const unsigned long long lab = keys[j0];
+        for (int h = tid; h < kTabSize; h += kReplayThreads) s_key[h] = -1;
+        if (tid == 0) {
+            s_count = 0;
+            s_end = n;
+            s_bad = 0;
+        }
+        __syncthreads();
+        // the segment's end: the first record of another label
+        for (int k = j0 + tid; k < n; k += kReplayThreads)
+            if (keys[k] != lab) {
+                atomicMin(&s_end, k);
+                break;
+            }
+        __syncthreads();
+        const int j1 = s_end;
+        // the records' points into the table
+        for (int j = j0 + tid; j < j1 && !s_bad; j += kReplayThreads) {
+            const UnionRec r = rec[vals[j]];
+            for (int q = 0; q < 4; ++q) {
+                const int p = r.p[q];
+                unsigned h = ((unsigned)p * 2654435761u) >> (32 - kTabBits);
+                for (int probe = 0; probe < kTabSize; ++probe) {
+                    const int old = atomicCAS(&s_key[h], -1, p);
+                    if (old == -1) {
+                        s_node[h] = uf[p];
+                        if (atomicAdd(&s_count, 1) >= kTabMax) s_bad = 1;
+                        break;
+                    }
+                    if (old == p) break;
+                    h = (h + 1) & (kTabSize - 1);
+                }
+            }
+        }
+        __syncthreads();
+        if (tid == 0 && !s_bad) {
+            SmemUf t{s_key, s_node, &s_count, uf};
+            for (int j = j0; j < j1 && !s_bad; ++j) {
+                const UnionRec r = rec[vals[j]];
+                int rt[4];
+                for (int q = 0; q < 4 && !s_bad; ++q) {
+                    rt[q] = t.find(r.p[q]);
+                    if (rt[q] < 0) s_bad = 1;
+                }
+                for (int a = 1; a < 4 && !s_bad; ++a)
+                    for (int b = 0; b < a && !s_bad; ++b) {
+                        if (!joins(fixed, r.p[a], r.p[b])) continue;
+                        int px = rt[a], py = rt[b];
+                        if (px == py) continue;
+                        int sx = t.slot(px), sy = t.slot(py);
+                        if (sx < 0 || sy < 0) {
+                            s_bad = 1;
+                            break;
+                        }
+                        if (s_node[sx].w > s_node[sy].w) {  // the heavier set keeps its root (the second on equal)
+                            const int t1 = px;
+                            px = py;
+                            py = t1;
+                            const int t2 = sx;
+                            sx = sy;
+                            sy = t2;
+                        }
+                        const int st = t.slot(s_node[sy].tail);
+                        if (st < 0) {
+                            s_bad = 1;
+                            break;
+                        }
+                        s_node[sy].w += s_node[sx].w;
+                        s_node[sx].root = py;
+                        s_node[st].next = px;
+                        s_node[sy].tail = s_node[sx].tail;
+                        for (int q = 0; q < 4; ++q)
+                            if (rt[q] == px) rt[q] = py;
+                    }
+            }
+        }
+        __syncthreads();
+        if (s_bad) {
+            // the table filled up: the zone from global memory (untouched so far)
+            if (tid == 0) {
+                RootCache cache;
+                for (int j = j0; j < j1; ++j) replay_record(uf, fixed, rec[vals[j]], cache);
+            }
+        } else {
+            for (int h = tid; h < kTabSize; h += kReplayThreads)
+                if (s_key[h] >= 0) uf[s_key[h]] = s_node[h];
+        }
+        __syncthreads();
     }
 }
 
@@ -325,7 +493,18 @@ cudaError_t zone_pass(const ZoneBufs& z, const PassCounters* ctr_c, const uint8_
     if (e != cudaSuccess) return e;
     if (marks) stage_mark(marks, mark0, s);
     count_launch(), k_union_segments<<<blocks, 256, 0, s>>>(z.keys, ctr, cap, z.seg);
-    count_launch(), k_union_replay<<<blocks, 128, 0, s>>>(z.rec, ctr, cap, z.keys, z.vals, z.seg, fixed, z.uf);
+    const int big = z.replay_cta_min > 0 ? z.replay_cta_min : cap + 1;
+    count_launch(), k_union_replay<<<blocks, 128, 0, s>>>(z.rec, ctr, cap, z.keys, z.vals, z.seg, fixed, z.uf, big);
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_union_replay_cta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTabBytes) !=
+            cudaSuccess)
+            return cudaGetLastError();
+        attr = true;
+    }
+    if (z.replay_cta_min > 0)
+        count_launch(), k_union_replay_cta<<<152, kReplayThreads, kTabBytes, s>>>(z.rec, ctr, cap, z.keys, z.vals,
+                                                                                   z.seg, fixed, z.uf, big);
     if (marks) stage_mark(marks, mark0 + 1, s);
     const int pb = dn_pts ? 152 * 8 : (nblk(n_pts, 256) < 152 * 8 ? nblk(n_pts, 256) : 152 * 8);
     if (pb > 0)

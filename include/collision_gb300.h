@@ -290,8 +290,12 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
  *                           the window. Same results
  *   CC_TUNE_ZONE_CTA_MIN    members from which an impact zone's rigid
  *                           motion is computed by a CTA of its own (>= 16,
- *                           default 256; smaller zones of 16+ members get a
+ *                           default 64; smaller zones of 16+ members get a
  *                           warp, the rest a thread). Same results
+ *   CC_TUNE_REPLAY_CTA_MIN  union records from which a final impact zone's
+ *                           unions are replayed by a CTA in shared memory
+ *                           (default 128; 0: every zone by one thread from
+ *                           global memory). Same results
  * cc_get_tuning returns the current value, or -1 for an unknown knob. */
 enum {
     CC_TUNE_SPLIT_NARROW = 0,
@@ -315,7 +319,8 @@ enum {
     CC_TUNE_SMALL_SORT = 18,
     CC_TUNE_PRUNED_WARP = 19,
     CC_TUNE_ROBUST_ROOTS = 20,
-    CC_TUNE_ZONE_CTA_MIN = 21
+    CC_TUNE_ZONE_CTA_MIN = 21,
+    CC_TUNE_REPLAY_CTA_MIN = 22
 };
 cc_status cc_set_tuning(cc_solver* s, int knob, int value);
 int cc_get_tuning(cc_solver* s, int knob);

@@ -56,12 +56,14 @@ def _split(a, off, i):
 def _run_batch(solver_cls, mix, nsteps, mode=0, window=True, record=False, split=True, graph=True, combined=True,
                warp=False, packet=False, roles=True, overlap=False, rope=True, subset_refit=True, device_loop=True,
                refill=8, zone_cap=None, pair_capacity=None, small_sort=True, pruned_warp=True, robust_roots=True,
-               zone_cta_min=None):
+               zone_cta_min=None, replay_cta_min=None):
     b = solver_cls(0)
     b.assembleBatch(mix)
     b.setMode(mode)
     if zone_cta_min is not None:
         b.setTuning(solver_cls.TUNE_ZONE_CTA_MIN, zone_cta_min)
+    if replay_cta_min is not None:
+        b.setTuning(solver_cls.TUNE_REPLAY_CTA_MIN, replay_cta_min)
     b.setTuning(solver_cls.TUNE_ROBUST_ROOTS, int(robust_roots))
     b.setTuning(solver_cls.TUNE_SMALL_SORT, int(small_sort))
     b.setTuning(solver_cls.TUNE_PRUNED_WARP, int(pruned_warp))
@@ -547,3 +549,18 @@ def test_zone_cta_solve_agrees(solver_cls):
             assert np.array_equal(u[key], w[key]), (k, key)
         zone_steps += u["counters"]["zone_passes"] > 0
     assert zone_steps > 0
+
+
+def test_zone_replay_in_shared_memory_agrees(solver_cls):
+    # every final zone's unions replayed by a CTA in a shared-memory table
+    # (threshold 1), by one thread from global memory (0), and the default:
+    # the same unions in the same order, so the same zones and bits
+    for mix in (_contact_sample(), [scenes.large(n=65)]):
+        runs = [_run_batch(solver_cls, mix, 8, mode=1, zone_cap=50, replay_cta_min=m)[0] for m in (None, 1, 0)]
+        unions = 0
+        for k in range(8):
+            for other in runs[1:]:
+                for key in ("x", "v", "hc", "hcol", "status", "zones"):
+                    assert np.array_equal(runs[0][k][key], other[k][key]), (k, key)
+            unions += runs[0][k]["counters"]["zone_unions"]
+        assert unions > 0
