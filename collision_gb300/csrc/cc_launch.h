@@ -331,7 +331,7 @@ struct ZoneBufs {
     int n_pts_cap = 0;
     bool small_sort = true;              // sorts of up to 8192 records in one CTA
     int zone_cta_min = 64;               // zones of this many members are solved by a CTA each
-    int replay_cta_min = 128;            // zones with this many records are replayed in shared memory (0: never)
+    int replay_cta_min = 0;              // zones with this many records are replayed in shared memory (0: never)
 };
 size_t zone_sort_temp_bytes(int cap);
 // After a pass's impulses: join the pass's createImpZone records in the

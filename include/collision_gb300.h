@@ -294,8 +294,8 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
  *                           warp, the rest a thread). Same results
  *   CC_TUNE_REPLAY_CTA_MIN  union records from which a final impact zone's
  *                           unions are replayed by a CTA in shared memory
- *                           (default 128; 0: every zone by one thread from
- *                           global memory). Same results
+ *                           (0, the default: every zone by one thread from
+ *                           global memory, measured faster). Same results
  * cc_get_tuning returns the current value, or -1 for an unknown knob. */
 enum {
     CC_TUNE_SPLIT_NARROW = 0,
