@@ -312,6 +312,7 @@ struct ZoneBufs {
     unsigned long long* keys = nullptr;  // cap sort keys
     unsigned int* vals = nullptr;        // cap record indices
     int* seg = nullptr;                  // cap segment starts
+    uint8_t* noop = nullptr;             // cap: the record joins nothing new (k_union_noop)
     void* sort_temp = nullptr;           // zone_sort_temp_bytes(cap)
     int* cc = nullptr;                   // per point: parent in the lock-free union-find
     UfNode* uf = nullptr;                // per point: the reference's union-find

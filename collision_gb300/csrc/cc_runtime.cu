@@ -494,7 +494,7 @@ struct cc_solver {
         dfree(d_xo); dfree(d_av);
         dfree(d_urec);
         urec_cap = 0;
-        dfree(zb.keys); dfree(zb.vals); dfree(zb.seg); dfree(zb.cc); dfree(zb.uf); dfree(zb.zone_rng);
+        dfree(zb.keys); dfree(zb.vals); dfree(zb.seg); dfree(zb.noop); dfree(zb.cc); dfree(zb.uf); dfree(zb.zone_rng);
         dfree(zb.zone_root); dfree(zb.members); dfree(d_uf0); dfree(d_cc0);
         dfree(zb.prev_members); dfree(zb.prev_off); dfree(zb.prev_len); dfree(zb.prev_epoch); dfree(zb.epoch);
         if (zb.sort_temp) cudaFree(zb.sort_temp);
@@ -625,10 +625,12 @@ struct cc_solver {
         dfree(zb.keys);
         dfree(zb.vals);
         dfree(zb.seg);
+        dfree(zb.noop);
         if (zb.sort_temp) cudaFree(zb.sort_temp);
         zb.sort_temp = nullptr;
         if (dalloc(&d_urec, (size_t)cap) != cudaSuccess || dalloc(&zb.keys, (size_t)cap) != cudaSuccess ||
             dalloc(&zb.vals, (size_t)cap) != cudaSuccess || dalloc(&zb.seg, (size_t)cap) != cudaSuccess ||
+            dalloc(&zb.noop, (size_t)cap) != cudaSuccess ||
             cudaMalloc(&zb.sort_temp, zone_sort_temp_bytes(cap)) != cudaSuccess)
             return fail(CC_NO_MEMORY, "union record buffer");
         urec_cap = cap;

@@ -210,6 +210,39 @@ __device__ __forceinline__ void replay_record(UfNode* uf, const uint8_t* __restr
 
 // One thread per final zone touched by the pass: its records' unions in
 // visiting order, as createImpZone makes them.
+// Records that join nothing new: every pair the call joins already shares a
+// root in the union-find as the pass starts. Sets only grow, so such a
+// record joins nothing at its turn in the replay either, and skipping it
+// changes no root, weight, tail or next link.
+__device__ __forceinline__ int uf_root_ro(const UfNode* uf, int p) {
+    int r = p;
+    for (int k = 0; k < 64; ++k) {
+        const int nx = uf[r].root;
+        if (nx == r) return r;
+        r = nx;
+    }
+    return -1;  // a longer chain: no claim
+}
+
+__global__ void k_union_noop(const UnionRec* __restrict__ rec, const PassCounters* ctr, int cap,
+                             const uint8_t* __restrict__ fixed, const UfNode* __restrict__ uf, uint8_t* noop) {
+    if (ctr->err & kErrRetry) return;
+    const int n = count_of(&ctr->nunion, cap);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const UnionRec r = rec[i];
+        int rt[4];
+        for (int q = 0; q < 4; ++q) rt[q] = uf_root_ro(uf, r.p[q]);
+        bool nothing = true;
+        for (int a = 1; a < 4 && nothing; ++a)
+            for (int b = 0; b < a; ++b)
+                if (joins(fixed, r.p[a], r.p[b]) && (rt[a] < 0 || rt[a] != rt[b])) {
+                    nothing = false;
+                    break;
+                }
+        noop[i] = nothing ? 1 : 0;
+    }
+}
+
 // Final zones with at least big records are replayed by k_union_replay_cta.
 __device__ __forceinline__ bool big_segment(const unsigned long long* keys, int j0, int n, int big) {
     return j0 + big - 1 < n && keys[j0 + big - 1] == keys[j0];  // keys sorted by label
@@ -217,7 +250,8 @@ __device__ __forceinline__ bool big_segment(const unsigned long long* keys, int 
 
 __global__ void k_union_replay(const UnionRec* __restrict__ rec, const PassCounters* ctr, int cap,
                                const unsigned long long* __restrict__ keys, const unsigned int* __restrict__ vals,
-                               const int* __restrict__ seg, const uint8_t* __restrict__ fixed, UfNode* uf, int big) {
+                               const int* __restrict__ seg, const uint8_t* __restrict__ fixed, UfNode* uf, int big,
+                               const uint8_t* __restrict__ noop) {
     if (ctr->err & kErrRetry) return;
     const int n = count_of(&ctr->nunion, cap);
     const int nseg = ctr->nseg;
@@ -226,7 +260,10 @@ __global__ void k_union_replay(const UnionRec* __restrict__ rec, const PassCount
         if (big_segment(keys, j0, n, big)) continue;
         const unsigned long long lab = keys[j0];
         RootCache cache;
-        for (int j = j0; j < n && keys[j] == lab; ++j) replay_record(uf, fixed, rec[vals[j]], cache);
+        for (int j = j0; j < n && keys[j] == lab; ++j) {
+            const unsigned v = vals[j];
+            if (!noop[v]) replay_record(uf, fixed, rec[v], cache);
+        }
     }
 }
 
@@ -494,7 +531,9 @@ cudaError_t zone_pass(const ZoneBufs& z, const PassCounters* ctr_c, const uint8_
     if (marks) stage_mark(marks, mark0, s);
     count_launch(), k_union_segments<<<blocks, 256, 0, s>>>(z.keys, ctr, cap, z.seg);
     const int big = z.replay_cta_min > 0 ? z.replay_cta_min : cap + 1;
-    count_launch(), k_union_replay<<<blocks, 128, 0, s>>>(z.rec, ctr, cap, z.keys, z.vals, z.seg, fixed, z.uf, big);
+    count_launch(), k_union_noop<<<blocks, 256, 0, s>>>(z.rec, ctr, cap, fixed, z.uf, z.noop);
+    count_launch(), k_union_replay<<<blocks, 128, 0, s>>>(z.rec, ctr, cap, z.keys, z.vals, z.seg, fixed, z.uf, big,
+                                                          z.noop);
     static bool attr = false;
     if (!attr) {
         if (cudaFuncSetAttribute(k_union_replay_cta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTabBytes) !=
