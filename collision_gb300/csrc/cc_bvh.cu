@@ -288,13 +288,108 @@ __device__ __forceinline__ void refit_from(const Box6* __restrict__ box, const u
     }
 }
 
+// Arrival at a node of the refit: an add with acquire-release semantics at
+// GPU scope, so that the box the first child wrote before it is visible to
+// the second child after it (one atomic instead of fence, atomic, fence).
+__device__ __forceinline__ int arrive_acq_rel(int* p) {
+    int old;
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+    return old;
+}
+
+// One child's box in its parent's record (child 0: b0, b1.xy; child 1:
+// b1.zw, b2), written by that child's thread and read back through L2.
+__device__ __forceinline__ void put_child(BvhNode32* nd, int side, const Box32& b) {
+    float* f = reinterpret_cast<float*>(nd);
+    if (side == 0) {
+        *reinterpret_cast<float4*>(f) = make_float4(b.lo[0], b.lo[1], b.lo[2], b.hi[0]);
+        *reinterpret_cast<float2*>(f + 4) = make_float2(b.hi[1], b.hi[2]);
+    } else {
+        *reinterpret_cast<float2*>(f + 6) = make_float2(b.lo[0], b.lo[1]);
+        *reinterpret_cast<float4*>(f + 8) = make_float4(b.lo[2], b.hi[0], b.hi[1], b.hi[2]);
+    }
+}
+__device__ __forceinline__ Box32 get_child_cg(const BvhNode32* nd, int side) {
+    const float* f = reinterpret_cast<const float*>(nd);
+    Box32 b;
+    if (side == 0) {
+        const float4 a = __ldcg(reinterpret_cast<const float4*>(f));
+        const float2 c = __ldcg(reinterpret_cast<const float2*>(f + 4));
+        b.lo[0] = a.x; b.lo[1] = a.y; b.lo[2] = a.z; b.hi[0] = a.w; b.hi[1] = c.x; b.hi[2] = c.y;
+    } else {
+        const float2 a = __ldcg(reinterpret_cast<const float2*>(f + 6));
+        const float4 c = __ldcg(reinterpret_cast<const float4*>(f + 8));
+        b.lo[0] = a.x; b.lo[1] = a.y; b.lo[2] = c.x; b.hi[0] = c.y; b.hi[1] = c.z; b.hi[2] = c.w;
+    }
+    return b;
+}
+
+// The same refit with a shorter chain per level. Each thread carries its
+// subtree's box in registers and writes it into its side of the parent's
+// record before arriving; the second arrival reads only the other side
+// (one L2 round trip), and the next node's children and parent are loaded
+// while the arrival is in flight. The walk ends at the leaf's scene root
+// (run given; the node records above it, which mix scenes, are read by no
+// traversal), so passes over many scenes do not climb the levels between
+// scenes. The records and rope boxes it writes equal refit_from's.
+__device__ __forceinline__ void refit_up(const Box6* __restrict__ box, const unsigned int* __restrict__ order, int n,
+                                         int i, const int* __restrict__ parent, int* flags, BvhNode32* node,
+                                         RopeNode* rn, const unsigned long long* __restrict__ keys,
+                                         const SceneRun* __restrict__ run) {
+    if (i < 0 || i >= n) return;
+    int root = -1;  // one scene: up to the top
+    if (run) {
+        root = run[(int)(keys[i] >> 30)].root;
+        if (root < 0) return;  // a scene of one element: no pairs, no nodes
+    }
+    Box32 mine = box32_out(box[order[i]]);
+    int child = ~i;
+    int nd = parent[n - 1 + i];
+    if (nd < 0) return;
+    int4 meta = node[nd].meta;
+    int up = parent[nd];
+    for (;;) {
+        const int side = meta.x == child ? 0 : 1;
+        put_child(&node[nd], side, mine);
+        int4 meta_up = make_int4(0, 0, 0, 0);
+        int up2 = -1;
+        if (nd != root && up >= 0) {
+            meta_up = node[up].meta;
+            up2 = parent[up];
+        }
+        if (arrive_acq_rel(&flags[nd]) == 0) return;
+        const Box32 other = get_child_cg(&node[nd], side ^ 1);
+        for (int d = 0; d < 3; ++d) {
+            mine.lo[d] = fminf(mine.lo[d], other.lo[d]);
+            mine.hi[d] = fmaxf(mine.hi[d], other.hi[d]);
+        }
+        if (rn) {
+            float* o = rn[nd].lo;
+            *reinterpret_cast<float4*>(o) = make_float4(mine.lo[0], mine.lo[1], mine.lo[2], mine.hi[0]);
+            *reinterpret_cast<float2*>(o + 4) = make_float2(mine.hi[1], mine.hi[2]);
+        }
+        if (nd == root || up < 0) return;
+        child = nd;
+        nd = up;
+        meta = meta_up;
+        up = up2;
+    }
+}
+
 // dnsub (may be null): the count of sub in device memory; the grid strides.
+// UP: refit_up (keys and run used), else refit_from.
+template <bool UP>
 __global__ void k_refit(const Box6* __restrict__ box, const unsigned int* __restrict__ order, int n,
                         const int* __restrict__ sub, int nsub, const int* __restrict__ dnsub,
-                        const int* __restrict__ parent, int* flags, BvhNode32* node, RopeNode* rn) {
+                        const int* __restrict__ parent, int* flags, BvhNode32* node, RopeNode* rn,
+                        const unsigned long long* __restrict__ keys, const SceneRun* __restrict__ run) {
     const int m = sub ? (dnsub ? *dnsub : nsub) : n;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x)
-        refit_from(box, order, n, sub ? sub[k] : k, parent, flags, node, rn);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+        if (UP)
+            refit_up(box, order, n, sub ? sub[k] : k, parent, flags, node, rn, keys, run);
+        else
+            refit_from(box, order, n, sub ? sub[k] : k, parent, flags, node, rn);
+    }
 }
 
 // The LBVH node whose leaves are exactly scene s's (keys carry the scene id
@@ -1123,6 +1218,16 @@ void boxes_bbox(const Box6* box, int n, unsigned long long* bbox_enc, cudaStream
     if (n > 0) count_launch(), k_boxes_bbox<<<nblk(n, 256), 256, 0, s>>>(box, n, bbox_enc);
 }
 
+static void launch_refit(const Box6* box, const BvhBufs& b, int n, const int* sub, int nsub, const int* dnsub, int grid,
+                         RopeNode* rn, cudaStream_t s) {
+    if (b.refit_up)
+        count_launch(), k_refit<true><<<grid, 256, 0, s>>>(box, b.order, n, sub, nsub, dnsub, b.parent, b.flags, b.node,
+                                                           rn, b.keys, b.run);
+    else
+        count_launch(), k_refit<false><<<grid, 256, 0, s>>>(box, b.order, n, sub, nsub, dnsub, b.parent, b.flags,
+                                                            b.node, rn, nullptr, nullptr);
+}
+
 void bvh_build(const Box6* box, BvhBufs& b, cudaStream_t s) {
     int n = b.n;
     if (n <= 1) return;
@@ -1134,26 +1239,26 @@ void bvh_build(const Box6* box, BvhBufs& b, cudaStream_t s) {
     count_launch(), k_karras<<<nblk(n - 1, 256), 256, 0, s>>>(b.keys, n, b.node, b.range_hi, b.range_lo, b.parent,
                                                               ropes ? b.rope : nullptr);
     if (ropes) count_launch(), k_ropes<<<nblk(n - 1, 256), 256, 0, s>>>(b.node, b.rope, n, b.rnode);
-    cudaMemsetAsync(b.flags, 0, sizeof(int) * (size_t)(n - 1), s);
-    count_launch(), k_refit<<<nblk(n, 256), 256, 0, s>>>(box, b.order, n, nullptr, 0, nullptr, b.parent, b.flags,
-                                                         b.node, ropes ? b.rnode : nullptr);
+    // the scenes' roots first: the refit's walks end there
     if (b.run)
         count_launch(), k_scene_roots<<<nblk(b.nscenes, 128), 128, 0, s>>>(b.scenes, b.run, b.nscenes, n, b.parent,
                                                                           b.range_lo, b.range_hi);
+    cudaMemsetAsync(b.flags, 0, sizeof(int) * (size_t)(n - 1), s);
+    launch_refit(box, b, n, nullptr, 0, nullptr, nblk(n, 256), ropes ? b.rnode : nullptr, s);
 }
 
-void bvh_refit(const Box6* box, BvhBufs& b, cudaStream_t s) {
+void bvh_refit(const Box6* box, BvhBufs& b, cudaStream_t s, bool roots) {
     int n = b.n;
     if (n <= 1) return;
+    if (b.run && roots)
+        count_launch(), k_scene_roots<<<nblk(b.nscenes, 128), 128, 0, s>>>(b.scenes, b.run, b.nscenes, n, b.parent,
+                                                                          b.range_lo, b.range_hi);
     cudaMemsetAsync(b.flags, 0, sizeof(int) * (size_t)(n - 1), s);
     const int nleaf = b.sub ? b.nsub : n;
     if (nleaf > 0)
-        count_launch(), k_refit<<<b.sub && b.dnsub ? dev_grid(nleaf, 256) : nblk(nleaf, 256), 256, 0, s>>>(
-            box, b.order, n, b.sub, b.nsub, b.sub ? b.dnsub : nullptr, b.parent, b.flags, b.node,
-            b.rnode && b.rope ? b.rnode : nullptr);
-    if (b.run)
-        count_launch(), k_scene_roots<<<nblk(b.nscenes, 128), 128, 0, s>>>(b.scenes, b.run, b.nscenes, n, b.parent,
-                                                                          b.range_lo, b.range_hi);
+        launch_refit(box, b, n, b.sub, b.nsub, b.sub ? b.dnsub : nullptr,
+                     b.sub && b.dnsub ? dev_grid(nleaf, 256) : nblk(nleaf, 256), b.rnode && b.rope ? b.rnode : nullptr,
+                     s);
 }
 
 template <int DEPTH>

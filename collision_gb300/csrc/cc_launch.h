@@ -135,6 +135,10 @@ struct BvhBufs {
     // optional: the traversal's query count in device memory, when it
     // differs from the leaf count dnsub (the queries are sub's first ones)
     const int* dnq;
+    // refit walk: 1 one acquire-release arrival per level, each thread
+    // carrying its box and ending at its scene's root; 0 fence, arrival,
+    // fence and both children loaded per level, up to the top
+    int refit_up = 1;
 };
 
 // Leaf boxes of every element (static: x_old; moving: x_old and
@@ -154,11 +158,13 @@ void expand_scenes(const int* scene_ids, const int* elem_off, const int* pt_off,
 // Union of n given boxes in bbox_enc (the scene box the Morton keys use).
 void boxes_bbox(const Box6* box, int n, unsigned long long* bbox_enc, cudaStream_t s);
 // Morton keys (scene id above the 30 Morton bits, each scene normalised to
-// its own box), sort, Karras hierarchy, refit, per-scene subtree roots.
+// its own box), sort, Karras hierarchy, per-scene subtree roots, refit.
 void bvh_build(const Box6* box, BvhBufs& b, cudaStream_t s);
-// New boxes for the same leaves in the same hierarchy (refit and scene
-// roots only): the pairs found are the same, the tree is only less tight.
-void bvh_refit(const Box6* box, BvhBufs& b, cudaStream_t s);
+// New boxes for the same leaves in the same hierarchy (scene roots and
+// refit only): the pairs found are the same, the tree is only less tight.
+// roots = false: the scenes' roots set by the build stand (the hierarchy and
+// each scene's first leaf are unchanged since).
+void bvh_refit(const Box6* box, BvhBufs& b, cudaStream_t s, bool roots = true);
 // All leaf pairs of one scene with overlapping boxes, each unordered pair
 // once; scenes idle in this pass are skipped. With skip_shared_ev (the
 // elements' point ids), pairs of elements sharing a point are left out.

@@ -816,7 +816,10 @@ __global__ void __launch_bounds__(256) k_strain(const StrainEdgeStep* __restrict
 // test) run. The averaging itself is FP64, as in the reference.
 constexpr int kWindowAhead = 8;
 static_assert(kWindowAhead == kStrainAhead, "copy-ins are scheduled for the sweep's look-ahead");
-constexpr size_t kStrainWindowBytes = 200 * 1024;  // dynamic shared memory of one sweep CTA at most
+// dynamic shared memory of one sweep CTA at most: with the kernel's 2 KB of
+// static shared memory, within the 227 KB a CTA may hold (3,584 slots; a
+// 1025x1025 cloth needs 3,330)
+constexpr size_t kStrainWindowBytes = 224 * 1024;
 constexpr size_t kStrainWarpBytes = 200 * 1024;
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
@@ -931,15 +934,34 @@ struct WinArgs {
     int cbase, wbase;
 };
 
+// A thread's second and third edge records of the next level, for levels
+// wider than the block (WIDE sweeps): loaded a level early, so that they do
+// not wait on a global load inside their level.
+struct WideNext {
+    StrainEdgeHot x1, x2;
+};
+__device__ __forceinline__ void wide_fetch(WideNext& w, const int4& h, const StrainEdgeHot* __restrict__ hot,
+                                           int tid) {
+    const int e1 = h.x + tid + (int)blockDim.x, e2 = e1 + (int)blockDim.x;
+    if (e1 < h.y) w.x1 = hot[e1];
+    if (e2 < h.y) w.x2 = hot[e2];
+}
+
 // One level of the window sweep; J = level mod kWindowAhead.
-template <int J>
-__device__ __forceinline__ void win_level(const WinArgs& A, WinRing& r, WinSlot* s_win, int l, int tid,
+template <int J, bool WIDE>
+__device__ __forceinline__ void win_level(const WinArgs& A, WinRing& r, WideNext& wn, WinSlot* s_win, int l, int tid,
                                           int* n_avg, int* n_exact, bool* has) {
     constexpr int R = J % kRing;
     const int4 h0 = r.h0[R], h1 = r.h1[R];
     const StrainEdgeHot cur = r.hot[R];
     const int2 ld = r.ld[R], wb = r.wb[R];
     const int tc = tid - A.cbase, tw = tid - A.wbase;
+    StrainEdgeHot c1, c2;
+    if (WIDE) {
+        c1 = wn.x1;
+        c2 = wn.x2;
+        if (l + 1 < A.nlevels) wide_fetch(wn, r.h0[(J + 1) % kRing], A.hot, tid);
+    }
     win_fetch(r, R, l + kRing, A.nlevels, tid, tc, tw, A.s_hdr, A.hot, A.load_list, A.wb_list);
     if (J % kHdrChunk == 0 && l % kHdrChunk == 0 && l > 0) {
         // headers of levels [l + kHdrAhead, l + kHdrRing) into the slots of
@@ -1003,14 +1025,24 @@ __device__ __forceinline__ void win_level(const WinArgs& A, WinRing& r, WinSlot*
             A.av[ps.x] = make_double4_32a(a2.x, a2.y, b2.x, 0.0);
         }
     }
+    const int bd = (int)blockDim.x;
     int e = h0.x + tid;
     if (e < h0.y) {
         strain_window_edge(cur, e, A.edges, A.xo, s_win, A.dt32, A.dt, n_avg, n_exact, has);
-        for (e += blockDim.x; e < h0.y; e += blockDim.x)
+        if (WIDE) {
+            if (e + bd < h0.y) strain_window_edge(c1, e + bd, A.edges, A.xo, s_win, A.dt32, A.dt, n_avg, n_exact, has);
+            if (e + 2 * bd < h0.y)
+                strain_window_edge(c2, e + 2 * bd, A.edges, A.xo, s_win, A.dt32, A.dt, n_avg, n_exact, has);
+            e += 2 * bd;
+        }
+        for (e += bd; e < h0.y; e += bd)
             strain_window_edge(A.hot[e], e, A.edges, A.xo, s_win, A.dt32, A.dt, n_avg, n_exact, has);
     }
 }
 
+// WIDE: levels up to three times the block's width take their second and
+// third edges from registers loaded a level early (WideNext).
+template <bool WIDE>
 __global__ void __launch_bounds__(256) k_strain_window(const StrainEdge* __restrict__ edges,
                                                        const double4_32a* __restrict__ xo,
                                                        const StrainEdgeHot* __restrict__ hot,
@@ -1044,15 +1076,17 @@ __global__ void __launch_bounds__(256) k_strain_window(const StrainEdge* __restr
 #pragma unroll
     for (int j = 0; j < kRing; ++j)
         win_fetch(r, j, j, nlevels, tid, tid - cbase, tid - wbase, s_hdr, hot, load_list, wb_list);
+    WideNext wn;
+    if (WIDE && nlevels > 0) wide_fetch(wn, r.h0[0], hot, tid);
     for (int lb = 0; lb < nlevels; lb += kWindowAhead) {
-        win_level<0>(A, r, s_win, lb + 0, tid, &n_avg, &n_exact, &has);
-        if (lb + 1 < nlevels) win_level<1>(A, r, s_win, lb + 1, tid, &n_avg, &n_exact, &has);
-        if (lb + 2 < nlevels) win_level<2>(A, r, s_win, lb + 2, tid, &n_avg, &n_exact, &has);
-        if (lb + 3 < nlevels) win_level<3>(A, r, s_win, lb + 3, tid, &n_avg, &n_exact, &has);
-        if (lb + 4 < nlevels) win_level<4>(A, r, s_win, lb + 4, tid, &n_avg, &n_exact, &has);
-        if (lb + 5 < nlevels) win_level<5>(A, r, s_win, lb + 5, tid, &n_avg, &n_exact, &has);
-        if (lb + 6 < nlevels) win_level<6>(A, r, s_win, lb + 6, tid, &n_avg, &n_exact, &has);
-        if (lb + 7 < nlevels) win_level<7>(A, r, s_win, lb + 7, tid, &n_avg, &n_exact, &has);
+        win_level<0, WIDE>(A, r, wn, s_win, lb + 0, tid, &n_avg, &n_exact, &has);
+        if (lb + 1 < nlevels) win_level<1, WIDE>(A, r, wn, s_win, lb + 1, tid, &n_avg, &n_exact, &has);
+        if (lb + 2 < nlevels) win_level<2, WIDE>(A, r, wn, s_win, lb + 2, tid, &n_avg, &n_exact, &has);
+        if (lb + 3 < nlevels) win_level<3, WIDE>(A, r, wn, s_win, lb + 3, tid, &n_avg, &n_exact, &has);
+        if (lb + 4 < nlevels) win_level<4, WIDE>(A, r, wn, s_win, lb + 4, tid, &n_avg, &n_exact, &has);
+        if (lb + 5 < nlevels) win_level<5, WIDE>(A, r, wn, s_win, lb + 5, tid, &n_avg, &n_exact, &has);
+        if (lb + 6 < nlevels) win_level<6, WIDE>(A, r, wn, s_win, lb + 6, tid, &n_avg, &n_exact, &has);
+        if (lb + 7 < nlevels) win_level<7, WIDE>(A, r, wn, s_win, lb + 7, tid, &n_avg, &n_exact, &has);
     }
     asm volatile("cp.async.wait_group 0;\n" ::);
     __syncthreads();
@@ -1377,7 +1411,8 @@ size_t strain_step_bytes(int nedges) {
 int strain_window_slot_cap() { return (int)(kStrainWindowBytes / sizeof(WinSlot)); }
 
 void strain_configure() {
-    cudaFuncSetAttribute(k_strain_window, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStrainWindowBytes);
+    cudaFuncSetAttribute(k_strain_window<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStrainWindowBytes);
+    cudaFuncSetAttribute(k_strain_window<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStrainWindowBytes);
     cudaFuncSetAttribute(k_strain_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStrainWarpBytes);
 }
 
@@ -1409,8 +1444,12 @@ void strain_limit(const StrainEdge* edges, int nedges, const int4* hdr, const in
             count_launch(), k_strain_warp<<<nscenes, 32, plan.warp_smem, s>>>(
                 edges, xo, hot, hdr, scenes, cap, load_list, wb_list, av, pass, flags, passes_out, plan.max_window_slots,
                 plan.ecap, plan.lcap, plan.wcap, plan.order);
+        else if (plan.window && plan.ecap > plan.block)
+            count_launch(), k_strain_window<true><<<nscenes, plan.block, smem, s>>>(
+                edges, xo, hot, hdr, scenes, cap, load_list, wb_list, av, pass, flags, passes_out, plan.lcap > plan.block,
+                plan.order, plan.cbase, plan.wbase);
         else if (plan.window)
-            count_launch(), k_strain_window<<<nscenes, plan.block, smem, s>>>(
+            count_launch(), k_strain_window<false><<<nscenes, plan.block, smem, s>>>(
                 edges, xo, hot, hdr, scenes, cap, load_list, wb_list, av, pass, flags, passes_out, plan.lcap > plan.block,
                 plan.order, plan.cbase, plan.wbase);
         if (!plan.window || plan.any_global)

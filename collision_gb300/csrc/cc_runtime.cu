@@ -325,6 +325,7 @@ struct cc_solver {
     // reference tree order built on the GPU (cc_tree_gpu.cu)
     bool host_tree = false;          // CC_TUNE_HOST_TREE: emulate the insertions on host threads instead
     bool pruned_warp = true;         // CC_TUNE_PRUNED_WARP: one warp per pruned query
+    bool refit_up = true;            // CC_TUNE_REFIT_UP: the refit walk with one arrival per level
     bool robust_roots = true;        // CC_TUNE_ROBUST_ROOTS: correctly rounded roots only where decisive
     void* d_tree_scratch = nullptr;  // nodes, parent links and leaf counts of the trees being built
     int* d_tree_jobs = nullptr;      // 3 per tree: scene, first element, elements
@@ -1214,6 +1215,7 @@ cc_status cc_solver::assemble(const cc_mesh* meshes, int n) {
     bvh.ne_all = ne;
     bvh.scenes = d_scenes;
     bvh.run = d_run;
+    bvh.refit_up = refit_up ? 1 : 0;
     cc_status st = grow_pairs(8 * ne + 4096);
     if (st) return st;
     st = grow_contrib(4 * ne + 4096);
@@ -1555,7 +1557,7 @@ cc_status cc_solver::build_loop_graph(int n_hier) {
     tree_check(d_run, nscenes, bvh.bbox_enc, d_tree_vol, d_tree_built + nscenes, 1, d_rebuild, d_loop, cs);
     loop_reset(d_ctr, d_run, nscenes, d_loop, cs);
     mark(kStLoopBoxes - m0, cs);
-    bvh_refit(d_box, lb, cs);
+    bvh_refit(d_box, lb, cs, false);  // the roots of the proximity pass's build stand
     if (mode == 1)
         point_boxes(d_xo, d_av, d_vscene, d_scenes, d_act_p, nv, 1, d_pbox_lo, d_pbox_hi, d_p32, d_v32, cs,
                     &d_loop->npts);
@@ -2606,6 +2608,11 @@ cc_status cc_set_tuning(cc_solver* s, int knob, int value) {
             s->zb.replay_cta_min = value;
             s->loop_dirty = true;
             return CC_OK;
+        case CC_TUNE_REFIT_UP:
+            s->refit_up = value != 0;
+            s->bvh.refit_up = s->refit_up ? 1 : 0;
+            s->loop_dirty = true;
+            return CC_OK;
         case CC_TUNE_TRAVERSE_REFILL:
             if (value < 0 || value > 32) return CC_BAD_INPUT;
             s->tune.traverse_refill = value;
@@ -2657,6 +2664,7 @@ int cc_get_tuning(cc_solver* s, int knob) {
         case CC_TUNE_ROBUST_ROOTS: return s->robust_roots ? 1 : 0;
         case CC_TUNE_ZONE_CTA_MIN: return s->zb.zone_cta_min;
         case CC_TUNE_REPLAY_CTA_MIN: return s->zb.replay_cta_min;
+        case CC_TUNE_REFIT_UP: return s->refit_up ? 1 : 0;
         case CC_TUNE_STACK_DEPTH: return s->tune.stack_depth;
         case CC_TUNE_PAIR_CAPACITY: return s->pair_cap;
         default: return -1;

@@ -296,6 +296,11 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
  *                           unions are replayed by a CTA in shared memory
  *                           (0, the default: every zone by one thread from
  *                           global memory, measured faster). Same results
+ *   CC_TUNE_REFIT_UP        1 (default): the hierarchy refit's walk up takes
+ *                           one acquire-release arrival per level, carries
+ *                           its box in registers and ends at its scene's
+ *                           root; 0: fence, arrival, fence and both children
+ *                           loaded per level. Same results
  * cc_get_tuning returns the current value, or -1 for an unknown knob. */
 enum {
     CC_TUNE_SPLIT_NARROW = 0,
@@ -320,7 +325,8 @@ enum {
     CC_TUNE_PRUNED_WARP = 19,
     CC_TUNE_ROBUST_ROOTS = 20,
     CC_TUNE_ZONE_CTA_MIN = 21,
-    CC_TUNE_REPLAY_CTA_MIN = 22
+    CC_TUNE_REPLAY_CTA_MIN = 22,
+    CC_TUNE_REFIT_UP = 23
 };
 cc_status cc_set_tuning(cc_solver* s, int knob, int value);
 int cc_get_tuning(cc_solver* s, int knob);

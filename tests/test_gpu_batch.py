@@ -56,10 +56,11 @@ def _split(a, off, i):
 def _run_batch(solver_cls, mix, nsteps, mode=0, window=True, record=False, split=True, graph=True, combined=True,
                warp=False, packet=False, roles=True, overlap=False, rope=True, subset_refit=True, device_loop=True,
                refill=8, zone_cap=None, pair_capacity=None, small_sort=True, pruned_warp=True, robust_roots=True,
-               zone_cta_min=None, replay_cta_min=None):
+               zone_cta_min=None, replay_cta_min=None, refit_up=True):
     b = solver_cls(0)
     b.assembleBatch(mix)
     b.setMode(mode)
+    b.setTuning(solver_cls.TUNE_REFIT_UP, int(refit_up))
     if zone_cta_min is not None:
         b.setTuning(solver_cls.TUNE_ZONE_CTA_MIN, zone_cta_min)
     if replay_cta_min is not None:
@@ -516,6 +517,22 @@ def test_pruned_walks_agree(solver_cls, mode):
         for c in ("passes", "candidate_pairs", "visits", "hit_pairs", "contacts", "pruned_queries"):
             assert u["counters"][c] == w["counters"][c], (k, c)
     assert sum(u["counters"]["pruned_queries"] for u in a) > 0
+
+
+@pytest.mark.parametrize("device_loop", [True, False])
+def test_refit_walks_agree(solver_cls, device_loop):
+    # the hierarchy refit with one acquire-release arrival per level, ending
+    # at each scene's root, writes the node boxes the fenced walk to the top
+    # writes: the same pairs, counts and results, through the device loop
+    # and through the host's passes
+    mix = _contact_sample()
+    a, _, _ = _run_batch(solver_cls, mix, 8, mode=1, zone_cap=3, device_loop=device_loop, refit_up=True)
+    b, _, _ = _run_batch(solver_cls, mix, 8, mode=1, zone_cap=3, device_loop=device_loop, refit_up=False)
+    for k, (u, w) in enumerate(zip(a, b)):
+        for key in ("x", "v", "hc", "hcol", "status"):
+            assert np.array_equal(u[key], w[key]), (k, key)
+        for c in ("passes", "candidate_pairs", "visits", "hit_pairs", "contacts"):
+            assert u["counters"][c] == w["counters"][c], (k, c)
 
 
 def test_robust_roots_change_nothing(solver_cls):

@@ -245,3 +245,29 @@ def test_strain_sweeps_agree(solver_cls):
         x, v, hc = ra
     a.close()
     b.close()
+
+
+def test_wide_strain_window_agrees(solver_cls):
+    """A cloth whose strain levels are wider than the sweep's block (385x385:
+    up to ~290 edges a level, ~1,250 shared-memory slots) takes the window
+    sweep that holds a thread's later edges of a level in registers; its
+    velocities equal the global-memory sweep's."""
+    sc = scenes.large(n=385)
+    a, b = solver_cls(0), solver_cls(0)
+    for s, win in ((a, True), (b, False)):
+        s.assembleFromScene(sc)
+        s.setStrainWindow(win)
+    x, v, hc = sc.x.copy(), sc.v.copy(), np.zeros(sc.nv, np.uint8)
+    averaged = 0
+    for step in range(4):
+        xc = scenes.candidate(sc, x, v)
+        ra = a.resolveCollision(x, xc, v, hc)
+        rb = b.resolveCollision(x, xc, v, hc)
+        for u, w in zip(ra, rb):
+            assert np.array_equal(u, w), step
+        assert a.counters()["strain_averaged"] == b.counters()["strain_averaged"]
+        averaged += a.counters()["strain_averaged"]
+        x, v, hc = ra
+    assert averaged > 0
+    a.close()
+    b.close()
