@@ -94,45 +94,42 @@ constexpr double kPio2_1 = 0x1.921fb54400000p+0, kPio2_2 = 0x1.0b4611a600000p-34
 constexpr double kTwoOverPi = 0x1.45f306dc9c883p-1;
 constexpr double kLn2Hi = 0x1.62e42fefa39efp-1, kLn2Lo = 0x1.abc9e3b39803fp-56;
 
-// sin(r)/r and cos(r) as polynomials in r2 = r*r (Taylor, to r^29 / r^28)
-CR_HD dd sin_poly(dd r2) {
-    double t = 0x1.259f98b4358adp-103;
-    t = t * r2.hi + -0x1.d1ab1c2dccea3p-94;
-    t = t * r2.hi + 0x1.3f3ccdd165fa9p-84;
-    t = t * r2.hi + -0x1.761b41316381ap-75;
-    t = t * r2.hi + 0x1.71b8ef6dcf572p-66;
-    t = t * r2.hi + -0x1.2f49b46814157p-57;
+// sin(r)/r (cosine false) and cos(r) (cosine true) as polynomials in
+// r2 = r*r (Taylor, to r^29 / r^28). Both have the same shape, so lanes of a
+// warp that evaluate different ones run one instruction sequence.
+CR_HD dd sc_poly(dd r2, bool cosine) {
+#define CR_SEL(s, c) (cosine ? (c) : (s))
+    double t = CR_SEL(0x1.259f98b4358adp-103, 0x1.0a18a2635085dp-98);
+    t = t * r2.hi + CR_SEL(-0x1.d1ab1c2dccea3p-94, -0x1.88e85fc6a4e5ap-89);
+    t = t * r2.hi + CR_SEL(0x1.3f3ccdd165fa9p-84, 0x1.f2cf01972f578p-80);
+    t = t * r2.hi + CR_SEL(-0x1.761b41316381ap-75, -0x1.0ce396db7f853p-70);
+    t = t * r2.hi + CR_SEL(0x1.71b8ef6dcf572p-66, 0x1.e542ba4020225p-62);
+    t = t * r2.hi + CR_SEL(-0x1.2f49b46814157p-57, -0x1.6827863b97d97p-53);
     dd p = {t, 0.0};
-    p = add(mul(p, r2), dd{0x1.952c77030ad4ap-49, 0x1.ac981465ddc6cp-103});
-    p = add(mul(p, r2), dd{-0x1.ae7f3e733b81fp-41, -0x1.1d8656b0ee8cbp-97});
-    p = add(mul(p, r2), dd{0x1.6124613a86d09p-33, 0x1.f28e0cc748ebep-87});
-    p = add(mul(p, r2), dd{-0x1.ae64567f544e4p-26, 0x1.c062e06d1f209p-80});
-    p = add(mul(p, r2), dd{0x1.71de3a556c734p-19, -0x1.c154f8ddc6c00p-73});
-    p = add(mul(p, r2), dd{-0x1.a01a01a01a01ap-13, -0x1.a01a01a01a01ap-73});
-    p = add(mul(p, r2), dd{0x1.1111111111111p-7, 0x1.1111111111111p-63});
-    p = add(mul(p, r2), dd{-0x1.5555555555555p-3, -0x1.5555555555555p-57});
+    p = add(mul(p, r2), dd{CR_SEL(0x1.952c77030ad4ap-49, 0x1.ae7f3e733b81fp-45),
+                           CR_SEL(0x1.ac981465ddc6cp-103, 0x1.1d8656b0ee8cbp-101)});
+    p = add(mul(p, r2), dd{CR_SEL(-0x1.ae7f3e733b81fp-41, -0x1.93974a8c07c9dp-37),
+                           CR_SEL(-0x1.1d8656b0ee8cbp-97, -0x1.05d6f8a2efd1fp-92)});
+    p = add(mul(p, r2), dd{CR_SEL(0x1.6124613a86d09p-33, 0x1.1eed8eff8d898p-29),
+                           CR_SEL(0x1.f28e0cc748ebep-87, -0x1.2aec959e14c06p-83)});
+    p = add(mul(p, r2), dd{CR_SEL(-0x1.ae64567f544e4p-26, -0x1.27e4fb7789f5cp-22),
+                           CR_SEL(0x1.c062e06d1f209p-80, -0x1.cbbc05b4fa99ap-76)});
+    p = add(mul(p, r2), dd{CR_SEL(0x1.71de3a556c734p-19, 0x1.a01a01a01a01ap-16),
+                           CR_SEL(-0x1.c154f8ddc6c00p-73, 0x1.a01a01a01a01ap-76)});
+    p = add(mul(p, r2), dd{CR_SEL(-0x1.a01a01a01a01ap-13, -0x1.6c16c16c16c17p-10),
+                           CR_SEL(-0x1.a01a01a01a01ap-73, 0x1.f49f49f49f49fp-65)});
+    p = add(mul(p, r2), dd{CR_SEL(0x1.1111111111111p-7, 0x1.5555555555555p-5),
+                           CR_SEL(0x1.1111111111111p-63, 0x1.5555555555555p-59)});
+    p = add(mul(p, r2), dd{CR_SEL(-0x1.5555555555555p-3, -0x1.0000000000000p-1),
+                           CR_SEL(-0x1.5555555555555p-57, 0x0.0p+0)});
     p = add(mul(p, r2), dd{0x1.0000000000000p+0, 0x0.0p+0});
+#undef CR_SEL
     return p;
 }
-CR_HD dd cos_poly(dd r2) {
-    double t = 0x1.0a18a2635085dp-98;
-    t = t * r2.hi + -0x1.88e85fc6a4e5ap-89;
-    t = t * r2.hi + 0x1.f2cf01972f578p-80;
-    t = t * r2.hi + -0x1.0ce396db7f853p-70;
-    t = t * r2.hi + 0x1.e542ba4020225p-62;
-    t = t * r2.hi + -0x1.6827863b97d97p-53;
-    dd p = {t, 0.0};
-    p = add(mul(p, r2), dd{0x1.ae7f3e733b81fp-45, 0x1.1d8656b0ee8cbp-101});
-    p = add(mul(p, r2), dd{-0x1.93974a8c07c9dp-37, -0x1.05d6f8a2efd1fp-92});
-    p = add(mul(p, r2), dd{0x1.1eed8eff8d898p-29, -0x1.2aec959e14c06p-83});
-    p = add(mul(p, r2), dd{-0x1.27e4fb7789f5cp-22, -0x1.cbbc05b4fa99ap-76});
-    p = add(mul(p, r2), dd{0x1.a01a01a01a01ap-16, 0x1.a01a01a01a01ap-76});
-    p = add(mul(p, r2), dd{-0x1.6c16c16c16c17p-10, 0x1.f49f49f49f49fp-65});
-    p = add(mul(p, r2), dd{0x1.5555555555555p-5, 0x1.5555555555555p-59});
-    p = add(mul(p, r2), dd{-0x1.0000000000000p-1, 0x0.0p+0});
-    p = add(mul(p, r2), dd{0x1.0000000000000p+0, 0x0.0p+0});
-    return p;
-}
+
+CR_HD dd sin_poly(dd r2) { return sc_poly(r2, false); }
+CR_HD dd cos_poly(dd r2) { return sc_poly(r2, true); }
+
 // atanh(u)/u as a polynomial in u2 = u*u (to u^46)
 CR_HD dd atanh_poly(dd u2) {
     double t = 0x1.5c9882b931057p-6;
@@ -233,6 +230,34 @@ CR_HD void sincos(double x, double* sn, double* cs) {
     *sn = s.hi;
     *cs = c.hi;
 }
+
+#ifdef __CUDACC__
+// sincos(x) by a whole warp, every lane passing the same x: lane 1
+// evaluates the cosine polynomial while the others evaluate the sine one
+// (sc_poly, no divergence), which halves the serial chain of a one-lane
+// sincos. Every lane gets the values sincos gives.
+__device__ __forceinline__ void sincos_warp(double x, double* sn, double* cs) {
+    if (!(fabs(x) < 1048576.0) || x == 0.0) {  // the same branch in every lane
+        sincos(x, sn, cs);
+        return;
+    }
+    int q;
+    const dd r = reduce_pio2(x, &q);
+    const dd r2 = mul(r, r);
+    const bool cosine = (threadIdx.x & 31) == 1;
+    const dd p = sc_poly(r2, cosine);
+    const dd pr = mul(p, r);
+    const dd v = cosine ? p : pr;
+    const dd sr = {__shfl_sync(0xffffffffu, v.hi, 0), __shfl_sync(0xffffffffu, v.lo, 0)};
+    const dd cr_ = {__shfl_sync(0xffffffffu, v.hi, 1), __shfl_sync(0xffffffffu, v.lo, 1)};
+    switch (q) {
+        case 0: *sn = sr.hi; *cs = cr_.hi; break;
+        case 1: *sn = cr_.hi; *cs = neg(sr).hi; break;
+        case 2: *sn = neg(sr).hi; *cs = neg(cr_).hi; break;
+        default: *sn = neg(cr_).hi; *cs = sr.hi; break;
+    }
+}
+#endif
 
 // asin(t) for t in [0, 0.5] given as a double-double, as a double-double.
 CR_HD dd asin_small_dd(dd t) {

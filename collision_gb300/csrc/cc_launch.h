@@ -308,7 +308,8 @@ void zone_solve(const int* members, const int* zone_off, int nzones, const uint8
 // zone count in device memory (*dnz, at most zone_cap).
 void zone_solve_dev(const int* members, const int2* zone_rng, const int* dnz, int zone_cap, const uint8_t* fixed,
                     const double4_32a* xo, double4_32a* av, const int* vscene, const SceneDev* scenes,
-                    PassCounters* ctr, cudaStream_t s, PassStamp ps = PassStamp{}, int cta_min = 64);
+                    PassCounters* ctr, cudaStream_t s, PassStamp ps = PassStamp{}, int cta_min = 64,
+                    int few = 1024);
 
 // Impact zones of a pass on the GPU (cc_zones.cu): buffers of the union
 // replay and of the zone lists.
@@ -338,6 +339,7 @@ struct ZoneBufs {
     int n_pts_cap = 0;
     bool small_sort = true;              // sorts of up to 8192 records in one CTA
     int zone_cta_min = 64;               // zones of this many members are solved by a CTA each
+    int zone_few = 1024;                 // passes with at most this many zones: a warp per zone of 2+ members
     int replay_cta_min = 0;              // zones with this many records are replayed in shared memory (0: never)
 };
 size_t zone_sort_temp_bytes(int cap);

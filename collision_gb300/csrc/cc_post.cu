@@ -251,8 +251,12 @@ __device__ void zone_motion(const int* __restrict__ members, int i, int end, con
 }
 
 // Zones of at least this many members are solved one warp per zone
-// (k_zone_solve_warp) where the zone list is built on the device.
+// (k_zone_solve_warp) where the zone list is built on the device; in a pass
+// with at most `few` zones (a knob), every zone of two or more members is:
+// one thread per zone keeps the FP64 pipe busiest when zones are many, one
+// warp per zone gives the shortest chain when they are few.
 constexpr int kZoneWarpMin = 16;
+__device__ __forceinline__ int zone_warp_min(int nzones, int few) { return nzones <= few ? 2 : kZoneWarpMin; }
 constexpr int kZoneWarpBlock = 128;
 constexpr int kZoneCtaThreads = 256;
 
@@ -263,14 +267,15 @@ __global__ void k_zone_solve(const int* __restrict__ members, const int* __restr
                              const int2* __restrict__ zone_rng, int nzones, const int* __restrict__ dnz,
                              const uint8_t* __restrict__ fixed, const double4_32a* __restrict__ xo, double4_32a* av,
                              const int* __restrict__ vscene, const SceneDev* __restrict__ scenes,
-                             PassCounters* ctr, const SceneRun* __restrict__ run, PassStamp ps) {
+                             PassCounters* ctr, const SceneRun* __restrict__ run, PassStamp ps, int few) {
     if (dnz) {
         if (ctr->err & kErrRetry) return;
         if (*dnz < nzones) nzones = *dnz;
     }
+    const int warp_min = zone_warp_min(nzones, few);
     for (int z = blockIdx.x * blockDim.x + threadIdx.x; z < nzones; z += gridDim.x * blockDim.x) {
         const int i = zone_rng ? zone_rng[z].x : zone_off[z], end = zone_rng ? zone_rng[z].y : zone_off[z + 1];
-        if (dnz && end - i >= kZoneWarpMin) continue;  // k_zone_solve_warp's
+        if (dnz && end - i >= warp_min) continue;  // k_zone_solve_warp's
         zone_motion(members, i, end, fixed, xo, av, vscene, scenes, ctr, run, ps);
     }
 }
@@ -288,17 +293,18 @@ __global__ void __launch_bounds__(kZoneWarpBlock) k_zone_solve_warp(
     const int* __restrict__ members, const int2* __restrict__ zone_rng, int nzones, const int* __restrict__ dnz,
     const uint8_t* __restrict__ fixed, const double4_32a* __restrict__ xo, double4_32a* av,
     const int* __restrict__ vscene, const SceneDev* __restrict__ scenes, PassCounters* ctr, PassStamp ps,
-    int cta_min) {
+    int cta_min, int few) {
     __shared__ double stage[kZoneWarpBlock / 32][32][12];
     if (ctr->err & kErrRetry) return;
     if (*dnz < nzones) nzones = *dnz;
+    const int warp_min = zone_warp_min(nzones, few);
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     double(*st)[12] = stage[wib];
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     bool bad = false;
     for (int z = gw; z < nzones; z += nw) {
         const int i = zone_rng[z].x, end = zone_rng[z].y;
-        if (end - i < kZoneWarpMin || end - i >= cta_min) continue;
+        if (end - i < warp_min || end - i >= cta_min) continue;
         const Params prm = scenes[vscene[members[i]]].p;
         const double m = prm.m, dt = prm.dt;
         const int num_pts = end - i;
@@ -353,19 +359,14 @@ __global__ void __launch_bounds__(kZoneWarpBlock) k_zone_solve_warp(
         for (int d = 0; d < 3; ++d) L[d] = __shfl_sync(0xffffffffu, acc, d);
         for (int r = 0; r < 3; ++r)
             for (int q = 0; q < 3; ++q) I[r][q] = __shfl_sync(0xffffffffu, acc, 3 + 3 * r + q);
-        double w[3] = {0.0, 0.0, 0.0}, mag_w = 0.0, sw = 0.0, cw = 0.0;
-        if (lane == 0) {
-            zone_omega(I, L, w);
-            mag_w = mag3(w);
-            double sn, cs;
-            cr::sincos(dt * mag_w, &sn, &cs);
-            sw = mag_w < kRoundEps ? 0.0 : sn / mag_w;
-            cw = cs;
-        }
-        for (int d = 0; d < 3; ++d) w[d] = __shfl_sync(0xffffffffu, w[d], 0);
-        mag_w = __shfl_sync(0xffffffffu, mag_w, 0);
-        sw = __shfl_sync(0xffffffffu, sw, 0);
-        cw = __shfl_sync(0xffffffffu, cw, 0);
+        // every lane forms the same rotation (sin and cos on two lanes)
+        double w[3];
+        zone_omega(I, L, w);
+        const double mag_w = mag3(w);
+        double sn, cs;
+        cr::sincos_warp(dt * mag_w, &sn, &cs);
+        const double sw = mag_w < kRoundEps ? 0.0 : sn / mag_w;
+        const double cw = cs;
         for (int q = i + lane; q < end; q += 32)
             bad |= zone_member_motion(members[q], fixed, xo, av, x_cm, v_cm, w, mag_w, sw, cw, dt, ps);
         __syncwarp();
@@ -445,7 +446,7 @@ __global__ void __launch_bounds__(kZoneCtaThreads) k_zone_solve_cta(
         }
         if (tid < 12) s_sum[tid] = acc;
         __syncthreads();
-        if (tid == 0) {
+        if (tid < 32) {  // warp 0: the same rotation in every lane, sin and cos on two lanes
             double L[3], I[3][3], w[3];
             for (int d = 0; d < 3; ++d) L[d] = s_sum[d];
             for (int r = 0; r < 3; ++r)
@@ -453,11 +454,13 @@ __global__ void __launch_bounds__(kZoneCtaThreads) k_zone_solve_cta(
             zone_omega(I, L, w);
             const double mag_w = mag3(w);
             double sn, cs;
-            cr::sincos(dt * mag_w, &sn, &cs);
-            for (int d = 0; d < 3; ++d) s_rot[d] = w[d];
-            s_rot[3] = mag_w;
-            s_rot[4] = mag_w < kRoundEps ? 0.0 : sn / mag_w;
-            s_rot[5] = cs;
+            cr::sincos_warp(dt * mag_w, &sn, &cs);
+            if (tid == 0) {
+                for (int d = 0; d < 3; ++d) s_rot[d] = w[d];
+                s_rot[3] = mag_w;
+                s_rot[4] = mag_w < kRoundEps ? 0.0 : sn / mag_w;
+                s_rot[5] = cs;
+            }
         }
         __syncthreads();
         const double w[3] = {s_rot[0], s_rot[1], s_rot[2]};
@@ -1367,23 +1370,24 @@ void zone_solve(const int* members, const int* zone_off, int nzones, const uint8
                 const SceneRun* run, PassStamp ps) {
     if (nzones > 0)
         count_launch(), k_zone_solve<<<nblk(nzones, 128), 128, 0, s>>>(members, zone_off, nullptr, nzones, nullptr,
-                                                                       fixed, xo, av, vscene, scenes, ctr, run, ps);
+                                                                       fixed, xo, av, vscene, scenes, ctr, run, ps, 0);
 }
 
 void zone_solve_dev(const int* members, const int2* zone_rng, const int* dnz, int zone_cap, const uint8_t* fixed,
                     const double4_32a* xo, double4_32a* av, const int* vscene, const SceneDev* scenes,
-                    PassCounters* ctr, cudaStream_t s, PassStamp ps, int cta_min) {
+                    PassCounters* ctr, cudaStream_t s, PassStamp ps, int cta_min, int few) {
     if (cta_min < kZoneWarpMin) cta_min = kZoneWarpMin;
     int blocks = nblk(zone_cap, 64);
     if (blocks > 152 * 8) blocks = 152 * 8;
     if (blocks > 0)
         count_launch(), k_zone_solve<<<blocks, 64, 0, s>>>(members, nullptr, zone_rng, zone_cap, dnz, fixed, xo, av,
-                                                           vscene, scenes, ctr, nullptr, ps);
+                                                           vscene, scenes, ctr, nullptr, ps, few);
     int wblocks = nblk(zone_cap, kZoneWarpBlock / 32);
     if (wblocks > 152 * 4) wblocks = 152 * 4;
     if (wblocks > 0)
         count_launch(), k_zone_solve_warp<<<wblocks, kZoneWarpBlock, 0, s>>>(members, zone_rng, zone_cap, dnz, fixed,
-                                                                            xo, av, vscene, scenes, ctr, ps, cta_min);
+                                                                            xo, av, vscene, scenes, ctr, ps, cta_min,
+                                                                            few);
     const int cblocks = zone_cap < 152 * 2 ? zone_cap : 152 * 2;
     if (cblocks > 0)
         count_launch(), k_zone_solve_cta<<<cblocks, kZoneCtaThreads, 0, s>>>(members, zone_rng, zone_cap, dnz, fixed,

@@ -500,10 +500,11 @@ struct cc_solver {
         dfree(zb.prev_members); dfree(zb.prev_off); dfree(zb.prev_len); dfree(zb.prev_epoch); dfree(zb.epoch);
         if (zb.sort_temp) cudaFree(zb.sort_temp);
         const bool small_sort = zb.small_sort;  // settings, not buffers
-        const int zone_cta_min = zb.zone_cta_min, replay_cta_min = zb.replay_cta_min;
+        const int zone_cta_min = zb.zone_cta_min, replay_cta_min = zb.replay_cta_min, zone_few = zb.zone_few;
         zb = ZoneBufs{};
         zb.small_sort = small_sort;
         zb.zone_cta_min = zone_cta_min;
+        zb.zone_few = zone_few;
         zb.replay_cta_min = replay_cta_min;
         uf_on_device = false;
         dfree(d_xold_in); dfree(d_xcand_in); dfree(d_vel); dfree(d_xout); dfree(d_hc);
@@ -2608,6 +2609,11 @@ cc_status cc_set_tuning(cc_solver* s, int knob, int value) {
             s->zb.replay_cta_min = value;
             s->loop_dirty = true;
             return CC_OK;
+        case CC_TUNE_ZONE_FEW:
+            if (value < 0) return CC_BAD_INPUT;
+            s->zb.zone_few = value;
+            s->loop_dirty = true;
+            return CC_OK;
         case CC_TUNE_REFIT_UP:
             s->refit_up = value != 0;
             s->bvh.refit_up = s->refit_up ? 1 : 0;
@@ -2665,6 +2671,7 @@ int cc_get_tuning(cc_solver* s, int knob) {
         case CC_TUNE_ZONE_CTA_MIN: return s->zb.zone_cta_min;
         case CC_TUNE_REPLAY_CTA_MIN: return s->zb.replay_cta_min;
         case CC_TUNE_REFIT_UP: return s->refit_up ? 1 : 0;
+        case CC_TUNE_ZONE_FEW: return s->zb.zone_few;
         case CC_TUNE_STACK_DEPTH: return s->tune.stack_depth;
         case CC_TUNE_PAIR_CAPACITY: return s->pair_cap;
         default: return -1;

@@ -558,7 +558,7 @@ cudaError_t zone_pass(const ZoneBufs& z, const PassCounters* ctr_c, const uint8_
     count_launch(), k_zone_epoch<<<1, 1, 0, s>>>(ctr, z.epoch);
     if (marks) stage_mark(marks, mark0 + 2, s);
     zone_solve_dev(z.members, z.zone_rng, &ctr->nzones, z.zone_cap, fixed, xo, av, vscene, scenes, ctr, s, ps,
-                   z.zone_cta_min);
+                   z.zone_cta_min, z.zone_few);
     if (marks) stage_mark(marks, mark0 + 3, s);
     return cudaGetLastError();
 }

@@ -187,7 +187,7 @@ class CollisionSolver3d:
     TUNE_COMBINED_BROAD, TUNE_STRAIN_WARP, TUNE_PACKET_TRAVERSE, TUNE_STRAIN_ROLES, TUNE_TAIL_OVERLAP = 5, 6, 7, 8, 9
     TUNE_ROPE_TRAVERSE, TUNE_SUBSET_REFIT, TUNE_TRAVERSE_REFILL, TUNE_STACK_DEPTH, TUNE_PAIR_CAPACITY = 10, 11, 12, 13, 14
     TUNE_DEVICE_LOOP, TUNE_PRUNE, TUNE_HOST_TREE, TUNE_SMALL_SORT, TUNE_PRUNED_WARP = 15, 16, 17, 18, 19
-    TUNE_ROBUST_ROOTS, TUNE_ZONE_CTA_MIN, TUNE_REPLAY_CTA_MIN, TUNE_REFIT_UP = 20, 21, 22, 23
+    TUNE_ROBUST_ROOTS, TUNE_ZONE_CTA_MIN, TUNE_REPLAY_CTA_MIN, TUNE_REFIT_UP, TUNE_ZONE_FEW = 20, 21, 22, 23, 24
 
     def setTuning(self, knob: int, value: int):
         """Launch shapes and the two-stage narrow phase; none changes results."""

@@ -301,6 +301,10 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
  *                           its box in registers and ends at its scene's
  *                           root; 0: fence, arrival, fence and both children
  *                           loaded per level. Same results
+ *   CC_TUNE_ZONE_FEW        impact zones in a pass at or below which every
+ *                           zone of two or more members is solved by a warp
+ *                           (default 1024; above it, zones under 16 members
+ *                           get a thread each). Same results
  * cc_get_tuning returns the current value, or -1 for an unknown knob. */
 enum {
     CC_TUNE_SPLIT_NARROW = 0,
@@ -326,7 +330,8 @@ enum {
     CC_TUNE_ROBUST_ROOTS = 20,
     CC_TUNE_ZONE_CTA_MIN = 21,
     CC_TUNE_REPLAY_CTA_MIN = 22,
-    CC_TUNE_REFIT_UP = 23
+    CC_TUNE_REFIT_UP = 23,
+    CC_TUNE_ZONE_FEW = 24
 };
 cc_status cc_set_tuning(cc_solver* s, int knob, int value);
 int cc_get_tuning(cc_solver* s, int knob);

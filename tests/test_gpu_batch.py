@@ -56,11 +56,13 @@ def _split(a, off, i):
 def _run_batch(solver_cls, mix, nsteps, mode=0, window=True, record=False, split=True, graph=True, combined=True,
                warp=False, packet=False, roles=True, overlap=False, rope=True, subset_refit=True, device_loop=True,
                refill=8, zone_cap=None, pair_capacity=None, small_sort=True, pruned_warp=True, robust_roots=True,
-               zone_cta_min=None, replay_cta_min=None, refit_up=True):
+               zone_cta_min=None, replay_cta_min=None, refit_up=True, zone_few=None):
     b = solver_cls(0)
     b.assembleBatch(mix)
     b.setMode(mode)
     b.setTuning(solver_cls.TUNE_REFIT_UP, int(refit_up))
+    if zone_few is not None:
+        b.setTuning(solver_cls.TUNE_ZONE_FEW, zone_few)
     if zone_cta_min is not None:
         b.setTuning(solver_cls.TUNE_ZONE_CTA_MIN, zone_cta_min)
     if replay_cta_min is not None:
@@ -566,6 +568,23 @@ def test_zone_cta_solve_agrees(solver_cls):
             assert np.array_equal(u[key], w[key]), (k, key)
         zone_steps += u["counters"]["zone_passes"] > 0
     assert zone_steps > 0
+
+
+def test_zone_warp_solve_for_few_zones_agrees(solver_cls):
+    # zones of 2-15 members solved one thread each (ZONE_FEW 0), one warp
+    # each in every pass (a large ZONE_FEW) and the default (a warp each
+    # where a pass has at most 1,024 zones): the same operations in the same
+    # order - the warps' sin and cos on two lanes equal one thread's sincos -
+    # so the same bits
+    for mix in (_contact_sample(), [scenes.large(n=65)]):
+        runs = [_run_batch(solver_cls, mix, 8, mode=1, zone_cap=50, zone_few=f)[0] for f in (0, 1 << 30, None)]
+        zone_steps = 0
+        for k in range(8):
+            for other in runs[1:]:
+                for key in ("x", "v", "hc", "hcol", "status", "zones"):
+                    assert np.array_equal(runs[0][k][key], other[k][key]), (k, key)
+            zone_steps += runs[0][k]["counters"]["zone_passes"] > 0
+        assert zone_steps > 0
 
 
 def test_zone_replay_in_shared_memory_agrees(solver_cls):
