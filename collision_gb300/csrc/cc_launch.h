@@ -236,6 +236,9 @@ struct NarrowArgs {
     // the split sub-tests form a root again with correctly rounded functions
     // only where a decision can depend on it (is_coplanar's rb); 0: always
     int robust_roots = 1;
+    // 1: both sub-test lists in one launch, a warp per sub-test in small
+    // passes (k_subtests_all); 0: one launch per list, a thread per sub-test
+    int sub_merge = 1;
     // movable rigid bodies: the body of each point (-1 none), each body's
     // mass, and the contribution slot of body 0 (the point count)
     const int* vbody;
@@ -372,6 +375,10 @@ void loop_expand(const int* sel, const int* eoff, const int* poff, const SceneDe
 void tree_check(const SceneRun* run, int nscenes, const unsigned long long* bbox_enc, const double* vol,
                 const int* built, int which, int* rebuild, LoopCtl* L, cudaStream_t s);
 void loop_reset(PassCounters* c, SceneRun* run, int nscenes, LoopCtl* L, cudaStream_t s);
+// tree_check then loop_reset as one launch (one block; the two launches
+// above 4,096 scenes).
+void tree_check_reset(SceneRun* run, int nscenes, const unsigned long long* bbox_enc, const double* vol,
+                      const int* built, int which, int* rebuild, LoopCtl* L, PassCounters* c, cudaStream_t s);
 // Stage profiling inside the loop graph: acc[0] the last boundary's time,
 // then (ns, count) for each of kLoopMarkSlots slots 1.. - the time since the
 // previous boundary - then a per-pass log (the row count, then

@@ -200,11 +200,10 @@ __device__ __forceinline__ double dec_double(unsigned long long e) {
 // every scene of the pass: its tree `which` is unbuilt, or the root volume of
 // this pass's boxes has grown by more than 20% over the volume both trees
 // share. Such a scene is flagged for the host, and the pass stops.
-__global__ void k_tree_check(const SceneRun* __restrict__ run, int nscenes, const unsigned long long* bbox_enc,
-                             const double* __restrict__ vol, const int* __restrict__ built, int which, int* rebuild,
-                             LoopCtl* L) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (L->nact == 0 || s >= nscenes || run[s].mode == kSceneIdle || run[s].leaf0 < 0) return;
+__device__ __forceinline__ void tree_check_one(const SceneRun* __restrict__ run, int s,
+                                               const unsigned long long* bbox_enc, const double* __restrict__ vol,
+                                               const int* __restrict__ built, int which, int* rebuild, LoopCtl* L) {
+    if (run[s].mode == kSceneIdle || run[s].leaf0 < 0) return;
     double lo[3], hi[3];
     for (int d = 0; d < 3; ++d) {
         lo[d] = dec_double(bbox_enc[6 * s + d]);
@@ -218,27 +217,53 @@ __global__ void k_tree_check(const SceneRun* __restrict__ run, int nscenes, cons
     }
 }
 
+__global__ void k_tree_check(const SceneRun* __restrict__ run, int nscenes, const unsigned long long* bbox_enc,
+                             const double* __restrict__ vol, const int* __restrict__ built, int which, int* rebuild,
+                             LoopCtl* L) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (L->nact == 0 || s >= nscenes) return;
+    tree_check_one(run, s, bbox_enc, vol, built, which, rebuild, L);
+}
+
 // Counters and hit counts of a pass about to run. A pass stopped for the
 // host keeps the error bit kErrHost (nothing of it is applied) and covers no
 // elements or points.
+__device__ __forceinline__ void loop_reset_counters(PassCounters* c, LoopCtl* L) {
+    const int keep = c->err & kErrNan;
+    const bool stop = L->host != 0;
+    c->npairs = (!stop && L->reuse_n >= 0) ? L->reuse_n : 0;
+    c->ncontrib = 0; c->nhit_pairs = 0; c->nrec = 0; c->nvisits = 0; c->ncontacts = 0; c->nsub = 0;
+    c->ncr = 0; c->nunion = 0; c->nsub_pt = 0; c->nsub_ee = 0; c->npairq = 0; c->nzones = 0; c->nmembers = 0;
+    c->nseg = 0;
+    c->err = keep | (stop ? kErrHost : 0);
+    if (stop) {
+        L->nbroad = 0;
+        L->npts = 0;
+        L->nq_full = 0;
+        L->prune = 0;
+    }
+}
+
 __global__ void k_loop_reset(PassCounters* c, SceneRun* run, int nscenes, LoopCtl* L) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) {
-        const int keep = c->err & kErrNan;
-        const bool stop = L->host != 0;
-        c->npairs = (!stop && L->reuse_n >= 0) ? L->reuse_n : 0;
-        c->ncontrib = 0; c->nhit_pairs = 0; c->nrec = 0; c->nvisits = 0; c->ncontacts = 0; c->nsub = 0;
-        c->ncr = 0; c->nunion = 0; c->nsub_pt = 0; c->nsub_ee = 0; c->npairq = 0; c->nzones = 0; c->nmembers = 0;
-        c->nseg = 0;
-        c->err = keep | (stop ? kErrHost : 0);
-        if (stop) {
-            L->nbroad = 0;
-            L->npts = 0;
-            L->nq_full = 0;
-            L->prune = 0;
-        }
-    }
+    if (i == 0) loop_reset_counters(c, L);
     if (i < nscenes) run[i].hits = 0;
+}
+
+// k_tree_check then k_loop_reset in one block (one launch less per pass):
+// every scene's test, a barrier (the reset reads the stop bit any test may
+// set), then the reset.
+__global__ void __launch_bounds__(1024) k_tree_check_reset(SceneRun* run, int nscenes,
+                                                            const unsigned long long* bbox_enc,
+                                                            const double* __restrict__ vol,
+                                                            const int* __restrict__ built, int which, int* rebuild,
+                                                            LoopCtl* L, PassCounters* c) {
+    if (L->nact != 0)
+        for (int s = threadIdx.x; s < nscenes; s += blockDim.x)
+            tree_check_one(run, s, bbox_enc, vol, built, which, rebuild, L);
+    __syncthreads();
+    if (threadIdx.x == 0) loop_reset_counters(c, L);
+    for (int s = threadIdx.x; s < nscenes; s += blockDim.x) run[s].hits = 0;
 }
 
 // Closes a pass. A pass that stopped or failed stops the loop (the host
@@ -352,6 +377,17 @@ void tree_check(const SceneRun* run, int nscenes, const unsigned long long* bbox
                 const int* built, int which, int* rebuild, LoopCtl* L, cudaStream_t s) {
     count_launch(), k_tree_check<<<nblk(nscenes, 128), 128, 0, s>>>(run, nscenes, bbox_enc, vol, built, which,
                                                                     rebuild, L);
+}
+
+void tree_check_reset(SceneRun* run, int nscenes, const unsigned long long* bbox_enc, const double* vol,
+                      const int* built, int which, int* rebuild, LoopCtl* L, PassCounters* c, cudaStream_t s) {
+    if (nscenes > 4096) {
+        tree_check(run, nscenes, bbox_enc, vol, built, which, rebuild, L, s);
+        loop_reset(c, run, nscenes, L, s);
+        return;
+    }
+    const int t = nscenes < 32 ? 32 : (nscenes < 1024 ? (nscenes + 31) / 32 * 32 : 1024);
+    count_launch(), k_tree_check_reset<<<1, t, 0, s>>>(run, nscenes, bbox_enc, vol, built, which, rebuild, L, c);
 }
 
 void loop_reset(PassCounters* c, SceneRun* run, int nscenes, LoopCtl* L, cudaStream_t s) {

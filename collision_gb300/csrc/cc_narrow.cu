@@ -285,12 +285,12 @@ __global__ void __launch_bounds__(128) k_zone_unions(NarrowArgs a) {
     }
 }
 
-// Stage 2: one queued sub-test per thread, the FP64 test of k_narrow.
-template <bool MOVING, bool EE>
-__global__ void __launch_bounds__(128, 4) k_subtests(NarrowArgs a) {
-    const SubRec* list = EE ? a.sub_ee : a.sub_pt;
-    int n = EE ? a.ctr->nsub_ee : a.ctr->nsub_pt;
-    if (n > a.sub_cap) n = a.sub_cap;
+// Stage 2: the FP64 test of k_narrow for each queued sub-test.
+struct SubTally {
+    int hits = 0, cr = 0, contacts = 0, sub = 0;
+};
+
+__device__ __forceinline__ NarrowCtx subtest_ctx(const NarrowArgs& a) {
     NarrowCtx c;
     c.xo = a.xo; c.av = a.av; c.fixed = a.fixed; c.ev = a.ev; c.esurf = a.esurf; c.erigid = a.erigid;
     c.vbody = a.vbody; c.body_mass = a.body_mass; c.body_slot0 = a.body_slot0;
@@ -301,41 +301,92 @@ __global__ void __launch_bounds__(128, 4) k_subtests(NarrowArgs a) {
     c.check = 0;
     c.robust_roots = a.robust_roots;
     c.zone = 0;
-    int t_hits = 0, t_cr = 0, t_contacts = 0, t_sub = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const SubRec r = list[i];
-        c.p = a.scenes[r.scene].p;
-        c.pass = 0;
-        CallState st;
-        st.keybase = r.keybase;
-        st.np = 0;
-        st.sub = r.sub;
-        st.nsub = 0;
-        st.ncr = 0;
-        st.ncontacts = 0;
-        bool hit = MOVING ? moving_test<EE>(c, st, r.p) : static_test<EE>(c, st, r.p);
-        t_sub++;
-        t_cr += st.ncr;
-        t_contacts += st.ncontacts;
-        if (hit)
-            for (int q = 0; q < 4; ++q) stamp_point(a.ps, r.p[q]);
-        if (hit && atomicOr(&a.pair_hit[r.pair], 1 << r.sub) == 0) {
-            t_hits++;
-            atomicAdd(&a.run[r.scene].hits, 1);
-        }
+    return c;
+}
+
+// One sub-test: its test, the stamps of its points and its pair's hit flag
+// when it hits, the scene's hit count when it is the pair's first.
+template <bool MOVING, bool EE>
+__device__ __forceinline__ void one_subtest(const NarrowArgs& a, NarrowCtx& c, const SubRec& r, SubTally& t) {
+    c.p = a.scenes[r.scene].p;
+    c.pass = 0;
+    CallState st;
+    st.keybase = r.keybase;
+    st.np = 0;
+    st.sub = r.sub;
+    st.nsub = 0;
+    st.ncr = 0;
+    st.ncontacts = 0;
+    bool hit = MOVING ? moving_test<EE>(c, st, r.p) : static_test<EE>(c, st, r.p);
+    t.sub++;
+    t.cr += st.ncr;
+    t.contacts += st.ncontacts;
+    if (hit)
+        for (int q = 0; q < 4; ++q) stamp_point(a.ps, r.p[q]);
+    if (hit && atomicOr(&a.pair_hit[r.pair], 1 << r.sub) == 0) {
+        t.hits++;
+        atomicAdd(&a.run[r.scene].hits, 1);
     }
+}
+
+// The pass's counters from every thread's tally (all lanes take part).
+__device__ __forceinline__ void subtest_counts(const NarrowArgs& a, SubTally t) {
     for (int o = 16; o > 0; o >>= 1) {
-        t_hits += __shfl_xor_sync(0xffffffffu, t_hits, o);
-        t_cr += __shfl_xor_sync(0xffffffffu, t_cr, o);
-        t_contacts += __shfl_xor_sync(0xffffffffu, t_contacts, o);
-        t_sub += __shfl_xor_sync(0xffffffffu, t_sub, o);
+        t.hits += __shfl_xor_sync(0xffffffffu, t.hits, o);
+        t.cr += __shfl_xor_sync(0xffffffffu, t.cr, o);
+        t.contacts += __shfl_xor_sync(0xffffffffu, t.contacts, o);
+        t.sub += __shfl_xor_sync(0xffffffffu, t.sub, o);
     }
     if ((threadIdx.x & 31) == 0) {
-        if (t_hits) atomicAdd(&a.ctr->nhit_pairs, t_hits);
-        if (t_cr) atomicAdd(&a.ctr->ncr, t_cr);
-        if (t_contacts) atomicAdd(&a.ctr->ncontacts, t_contacts);
-        if (t_sub) atomicAdd(&a.ctr->nsub, t_sub);
+        if (t.hits) atomicAdd(&a.ctr->nhit_pairs, t.hits);
+        if (t.cr) atomicAdd(&a.ctr->ncr, t.cr);
+        if (t.contacts) atomicAdd(&a.ctr->ncontacts, t.contacts);
+        if (t.sub) atomicAdd(&a.ctr->nsub, t.sub);
     }
+}
+
+// One list (point-triangle or edge-edge), one sub-test per thread.
+template <bool MOVING, bool EE>
+__global__ void __launch_bounds__(128, 4) k_subtests(NarrowArgs a) {
+    const SubRec* list = EE ? a.sub_ee : a.sub_pt;
+    int n = EE ? a.ctr->nsub_ee : a.ctr->nsub_pt;
+    if (n > a.sub_cap) n = a.sub_cap;
+    NarrowCtx c = subtest_ctx(a);
+    SubTally t;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        one_subtest<MOVING, EE>(a, c, list[i], t);
+    subtest_counts(a, t);
+}
+
+// Both lists in one launch, point-triangle sub-tests first, so that a small
+// pass's two lists run side by side. A warp pays for an FP64 instruction the
+// same whatever the number of its lanes that execute it, and the lanes of a
+// warp running different sub-tests follow the union of their paths: a pass
+// with at most kSubSparse sub-tests (two warps per SM sub-partition) gives
+// each its own warp, which then follows one path; larger passes take one
+// sub-test per thread, which keeps the FP64 pipe's issue slots full.
+// Two blocks per SM: one warp per SM sub-partition already keeps its FP64
+// pipe issuing, and the registers then hold both tests without spills.
+constexpr int kSubSparse = 1216;
+template <bool MOVING>
+__global__ void __launch_bounds__(128, 2) k_subtests_all(NarrowArgs a) {
+    const int npt = a.ctr->nsub_pt < a.sub_cap ? a.ctr->nsub_pt : a.sub_cap;
+    const int nee = a.ctr->nsub_ee < a.sub_cap ? a.ctr->nsub_ee : a.sub_cap;
+    const int n = npt + nee;
+    NarrowCtx c = subtest_ctx(a);
+    SubTally t;
+    const int g = blockIdx.x * blockDim.x + threadIdx.x, threads = gridDim.x * blockDim.x;
+    const bool sparse = n <= kSubSparse;
+    if (!sparse || (threadIdx.x & 31) == 0) {
+        const int first = sparse ? g >> 5 : g, stride = sparse ? threads >> 5 : threads;
+        for (int i = first; i < n; i += stride) {
+            if (i < npt)
+                one_subtest<MOVING, false>(a, c, a.sub_pt[i], t);
+            else
+                one_subtest<MOVING, true>(a, c, a.sub_ee[i - npt], t);
+        }
+    }
+    subtest_counts(a, t);
 }
 
 // FP32 box of every point over the pass's time window, rounded outward:
@@ -414,18 +465,30 @@ void narrow_pass_split(const NarrowArgs& a, int moving, int max_pairs, cudaStrea
     if (blocks > cap_blocks) blocks = cap_blocks;
     int sblocks = (a.sub_cap + 127) / 128;
     if (sblocks > 152 * 16) sblocks = 152 * 16;
+    // both lists in one grid; at least kSubSparse warps for a sparse pass
+    long long mb = (2ll * a.sub_cap + 127) / 128;
+    if (mb < (kSubSparse + 3) / 4) mb = (kSubSparse + 3) / 4;
+    const int mblocks = mb > 152 * 16 ? 152 * 16 : (int)mb;
     if (moving) {
         if (parts & kSplitFilter) count_launch(), k_narrow_filter<true><<<blocks, block, 0, s>>>(a, max_pairs);
         if (parts & kSplitSubtests) {
-            count_launch(), k_subtests<true, false><<<sblocks, 128, 0, s>>>(a);
-            count_launch(), k_subtests<true, true><<<sblocks, 128, 0, s>>>(a);
+            if (a.sub_merge) {
+                count_launch(), k_subtests_all<true><<<mblocks, 128, 0, s>>>(a);
+            } else {
+                count_launch(), k_subtests<true, false><<<sblocks, 128, 0, s>>>(a);
+                count_launch(), k_subtests<true, true><<<sblocks, 128, 0, s>>>(a);
+            }
             if (zone) count_launch(), k_zone_unions<<<blocks, 128, 0, s>>>(a);
         }
     } else {
         if (parts & kSplitFilter) count_launch(), k_narrow_filter<false><<<blocks, block, 0, s>>>(a, max_pairs);
         if (parts & kSplitSubtests) {
-            count_launch(), k_subtests<false, false><<<sblocks, 128, 0, s>>>(a);
-            count_launch(), k_subtests<false, true><<<sblocks, 128, 0, s>>>(a);
+            if (a.sub_merge) {
+                count_launch(), k_subtests_all<false><<<mblocks, 128, 0, s>>>(a);
+            } else {
+                count_launch(), k_subtests<false, false><<<sblocks, 128, 0, s>>>(a);
+                count_launch(), k_subtests<false, true><<<sblocks, 128, 0, s>>>(a);
+            }
         }
     }
 }

@@ -327,6 +327,7 @@ struct cc_solver {
     bool pruned_warp = true;         // CC_TUNE_PRUNED_WARP: one warp per pruned query
     bool refit_up = true;            // CC_TUNE_REFIT_UP: the refit walk with one arrival per level
     bool robust_roots = true;        // CC_TUNE_ROBUST_ROOTS: correctly rounded roots only where decisive
+    bool sub_merge = true;           // CC_TUNE_SUBTEST_MERGE: both sub-test lists in one launch
     void* d_tree_scratch = nullptr;  // nodes, parent links and leaf counts of the trees being built
     int* d_tree_jobs = nullptr;      // 3 per tree: scene, first element, elements
     int* h_tree_jobs = nullptr;      // pinned
@@ -367,6 +368,7 @@ struct cc_solver {
     NarrowArgs narrow_args(int moving, bool combined) const {
         NarrowArgs a{};
         a.robust_roots = robust_roots ? 1 : 0;
+        a.sub_merge = sub_merge ? 1 : 0;
         a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
         a.vbody = d_vbody; a.body_mass = d_body_mass; a.body_slot0 = nv;
         a.rank = d_rank[moving]; a.escene = d_escene; a.scenes = d_scenes; a.run = d_run;
@@ -1555,8 +1557,8 @@ cc_status cc_solver::build_loop_graph(int n_hier) {
     mark(kStLoopPlan - m0, cs);
     leaf_boxes(d_ev, d_act_e, ne, d_escene, d_scenes, nscenes, d_xo, d_av, 1, d_box, bvh.bbox_enc, cs,
                &d_loop->nbroad);
-    tree_check(d_run, nscenes, bvh.bbox_enc, d_tree_vol, d_tree_built + nscenes, 1, d_rebuild, d_loop, cs);
-    loop_reset(d_ctr, d_run, nscenes, d_loop, cs);
+    tree_check_reset(d_run, nscenes, bvh.bbox_enc, d_tree_vol, d_tree_built + nscenes, 1, d_rebuild, d_loop, d_ctr,
+                     cs);
     mark(kStLoopBoxes - m0, cs);
     bvh_refit(d_box, lb, cs, false);  // the roots of the proximity pass's build stand
     if (mode == 1)
@@ -1851,6 +1853,7 @@ cc_status cc_solver::detect_pass(int moving, bool any_zone) {
         }
         NarrowArgs a;
         a.robust_roots = robust_roots ? 1 : 0;
+        a.sub_merge = sub_merge ? 1 : 0;
         a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
         a.vbody = d_vbody; a.body_mass = d_body_mass; a.body_slot0 = nv;
         a.rank = d_rank[moving]; a.escene = d_escene; a.scenes = d_scenes; a.run = d_run;
@@ -2198,6 +2201,7 @@ cc_status cc_solver::check_ccd(const double* x_old, const double* x_new, long lo
                   tune.packet_traverse, tune.rope_traverse, tune.traverse_refill, kTraversalStack);
         NarrowArgs a{};
         a.robust_roots = robust_roots ? 1 : 0;
+        a.sub_merge = sub_merge ? 1 : 0;
         a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
         a.vbody = d_vbody; a.body_mass = d_body_mass; a.body_slot0 = nv;
         a.rank = nullptr; a.escene = d_escene; a.scenes = d_scenes; a.run = d_run;
@@ -2264,6 +2268,7 @@ cc_status cc_solver::autotune(double* best_ms) {
                       t.packet_traverse, t.rope_traverse, t.traverse_refill, t.stack_depth);
             NarrowArgs a{};
             a.robust_roots = robust_roots ? 1 : 0;
+            a.sub_merge = sub_merge ? 1 : 0;
             a.xo = d_xo; a.av = d_av; a.fixed = d_fixed; a.ev = d_ev; a.esurf = d_esurf; a.erigid = d_erigid;
         a.vbody = d_vbody; a.body_mass = d_body_mass; a.body_slot0 = nv;
             a.rank = rank; a.escene = d_escene; a.scenes = d_scenes; a.run = d_run;
@@ -2609,6 +2614,10 @@ cc_status cc_set_tuning(cc_solver* s, int knob, int value) {
             s->zb.replay_cta_min = value;
             s->loop_dirty = true;
             return CC_OK;
+        case CC_TUNE_SUBTEST_MERGE:
+            s->sub_merge = value != 0;
+            s->loop_dirty = true;
+            return CC_OK;
         case CC_TUNE_ZONE_FEW:
             if (value < 0) return CC_BAD_INPUT;
             s->zb.zone_few = value;
@@ -2672,6 +2681,7 @@ int cc_get_tuning(cc_solver* s, int knob) {
         case CC_TUNE_REPLAY_CTA_MIN: return s->zb.replay_cta_min;
         case CC_TUNE_REFIT_UP: return s->refit_up ? 1 : 0;
         case CC_TUNE_ZONE_FEW: return s->zb.zone_few;
+        case CC_TUNE_SUBTEST_MERGE: return s->sub_merge ? 1 : 0;
         case CC_TUNE_STACK_DEPTH: return s->tune.stack_depth;
         case CC_TUNE_PAIR_CAPACITY: return s->pair_cap;
         default: return -1;

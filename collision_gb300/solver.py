@@ -188,6 +188,7 @@ class CollisionSolver3d:
     TUNE_ROPE_TRAVERSE, TUNE_SUBSET_REFIT, TUNE_TRAVERSE_REFILL, TUNE_STACK_DEPTH, TUNE_PAIR_CAPACITY = 10, 11, 12, 13, 14
     TUNE_DEVICE_LOOP, TUNE_PRUNE, TUNE_HOST_TREE, TUNE_SMALL_SORT, TUNE_PRUNED_WARP = 15, 16, 17, 18, 19
     TUNE_ROBUST_ROOTS, TUNE_ZONE_CTA_MIN, TUNE_REPLAY_CTA_MIN, TUNE_REFIT_UP, TUNE_ZONE_FEW = 20, 21, 22, 23, 24
+    TUNE_SUBTEST_MERGE = 25
 
     def setTuning(self, knob: int, value: int):
         """Launch shapes and the two-stage narrow phase; none changes results."""

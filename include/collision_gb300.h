@@ -305,6 +305,11 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
  *                           zone of two or more members is solved by a warp
  *                           (default 1024; above it, zones under 16 members
  *                           get a thread each). Same results
+ *   CC_TUNE_SUBTEST_MERGE   1 (default): the mixed path's point-triangle
+ *                           and edge-edge FP64 sub-tests in one launch, a
+ *                           warp per sub-test in passes with at most 1,216
+ *                           of them; 0: one launch per kind, a thread per
+ *                           sub-test. Same results
  * cc_get_tuning returns the current value, or -1 for an unknown knob. */
 enum {
     CC_TUNE_SPLIT_NARROW = 0,
@@ -331,7 +336,8 @@ enum {
     CC_TUNE_ZONE_CTA_MIN = 21,
     CC_TUNE_REPLAY_CTA_MIN = 22,
     CC_TUNE_REFIT_UP = 23,
-    CC_TUNE_ZONE_FEW = 24
+    CC_TUNE_ZONE_FEW = 24,
+    CC_TUNE_SUBTEST_MERGE = 25
 };
 cc_status cc_set_tuning(cc_solver* s, int knob, int value);
 int cc_get_tuning(cc_solver* s, int knob);

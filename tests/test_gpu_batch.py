@@ -56,11 +56,12 @@ def _split(a, off, i):
 def _run_batch(solver_cls, mix, nsteps, mode=0, window=True, record=False, split=True, graph=True, combined=True,
                warp=False, packet=False, roles=True, overlap=False, rope=True, subset_refit=True, device_loop=True,
                refill=8, zone_cap=None, pair_capacity=None, small_sort=True, pruned_warp=True, robust_roots=True,
-               zone_cta_min=None, replay_cta_min=None, refit_up=True, zone_few=None):
+               zone_cta_min=None, replay_cta_min=None, refit_up=True, zone_few=None, sub_merge=True):
     b = solver_cls(0)
     b.assembleBatch(mix)
     b.setMode(mode)
     b.setTuning(solver_cls.TUNE_REFIT_UP, int(refit_up))
+    b.setTuning(solver_cls.TUNE_SUBTEST_MERGE, int(sub_merge))
     if zone_few is not None:
         b.setTuning(solver_cls.TUNE_ZONE_FEW, zone_few)
     if zone_cta_min is not None:
@@ -568,6 +569,21 @@ def test_zone_cta_solve_agrees(solver_cls):
             assert np.array_equal(u[key], w[key]), (k, key)
         zone_steps += u["counters"]["zone_passes"] > 0
     assert zone_steps > 0
+
+
+@pytest.mark.parametrize("device_loop", [True, False])
+def test_merged_subtests_agree(solver_cls, device_loop):
+    # the FP64 sub-tests of both kinds in one launch (a warp each in small
+    # passes) and one launch per kind (a thread each): the same tests on the
+    # same records, so the same counts and bits
+    mix = _contact_sample()
+    a, _, _ = _run_batch(solver_cls, mix, 8, mode=1, zone_cap=3, device_loop=device_loop, sub_merge=True)
+    b, _, _ = _run_batch(solver_cls, mix, 8, mode=1, zone_cap=3, device_loop=device_loop, sub_merge=False)
+    for k, (u, w) in enumerate(zip(a, b)):
+        for key in ("x", "v", "hc", "hcol", "status"):
+            assert np.array_equal(u[key], w[key]), (k, key)
+        for c in ("passes", "visits", "hit_pairs", "contacts", "fp64_subtests"):
+            assert u["counters"][c] == w["counters"][c], (k, c)
 
 
 def test_zone_warp_solve_for_few_zones_agrees(solver_cls):
