@@ -690,7 +690,8 @@ def run_gpu(args):
         if t_sub > 0 and kc.get("fp64_subtests"):
             flops = SUBTEST_FP64_FLOPS * kc["fp64_subtests"]
             kern["ccd_subtests"] = {
-                "kernel": "k_subtests (the FP64 sub-tests that pass the FP32 filters)", "bound": "fp64",
+                "kernel": "k_subtests_all (the FP64 sub-tests that pass the FP32 filters, both kinds in one launch)",
+                "bound": "fp64",
                 "flops": flops, "s": t_sub, "achieved_tflops": flops / t_sub / 1e12, "peak_tflops": FP64_PEAK_TFLOPS,
                 "frac": flops / t_sub / 1e12 / FP64_PEAK_TFLOPS, "peak_source": "nominal",
                 "flops_per_subtest": SUBTEST_FP64_FLOPS, "cr_roots": kc.get("cr_roots"),
