@@ -345,12 +345,24 @@ __device__ __forceinline__ void subtest_counts(const NarrowArgs& a, SubTally t) 
     }
 }
 
-// One list (point-triangle or edge-edge), one sub-test per thread.
+// Passes with more sub-tests than this run them as two launches, one per
+// kind (k_subtests): measured faster than one launch for both kinds when the
+// pass is large, where the FP64 pipes are full either way (each kind's
+// kernel keeps a smaller body).
+constexpr int kSubMergeMax = 65536;
+
+// One list (point-triangle or edge-edge), one sub-test per thread. merged:
+// k_subtests_all takes the passes of at most kSubMergeMax sub-tests.
 template <bool MOVING, bool EE>
-__global__ void __launch_bounds__(128, 4) k_subtests(NarrowArgs a) {
+__global__ void __launch_bounds__(128, 4) k_subtests(NarrowArgs a, int merged) {
     const SubRec* list = EE ? a.sub_ee : a.sub_pt;
     int n = EE ? a.ctr->nsub_ee : a.ctr->nsub_pt;
     if (n > a.sub_cap) n = a.sub_cap;
+    if (merged) {
+        const int npt = a.ctr->nsub_pt < a.sub_cap ? a.ctr->nsub_pt : a.sub_cap;
+        const int nee = a.ctr->nsub_ee < a.sub_cap ? a.ctr->nsub_ee : a.sub_cap;
+        if (npt + nee <= kSubMergeMax) return;
+    }
     NarrowCtx c = subtest_ctx(a);
     SubTally t;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -358,8 +370,9 @@ __global__ void __launch_bounds__(128, 4) k_subtests(NarrowArgs a) {
     subtest_counts(a, t);
 }
 
-// Both lists in one launch, point-triangle sub-tests first, so that a small
-// pass's two lists run side by side. A warp pays for an FP64 instruction the
+// Both lists in one launch (passes of at most kSubMergeMax sub-tests),
+// point-triangle sub-tests first, so that a small pass's two lists run side
+// by side. A warp pays for an FP64 instruction the
 // same whatever the number of its lanes that execute it, and the lanes of a
 // warp running different sub-tests follow the union of their paths: a pass
 // with at most kSubSparse sub-tests (two warps per SM sub-partition) gives
@@ -373,6 +386,7 @@ __global__ void __launch_bounds__(128, 2) k_subtests_all(NarrowArgs a) {
     const int npt = a.ctr->nsub_pt < a.sub_cap ? a.ctr->nsub_pt : a.sub_cap;
     const int nee = a.ctr->nsub_ee < a.sub_cap ? a.ctr->nsub_ee : a.sub_cap;
     const int n = npt + nee;
+    if (n > kSubMergeMax) return;  // k_subtests's
     NarrowCtx c = subtest_ctx(a);
     SubTally t;
     const int g = blockIdx.x * blockDim.x + threadIdx.x, threads = gridDim.x * blockDim.x;
@@ -465,30 +479,26 @@ void narrow_pass_split(const NarrowArgs& a, int moving, int max_pairs, cudaStrea
     if (blocks > cap_blocks) blocks = cap_blocks;
     int sblocks = (a.sub_cap + 127) / 128;
     if (sblocks > 152 * 16) sblocks = 152 * 16;
-    // both lists in one grid; at least kSubSparse warps for a sparse pass
+    // both lists of a pass of at most kSubMergeMax in one grid, at least one
+    // warp per sub-test of a sparse pass
     long long mb = (2ll * a.sub_cap + 127) / 128;
+    if (mb > (kSubMergeMax + 127) / 128) mb = (kSubMergeMax + 127) / 128;
     if (mb < (kSubSparse + 3) / 4) mb = (kSubSparse + 3) / 4;
-    const int mblocks = mb > 152 * 16 ? 152 * 16 : (int)mb;
+    const int mblocks = (int)mb;
     if (moving) {
         if (parts & kSplitFilter) count_launch(), k_narrow_filter<true><<<blocks, block, 0, s>>>(a, max_pairs);
         if (parts & kSplitSubtests) {
-            if (a.sub_merge) {
-                count_launch(), k_subtests_all<true><<<mblocks, 128, 0, s>>>(a);
-            } else {
-                count_launch(), k_subtests<true, false><<<sblocks, 128, 0, s>>>(a);
-                count_launch(), k_subtests<true, true><<<sblocks, 128, 0, s>>>(a);
-            }
+            if (a.sub_merge) count_launch(), k_subtests_all<true><<<mblocks, 128, 0, s>>>(a);
+            count_launch(), k_subtests<true, false><<<sblocks, 128, 0, s>>>(a, a.sub_merge);
+            count_launch(), k_subtests<true, true><<<sblocks, 128, 0, s>>>(a, a.sub_merge);
             if (zone) count_launch(), k_zone_unions<<<blocks, 128, 0, s>>>(a);
         }
     } else {
         if (parts & kSplitFilter) count_launch(), k_narrow_filter<false><<<blocks, block, 0, s>>>(a, max_pairs);
         if (parts & kSplitSubtests) {
-            if (a.sub_merge) {
-                count_launch(), k_subtests_all<false><<<mblocks, 128, 0, s>>>(a);
-            } else {
-                count_launch(), k_subtests<false, false><<<sblocks, 128, 0, s>>>(a);
-                count_launch(), k_subtests<false, true><<<sblocks, 128, 0, s>>>(a);
-            }
+            if (a.sub_merge) count_launch(), k_subtests_all<false><<<mblocks, 128, 0, s>>>(a);
+            count_launch(), k_subtests<false, false><<<sblocks, 128, 0, s>>>(a, a.sub_merge);
+            count_launch(), k_subtests<false, true><<<sblocks, 128, 0, s>>>(a, a.sub_merge);
         }
     }
 }

@@ -306,10 +306,11 @@ cc_status cc_set_scene_enabled(cc_solver* s, int scene, int on);
  *                           (default 1024; above it, zones under 16 members
  *                           get a thread each). Same results
  *   CC_TUNE_SUBTEST_MERGE   1 (default): the mixed path's point-triangle
- *                           and edge-edge FP64 sub-tests in one launch, a
- *                           warp per sub-test in passes with at most 1,216
- *                           of them; 0: one launch per kind, a thread per
- *                           sub-test. Same results
+ *                           and edge-edge FP64 sub-tests of a pass with at
+ *                           most 65,536 of them in one launch, a warp per
+ *                           sub-test where there are at most 1,216 (larger
+ *                           passes: one launch per kind); 0: one launch per
+ *                           kind, a thread per sub-test. Same results
  * cc_get_tuning returns the current value, or -1 for an unknown knob. */
 enum {
     CC_TUNE_SPLIT_NARROW = 0,
