@@ -103,7 +103,7 @@ def _match(g, ref):
             (g["sha"] is None or g["sha"] == ref["sha"]))
 
 
-def _judge(t: Tally, g, ro, rc, where):
+def _assess(t: Tally, g, ro, rc, where):
     """Count a step exact or glibc-residual, or fail with the differences."""
     if _match(g, ro):
         t.exact += 1
@@ -155,7 +155,7 @@ def run_scene(solver_cls, sc, nsteps, start=None, record=True, label="") -> Tall
             r, q = fo.result(), fc.result()
             assert r["rc"] == 0 and q["rc"] == 0, (where, r["rc"], q["rc"])
             ro, rc = ref.view(ref.o, r), ref.view(ref.c, q)
-            _judge(t, g, ro, rc, where)
+            _assess(t, g, ro, rc, where)
             t.note(g["kinds"])
             t.steps += 1
             x, v, hc = r["x"], r["v"], r["has_collsn"]
@@ -216,7 +216,7 @@ def run_batch(solver_cls, scs, nsteps, mode=1, zone_cap=200, threads=16, label="
                 g = dict(x=xo[a:e], v=vo[a:e], hc=ho[a:e], hcol=bool(hcol[i]), kinds=kinds[i],
                          zones=zone_labels(roots[a:e]), sha=None)
                 exact_before = t.exact
-                _judge(t, g, refs[i].view(refs[i].o, r), refs[i].view(refs[i].c, q), where)
+                _assess(t, g, refs[i].view(refs[i].o, r), refs[i].view(refs[i].c, q), where)
                 if t.exact > exact_before:
                     om = refs[i].o.check_ccd(x_in[a:e], r["x"])
                     assert om == missed[i], f"{where}: CCD re-check, GPU {missed[i]} vs oracle {om}"
