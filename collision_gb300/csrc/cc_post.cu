@@ -697,6 +697,20 @@ __device__ __forceinline__ bool strain_flag_vals(const StrainEdgeStep& ed, const
     return true;
 }
 
+// 0.5 * x, the averaging of the strain sweep: one less in the exponent field
+// (in the high 32 bits) when that field is 2..2046, where the halving is
+// exact; x itself for +-0; the FP64 multiply otherwise. GB300 issues a
+// warp's FP64 multiply in ~64 cycles whatever its active lanes, and the
+// averaging lies on the sweep's per-level critical path; these are a few
+// 32-bit integer instructions with the same result.
+__device__ __forceinline__ double half_of(double x) {
+    const int hi = __double2hiint(x), lo = __double2loint(x);
+    const unsigned e = ((unsigned)hi >> 20) & 0x7ffu;
+    if (e - 2u < 0x7fdu) return __hiloint2double(hi - 0x00100000, lo);
+    if ((((unsigned)hi << 1) | (unsigned)lo) == 0u) return x;
+    return 0.5 * x;
+}
+
 // reduceSuperelast, dcollid.cpp:586-596: up to 10 Gauss-Seidel passes over
 // the edges in element order, each averaging the two end velocities of an
 // over-strained edge before the next edge is tested (one pass per launch). The edges arrive sorted
@@ -785,7 +799,7 @@ __global__ void __launch_bounds__(256) k_strain(const StrainEdgeStep* __restrict
             if (strain_flag_vals(cur, v0, v1, dt, &n_exact)) {
                 ++n_avg;
                 double t0 = a0.x + a1.x, t1 = a0.y + a1.y, t2 = a0.z + a1.z;
-                t0 = 0.5 * t0; t1 = 0.5 * t1; t2 = 0.5 * t2;
+                t0 = half_of(t0); t1 = half_of(t1); t2 = half_of(t2);
                 double4_32a nv4 = make_double4_32a(t0, t1, t2, 0.0);
                 av[cur.p0] = nv4;
                 av[cur.p1] = nv4;
@@ -872,7 +886,7 @@ __device__ __forceinline__ void strain_window_edge(const StrainEdgeHot& h, int e
     double t[3];
     for (int k = 0; k < 3; ++k) {
         t[k] = v0[k] + v1[k];
-        t[k] = 0.5 * t[k];
+        t[k] = half_of(t[k]);
     }
     double2 na = make_double2(t[0], t[1]), nb = make_double2(t[2], 0.0);
     float4 nf = make_float4((float)t[0], (float)t[1], (float)t[2], 0.f);
@@ -1210,7 +1224,7 @@ __global__ void __launch_bounds__(32) k_strain_warp(const StrainEdge* __restrict
             double t[3];
             for (int k = 0; k < 3; ++k) {
                 t[k] = v0[k] + v1[k];
-                t[k] = 0.5 * t[k];
+                t[k] = half_of(t[k]);
             }
             const double2 na = make_double2(t[0], t[1]), nb = make_double2(t[2], 0.0);
             w0.a = na; w0.b = nb;
